@@ -1,0 +1,168 @@
+/*
+ * locarna_gb300 — C ABI of the GB300-native sparsified Sankoff (LocARNA)
+ * alignment engine and the LocARNA-P partition-function engine.
+ *
+ * Plain pointers and sizes only; no exceptions cross this boundary. Every
+ * entry point returns an lcg_status (0 = ok, < 0 = error) and, on error,
+ * lcg_last_error() returns a thread-local message.
+ *
+ * The boundary sits where the reference's LocARNA::Aligner sits
+ * (src/LocARNA/aligner.hh:67-189): the caller prepares the same tables the
+ * reference's Scoring / ArcMatches / BasePairs / TraceController /
+ * AnchorConstraints objects hold (src/LocARNA/scoring.hh:488-607,
+ * arc_matches.hh:404-413, basepairs.hh:217-222, trace_controller.hh:122-139,
+ * anchor_constraints.hh:157-215) and the engine runs Aligner::align() +
+ * Aligner::trace() (aligner.cc:924-957, :1345-1358) on the GPU.
+ *
+ * Score semantics follow the reference's InftyInt (infty_int.hh:56-480):
+ * an alignment score is a finite integer or negative infinity, reported as
+ * LCG_NEG_INF.
+ */
+#ifndef LOCARNA_GB300_H
+#define LOCARNA_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LCG_ABI_VERSION 1
+
+typedef int32_t lcg_status;
+#define LCG_OK 0
+#define LCG_ERR_ARG (-1)       /* invalid argument (sizes, indices, NULL) */
+#define LCG_ERR_CUDA (-2)      /* a CUDA runtime call failed */
+#define LCG_ERR_NOMEM (-3)     /* device or host allocation failed */
+#define LCG_ERR_RANGE (-4)     /* scores could overflow the int32 device range */
+#define LCG_ERR_TIMEOUT (-5)   /* a bounded device wait gave up */
+#define LCG_ERR_PARSE (-6)     /* malformed input file / text */
+#define LCG_ERR_UNSUPPORTED (-7) /* option outside the implemented scope */
+#define LCG_ERR_DEVICE (-8)    /* a kernel reported an internal error */
+
+/* negative infinity as returned in lcg_align_result.score */
+#define LCG_NEG_INF ((int64_t)(-((int64_t)1 << 40)))
+
+/* free end gaps bits, same meaning as LocARNA::FreeEndgaps("abcd")
+ * (free_endgaps.hh:27-71): character k == '+' sets bit k. */
+#define LCG_FREE_LEFT_1 1   /* allow_left_1: free gaps at the start of B vs A */
+#define LCG_FREE_RIGHT_1 2  /* allow_right_1 */
+#define LCG_FREE_LEFT_2 4   /* allow_left_2 */
+#define LCG_FREE_RIGHT_2 8  /* allow_right_2 */
+
+/*
+ * Prepared tables of one sequence pair (A of length len_a, B of length len_b).
+ * Positions are 1-based as in the reference; index 0 of per-position arrays is
+ * unused unless stated otherwise. All arrays are caller-owned host memory.
+ */
+typedef struct lcg_pair_tables {
+    int32_t len_a, len_b;
+    /* Scoring::basematch(i,j) = sigma[i*(len_b+1)+j]   (scoring.hh:489) */
+    const int32_t *sigma;
+    /* Scoring::gapA(i) / gapB(j)                        (scoring.hh:589-606) */
+    const int32_t *gap_a; /* len_a+1 */
+    const int32_t *gap_b; /* len_b+1 */
+    int32_t indel_opening; /* Scoring::indel_opening() (scoring.hh:617) */
+    int32_t exclusion;     /* Scoring::exclusion()     (scoring.hh:611) */
+    /* arcs in the reference's arc index order (basepairs.cc:155-205):
+     * arcs_x[2k] = left end, arcs_x[2k+1] = right end of arc k */
+    int32_t num_arcs_a, num_arcs_b;
+    const int32_t *arcs_a;
+    const int32_t *arcs_b;
+    /* valid arc matches in the reference's index order (arc_matches.cc:159-184):
+     * am_arcs[2k] = arc index in A, am_arcs[2k+1] = arc index in B,
+     * am_score[k] = Scoring::arcmatch(am_k) (scoring.cc:440-554) */
+    int32_t num_arcmatches;
+    const int32_t *am_arcs;
+    const int32_t *am_score;
+    /* TraceController band: is_valid(i,j) iff min_col[i] <= j <= max_col[i],
+     * i in 0..len_a (trace_controller.hh:328-336) */
+    const int32_t *min_col; /* len_a+1 */
+    const int32_t *max_col; /* len_a+1 */
+    /* Anchor constraints as ranges (anchor_constraints.hh:157-253); all six
+     * pointers NULL means "no anchors" (everything allowed).
+     * allowed_match(i,j) iff match_lo[i] <= j <= match_hi[i]   (i 1..len_a)
+     * allowed_del(i,j)   iff del_lo[i]   <= j <= del_hi[i]     (i 1..len_a)
+     * allowed_ins(i,j)   iff ins_lo[j]   <= i <= ins_hi[j]     (j 1..len_b) */
+    const int32_t *match_lo, *match_hi;
+    const int32_t *del_lo, *del_hi;
+    const int32_t *ins_lo, *ins_hi;
+    /* rightmost_anchor() / leftmost_anchor() (anchor_constraints.hh:282-306);
+     * without anchors (0,0) and (len_a+1,len_b+1) */
+    int32_t right_anchor_a, right_anchor_b;
+    int32_t left_anchor_a, left_anchor_b;
+} lcg_pair_tables;
+
+/* AlignerParams subset (aligner_params.hh:51-64) */
+typedef struct lcg_align_opts {
+    int32_t struct_local;  /* AlignerParams::struct_local */
+    int32_t sequ_local;    /* AlignerParams::sequ_local */
+    int32_t free_endgaps;  /* LCG_FREE_* bits */
+    int32_t do_trace;      /* run Aligner::trace() after align() */
+} lcg_align_opts;
+
+/*
+ * Result of one pair. The caller provides the edge and arc-match buffers:
+ * edges needs capacity 2*(len_a+len_b) int32, traced_am needs capacity
+ * min(len_a,len_b) int32 (either may be NULL when do_trace == 0).
+ *
+ * edges holds the raw traceback edges in the order the reference appends them
+ * (Alignment::append, alignment.cc:91-95): pairs (pos_a, pos_b) with -1 for a
+ * gap. traced_am lists the arc matches of the traced alignment (reference arc
+ * match indices) in the order the reference's trace visits them; their arcs
+ * give the structure strings (Alignment::add_basepairA/B).
+ */
+typedef struct lcg_align_result {
+    int64_t score;               /* Aligner::align(); LCG_NEG_INF for -inf */
+    int32_t max_i, max_j;        /* end of the (local) alignment */
+    int32_t min_i, min_j;        /* start of a sequence-local alignment */
+    int32_t num_edges;           /* number of (pos_a,pos_b) pairs in edges */
+    int32_t num_traced_am;
+    int32_t *edges;
+    int32_t *traced_am;
+} lcg_align_result;
+
+/* Work counts of one pair, over the reference's iteration space. */
+typedef struct lcg_work_counts {
+    int64_t groups;          /* left-end groups (al,bl) aligned in align_D */
+    int64_t cells;           /* M cells evaluated (groups + top level), state NO_NO */
+    int64_t arc_terms;       /* arc-pair candidates evaluated in align_noex */
+    int64_t valid_arc_terms; /* of those, valid arc matches (finite or not) */
+} lcg_work_counts;
+
+/* ---------------------------------------------------------------- engine */
+
+typedef struct lcg_engine_s *lcg_engine;
+
+/* Message of the last failed call on this thread ("" if none). */
+const char *lcg_last_error(void);
+
+/* ABI version (LCG_ABI_VERSION). */
+int32_t lcg_abi_version(void);
+
+/* Create an engine on CUDA device `device`, launching on `stream`
+ * (a cudaStream_t, or NULL for a stream the engine creates). The engine owns
+ * its device buffers; one engine per host thread. */
+lcg_status lcg_engine_create(int32_t device, void *stream, lcg_engine *out);
+lcg_status lcg_engine_destroy(lcg_engine eng);
+
+/*
+ * Align `npairs` independent pairs: the batched equivalent of constructing one
+ * LocARNA::Aligner per pair and calling align() (+ trace()) on each
+ * (reference: src/locarna.cc:727-785, aligner.cc:924-957,1345-1358).
+ * Host tables in, host results out; all device traffic is inside the call.
+ */
+lcg_status lcg_align_pairs(lcg_engine eng, const lcg_pair_tables *pairs,
+                           int32_t npairs, const lcg_align_opts *opts,
+                           lcg_align_result *results);
+
+/* Device time (ms) of the last lcg_align_pairs call's kernels, and the number
+ * of kernel launches it made. */
+lcg_status lcg_engine_last_stats(lcg_engine eng, double *kernel_ms,
+                                 int64_t *launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LOCARNA_GB300_H */

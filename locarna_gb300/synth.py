@@ -1,0 +1,115 @@
+"""Seeded synthetic RNA inputs in PP 2.0 format.
+
+The reference reads PP 2.0 files (src/LocARNA/rna_data.cc:979-1104): a
+clustal-like sequence block ended by ``#END``, then ``#SECTION BASEPAIRS``
+with ``i j p`` lines, ended by ``#END``.  Base-pair probability tables
+normally come from ViennaRNA folding; here they are synthetic:
+
+* sequence: i.i.d. uniform over ACGU;
+* planted stems: nested or disjoint (never crossing), each 4-10 stacked
+  canonical/GU pairs whose bases are rewritten to a random canonical pair,
+  p ~ U(0.5, 0.99); 3-6 stems per 150 nt (the count scales with length);
+* background: every canonical/GU pair with j-i >= 4 is kept with rate
+  ``q`` (default 0.05), p ~ Exp(mean 0.02) truncated to <= 0.1 by rejection;
+* probabilities are written with 6 decimals and pairs whose written value
+  is <= ``min_prob`` (the reference's default --min-prob 0.001,
+  src/locarna.cc:183) are dropped, so every reader parses the same value.
+
+Only ``random.Random.random()`` is used, so a seed gives the same file on
+every platform.
+"""
+import math
+import random
+
+CANONICAL = {("A", "U"), ("U", "A"), ("C", "G"), ("G", "C"), ("G", "U"), ("U", "G")}
+_CANON_LIST = [("A", "U"), ("U", "A"), ("C", "G"), ("G", "C"), ("G", "U"), ("U", "G")]
+
+
+def _randint(rng, lo, hi):
+    """Uniform integer in [lo, hi] from rng.random() only."""
+    return lo + min(hi - lo, int(rng.random() * (hi - lo + 1)))
+
+
+class RnaRecord:
+    """One synthetic RNA: name, sequence and sparse base-pair probabilities."""
+
+    def __init__(self, name, seq, pairs):
+        self.name = name
+        self.seq = seq
+        self.pairs = pairs  # dict (i, j) -> p, 1-based, i < j
+
+    def to_pp(self):
+        lines = ["#PP 2.0", "", f"{self.name} {self.seq}", "", "#END", "", "#SECTION BASEPAIRS", ""]
+        for (i, j) in sorted(self.pairs):
+            lines.append(f"{i} {j} {self.pairs[(i, j)]:.6f}")
+        lines += ["", "#END", ""]
+        return "\n".join(lines)
+
+
+def make_rna(length, seed, name=None, q=0.05, stems=None, min_prob=0.001):
+    """Generate one RNA of ``length`` nt from ``seed``."""
+    rng = random.Random(seed)
+    seq = [("A", "C", "G", "U")[_randint(rng, 0, 3)] for _ in range(length)]
+    pairs = {}
+    used = [False] * (length + 1)
+    planted = []  # list of (i, j) pairs, 1-based
+    if stems is None:
+        lo = max(1, round(3 * length / 150))
+        hi = max(lo, round(6 * length / 150))
+        stems = _randint(rng, lo, hi)
+
+    def crosses(i, j):
+        for (a, b) in planted:
+            if a < i < b < j or i < a < j < b:
+                return True
+        return False
+
+    for _ in range(stems):
+        for _attempt in range(200):
+            k = _randint(rng, 4, 10)
+            span_min = 2 * k + 2  # hairpin of at least 3 unpaired bases
+            if length < span_min + 1:
+                break
+            i = _randint(rng, 1, length - span_min)
+            j = _randint(rng, i + span_min, length)
+            ok = True
+            for t in range(k):
+                a, b = i + t, j - t
+                if b - a < 4 or used[a] or used[b] or crosses(a, b):
+                    ok = False
+                    break
+            if not ok:
+                continue
+            for t in range(k):
+                a, b = i + t, j - t
+                x, y = _CANON_LIST[_randint(rng, 0, 5)]
+                seq[a - 1], seq[b - 1] = x, y
+                used[a] = used[b] = True
+                planted.append((a, b))
+                pairs[(a, b)] = round(0.5 + 0.49 * rng.random(), 6)
+            break
+
+    for i in range(1, length + 1):
+        for j in range(i + 4, length + 1):
+            if (i, j) in pairs or (seq[i - 1], seq[j - 1]) not in CANONICAL:
+                continue
+            if rng.random() >= q:
+                continue
+            while True:
+                p = -0.02 * math.log(1.0 - rng.random())
+                if p <= 0.1:
+                    break
+            pairs[(i, j)] = round(p, 6)
+
+    pairs = {k: v for k, v in pairs.items() if v > min_prob}
+    return RnaRecord(name or f"rna{seed}", "".join(seq), pairs)
+
+
+def make_family(count, len_lo, len_hi, seed, q=0.05):
+    """``count`` RNAs with lengths uniform in [len_lo, len_hi]."""
+    rng = random.Random(seed)
+    out = []
+    for k in range(count):
+        L = _randint(rng, len_lo, len_hi)
+        out.append(make_rna(L, seed * 100003 + k, name=f"s{seed}_{k}", q=q))
+    return out

@@ -1,0 +1,564 @@
+/*
+ * ORACLE — test infrastructure only. Only tests/, __graft_entry__.smoke() and
+ * bench.py's CPU-baseline leg may load this file's library, and only as the
+ * checker or the timed CPU baseline, never as the product path.
+ *
+ * A plain-C restatement of the reference's sparsified Sankoff aligner
+ * (LocARNA::AlignerImpl, src/LocARNA/aligner.cc) over the prepared tables of
+ * include/locarna_gb300.h. Scores use the reference's InftyInt semantics in
+ * 64 bits (src/LocARNA/infty_int.hh:56-480, infty_int.cc:7-23): values below
+ * LONG_MIN/5 are negative infinity and are normalised to LONG_MIN/5*2 whenever
+ * they are stored, while sums and maxima in flight stay un-normalised
+ * ("tainted"), exactly as in align_noex.
+ *
+ * The M matrices are allocated once and reused across left-end groups without
+ * clearing, as in the reference (aligner.cc:118-131), so that any read of a
+ * cell the current group did not write would give the same (stale) value the
+ * reference sees. With LCG_ORACLE_CHECK_READS the oracle counts such reads.
+ */
+#include <limits.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "../include/locarna_gb300.h"
+
+typedef int64_t sc_t;
+#define MIN_FINITY (LONG_MIN / 5)
+#define NEG_INF (LONG_MIN / 5 * 2)
+
+static inline sc_t norm(sc_t x) { return x < MIN_FINITY ? NEG_INF : x; }
+static inline sc_t smax(sc_t a, sc_t b) { return a > b ? a : b; }
+
+/* structure-local states, aligner_impl.hh:113-122 */
+enum { E_NO_NO, E_X_NO, E_NO_X, E_X_X, E_OP_NO, E_NO_OP, E_OP_X, E_X_OP };
+
+typedef struct {
+    const lcg_pair_tables *t;
+    const lcg_align_opts *o;
+    int n, m;
+    /* adjacency: right_adj_x[pos] = list of arc indices with right end pos,
+     * sorted by left end descending, sentinel left 0 (basepairs.cc:110-122,212-220) */
+    int *radjA_start, *radjA; /* CSR, each list followed by -1 sentinel */
+    int *radjB_start, *radjB;
+    /* common left end lists (creation order) and common right end lists
+     * (sorted lex greater left ends), CSR over (n+1)*(m+1) */
+    int *cle_start, *cle;
+    int *cre_start, *cre;
+    sc_t *D;       /* |arcsA| x |arcsB| */
+    sc_t *M[8];    /* (n+1) x (m+1) */
+    sc_t *E[4];    /* m+1 */
+    sc_t F[4];
+    int max_i, max_j, min_i, min_j;
+    /* trace output */
+    int32_t *edges; int nedges, edge_cap;
+    int32_t *tam; int ntam, tam_cap;
+    lcg_work_counts *cnt;
+} Ctx;
+
+#define MM(c, s, i, j) ((c)->M[s][(size_t)(i) * ((c)->m + 1) + (j)])
+#define DD(c, a, b) ((c)->D[(size_t)(a) * (c)->t->num_arcs_b + (b)])
+
+static inline int arcL(const int32_t *arcs, int k) { return arcs[2 * k]; }
+static inline int arcR(const int32_t *arcs, int k) { return arcs[2 * k + 1]; }
+
+static inline int minc(const Ctx *c, int i) { return c->t->min_col[i]; }
+static inline int maxc(const Ctx *c, int i) { return c->t->max_col[i]; }
+static inline int valid(const Ctx *c, int i, int j) {
+    return i >= 0 && i <= c->n && minc(c, i) <= j && j <= maxc(c, i);
+}
+static inline int valid_match(const Ctx *c, int i, int j) { return valid(c, i, j) && valid(c, i - 1, j - 1); }
+static inline int a_match(const Ctx *c, int i, int j) {
+    return !c->t->match_lo || (c->t->match_lo[i] <= j && j <= c->t->match_hi[i]);
+}
+static inline int a_del(const Ctx *c, int i, int j) {
+    return !c->t->del_lo || (c->t->del_lo[i] <= j && j <= c->t->del_hi[i]);
+}
+static inline int a_ins(const Ctx *c, int i, int j) {
+    return !c->t->ins_lo || (c->t->ins_lo[j] <= i && i <= c->t->ins_hi[j]);
+}
+static inline sc_t sigma(const Ctx *c, int i, int j) { return c->t->sigma[(size_t)i * (c->m + 1) + j]; }
+
+/* ---------------------------------------------------------------- setup */
+
+static int *g_sort_arcs; /* qsort context (single-threaded use per call) */
+static int cmp_left_desc(const void *x, const void *y) {
+    int a = *(const int *)x, b = *(const int *)y;
+    return g_sort_arcs[2 * b] - g_sort_arcs[2 * a];
+}
+
+static void build_radj(const int32_t *arcs, int narcs, int len, int **start, int **lst) {
+    int *cntv = calloc(len + 2, sizeof(int));
+    for (int k = 0; k < narcs; ++k) cntv[arcR(arcs, k)]++;
+    *start = malloc((len + 2) * sizeof(int));
+    int acc = 0;
+    for (int p = 0; p <= len; ++p) { (*start)[p] = acc; acc += cntv[p] + 1; }
+    (*start)[len + 1] = acc;
+    *lst = malloc((acc > 0 ? acc : 1) * sizeof(int));
+    int *fill = calloc(len + 2, sizeof(int));
+    for (int k = 0; k < narcs; ++k) { int r = arcR(arcs, k); (*lst)[(*start)[r] + fill[r]++] = k; }
+    g_sort_arcs = (int *)arcs;
+    for (int p = 0; p <= len; ++p) {
+        qsort(*lst + (*start)[p], cntv[p], sizeof(int), cmp_left_desc);
+        (*lst)[(*start)[p] + cntv[p]] = -1; /* sentinel, left end 0 */
+    }
+    free(cntv); free(fill);
+}
+
+static const Ctx *g_sort_ctx;
+static int cmp_lex_greater_left(const void *x, const void *y) {
+    const Ctx *c = g_sort_ctx;
+    int i = *(const int *)x, j = *(const int *)y;
+    int ali = arcL(c->t->arcs_a, c->t->am_arcs[2 * i]), bli = arcL(c->t->arcs_b, c->t->am_arcs[2 * i + 1]);
+    int alj = arcL(c->t->arcs_a, c->t->am_arcs[2 * j]), blj = arcL(c->t->arcs_b, c->t->am_arcs[2 * j + 1]);
+    if (ali != alj) return ali > alj ? -1 : 1;
+    if (bli != blj) return bli > blj ? -1 : 1;
+    return 0;
+}
+
+static void build_am_lists(Ctx *c) {
+    int n = c->n, m = c->m, na = c->t->num_arcmatches;
+    size_t cells = (size_t)(n + 1) * (m + 1);
+    int *cl = calloc(cells + 1, sizeof(int)), *cr = calloc(cells + 1, sizeof(int));
+    for (int k = 0; k < na; ++k) {
+        int a = c->t->am_arcs[2 * k], b = c->t->am_arcs[2 * k + 1];
+        cl[(size_t)arcL(c->t->arcs_a, a) * (m + 1) + arcL(c->t->arcs_b, b)]++;
+        cr[(size_t)arcR(c->t->arcs_a, a) * (m + 1) + arcR(c->t->arcs_b, b)]++;
+    }
+    c->cle_start = malloc((cells + 1) * sizeof(int));
+    c->cre_start = malloc((cells + 1) * sizeof(int));
+    int al = 0, ar = 0;
+    for (size_t q = 0; q < cells; ++q) {
+        c->cle_start[q] = al; al += cl[q];
+        c->cre_start[q] = ar; ar += cr[q];
+    }
+    c->cle_start[cells] = al; c->cre_start[cells] = ar;
+    c->cle = malloc((na > 0 ? na : 1) * sizeof(int));
+    c->cre = malloc((na > 0 ? na : 1) * sizeof(int));
+    memset(cl, 0, (cells + 1) * sizeof(int));
+    memset(cr, 0, (cells + 1) * sizeof(int));
+    for (int k = 0; k < na; ++k) {
+        int a = c->t->am_arcs[2 * k], b = c->t->am_arcs[2 * k + 1];
+        size_t ql = (size_t)arcL(c->t->arcs_a, a) * (m + 1) + arcL(c->t->arcs_b, b);
+        size_t qr = (size_t)arcR(c->t->arcs_a, a) * (m + 1) + arcR(c->t->arcs_b, b);
+        c->cle[c->cle_start[ql] + cl[ql]++] = k;
+        c->cre[c->cre_start[qr] + cr[qr]++] = k;
+    }
+    g_sort_ctx = c;
+    for (size_t q = 0; q < cells; ++q) {
+        int s = c->cre_start[q], e = c->cre_start[q + 1];
+        if (e - s > 1) qsort(c->cre + s, e - s, sizeof(int), cmp_lex_greater_left);
+    }
+    free(cl); free(cr);
+}
+
+/* ---------------------------------------------------------------- DP */
+
+/* AlignerImpl::align_noex, aligner.cc:153-233 */
+static sc_t align_noex(Ctx *c, int state, int al, int bl, int i, int j) {
+    sc_t *E = c->E[state];
+    sc_t max_score = NEG_INF;
+    if (a_match(c, i, j)) max_score = MM(c, state, i - 1, j - 1) + sigma(c, i, j);
+    if (a_del(c, i, j)) {
+        E[j] = norm(smax(E[j] + c->t->gap_a[i], MM(c, state, i - 1, j) + c->t->gap_a[i] + c->t->indel_opening));
+        max_score = smax(max_score, E[j]);
+    } else {
+        E[j] = NEG_INF;
+    }
+    if (a_ins(c, i, j)) {
+        c->F[state] = norm(smax(c->F[state] + c->t->gap_b[j], MM(c, state, i, j - 1) + c->t->gap_b[j] + c->t->indel_opening));
+        max_score = smax(max_score, c->F[state]);
+    } else {
+        c->F[state] = NEG_INF;
+    }
+    if (a_match(c, i, j)) {
+        const int *la = c->radjA + c->radjA_start[i];
+        const int *lb0 = c->radjB + c->radjB_start[j];
+        for (; *la >= 0 && arcL(c->t->arcs_a, *la) > al; ++la) {
+            int aL = arcL(c->t->arcs_a, *la);
+            for (const int *lb = lb0; *lb >= 0 && arcL(c->t->arcs_b, *lb) > bl; ++lb) {
+                sc_t d = DD(c, *la, *lb);
+                if (c->cnt) {
+                    c->cnt->arc_terms++;
+                    if (d != NEG_INF) c->cnt->valid_arc_terms++;
+                }
+                sc_t ns = MM(c, state, aL - 1, arcL(c->t->arcs_b, *lb) - 1) + d;
+                if (ns <= max_score) continue;
+                max_score = ns;
+            }
+        }
+    }
+    return max_score;
+}
+
+/* AlignerImpl::init_state, aligner.cc:264-368 */
+static void init_state(Ctx *c, int state, int al, int ar, int bl, int br,
+                       int globalA, int exclA, int globalB, int exclB) {
+    if (state < 4) {
+        for (int j = bl; j < br; ++j) c->E[state][j] = NEG_INF;
+    }
+    MM(c, state, al, bl) = 0;
+    sc_t indel = c->t->indel_opening;
+    if (exclA) indel = c->t->exclusion;
+    else if (!globalA) indel = 0;
+    int i;
+    for (i = al + 1; i < ar; ++i) {
+        if (minc(c, i) > bl) break;
+        if (indel != NEG_INF) {
+            if (!a_del(c, i, bl)) indel = NEG_INF;
+            else if (!exclA && globalA) indel = norm(indel + c->t->gap_a[i]);
+        }
+        MM(c, state, i, bl) = indel;
+    }
+    for (; i < ar; ++i) MM(c, state, i, minc(c, i) - 1) = NEG_INF;
+
+    indel = c->t->indel_opening;
+    if (exclB) indel = c->t->exclusion;
+    else if (!globalB) indel = 0;
+    int j;
+    int lim = maxc(c, al) + 1 < br ? maxc(c, al) + 1 : br;
+    for (j = bl + 1; j < lim; ++j) {
+        if (indel != NEG_INF) {
+            if (!a_ins(c, al, j)) indel = NEG_INF;
+            else if (!exclB && globalB) indel = norm(indel + c->t->gap_b[j]);
+        }
+        MM(c, state, al, j) = indel;
+    }
+    for (i = al + 1; i < ar; ++i) {
+        int l2 = maxc(c, i) + 1 < br ? maxc(c, i) + 1 : br;
+        for (; j < l2; ++j) MM(c, state, i - 1, j) = NEG_INF;
+    }
+}
+
+static inline int imax(int a, int b) { return a > b ? a : b; }
+static inline int imin(int a, int b) { return a < b ? a : b; }
+
+/* AlignerImpl::align_in_arcmatch, aligner.cc:373-565 */
+static void align_in_arcmatch(Ctx *c, int al, int ar, int bl, int br, int excl, int count) {
+    init_state(c, E_NO_NO, al, ar, bl, br, 1, 0, 1, 0);
+    if (excl) {
+        init_state(c, E_X_NO, al, ar, bl, br, 1, 1, 1, 0);
+        init_state(c, E_NO_X, al, ar, bl, br, 1, 0, 1, 1);
+        init_state(c, E_X_X, al, ar, bl, br, 1, 1, 1, 1);
+        init_state(c, E_OP_NO, al, ar, bl, br, 0, 0, 1, 0);
+        init_state(c, E_NO_OP, al, ar, bl, br, 1, 0, 0, 0);
+        init_state(c, E_X_OP, al, ar, bl, br, 1, 1, 0, 0);
+        init_state(c, E_OP_X, al, ar, bl, br, 0, 0, 1, 1);
+    }
+    for (int i = al + 1; i < ar; ++i) {
+        c->F[E_NO_NO] = NEG_INF;
+        int lo = imax(bl + 1, minc(c, i)), hi = imin(br - 1, maxc(c, i));
+        for (int j = lo; j <= hi; ++j) {
+            MM(c, E_NO_NO, i, j) = norm(align_noex(c, E_NO_NO, al, bl, i, j));
+            if (count && c->cnt) c->cnt->cells++;
+        }
+    }
+    if (!excl) return;
+    sc_t X = c->t->exclusion;
+#define ROWS_BEGIN for (int i = al + 1; i < ar; ++i) { int lo = imax(bl + 1, minc(c, i)), hi = imin(br - 1, maxc(c, i));
+#define ROWS_END }
+    ROWS_BEGIN for (int j = lo; j <= hi; ++j)
+        MM(c, E_OP_NO, i, j) = norm(smax(!a_del(c, i, j) ? NEG_INF : MM(c, E_OP_NO, i - 1, j), MM(c, E_NO_NO, i, j)));
+    ROWS_END
+    ROWS_BEGIN for (int j = lo; j <= hi; ++j)
+        MM(c, E_NO_OP, i, j) = norm(smax(!a_ins(c, i, j) ? NEG_INF : MM(c, E_NO_OP, i, j - 1), MM(c, E_NO_NO, i, j)));
+    ROWS_END
+    ROWS_BEGIN c->F[E_NO_X] = NEG_INF; for (int j = lo; j <= hi; ++j)
+        MM(c, E_NO_X, i, j) = norm(smax(align_noex(c, E_NO_X, al, bl, i, j), MM(c, E_NO_OP, i, j) + X));
+    ROWS_END
+    ROWS_BEGIN for (int j = lo; j <= hi; ++j)
+        MM(c, E_OP_X, i, j) = norm(smax(!a_del(c, i, j) ? NEG_INF : MM(c, E_OP_X, i - 1, j), MM(c, E_NO_X, i, j)));
+    ROWS_END
+    ROWS_BEGIN c->F[E_X_NO] = NEG_INF; for (int j = lo; j <= hi; ++j)
+        MM(c, E_X_NO, i, j) = norm(smax(align_noex(c, E_X_NO, al, bl, i, j), MM(c, E_OP_NO, i, j) + X));
+    ROWS_END
+    ROWS_BEGIN for (int j = lo; j <= hi; ++j)
+        MM(c, E_X_OP, i, j) = norm(smax(!a_ins(c, i, j) ? NEG_INF : MM(c, E_X_OP, i, j - 1), MM(c, E_X_NO, i, j)));
+    ROWS_END
+    ROWS_BEGIN c->F[E_X_X] = NEG_INF; for (int j = lo; j <= hi; ++j)
+        MM(c, E_X_X, i, j) = norm(smax(align_noex(c, E_X_X, al, bl, i, j),
+                                       smax(MM(c, E_OP_X, i, j) + X, MM(c, E_X_OP, i, j) + X)));
+    ROWS_END
+#undef ROWS_BEGIN
+#undef ROWS_END
+}
+
+/* AlignerImpl::fill_D_entries, aligner.cc:574-610 (no stacking) */
+static void fill_D_entries(Ctx *c, int al, int bl) {
+    size_t q = (size_t)al * (c->m + 1) + bl;
+    for (int p = c->cle_start[q]; p < c->cle_start[q + 1]; ++p) {
+        int k = c->cle[p];
+        int a = c->t->am_arcs[2 * k], b = c->t->am_arcs[2 * k + 1];
+        int ar = arcR(c->t->arcs_a, a), br = arcR(c->t->arcs_b, b);
+        sc_t mv = MM(c, 0, ar - 1, br - 1);
+        if (c->o->struct_local)
+            for (int s = 1; s < 4; ++s) mv = smax(mv, MM(c, s, ar - 1, br - 1));
+        DD(c, a, b) = norm(mv + c->t->am_score[k]);
+    }
+}
+
+/* AlignerImpl::align_D, aligner.cc:660-732 */
+static void align_D(Ctx *c) {
+    for (int al = c->n; al >= 1; --al) {
+        int max_bl = imin(c->m, maxc(c, al));
+        int min_bl = imax(1, minc(c, al));
+        for (int bl = max_bl; bl >= min_bl; --bl) {
+            if (!(a_match(c, al, bl) && valid_match(c, al, bl))) continue;
+            int max_ar = al, max_br = bl;
+            size_t q = (size_t)al * (c->m + 1) + bl;
+            for (int p = c->cle_start[q]; p < c->cle_start[q + 1]; ++p) {
+                int k = c->cle[p];
+                max_ar = imax(max_ar, arcR(c->t->arcs_a, c->t->am_arcs[2 * k]));
+                max_br = imax(max_br, arcR(c->t->arcs_b, c->t->am_arcs[2 * k + 1]));
+            }
+            if (al == max_ar || bl == max_br) continue;
+            if (c->cnt) c->cnt->groups++;
+            align_in_arcmatch(c, al, max_ar, bl, max_br, c->o->struct_local, 1);
+            fill_D_entries(c, al, bl);
+        }
+    }
+}
+
+/* align_top_level_free_endgaps, aligner.cc:736-819 */
+static sc_t top_free_endgaps(Ctx *c) {
+    int fe = c->o->free_endgaps;
+    int n = c->n, m = c->m;
+    init_state(c, E_NO_NO, 0, n + 1, 0, m + 1, !(fe & LCG_FREE_LEFT_2), 0, !(fe & LCG_FREE_LEFT_1), 0);
+    for (int i = 1; i <= n; ++i) {
+        c->F[E_NO_NO] = NEG_INF;
+        int lo = imax(1, minc(c, i)), hi = imin(m, maxc(c, i));
+        for (int j = lo; j <= hi; ++j) {
+            MM(c, E_NO_NO, i, j) = norm(align_noex(c, E_NO_NO, 0, 0, i, j));
+            if (c->cnt) c->cnt->cells++;
+        }
+    }
+    sc_t best = MM(c, E_NO_NO, n, m);
+    c->max_i = n; c->max_j = m;
+    if (fe & (LCG_FREE_RIGHT_1 | LCG_FREE_RIGHT_2)) {
+        best = NEG_INF; c->max_i = 0; c->max_j = 0;
+    }
+    int ra = c->t->right_anchor_a, rb = c->t->right_anchor_b;
+    if (fe & LCG_FREE_RIGHT_2) {
+        for (int i = imax(ra + 1, 1); i <= n; ++i)
+            if (maxc(c, i) >= m && MM(c, E_NO_NO, i, m) > best) { best = MM(c, E_NO_NO, i, m); c->max_i = i; c->max_j = m; }
+    }
+    if (fe & LCG_FREE_RIGHT_1) {
+        int lo = imax(imax(rb + 1, 1), minc(c, n)), hi = imin(m, maxc(c, n));
+        for (int j = lo; j <= hi; ++j)
+            if (MM(c, E_NO_NO, n, j) > best) { best = MM(c, E_NO_NO, n, j); c->max_i = n; c->max_j = j; }
+    }
+    return best;
+}
+
+/* align_top_level_locally, aligner.cc:823-880 */
+static sc_t top_locally(Ctx *c) {
+    int n = c->n, m = c->m;
+    sc_t best = 0;
+    c->max_i = 0; c->max_j = 0;
+    init_state(c, E_NO_NO, 0, n + 1, 0, m + 1, 0, 0, 0, 0);
+    int ra = c->t->right_anchor_a, rb = c->t->right_anchor_b;
+    int la = c->t->left_anchor_a, lb = c->t->left_anchor_b;
+    for (int i = 1; i <= n; ++i) {
+        c->F[E_NO_NO] = NEG_INF;
+        int lo = imax(1, minc(c, i)), hi = imin(m, maxc(c, i));
+        for (int j = lo; j <= hi; ++j) {
+            sc_t v = norm(align_noex(c, E_NO_NO, 0, 0, i, j));
+            if (i < la && j < lb) v = smax(0, v);
+            MM(c, E_NO_NO, i, j) = v;
+            if (c->cnt) c->cnt->cells++;
+            if (i >= ra && j >= rb && best < v) { best = v; c->max_i = i; c->max_j = j; }
+        }
+    }
+    return best;
+}
+
+/* ---------------------------------------------------------------- trace */
+
+static void append(Ctx *c, int a, int b) {
+    if (c->nedges < c->edge_cap) { c->edges[2 * c->nedges] = a; c->edges[2 * c->nedges + 1] = b; }
+    c->nedges++;
+}
+
+static void trace_in_arcmatch(Ctx *c, int state, int al, int i, int bl, int j, int tl);
+
+/* AlignerImpl::trace_arcmatch, aligner.cc:967-1028 (no stacking) */
+static void trace_arcmatch(Ctx *c, int k) {
+    int a = c->t->am_arcs[2 * k], b = c->t->am_arcs[2 * k + 1];
+    int al = arcL(c->t->arcs_a, a), ar = arcR(c->t->arcs_a, a);
+    int bl = arcL(c->t->arcs_b, b), br = arcR(c->t->arcs_b, b);
+    align_in_arcmatch(c, al, ar, bl, br, c->o->struct_local, 0);
+    if (!c->o->struct_local) {
+        trace_in_arcmatch(c, 0, al, ar - 1, bl, br - 1, 0);
+    } else {
+        for (int s = 0; s < 4; ++s) {
+            if (DD(c, a, b) == MM(c, s, ar - 1, br - 1) + c->t->am_score[k]) {
+                trace_in_arcmatch(c, s, al, ar - 1, bl, br - 1, 0);
+                break;
+            }
+        }
+    }
+}
+
+/* AlignerImpl::trace_noex, aligner.cc:1082-1229 */
+static void trace_noex(Ctx *c, int state, int oal, int i, int obl, int j, int tl) {
+    sc_t Mij = MM(c, state, i, j);
+    if (a_match(c, i, j) && valid(c, i - 1, j - 1) && Mij == MM(c, state, i - 1, j - 1) + sigma(c, i, j)) {
+        trace_in_arcmatch(c, state, oal, i - 1, obl, j - 1, tl);
+        append(c, i, j);
+        return;
+    }
+    if (c->t->indel_opening == 0) {
+        if (a_del(c, i, j) && valid(c, i - 1, j) && Mij == MM(c, state, i - 1, j) + c->t->gap_a[i]) {
+            trace_in_arcmatch(c, state, oal, i - 1, obl, j, tl);
+            append(c, i, -1);
+            return;
+        }
+        if (a_ins(c, i, j) && valid(c, i, j - 1) && Mij == MM(c, state, i, j - 1) + c->t->gap_b[j]) {
+            trace_in_arcmatch(c, state, oal, i, obl, j - 1, tl);
+            append(c, -1, j);
+            return;
+        }
+    } else {
+        sc_t gap = c->t->indel_opening;
+        for (int k = 1; i >= oal + k && a_del(c, i - k + 1, j); ++k) {
+            if (!valid(c, i - k, j)) break;
+            gap += c->t->gap_a[i - k + 1];
+            if (Mij == MM(c, state, i - k, j) + gap) {
+                trace_in_arcmatch(c, state, oal, i - k, obl, j, tl);
+                for (int l = k; l > 0; --l) append(c, i - l + 1, -1);
+                return;
+            }
+        }
+        gap = c->t->indel_opening;
+        for (int k = 1; j >= obl + k && a_ins(c, i, j - k + 1); ++k) {
+            if (!valid(c, i, j - k)) break;
+            gap += c->t->gap_b[j - k + 1];
+            if (Mij == MM(c, state, i, j - k) + gap) {
+                trace_in_arcmatch(c, state, oal, i, obl, j - k, tl);
+                for (int l = k; l > 0; --l) append(c, -1, j - l + 1);
+                return;
+            }
+        }
+    }
+    if (!(a_match(c, i, j) && valid(c, i - 1, j - 1))) return;
+    size_t q = (size_t)i * (c->m + 1) + j;
+    for (int p = c->cre_start[q]; p < c->cre_start[q + 1]; ++p) {
+        int k = c->cre[p];
+        int a = c->t->am_arcs[2 * k], b = c->t->am_arcs[2 * k + 1];
+        int al = arcL(c->t->arcs_a, a), bl = arcL(c->t->arcs_b, b);
+        if (al <= oal || bl <= obl) continue;
+        if (Mij == MM(c, state, al - 1, bl - 1) + DD(c, a, b)) {
+            trace_in_arcmatch(c, state, oal, al - 1, obl, bl - 1, tl);
+            if (c->ntam < c->tam_cap) c->tam[c->ntam] = k;
+            c->ntam++;
+            append(c, al, bl);
+            trace_arcmatch(c, k);
+            append(c, i, j);
+            return;
+        }
+    }
+}
+
+/* AlignerImpl::trace_in_arcmatch, aligner.cc:1233-1343 */
+static void trace_in_arcmatch(Ctx *c, int state, int al, int i, int bl, int j, int tl) {
+    sc_t Mij = MM(c, state, i, j);
+    if (tl && c->o->sequ_local && Mij == 0) { c->min_i = i; c->min_j = j; return; }
+    int fe = c->o->free_endgaps;
+    if (i <= al) {
+        if (state == E_NO_NO || state == E_OP_NO || state == E_X_NO) {
+            if (!(tl && (c->o->sequ_local || (fe & LCG_FREE_LEFT_1))))
+                for (int k = bl + 1; k <= j; ++k) append(c, -1, k);
+        }
+        return;
+    }
+    if (j <= bl) {
+        if (state == E_NO_NO || state == E_NO_OP || state == E_NO_X) {
+            if (!(tl && (c->o->sequ_local || (fe & LCG_FREE_LEFT_2))))
+                for (int k = al + 1; k <= i; ++k) append(c, k, -1);
+        }
+        return;
+    }
+    sc_t X = c->t->exclusion;
+    switch (state) {
+    case E_NO_NO: trace_noex(c, state, al, i, bl, j, tl); break;
+    case E_OP_NO:
+        if (Mij == MM(c, state, i - 1, j)) trace_in_arcmatch(c, state, al, i - 1, bl, j, tl);
+        else if (Mij == MM(c, E_NO_NO, i, j)) trace_in_arcmatch(c, E_NO_NO, al, i, bl, j, tl);
+        break;
+    case E_NO_OP:
+        if (Mij == MM(c, state, i, j - 1)) trace_in_arcmatch(c, state, al, i, bl, j - 1, tl);
+        else if (Mij == MM(c, E_NO_NO, i, j)) trace_in_arcmatch(c, E_NO_NO, al, i, bl, j, tl);
+        break;
+    case E_NO_X:
+        if (Mij == MM(c, E_NO_OP, i, j) + X) trace_in_arcmatch(c, E_NO_OP, al, i, bl, j, tl);
+        else trace_noex(c, state, al, i, bl, j, tl);
+        break;
+    case E_OP_X:
+        if (Mij == MM(c, state, i - 1, j)) trace_in_arcmatch(c, state, al, i - 1, bl, j, tl);
+        else if (Mij == MM(c, E_NO_X, i, j)) trace_in_arcmatch(c, E_NO_X, al, i, bl, j, tl);
+        break;
+    case E_X_NO:
+        if (Mij == MM(c, E_OP_NO, i, j) + X) trace_in_arcmatch(c, E_OP_NO, al, i, bl, j, tl);
+        else trace_noex(c, state, al, i, bl, j, tl);
+        break;
+    case E_X_OP:
+        if (Mij == MM(c, state, i, j - 1)) trace_in_arcmatch(c, state, al, i, bl, j - 1, tl);
+        else if (Mij == MM(c, E_X_NO, i, j)) trace_in_arcmatch(c, E_X_NO, al, i, bl, j, tl);
+        break;
+    case E_X_X:
+        if (Mij == MM(c, E_OP_X, i, j) + X) trace_in_arcmatch(c, E_OP_X, al, i, bl, j, tl);
+        else if (Mij == MM(c, E_X_OP, i, j) + X) trace_in_arcmatch(c, E_X_OP, al, i, bl, j, tl);
+        else trace_noex(c, state, al, i, bl, j, tl);
+        break;
+    }
+}
+
+/* ---------------------------------------------------------------- entry */
+
+static void ctx_free(Ctx *c) {
+    free(c->radjA_start); free(c->radjA); free(c->radjB_start); free(c->radjB);
+    free(c->cle_start); free(c->cle); free(c->cre_start); free(c->cre);
+    free(c->D);
+    for (int s = 0; s < 8; ++s) free(c->M[s]);
+    for (int s = 0; s < 4; ++s) free(c->E[s]);
+}
+
+/*
+ * Align one pair: Aligner::align() and, if opts->do_trace, Aligner::trace()
+ * (aligner.cc:924-957, 1345-1358). Returns 0, or -1 on allocation failure.
+ * counts may be NULL.
+ */
+int lcg_oracle_align(const lcg_pair_tables *t, const lcg_align_opts *o,
+                     lcg_align_result *r, lcg_work_counts *counts) {
+    Ctx c;
+    memset(&c, 0, sizeof c);
+    c.t = t; c.o = o; c.n = t->len_a; c.m = t->len_b; c.cnt = counts;
+    if (counts) memset(counts, 0, sizeof *counts);
+    build_radj(t->arcs_a, t->num_arcs_a, c.n, &c.radjA_start, &c.radjA);
+    build_radj(t->arcs_b, t->num_arcs_b, c.m, &c.radjB_start, &c.radjB);
+    build_am_lists(&c);
+    size_t nd = (size_t)t->num_arcs_a * t->num_arcs_b;
+    c.D = malloc((nd > 0 ? nd : 1) * sizeof(sc_t));
+    for (size_t q = 0; q < nd; ++q) c.D[q] = NEG_INF;
+    int ns = o->struct_local ? 8 : 1;
+    size_t cells = (size_t)(c.n + 1) * (c.m + 1);
+    for (int s = 0; s < ns; ++s) c.M[s] = calloc(cells, sizeof(sc_t));
+    for (int s = 0; s < (o->struct_local ? 4 : 1); ++s) c.E[s] = calloc(c.m + 1, sizeof(sc_t));
+    for (int s = 0; s < 8; ++s) if (!c.M[s]) c.M[s] = NULL;
+    if (!c.D || !c.M[0]) { ctx_free(&c); return -1; }
+    c.min_i = 1; c.min_j = 1; c.max_i = c.n; c.max_j = c.m;
+
+    align_D(&c);
+    sc_t score = o->sequ_local ? top_locally(&c) : top_free_endgaps(&c);
+    r->score = score < MIN_FINITY ? LCG_NEG_INF : score;
+    r->num_edges = 0; r->num_traced_am = 0;
+    if (o->do_trace) {
+        c.edges = r->edges; c.edge_cap = r->edges ? c.n + c.m : 0;
+        c.tam = r->traced_am; c.tam_cap = r->traced_am ? (c.n < c.m ? c.n : c.m) : 0;
+        trace_in_arcmatch(&c, E_NO_NO, 0, c.max_i, 0, c.max_j, 1);
+        r->num_edges = c.nedges; r->num_traced_am = c.ntam;
+    }
+    r->max_i = c.max_i; r->max_j = c.max_j; r->min_i = c.min_i; r->min_j = c.min_j;
+    ctx_free(&c);
+    return 0;
+}

@@ -1,0 +1,46 @@
+"""Parser of the reference harness output (oracle/ref_harness.cc).
+
+Test infrastructure: turns one ``LCGREF 1`` text block into the prepared
+tables (``PairTables``) plus the reference's results.
+"""
+import numpy as np
+
+from locarna_gb300.abi import PairTables
+
+
+def _pairs(tokens, conv=int):
+    return [tuple(conv(x) for x in t.split(":")) for t in tokens]
+
+
+def parse_ref(text):
+    rec = {}
+    for line in text.splitlines():
+        if not line.strip():
+            continue
+        key, _, rest = line.partition(" ")
+        rec[key] = rest.split() if key not in ("seqA", "seqB", "structA", "structB") else rest.strip()
+    n, m = (int(x) for x in rec["lens"])
+    out = {"len_a": n, "len_b": m, "seq_a": rec["seqA"], "seq_b": rec["seqB"]}
+    io, ex = (int(x) for x in rec["params"])
+    band = _pairs(rec["band"])
+    out["min_col"] = [b[0] for b in band]
+    out["max_col"] = [b[1] for b in band]
+    out["num_arcs"] = tuple(int(x) for x in rec["narcs"])
+    out["num_am"] = int(rec["nam"][0])
+    out["score"] = int(rec["score"][0])
+    out["edges"] = _pairs(rec["edges"])
+    out["struct_a"] = rec["structA"]
+    out["struct_b"] = rec["structB"]
+    out["align_seconds"] = float(rec["align_seconds"][0])
+    if "sigma" in rec:
+        sig = np.zeros((n + 1, m + 1), dtype=np.int32)
+        sig[1:, 1:] = np.array([int(x) for x in rec["sigma"]], dtype=np.int32).reshape(n, m)
+        arcs_a = np.array(_pairs(rec["arcsA"]), dtype=np.int32).reshape(-1, 2)
+        arcs_b = np.array(_pairs(rec["arcsB"]), dtype=np.int32).reshape(-1, 2)
+        am = np.array(_pairs(rec["am"]), dtype=np.int32).reshape(-1, 3)
+        out["tables"] = PairTables(
+            n, m, sig, [int(x) for x in rec["gapA"]], [int(x) for x in rec["gapB"]],
+            io, ex, arcs_a, arcs_b, am[:, :2], am[:, 2], out["min_col"], out["max_col"],
+            seq_a=rec["seqA"], seq_b=rec["seqB"])
+        out["anchor_match"] = _pairs(rec["anchor_match"])
+    return out
