@@ -162,6 +162,54 @@ lcg_status lcg_align_pairs(lcg_engine eng, const lcg_pair_tables *pairs,
 lcg_status lcg_engine_last_stats(lcg_engine eng, double *kernel_ms,
                                  int64_t *launches);
 
+
+/* ------------------------------------------------------ host preparation
+ *
+ * Builds lcg_pair_tables from two PP 2.0 inputs the way the reference's
+ * locarna driver builds its Scoring / ArcMatches / TraceController objects
+ * (src/locarna.cc:398-703): PP reading (rna_data.cc:979-1104), arcs
+ * (basepairs.cc:155-205), sigma / gap / arc weights / arc-match scores
+ * (scoring.cc:28-554, RIBOSUM85_60 built in), the max-diff band
+ * (trace_controller.cc:360-390) and the sequence envelope
+ * (edge_probs.icc:7-268, trace_controller.cc:565-597). Single-sequence
+ * inputs without anchors.
+ */
+typedef struct lcg_prep_opts {
+    double min_prob;              /* --min-prob (0.001) */
+    int32_t indel;                /* --indel (-150) */
+    int32_t indel_opening;        /* --indel-opening (-750) */
+    int32_t struct_weight;        /* --struct-weight (200) */
+    int32_t tau;                  /* --tau (50) */
+    int32_t exclusion;            /* --exclusion (0) */
+    int32_t match, mismatch;      /* --match (50) / --mismatch (0) */
+    int32_t use_ribosum;          /* --use-ribosum (1) */
+    double min_trace_probability; /* --min-trace-probability (1e-4) */
+    int32_t max_diff;             /* --max-diff (-1) */
+    int32_t max_diff_am;          /* --max-diff-am (-1) */
+    int32_t max_diff_at_am;       /* --max-diff-at-am (-1) */
+    int32_t temperature_alipf;    /* --temperature-alipf (300) */
+    int32_t sequ_local;           /* --sequ-local: local envelope */
+    int32_t free_endgaps;         /* LCG_FREE_* bits for the envelope */
+    int32_t pf_precision;         /* envelope float type: 0 double, 1 long double (locarna's default) */
+    double exp_prob;              /* --exp-prob; <= 0 means 1/(2 len) per sequence */
+} lcg_prep_opts;
+
+typedef struct lcg_prepared_s *lcg_prepared;
+
+/* Defaults of the locarna command line (src/locarna.cc:83-272). */
+void lcg_prep_opts_default(lcg_prep_opts *opts);
+
+/* Parse two PP 2.0 texts and build the pair's tables (opts NULL = defaults). */
+lcg_status lcg_prepare_pair(const char *pp_a, const char *pp_b, const lcg_prep_opts *opts,
+                            lcg_prepared *out);
+/* Views into the prepared tables; valid until lcg_prepared_free. */
+lcg_status lcg_prepared_tables(lcg_prepared p, lcg_pair_tables *out);
+/* which: 0 sequence A, 1 sequence B, 2 name A, 3 name B */
+const char *lcg_prepared_sequence(lcg_prepared p, int32_t which);
+/* 0 if the envelope partition function failed (PFGotoh::fail, edge_probs.hh:202) */
+int32_t lcg_prepared_envelope_ok(lcg_prepared p);
+lcg_status lcg_prepared_free(lcg_prepared p);
+
 #ifdef __cplusplus
 }
 #endif

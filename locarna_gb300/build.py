@@ -1,0 +1,101 @@
+"""Build the native parts in-tree.
+
+* ``locarna_gb300/_build/liblocarna_gb300.so``: the CUDA engine (sm_103a) and
+  the C ABI of include/locarna_gb300.h;
+* ``oracle/_build/liboracle.so``: the plain-C oracle (test infrastructure);
+* ``oracle/_ref/*``: the reference's own sources compiled as an oracle, only
+  where the reference sources are present (``oracle/build_ref.sh``).
+
+Translation units are compiled in parallel; one ``-gencode`` for sm_103a.
+"""
+import os
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+PKG = os.path.join(ROOT, "locarna_gb300")
+CSRC = os.path.join(PKG, "csrc")
+OUT = os.path.join(PKG, "_build")
+ORACLE = os.path.join(ROOT, "oracle")
+NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
+GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
+
+CUDA_SOURCES = ["engine.cu", "sankoff_kernels.cu"]
+HOST_SOURCES = ["host_prep.cpp"]  # C++ host-only translation units
+
+
+def _run(cmd):
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("build failed: " + " ".join(cmd) + "\n" + r.stdout + r.stderr)
+    return r.stdout + r.stderr
+
+
+def _newer(target, deps):
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def build_engine(verbose=False, force=False):
+    os.makedirs(OUT, exist_ok=True)
+    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h", ".hh"))]
+    headers.append(os.path.join(ROOT, "include", "locarna_gb300.h"))
+    objs = []
+    jobs = []
+    for src in CUDA_SOURCES:
+        s = os.path.join(CSRC, src)
+        o = os.path.join(OUT, src + ".o")
+        objs.append(o)
+        if force or _newer(o, [s] + headers):
+            jobs.append([NVCC, GENCODE, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+                         "-Xptxas", "-v" if verbose else "-O3", "-c", s, "-o", o])
+    for src in HOST_SOURCES:
+        s = os.path.join(CSRC, src)
+        o = os.path.join(OUT, src + ".o")
+        objs.append(o)
+        if force or _newer(o, [s] + headers):
+            jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off",
+                         "-I", os.path.join(ROOT, "include"), "-c", s, "-o", o])
+    with ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
+        logs = list(ex.map(_run, jobs))
+    if verbose:
+        for log in logs:
+            sys.stdout.write(log)
+    lib = os.path.join(OUT, "liblocarna_gb300.so")
+    if force or jobs or not os.path.exists(lib):
+        _run([NVCC, GENCODE, "-shared", "-o", lib] + objs + ["-lcudart"])
+    return lib
+
+
+def build_oracle():
+    out = os.path.join(ORACLE, "_build")
+    os.makedirs(out, exist_ok=True)
+    lib = os.path.join(out, "liboracle.so")
+    srcs = [os.path.join(ORACLE, "sankoff_oracle.c")]
+    if _newer(lib, srcs + [os.path.join(ROOT, "include", "locarna_gb300.h")]):
+        _run(["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-ffp-contract=off"] + srcs + ["-o", lib])
+    return lib
+
+
+def build_reference_oracle():
+    """Compile the reference sources as an oracle when they are present."""
+    ref = os.environ.get("LOCARNA_REF", "/root/reference")
+    if not os.path.isdir(os.path.join(ref, "src", "LocARNA")):
+        return None
+    _run(["bash", os.path.join(ORACLE, "build_ref.sh")])
+    return os.path.join(ORACLE, "_ref")
+
+
+def build_all(verbose=False):
+    with ThreadPoolExecutor(max_workers=3) as ex:
+        f1 = ex.submit(build_engine, verbose)
+        f2 = ex.submit(build_oracle)
+        f3 = ex.submit(build_reference_oracle)
+        return f1.result(), f2.result(), f3.result()
+
+
+if __name__ == "__main__":
+    print(build_all(verbose="-v" in sys.argv))

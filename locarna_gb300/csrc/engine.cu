@@ -1,0 +1,651 @@
+// Host side of the GB300 Sankoff engine: validation of the prepared tables,
+// derived index structures, one packed host->device upload per batch, the two
+// kernel launches, one device->host download, and assembly of the traceback
+// tokens into the reference's edge order. Exposes the C ABI of
+// include/locarna_gb300.h.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/locarna_gb300.h"
+#include "lcg_device.cuh"
+
+namespace lcg {
+cudaError_t launch_fill(const PairDev *, const GroupItem *, int, const int4 *, int *, long long,
+                        int, unsigned int *, int *, int *, int, cudaStream_t);
+cudaError_t launch_trace(const PairDev *, int, int *, long long, int, int *, cudaStream_t);
+int fill_warps_per_block();
+cudaError_t fill_occupancy(int sw, int *blocks_per_sm);
+cudaError_t trace_prepare(int sw);
+}  // namespace lcg
+
+using namespace lcg;
+
+static thread_local std::string g_last_error;
+
+namespace lcg_host {
+void set_error(const std::string &msg) { g_last_error = msg; }
+}  // namespace lcg_host
+
+static lcg_status fail(lcg_status code, const std::string &msg) {
+    g_last_error = msg;
+    return code;
+}
+
+#define CUDA_TRY(call)                                                                  \
+    do {                                                                                \
+        cudaError_t _e = (call);                                                        \
+        if (_e != cudaSuccess)                                                          \
+            return fail(LCG_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(_e)); \
+    } while (0)
+
+// ------------------------------------------------------------------ per-pair prep
+
+namespace {
+
+struct Prep {
+    int n = 0, m = 0;
+    int flags = 0, fe = 0;
+    int bandcells = 0;
+    std::vector<int> min_col, max_col, bandoff;  // n+2
+    std::vector<int> cre_start;                  // bandcells+1
+    std::vector<int> cre;                        // 2 per entry
+    std::vector<int> am_ends;                    // 4 per am
+    std::vector<int> Dinit;                      // per am
+    std::vector<GroupItem> groups;               // pair field filled later
+    std::vector<int4> dw;                        // dw_start relative to this pair
+    int rows_max = 0, width_max = 0;             // over groups
+    int token_cap = 0, tq_cap = 0;
+    std::string err;
+    lcg_status code = LCG_OK;
+};
+
+inline bool allowed_match(const lcg_pair_tables &t, int i, int j) {
+    return !t.match_lo || (t.match_lo[i] <= j && j <= t.match_hi[i]);
+}
+
+lcg_status prep_pair(const lcg_pair_tables &t, const lcg_align_opts &o, Prep &p) {
+    auto bad = [&](lcg_status c, const std::string &s) {
+        p.code = c;
+        p.err = s;
+        return c;
+    };
+    const int n = t.len_a, m = t.len_b;
+    if (n < 1 || m < 1) return bad(LCG_ERR_UNSUPPORTED, "empty sequence");
+    if (n > 32000 || m > 32000) return bad(LCG_ERR_UNSUPPORTED, "sequence longer than 32000");
+    if (!t.sigma || !t.gap_a || !t.gap_b || !t.min_col || !t.max_col)
+        return bad(LCG_ERR_ARG, "NULL table pointer");
+    if (t.num_arcs_a < 0 || t.num_arcs_b < 0 || t.num_arcmatches < 0)
+        return bad(LCG_ERR_ARG, "negative count");
+    if ((t.num_arcs_a && !t.arcs_a) || (t.num_arcs_b && !t.arcs_b) ||
+        (t.num_arcmatches && (!t.am_arcs || !t.am_score)))
+        return bad(LCG_ERR_ARG, "NULL arc table");
+    const bool anchors = t.match_lo != nullptr;
+    if (anchors && (!t.match_hi || !t.del_lo || !t.del_hi || !t.ins_lo || !t.ins_hi))
+        return bad(LCG_ERR_ARG, "anchor ranges must be all set or all NULL");
+    if (o.struct_local) return bad(LCG_ERR_UNSUPPORTED, "structure-local mode is not implemented on the GPU yet");
+    p.n = n;
+    p.m = m;
+    p.fe = o.free_endgaps & 15;
+    p.flags = (o.sequ_local ? PF_SEQU_LOCAL : 0) | (anchors ? PF_ANCHORS : 0) |
+              (o.do_trace ? PF_TRACE : 0);
+    if (o.sequ_local && p.fe) return bad(LCG_ERR_ARG, "free end gaps cannot be combined with local alignment");
+
+    // band: monotone, inside [0,m], rows non-empty and connected
+    // (trace_controller.cc:320-339 asserts the same invariants)
+    p.min_col.resize(n + 2);
+    p.max_col.resize(n + 2);
+    p.bandoff.resize(n + 2);
+    long long cells = 0;
+    for (int i = 0; i <= n; ++i) {
+        int lo = t.min_col[i], hi = t.max_col[i];
+        if (lo < 0 || hi > m || lo > hi) return bad(LCG_ERR_ARG, "band row " + std::to_string(i) + " out of range");
+        if (i > 0 && (lo < t.min_col[i - 1] || hi < t.max_col[i - 1] || t.max_col[i - 1] + 1 < lo))
+            return bad(LCG_ERR_ARG, "band not monotone/connected at row " + std::to_string(i));
+        p.min_col[i] = lo;
+        p.max_col[i] = hi;
+        p.bandoff[i] = (int)cells;
+        cells += hi - lo + 1;
+    }
+    p.min_col[n + 1] = m + 1;
+    p.max_col[n + 1] = m;
+    p.bandoff[n + 1] = (int)cells;
+    if (cells > (1ll << 30)) return bad(LCG_ERR_UNSUPPORTED, "band too large");
+    p.bandcells = (int)cells;
+    if (!o.sequ_local && !(p.fe & (LCG_FREE_RIGHT_1 | LCG_FREE_RIGHT_2)) && p.max_col[n] != m)
+        return bad(LCG_ERR_UNSUPPORTED, "global alignment needs (lenA,lenB) inside the band");
+    if (p.min_col[0] != 0) return bad(LCG_ERR_UNSUPPORTED, "band must contain (0,0)");
+
+    // score range: every alignment score is a sum of at most (n+m) position
+    // terms, (n+m) gap openings and min(n,m)/2 arc-match terms
+    long long ms = 0, mg = 0, mam = 0;
+    for (long long q = 0; q < (long long)(n + 1) * (m + 1); ++q) ms = std::max(ms, (long long)std::llabs(t.sigma[q]));
+    for (int i = 0; i <= n; ++i) mg = std::max(mg, (long long)std::llabs(t.gap_a[i]));
+    for (int j = 0; j <= m; ++j) mg = std::max(mg, (long long)std::llabs(t.gap_b[j]));
+    for (int k = 0; k < t.num_arcmatches; ++k) mam = std::max(mam, (long long)std::llabs(t.am_score[k]));
+    long long bound = (long long)(n + m) * (ms + mg + std::llabs(t.indel_opening) + std::llabs(t.exclusion)) +
+                      (long long)(std::min(n, m) / 2 + 1) * mam;
+    if (bound >= (1ll << 27)) return bad(LCG_ERR_RANGE, "scores may exceed the int32 device range");
+
+    for (int k = 0; k < t.num_arcs_a; ++k) {
+        int l = t.arcs_a[2 * k], r = t.arcs_a[2 * k + 1];
+        if (l < 1 || r > n || l >= r) return bad(LCG_ERR_ARG, "arc of A out of range");
+    }
+    for (int k = 0; k < t.num_arcs_b; ++k) {
+        int l = t.arcs_b[2 * k], r = t.arcs_b[2 * k + 1];
+        if (l < 1 || r > m || l >= r) return bad(LCG_ERR_ARG, "arc of B out of range");
+    }
+    const int na = t.num_arcmatches;
+    p.am_ends.resize(4 * (size_t)na);
+    for (int k = 0; k < na; ++k) {
+        int a = t.am_arcs[2 * k], b = t.am_arcs[2 * k + 1];
+        if (a < 0 || a >= t.num_arcs_a || b < 0 || b >= t.num_arcs_b) return bad(LCG_ERR_ARG, "arc match index out of range");
+        p.am_ends[4 * k] = t.arcs_a[2 * a];
+        p.am_ends[4 * k + 1] = t.arcs_a[2 * a + 1];
+        p.am_ends[4 * k + 2] = t.arcs_b[2 * b];
+        p.am_ends[4 * k + 3] = t.arcs_b[2 * b + 1];
+    }
+    auto in_band = [&](int i, int j) { return i >= 0 && i <= n && p.min_col[i] <= j && j <= p.max_col[i]; };
+
+    // common right end lists over band cells, lex greater left ends
+    // (arc_matches.cc:76-110, arc_matches.hh:188-220)
+    std::vector<int> cnt(p.bandcells + 1, 0);
+    std::vector<int> cell_of(na, -1);
+    for (int k = 0; k < na; ++k) {
+        int ar = p.am_ends[4 * k + 1], br = p.am_ends[4 * k + 3];
+        if (in_band(ar, br)) {
+            cell_of[k] = p.bandoff[ar] + br - p.min_col[ar];
+            cnt[cell_of[k]]++;
+        }
+    }
+    p.cre_start.assign(p.bandcells + 1, 0);
+    for (int c = 0; c < p.bandcells; ++c) p.cre_start[c + 1] = p.cre_start[c] + cnt[c];
+    std::vector<int> fillp(p.cre_start.begin(), p.cre_start.end() - 1);
+    std::vector<int> ord(p.cre_start[p.bandcells]);
+    for (int k = 0; k < na; ++k)
+        if (cell_of[k] >= 0) ord[fillp[cell_of[k]]++] = k;
+    p.cre.resize(2 * ord.size());
+    for (int c = 0; c < p.bandcells; ++c) {
+        auto b = ord.begin() + p.cre_start[c], e = ord.begin() + p.cre_start[c + 1];
+        if (e - b > 1)
+            std::sort(b, e, [&](int x, int y) {
+                int alx = p.am_ends[4 * x], aly = p.am_ends[4 * y];
+                if (alx != aly) return alx > aly;
+                return p.am_ends[4 * x + 2] > p.am_ends[4 * y + 2];
+            });
+    }
+    for (size_t q = 0; q < ord.size(); ++q) {
+        int k = ord[q];
+        p.cre[2 * q] = k;
+        p.cre[2 * q + 1] = (p.am_ends[4 * k] << 16) | p.am_ends[4 * k + 2];
+    }
+
+    // left-end groups (aligner.cc:660-732): bucket arc matches by (al,bl)
+    std::vector<std::pair<long long, int>> byleft(na);
+    for (int k = 0; k < na; ++k)
+        byleft[k] = {(long long)p.am_ends[4 * k] * (m + 1) + p.am_ends[4 * k + 2], k};
+    std::stable_sort(byleft.begin(), byleft.end(),
+                     [](const auto &x, const auto &y) { return x.first > y.first; });
+    p.Dinit.assign(na, NEG);
+    p.rows_max = 0;
+    p.width_max = 0;
+    for (size_t s = 0; s < byleft.size();) {
+        size_t e = s;
+        while (e < byleft.size() && byleft[e].first == byleft[s].first) ++e;
+        int k0 = byleft[s].second;
+        int al = p.am_ends[4 * k0], bl = p.am_ends[4 * k0 + 2];
+        if (allowed_match(t, al, bl) && in_band(al, bl) && in_band(al - 1, bl - 1)) {
+            int max_ar = al, max_br = bl;
+            for (size_t q = s; q < e; ++q) {
+                int k = byleft[q].second;
+                max_ar = std::max(max_ar, p.am_ends[4 * k + 1]);
+                max_br = std::max(max_br, p.am_ends[4 * k + 3]);
+            }
+            GroupItem g{};
+            g.al = al;
+            g.ar = max_ar;
+            g.bl = bl;
+            g.br = max_br;
+            g.dw_start = (int)p.dw.size();
+            g.top = 0;
+            std::vector<int> ks;
+            for (size_t q = s; q < e; ++q) ks.push_back(byleft[q].second);
+            std::stable_sort(ks.begin(), ks.end(), [&](int x, int y) { return p.am_ends[4 * x + 1] < p.am_ends[4 * y + 1]; });
+            for (int k : ks) {
+                int ar = p.am_ends[4 * k + 1], br = p.am_ends[4 * k + 3];
+                // the inner corner (ar-1,br-1) is computed by this group iff it is in the band
+                if (ar - 1 > al && br - 1 > bl && in_band(ar - 1, br - 1)) {
+                    p.dw.push_back(make_int4(k, ar - 1, br - 1, t.am_score[k]));
+                    p.Dinit[k] = NOT_READY;
+                }
+            }
+            g.dw_count = (int)p.dw.size() - g.dw_start;
+            p.groups.push_back(g);
+            p.rows_max = std::max(p.rows_max, max_ar - al);
+            p.width_max = std::max(p.width_max, max_br - bl + 1);
+        }
+        s = e;
+    }
+    // byleft is sorted by (al*(m+1)+bl) descending = al descending, bl descending
+    GroupItem top{};
+    top.al = 0;
+    top.ar = n + 1;
+    top.bl = 0;
+    top.br = m + 1;
+    top.top = 1;
+    p.groups.push_back(top);
+    p.token_cap = 2 * (n + m) + 3 * std::min(n, m) + 16;
+    p.tq_cap = std::min(n, m) / 2 + 2;
+    return LCG_OK;
+}
+
+// expand token segments into the reference's append order
+struct Assembler {
+    const int2 *tok;
+    std::vector<std::pair<int, int>> seg_of;  // am -> (start,end) ; index via map
+    std::vector<int> seg_am;
+    std::vector<int> seg_start, seg_end;
+    int32_t *edges;
+    int edge_cap, nedges = 0;
+    int32_t *tam;
+    int tam_cap, ntam = 0;
+    bool ok = true;
+    int find(int am) const {
+        for (size_t s = 0; s < seg_am.size(); ++s)
+            if (seg_am[s] == am) return (int)s;
+        return -1;
+    }
+    void expand(int s, int depth) {
+        if (s < 0 || depth > 100000) {
+            ok = false;
+            return;
+        }
+        for (int q = seg_end[s] - 1; q >= seg_start[s]; --q) {
+            int2 t = tok[q];
+            if (t.x == -2) {
+                if (ntam < tam_cap && tam) tam[ntam] = t.y;
+                ++ntam;
+                expand(find(t.y), depth + 1);
+            } else {
+                if (nedges < edge_cap && edges) {
+                    edges[2 * nedges] = t.x;
+                    edges[2 * nedges + 1] = t.y;
+                }
+                ++nedges;
+            }
+        }
+    }
+};
+
+size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+}  // namespace
+
+// ------------------------------------------------------------------ engine
+
+struct lcg_engine_s {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int sms = 0;
+    char *d_arena = nullptr;
+    size_t arena_cap = 0;
+    char *h_stage = nullptr;
+    size_t stage_cap = 0;
+    int *d_scratch = nullptr;
+    size_t scratch_cap = 0;  // ints
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr;
+    double last_ms = 0;
+    long long last_launches = 0;
+};
+
+extern "C" {
+
+const char *lcg_last_error(void) { return g_last_error.c_str(); }
+
+int32_t lcg_abi_version(void) { return LCG_ABI_VERSION; }
+
+lcg_status lcg_engine_create(int32_t device, void *stream, lcg_engine *out) {
+    if (!out) return fail(LCG_ERR_ARG, "out is NULL");
+    *out = nullptr;
+    int ndev = 0;
+    CUDA_TRY(cudaGetDeviceCount(&ndev));
+    if (device < 0 || device >= ndev) return fail(LCG_ERR_ARG, "no such CUDA device");
+    CUDA_TRY(cudaSetDevice(device));
+    auto *e = new lcg_engine_s();
+    e->device = device;
+    if (stream) {
+        e->stream = (cudaStream_t)stream;
+    } else {
+        if (cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) != cudaSuccess) {
+            delete e;
+            return fail(LCG_ERR_CUDA, "cudaStreamCreate failed");
+        }
+        e->own_stream = true;
+    }
+    cudaDeviceGetAttribute(&e->sms, cudaDevAttrMultiProcessorCount, device);
+    cudaEventCreate(&e->ev0);
+    cudaEventCreate(&e->ev1);
+    cudaEventCreate(&e->ev2);
+    *out = e;
+    return LCG_OK;
+}
+
+lcg_status lcg_engine_destroy(lcg_engine e) {
+    if (!e) return LCG_OK;
+    cudaSetDevice(e->device);
+    if (e->stream) cudaStreamSynchronize(e->stream);
+    if (e->d_arena) cudaFree(e->d_arena);
+    if (e->d_scratch) cudaFree(e->d_scratch);
+    if (e->h_stage) cudaFreeHost(e->h_stage);
+    if (e->ev0) cudaEventDestroy(e->ev0);
+    if (e->ev1) cudaEventDestroy(e->ev1);
+    if (e->ev2) cudaEventDestroy(e->ev2);
+    if (e->own_stream) cudaStreamDestroy(e->stream);
+    delete e;
+    return LCG_OK;
+}
+
+lcg_status lcg_engine_last_stats(lcg_engine e, double *kernel_ms, int64_t *launches) {
+    if (!e) return fail(LCG_ERR_ARG, "engine is NULL");
+    if (kernel_ms) *kernel_ms = e->last_ms;
+    if (launches) *launches = e->last_launches;
+    return LCG_OK;
+}
+
+lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t npairs,
+                           const lcg_align_opts *opts, lcg_align_result *results) {
+    if (!e || !pairs || !opts || !results || npairs < 0) return fail(LCG_ERR_ARG, "NULL argument");
+    if (npairs == 0) return LCG_OK;
+    CUDA_TRY(cudaSetDevice(e->device));
+
+    // ---- host preparation (threads over pairs)
+    std::vector<Prep> prep(npairs);
+    {
+        std::atomic<int> next(0);
+        int nth = (int)std::min<unsigned>(std::max(1u, std::thread::hardware_concurrency()), (unsigned)npairs);
+        nth = std::min(nth, 64);
+        auto work = [&]() {
+            for (int q; (q = next.fetch_add(1)) < npairs;) prep_pair(pairs[q], *opts, prep[q]);
+        };
+        std::vector<std::thread> th;
+        for (int t = 1; t < nth; ++t) th.emplace_back(work);
+        work();
+        for (auto &t : th) t.join();
+    }
+    for (int q = 0; q < npairs; ++q)
+        if (prep[q].code != LCG_OK) return fail(prep[q].code, "pair " + std::to_string(q) + ": " + prep[q].err);
+
+    // ---- arena layout
+    int sw = 0, rows_max = 1;
+    for (auto &p : prep) {
+        sw = std::max(sw, std::max(p.width_max + 1, p.m + 2));
+        rows_max = std::max(rows_max, p.rows_max + 1);
+    }
+    struct Off {
+        size_t sigma, gapA, gapB, minc, maxc, bandoff, anc, cre_start, cre, am_ends, am_score, D,
+            topM, res, tok, tq, segs;
+    };
+    std::vector<Off> off(npairs);
+    size_t up = 0;  // upload section (bytes)
+    auto take = [](size_t &cur, size_t bytes) {
+        size_t o = cur;
+        cur = align_up(cur + bytes, 16);
+        return o;
+    };
+    size_t off_pairs = take(up, sizeof(PairDev) * npairs);
+    size_t nitems = 0, ndw = 0;
+    for (auto &p : prep) {
+        nitems += p.groups.size();
+        ndw += p.dw.size();
+    }
+    size_t off_items = take(up, sizeof(GroupItem) * nitems);
+    size_t off_dw = take(up, sizeof(int4) * std::max<size_t>(ndw, 1));
+    size_t off_ctrl = take(up, 64);
+    for (int q = 0; q < npairs; ++q) {
+        const auto &p = prep[q];
+        const auto &t = pairs[q];
+        Off &o = off[q];
+        o.sigma = take(up, 4ull * (p.n + 1) * (p.m + 1));
+        o.gapA = take(up, 4ull * (p.n + 1));
+        o.gapB = take(up, 4ull * (p.m + 1));
+        o.minc = take(up, 4ull * (p.n + 2));
+        o.maxc = take(up, 4ull * (p.n + 2));
+        o.bandoff = take(up, 4ull * (p.n + 2));
+        o.anc = t.match_lo ? take(up, 4ull * (2 * (p.n + 1) + 2 * (p.n + 1) + 2 * (p.m + 1))) : 0;
+        o.cre_start = take(up, 4ull * (p.bandcells + 1));
+        o.cre = take(up, 4ull * std::max<size_t>(p.cre.size(), 2));
+        o.am_ends = take(up, 4ull * std::max<size_t>(p.am_ends.size(), 4));
+        o.am_score = take(up, 4ull * std::max(t.num_arcmatches, 1));
+        o.D = take(up, 4ull * std::max(t.num_arcmatches, 1));
+    }
+    size_t down_begin = up;
+    size_t dn = up;
+    for (int q = 0; q < npairs; ++q) {
+        const auto &p = prep[q];
+        Off &o = off[q];
+        o.res = take(dn, 4ull * R_NWORDS);
+        o.tok = take(dn, 8ull * p.token_cap);
+        o.segs = take(dn, 16ull * (p.tq_cap + 1));
+    }
+    size_t down_end = dn;
+    size_t dev_only = dn;
+    for (int q = 0; q < npairs; ++q) {
+        const auto &p = prep[q];
+        Off &o = off[q];
+        o.tq = take(dev_only, 4ull * p.tq_cap);
+        o.topM = take(dev_only, 4ull * (p.n + 1) * (p.m + 1));
+    }
+    size_t total = dev_only;
+
+    if (total > e->arena_cap) {
+        if (e->d_arena) cudaFree(e->d_arena);
+        e->d_arena = nullptr;
+        e->arena_cap = 0;
+        size_t cap = total + total / 4;
+        if (cudaMalloc(&e->d_arena, cap) != cudaSuccess) return fail(LCG_ERR_NOMEM, "device arena allocation failed");
+        e->arena_cap = cap;
+    }
+    if (down_end > e->stage_cap) {
+        if (e->h_stage) cudaFreeHost(e->h_stage);
+        e->h_stage = nullptr;
+        e->stage_cap = 0;
+        size_t cap = down_end + down_end / 4;
+        if (cudaMallocHost(&e->h_stage, cap) != cudaSuccess) return fail(LCG_ERR_NOMEM, "pinned staging allocation failed");
+        e->stage_cap = cap;
+    }
+    char *H = e->h_stage;
+    char *Dv = e->d_arena;
+
+    // ---- pack the upload
+    PairDev *hp = (PairDev *)(H + off_pairs);
+    GroupItem *hitems = (GroupItem *)(H + off_items);
+    int4 *hdw = (int4 *)(H + off_dw);
+    size_t it = 0, dwb = 0;
+    {
+        // interleave the pairs' work lists so that every pair progresses
+        // proportionally; within a pair the order is kept
+        std::vector<std::pair<double, std::pair<int, int>>> order;
+        order.reserve(nitems);
+        for (int q = 0; q < npairs; ++q) {
+            size_t G = prep[q].groups.size();
+            for (size_t g = 0; g < G; ++g) order.push_back({(double)(g + 1) / (double)G, {q, (int)g}});
+        }
+        std::stable_sort(order.begin(), order.end(), [](const auto &a, const auto &b) { return a.first < b.first; });
+        std::vector<size_t> dwbase(npairs);
+        for (int q = 0; q < npairs; ++q) {
+            dwbase[q] = dwb;
+            std::memcpy(hdw + dwb, prep[q].dw.data(), sizeof(int4) * prep[q].dw.size());
+            dwb += prep[q].dw.size();
+        }
+        for (auto &x : order) {
+            int q = x.second.first;
+            GroupItem g = prep[q].groups[x.second.second];
+            g.pair = q;
+            g.dw_start += (int)dwbase[q];
+            hitems[it++] = g;
+        }
+    }
+    std::memset(H + off_ctrl, 0, 64);
+    for (int q = 0; q < npairs; ++q) {
+        const auto &p = prep[q];
+        const auto &t = pairs[q];
+        const Off &o = off[q];
+        std::memcpy(H + o.sigma, t.sigma, 4ull * (p.n + 1) * (p.m + 1));
+        std::memcpy(H + o.gapA, t.gap_a, 4ull * (p.n + 1));
+        std::memcpy(H + o.gapB, t.gap_b, 4ull * (p.m + 1));
+        std::memcpy(H + o.minc, p.min_col.data(), 4ull * (p.n + 2));
+        std::memcpy(H + o.maxc, p.max_col.data(), 4ull * (p.n + 2));
+        std::memcpy(H + o.bandoff, p.bandoff.data(), 4ull * (p.n + 2));
+        if (t.match_lo) {
+            int *a = (int *)(H + o.anc);
+            std::memcpy(a, t.match_lo, 4ull * (p.n + 1));
+            std::memcpy(a + (p.n + 1), t.match_hi, 4ull * (p.n + 1));
+            std::memcpy(a + 2 * (p.n + 1), t.del_lo, 4ull * (p.n + 1));
+            std::memcpy(a + 3 * (p.n + 1), t.del_hi, 4ull * (p.n + 1));
+            std::memcpy(a + 4 * (p.n + 1), t.ins_lo, 4ull * (p.m + 1));
+            std::memcpy(a + 4 * (p.n + 1) + (p.m + 1), t.ins_hi, 4ull * (p.m + 1));
+        }
+        std::memcpy(H + o.cre_start, p.cre_start.data(), 4ull * (p.bandcells + 1));
+        if (!p.cre.empty()) std::memcpy(H + o.cre, p.cre.data(), 4ull * p.cre.size());
+        if (!p.am_ends.empty()) std::memcpy(H + o.am_ends, p.am_ends.data(), 4ull * p.am_ends.size());
+        if (t.num_arcmatches) {
+            std::memcpy(H + o.am_score, t.am_score, 4ull * t.num_arcmatches);
+            std::memcpy(H + o.D, p.Dinit.data(), 4ull * t.num_arcmatches);
+        }
+        PairDev &d = hp[q];
+        std::memset(&d, 0, sizeof d);
+        d.n = p.n;
+        d.m = p.m;
+        d.go = t.indel_opening;
+        d.excl = t.exclusion;
+        d.flags = p.flags;
+        d.free_endgaps = p.fe;
+        d.la = t.match_lo ? t.left_anchor_a : p.n + 1;
+        d.lb = t.match_lo ? t.left_anchor_b : p.m + 1;
+        d.ra = t.match_lo ? t.right_anchor_a : 0;
+        d.rb = t.match_lo ? t.right_anchor_b : 0;
+        d.num_am = t.num_arcmatches;
+        d.bandcells = p.bandcells;
+        d.sigma = (const int *)(Dv + o.sigma);
+        d.gapA = (const int *)(Dv + o.gapA);
+        d.gapB = (const int *)(Dv + o.gapB);
+        d.min_col = (const int *)(Dv + o.minc);
+        d.max_col = (const int *)(Dv + o.maxc);
+        d.bandoff = (const int *)(Dv + o.bandoff);
+        if (t.match_lo) {
+            const int *a = (const int *)(Dv + o.anc);
+            d.match_lo = a;
+            d.match_hi = a + (p.n + 1);
+            d.del_lo = a + 2 * (p.n + 1);
+            d.del_hi = a + 3 * (p.n + 1);
+            d.ins_lo = a + 4 * (p.n + 1);
+            d.ins_hi = a + 4 * (p.n + 1) + (p.m + 1);
+        }
+        d.cre_start = (const int *)(Dv + o.cre_start);
+        d.cre = (const int2 *)(Dv + o.cre);
+        d.D = (int *)(Dv + o.D);
+        d.am_ends = (const int4 *)(Dv + o.am_ends);
+        d.am_score = (const int *)(Dv + o.am_score);
+        d.topM = (int *)(Dv + o.topM);
+        d.res = (int *)(Dv + o.res);
+        d.tokens = (int2 *)(Dv + o.tok);
+        d.token_cap = p.token_cap;
+        d.tq = (int *)(Dv + o.tq);
+        d.tq_cap = p.tq_cap;
+        d.segs = (int4 *)(Dv + o.segs);
+    }
+
+    // ---- scratch
+    int blocks_per_sm = 0;
+    CUDA_TRY(fill_occupancy(sw, &blocks_per_sm));
+    if (blocks_per_sm < 1) return fail(LCG_ERR_UNSUPPORTED, "fill kernel does not fit on an SM");
+    CUDA_TRY(trace_prepare(sw));
+    int blocks = e->sms * blocks_per_sm;
+    long long stride = (long long)rows_max * sw;
+    size_t slots = std::max<size_t>((size_t)blocks * fill_warps_per_block(), (size_t)npairs);
+    size_t need = slots * (size_t)stride;
+    if (need > e->scratch_cap) {
+        if (e->d_scratch) cudaFree(e->d_scratch);
+        e->d_scratch = nullptr;
+        e->scratch_cap = 0;
+        if (cudaMalloc(&e->d_scratch, need * sizeof(int)) != cudaSuccess)
+            return fail(LCG_ERR_NOMEM, "device scratch allocation failed");
+        e->scratch_cap = need;
+    }
+
+    // ---- transfer + launch + transfer
+    cudaStream_t st = e->stream;
+    CUDA_TRY(cudaMemcpyAsync(Dv, H, down_begin, cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemsetAsync(Dv + down_begin, 0, down_end - down_begin, st));
+    unsigned int *qhead = (unsigned int *)(Dv + off_ctrl);
+    int *status = (int *)(Dv + off_ctrl + 4);
+    int *abort_flag = (int *)(Dv + off_ctrl + 8);
+    CUDA_TRY(cudaEventRecord(e->ev0, st));
+    CUDA_TRY(launch_fill((const PairDev *)(Dv + off_pairs), (const GroupItem *)(Dv + off_items), (int)nitems,
+                         (const int4 *)(Dv + off_dw), e->d_scratch, stride, sw, qhead, status, abort_flag,
+                         blocks, st));
+    CUDA_TRY(cudaEventRecord(e->ev1, st));
+    long long launches = 1;
+    if (opts->do_trace) {
+        CUDA_TRY(launch_trace((const PairDev *)(Dv + off_pairs), npairs, e->d_scratch, stride, sw, status, st));
+        ++launches;
+    }
+    CUDA_TRY(cudaEventRecord(e->ev2, st));
+    CUDA_TRY(cudaMemcpyAsync(H + off_ctrl, Dv + off_ctrl, 64, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaMemcpyAsync(H + down_begin, Dv + down_begin, down_end - down_begin, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e->ev0, e->ev2);
+    e->last_ms = ms;
+    e->last_launches = launches;
+    int hstatus = ((int *)(H + off_ctrl))[1];
+    if (hstatus & ST_TIMEOUT) return fail(LCG_ERR_TIMEOUT, "a device wait for an arc-match entry timed out");
+    if (hstatus & ST_OVERFLOW) return fail(LCG_ERR_DEVICE, "traceback buffer overflow");
+    if (hstatus & ST_INTERNAL) return fail(LCG_ERR_DEVICE, "traceback found no predecessor");
+
+    // ---- results
+    for (int q = 0; q < npairs; ++q) {
+        const auto &p = prep[q];
+        const Off &o = off[q];
+        const int *res = (const int *)(H + o.res);
+        lcg_align_result &r = results[q];
+        int sc = res[R_SCORE];
+        r.score = sc < MIN_FINITE ? LCG_NEG_INF : (int64_t)sc;
+        r.max_i = res[R_MAXI];
+        r.max_j = res[R_MAXJ];
+        r.min_i = opts->do_trace ? res[R_MINI] : 1;
+        r.min_j = opts->do_trace ? res[R_MINJ] : 1;
+        r.num_edges = 0;
+        r.num_traced_am = 0;
+        if (!opts->do_trace) continue;
+        Assembler as;
+        as.tok = (const int2 *)(H + o.tok);
+        int nseg = res[R_NSEG];
+        const int4 *segs = (const int4 *)(H + o.segs);
+        if (nseg < 1 || nseg > p.tq_cap + 1) return fail(LCG_ERR_DEVICE, "bad traceback segment count");
+        for (int s = 0; s < nseg; ++s) {
+            as.seg_am.push_back(segs[s].x);
+            as.seg_start.push_back(segs[s].y);
+            as.seg_end.push_back(segs[s].z);
+        }
+        as.edges = r.edges;
+        as.edge_cap = r.edges ? p.n + p.m : 0;
+        as.tam = r.traced_am;
+        as.tam_cap = r.traced_am ? std::min(p.n, p.m) : 0;
+        as.expand(0, 0);
+        if (!as.ok) return fail(LCG_ERR_DEVICE, "traceback assembly failed");
+        r.num_edges = as.nedges;
+        r.num_traced_am = as.ntam;
+    }
+    return LCG_OK;
+}
+
+}  // extern "C"

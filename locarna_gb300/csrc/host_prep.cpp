@@ -1,0 +1,655 @@
+// Host-side preparation of the tables the Sankoff engine consumes, restating
+// the reference's input and scoring objects for single-sequence PP inputs:
+//
+//   PP 2.0 reader ............ RnaData::read_pp / read_pp_arc_probabilities
+//                              (src/LocARNA/rna_data.cc:979-1104) and the
+//                              clustal-like sequence block of
+//                              MultipleAlignment::read_clustallike
+//                              (multiple_alignment.cc:279-420)
+//   arcs ..................... BasePairs::generateBPLists (basepairs.cc:155-205)
+//   sigma / gaps / weights ... Scoring (scoring.cc:28-311), arc-match scores
+//                              Scoring::arcmatch / riboX_arcmatch_score
+//                              (scoring.cc:368-554)
+//   band ..................... TraceController (trace_controller.cc:360-597)
+//   envelope ................. PFGotoh / PFTraceProbs (edge_probs.icc:7-268)
+//                              with StralScore (stral_score.cc:10-100)
+//   arc matches .............. ArcMatches ctor + is_valid_arcmatch
+//                              (arc_matches.cc:19-48, 130-188)
+//
+// Floating-point expressions are evaluated in the same order and precision as
+// in the reference, so that thresholds (p >= min_prob, envelope >= 1e-4) and
+// rounded integer scores come out identical on the same host.
+#include <algorithm>
+#include <cctype>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "../../include/locarna_gb300.h"
+
+namespace {
+
+#include "ribosum85_60.inc"
+
+struct PrepError {
+    lcg_status code;
+    std::string msg;
+};
+
+[[noreturn]] void perr(lcg_status c, const std::string &m) { throw PrepError{c, m}; }
+
+// ---------------------------------------------------------------- PP reader
+
+struct RnaInput {
+    std::string name;
+    std::string seq;                  // normalised (upper case, T -> U), 1-based via seq[i-1]
+    std::map<std::pair<int, int>, double> arc_probs;  // (i,j) -> p, i<j (sparse matrix)
+    std::string anchors;
+};
+
+// get_nonempty_line (aux.cc:122-145): skip empty lines and lines starting with
+// white space; join lines ending in a backslash
+bool next_line(std::istream &in, std::string &line) {
+    while (std::getline(in, line)) {
+        if (!line.empty() && line.back() == '\r') line.pop_back();
+        if (!line.empty() && !std::isspace((unsigned char)line[0])) {
+            while (!line.empty() && line.back() == '\\') {
+                line.pop_back();
+                std::string l1;
+                if (std::getline(in, l1)) {
+                    if (!l1.empty() && l1.back() == '\r') l1.pop_back();
+                    line += " " + l1;
+                } else {
+                    break;
+                }
+            }
+            return true;
+        }
+    }
+    return false;
+}
+
+bool has_prefix(const std::string &s, const std::string &p) { return s.compare(0, p.size(), p) == 0; }
+
+RnaInput read_pp(const std::string &text, double p_bpcut) {
+    std::istringstream in(text);
+    std::string line;
+    RnaInput r;
+    if (!std::getline(in, line) || !has_prefix(line, "#PP 2")) perr(LCG_ERR_PARSE, "not a PP 2.0 file (header #PP 2.0 missing)");
+    // sequence section
+    std::vector<std::string> names;
+    std::map<std::string, std::string> seqs;
+    std::vector<std::string> anchors;
+    if (!next_line(in, line)) perr(LCG_ERR_PARSE, "PP file ends before the sequence section");
+    do {
+        if (line[0] == '#') {
+            if (has_prefix(line, "#END")) break;
+            if (has_prefix(line, "#A")) {
+                std::istringstream a(line.substr(2));
+                int idx;
+                std::string s;
+                a >> idx >> s;
+                if (a.fail() || idx < 1) perr(LCG_ERR_PARSE, "invalid anchor line");
+                if ((size_t)idx > anchors.size() + 1) perr(LCG_ERR_PARSE, "non-contiguous anchor specification");
+                if ((size_t)idx > anchors.size()) anchors.resize(idx);
+                anchors[idx - 1] += s;
+            }
+            // #S / #FS structure annotations and unknown tags are ignored here
+        } else {
+            std::istringstream ls(line);
+            std::string name, s;
+            ls >> name;
+            if (ls.fail() || name.empty()) perr(LCG_ERR_PARSE, "unexpected line in sequence section");
+            ls >> s;
+            if (ls.fail()) s = "";
+            if (!seqs.count(name)) {
+                seqs[name] = "";
+                names.push_back(name);
+            }
+            seqs[name] += s;
+        }
+    } while (next_line(in, line));
+    if (names.empty()) perr(LCG_ERR_PARSE, "PP file without sequence");
+    if (names.size() > 1) perr(LCG_ERR_UNSUPPORTED, "multiple-sequence (alignment) PP input is not supported yet");
+    if (!anchors.empty()) perr(LCG_ERR_UNSUPPORTED, "anchor constraints (#A lines) are not supported yet");
+    r.name = names[0];
+    r.seq = seqs[names[0]];
+    if (r.seq.empty()) perr(LCG_ERR_PARSE, "empty sequence");
+    for (auto &c : r.seq) {
+        c = (char)std::toupper((unsigned char)c);
+        if (c == 'T') c = 'U';
+    }
+    // base pair section
+    if (!next_line(in, line) || line != "#SECTION BASEPAIRS") perr(LCG_ERR_PARSE, "Expected base pair section header.");
+    const size_t len = r.seq.size();
+    while (next_line(in, line)) {
+        if (line[0] == '#') {
+            if (has_prefix(line, "#END")) break;
+            if (has_prefix(line, "#BPCUT")) {
+                std::istringstream ls(line);
+                std::string dummy;
+                double p;
+                ls >> dummy >> p;
+                if (ls.fail()) perr(LCG_ERR_PARSE, "Cannot parse line \"" + line + "\" in base pairs section.");
+                p_bpcut = std::max(p, p_bpcut);
+            }
+            continue;
+        }
+        std::istringstream ls(line);
+        size_t i, j;
+        double p;
+        ls >> i >> j >> p;
+        if (ls.fail()) perr(LCG_ERR_PARSE, "Cannot parse line \"" + line + "\" in base pairs section.");
+        if (!(1 <= i && i < j && j <= len)) perr(LCG_ERR_PARSE, "Invalid indices in PP input line \"" + line + "\".");
+        if (p <= p_bpcut) continue;
+        r.arc_probs[{(int)i, (int)j}] = p;
+    }
+    return r;
+}
+
+// ---------------------------------------------------------------- scoring
+
+int idx_acgu(char c) {
+    switch (c) {
+    case 'A': return 0;
+    case 'C': return 1;
+    case 'G': return 2;
+    case 'U': return 3;
+    default: return -1;
+    }
+}
+
+long round2score(double d) { return (long)((d < 0) ? (d - 0.5) : (d + 0.5)); }
+
+struct Arc {
+    int l, r;
+    double p;
+};
+
+struct Side {
+    RnaInput in;
+    int len = 0;
+    std::vector<Arc> arcs;        // reference index order
+    std::vector<long> weights;    // probToWeight per arc
+    std::vector<double> p_up, p_down;  // prob_paired_upstream / downstream
+};
+
+// BasePairs::generateBPLists: i from len-3 down to 1, j ascending from i+3
+void make_arcs(Side &s, double min_prob) {
+    s.len = (int)s.in.seq.size();
+    for (int i = s.len - 3; i >= 1; --i) {
+        for (int j = i + 3; j <= s.len; ++j) {
+            auto it = s.in.arc_probs.find({i, j});
+            double p = it == s.in.arc_probs.end() ? 0.0 : it->second;
+            if (p >= min_prob) s.arcs.push_back({i, j, p});
+        }
+    }
+    // RnaData::prob_paired_upstream / downstream (rna_data.cc:713-732):
+    // ascending sums over the sparse probability matrix
+    s.p_up.assign(s.len + 1, 0.0);
+    s.p_down.assign(s.len + 1, 0.0);
+    std::vector<std::vector<std::pair<int, double>>> by_left(s.len + 1), by_right(s.len + 1);
+    for (auto &kv : s.in.arc_probs) {
+        by_left[kv.first.first].push_back({kv.first.second, kv.second});
+        by_right[kv.first.second].push_back({kv.first.first, kv.second});
+    }
+    for (int i = 1; i <= s.len; ++i) {
+        double up = 0.0, down = 0.0;
+        for (auto &x : by_left[i]) up += x.second;    // j ascending (map order)
+        for (auto &x : by_right[i]) down += x.second; // j ascending
+        s.p_up[i] = up;
+        s.p_down[i] = down;
+    }
+}
+
+double basematch_score_corrected(int a, int b) {
+    // RibosumFreq::basematch_score_corrected (ribosum.cc:324-331)
+    double bi = kBaseNonstructProbs[a], bj = kBaseNonstructProbs[b];
+    return log(kBasematchProbs[a * 4 + b] / (bi * bj)) / log(2);
+}
+
+long sigma_single(const lcg_prep_opts &o, char ca, char cb) {
+    // Scoring::sigma_ for one row in each input (scoring.cc:140-198)
+    long score = 0;
+    int a = idx_acgu(ca), b = idx_acgu(cb);
+    if (o.use_ribosum && a >= 0 && b >= 0) {
+        score += round2score(100.0 * basematch_score_corrected(a, b));
+    } else if (ca != 'N' && cb != 'N') {
+        score += (ca == cb) ? o.match : o.mismatch;
+    }
+    return round2score((double)(score / (int)(1 * 1)));
+}
+
+long riboX_single(char al, char ar, char bl, char br) {
+    // Scoring::riboX_arcmatch_score for one row each (scoring.cc:368-438)
+    int a1 = idx_acgu(al), a2 = idx_acgu(ar), b1 = idx_acgu(bl), b2 = idx_acgu(br);
+    if (al == '-' || ar == '-' || bl == '-' || br == '-') return 0;
+    if (a1 < 0 || a2 < 0 || b1 < 0 || b2 < 0) return 0;
+    double score = 0;
+    score += log(kArcmatchProbs[(a1 * 4 + a2) * 16 + (b1 * 4 + b2)] /
+                 (kBasepairProbs[a1 * 4 + a2] * kBasepairProbs[b1 * 4 + b2])) /
+             log(2);
+    return round2score(100.0 * score / 1);
+}
+
+long prob_to_weight(double p, double pe, int struct_weight) {
+    // Scoring::probToWeight (scoring.cc:250-265)
+    return round2score(round(struct_weight * (1 - log(p) / log(pe))));
+}
+
+// ---------------------------------------------------------------- envelope
+
+struct Band {
+    std::vector<long> minc, maxc;  // size_t in the reference; all values >= 0
+};
+
+// StralScore::sigma (stral_score.cc:29-60) for single sequences; `rev`
+// evaluates the reversed object (StralScore::reverse, :78-100), whose
+// up/down vectors are swapped and reversed.
+struct Stral {
+    const Side *A, *B;
+    double sw;
+    bool rev;
+    bool ribosum;
+    double match, mismatch;
+    double sigma(int i, int j) const {
+        int n = A->len, m = B->len;
+        int ia = rev ? n + 1 - i : i, jb = rev ? m + 1 - j : j;
+        double seq_score = 0;
+        int pairs = 0;
+        int a = idx_acgu(A->in.seq[ia - 1]), b = idx_acgu(B->in.seq[jb - 1]);
+        if (a >= 0 && b >= 0) {
+            // sim_mat: ribosum base-match scores, or match/mismatch
+            // (MainHelper::select_basematch_scores, main_helper.icc:281-306)
+            seq_score += ribosum ? kBmScore[a * 4 + b] : (a == b ? match : mismatch);
+            pairs++;
+        }
+        if (pairs != 0) seq_score /= pairs;
+        double dA = rev ? A->p_up[ia] : A->p_down[ia];
+        double dB = rev ? B->p_up[jb] : B->p_down[jb];
+        double uA = rev ? A->p_down[ia] : A->p_up[ia];
+        double uB = rev ? B->p_down[jb] : B->p_up[jb];
+        return sw * (sqrt(dA * dB) + sqrt(uA * uB)) + seq_score;
+    }
+};
+
+template <class T>
+struct Mat {
+    int rows, cols;
+    std::vector<T> v;
+    Mat(int r, int c) : rows(r), cols(c), v((size_t)r * c, T(0)) {}
+    T &operator()(int i, int j) { return v[(size_t)i * cols + j]; }
+    const T &operator()(int i, int j) const { return v[(size_t)i * cols + j]; }
+};
+
+// PFGotoh::pf_gotoh (edge_probs.icc:76-162)
+template <class T>
+void pf_gotoh(Mat<T> &zM, Mat<T> &zA, Mat<T> &zB, const Band &tc, const Stral &score, int fe,
+              bool local, double gap_opening, double gap_extension, double temp) {
+    const int lenA = zM.rows - 1, lenB = zM.cols - 1;
+    double g_open = exp(gap_opening / temp);
+    double g_ext = exp(gap_extension / temp);
+    auto valid = [&](int i, int j) { return tc.minc[i] <= j && j <= tc.maxc[i]; };
+    if (valid(0, 0)) zM(0, 0) = local ? 0 : 1;
+    if (lenA > 0 && valid(1, 0)) zA(1, 0) = g_open * g_ext;
+    if (lenB > 0 && valid(0, 1)) zB(0, 1) = g_open * g_ext;
+    for (int i = 2; i <= lenA; i++) {
+        if (tc.minc[i] > 0) break;
+        zA(i, 0) = zA(i - 1, 0) * g_ext;
+    }
+    for (long j = std::max(tc.minc[0], 2L); j <= std::min(tc.maxc[0], (long)lenB); j++) zB(0, j) = zB(0, j - 1) * g_ext;
+    if (fe & LCG_FREE_LEFT_2)
+        for (int i = 1; i <= lenA; i++) zA(i, 0) += 1;
+    if (fe & LCG_FREE_LEFT_1)
+        for (int j = 1; j <= lenB; j++) zB(0, j) += 1;
+    for (int i = 1; i <= lenA; i++) {
+        for (long j = std::max(tc.minc[i], 1L); j <= std::min(tc.maxc[i], (long)lenB); j++) {
+            double match_score_ij = score.sigma(i, (int)j);
+            double match_ij = exp(match_score_ij / temp);
+            zM(i, j) = zM(i - 1, j - 1) * match_ij + zA(i - 1, j - 1) * match_ij + zB(i - 1, j - 1) * match_ij +
+                       (local ? match_ij : 0);
+            zA(i, j) = zA(i - 1, j) * g_ext + zM(i - 1, j) * g_open * g_ext + zB(i - 1, j) * g_open * g_ext;
+            zB(i, j) = zB(i, j - 1) * g_ext + zM(i, j - 1) * g_open * g_ext + zA(i, j - 1) * g_open * g_ext;
+        }
+    }
+}
+
+int reverse_fe(int fe) {
+    // FreeEndgaps::reverse (free_endgaps.hh:74-79): swap left/right per sequence
+    int r = 0;
+    if (fe & LCG_FREE_LEFT_1) r |= LCG_FREE_RIGHT_1;
+    if (fe & LCG_FREE_RIGHT_1) r |= LCG_FREE_LEFT_1;
+    if (fe & LCG_FREE_LEFT_2) r |= LCG_FREE_RIGHT_2;
+    if (fe & LCG_FREE_RIGHT_2) r |= LCG_FREE_LEFT_2;
+    return r;
+}
+
+// PFTraceProbs (edge_probs.icc:212-268) followed by
+// TraceController::restrict_by_trace_probabilities (trace_controller.cc:565-597)
+template <class T>
+bool restrict_by_envelope(Band &tc, const Side &A, const Side &B, const lcg_prep_opts &o) {
+    const int n = A.len, m = B.len;
+    const double gap_opening = o.indel_opening / 100.0, gap_ext = o.indel / 100.0;
+    const double sw = o.struct_weight / 100.0, temp = o.temperature_alipf / 100.0;
+    const bool local = o.sequ_local != 0;
+    const int fe = o.free_endgaps & 15;
+    Mat<T> zM(n + 1, m + 1), zA(n + 1, m + 1), zB(n + 1, m + 1);
+    Mat<T> zMr(n + 1, m + 1), zAr(n + 1, m + 1), zBr(n + 1, m + 1);
+    Stral fwd{&A, &B, sw, false, o.use_ribosum != 0, (double)o.match, (double)o.mismatch};
+    Stral rev{&A, &B, sw, true, o.use_ribosum != 0, (double)o.match, (double)o.mismatch};
+    pf_gotoh(zM, zA, zB, tc, fwd, fe, local, gap_opening, gap_ext, temp);
+    // TraceRange::reverse (trace_controller.cc:319-338)
+    Band rtc;
+    rtc.minc.resize(n + 1);
+    rtc.maxc.resize(n + 1);
+    for (int i = 0; i <= n; ++i) {
+        rtc.maxc[n - i] = m - tc.minc[i];
+        rtc.minc[n - i] = m - tc.maxc[i];
+    }
+    pf_gotoh(zMr, zAr, zBr, rtc, rev, reverse_fe(fe), local, gap_opening, gap_ext, temp);
+    T z;
+    if (local) {
+        z = 1;
+        for (int i = 0; i <= n; i++)
+            for (int j = 0; j <= m; j++) z += zM(i, j);
+    } else {
+        z = zM(n, m) + zA(n, m) + zB(n, m);
+        if (fe & LCG_FREE_LEFT_2)
+            for (int i = 0; i <= n; i++) z += zA(i, m);
+        if (fe & LCG_FREE_LEFT_1)
+            for (int j = 0; j <= m; j++) z += zB(n, j);
+    }
+    bool failed = z == (T)0 || std::isnan((long double)z) || std::isinf((long double)z);
+    double locality_add = local ? 1 : 0;
+    double g_open = exp(gap_opening / temp);
+    Mat<double> probs(n + 1, m + 1);
+    for (int i = 0; i <= n; i++) {
+        for (long j = std::max(tc.minc[i], 0L); j <= std::min(tc.maxc[i], (long)m); j++) {
+            T z_ij = zM(i, j) * (zMr(n - i, m - j) + zAr(n - i, m - j) + zBr(n - i, m - j) + locality_add) +
+                     zA(i, j) * (zMr(n - i, m - j) + zAr(n - i, m - j) / g_open + zBr(n - i, m - j)) +
+                     zB(i, j) * (zMr(n - i, m - j) + zAr(n - i, m - j) + zBr(n - i, m - j) / g_open);
+            probs(i, j) = z_ij / z;
+        }
+    }
+    const double min_prob = o.min_trace_probability;
+    for (int i = 0; i <= n; ++i) {
+        long new_min = tc.maxc[i], new_max = tc.minc[i];
+        for (long j = tc.minc[i]; j <= tc.maxc[i]; ++j) {
+            if (probs(i, j) >= min_prob) {
+                new_min = std::min(new_min, j);
+                new_max = std::max(new_max, j);
+            }
+        }
+        tc.minc[i] = std::max(tc.minc[i], new_min);
+        tc.maxc[i] = std::min(tc.maxc[i], new_max);
+    }
+    long mx = 0;
+    for (int i = 0; i <= n; ++i) {
+        tc.maxc[i] = std::max(tc.maxc[i], mx);
+        mx = tc.maxc[i];
+    }
+    long mn = tc.maxc[n];
+    for (int i = n + 1; i > 0;) {
+        --i;
+        tc.minc[i] = std::min(tc.minc[i], mn);
+        mn = tc.minc[i];
+    }
+    return !failed;
+}
+
+// TraceController::constrain_wo_ref (trace_controller.cc:360-390)
+void constrain_wo_ref(Band &tc, size_t lenA, size_t lenB, size_t delta) {
+    if (lenA == 0 || lenB == 0) return;
+    for (size_t i = 0; i <= lenA; i++) {
+        size_t x = i * lenB * (lenA + lenB);
+        size_t y = 2 * delta * lenA * lenB;
+        size_t z = lenA * (lenA + lenB);
+        if (lenA > lenB) y = std::max(y, (lenA + lenB) * lenA / 2);
+        else if (lenB > lenA) y = std::max(y, (lenA + lenB) * lenB / 2);
+        tc.minc[i] = x > y ? (long)((x - y + z - 1) / z) : 0;
+        tc.maxc[i] = (long)std::min((x + y) / z, lenB);
+    }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- prepared pair
+
+struct lcg_prepared_s {
+    int n = 0, m = 0;
+    std::string seq_a, seq_b, name_a, name_b;
+    std::vector<int32_t> sigma, gap_a, gap_b, arcs_a, arcs_b, am_arcs, am_score, min_col, max_col;
+    std::vector<double> arc_p_a, arc_p_b;
+    int32_t indel_opening = 0, exclusion = 0;
+    int envelope_ok = 1;
+};
+
+extern "C" {
+
+void lcg_prep_opts_default(lcg_prep_opts *o) {
+    std::memset(o, 0, sizeof *o);
+    o->min_prob = 0.001;
+    o->indel = -150;
+    o->indel_opening = -750;
+    o->struct_weight = 200;
+    o->tau = 50;
+    o->exclusion = 0;
+    o->match = 50;
+    o->mismatch = 0;
+    o->use_ribosum = 1;
+    o->min_trace_probability = 1e-4;
+    o->max_diff = -1;
+    o->max_diff_am = -1;
+    o->max_diff_at_am = -1;
+    o->temperature_alipf = 300;
+    o->sequ_local = 0;
+    o->free_endgaps = 0;
+    o->pf_precision = 1;
+    o->exp_prob = -1.0;
+}
+
+lcg_status lcg_prepare_pair(const char *pp_a, const char *pp_b, const lcg_prep_opts *opts,
+                            lcg_prepared *out);
+lcg_status lcg_prepared_tables(lcg_prepared p, lcg_pair_tables *t);
+const char *lcg_prepared_sequence(lcg_prepared p, int32_t which);
+lcg_status lcg_prepared_free(lcg_prepared p);
+int32_t lcg_prepared_envelope_ok(lcg_prepared p);
+
+}  // extern "C"
+
+namespace lcg_host {
+void set_error(const std::string &msg);
+}
+
+lcg_status lcg_prepare_pair(const char *pp_a, const char *pp_b, const lcg_prep_opts *opts,
+                            lcg_prepared *out) {
+    if (!pp_a || !pp_b || !out) {
+        lcg_host::set_error("NULL argument");
+        return LCG_ERR_ARG;
+    }
+    *out = nullptr;
+    lcg_prep_opts o;
+    if (opts) o = *opts;
+    else lcg_prep_opts_default(&o);
+    try {
+        auto P = std::make_unique<lcg_prepared_s>();
+        Side A, B;
+        A.in = read_pp(pp_a, o.min_prob);
+        B.in = read_pp(pp_b, o.min_prob);
+        make_arcs(A, o.min_prob);
+        make_arcs(B, o.min_prob);
+        const int n = A.len, m = B.len;
+        P->n = n;
+        P->m = m;
+        P->seq_a = A.in.seq;
+        P->seq_b = B.in.seq;
+        P->name_a = A.in.name;
+        P->name_b = B.in.name;
+
+        // trace controller (no reference alignment, no anchors)
+        Band tc;
+        tc.minc.assign(n + 1, 0);
+        tc.maxc.assign(n + 1, m);
+        if (o.max_diff >= 0) constrain_wo_ref(tc, n, m, (size_t)o.max_diff);
+        if (o.min_trace_probability > 0.0) {
+            bool ok;
+            if (o.pf_precision == 0) ok = restrict_by_envelope<double>(tc, A, B, o);
+            else ok = restrict_by_envelope<long double>(tc, A, B, o);
+            P->envelope_ok = ok ? 1 : 0;
+        }
+
+        // scoring tables
+        P->sigma.assign((size_t)(n + 1) * (m + 1), 0);
+        long tab[256][256];
+        bool have[256][256];
+        std::memset(have, 0, sizeof have);
+        for (int i = 1; i <= n; ++i) {
+            unsigned char ca = (unsigned char)A.in.seq[i - 1];
+            for (int j = 1; j <= m; ++j) {
+                unsigned char cb = (unsigned char)B.in.seq[j - 1];
+                if (!have[ca][cb]) {
+                    tab[ca][cb] = sigma_single(o, (char)ca, (char)cb);
+                    have[ca][cb] = true;
+                }
+                P->sigma[(size_t)i * (m + 1) + j] = (int32_t)tab[ca][cb];
+            }
+        }
+        // Scoring::precompute_gapcost (scoring.cc:271-311) for gap-free rows
+        P->gap_a.assign(n + 1, 0);
+        P->gap_b.assign(m + 1, 0);
+        for (int i = 1; i <= n; ++i) {
+            float gf = A.in.seq[i - 1] == '-' ? 1.0f : 0.0f;
+            P->gap_a[i] = (int32_t)round2score((1 - gf) * o.indel);
+        }
+        for (int j = 1; j <= m; ++j) {
+            float gf = B.in.seq[j - 1] == '-' ? 1.0f : 0.0f;
+            P->gap_b[j] = (int32_t)round2score((1 - gf) * o.indel);
+        }
+        P->indel_opening = o.indel_opening;
+        P->exclusion = o.exclusion;
+        double peA = o.exp_prob > 0 ? o.exp_prob : 1.0 / (2.0 * n);
+        double peB = o.exp_prob > 0 ? o.exp_prob : 1.0 / (2.0 * m);
+        for (auto &a : A.arcs) A.weights.push_back(prob_to_weight(a.p, peA, o.struct_weight));
+        for (auto &b : B.arcs) B.weights.push_back(prob_to_weight(b.p, peB, o.struct_weight));
+
+        // arc matches (arc_matches.cc:130-188), A index outer, B index inner
+        const size_t mdam = o.max_diff_am != -1 ? (size_t)o.max_diff_am : (size_t)std::max(n, m);
+        const size_t mdaam = o.max_diff_at_am != -1 ? (size_t)o.max_diff_at_am : (size_t)std::max(n, m);
+        auto valid = [&](long i, long j) { return i >= 0 && i <= n && tc.minc[i] <= j && j <= tc.maxc[i]; };
+        auto valid_match = [&](long i, long j) { return valid(i, j) && valid(i - 1, j - 1); };
+        long ribo_cache[4][4][4][4];
+        bool ribo_have[4][4][4][4];
+        std::memset(ribo_have, 0, sizeof ribo_have);
+        for (size_t ia = 0; ia < A.arcs.size(); ++ia) {
+            const Arc &a = A.arcs[ia];
+            for (size_t ib = 0; ib < B.arcs.size(); ++ib) {
+                const Arc &b = B.arcs[ib];
+                bool ok = valid_match(a.l, b.l) && valid_match(a.r, b.r) &&
+                          (size_t)std::abs((a.r - a.l) - (b.r - b.l)) <= mdam &&
+                          (size_t)a.l <= b.l + mdaam && (size_t)b.l <= a.l + mdaam &&
+                          (size_t)a.r <= b.r + mdaam && (size_t)b.r <= a.r + mdaam;
+                if (!ok) continue;
+                long seqc = 0;
+                if (o.tau != 0) {
+                    if (o.use_ribosum) {
+                        char c1 = A.in.seq[a.l - 1], c2 = A.in.seq[a.r - 1];
+                        char c3 = B.in.seq[b.l - 1], c4 = B.in.seq[b.r - 1];
+                        int x1 = idx_acgu(c1), x2 = idx_acgu(c2), x3 = idx_acgu(c3), x4 = idx_acgu(c4);
+                        if (x1 >= 0 && x2 >= 0 && x3 >= 0 && x4 >= 0) {
+                            if (!ribo_have[x1][x2][x3][x4]) {
+                                ribo_cache[x1][x2][x3][x4] = riboX_single(c1, c2, c3, c4);
+                                ribo_have[x1][x2][x3][x4] = true;
+                            }
+                            seqc = ribo_cache[x1][x2][x3][x4];
+                        } else {
+                            seqc = riboX_single(c1, c2, c3, c4);
+                        }
+                    } else {
+                        seqc = P->sigma[(size_t)a.l * (m + 1) + b.l] + P->sigma[(size_t)a.r * (m + 1) + b.r];
+                    }
+                }
+                long s = ((long)o.tau * seqc) / 100 + (A.weights[ia] + B.weights[ib]);
+                P->am_arcs.push_back((int32_t)ia);
+                P->am_arcs.push_back((int32_t)ib);
+                P->am_score.push_back((int32_t)s);
+            }
+        }
+        for (auto &a : A.arcs) {
+            P->arcs_a.push_back(a.l);
+            P->arcs_a.push_back(a.r);
+            P->arc_p_a.push_back(a.p);
+        }
+        for (auto &b : B.arcs) {
+            P->arcs_b.push_back(b.l);
+            P->arcs_b.push_back(b.r);
+            P->arc_p_b.push_back(b.p);
+        }
+        P->min_col.resize(n + 1);
+        P->max_col.resize(n + 1);
+        for (int i = 0; i <= n; ++i) {
+            P->min_col[i] = (int32_t)tc.minc[i];
+            P->max_col[i] = (int32_t)tc.maxc[i];
+        }
+        *out = P.release();
+        return LCG_OK;
+    } catch (const PrepError &e) {
+        lcg_host::set_error(e.msg);
+        return e.code;
+    } catch (const std::exception &e) {
+        lcg_host::set_error(e.what());
+        return LCG_ERR_NOMEM;
+    }
+}
+
+lcg_status lcg_prepared_tables(lcg_prepared p, lcg_pair_tables *t) {
+    if (!p || !t) {
+        lcg_host::set_error("NULL argument");
+        return LCG_ERR_ARG;
+    }
+    std::memset(t, 0, sizeof *t);
+    t->len_a = p->n;
+    t->len_b = p->m;
+    t->sigma = p->sigma.data();
+    t->gap_a = p->gap_a.data();
+    t->gap_b = p->gap_b.data();
+    t->indel_opening = p->indel_opening;
+    t->exclusion = p->exclusion;
+    t->num_arcs_a = (int32_t)(p->arcs_a.size() / 2);
+    t->num_arcs_b = (int32_t)(p->arcs_b.size() / 2);
+    t->arcs_a = p->arcs_a.data();
+    t->arcs_b = p->arcs_b.data();
+    t->num_arcmatches = (int32_t)p->am_score.size();
+    t->am_arcs = p->am_arcs.data();
+    t->am_score = p->am_score.data();
+    t->min_col = p->min_col.data();
+    t->max_col = p->max_col.data();
+    t->right_anchor_a = 0;
+    t->right_anchor_b = 0;
+    t->left_anchor_a = p->n + 1;
+    t->left_anchor_b = p->m + 1;
+    return LCG_OK;
+}
+
+const char *lcg_prepared_sequence(lcg_prepared p, int32_t which) {
+    if (!p) return "";
+    switch (which) {
+    case 0: return p->seq_a.c_str();
+    case 1: return p->seq_b.c_str();
+    case 2: return p->name_a.c_str();
+    case 3: return p->name_b.c_str();
+    default: return "";
+    }
+}
+
+int32_t lcg_prepared_envelope_ok(lcg_prepared p) { return p ? p->envelope_ok : 0; }
+
+lcg_status lcg_prepared_free(lcg_prepared p) {
+    delete p;
+    return LCG_OK;
+}

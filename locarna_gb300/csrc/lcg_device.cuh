@@ -1,0 +1,93 @@
+// Device-side data layout of the GB300 Sankoff engine.
+//
+// One batch = many independent sequence pairs. Every per-pair table lives in
+// one device arena; PairDev holds device pointers into it. The work list is a
+// flat array of GroupItem, one per left-end group (al,bl) of the reference's
+// align_D (src/LocARNA/aligner.cc:660-732) plus one top-level item per pair
+// (aligner.cc:736-880), in an order where every group comes after all groups
+// whose D entries it reads (per pair: al descending, then bl descending, as
+// the reference iterates).
+#pragma once
+#include <stdint.h>
+
+namespace lcg {
+
+// Scores are int32 with the reference's InftyInt semantics
+// (src/LocARNA/infty_int.hh:56-480) scaled down: finite values satisfy
+// |v| < 2^27 (checked on the host), every value below MIN_FINITE is negative
+// infinity, and stored values are normalised to NEG. Sums of up to four
+// stored values never overflow int32.
+constexpr int NEG = -(1 << 29);
+constexpr int MIN_FINITE = -(1 << 28);
+// D entries not yet written by their producer group (a D wait spins on this)
+constexpr int NOT_READY = INT32_MIN;
+
+__host__ __device__ __forceinline__ int norm(int v) { return v < MIN_FINITE ? NEG : v; }
+
+enum PairFlags : int {
+    PF_STRUCT_LOCAL = 1,
+    PF_SEQU_LOCAL = 2,
+    PF_ANCHORS = 4,
+    PF_TRACE = 8,
+};
+
+// status word bits (device -> host)
+enum StatusBits : int {
+    ST_TIMEOUT = 1,     // a bounded D wait gave up
+    ST_OVERFLOW = 2,    // a token / queue buffer would overflow
+    ST_INTERNAL = 4,    // traceback found no predecessor
+};
+
+struct PairDev {
+    int n, m;
+    int go, excl;
+    int flags;       // PairFlags
+    int free_endgaps;
+    int la, lb, ra, rb;  // leftmost / rightmost anchor
+    int num_am;
+    int bandcells;
+    const int *sigma;     // (n+1)*(m+1)
+    const int *gapA;      // n+1
+    const int *gapB;      // m+1
+    const int *min_col;   // n+2 (entry n+1 = m+1 sentinel)
+    const int *max_col;   // n+2
+    const int *bandoff;   // n+2: band cell offset of row i
+    const int *match_lo, *match_hi, *del_lo, *del_hi, *ins_lo, *ins_hi;
+    const int *cre_start; // bandcells+1: arc matches with right ends at a band cell
+    const int2 *cre;      // (am index, (a.l<<16)|b.l), lex-greater-left-ends order
+    int *D;               // num_am
+    const int4 *am_ends;  // per am: a.l, a.r, b.l, b.r
+    const int *am_score;  // per am
+    int *topM;            // (n+1)*(m+1), top-level M
+    int *res;             // result words, see Res
+    int2 *tokens;         // traceback tokens
+    int token_cap;
+    int *tq;              // traceback queue of arc matches (capacity tq_cap)
+    int tq_cap;
+    int4 *segs;           // traceback segments: (am or -1, token start, token end, 0)
+};
+
+enum Res : int {
+    R_SCORE = 0, R_MAXI, R_MAXJ, R_MINI, R_MINJ, R_NTOK, R_NSEG, R_NWORDS
+};
+
+struct GroupItem {
+    int pair;
+    int al, ar, bl, br;
+    int dw_start, dw_count;  // D writes: int4 (am, ar-1, br-1, score), ar ascending
+    int top;                 // 1 for the top-level item
+};
+
+// anchor helpers: reference AnchorConstraints::allowed_match/del/ins
+// (anchor_constraints.hh:157-253)
+__device__ __forceinline__ bool a_match(const PairDev &P, int i, int j) {
+    return !(P.flags & PF_ANCHORS) || (P.match_lo[i] <= j && j <= P.match_hi[i]);
+}
+__device__ __forceinline__ bool a_del(const PairDev &P, int i, int j) {
+    return !(P.flags & PF_ANCHORS) || (P.del_lo[i] <= j && j <= P.del_hi[i]);
+}
+__device__ __forceinline__ bool a_ins(const PairDev &P, int i, int j) {
+    return !(P.flags & PF_ANCHORS) || (P.ins_lo[j] <= i && i <= P.ins_hi[j]);
+}
+
+}  // namespace lcg

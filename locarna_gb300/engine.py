@@ -1,0 +1,95 @@
+"""Python binding of the C ABI (include/locarna_gb300.h) through ctypes.
+
+This is a thin mirror of the C entry points: ``Engine.align_pairs`` is
+``lcg_align_pairs``. The CUDA library must have been built
+(``locarna_gb300.build.build_engine``); there is no fallback path.
+"""
+import ctypes as C
+import os
+
+from .abi import (PairTables, ResultBuffers, lcg_align_opts, lcg_align_result,
+                  lcg_pair_tables, make_opts)
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "liblocarna_gb300.so")
+
+EXPORTS = ("lcg_last_error", "lcg_abi_version", "lcg_engine_create", "lcg_engine_destroy",
+           "lcg_align_pairs", "lcg_engine_last_stats")
+
+_lib = None
+
+
+class LcgError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"lcg error {code}: {msg}")
+        self.code = code
+
+
+def load_library(path=LIB_PATH):
+    """Load the engine library; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"locarna_gb300 CUDA library missing ({path}); run __graft_entry__.build()")
+    lib = C.CDLL(path)
+    lib.lcg_last_error.restype = C.c_char_p
+    lib.lcg_abi_version.restype = C.c_int32
+    lib.lcg_engine_create.argtypes = [C.c_int32, C.c_void_p, C.POINTER(C.c_void_p)]
+    lib.lcg_engine_create.restype = C.c_int32
+    lib.lcg_engine_destroy.argtypes = [C.c_void_p]
+    lib.lcg_engine_destroy.restype = C.c_int32
+    lib.lcg_align_pairs.argtypes = [C.c_void_p, C.POINTER(lcg_pair_tables), C.c_int32,
+                                    C.POINTER(lcg_align_opts), C.POINTER(lcg_align_result)]
+    lib.lcg_align_pairs.restype = C.c_int32
+    lib.lcg_engine_last_stats.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int64)]
+    lib.lcg_engine_last_stats.restype = C.c_int32
+    _lib = lib
+    return lib
+
+
+def _check(lib, rc):
+    if rc != 0:
+        raise LcgError(rc, lib.lcg_last_error().decode())
+
+
+class Engine:
+    """One GPU engine (lcg_engine): owns device buffers, launches on a stream."""
+
+    def __init__(self, device=0, stream=None):
+        self.lib = load_library()
+        h = C.c_void_p()
+        _check(self.lib, self.lib.lcg_engine_create(int(device), stream, C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.lib.lcg_engine_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def align_pairs(self, tables, opts=None, **kw):
+        """Align a list of PairTables; returns a list of AlignResult."""
+        if opts is None:
+            opts = make_opts(**kw)
+        n = len(tables)
+        arr = (lcg_pair_tables * n)(*[t.to_c() for t in tables])
+        bufs = [ResultBuffers(t.len_a, t.len_b) for t in tables]
+        res = (lcg_align_result * n)(*[b.c for b in bufs])
+        _check(self.lib, self.lib.lcg_align_pairs(self.h, arr, n, C.byref(opts), res))
+        out = []
+        for k, b in enumerate(bufs):
+            b.c = res[k]
+            out.append(b.decode())
+        return out
+
+    def last_stats(self):
+        ms = C.c_double()
+        nl = C.c_int64()
+        _check(self.lib, self.lib.lcg_engine_last_stats(self.h, C.byref(ms), C.byref(nl)))
+        return ms.value, nl.value

@@ -1,0 +1,99 @@
+"""Host preparation (lcg_prepare_pair): PP 2.0 texts -> PairTables.
+
+Mirror of the reference locarna driver's input side (src/locarna.cc:398-703):
+the options have the command line's names and defaults.
+"""
+import ctypes as C
+
+import numpy as np
+
+from .abi import LCG_FREE_LEFT_1, PairTables, lcg_pair_tables
+from .engine import LcgError, load_library
+
+
+class lcg_prep_opts(C.Structure):
+    _fields_ = [
+        ("min_prob", C.c_double), ("indel", C.c_int32), ("indel_opening", C.c_int32),
+        ("struct_weight", C.c_int32), ("tau", C.c_int32), ("exclusion", C.c_int32),
+        ("match", C.c_int32), ("mismatch", C.c_int32), ("use_ribosum", C.c_int32),
+        ("min_trace_probability", C.c_double), ("max_diff", C.c_int32),
+        ("max_diff_am", C.c_int32), ("max_diff_at_am", C.c_int32),
+        ("temperature_alipf", C.c_int32), ("sequ_local", C.c_int32),
+        ("free_endgaps", C.c_int32), ("pf_precision", C.c_int32), ("exp_prob", C.c_double),
+    ]
+
+
+_ready = False
+
+
+def _lib():
+    global _ready
+    lib = load_library()
+    if not _ready:
+        lib.lcg_prep_opts_default.argtypes = [C.POINTER(lcg_prep_opts)]
+        lib.lcg_prep_opts_default.restype = None
+        lib.lcg_prepare_pair.argtypes = [C.c_char_p, C.c_char_p, C.POINTER(lcg_prep_opts), C.POINTER(C.c_void_p)]
+        lib.lcg_prepare_pair.restype = C.c_int32
+        lib.lcg_prepared_tables.argtypes = [C.c_void_p, C.POINTER(lcg_pair_tables)]
+        lib.lcg_prepared_tables.restype = C.c_int32
+        lib.lcg_prepared_sequence.argtypes = [C.c_void_p, C.c_int32]
+        lib.lcg_prepared_sequence.restype = C.c_char_p
+        lib.lcg_prepared_envelope_ok.argtypes = [C.c_void_p]
+        lib.lcg_prepared_envelope_ok.restype = C.c_int32
+        lib.lcg_prepared_free.argtypes = [C.c_void_p]
+        lib.lcg_prepared_free.restype = C.c_int32
+        _ready = True
+    return lib
+
+
+def _fe_bits(spec):
+    bits = 0
+    for k, ch in enumerate(spec[:4]):
+        if ch == "+":
+            bits |= LCG_FREE_LEFT_1 << k
+    return bits
+
+
+def prep_options(**kw):
+    lib = _lib()
+    o = lcg_prep_opts()
+    lib.lcg_prep_opts_default(C.byref(o))
+    for k, v in kw.items():
+        if k == "free_endgaps" and isinstance(v, str):
+            v = _fe_bits(v)
+        if not hasattr(o, k):
+            raise KeyError(f"unknown preparation option {k}")
+        setattr(o, k, v)
+    return o
+
+
+def _arr(ptr, n):
+    if n == 0:
+        return np.zeros(0, dtype=np.int32)
+    return np.ctypeslib.as_array(ptr, shape=(n,)).copy()
+
+
+def prepare_pair(pp_a, pp_b, **kw):
+    """Build the tables of one pair from two PP 2.0 texts."""
+    lib = _lib()
+    o = prep_options(**kw)
+    h = C.c_void_p()
+    rc = lib.lcg_prepare_pair(pp_a.encode(), pp_b.encode(), C.byref(o), C.byref(h))
+    if rc != 0:
+        raise LcgError(rc, lib.lcg_last_error().decode())
+    try:
+        t = lcg_pair_tables()
+        lib.lcg_prepared_tables(h, C.byref(t))
+        n, m = t.len_a, t.len_b
+        na, nb, nam = t.num_arcs_a, t.num_arcs_b, t.num_arcmatches
+        pt = PairTables(
+            n, m, _arr(t.sigma, (n + 1) * (m + 1)), _arr(t.gap_a, n + 1), _arr(t.gap_b, m + 1),
+            t.indel_opening, t.exclusion, _arr(t.arcs_a, 2 * na), _arr(t.arcs_b, 2 * nb),
+            _arr(t.am_arcs, 2 * nam), _arr(t.am_score, nam), _arr(t.min_col, n + 1), _arr(t.max_col, n + 1),
+            seq_a=lib.lcg_prepared_sequence(h, 0).decode(), seq_b=lib.lcg_prepared_sequence(h, 1).decode())
+        pt.name_a = lib.lcg_prepared_sequence(h, 2).decode()
+        pt.name_b = lib.lcg_prepared_sequence(h, 3).decode()
+        pt.envelope_ok = bool(lib.lcg_prepared_envelope_ok(h))
+        return pt
+    finally:
+        lib.lcg_prepared_free(h)

@@ -1,0 +1,89 @@
+"""Generate the golden fixtures of tests/golden/ from the REFERENCE itself.
+
+Test infrastructure. Runs the reference's own code (oracle/_ref/ref_harness,
+built from the reference sources by oracle/build_ref.sh) on seeded synthetic
+PP inputs (locarna_gb300/synth.py) and stores, per case, the inputs, the
+prepared tables the reference's Scoring/ArcMatches/TraceController objects
+hold, and the reference's results (score, traceback edges, structure strings).
+
+Usage: python tests/golden/make_golden.py   (needs the reference sources)
+"""
+import json
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.dirname(HERE))
+
+from locarna_gb300.synth import make_rna  # noqa: E402
+from refdump import parse_ref  # noqa: E402
+
+HARNESS = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
+
+# name: (lenA, seedA, lenB, seedB, options, keep_tables)
+CASES = {
+    "c150_global": (150, 1, 150, 2, {}, True),
+    "c150_seqlocal": (150, 1, 150, 2, {"sequ_local": "1"}, True),
+    "c150_structlocal": (150, 1, 150, 2, {"struct_local": "1"}, True),
+    "c150_freeall": (150, 1, 150, 2, {"free_endgaps": "++++"}, True),
+    "c150_freeright": (150, 1, 150, 2, {"free_endgaps": "-+-+"}, True),
+    "c150_freeleft": (150, 1, 150, 2, {"free_endgaps": "+-+-"}, True),
+    "c150_noenv": (150, 1, 150, 2, {"min_trace_prob": "0"}, True),
+    "c150_b": (150, 11, 140, 12, {}, True),
+    "c120_opening0": (120, 21, 130, 22, {"indel_opening": "0"}, True),
+    "c90_seqlocal_b": (90, 31, 100, 32, {"sequ_local": "1"}, True),
+    "c60_short": (60, 41, 70, 42, {}, True),
+    "c200_global": (200, 5, 200, 6, {}, True),
+    "c400_global": (400, 3, 400, 4, {}, True),
+}
+
+
+def make_case(name, spec, workdir):
+    la, sa, lb, sb, opts, keep = spec
+    ra, rb = make_rna(la, sa), make_rna(lb, sb)
+    pa, pb = os.path.join(workdir, name + "_A.pp"), os.path.join(workdir, name + "_B.pp")
+    with open(pa, "w") as f:
+        f.write(ra.to_pp())
+    with open(pb, "w") as f:
+        f.write(rb.to_pp())
+    args = [HARNESS, pa, pb] + [f"{k}={v}" for k, v in opts.items()]
+    txt = subprocess.run(args, capture_output=True, text=True, check=True).stdout
+    ref = parse_ref(txt)
+    t = ref["tables"]
+    out = {
+        "pp_a": ra.to_pp(), "pp_b": rb.to_pp(), "opts": json.dumps(opts),
+        "score": ref["score"], "edges": np.array(ref["edges"], dtype=np.int32),
+        "struct_a": ref["struct_a"], "struct_b": ref["struct_b"],
+        "min_col": np.array(ref["min_col"], dtype=np.int32),
+        "max_col": np.array(ref["max_col"], dtype=np.int32),
+        "num_arcs": np.array(ref["num_arcs"], dtype=np.int32),
+        "num_am": ref["num_am"],
+        "seq_a": ref["seq_a"], "seq_b": ref["seq_b"],
+        "indel_opening": t.indel_opening, "exclusion": t.exclusion,
+        "gap_a": t.gap_a, "gap_b": t.gap_b,
+        "arcs_a": t.arcs_a, "arcs_b": t.arcs_b,
+        "am_arcs": t.am_arcs, "am_score": t.am_score,
+        "sigma": t.sigma.astype(np.int16) if np.abs(t.sigma).max() < 32000 else t.sigma,
+    }
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    return ref
+
+
+def main():
+    if not os.path.exists(HARNESS):
+        raise SystemExit("build the reference oracle first: oracle/build_ref.sh")
+    work = os.path.join(ROOT, "_work", "golden_pp")
+    os.makedirs(work, exist_ok=True)
+    names = sys.argv[1:] or list(CASES)
+    for name in names:
+        ref = make_case(name, CASES[name], work)
+        print(name, "score", ref["score"], "am", ref["num_am"])
+
+
+if __name__ == "__main__":
+    main()

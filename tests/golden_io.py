@@ -1,0 +1,51 @@
+"""Loader of the golden fixtures in tests/golden/*.npz (made by make_golden.py)."""
+import glob
+import json
+import os
+
+import numpy as np
+
+from locarna_gb300.abi import PairTables
+
+GOLDEN_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def golden_names():
+    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN_DIR, "*.npz")))
+
+
+class Golden:
+    def __init__(self, name):
+        z = np.load(os.path.join(GOLDEN_DIR, name + ".npz"))
+        self.name = name
+        self.opts = json.loads(str(z["opts"]))
+        self.pp_a, self.pp_b = str(z["pp_a"]), str(z["pp_b"])
+        self.seq_a, self.seq_b = str(z["seq_a"]), str(z["seq_b"])
+        self.score = int(z["score"])
+        self.edges = [tuple(int(v) for v in e) for e in z["edges"]]
+        self.struct_a, self.struct_b = str(z["struct_a"]), str(z["struct_b"])
+        self.min_col, self.max_col = z["min_col"], z["max_col"]
+        self.num_arcs = tuple(int(x) for x in z["num_arcs"])
+        self.num_am = int(z["num_am"])
+        n, m = len(self.seq_a), len(self.seq_b)
+        self.tables = PairTables(
+            n, m, z["sigma"].astype(np.int32), z["gap_a"], z["gap_b"],
+            int(z["indel_opening"]), int(z["exclusion"]), z["arcs_a"], z["arcs_b"],
+            z["am_arcs"], z["am_score"], self.min_col, self.max_col,
+            seq_a=self.seq_a, seq_b=self.seq_b)
+
+    @property
+    def struct_local(self):
+        return self.opts.get("struct_local") == "1"
+
+    @property
+    def sequ_local(self):
+        return self.opts.get("sequ_local") == "1"
+
+    @property
+    def free_endgaps(self):
+        return self.opts.get("free_endgaps", "----")
+
+    def align_kwargs(self):
+        return dict(struct_local=self.struct_local, sequ_local=self.sequ_local,
+                    free_endgaps=self.free_endgaps)
