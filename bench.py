@@ -1,0 +1,366 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 sparsified Sankoff engine.
+
+Workload (one "step"): all-pairs structural alignment of 64 synthetic RNAs with
+lengths uniform in [60, 400] nt = 2,016 pairs, locarna default scoring and
+flags (global, RIBOSUM85_60, envelope 1e-4), bit-exact scores + traceback.
+Inputs are seeded synthetic PP data (locarna_gb300/synth.py) with the shapes of
+the all-pairs workload; there is no public dataset involved.
+
+Metric: aligns/s (pairs aligned per second, whole job).
+  value : pairs / device time of the kernels (inputs resident in HBM)
+  e2e   : pairs / wall time of the public C-ABI call lcg_align_pairs with
+          host tables in and host results out (all copies inside)
+
+--impl reference times the reference CPU implementation of the same path
+(the plain-C oracle restatement of the reference's Aligner, since the
+reference itself cannot be built on this host) on a bounded sample of the
+same workload with one process per host core.
+"""
+import argparse
+import json
+import multiprocessing as mp
+import os
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = dict(count=64, len_lo=60, len_hi=400, seed=2024, q=0.05)
+WORKLOAD_NAME = "sankoff_allpairs_64rnas_60-400nt_global"
+PER_PAIR = dict(len_a=400, seed_a=3, len_b=400, seed_b=4)
+CPU_SAMPLE_SECONDS = 20.0
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def build_tables(threads=None):
+    from concurrent.futures import ThreadPoolExecutor
+
+    from locarna_gb300.prep import prepare_pair
+    from locarna_gb300.synth import make_family
+    fam = make_family(WORKLOAD["count"], WORKLOAD["len_lo"], WORKLOAD["len_hi"], WORKLOAD["seed"],
+                      q=WORKLOAD["q"])
+    pp = [r.to_pp() for r in fam]
+    pairs = [(a, b) for a in range(len(fam)) for b in range(a + 1, len(fam))]
+    threads = threads or os.cpu_count() or 4
+    with ThreadPoolExecutor(threads) as ex:
+        tables = list(ex.map(lambda ab: prepare_pair(pp[ab[0]], pp[ab[1]]), pairs))
+    return tables, pairs
+
+
+def per_pair_tables():
+    from locarna_gb300.prep import prepare_pair
+    from locarna_gb300.synth import make_rna
+    a = make_rna(PER_PAIR["len_a"], PER_PAIR["seed_a"])
+    b = make_rna(PER_PAIR["len_b"], PER_PAIR["seed_b"])
+    return prepare_pair(a.to_pp(), b.to_pp())
+
+
+# ---------------------------------------------------------------- CPU side
+
+_CPU_TABLES = None  # inherited by forked workers (the pool starts before any GPU call)
+
+
+def _cpu_worker(args):
+    idx, budget = args
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from oracle_ffi import oracle_align
+    t0 = time.perf_counter()
+    done = 0
+    for k in idx:
+        if time.perf_counter() - t0 >= budget:
+            break
+        oracle_align(_CPU_TABLES[k])
+        done += 1
+    return done, time.perf_counter() - t0
+
+
+def cpu_sample(tables, budget_s, cores, seed=7):
+    """Time-bounded CPU sample of the workload: a seeded permutation of the
+    pairs dealt round-robin to one forked process per core; each process
+    aligns its pairs until budget_s is spent. Returns (pairs, aligns/s)."""
+    import random
+    global _CPU_TABLES
+    _CPU_TABLES = tables
+    order = list(range(len(tables)))
+    random.Random(seed).shuffle(order)
+    lists = [order[c::cores] for c in range(cores)]
+    ctx = mp.get_context("fork")
+    with ctx.Pool(cores) as pool:
+        res = pool.map(_cpu_worker, [(lst, budget_s) for lst in lists])
+    done = sum(d for d, _ in res)
+    rate = sum(d / t for d, t in res if t > 0)
+    return done, rate
+
+
+# ---------------------------------------------------------------- clocks
+
+class ClockSampler:
+    def __init__(self):
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", "bench_clocks.csv")
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,"
+                 "clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+                 "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_power_cap", "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sms, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sms.append(float(p[1]))
+                mx = float(p[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        sms.sort()
+        return {"sm_mhz": sms[len(sms) // 2] if sms else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sms)}
+
+
+# ---------------------------------------------------------------- arms
+
+def run_ours(args):
+    import numpy as np
+    from locarna_gb300.engine import Engine
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    t0 = time.time()
+    tables, pairs = build_tables()
+    log(f"host preparation of {len(tables)} pairs: {time.time() - t0:.1f} s")
+    npairs = len(tables)
+    # CPU baseline first (forked workers must start before the first GPU call):
+    # the oracle restatement of the reference's Aligner on a bounded sample
+    cores = os.cpu_count() or 1
+    cpu_done, cpu_rate = cpu_sample(tables, CPU_SAMPLE_SECONDS, cores)
+    log(f"cpu baseline: {cpu_done} pairs, {cpu_rate:.2f} aligns/s on {cores} cores")
+    eng = Engine(0)
+    call = eng.prepare_call(tables)
+
+    # measurement-only runs (outside the timed region): work counts
+    eng.set_counting(True)
+    eng.run_call(call)
+    work = eng.last_work()
+    eng.set_counting(False)
+    int_peak = max(eng.int_peak_gops(False), eng.int_peak_gops(True))
+
+    # L2 flush buffer (larger than the 129 MB L2)
+    flush = None
+    try:
+        import torch
+        flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.int32, device="cuda:0")
+    except Exception:
+        flush = None
+
+    def flush_l2():
+        if flush is not None:
+            flush.fill_(1)
+            import torch
+            torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        eng.run_call(call)
+    sampler = ClockSampler()
+    sampler.start()
+    kern_ms, fill_ms, wall_s = 0.0, 0.0, 0.0
+    launches = 0
+    for _ in range(args.steps):
+        flush_l2()
+        s0 = time.perf_counter()
+        eng.run_call(call)  # synchronises inside (results are on the host)
+        wall_s += time.perf_counter() - s0
+        ms, nl = eng.last_stats()
+        f, _ = eng.last_timing()
+        kern_ms += ms
+        fill_ms += f
+        launches += nl
+    clocks = sampler.stop()
+    h2d, d2h = eng.last_transfer()
+    res = Engine.decode_call(call)
+    # spot check: the first pairs against the oracle
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from checks import assert_same_result
+    from oracle_ffi import oracle_align
+    for k in range(0, npairs, max(1, npairs // 6)):
+        assert_same_result(res[k], oracle_align(tables[k]), f"pair {k}")
+
+    # per-pair: the 400 x 400 pair alone, and the workload one pair per call
+    pt = per_pair_tables()
+    pcall = eng.prepare_call([pt])
+    for _ in range(3):
+        eng.run_call(pcall)
+    single_ms = []
+    for _ in range(5):
+        flush_l2()
+        eng.run_call(pcall)
+        single_ms.append(eng.last_stats()[0])
+    single_ms.sort()
+    sample = list(range(0, npairs, 16))
+    per_calls = [eng.prepare_call([tables[k]]) for k in sample]
+    for c in per_calls[:4]:
+        eng.run_call(c)
+    t1 = time.perf_counter()
+    dev_ms_single = 0.0
+    for c in per_calls:
+        eng.run_call(c)
+        dev_ms_single += eng.last_stats()[0]
+    wall_single = time.perf_counter() - t1
+
+    T = kern_ms / 1e3 / args.steps
+    Tf = fill_ms / 1e3 / args.steps
+    We = wall_s / args.steps
+    value = npairs / T
+    ops = 10 * work["cells"] + 2 * max(work["arc_terms"], 0)
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    alg_bytes = h2d + d2h  # every input table read once, every result written once
+    out = {
+        "metric": "aligns/s (Sankoff all-pairs, bit-exact score+traceback)",
+        "value": value,
+        "unit": "aligns/s",
+        "n_gpus": 1,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": T * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "int32",
+        "data": "synthetic (seeded PP inputs, locarna_gb300/synth.py)",
+        "config": {"workload": WORKLOAD_NAME, "pairs": npairs, "rnas": WORKLOAD["count"],
+                   "len_range": [WORKLOAD["len_lo"], WORKLOAD["len_hi"]], "seed": WORKLOAD["seed"],
+                   "mode": "global, default locarna scoring, envelope 1e-4",
+                   "l2": "flushed between steps (256 MB write)"},
+        "gcups": work["cells"] / T / 1e9,
+        "e2e": {"value": npairs / We, "unit": "aligns/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "ms_per_step": We * 1e3},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "achieved": alg_bytes / Tf / 1e9, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": alg_bytes / Tf / 1e9 / hbm_peak, "traffic": None,
+                     "note": "dominant kernel sankoff_fill_kernel; integer/latency bound, see int_ops"},
+        "int_ops": {"ops_per_step": ops, "achieved_gops": ops / Tf / 1e9, "peak_gops": int_peak,
+                    "frac": ops / Tf / 1e9 / int_peak, "cells": work["cells"],
+                    "arc_terms": work["arc_terms"], "groups": work["groups"]},
+        "per_pair": {"workload": "one 400x400 nt pair, global", "device_ms": single_ms[len(single_ms) // 2],
+                     "aligns_per_s": 1e3 / single_ms[len(single_ms) // 2],
+                     "per_pair_launch_aligns_per_s_device": len(sample) / (dev_ms_single / 1e3),
+                     "per_pair_launch_aligns_per_s_wall": len(sample) / wall_single,
+                     "batched_over_per_pair_launch": value / (len(sample) / (dev_ms_single / 1e3))},
+        "cpu_baseline": {"value": cpu_rate, "unit": "aligns/s", "cores": cores, "kind": "port",
+                         "sample": f"{cpu_done} of the {npairs} pairs (seeded permutation), one process "
+                                   f"per core, {CPU_SAMPLE_SECONDS:.0f} s per process"},
+        "clocks": clocks,
+    }
+    print(json.dumps(out), flush=True)
+    eng.close()
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    t0 = time.time()
+    tables, pairs = build_tables()
+    log(f"host preparation of {len(tables)} pairs: {time.time() - t0:.1f} s")
+    cores = os.cpu_count() or 1
+    budget = max(2.0, 60.0 / max(1, args.steps + args.warmup))
+    vals, dones = [], []
+    for s in range(args.warmup + args.steps):
+        done, rate = cpu_sample(tables, budget, cores, seed=7 + s)
+        if s >= args.warmup:
+            vals.append(rate)
+            dones.append(done)
+    v = sum(vals) / len(vals)
+    out = {
+        "metric": "aligns/s (Sankoff all-pairs, bit-exact score+traceback)",
+        "value": v, "unit": "aligns/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * len(tables) / v, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int64", "data": "synthetic (seeded PP inputs)",
+        "impl": "reference",
+        "config": {"workload": WORKLOAD_NAME, "pairs": len(tables)},
+        "cpu_baseline": {"value": v, "unit": "aligns/s", "cores": cores, "kind": "port",
+                         "sample": f"~{sum(dones) // len(dones)} pairs per step of the {len(tables)} "
+                                   f"(time-bounded {budget:.0f} s per process), one process per core"},
+        "e2e": {"value": v, "unit": "aligns/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+
+
+def run_small_case(args):
+    """A small batch of the same kind of work, one plain run, for profiling:
+    `--case small` aligns all pairs of 32 RNAs of 100-150 nt (496 pairs)."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    from locarna_gb300.engine import Engine
+    from locarna_gb300.prep import prepare_pair
+    from locarna_gb300.synth import make_family
+    fam = make_family(32, 100, 150, 77)
+    pp = [r.to_pp() for r in fam]
+    pairs = [(a, b) for a in range(len(fam)) for b in range(a + 1, len(fam))]
+    with ThreadPoolExecutor(os.cpu_count() or 4) as ex:
+        tables = list(ex.map(lambda ab: prepare_pair(pp[ab[0]], pp[ab[1]]), pairs))
+    eng = Engine(0)
+    for mode in ({}, {"struct_local": True}) if args.struct_local else ({},):
+        call = eng.prepare_call(tables, **mode)
+        for _ in range(max(1, args.warmup)):
+            eng.run_call(call)
+        ms, nl = eng.last_stats()
+        f, t = eng.last_timing()
+        print(json.dumps({"case": "small", "mode": mode, "pairs": len(tables), "kernel_ms": ms,
+                          "fill_ms": f, "trace_ms": t, "launches": nl}), flush=True)
+    eng.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--case", default="full", choices=["full", "small"])
+    ap.add_argument("--struct-local", action="store_true", help="small case: also struct-local")
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    if int(os.environ.get("WORLD_SIZE", "1")) > 1 and int(os.environ.get("RANK", "0")) != 0:
+        # pairs shard with no exchange; this build measures one GPU
+        return
+    from locarna_gb300.build import build_engine, build_oracle
+    build_engine()
+    build_oracle()
+    if args.case == "small":
+        run_small_case(args)
+        return
+    run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -162,6 +162,24 @@ lcg_status lcg_align_pairs(lcg_engine eng, const lcg_pair_tables *pairs,
 lcg_status lcg_engine_last_stats(lcg_engine eng, double *kernel_ms,
                                  int64_t *launches);
 
+/* Device time (ms) of the last call's D-fill kernel and traceback kernel. */
+lcg_status lcg_engine_last_timing(lcg_engine eng, double *fill_ms, double *trace_ms);
+
+/* Bytes the last lcg_align_pairs call copied host->device and device->host. */
+lcg_status lcg_engine_last_transfer(lcg_engine eng, int64_t *h2d_bytes,
+                                    int64_t *d2h_bytes);
+
+/* Work counts of the last call (all pairs): groups and cells always; with
+ * counting on, arc_terms = candidate list entries visited and
+ * valid_arc_terms = arc-match terms evaluated (else -1). Counting makes the
+ * fill kernel slower: use it for measurement runs only. */
+lcg_status lcg_engine_set_counting(lcg_engine eng, int32_t on);
+lcg_status lcg_engine_last_work(lcg_engine eng, lcg_work_counts *out);
+
+/* Measured device rate of int32 add+max (2 ops each) in G ops/s, with plain
+ * add/max instructions (dpx = 0) or the fused __viaddmax_s32 (dpx = 1). */
+lcg_status lcg_measure_int_peak(lcg_engine eng, int32_t dpx, double *gops);
+
 
 /* ------------------------------------------------------ host preparation
  *

@@ -21,7 +21,7 @@ ORACLE = os.path.join(ROOT, "oracle")
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 
-CUDA_SOURCES = ["engine.cu", "sankoff_kernels.cu"]
+CUDA_SOURCES = ["engine.cu", "sankoff_kernels.cu", "sankoff_sl_kernels.cu", "microbench.cu"]
 HOST_SOURCES = ["host_prep.cpp"]  # C++ host-only translation units
 
 

@@ -19,7 +19,13 @@
 
 namespace lcg {
 cudaError_t launch_fill(const PairDev *, const GroupItem *, int, const int4 *, int *, long long,
-                        int, unsigned int *, int *, int *, int, cudaStream_t);
+                        int, unsigned int *, int *, int *, int, cudaStream_t, unsigned long long *);
+cudaError_t measure_int_peak(int sms, bool dpx, cudaStream_t st, double *gops);
+cudaError_t sl_prepare(int sw, int *blocks_per_sm);
+int sl_fill_warps_per_block();
+cudaError_t launch_sl_fill(const PairDev *, const GroupItem *, int, const int4 *, int *, long long, int,
+                           unsigned int *, int *, int *, int, cudaStream_t);
+cudaError_t launch_sl_trace(const PairDev *, int, int *, long long, int, int *, cudaStream_t);
 cudaError_t launch_trace(const PairDev *, int, int *, long long, int, int *, cudaStream_t);
 int fill_warps_per_block();
 cudaError_t fill_occupancy(int sw, int *blocks_per_sm);
@@ -63,6 +69,7 @@ struct Prep {
     std::vector<int4> dw;                        // dw_start relative to this pair
     int rows_max = 0, width_max = 0;             // over groups
     int token_cap = 0, tq_cap = 0;
+    long long cells = 0;                         // M cells of all groups + top level
     std::string err;
     lcg_status code = LCG_OK;
 };
@@ -90,12 +97,11 @@ lcg_status prep_pair(const lcg_pair_tables &t, const lcg_align_opts &o, Prep &p)
     const bool anchors = t.match_lo != nullptr;
     if (anchors && (!t.match_hi || !t.del_lo || !t.del_hi || !t.ins_lo || !t.ins_hi))
         return bad(LCG_ERR_ARG, "anchor ranges must be all set or all NULL");
-    if (o.struct_local) return bad(LCG_ERR_UNSUPPORTED, "structure-local mode is not implemented on the GPU yet");
     p.n = n;
     p.m = m;
     p.fe = o.free_endgaps & 15;
     p.flags = (o.sequ_local ? PF_SEQU_LOCAL : 0) | (anchors ? PF_ANCHORS : 0) |
-              (o.do_trace ? PF_TRACE : 0);
+              (o.do_trace ? PF_TRACE : 0) | (o.struct_local ? PF_STRUCT_LOCAL : 0);
     if (o.sequ_local && p.fe) return bad(LCG_ERR_ARG, "free end gaps cannot be combined with local alignment");
 
     // band: monotone, inside [0,m], rows non-empty and connected
@@ -228,6 +234,10 @@ lcg_status prep_pair(const lcg_pair_tables &t, const lcg_align_opts &o, Prep &p)
             }
             g.dw_count = (int)p.dw.size() - g.dw_start;
             p.groups.push_back(g);
+            for (int i = al + 1; i < max_ar; ++i) {
+                int lo = std::max(bl + 1, p.min_col[i]), hi = std::min(max_br - 1, p.max_col[i]);
+                if (hi >= lo) p.cells += hi - lo + 1;
+            }
             p.rows_max = std::max(p.rows_max, max_ar - al);
             p.width_max = std::max(p.width_max, max_br - bl + 1);
         }
@@ -241,6 +251,7 @@ lcg_status prep_pair(const lcg_pair_tables &t, const lcg_align_opts &o, Prep &p)
     top.br = m + 1;
     top.top = 1;
     p.groups.push_back(top);
+    for (int i = 1; i <= n; ++i) p.cells += std::min(m, p.max_col[i]) - std::max(1, p.min_col[i]) + 1;
     p.token_cap = 2 * (n + m) + 3 * std::min(n, m) + 16;
     p.tq_cap = std::min(n, m) / 2 + 2;
     return LCG_OK;
@@ -302,8 +313,11 @@ struct lcg_engine_s {
     int *d_scratch = nullptr;
     size_t scratch_cap = 0;  // ints
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr;
-    double last_ms = 0;
+    double last_ms = 0, last_fill_ms = 0, last_trace_ms = 0;
     long long last_launches = 0;
+    long long last_h2d = 0, last_d2h = 0;
+    long long last_groups = 0, last_cells = 0, last_terms = -1, last_visits = -1;
+    bool counting = false;
 };
 
 extern "C" {
@@ -360,6 +374,42 @@ lcg_status lcg_engine_last_stats(lcg_engine e, double *kernel_ms, int64_t *launc
     return LCG_OK;
 }
 
+lcg_status lcg_engine_last_transfer(lcg_engine e, int64_t *h2d_bytes, int64_t *d2h_bytes) {
+    if (!e) return fail(LCG_ERR_ARG, "engine is NULL");
+    if (h2d_bytes) *h2d_bytes = e->last_h2d;
+    if (d2h_bytes) *d2h_bytes = e->last_d2h;
+    return LCG_OK;
+}
+
+lcg_status lcg_engine_last_timing(lcg_engine e, double *fill_ms, double *trace_ms) {
+    if (!e) return fail(LCG_ERR_ARG, "engine is NULL");
+    if (fill_ms) *fill_ms = e->last_fill_ms;
+    if (trace_ms) *trace_ms = e->last_trace_ms;
+    return LCG_OK;
+}
+
+lcg_status lcg_engine_set_counting(lcg_engine e, int32_t on) {
+    if (!e) return fail(LCG_ERR_ARG, "engine is NULL");
+    e->counting = on != 0;
+    return LCG_OK;
+}
+
+lcg_status lcg_engine_last_work(lcg_engine e, lcg_work_counts *w) {
+    if (!e || !w) return fail(LCG_ERR_ARG, "NULL argument");
+    w->groups = e->last_groups;
+    w->cells = e->last_cells;
+    w->arc_terms = e->last_visits;
+    w->valid_arc_terms = e->last_terms;
+    return LCG_OK;
+}
+
+lcg_status lcg_measure_int_peak(lcg_engine e, int32_t dpx, double *gops) {
+    if (!e || !gops) return fail(LCG_ERR_ARG, "NULL argument");
+    CUDA_TRY(cudaSetDevice(e->device));
+    CUDA_TRY(measure_int_peak(e->sms, dpx != 0, e->stream, gops));
+    return LCG_OK;
+}
+
 lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t npairs,
                            const lcg_align_opts *opts, lcg_align_result *results) {
     if (!e || !pairs || !opts || !results || npairs < 0) return fail(LCG_ERR_ARG, "NULL argument");
@@ -408,7 +458,7 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
     }
     size_t off_items = take(up, sizeof(GroupItem) * nitems);
     size_t off_dw = take(up, sizeof(int4) * std::max<size_t>(ndw, 1));
-    size_t off_ctrl = take(up, 64);
+    size_t off_ctrl = take(up, 64);  // qhead, status, abort, pad, 2 x u64 counters
     for (int q = 0; q < npairs; ++q) {
         const auto &p = prep[q];
         const auto &t = pairs[q];
@@ -564,14 +614,21 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
     }
 
     // ---- scratch
+    const bool sl = opts->struct_local != 0;
     int blocks_per_sm = 0;
-    CUDA_TRY(fill_occupancy(sw, &blocks_per_sm));
+    if (sl) {
+        CUDA_TRY(sl_prepare(sw, &blocks_per_sm));
+    } else {
+        CUDA_TRY(fill_occupancy(sw, &blocks_per_sm));
+        CUDA_TRY(trace_prepare(sw));
+    }
     if (blocks_per_sm < 1) return fail(LCG_ERR_UNSUPPORTED, "fill kernel does not fit on an SM");
-    CUDA_TRY(trace_prepare(sw));
     int blocks = e->sms * blocks_per_sm;
     long long stride = (long long)rows_max * sw;
-    size_t slots = std::max<size_t>((size_t)blocks * fill_warps_per_block(), (size_t)npairs);
-    size_t need = slots * (size_t)stride;
+    // state matrices per slot: fill 1 (plain) / 4 (struct-local); traceback 1 / 8
+    size_t fill_slots = (size_t)blocks * (sl ? sl_fill_warps_per_block() * 4 : fill_warps_per_block());
+    size_t trace_slots = (size_t)npairs * (sl ? 8 : 1);
+    size_t need = std::max(fill_slots, trace_slots) * (size_t)stride;
     if (need > e->scratch_cap) {
         if (e->d_scratch) cudaFree(e->d_scratch);
         e->d_scratch = nullptr;
@@ -589,23 +646,54 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
     int *status = (int *)(Dv + off_ctrl + 4);
     int *abort_flag = (int *)(Dv + off_ctrl + 8);
     CUDA_TRY(cudaEventRecord(e->ev0, st));
-    CUDA_TRY(launch_fill((const PairDev *)(Dv + off_pairs), (const GroupItem *)(Dv + off_items), (int)nitems,
-                         (const int4 *)(Dv + off_dw), e->d_scratch, stride, sw, qhead, status, abort_flag,
-                         blocks, st));
+    unsigned long long *counters = e->counting ? (unsigned long long *)(Dv + off_ctrl + 16) : nullptr;
+    if (sl) {
+        if (counters) return fail(LCG_ERR_UNSUPPORTED, "work counting covers the plain mode only");
+        CUDA_TRY(launch_sl_fill((const PairDev *)(Dv + off_pairs), (const GroupItem *)(Dv + off_items),
+                                (int)nitems, (const int4 *)(Dv + off_dw), e->d_scratch, stride, sw, qhead,
+                                status, abort_flag, blocks, st));
+    } else {
+        CUDA_TRY(launch_fill((const PairDev *)(Dv + off_pairs), (const GroupItem *)(Dv + off_items),
+                             (int)nitems, (const int4 *)(Dv + off_dw), e->d_scratch, stride, sw, qhead,
+                             status, abort_flag, blocks, st, counters));
+    }
     CUDA_TRY(cudaEventRecord(e->ev1, st));
     long long launches = 1;
     if (opts->do_trace) {
-        CUDA_TRY(launch_trace((const PairDev *)(Dv + off_pairs), npairs, e->d_scratch, stride, sw, status, st));
+        if (sl)
+            CUDA_TRY(launch_sl_trace((const PairDev *)(Dv + off_pairs), npairs, e->d_scratch, stride, sw,
+                                     status, st));
+        else
+            CUDA_TRY(launch_trace((const PairDev *)(Dv + off_pairs), npairs, e->d_scratch, stride, sw, status,
+                                  st));
         ++launches;
     }
     CUDA_TRY(cudaEventRecord(e->ev2, st));
     CUDA_TRY(cudaMemcpyAsync(H + off_ctrl, Dv + off_ctrl, 64, cudaMemcpyDeviceToHost, st));
     CUDA_TRY(cudaMemcpyAsync(H + down_begin, Dv + down_begin, down_end - down_begin, cudaMemcpyDeviceToHost, st));
     CUDA_TRY(cudaStreamSynchronize(st));
-    float ms = 0;
+    float ms = 0, ms1 = 0;
     cudaEventElapsedTime(&ms, e->ev0, e->ev2);
+    cudaEventElapsedTime(&ms1, e->ev0, e->ev1);
     e->last_ms = ms;
+    e->last_fill_ms = ms1;
+    e->last_trace_ms = ms - ms1;
     e->last_launches = launches;
+    e->last_h2d = (long long)down_begin;
+    e->last_d2h = 64 + (long long)(down_end - down_begin);
+    e->last_groups = 0;
+    e->last_cells = 0;
+    for (auto &p : prep) {
+        e->last_groups += (long long)p.groups.size() - 1;
+        e->last_cells += p.cells;
+    }
+    if (e->counting) {
+        const unsigned long long *cn = (const unsigned long long *)(H + off_ctrl + 16);
+        e->last_terms = (long long)cn[0];
+        e->last_visits = (long long)cn[1];
+    } else {
+        e->last_terms = e->last_visits = -1;
+    }
     int hstatus = ((int *)(H + off_ctrl))[1];
     if (hstatus & ST_TIMEOUT) return fail(LCG_ERR_TIMEOUT, "a device wait for an arc-match entry timed out");
     if (hstatus & ST_OVERFLOW) return fail(LCG_ERR_DEVICE, "traceback buffer overflow");

@@ -31,330 +31,16 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
-#include "lcg_device.cuh"
+#include "sankoff_group.cuh"
 
 namespace lcg {
 
-constexpr int FILL_WARPS = 8;   // warps per block of the fill kernel
-constexpr int TRACE_WARPS = 4;  // warps per block of the trace kernel
-constexpr long long SPIN_LIMIT = 1ll << 22;  // ~ seconds of polling, then ST_TIMEOUT
-
-__device__ __forceinline__ int addc(int x, int y) {
-    // saturating add of two values >= 2*NEG; result clamped to >= NEG
-    int s = x + y;
-    return s < NEG ? NEG : s;
-}
-
-__device__ __forceinline__ int ld_volatile(const int *p) {
-    return *(const volatile int *)p;
-}
-__device__ __forceinline__ void st_volatile(int *p, int v) { *(volatile int *)p = v; }
-
-struct TopOut {
-    int best, bi, bj;
-};
-
-// Read D[k], spinning while its producer has not written it yet.
-__device__ __forceinline__ int wait_D(int *D, int k, int *status, volatile int *abort_flag) {
-    int v = ld_volatile(D + k);
-    if (v != NOT_READY) return v;
-    long long spins = 0;
-    while (v == NOT_READY) {
-        __nanosleep(64);
-        v = ld_volatile(D + k);
-        if (++spins > SPIN_LIMIT || *abort_flag) {
-            atomicOr(status, ST_TIMEOUT);
-            *abort_flag = 1;
-            return NEG;
-        }
-    }
-    return v;
-}
-
-// One left-end group (or the top level) in state E_NO_NO:
-// init_state (aligner.cc:264-368) + the row sweep of align_in_arcmatch
-// (aligner.cc:424-437) with align_noex per cell. M of the rectangle is
-// written to Mg (row r = i-al, column c = j-bl, row pitch `pitch`).
-// prev/cur/E are per-warp shared-memory rows indexed by c.
-template <bool TOP, bool WAIT, bool DWRITE>
-__device__ void run_group(const PairDev &P, int al, int ar, int bl, int br, int *__restrict__ Mg,
-                          int pitch, int *prev, int *cur, int *E, const int4 *__restrict__ dw,
-                          int ndw, bool globalA, bool globalB, bool local_top, int *status,
-                          volatile int *abort_flag, TopOut *tout) {
-    const int lane = threadIdx.x & 31;
-    const int m1 = P.m + 1;
-    const int go = P.go;
-    const int W = br - bl;
-    for (int c = lane; c < W; c += 32) E[c] = NEG;
-
-    // ---- row al: M(al,bl)=0, M(al,j) = prefix of gap costs, -inf once blocked
-    const int L0 = min(br, P.max_col[al] + 1);
-    {
-        int carry = globalB ? go : 0;
-        bool blocked_carry = false;
-        for (int base = bl + 1; base < L0; base += 32) {
-            int j = base + lane;
-            bool act = j < L0;
-            bool blk = act && !a_ins(P, al, j);
-            int s = (act && globalB) ? P.gapB[j] : 0;
-            unsigned bm = __ballot_sync(0xffffffffu, blk);
-#pragma unroll
-            for (int off = 1; off < 32; off <<= 1) {
-                int t = __shfl_up_sync(0xffffffffu, s, off);
-                if (lane >= off) s += t;
-            }
-            bool anyblk = blocked_carry || (bm & (0xffffffffu >> (31 - lane)));
-            int val = anyblk ? NEG : carry + s;
-            if (act) {
-                prev[j - bl] = val;
-                Mg[j - bl] = val;
-            }
-            carry += __shfl_sync(0xffffffffu, s, 31);
-            blocked_carry = blocked_carry || bm != 0;
-        }
-        if (lane == 0) {
-            prev[0] = 0;
-            Mg[0] = 0;
-        }
-        // cells above the band of row al+1 (aligner.cc:361-367)
-        if (al + 1 < ar) {
-            int L1 = min(br, P.max_col[al + 1] + 1);
-            for (int j = L0 + lane; j < L1; j += 32) prev[j - bl] = NEG;
-        }
-    }
-    __syncwarp();
-
-    int colval = globalA ? go : 0;
-    bool colblocked = false;
-    int dwp = 0;
-    int best = TOP ? 0 : NEG, bi = 0, bj = 0;  // sequence-local argmax (aligner.cc:865-875)
-    const int la = P.la, lb = P.lb, ra = P.ra, rb = P.rb;
-
-    for (int i = al + 1; i < ar; ++i) {
-        const int minc = P.min_col[i];
-        const int maxc = P.max_col[i];
-        const int lo = max(bl + 1, minc);
-        const int hi = min(br - 1, maxc);
-        const int gAi = P.gapA[i];
-        int B;  // M(i, lo-1)
-        if (minc <= bl) {
-            if (!colblocked) {
-                if (!a_del(P, i, bl)) colblocked = true;
-                else if (globalA) colval += gAi;
-            }
-            B = colblocked ? NEG : colval;
-            if (lane == 0) Mg[(i - al) * pitch] = B;
-        } else {
-            B = NEG;
-        }
-        if (lane == 0 && lo - 1 - bl < W) cur[lo - 1 - bl] = B;
-        const int *sig_row = P.sigma + (size_t)i * m1;
-        int *Mrow = Mg + (size_t)(i - al) * pitch - bl;
-        const int cell0 = P.bandoff[i] - minc;
-        int Fc = NEG, Xc = B;
-        for (int base = lo; base <= hi; base += 32) {
-            const int j = base + lane;
-            const bool act = j <= hi;
-            const int c = j - bl;
-            int X = NEG;
-            if (act) {
-                const bool mok = a_match(P, i, j);
-                int d = mok ? prev[c - 1] + sig_row[j] : NEG;
-                int e = a_del(P, i, j) ? max(E[c] + gAi, prev[c] + gAi + go) : NEG;
-                e = norm(e);
-                E[c] = e;
-                X = max(d, e);
-                if (mok) {
-                    const int cell = cell0 + j;
-                    const int q1 = P.cre_start[cell + 1];
-                    for (int q = P.cre_start[cell]; q < q1; ++q) {
-                        const int2 ent = P.cre[q];
-                        const int alq = ent.y >> 16, blq = ent.y & 0xffff;
-                        if (alq <= al) break;
-                        if (blq <= bl) continue;
-                        const int dv = WAIT ? wait_D(P.D, ent.x, status, abort_flag) : P.D[ent.x];
-                        const int mv = Mg[(size_t)(alq - 1 - al) * pitch + (blq - 1 - bl)];
-                        X = max(X, mv + dv);
-                    }
-                }
-                if (TOP && local_top && i < la && j < lb) X = max(X, 0);
-            }
-            // horizontal gaps: max-plus scan of F(j) = max(F(j-1)+a_j, b_j)
-            int Xp = __shfl_up_sync(0xffffffffu, X, 1);
-            if (lane == 0) Xp = Xc;
-            int a = 0, b = NEG;
-            if (act) {
-                if (a_ins(P, i, j)) {
-                    const int gb = P.gapB[j];
-                    a = gb + max(go, 0);
-                    b = addc(Xp, gb + go);
-                } else {
-                    a = NEG;
-                }
-            }
-#pragma unroll
-            for (int off = 1; off < 32; off <<= 1) {
-                int a1 = __shfl_up_sync(0xffffffffu, a, off);
-                int b1 = __shfl_up_sync(0xffffffffu, b, off);
-                if (lane >= off) {
-                    b = max(addc(b1, a), b);
-                    a = addc(a1, a);
-                }
-            }
-            const int F = max(addc(Fc, a), b);
-            const int M = norm(max(X, F));
-            if (act) {
-                cur[c] = M;
-                Mrow[j] = M;
-                if (TOP && local_top && i >= ra && j >= rb && M > best) {
-                    best = M;
-                    bi = i;
-                    bj = j;
-                }
-            }
-            Fc = __shfl_sync(0xffffffffu, F, 31);
-            Xc = __shfl_sync(0xffffffffu, X, 31);
-        }
-        __syncwarp();
-        if (DWRITE) {
-            // fill_D_entries for arc matches whose inner corner is in row i
-            while (dwp < ndw) {
-                const int q = dwp + lane;
-                int4 e = make_int4(0, -1, 0, 0);
-                if (q < ndw) e = dw[q];
-                const bool mine = q < ndw && e.y == i;
-                if (mine) st_volatile(P.D + e.x, norm(cur[e.z - bl] + e.w));
-                const int cnt = __popc(__ballot_sync(0xffffffffu, mine));
-                dwp += cnt;
-                if (cnt < 32) break;
-            }
-        }
-        if (i + 1 < ar) {
-            const int Ln = min(br, P.max_col[i + 1] + 1);
-            for (int j = max(hi + 1, bl + 1) + lane; j < Ln; j += 32) cur[j - bl] = NEG;
-        }
-        __syncwarp();
-        int *t = prev;
-        prev = cur;
-        cur = t;
-        if (WAIT && *abort_flag) return;
-    }
-    if (TOP) {
-        tout->best = best;
-        tout->bi = bi;
-        tout->bj = bj;
-    }
-}
-
-__device__ __forceinline__ void warp_argmax(int &v, int &k1, int &k2) {
-    // max v; ties -> smallest (k1,k2) lexicographically
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-        int v2 = __shfl_xor_sync(0xffffffffu, v, off);
-        int a2 = __shfl_xor_sync(0xffffffffu, k1, off);
-        int b2 = __shfl_xor_sync(0xffffffffu, k2, off);
-        bool take = v2 > v || (v2 == v && (a2 < k1 || (a2 == k1 && b2 < k2)));
-        if (take) {
-            v = v2;
-            k1 = a2;
-            k2 = b2;
-        }
-    }
-}
-
-// top level + final argmax: align_top_level_free_endgaps (aligner.cc:736-819)
-// and align_top_level_locally (aligner.cc:823-880)
-__device__ void run_top(const PairDev &P, int *prev, int *cur, int *E, int *status,
-                        volatile int *abort_flag) {
-    const int lane = threadIdx.x & 31;
-    const int n = P.n, m = P.m, m1 = m + 1;
-    const bool local = P.flags & PF_SEQU_LOCAL;
-    const int fe = P.free_endgaps;
-    TopOut to;
-    if (local) {
-        run_group<true, true, false>(P, 0, n + 1, 0, m + 1, P.topM, m1, prev, cur, E, nullptr, 0,
-                                     false, false, true, status, abort_flag, &to);
-        int v = to.best, i = to.bi, j = to.bj;
-        if (v <= 0) {
-            v = 0;
-            i = 0;
-            j = 0;
-        }
-        warp_argmax(v, i, j);
-        if (lane == 0) {
-            if (v <= 0) {
-                v = 0;
-                i = 0;
-                j = 0;
-            }
-            P.res[R_SCORE] = v;
-            P.res[R_MAXI] = i;
-            P.res[R_MAXJ] = j;
-        }
-        return;
-    }
-    run_group<true, true, false>(P, 0, n + 1, 0, m + 1, P.topM, m1, prev, cur, E, nullptr, 0,
-                                 !(fe & 4), !(fe & 1), false, status, abort_flag, &to);
-    __syncwarp();
-    if (!(fe & (2 | 8))) {
-        if (lane == 0) {
-            P.res[R_SCORE] = P.topM[(size_t)n * m1 + m];
-            P.res[R_MAXI] = n;
-            P.res[R_MAXJ] = m;
-        }
-        return;
-    }
-    // free right end gaps: first strict maximum over column m (i ascending),
-    // then over row n (j ascending); order key = position in that scan
-    int v = NEG, k1 = INT32_MAX, k2 = 0;
-    if (fe & 8) {
-        for (int i = max(P.ra + 1, 1) + lane; i <= n; i += 32) {
-            if (P.max_col[i] >= m) {
-                int x = P.topM[(size_t)i * m1 + m];
-                if (x > v) {
-                    v = x;
-                    k1 = i;
-                    k2 = 0;
-                }
-            }
-        }
-    }
-    if (fe & 2) {
-        int lo = max(max(P.rb + 1, 1), P.min_col[n]), hi = min(m, P.max_col[n]);
-        for (int j = lo + lane; j <= hi; j += 32) {
-            int x = P.topM[(size_t)n * m1 + j];
-            if (x > v) {
-                v = x;
-                k1 = n + 1 + j;  // after every column-m entry
-                k2 = 0;
-            }
-        }
-    }
-    warp_argmax(v, k1, k2);
-    if (lane == 0) {
-        int mi = 0, mj = 0;
-        if (v > NEG) {
-            if (k1 <= n) {
-                mi = k1;
-                mj = m;
-            } else {
-                mi = n;
-                mj = k1 - n - 1;
-            }
-        } else {
-            v = NEG;
-        }
-        P.res[R_SCORE] = v;
-        P.res[R_MAXI] = mi;
-        P.res[R_MAXJ] = mj;
-    }
-}
-
+template <bool COUNT>
 __global__ void __launch_bounds__(FILL_WARPS * 32)
     sankoff_fill_kernel(const PairDev *__restrict__ pairs, const GroupItem *__restrict__ items,
                         int nitems, const int4 *__restrict__ dw, int *scratch,
                         long long scratch_stride, int sw, unsigned int *qhead, int *status,
-                        int *abort_flag_ptr) {
+                        int *abort_flag_ptr, unsigned long long *counters) {
     extern __shared__ int smem[];
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
@@ -371,129 +57,14 @@ __global__ void __launch_bounds__(FILL_WARPS * 32)
         const GroupItem it = items[idx];
         const PairDev &P = pairs[it.pair];
         if (it.top) {
-            run_top(P, prev, cur, E, status, abort_flag);
+            run_top<COUNT>(P, prev, cur, E, status, abort_flag, counters);
         } else {
-            run_group<false, true, true>(P, it.al, it.ar, it.bl, it.br, Mg, sw, prev, cur, E,
-                                         dw + it.dw_start, it.dw_count, true, true, false,
-                                         status, abort_flag, nullptr);
+            run_group<false, true, true, COUNT>(P, it.al, it.ar, it.bl, it.br, Mg, sw, prev, cur,
+                                                E, dw + it.dw_start, it.dw_count, true, true,
+                                                false, status, abort_flag, nullptr, counters);
         }
         __syncwarp();
     }
-}
-
-// ---------------------------------------------------------------- traceback
-
-struct Walker {
-    const PairDev &P;
-    int ntok, qtail;
-    bool ok;
-    __device__ Walker(const PairDev &p) : P(p), ntok(0), qtail(0), ok(true) {}
-    __device__ void emit(int a, int b) {
-        if (ntok < P.token_cap) P.tokens[ntok] = make_int2(a, b);
-        else ok = false;
-        ++ntok;
-    }
-    __device__ bool valid(int i, int j) const {
-        return i >= 0 && i <= P.n && P.min_col[i] <= j && j <= P.max_col[i];
-    }
-};
-
-// Walk back from (i,j) inside the rectangle with origin (al,bl) whose M is
-// Mg (pitch), emitting tokens in reverse append order. Arc-match tokens are
-// (-2, am); each traced arc match is queued for its own walk.
-__device__ void walk(Walker &w, const int *Mg, int pitch, int al, int bl, int i, int j, bool tl,
-                     int *status) {
-    const PairDev &P = w.P;
-    const bool local = P.flags & PF_SEQU_LOCAL;
-    const int fe = P.free_endgaps;
-    const int m1 = P.m + 1;
-    const int go = P.go;
-#define MM(x, y) Mg[(size_t)((x) - al) * pitch + ((y) - bl)]
-    for (int guard = 0; guard < 4 * (P.n + P.m + 4); ++guard) {
-        const int Mij = MM(i, j);
-        if (tl && local && Mij == 0) {
-            P.res[R_MINI] = i;
-            P.res[R_MINJ] = j;
-            return;
-        }
-        if (i <= al) {
-            if (!(tl && (local || (fe & 1))))
-                for (int k = j; k > bl; --k) w.emit(-1, k);
-            return;
-        }
-        if (j <= bl) {
-            if (!(tl && (local || (fe & 4))))
-                for (int k = i; k > al; --k) w.emit(k, -1);
-            return;
-        }
-        if (a_match(P, i, j) && w.valid(i - 1, j - 1) &&
-            Mij == MM(i - 1, j - 1) + P.sigma[(size_t)i * m1 + j]) {
-            w.emit(i, j);
-            --i;
-            --j;
-            continue;
-        }
-        bool found = false;
-        if (go == 0) {
-            if (a_del(P, i, j) && w.valid(i - 1, j) && Mij == MM(i - 1, j) + P.gapA[i]) {
-                w.emit(i, -1);
-                --i;
-                continue;
-            }
-            if (a_ins(P, i, j) && w.valid(i, j - 1) && Mij == MM(i, j - 1) + P.gapB[j]) {
-                w.emit(-1, j);
-                --j;
-                continue;
-            }
-        } else {
-            int gap = go;
-            for (int k = 1; i >= al + k && a_del(P, i - k + 1, j); ++k) {
-                if (!w.valid(i - k, j)) break;
-                gap += P.gapA[i - k + 1];
-                if (Mij == MM(i - k, j) + gap) {
-                    for (int l = 1; l <= k; ++l) w.emit(i - l + 1, -1);
-                    i -= k;
-                    found = true;
-                    break;
-                }
-            }
-            if (found) continue;
-            gap = go;
-            for (int k = 1; j >= bl + k && a_ins(P, i, j - k + 1); ++k) {
-                if (!w.valid(i, j - k)) break;
-                gap += P.gapB[j - k + 1];
-                if (Mij == MM(i, j - k) + gap) {
-                    for (int l = 1; l <= k; ++l) w.emit(-1, j - l + 1);
-                    j -= k;
-                    found = true;
-                    break;
-                }
-            }
-            if (found) continue;
-        }
-        if (!(a_match(P, i, j) && w.valid(i - 1, j - 1))) return;
-        const int cell = P.bandoff[i] + j - P.min_col[i];
-        for (int q = P.cre_start[cell]; q < P.cre_start[cell + 1]; ++q) {
-            const int2 ent = P.cre[q];
-            const int alq = ent.y >> 16, blq = ent.y & 0xffff;
-            if (alq <= al || blq <= bl) continue;
-            if (Mij == MM(alq - 1, blq - 1) + P.D[ent.x]) {
-                w.emit(i, j);
-                w.emit(-2, ent.x);
-                w.emit(alq, blq);
-                if (w.qtail < P.tq_cap) P.tq[w.qtail] = ent.x;
-                else w.ok = false;
-                ++w.qtail;
-                i = alq - 1;
-                j = blq - 1;
-                found = true;
-                break;
-            }
-        }
-        if (!found) return;
-    }
-    atomicOr(status, ST_INTERNAL);
-#undef MM
 }
 
 __global__ void __launch_bounds__(TRACE_WARPS * 32)
@@ -552,10 +123,17 @@ __global__ void __launch_bounds__(TRACE_WARPS * 32)
 
 cudaError_t launch_fill(const PairDev *pairs, const GroupItem *items, int nitems, const int4 *dw,
                         int *scratch, long long scratch_stride, int sw, unsigned int *qhead,
-                        int *status, int *abort_flag, int blocks, cudaStream_t st) {
+                        int *status, int *abort_flag, int blocks, cudaStream_t st,
+                        unsigned long long *counters) {
     size_t smem = (size_t)FILL_WARPS * 3 * sw * sizeof(int);
-    sankoff_fill_kernel<<<blocks, FILL_WARPS * 32, smem, st>>>(
-        pairs, items, nitems, dw, scratch, scratch_stride, sw, qhead, status, abort_flag);
+    if (counters)
+        sankoff_fill_kernel<true><<<blocks, FILL_WARPS * 32, smem, st>>>(
+            pairs, items, nitems, dw, scratch, scratch_stride, sw, qhead, status, abort_flag,
+            counters);
+    else
+        sankoff_fill_kernel<false><<<blocks, FILL_WARPS * 32, smem, st>>>(
+            pairs, items, nitems, dw, scratch, scratch_stride, sw, qhead, status, abort_flag,
+            counters);
     return cudaGetLastError();
 }
 
@@ -574,12 +152,21 @@ int trace_warps_per_block() { return TRACE_WARPS; }
 cudaError_t fill_occupancy(int sw, int *blocks_per_sm) {
     size_t smem = (size_t)FILL_WARPS * 3 * sw * sizeof(int);
     if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(sankoff_fill_kernel,
+        cudaError_t e = cudaFuncSetAttribute(sankoff_fill_kernel<false>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
+        e = cudaFuncSetAttribute(sankoff_fill_kernel<true>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
     }
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, sankoff_fill_kernel,
-                                                         FILL_WARPS * 32, smem);
+    int a = 0, b = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, sankoff_fill_kernel<false>,
+                                                                  FILL_WARPS * 32, smem);
+    if (e != cudaSuccess) return e;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, sankoff_fill_kernel<true>,
+                                                      FILL_WARPS * 32, smem);
+    *blocks_per_sm = a < b ? a : b;
+    return e;
 }
 
 cudaError_t trace_prepare(int sw) {

@@ -7,14 +7,11 @@ This is a thin mirror of the C entry points: ``Engine.align_pairs`` is
 import ctypes as C
 import os
 
-from .abi import (PairTables, ResultBuffers, lcg_align_opts, lcg_align_result,
-                  lcg_pair_tables, make_opts)
+from .abi import (ResultBuffers, lcg_align_opts, lcg_align_result, lcg_pair_tables,
+                  lcg_work_counts, make_opts)
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_build", "liblocarna_gb300.so")
-
-EXPORTS = ("lcg_last_error", "lcg_abi_version", "lcg_engine_create", "lcg_engine_destroy",
-           "lcg_align_pairs", "lcg_engine_last_stats")
 
 _lib = None
 
@@ -44,6 +41,16 @@ def load_library(path=LIB_PATH):
     lib.lcg_align_pairs.restype = C.c_int32
     lib.lcg_engine_last_stats.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int64)]
     lib.lcg_engine_last_stats.restype = C.c_int32
+    lib.lcg_engine_last_timing.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    lib.lcg_engine_last_timing.restype = C.c_int32
+    lib.lcg_engine_last_transfer.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
+    lib.lcg_engine_last_transfer.restype = C.c_int32
+    lib.lcg_engine_set_counting.argtypes = [C.c_void_p, C.c_int32]
+    lib.lcg_engine_set_counting.restype = C.c_int32
+    lib.lcg_engine_last_work.argtypes = [C.c_void_p, C.POINTER(lcg_work_counts)]
+    lib.lcg_engine_last_work.restype = C.c_int32
+    lib.lcg_measure_int_peak.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_double)]
+    lib.lcg_measure_int_peak.restype = C.c_int32
     _lib = lib
     return lib
 
@@ -73,23 +80,61 @@ class Engine:
         except Exception:
             pass
 
-    def align_pairs(self, tables, opts=None, **kw):
-        """Align a list of PairTables; returns a list of AlignResult."""
+    def prepare_call(self, tables, opts=None, **kw):
+        """Build the C argument arrays once (see run_call / decode_call)."""
         if opts is None:
             opts = make_opts(**kw)
         n = len(tables)
         arr = (lcg_pair_tables * n)(*[t.to_c() for t in tables])
         bufs = [ResultBuffers(t.len_a, t.len_b) for t in tables]
         res = (lcg_align_result * n)(*[b.c for b in bufs])
+        return (arr, n, opts, res, bufs, tables)
+
+    def run_call(self, call):
+        """One lcg_align_pairs call on prepared arguments (the timed unit)."""
+        arr, n, opts, res, _, _ = call
         _check(self.lib, self.lib.lcg_align_pairs(self.h, arr, n, C.byref(opts), res))
+
+    @staticmethod
+    def decode_call(call):
+        _, _, _, res, bufs, _ = call
         out = []
         for k, b in enumerate(bufs):
             b.c = res[k]
             out.append(b.decode())
         return out
 
+    def align_pairs(self, tables, opts=None, **kw):
+        """Align a list of PairTables; returns a list of AlignResult."""
+        call = self.prepare_call(tables, opts, **kw)
+        self.run_call(call)
+        return self.decode_call(call)
+
     def last_stats(self):
         ms = C.c_double()
         nl = C.c_int64()
         _check(self.lib, self.lib.lcg_engine_last_stats(self.h, C.byref(ms), C.byref(nl)))
         return ms.value, nl.value
+
+    def last_timing(self):
+        a, b = C.c_double(), C.c_double()
+        _check(self.lib, self.lib.lcg_engine_last_timing(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def last_transfer(self):
+        a, b = C.c_int64(), C.c_int64()
+        _check(self.lib, self.lib.lcg_engine_last_transfer(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def set_counting(self, on):
+        _check(self.lib, self.lib.lcg_engine_set_counting(self.h, int(bool(on))))
+
+    def last_work(self):
+        w = lcg_work_counts()
+        _check(self.lib, self.lib.lcg_engine_last_work(self.h, C.byref(w)))
+        return dict(groups=w.groups, cells=w.cells, visits=w.arc_terms, arc_terms=w.valid_arc_terms)
+
+    def int_peak_gops(self, dpx=False):
+        g = C.c_double()
+        _check(self.lib, self.lib.lcg_measure_int_peak(self.h, int(bool(dpx)), C.byref(g)))
+        return g.value

@@ -87,6 +87,9 @@ static int cmp_left_desc(const void *x, const void *y) {
     return g_sort_arcs[2 * b] - g_sort_arcs[2 * a];
 }
 
+/* right adjacency lists (basepairs.cc:110-122, 212-220): per right end, the
+ * arcs sorted by left end descending, followed by a sentinel with left end 0;
+ * stored as (arc index, left end) pairs */
 static void build_radj(const int32_t *arcs, int narcs, int len, int **start, int **lst) {
     int *cntv = calloc(len + 2, sizeof(int));
     for (int k = 0; k < narcs; ++k) cntv[arcR(arcs, k)]++;
@@ -94,15 +97,22 @@ static void build_radj(const int32_t *arcs, int narcs, int len, int **start, int
     int acc = 0;
     for (int p = 0; p <= len; ++p) { (*start)[p] = acc; acc += cntv[p] + 1; }
     (*start)[len + 1] = acc;
-    *lst = malloc((acc > 0 ? acc : 1) * sizeof(int));
+    int *tmp = malloc((acc > 0 ? acc : 1) * sizeof(int));
     int *fill = calloc(len + 2, sizeof(int));
-    for (int k = 0; k < narcs; ++k) { int r = arcR(arcs, k); (*lst)[(*start)[r] + fill[r]++] = k; }
+    for (int k = 0; k < narcs; ++k) { int r = arcR(arcs, k); tmp[(*start)[r] + fill[r]++] = k; }
     g_sort_arcs = (int *)arcs;
+    *lst = malloc(2 * (acc > 0 ? acc : 1) * sizeof(int));
     for (int p = 0; p <= len; ++p) {
-        qsort(*lst + (*start)[p], cntv[p], sizeof(int), cmp_left_desc);
-        (*lst)[(*start)[p] + cntv[p]] = -1; /* sentinel, left end 0 */
+        qsort(tmp + (*start)[p], cntv[p], sizeof(int), cmp_left_desc);
+        for (int q = 0; q < cntv[p]; ++q) {
+            int k = tmp[(*start)[p] + q];
+            (*lst)[2 * ((*start)[p] + q)] = k;
+            (*lst)[2 * ((*start)[p] + q) + 1] = arcL(arcs, k);
+        }
+        (*lst)[2 * ((*start)[p] + cntv[p])] = -1;
+        (*lst)[2 * ((*start)[p] + cntv[p]) + 1] = 0;
     }
-    free(cntv); free(fill);
+    free(tmp); free(cntv); free(fill);
 }
 
 static const Ctx *g_sort_ctx;
@@ -172,17 +182,22 @@ static sc_t align_noex(Ctx *c, int state, int al, int bl, int i, int j) {
         c->F[state] = NEG_INF;
     }
     if (a_match(c, i, j)) {
-        const int *la = c->radjA + c->radjA_start[i];
-        const int *lb0 = c->radjB + c->radjB_start[j];
-        for (; *la >= 0 && arcL(c->t->arcs_a, *la) > al; ++la) {
-            int aL = arcL(c->t->arcs_a, *la);
-            for (const int *lb = lb0; *lb >= 0 && arcL(c->t->arcs_b, *lb) > bl; ++lb) {
-                sc_t d = DD(c, *la, *lb);
+        /* adjacency entries carry (arc index, left end); the sentinel has left end 0 */
+        const int *la = c->radjA + 2 * c->radjA_start[i];
+        const int *lb0 = c->radjB + 2 * c->radjB_start[j];
+        const int nb = c->t->num_arcs_b;
+        const size_t mp = (size_t)c->m + 1;
+        const sc_t *Ms = c->M[state];
+        for (; la[1] > al; la += 2) {
+            const sc_t *Drow = c->D + (size_t)la[0] * nb;
+            const sc_t *Mrow = Ms + (size_t)(la[1] - 1) * mp - 1;
+            for (const int *lb = lb0; lb[1] > bl; lb += 2) {
+                sc_t d = Drow[lb[0]];
                 if (c->cnt) {
                     c->cnt->arc_terms++;
                     if (d != NEG_INF) c->cnt->valid_arc_terms++;
                 }
-                sc_t ns = MM(c, state, aL - 1, arcL(c->t->arcs_b, *lb) - 1) + d;
+                sc_t ns = Mrow[lb[1]] + d;
                 if (ns <= max_score) continue;
                 max_score = ns;
             }

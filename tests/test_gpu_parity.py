@@ -6,7 +6,7 @@ from checks import assert_matches_golden, assert_same_result
 from golden_io import Golden, golden_names
 from oracle_ffi import oracle_align
 
-GPU_CASES = [n for n in golden_names() if "structlocal" not in n]
+GPU_CASES = golden_names()
 
 
 @pytest.mark.gpu
