@@ -21,6 +21,9 @@ ORACLE = os.path.join(ROOT, "oracle")
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 
+# tuning defines for the CUDA sources, e.g. LCG_NVCC_DEFS="-DLCG_FILL_WARPS=4"
+EXTRA_DEFS = os.environ.get("LCG_NVCC_DEFS", "").split()
+
 CUDA_SOURCES = ["engine.cu", "sankoff_kernels.cu", "sankoff_sl_kernels.cu", "microbench.cu"]
 HOST_SOURCES = ["host_prep.cpp"]  # C++ host-only translation units
 
@@ -51,7 +54,7 @@ def build_engine(verbose=False, force=False):
         objs.append(o)
         if force or _newer(o, [s] + headers):
             jobs.append([NVCC, GENCODE, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
-                         "-Xptxas", "-v" if verbose else "-O3", "-c", s, "-o", o])
+                         "-Xptxas", "-v" if verbose else "-O3"] + EXTRA_DEFS + ["-c", s, "-o", o])
     for src in HOST_SOURCES:
         s = os.path.join(CSRC, src)
         o = os.path.join(OUT, src + ".o")
@@ -73,11 +76,13 @@ def build_engine(verbose=False, force=False):
 def build_oracle():
     out = os.path.join(ORACLE, "_build")
     os.makedirs(out, exist_ok=True)
-    lib = os.path.join(out, "liboracle.so")
-    srcs = [os.path.join(ORACLE, "sankoff_oracle.c")]
-    if _newer(lib, srcs + [os.path.join(ROOT, "include", "locarna_gb300.h")]):
-        _run(["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-ffp-contract=off"] + srcs + ["-o", lib])
-    return lib
+    hdr = os.path.join(ROOT, "include", "locarna_gb300.h")
+    for src, name in (("sankoff_oracle.c", "liboracle.so"), ("pf_oracle.c", "libpforacle.so")):
+        lib = os.path.join(out, name)
+        s = os.path.join(ORACLE, src)
+        if _newer(lib, [s, hdr]):
+            _run(["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-ffp-contract=off", s, "-o", lib, "-lm"])
+    return os.path.join(out, "liboracle.so")
 
 
 def build_reference_oracle():

@@ -61,6 +61,8 @@ struct Prep {
     int flags = 0, fe = 0;
     int bandcells = 0;
     std::vector<int> min_col, max_col, bandoff;  // n+2
+    std::vector<int4> rowinfo;                   // n+2
+    int maxband = 0;
     std::vector<int> cre_start;                  // bandcells+1
     std::vector<int> cre;                        // 2 per entry
     std::vector<int> am_ends;                    // 4 per am
@@ -123,6 +125,11 @@ lcg_status prep_pair(const lcg_pair_tables &t, const lcg_align_opts &o, Prep &p)
     p.min_col[n + 1] = m + 1;
     p.max_col[n + 1] = m;
     p.bandoff[n + 1] = (int)cells;
+    p.rowinfo.resize(n + 2);
+    for (int i = 0; i <= n + 1; ++i) {
+        p.rowinfo[i] = make_int4(p.min_col[i], p.max_col[i], i <= n ? t.gap_a[i] : 0, p.bandoff[i]);
+        if (i <= n) p.maxband = std::max(p.maxband, p.max_col[i] - p.min_col[i] + 1);
+    }
     if (cells > (1ll << 30)) return bad(LCG_ERR_UNSUPPORTED, "band too large");
     p.bandcells = (int)cells;
     if (!o.sequ_local && !(p.fe & (LCG_FREE_RIGHT_1 | LCG_FREE_RIGHT_2)) && p.max_col[n] != m)
@@ -233,11 +240,16 @@ lcg_status prep_pair(const lcg_pair_tables &t, const lcg_align_opts &o, Prep &p)
                 }
             }
             g.dw_count = (int)p.dw.size() - g.dw_start;
-            p.groups.push_back(g);
+            int wmax = 1;
             for (int i = al + 1; i < max_ar; ++i) {
                 int lo = std::max(bl + 1, p.min_col[i]), hi = std::min(max_br - 1, p.max_col[i]);
-                if (hi >= lo) p.cells += hi - lo + 1;
+                if (hi >= lo) {
+                    p.cells += hi - lo + 1;
+                    wmax = std::max(wmax, hi - lo + 1);
+                }
             }
+            g.cpl = std::min(4, (wmax + 31) / 32);
+            p.groups.push_back(g);
             p.rows_max = std::max(p.rows_max, max_ar - al);
             p.width_max = std::max(p.width_max, max_br - bl + 1);
         }
@@ -250,8 +262,14 @@ lcg_status prep_pair(const lcg_pair_tables &t, const lcg_align_opts &o, Prep &p)
     top.bl = 0;
     top.br = m + 1;
     top.top = 1;
+    int twmax = 1;
+    for (int i = 1; i <= n; ++i) {
+        int w = std::min(m, p.max_col[i]) - std::max(1, p.min_col[i]) + 1;
+        p.cells += std::max(w, 0);
+        twmax = std::max(twmax, w);
+    }
+    top.cpl = std::min(4, (twmax + 31) / 32);
     p.groups.push_back(top);
-    for (int i = 1; i <= n; ++i) p.cells += std::min(m, p.max_col[i]) - std::max(1, p.min_col[i]) + 1;
     p.token_cap = 2 * (n + m) + 3 * std::min(n, m) + 16;
     p.tq_cap = std::min(n, m) / 2 + 2;
     return LCG_OK;
@@ -440,7 +458,7 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
         rows_max = std::max(rows_max, p.rows_max + 1);
     }
     struct Off {
-        size_t sigma, gapA, gapB, minc, maxc, bandoff, anc, cre_start, cre, am_ends, am_score, D,
+        size_t sigma, gapA, gapB, minc, maxc, bandoff, rowinfo, anc, cre_start, cre, am_ends, am_score, D,
             topM, res, tok, tq, segs;
     };
     std::vector<Off> off(npairs);
@@ -469,6 +487,7 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
         o.minc = take(up, 4ull * (p.n + 2));
         o.maxc = take(up, 4ull * (p.n + 2));
         o.bandoff = take(up, 4ull * (p.n + 2));
+        o.rowinfo = take(up, 16ull * (p.n + 2));
         o.anc = t.match_lo ? take(up, 4ull * (2 * (p.n + 1) + 2 * (p.n + 1) + 2 * (p.m + 1))) : 0;
         o.cre_start = take(up, 4ull * (p.bandcells + 1));
         o.cre = take(up, 4ull * std::max<size_t>(p.cre.size(), 2));
@@ -554,6 +573,7 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
         std::memcpy(H + o.minc, p.min_col.data(), 4ull * (p.n + 2));
         std::memcpy(H + o.maxc, p.max_col.data(), 4ull * (p.n + 2));
         std::memcpy(H + o.bandoff, p.bandoff.data(), 4ull * (p.n + 2));
+        std::memcpy(H + o.rowinfo, p.rowinfo.data(), 16ull * (p.n + 2));
         if (t.match_lo) {
             int *a = (int *)(H + o.anc);
             std::memcpy(a, t.match_lo, 4ull * (p.n + 1));
@@ -590,6 +610,8 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
         d.min_col = (const int *)(Dv + o.minc);
         d.max_col = (const int *)(Dv + o.maxc);
         d.bandoff = (const int *)(Dv + o.bandoff);
+        d.rowinfo = (const int4 *)(Dv + o.rowinfo);
+        d.maxband = p.maxband;
         if (t.match_lo) {
             const int *a = (const int *)(Dv + o.anc);
             d.match_lo = a;

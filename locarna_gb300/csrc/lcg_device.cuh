@@ -46,12 +46,14 @@ struct PairDev {
     int la, lb, ra, rb;  // leftmost / rightmost anchor
     int num_am;
     int bandcells;
+    int maxband;          // widest band row (columns)
     const int *sigma;     // (n+1)*(m+1)
     const int *gapA;      // n+1
     const int *gapB;      // m+1
     const int *min_col;   // n+2 (entry n+1 = m+1 sentinel)
     const int *max_col;   // n+2
     const int *bandoff;   // n+2: band cell offset of row i
+    const int4 *rowinfo;  // n+2: (min_col, max_col, gapA, bandoff) of row i
     const int *match_lo, *match_hi, *del_lo, *del_hi, *ins_lo, *ins_hi;
     const int *cre_start; // bandcells+1: arc matches with right ends at a band cell
     const int2 *cre;      // (am index, (a.l<<16)|b.l), lex-greater-left-ends order
@@ -76,6 +78,7 @@ struct GroupItem {
     int al, ar, bl, br;
     int dw_start, dw_count;  // D writes: int4 (am, ar-1, br-1, score), ar ascending
     int top;                 // 1 for the top-level item
+    int cpl;                 // columns per lane: ceil(widest band row of the group / 32), <= 4
 };
 
 // anchor helpers: reference AnchorConstraints::allowed_match/del/ins

@@ -11,7 +11,13 @@
 namespace lcg {
 
 
-constexpr int FILL_WARPS = 8;   // warps per block of the fill kernel
+// dynamic shared memory of every kernel in this family
+extern __shared__ int lcg_smem[];
+
+#ifndef LCG_FILL_WARPS
+#define LCG_FILL_WARPS 8
+#endif
+constexpr int FILL_WARPS = LCG_FILL_WARPS;  // warps per block of the fill kernel
 constexpr int TRACE_WARPS = 4;  // warps per block of the trace kernel
 constexpr long long SPIN_LIMIT = 1ll << 22;  // ~ seconds of polling, then ST_TIMEOUT
 
@@ -51,29 +57,52 @@ __device__ __forceinline__ int wait_D(int *D, int k, int *status, volatile int *
 // init_state (aligner.cc:264-368) + the row sweep of align_in_arcmatch
 // (aligner.cc:424-437) with align_noex per cell. M of the rectangle is
 // written to Mg (row r = i-al, column c = j-bl, row pitch `pitch`).
-// prev/cur/E are per-warp shared-memory rows indexed by c.
-template <bool TOP, bool WAIT, bool DWRITE, bool COUNT = false>
-__device__ void run_group(const PairDev &P, int al, int ar, int bl, int br, int *__restrict__ Mg,
-                          int pitch, int *prev, int *cur, int *E, const int4 *__restrict__ dw,
-                          int ndw, bool globalA, bool globalB, bool local_top, int *status,
-                          volatile int *abort_flag, TopOut *tout,
-                          unsigned long long *counters = nullptr) {
+// Shared-memory rows (offsets into lcg_smem) hold the previous and current M
+// row, the E vector and the group's gap costs gapB, indexed by c = j-bl.
+//
+// Lanes own consecutive columns (lane-stride chunks of 32, so every shared
+// and global row access is unit-stride). Per row, the band metadata is read
+// as one int4 loaded a row ahead, and the sigma values and candidate-list
+// bounds of up to NCH chunks are loaded together before any cell of the row
+// is computed. Each cell walks its candidate list (sorted by a.l descending)
+// until the first a.l <= al, one entry ahead.
+template <int NCH, bool TOP, bool WAIT, bool DWRITE, bool COUNT>
+__device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, int *__restrict__ Mg,
+                            int pitch, int prev_o, int cur_o, int E_o, int gB_o,
+                            const int4 *__restrict__ dw, int ndw, bool globalA, bool globalB,
+                            bool local_top, int *status, volatile int *abort_flag, TopOut *tout,
+                            unsigned long long *counters) {
     unsigned long long n_terms = 0, n_visits = 0;
     const int lane = threadIdx.x & 31;
+    const int4 *__restrict__ rowinfo = P.rowinfo;
+    const int *__restrict__ sigma = P.sigma;
+    const int *__restrict__ cre_start = P.cre_start;
+    const int2 *__restrict__ cre = P.cre;
+    int *const Dp = P.D;
+    const bool anch = (P.flags & PF_ANCHORS) != 0;
     const int m1 = P.m + 1;
     const int go = P.go;
+    const int gop = max(go, 0);
     const int W = br - bl;
-    for (int c = lane; c < W; c += 32) E[c] = NEG;
+    int *const E = lcg_smem + E_o;
+    int *const gBs = lcg_smem + gB_o;
+    int pv = prev_o, cu = cur_o;  // shared-memory offsets of the previous / current row
+#define PREV(c) lcg_smem[pv + (c)]
+#define CUR(c) lcg_smem[cu + (c)]
+    for (int c = lane; c < W; c += 32) {
+        E[c] = NEG;
+        gBs[c] = P.gapB[bl + c];
+    }
 
     // ---- row al: M(al,bl)=0, M(al,j) = prefix of gap costs, -inf once blocked
-    const int L0 = min(br, P.max_col[al] + 1);
+    const int L0 = min(br, rowinfo[al].y + 1);
     {
         int carry = globalB ? go : 0;
         bool blocked_carry = false;
         for (int base = bl + 1; base < L0; base += 32) {
             int j = base + lane;
             bool act = j < L0;
-            bool blk = act && !a_ins(P, al, j);
+            bool blk = act && anch && !a_ins(P, al, j);
             int s = (act && globalB) ? P.gapB[j] : 0;
             unsigned bm = __ballot_sync(0xffffffffu, blk);
 #pragma unroll
@@ -84,20 +113,20 @@ __device__ void run_group(const PairDev &P, int al, int ar, int bl, int br, int 
             bool anyblk = blocked_carry || (bm & (0xffffffffu >> (31 - lane)));
             int val = anyblk ? NEG : carry + s;
             if (act) {
-                prev[j - bl] = val;
+                PREV(j - bl) = val;
                 Mg[j - bl] = val;
             }
             carry += __shfl_sync(0xffffffffu, s, 31);
             blocked_carry = blocked_carry || bm != 0;
         }
         if (lane == 0) {
-            prev[0] = 0;
+            PREV(0) = 0;
             Mg[0] = 0;
         }
         // cells above the band of row al+1 (aligner.cc:361-367)
         if (al + 1 < ar) {
-            int L1 = min(br, P.max_col[al + 1] + 1);
-            for (int j = L0 + lane; j < L1; j += 32) prev[j - bl] = NEG;
+            int L1 = min(br, rowinfo[al + 1].y + 1);
+            for (int j = L0 + lane; j < L1; j += 32) PREV(j - bl) = NEG;
         }
     }
     __syncwarp();
@@ -107,17 +136,35 @@ __device__ void run_group(const PairDev &P, int al, int ar, int bl, int br, int 
     int dwp = 0;
     int best = TOP ? 0 : NEG, bi = 0, bj = 0;  // sequence-local argmax (aligner.cc:865-875)
     const int la = P.la, lb = P.lb, ra = P.ra, rb = P.rb;
+    int4 rnxt = rowinfo[min(al + 1, P.n + 1)];
 
     for (int i = al + 1; i < ar; ++i) {
-        const int minc = P.min_col[i];
-        const int maxc = P.max_col[i];
+        const int4 rcur = rnxt;
+        rnxt = rowinfo[min(i + 1, P.n + 1)];
+        const int minc = rcur.x;
+        const int gAi = rcur.z;
         const int lo = max(bl + 1, minc);
-        const int hi = min(br - 1, maxc);
-        const int gAi = P.gapA[i];
+        const int hi = min(br - 1, rcur.y);
+        const int *srow = sigma + (size_t)i * m1;
+        const int cb = rcur.w - minc;  // band cell index of (i,j) = cb + j
+        // loads of the first NCH chunks of the row, issued before any use
+        int sgv[NCH], q0v[NCH], q1v[NCH];
+#pragma unroll
+        for (int k = 0; k < NCH; ++k) {
+            const int j = lo + 32 * k + lane;
+            sgv[k] = 0;
+            q0v[k] = 0;
+            q1v[k] = 0;
+            if (j <= hi) {
+                sgv[k] = srow[j];
+                q0v[k] = cre_start[cb + j];
+                q1v[k] = cre_start[cb + j + 1];
+            }
+        }
         int B;  // M(i, lo-1)
         if (minc <= bl) {
             if (!colblocked) {
-                if (!a_del(P, i, bl)) colblocked = true;
+                if (anch && !a_del(P, i, bl)) colblocked = true;
                 else if (globalA) colval += gAi;
             }
             B = colblocked ? NEG : colval;
@@ -125,48 +172,68 @@ __device__ void run_group(const PairDev &P, int al, int ar, int bl, int br, int 
         } else {
             B = NEG;
         }
-        if (lane == 0 && lo - 1 - bl < W) cur[lo - 1 - bl] = B;
-        const int *sig_row = P.sigma + (size_t)i * m1;
-        int *Mrow = Mg + (size_t)(i - al) * pitch - bl;
-        const int cell0 = P.bandoff[i] - minc;
+        if (lane == 0 && lo - 1 - bl < W) CUR(lo - 1 - bl) = B;
+        int *Mrow = Mg + (i - al) * pitch - bl;
         int Fc = NEG, Xc = B;
-        for (int base = lo; base <= hi; base += 32) {
+        int k = 0;
+        for (int base = lo; base <= hi; base += 32, ++k) {
             const int j = base + lane;
             const bool act = j <= hi;
             const int c = j - bl;
+            int sgx = 0, q = 0, q1 = 0;
+#pragma unroll
+            for (int kk = 0; kk < NCH; ++kk) {
+                if (k == kk) {
+                    sgx = sgv[kk];
+                    q = q0v[kk];
+                    q1 = q1v[kk];
+                }
+            }
+            if (k >= NCH && act) {
+                sgx = srow[j];
+                q = cre_start[cb + j];
+                q1 = cre_start[cb + j + 1];
+            }
             int X = NEG;
             if (act) {
-                const bool mok = a_match(P, i, j);
-                int d = mok ? prev[c - 1] + sig_row[j] : NEG;
-                int e = a_del(P, i, j) ? max(E[c] + gAi, prev[c] + gAi + go) : NEG;
+                const bool mok = !anch || a_match(P, i, j);
+                const bool dok = !anch || a_del(P, i, j);
+                int d = mok ? PREV(c - 1) + sgx : NEG;
+                int e = dok ? max(E[c] + gAi, PREV(c) + gAi + go) : NEG;
                 e = norm(e);
                 E[c] = e;
                 X = max(d, e);
-                if (mok) {
-                    const int cell = cell0 + j;
-                    const int q1 = P.cre_start[cell + 1];
-                    for (int q = P.cre_start[cell]; q < q1; ++q) {
-                        const int2 ent = P.cre[q];
-                        const int alq = ent.y >> 16, blq = ent.y & 0xffff;
-                        if (COUNT) ++n_visits;
-                        if (alq <= al) break;
-                        if (blq <= bl) continue;
-                        if (COUNT) ++n_terms;
-                        const int dv = WAIT ? wait_D(P.D, ent.x, status, abort_flag) : P.D[ent.x];
-                        const int mv = Mg[(size_t)(alq - 1 - al) * pitch + (blq - 1 - bl)];
-                        X = max(X, mv + dv);
-                    }
-                }
-                if (TOP && local_top && i < la && j < lb) X = max(X, 0);
+                if (!mok) q1 = q;
+            } else {
+                q1 = q;
             }
+            // arc-match terms: candidates (a,b) with right ends (i,j), sorted
+            // by a.l descending; valid while a.l > al, and when b.l > bl
+            int2 en = make_int2(0, 0);
+            if (q < q1) en = cre[q];
+            while (q < q1) {
+                const int2 cur_en = en;
+                if (q + 1 < q1) en = cre[q + 1];
+                ++q;
+                const int alq = cur_en.y >> 16, blq = cur_en.y & 0xffff;
+                if (COUNT) ++n_visits;
+                if (alq <= al) break;
+                if (blq <= bl) continue;
+                if (COUNT) ++n_terms;
+                int dv = WAIT ? ld_volatile(Dp + cur_en.x) : Dp[cur_en.x];
+                const int mv = Mg[(alq - 1 - al) * pitch + (blq - 1 - bl)];
+                if (WAIT && dv == NOT_READY) dv = wait_D(Dp, cur_en.x, status, abort_flag);
+                X = max(X, mv + dv);
+            }
+            if (TOP && local_top && act && i < la && j < lb) X = max(X, 0);
             // horizontal gaps: max-plus scan of F(j) = max(F(j-1)+a_j, b_j)
             int Xp = __shfl_up_sync(0xffffffffu, X, 1);
             if (lane == 0) Xp = Xc;
             int a = 0, b = NEG;
             if (act) {
-                if (a_ins(P, i, j)) {
-                    const int gb = P.gapB[j];
-                    a = gb + max(go, 0);
+                if (!anch || a_ins(P, i, j)) {
+                    const int gb = gBs[c];
+                    a = gb + gop;
                     b = addc(Xp, gb + go);
                 } else {
                     a = NEG;
@@ -184,7 +251,7 @@ __device__ void run_group(const PairDev &P, int al, int ar, int bl, int br, int 
             const int F = max(addc(Fc, a), b);
             const int M = norm(max(X, F));
             if (act) {
-                cur[c] = M;
+                CUR(c) = M;
                 Mrow[j] = M;
                 if (TOP && local_top && i >= ra && j >= rb && M > best) {
                     best = M;
@@ -203,22 +270,24 @@ __device__ void run_group(const PairDev &P, int al, int ar, int bl, int br, int 
                 int4 e = make_int4(0, -1, 0, 0);
                 if (q < ndw) e = dw[q];
                 const bool mine = q < ndw && e.y == i;
-                if (mine) st_volatile(P.D + e.x, norm(cur[e.z - bl] + e.w));
+                if (mine) st_volatile(Dp + e.x, norm(CUR(e.z - bl) + e.w));
                 const int cnt = __popc(__ballot_sync(0xffffffffu, mine));
                 dwp += cnt;
                 if (cnt < 32) break;
             }
         }
         if (i + 1 < ar) {
-            const int Ln = min(br, P.max_col[i + 1] + 1);
-            for (int j = max(hi + 1, bl + 1) + lane; j < Ln; j += 32) cur[j - bl] = NEG;
+            const int Ln = min(br, rnxt.y + 1);
+            for (int j = max(hi + 1, bl + 1) + lane; j < Ln; j += 32) CUR(j - bl) = NEG;
         }
         __syncwarp();
-        int *t = prev;
-        prev = cur;
-        cur = t;
+        const int tp = pv;
+        pv = cu;
+        cu = tp;
         if (WAIT && *abort_flag) return;
     }
+#undef PREV
+#undef CUR
     if (TOP) {
         tout->best = best;
         tout->bi = bi;
@@ -235,6 +304,20 @@ __device__ void run_group(const PairDev &P, int al, int ar, int bl, int br, int 
             atomicAdd(counters + 1, n_visits);
         }
     }
+}
+
+// All groups use the same routine; `cpl` (columns per lane in an earlier
+// design) is ignored.
+template <bool TOP, bool WAIT, bool DWRITE, bool COUNT = false>
+__device__ __forceinline__ void run_group(const PairDev &P, int cpl, int al, int ar, int bl, int br,
+                                          int *__restrict__ Mg, int pitch, int prev, int cur,
+                                          int E, int gBs, const int4 *__restrict__ dw, int ndw,
+                                          bool globalA, bool globalB, bool local_top, int *status,
+                                          volatile int *abort_flag, TopOut *tout,
+                                          unsigned long long *counters = nullptr) {
+    run_group_c<4, TOP, WAIT, DWRITE, COUNT>(P, al, ar, bl, br, Mg, pitch, prev, cur, E, gBs, dw, ndw,
+                                             globalA, globalB, local_top, status, abort_flag, tout,
+                                             counters);
 }
 
 static __device__ __forceinline__ void warp_argmax(int &v, int &k1, int &k2) {
@@ -256,16 +339,17 @@ static __device__ __forceinline__ void warp_argmax(int &v, int &k1, int &k2) {
 // top level + final argmax: align_top_level_free_endgaps (aligner.cc:736-819)
 // and align_top_level_locally (aligner.cc:823-880)
 template <bool COUNT>
-__device__ __noinline__ void run_top(const PairDev &P, int *prev, int *cur, int *E, int *status,
-                        volatile int *abort_flag, unsigned long long *counters) {
+__device__ __forceinline__ void run_top(const PairDev &P, int cpl, int prev, int cur, int E, int gBs,
+                                     int *status, volatile int *abort_flag,
+                                     unsigned long long *counters) {
     const int lane = threadIdx.x & 31;
     const int n = P.n, m = P.m, m1 = m + 1;
     const bool local = P.flags & PF_SEQU_LOCAL;
     const int fe = P.free_endgaps;
     TopOut to;
     if (local) {
-        run_group<true, true, false, COUNT>(P, 0, n + 1, 0, m + 1, P.topM, m1, prev, cur, E,
-                                            nullptr, 0, false, false, true, status, abort_flag,
+        run_group<true, true, false, COUNT>(P, cpl, 0, n + 1, 0, m + 1, P.topM, m1, prev, cur, E,
+                                            gBs, nullptr, 0, false, false, true, status, abort_flag,
                                             &to, counters);
         int v = to.best, i = to.bi, j = to.bj;
         if (v <= 0) {
@@ -286,9 +370,9 @@ __device__ __noinline__ void run_top(const PairDev &P, int *prev, int *cur, int 
         }
         return;
     }
-    run_group<true, true, false, COUNT>(P, 0, n + 1, 0, m + 1, P.topM, m1, prev, cur, E, nullptr,
-                                        0, !(fe & 4), !(fe & 1), false, status, abort_flag, &to,
-                                        counters);
+    run_group<true, true, false, COUNT>(P, cpl, 0, n + 1, 0, m + 1, P.topM, m1, prev, cur, E, gBs,
+                                        nullptr, 0, !(fe & 4), !(fe & 1), false, status, abort_flag,
+                                        &to, counters);
     __syncwarp();
     if (!(fe & (2 | 8))) {
         if (lane == 0) {

@@ -317,7 +317,9 @@ __global__ void __launch_bounds__(SL_FILL_WARPS * 32)
         const GroupItem it = items[idx];
         const PairDev &P = pairs[it.pair];
         if (it.top) {
-            run_top<false>(P, sm, sm + sw, sm + 2 * sw, status, abort_flag, nullptr);
+            const int base = (int)(sm - smem);
+            run_top<false>(P, it.cpl, base, base + sw, base + 2 * sw, base + 3 * sw, status, abort_flag,
+                           nullptr);
         } else {
             run_group_sl<true, true, 4>(P, it.al, it.ar, it.bl, it.br, Mg, scratch_stride, sw, sm, sw,
                                         dw + it.dw_start, it.dw_count, status, abort_flag);

@@ -37,5 +37,6 @@ $CXX $FLAGS $INC "$SRC/ribosum2cc.cc" "$OUT/obj/ribosum.o" "$OUT/obj/aux.o" -o "
 $CXX $FLAGS $INC "$SRC/locarna.cc" "$OUT"/obj/*.o -lquadmath -o "$OUT/locarna" &
 $CXX $FLAGS $INC "$SRC/locarna_p.cc" "$OUT"/obj/*.o -lquadmath -o "$OUT/locarna_p" &
 $CXX $FLAGS $INC "$HERE/ref_harness.cc" "$OUT"/obj/*.o -lquadmath -o "$OUT/ref_harness" &
+$CXX $FLAGS $INC "$HERE/ref_harness_p.cc" "$OUT"/obj/*.o -lquadmath -o "$OUT/ref_harness_p" &
 wait
 echo "build_ref: ok ($OUT)"

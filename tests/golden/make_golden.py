@@ -85,5 +85,75 @@ def main():
         print(name, "score", ref["score"], "am", ref["num_am"])
 
 
-if __name__ == "__main__":
+if __name__ == "__main__" and not os.environ.get("LCG_GOLDEN_PF"):
     main()
+
+
+# ---------------------------------------------------------------- LocARNA-P
+
+HARNESS_P = os.path.join(ROOT, "oracle", "_ref", "ref_harness_p")
+
+# name: (lenA, seedA, lenB, seedB, options)
+PF_CASES = {
+    "pf150": (150, 1, 150, 2, {}),
+    "pf200": (200, 5, 200, 6, {}),
+    "pf90_b": (90, 51, 110, 52, {}),
+}
+
+
+def parse_pf(txt):
+    lines = {}
+    for l in txt.splitlines():
+        k, _, v = l.partition(" ")
+        lines[k] = v
+    fake = txt + "\nscore 0\nedges 1:1\nstructA .\nstructB .\nalign_seconds 0\nanchor_match 1:1\n"
+    ref = parse_ref(fake)
+    am = []
+    for tok in lines["amprobs"].split():
+        a1, a2, b1, b2, p = tok.split(":")
+        am.append((int(a1), int(a2), int(b1), int(b2), float(p)))
+    bm = []
+    for tok in lines["bmprobs"].split():
+        i, j, p = tok.split(":")
+        bm.append((int(i), int(j), float(p)))
+    return ref, float(lines["Z"]), am, bm
+
+
+def make_pf_case(name, spec, workdir):
+    la, sa, lb, sb, opts = spec
+    ra, rb = make_rna(la, sa), make_rna(lb, sb)
+    pa, pb = os.path.join(workdir, name + "_A.pp"), os.path.join(workdir, name + "_B.pp")
+    with open(pa, "w") as f:
+        f.write(ra.to_pp())
+    with open(pb, "w") as f:
+        f.write(rb.to_pp())
+    args = [HARNESS_P, pa, pb, "min_am_prob=0"] + [f"{k}={v}" for k, v in opts.items()]
+    txt = subprocess.run(args, capture_output=True, text=True, check=True).stdout
+    ref, Z, am, bm = parse_pf(txt)
+    t = ref["tables"]
+    out = {
+        "pp_a": ra.to_pp(), "pp_b": rb.to_pp(), "opts": json.dumps(opts), "Z": Z,
+        "am": np.array([x[:4] for x in am], dtype=np.int32).reshape(-1, 4),
+        "am_p": np.array([x[4] for x in am], dtype=np.float64),
+        "bm": np.array([x[:2] for x in bm], dtype=np.int32).reshape(-1, 2),
+        "bm_p": np.array([x[2] for x in bm], dtype=np.float64),
+        "min_col": np.array(ref["min_col"], dtype=np.int32),
+        "max_col": np.array(ref["max_col"], dtype=np.int32),
+        "seq_a": ref["seq_a"], "seq_b": ref["seq_b"],
+        "indel_opening": t.indel_opening, "exclusion": t.exclusion,
+        "gap_a": t.gap_a, "gap_b": t.gap_b, "arcs_a": t.arcs_a, "arcs_b": t.arcs_b,
+        "am_arcs": t.am_arcs, "am_score": t.am_score, "sigma": t.sigma.astype(np.int16),
+    }
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    return Z, len(am)
+
+
+def main_pf():
+    work = os.path.join(ROOT, "_work", "golden_pp")
+    os.makedirs(work, exist_ok=True)
+    for name, spec in PF_CASES.items():
+        print(name, *make_pf_case(name, spec, work))
+
+
+if __name__ == "__main__" and os.environ.get("LCG_GOLDEN_PF"):
+    main_pf()

@@ -14,6 +14,10 @@ def golden_names():
     return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN_DIR, "*.npz")))
 
 
+def sankoff_golden_names():
+    return [n for n in golden_names() if not n.startswith("pf")]
+
+
 class Golden:
     def __init__(self, name):
         z = np.load(os.path.join(GOLDEN_DIR, name + ".npz"))
@@ -49,3 +53,39 @@ class Golden:
     def align_kwargs(self):
         return dict(struct_local=self.struct_local, sequ_local=self.sequ_local,
                     free_endgaps=self.free_endgaps)
+
+
+class GoldenPF:
+    """LocARNA-P golden case (made by make_golden.py with LCG_GOLDEN_PF=1)."""
+
+    def __init__(self, name):
+        z = np.load(os.path.join(GOLDEN_DIR, name + ".npz"))
+        self.name = name
+        self.pp_a, self.pp_b = str(z["pp_a"]), str(z["pp_b"])
+        self.seq_a, self.seq_b = str(z["seq_a"]), str(z["seq_b"])
+        self.Z = float(z["Z"])
+        self.am_ends = z["am"]
+        self.am_p = z["am_p"]
+        self.bm_ij = z["bm"]
+        self.bm_p = z["bm_p"]
+        self.min_col, self.max_col = z["min_col"], z["max_col"]
+        n, m = len(self.seq_a), len(self.seq_b)
+        self.tables = PairTables(
+            n, m, z["sigma"].astype(np.int32), z["gap_a"], z["gap_b"],
+            int(z["indel_opening"]), int(z["exclusion"]), z["arcs_a"], z["arcs_b"],
+            z["am_arcs"], z["am_score"], self.min_col, self.max_col,
+            seq_a=self.seq_a, seq_b=self.seq_b)
+
+    def am_by_ends(self):
+        return {tuple(int(v) for v in e): float(p) for e, p in zip(self.am_ends, self.am_p)}
+
+    def bm_dense(self):
+        n, m = len(self.seq_a), len(self.seq_b)
+        out = np.zeros((n + 1, m + 1))
+        for (i, j), p in zip(self.bm_ij, self.bm_p):
+            out[i, j] = p
+        return out
+
+
+def pf_golden_names():
+    return [n for n in golden_names() if n.startswith("pf")]

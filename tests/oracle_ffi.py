@@ -34,3 +34,35 @@ def oracle_align(tables, counts=False, **kw):
     if counts:
         return r, cnt
     return r
+
+
+_pflib = None
+
+
+def load_pf_oracle():
+    global _pflib
+    if _pflib is None:
+        from locarna_gb300.build import build_oracle
+        build_oracle()
+        lib = C.CDLL(os.path.join(ROOT, "oracle", "_build", "libpforacle.so"))
+        lib.lcg_oracle_pf.argtypes = [C.POINTER(lcg_pair_tables), C.c_double, C.c_double, C.c_double,
+                                      C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                      C.POINTER(C.c_double)]
+        lib.lcg_oracle_pf.restype = C.c_int
+        _pflib = lib
+    return _pflib
+
+
+def oracle_pf(tables, temperature=300.0, pf_scale=1.0, min_am_prob=0.0, include_am=False, probs=True):
+    """LocARNA-P oracle: returns (Z, am_prob per arc match, bm_prob (n+1)x(m+1))."""
+    import numpy as np
+    lib = load_pf_oracle()
+    ct = tables.to_c()
+    Z = C.c_double()
+    am = np.zeros(max(1, tables.num_arcmatches), dtype=np.float64)
+    bm = np.zeros((tables.len_a + 1) * (tables.len_b + 1), dtype=np.float64)
+    P = C.POINTER(C.c_double)
+    rc = lib.lcg_oracle_pf(C.byref(ct), temperature, pf_scale, min_am_prob, int(include_am), C.byref(Z),
+                           am.ctypes.data_as(P) if probs else None, bm.ctypes.data_as(P) if probs else None)
+    assert rc == 0
+    return Z.value, am[:tables.num_arcmatches], bm.reshape(tables.len_a + 1, tables.len_b + 1)

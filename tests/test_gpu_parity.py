@@ -3,7 +3,7 @@ golden results and against the oracle on the same tables."""
 import pytest
 
 from checks import assert_matches_golden, assert_same_result
-from golden_io import Golden, golden_names
+from golden_io import Golden, sankoff_golden_names as golden_names
 from oracle_ffi import oracle_align
 
 GPU_CASES = golden_names()

@@ -2,7 +2,7 @@
 import pytest
 
 from checks import assert_matches_golden
-from golden_io import Golden, golden_names
+from golden_io import Golden, sankoff_golden_names as golden_names
 from oracle_ffi import oracle_align
 
 CPU_CASES = [n for n in golden_names() if not n.startswith("c400")]

@@ -3,7 +3,7 @@ the sequence envelope) against the reference's own tables (CPU)."""
 import numpy as np
 import pytest
 
-from golden_io import Golden, golden_names
+from golden_io import Golden, sankoff_golden_names as golden_names
 
 _OPT_MAP = {"sequ_local": ("sequ_local", int), "free_endgaps": ("free_endgaps", str),
             "min_trace_prob": ("min_trace_probability", float), "indel_opening": ("indel_opening", int),
