@@ -181,6 +181,28 @@ lcg_status lcg_engine_last_work(lcg_engine eng, lcg_work_counts *out);
 lcg_status lcg_measure_int_peak(lcg_engine eng, int32_t dpx, double *gops);
 
 
+/* -------------------------------------------- allocation-free entry point
+ *
+ * No counterpart in the reference: an addition of this library for callers
+ * that must not allocate device memory while they run (work recorded into a
+ * CUDA graph, memory reserved up front by another framework, real-time loops
+ * where cudaMalloc / cudaFree would synchronise the device). It computes what
+ * lcg_align_pairs computes without traceback (the score and the end cell of
+ * one pair, plain mode) and takes every device byte from one fixed
+ * file-scope device array of LCG_STATIC_SCRATCH_BYTES held per GPU for the
+ * life of the process; it calls no cudaMalloc, cudaFree, cudaMallocHost or
+ * other allocating CUDA routine. Pairs whose data do not fit are rejected
+ * with LCG_ERR_RANGE. All calls share the array: calls whose GPU work
+ * overlaps race on it. The first call on a device looks the array's address
+ * up (cudaGetSymbolAddress); make it before any stream capture.
+ * opts->struct_local and opts->do_trace must be 0. stream is a cudaStream_t
+ * (NULL = default stream); the call returns when its results are on the host.
+ */
+#define LCG_STATIC_SCRATCH_BYTES (64u << 20)
+lcg_status lcg_align_score_static(const lcg_pair_tables *pair, const lcg_align_opts *opts,
+                                  int64_t *score, int32_t *max_i, int32_t *max_j,
+                                  void *stream);
+
 /* ------------------------------------------------------ host preparation
  *
  * Builds lcg_pair_tables from two PP 2.0 inputs the way the reference's

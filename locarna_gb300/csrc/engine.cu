@@ -16,6 +16,7 @@
 
 #include "../../include/locarna_gb300.h"
 #include "lcg_device.cuh"
+#include "engine_prep.hh"
 
 namespace lcg {
 cudaError_t launch_fill(const PairDev *, const GroupItem *, int, const int4 *, int *, long long,
@@ -33,6 +34,8 @@ cudaError_t trace_prepare(int sw);
 }  // namespace lcg
 
 using namespace lcg;
+using lcg_host::Prep;
+using lcg_host::prep_pair;
 
 static thread_local std::string g_last_error;
 
@@ -54,27 +57,7 @@ static lcg_status fail(lcg_status code, const std::string &msg) {
 
 // ------------------------------------------------------------------ per-pair prep
 
-namespace {
-
-struct Prep {
-    int n = 0, m = 0;
-    int flags = 0, fe = 0;
-    int bandcells = 0;
-    std::vector<int> min_col, max_col, bandoff;  // n+2
-    std::vector<int4> rowinfo;                   // n+2
-    int maxband = 0;
-    std::vector<int> cre_start;                  // bandcells+1
-    std::vector<int> cre;                        // 2 per entry
-    std::vector<int> am_ends;                    // 4 per am
-    std::vector<int> Dinit;                      // per am
-    std::vector<GroupItem> groups;               // pair field filled later
-    std::vector<int4> dw;                        // dw_start relative to this pair
-    int rows_max = 0, width_max = 0;             // over groups
-    int token_cap = 0, tq_cap = 0;
-    long long cells = 0;                         // M cells of all groups + top level
-    std::string err;
-    lcg_status code = LCG_OK;
-};
+namespace lcg_host {
 
 inline bool allowed_match(const lcg_pair_tables &t, int i, int j) {
     return !t.match_lo || (t.match_lo[i] <= j && j <= t.match_hi[i]);
@@ -274,6 +257,10 @@ lcg_status prep_pair(const lcg_pair_tables &t, const lcg_align_opts &o, Prep &p)
     p.tq_cap = std::min(n, m) / 2 + 2;
     return LCG_OK;
 }
+
+}  // namespace lcg_host
+
+namespace {
 
 // expand token segments into the reference's append order
 struct Assembler {

@@ -1,0 +1,40 @@
+// Per-pair host preparation shared by the entry points of engine.cu and
+// noalloc.cu: validation of the prepared tables and the derived index
+// structures the kernels read (band offsets, candidate lists by right-end
+// cell, left-end groups in dependency order, D-write lists).
+#pragma once
+#include <string>
+#include <vector>
+
+#include "../../include/locarna_gb300.h"
+#include "lcg_device.cuh"
+
+namespace lcg_host {
+
+struct Prep {
+    int n = 0, m = 0;
+    int flags = 0, fe = 0;
+    int bandcells = 0;
+    std::vector<int> min_col, max_col, bandoff;  // n+2
+    std::vector<int4> rowinfo;                   // n+2
+    int maxband = 0;
+    std::vector<int> cre_start;                  // bandcells+1
+    std::vector<int> cre;                        // 2 per entry
+    std::vector<int> am_ends;                    // 4 per am
+    std::vector<int> Dinit;                      // per am
+    std::vector<lcg::GroupItem> groups;          // pair field filled later
+    std::vector<int4> dw;                        // dw_start relative to this pair
+    int rows_max = 0, width_max = 0;             // over groups
+    int token_cap = 0, tq_cap = 0;
+    long long cells = 0;                         // M cells of all groups + top level
+    std::string err;
+    lcg_status code = LCG_OK;
+};
+
+// Validate one pair's tables and build its derived structures; on error
+// p.code / p.err describe it.
+lcg_status prep_pair(const lcg_pair_tables &t, const lcg_align_opts &o, Prep &p);
+
+void set_error(const std::string &msg);
+
+}  // namespace lcg_host
