@@ -32,6 +32,12 @@ WORKLOAD = dict(count=64, len_lo=60, len_hi=400, seed=2024, q=0.05)
 WORKLOAD_NAME = "sankoff_allpairs_64rnas_60-400nt_global"
 PER_PAIR = dict(len_a=400, seed_a=3, len_b=400, seed_b=4)
 CPU_SAMPLE_SECONDS = 20.0
+# LocARNA-P: all pairs of 128 RNAs of 80-500 nt, inside + adjoint outside, in
+# launches grouped by pair size (buckets of PF_BUCKET pairs)
+PF_WORKLOAD = dict(count=128, len_lo=80, len_hi=500, seed=2025, q=0.05)
+PF_WORKLOAD_NAME = "locarna_p_allpairs_128rnas_80-500nt"
+PF_BUCKET = 1024
+PF_CPU_SECONDS = 20.0
 
 
 def log(*a):
@@ -51,6 +57,24 @@ def build_tables(threads=None):
     with ThreadPoolExecutor(threads) as ex:
         tables = list(ex.map(lambda ab: prepare_pair(pp[ab[0]], pp[ab[1]]), pairs))
     return tables, pairs
+
+
+def build_pf_tables(threads=None):
+    """Tables of the LocARNA-P workload, prepared as locarna_p prepares them
+    (envelope 1e-5 in double precision, src/locarna_p.cc defaults)."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    from locarna_gb300.prep import prepare_pair
+    from locarna_gb300.synth import make_family
+    W = PF_WORKLOAD
+    fam = make_family(W["count"], W["len_lo"], W["len_hi"], W["seed"], q=W["q"])
+    pp = [r.to_pp() for r in fam]
+    pairs = [(a, b) for a in range(len(fam)) for b in range(a + 1, len(fam))]
+    threads = threads or os.cpu_count() or 4
+    with ThreadPoolExecutor(threads) as ex:
+        tables = list(ex.map(lambda ab: prepare_pair(pp[ab[0]], pp[ab[1]], min_trace_probability=1e-5,
+                                                     pf_precision=0), pairs))
+    return tables
 
 
 def per_pair_tables():
@@ -80,7 +104,21 @@ def _cpu_worker(args):
     return done, time.perf_counter() - t0
 
 
-def cpu_sample(tables, budget_s, cores, seed=7):
+def _cpu_pf_worker(args):
+    idx, budget = args
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from oracle_ffi import oracle_pf
+    t0 = time.perf_counter()
+    done = 0
+    for k in idx:
+        if time.perf_counter() - t0 >= budget:
+            break
+        oracle_pf(_CPU_TABLES[k])
+        done += 1
+    return done, time.perf_counter() - t0
+
+
+def cpu_sample(tables, budget_s, cores, seed=7, worker=None):
     """Time-bounded CPU sample of the workload: a seeded permutation of the
     pairs dealt round-robin to one forked process per core; each process
     aligns its pairs until budget_s is spent. Returns (pairs, aligns/s)."""
@@ -92,7 +130,7 @@ def cpu_sample(tables, budget_s, cores, seed=7):
     lists = [order[c::cores] for c in range(cores)]
     ctx = mp.get_context("fork")
     with ctx.Pool(cores) as pool:
-        res = pool.map(_cpu_worker, [(lst, budget_s) for lst in lists])
+        res = pool.map(worker or _cpu_worker, [(lst, budget_s) for lst in lists])
     done = sum(d for d, _ in res)
     rate = sum(d / t for d, t in res if t > 0)
     return done, rate
@@ -146,6 +184,84 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sms)}
 
 
+# ---------------------------------------------------------------- LocARNA-P
+
+def run_pf(eng, tables, flush_l2, cpu):
+    """LocARNA-P: FP64 and FP32-scaled inside + adjoint outside over all pairs
+    in size-sorted buckets; device and end-to-end rates, FP32 error against
+    the FP64 run of the same kernels, and one 200-nt pair with gradients."""
+    import numpy as np
+    order = sorted(range(len(tables)), key=lambda k: tables[k].len_a * tables[k].len_b)
+    buckets = [order[i:i + PF_BUCKET] for i in range(0, len(order), PF_BUCKET)]
+    for prec in (64, 32):  # warm-up: the smallest bucket
+        eng.pf_forward([tables[k] for k in buckets[0]], precision=prec)
+        eng.pf_backward(probs=False)
+    dev = {64: 0.0, 32: 0.0}
+    wall = {64: 0.0, 32: 0.0}
+    err_am, err_bm, pair_err = 0.0, 0.0, []
+    launches = 0
+    for b in buckets:
+        tb = [tables[k] for k in b]
+        res = {}
+        for prec in (64, 32):
+            flush_l2()
+            t0 = time.perf_counter()
+            eng.pf_forward(tb, precision=prec)
+            r = eng.pf_backward(probs=True)
+            wall[prec] += time.perf_counter() - t0
+            f, bw = eng.pf_last_timing()
+            dev[prec] += f + bw
+            launches += 2
+            res[prec] = r
+        for r64, r32 in zip(res[64], res[32]):
+            ea = float(np.max(np.abs(r64["am_prob"] - r32["am_prob"]))) if r64["am_prob"].size else 0.0
+            eb = float(np.max(np.abs(r64["bm_prob"] - r32["bm_prob"])))
+            err_am, err_bm = max(err_am, ea), max(err_bm, eb)
+            pair_err.append(max(ea, eb))
+        del res
+    n = len(tables)
+    pair_err.sort()
+    out = {
+        "workload": PF_WORKLOAD_NAME, "pairs": n, "buckets": len(buckets), "bucket_pairs": PF_BUCKET,
+        "fp64": {"pairs_per_s": n / (dev[64] / 1e3), "device_ms": dev[64], "e2e_pairs_per_s": n / wall[64]},
+        "fp32": {"pairs_per_s": n / (dev[32] / 1e3), "device_ms": dev[32], "e2e_pairs_per_s": n / wall[32]},
+        "fp32_over_fp64_device": dev[64] / dev[32], "fp32_over_fp64_e2e": wall[64] / wall[32],
+        "fp32_max_abs_err": {"am_prob": err_am, "bm_prob": err_bm,
+                             "pair_max_median": pair_err[len(pair_err) // 2], "pair_max_max": pair_err[-1],
+                             "tolerance": 1e-5, "against": "FP64 run of the same kernels"},
+        "gpu_launches": launches,
+        "cpu_baseline": cpu,
+    }
+    # one pair of 200 nt: log Z and gradients, FP64 and FP32
+    from locarna_gb300.prep import prepare_pair
+    from locarna_gb300.synth import make_rna
+    t = prepare_pair(make_rna(200, 11).to_pp(), make_rna(200, 12).to_pp(), min_trace_probability=1e-5,
+                     pf_precision=0)
+    one = {}
+    for prec in (64, 32):
+        for _ in range(3):
+            eng.pf_forward([t], precision=prec)
+            eng.pf_backward(probs=False)
+        ms = []
+        for _ in range(5):
+            flush_l2()
+            lz = eng.pf_forward([t], precision=prec)[0]
+            r = eng.pf_backward(probs=False)[0]
+            f, bw = eng.pf_last_timing()
+            ms.append(f + bw)
+        ms.sort()
+        one[prec] = (lz, r, ms[len(ms) // 2])
+    g64 = np.array([one[64][1][k] for k in ("dlogz_dindel", "dlogz_dindel_opening", "dlogz_dstruct_weight")]
+                   + list(one[64][1]["dlogz_dbasematch"]))
+    g32 = np.array([one[32][1][k] for k in ("dlogz_dindel", "dlogz_dindel_opening", "dlogz_dstruct_weight")]
+                   + list(one[32][1]["dlogz_dbasematch"]))
+    nz = np.abs(g64) > 0
+    out["pair_200nt"] = {"fp64_ms": one[64][2], "fp32_ms": one[32][2], "log_z_fp64": one[64][0],
+                         "log_z_fp32": one[32][0],
+                         "grad_fp32_max_rel_err": float(np.max(np.abs(g32[nz] - g64[nz]) / np.abs(g64[nz])))}
+    return out
+
+
 # ---------------------------------------------------------------- arms
 
 def run_ours(args):
@@ -162,6 +278,17 @@ def run_ours(args):
     cores = os.cpu_count() or 1
     cpu_done, cpu_rate = cpu_sample(tables, CPU_SAMPLE_SECONDS, cores)
     log(f"cpu baseline: {cpu_done} pairs, {cpu_rate:.2f} aligns/s on {cores} cores")
+    pf_tables, pf_cpu = None, None
+    if not args.no_pf:
+        t0 = time.time()
+        pf_tables = build_pf_tables()
+        log(f"host preparation of {len(pf_tables)} LocARNA-P pairs: {time.time() - t0:.1f} s")
+        pf_done, pf_rate = cpu_sample(pf_tables, PF_CPU_SECONDS, cores, seed=9, worker=_cpu_pf_worker)
+        log(f"cpu baseline LocARNA-P: {pf_done} pairs, {pf_rate:.3f} pairs/s on {cores} cores")
+        pf_cpu = {"value": pf_rate, "unit": "pairs/s", "cores": cores, "kind": "port",
+                  "sample": f"{pf_done} of the {len(pf_tables)} pairs (seeded permutation), one process per "
+                            f"core, {PF_CPU_SECONDS:.0f} s per process; the oracle restatement of AlignerP "
+                            f"(inside, outside, arc-match and base-match probabilities)"}
     eng = Engine(0)
     call = eng.prepare_call(tables)
 
@@ -278,6 +405,8 @@ def run_ours(args):
                                    f"per core, {CPU_SAMPLE_SECONDS:.0f} s per process"},
         "clocks": clocks,
     }
+    if pf_tables is not None:
+        out["locarna_p"] = run_pf(eng, pf_tables, flush_l2, pf_cpu)
     print(json.dumps(out), flush=True)
     eng.close()
 
@@ -346,6 +475,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-pf", action="store_true", help="skip the LocARNA-P part")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -181,6 +181,77 @@ lcg_status lcg_engine_last_work(lcg_engine eng, lcg_work_counts *out);
 lcg_status lcg_measure_int_peak(lcg_engine eng, int32_t dpx, double *gops);
 
 
+/* --------------------------------------------- LocARNA-P forward/backward
+ *
+ * The partition-function aligner LocARNA::AlignerP<T> (aligner_p.hh:53-622,
+ * driven by src/locarna_p.cc:466-531) as a forward/backward pair:
+ *   forward  = AlignerP::align_inside() (aligner_p.icc:413-438): log Z;
+ *   backward = the adjoint of the inside recursion, which yields what
+ *              align_outside() + compute_arcmatch_probabilities() +
+ *              compute_basematch_probabilities() (aligner_p.icc:1113-1399)
+ *              yield, and the derivatives of log Z with respect to the
+ *              scoring parameters, in one pass.
+ * Global mode without anchors (the reference's AlignerP supports no other).
+ * The Boltzmann weights are exp(score / temperature) (scoring.hh:857-860)
+ * from the same integer tables lcg_align_pairs takes. precision 64 runs
+ * the recursions in double; precision 32 runs them in float with a
+ * per-position scale factor chosen on the host, accumulating log Z, the
+ * expected counts and the normalisation in double.
+ */
+typedef struct lcg_pf_opts {
+    double temperature; /* --temperature-alipf (300) */
+    double pf_scale;    /* AlignerPParams::pf_scale (1): arc terms times pf_scale, D divided */
+    int32_t precision;  /* 64 or 32 */
+    /* Continuous offsets of the scoring parameters the gradients are taken
+     * with respect to (all 0 = the integer tables as given): [0] indel (added
+     * to gap_a, gap_b), [1] indel_opening, [2] struct_weight (arc-match score
+     * plus delta * am_dscore_dsw), [3 + 4x + y] base-match score S[x][y]
+     * (sigma(i,j) plus delta where code_a[i] = x, code_b[j] = y). Offsets
+     * [2..18] need the grad specs of lcg_pf_forward. */
+    double param_delta[19];
+} lcg_pf_opts;
+
+/* Per pair input of the parameter gradients (all optional, see below). */
+typedef struct lcg_pf_grad_spec {
+    const int8_t *code_a; /* [len_a+1]; code_a[i] in 0..3 for A,C,G,U of position i, -1 otherwise */
+    const int8_t *code_b; /* [len_b+1] */
+    const double *am_dscore_dsw; /* [num_arcmatches]: d arc-match score / d struct_weight */
+} lcg_pf_grad_spec;
+
+typedef struct lcg_pf_result {
+    /* caller-owned outputs, NULL = not wanted */
+    double *am_prob; /* [num_arcmatches] arc-match probabilities (compute_arcmatch_probabilities) */
+    double *bm_prob; /* [(len_a+1)*(len_b+1)] base-match probabilities, arc-match ends not included */
+    /* filled by lcg_pf_backward */
+    double log_z;
+    double gap_ext_uses;  /* expected number of gapped positions (uses of gap_a / gap_b) */
+    double gap_open_uses; /* expected number of gap openings (uses of indel_opening) */
+    /* d log Z / d parameter: indel (gap_a[i] = gap_b[j] = indel), indel_opening
+     * always; struct_weight and the 16 base-match scores (sigma(i,j) =
+     * S[code_a[i]][code_b[j]], index 4*x+y) when a grad spec is given */
+    double dlogz_dindel;
+    double dlogz_dindel_opening;
+    double dlogz_dstruct_weight;
+    double dlogz_dbasematch[16];
+} lcg_pf_result;
+
+void lcg_pf_opts_default(lcg_pf_opts *opts);
+
+/* log Z of `npairs` pairs in one batched launch. specs: NULL or [npairs]
+ * (needed for nonzero param_delta[2..18]). The engine keeps the state the
+ * backward pass needs until the next lcg_pf_forward or lcg_pf_backward. */
+lcg_status lcg_pf_forward(lcg_engine eng, const lcg_pair_tables *pairs, int32_t npairs,
+                          const lcg_pf_opts *opts, const lcg_pf_grad_spec *specs,
+                          double *log_z);
+
+/* Backward pass of the last lcg_pf_forward: results[npairs]; specs NULL or
+ * [npairs] (entries with NULL members skip those gradients). */
+lcg_status lcg_pf_backward(lcg_engine eng, const lcg_pf_grad_spec *specs,
+                           lcg_pf_result *results);
+
+/* Device time (ms) of the last forward and backward kernels. */
+lcg_status lcg_pf_last_timing(lcg_engine eng, double *forward_ms, double *backward_ms);
+
 /* -------------------------------------------- allocation-free entry point
  *
  * No counterpart in the reference: an addition of this library for callers
@@ -248,6 +319,11 @@ lcg_status lcg_prepared_tables(lcg_prepared p, lcg_pair_tables *out);
 const char *lcg_prepared_sequence(lcg_prepared p, int32_t which);
 /* 0 if the envelope partition function failed (PFGotoh::fail, edge_probs.hh:202) */
 int32_t lcg_prepared_envelope_ok(lcg_prepared p);
+/* Gradient inputs of the prepared pair for lcg_pf_backward: base codes and
+ * d am_score / d struct_weight of the unrounded arc weights,
+ * (1 - ln p_a / ln pe_A) + (1 - ln p_b / ln pe_B) (scoring.cc:250-265);
+ * views valid until lcg_prepared_free. */
+lcg_status lcg_prepared_grad_spec(lcg_prepared p, lcg_pf_grad_spec *out);
 lcg_status lcg_prepared_free(lcg_prepared p);
 
 #ifdef __cplusplus

@@ -52,6 +52,28 @@ class lcg_work_counts(C.Structure):
                 ("arc_terms", C.c_int64), ("valid_arc_terms", C.c_int64)]
 
 
+_PD = C.POINTER(C.c_double)
+_P8 = C.POINTER(C.c_int8)
+
+
+class lcg_pf_opts(C.Structure):
+    _fields_ = [("temperature", C.c_double), ("pf_scale", C.c_double), ("precision", C.c_int32),
+                ("param_delta", C.c_double * 19)]
+
+
+class lcg_pf_grad_spec(C.Structure):
+    _fields_ = [("code_a", _P8), ("code_b", _P8), ("am_dscore_dsw", _PD)]
+
+
+class lcg_pf_result(C.Structure):
+    _fields_ = [
+        ("am_prob", _PD), ("bm_prob", _PD),
+        ("log_z", C.c_double), ("gap_ext_uses", C.c_double), ("gap_open_uses", C.c_double),
+        ("dlogz_dindel", C.c_double), ("dlogz_dindel_opening", C.c_double),
+        ("dlogz_dstruct_weight", C.c_double), ("dlogz_dbasematch", C.c_double * 16),
+    ]
+
+
 def _i32(a):
     return np.ascontiguousarray(np.asarray(a, dtype=np.int32))
 

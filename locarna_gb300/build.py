@@ -24,7 +24,8 @@ GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 # tuning defines for the CUDA sources, e.g. LCG_NVCC_DEFS="-DLCG_FILL_WARPS=4"
 EXTRA_DEFS = os.environ.get("LCG_NVCC_DEFS", "").split()
 
-CUDA_SOURCES = ["engine.cu", "sankoff_kernels.cu", "sankoff_sl_kernels.cu", "microbench.cu", "noalloc.cu"]
+CUDA_SOURCES = ["engine.cu", "sankoff_kernels.cu", "sankoff_sl_kernels.cu", "microbench.cu", "noalloc.cu",
+                "pf_kernels.cu", "engine_pf.cu"]
 HOST_SOURCES = ["host_prep.cpp"]  # C++ host-only translation units
 
 

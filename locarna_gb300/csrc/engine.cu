@@ -17,6 +17,7 @@
 #include "../../include/locarna_gb300.h"
 #include "lcg_device.cuh"
 #include "engine_prep.hh"
+#include "engine_state.hh"
 
 namespace lcg {
 cudaError_t launch_fill(const PairDev *, const GroupItem *, int, const int4 *, int *, long long,
@@ -29,7 +30,7 @@ cudaError_t launch_sl_fill(const PairDev *, const GroupItem *, int, const int4 *
 cudaError_t launch_sl_trace(const PairDev *, int, int *, long long, int, int *, cudaStream_t);
 cudaError_t launch_trace(const PairDev *, int, int *, long long, int, int *, cudaStream_t);
 int fill_warps_per_block();
-cudaError_t fill_occupancy(int sw, int *blocks_per_sm);
+cudaError_t fill_occupancy(int sw, bool counting, int *blocks_per_sm);
 cudaError_t trace_prepare(int sw);
 }  // namespace lcg
 
@@ -167,7 +168,7 @@ lcg_status prep_pair(const lcg_pair_tables &t, const lcg_align_opts &o, Prep &p)
     std::vector<int> ord(p.cre_start[p.bandcells]);
     for (int k = 0; k < na; ++k)
         if (cell_of[k] >= 0) ord[fillp[cell_of[k]]++] = k;
-    p.cre.resize(2 * ord.size());
+    p.cre.resize(4 * ord.size());
     for (int c = 0; c < p.bandcells; ++c) {
         auto b = ord.begin() + p.cre_start[c], e = ord.begin() + p.cre_start[c + 1];
         if (e - b > 1)
@@ -179,8 +180,10 @@ lcg_status prep_pair(const lcg_pair_tables &t, const lcg_align_opts &o, Prep &p)
     }
     for (size_t q = 0; q < ord.size(); ++q) {
         int k = ord[q];
-        p.cre[2 * q] = k;
-        p.cre[2 * q + 1] = (p.am_ends[4 * k] << 16) | p.am_ends[4 * k + 2];
+        p.cre[4 * q] = k;
+        p.cre[4 * q + 1] = p.am_ends[4 * k] - 1;      // a.l - 1: row of the inner corner
+        p.cre[4 * q + 2] = p.am_ends[4 * k + 2] - 1;  // b.l - 1: column of the inner corner
+        p.cre[4 * q + 3] = p.am_ends[4 * k + 3];      // b.r: the cell's column
     }
 
     // left-end groups (aligner.cc:660-732): bucket arc matches by (al,bl)
@@ -306,25 +309,6 @@ size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 // ------------------------------------------------------------------ engine
 
-struct lcg_engine_s {
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    bool own_stream = false;
-    int sms = 0;
-    char *d_arena = nullptr;
-    size_t arena_cap = 0;
-    char *h_stage = nullptr;
-    size_t stage_cap = 0;
-    int *d_scratch = nullptr;
-    size_t scratch_cap = 0;  // ints
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr;
-    double last_ms = 0, last_fill_ms = 0, last_trace_ms = 0;
-    long long last_launches = 0;
-    long long last_h2d = 0, last_d2h = 0;
-    long long last_groups = 0, last_cells = 0, last_terms = -1, last_visits = -1;
-    bool counting = false;
-};
-
 extern "C" {
 
 const char *lcg_last_error(void) { return g_last_error.c_str(); }
@@ -368,6 +352,7 @@ lcg_status lcg_engine_destroy(lcg_engine e) {
     if (e->ev1) cudaEventDestroy(e->ev1);
     if (e->ev2) cudaEventDestroy(e->ev2);
     if (e->own_stream) cudaStreamDestroy(e->stream);
+    lcg_host::pf_release(e);
     delete e;
     return LCG_OK;
 }
@@ -477,7 +462,7 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
         o.rowinfo = take(up, 16ull * (p.n + 2));
         o.anc = t.match_lo ? take(up, 4ull * (2 * (p.n + 1) + 2 * (p.n + 1) + 2 * (p.m + 1))) : 0;
         o.cre_start = take(up, 4ull * (p.bandcells + 1));
-        o.cre = take(up, 4ull * std::max<size_t>(p.cre.size(), 2));
+        o.cre = take(up, 4ull * std::max<size_t>(p.cre.size(), 4));
         o.am_ends = take(up, 4ull * std::max<size_t>(p.am_ends.size(), 4));
         o.am_score = take(up, 4ull * std::max(t.num_arcmatches, 1));
         o.D = take(up, 4ull * std::max(t.num_arcmatches, 1));
@@ -609,7 +594,7 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
             d.ins_hi = a + 4 * (p.n + 1) + (p.m + 1);
         }
         d.cre_start = (const int *)(Dv + o.cre_start);
-        d.cre = (const int2 *)(Dv + o.cre);
+        d.cre = (const int4 *)(Dv + o.cre);
         d.D = (int *)(Dv + o.D);
         d.am_ends = (const int4 *)(Dv + o.am_ends);
         d.am_score = (const int *)(Dv + o.am_score);
@@ -628,7 +613,7 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
     if (sl) {
         CUDA_TRY(sl_prepare(sw, &blocks_per_sm));
     } else {
-        CUDA_TRY(fill_occupancy(sw, &blocks_per_sm));
+        CUDA_TRY(fill_occupancy(sw, e->counting, &blocks_per_sm));
         CUDA_TRY(trace_prepare(sw));
     }
     if (blocks_per_sm < 1) return fail(LCG_ERR_UNSUPPORTED, "fill kernel does not fit on an SM");

@@ -1,0 +1,513 @@
+// Host side of the LocARNA-P engine: the forward (log Z) / backward
+// (probabilities and weight derivatives) C-ABI pair of include/locarna_gb300.h.
+//
+// The forward keeps its device state in the engine so that the backward pass
+// can run on it: D entries, the per-arc-match use counters, and the
+// accumulators of the adjoint.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/locarna_gb300.h"
+#include "engine_prep.hh"
+#include "engine_state.hh"
+#include "lcg_device.cuh"
+#include "pf_device.cuh"
+
+
+using namespace lcg;
+
+namespace {
+
+lcg_status pf_fail(lcg_status c, const std::string &m) {
+    lcg_host::set_error(m);
+    return c;
+}
+
+#define PF_TRY(call)                                                                          \
+    do {                                                                                      \
+        cudaError_t _e = (call);                                                              \
+        if (_e != cudaSuccess) return pf_fail(LCG_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(_e)); \
+    } while (0)
+
+size_t up16(size_t x) { return (x + 15) / 16 * 16; }
+
+struct PFLayout {
+    int n, m, na, bandcells;
+    size_t rowinfo, cre_start, cre, bm, gA, gB, w, D, Dbar, cnt, bmacc, res, topM;
+    double log_c_total;  // (n+m) log c
+};
+
+struct PFState {
+    int precision = 64;
+    int npairs = 0;
+    char *d_arena = nullptr;
+    size_t cap = 0;
+    char *h_stage = nullptr;
+    size_t hcap = 0;
+    char *d_scratch = nullptr;
+    size_t scratch_cap = 0;
+    std::vector<PFLayout> lay;
+    size_t off_pairs = 0, off_items = 0, off_dw = 0, off_ctrl = 0, out_begin = 0, out_end = 0, total = 0;
+    size_t nitems = 0;
+    int sw = 0;
+    long long stride = 0;
+    bool have_forward = false;
+    double fwd_ms = 0, back_ms = 0;
+    double temperature = 300.0;
+    std::vector<double> log_z;
+};
+
+PFState *state_of(lcg_engine e) {
+    if (!e->pf) e->pf = new PFState();
+    return (PFState *)e->pf;
+}
+
+// log of the sequence-only partition function (base matches and affine gaps,
+// no arc matches) over the band, in double with per-row rescaling; its value
+// per alignment position sets the FP32 scale factor.
+double seq_log_pf(const lcg_pair_tables &t, const std::vector<double> &bm, const std::vector<double> &gA,
+                  const std::vector<double> &gB, double o) {
+    const int n = t.len_a, m = t.len_b;
+    std::vector<double> Mp(m + 1, 0.0), Mc(m + 1, 0.0), Ep(m + 1, 0.0), Ec(m + 1, 0.0);
+    double logscale = 0.0;
+    Mp[0] = 1.0;
+    double g = o;
+    for (int j = 1; j <= std::min(m, t.max_col[0]); ++j) {
+        g *= gB[j];
+        Mp[j] = g;
+    }
+    double colv = o;
+    for (int i = 1; i <= n; ++i) {
+        std::fill(Mc.begin(), Mc.end(), 0.0);
+        std::fill(Ec.begin(), Ec.end(), 0.0);
+        colv *= gA[i];
+        if (t.min_col[i] == 0) Mc[0] = colv;
+        double F = 0.0;
+        const int lo = std::max(1, t.min_col[i]), hi = std::min(m, t.max_col[i]);
+        for (int j = lo; j <= hi; ++j) {
+            const double E = Ep[j] * gA[i] + (Mp[j] - Ep[j]) * gA[i] * o;
+            F = F * gB[j] + (Mc[j - 1] - F) * gB[j] * o;
+            Ec[j] = E;
+            Mc[j] = Mp[j - 1] * bm[(size_t)i * (m + 1) + j] + E + F;
+        }
+        double mx = 0.0;
+        for (int j = 0; j <= m; ++j) mx = std::max(mx, Mc[j]);
+        if (mx > 0.0) {
+            for (int j = 0; j <= m; ++j) {
+                Mc[j] /= mx;
+                Ec[j] /= mx;
+            }
+            colv /= mx;
+            logscale += std::log(mx);
+        }
+        std::swap(Mp, Mc);
+        std::swap(Ep, Ec);
+    }
+    return logscale + std::log(std::max(Mp[m], 1e-300));
+}
+
+template <typename T>
+lcg_status pf_forward_t(lcg_engine e, PFState *S, const lcg_pair_tables *pairs, int npairs, const lcg_pf_opts *o,
+                        const lcg_pf_grad_spec *specs, double *log_z) {
+    const double temp = o->temperature > 0 ? o->temperature : 300.0;
+    const double pf_scale = o->pf_scale > 0 ? o->pf_scale : 1.0;
+    lcg_align_opts ao{0, 0, 0, 0};
+    std::vector<lcg_host::Prep> prep(npairs);
+    {
+        std::atomic<int> next(0);
+        int nth = (int)std::min<unsigned>(std::max(1u, std::thread::hardware_concurrency()), (unsigned)npairs);
+        nth = std::min(nth, 64);
+        auto work = [&]() {
+            for (int q; (q = next.fetch_add(1)) < npairs;) lcg_host::prep_pair(pairs[q], ao, prep[q]);
+        };
+        std::vector<std::thread> th;
+        for (int t = 1; t < nth; ++t) th.emplace_back(work);
+        work();
+        for (auto &t : th) t.join();
+    }
+    bool need_spec = false;
+    for (int k = 2; k < 19; ++k) need_spec |= o->param_delta[k] != 0.0;
+    if (need_spec && !specs) return pf_fail(LCG_ERR_ARG, "param_delta[2..18] needs grad specs");
+    for (int q = 0; q < npairs; ++q) {
+        if (prep[q].code != LCG_OK) return pf_fail(prep[q].code, "pair " + std::to_string(q) + ": " + prep[q].err);
+        if (pairs[q].match_lo) return pf_fail(LCG_ERR_UNSUPPORTED, "LocARNA-P ignores anchors in the reference; pass none");
+    }
+    // layout
+    S->lay.assign(npairs, PFLayout{});
+    size_t up = 0;
+    auto take = [](size_t &cur, size_t bytes) {
+        size_t r = cur;
+        cur = up16(cur + bytes);
+        return r;
+    };
+    size_t nitems = 0, ndw = 0;
+    int sw = 0, rows_max = 1;
+    for (auto &p : prep) {
+        nitems += p.groups.size();
+        ndw += p.dw.size();
+        sw = std::max(sw, std::max(p.width_max + 1, p.m + 2));
+        rows_max = std::max(rows_max, std::max(p.rows_max + 1, p.n + 1));
+    }
+    S->off_pairs = take(up, sizeof(PFPair<T>) * npairs);
+    S->off_items = take(up, sizeof(PFItem<T>) * nitems);
+    S->off_dw = take(up, sizeof(int4) * std::max<size_t>(ndw, 1));
+    S->off_ctrl = take(up, 64);
+    for (int q = 0; q < npairs; ++q) {
+        const auto &p = prep[q];
+        PFLayout &L = S->lay[q];
+        L.n = p.n;
+        L.m = p.m;
+        L.na = pairs[q].num_arcmatches;
+        L.bandcells = p.bandcells;
+        L.rowinfo = take(up, 16ull * (p.n + 2));
+        L.cre_start = take(up, 4ull * (p.bandcells + 1));
+        L.cre = take(up, 4ull * std::max<size_t>(p.cre.size(), 4));
+        L.bm = take(up, sizeof(T) * (p.n + 1) * (p.m + 1));
+        L.gA = take(up, sizeof(T) * (p.n + 1));
+        L.gB = take(up, sizeof(T) * (p.m + 1));
+        L.w = take(up, sizeof(T) * std::max(L.na, 1));
+        L.D = take(up, sizeof(T) * std::max(L.na, 1));
+    }
+    // zero-initialised device section, then the output section
+    const size_t zero_begin = up;
+    for (int q = 0; q < npairs; ++q) S->lay[q].cnt = take(up, 4ull * std::max(S->lay[q].na, 1));
+    const size_t out_begin = up;
+    for (int q = 0; q < npairs; ++q) {
+        PFLayout &L = S->lay[q];
+        L.res = take(up, 8ull * 4);
+        L.Dbar = take(up, sizeof(T) * std::max(L.na, 1));
+        L.bmacc = take(up, sizeof(T) * std::max(L.bandcells, 1));
+    }
+    const size_t out_end = up;
+    for (int q = 0; q < npairs; ++q) S->lay[q].topM = take(up, sizeof(T) * (S->lay[q].n + 1) * (S->lay[q].m + 1));
+    const size_t total = up;
+    if (total > S->cap) {
+        if (S->d_arena) cudaFree(S->d_arena);
+        S->d_arena = nullptr;
+        S->cap = 0;
+        if (cudaMalloc(&S->d_arena, total + total / 4) != cudaSuccess) return pf_fail(LCG_ERR_NOMEM, "PF device arena allocation failed");
+        S->cap = total + total / 4;
+    }
+    if (out_end > S->hcap) {
+        if (S->h_stage) cudaFreeHost(S->h_stage);
+        S->h_stage = nullptr;
+        S->hcap = 0;
+        if (cudaMallocHost(&S->h_stage, out_end + out_end / 4) != cudaSuccess) return pf_fail(LCG_ERR_NOMEM, "PF pinned staging allocation failed");
+        S->hcap = out_end + out_end / 4;
+    }
+    char *H = S->h_stage, *Dv = S->d_arena;
+    // pack
+    PFPair<T> *hp = (PFPair<T> *)(H + S->off_pairs);
+    PFItem<T> *hit = (PFItem<T> *)(H + S->off_items);
+    int4 *hdw = (int4 *)(H + S->off_dw);
+    {
+        std::vector<std::pair<double, std::pair<int, int>>> order;
+        order.reserve(nitems);
+        for (int q = 0; q < npairs; ++q) {
+            size_t G = prep[q].groups.size();
+            for (size_t g = 0; g < G; ++g) order.push_back({(double)(g + 1) / (double)G, {q, (int)g}});
+        }
+        std::stable_sort(order.begin(), order.end(), [](const auto &a, const auto &b) { return a.first < b.first; });
+        std::vector<size_t> dwbase(npairs);
+        size_t dwb = 0;
+        for (int q = 0; q < npairs; ++q) {
+            dwbase[q] = dwb;
+            for (size_t k = 0; k < prep[q].dw.size(); ++k) hdw[dwb + k] = prep[q].dw[k];
+            dwb += prep[q].dw.size();
+        }
+        size_t it = 0;
+        for (auto &x : order) {
+            const int q = x.second.first;
+            const GroupItem &g = prep[q].groups[x.second.second];
+            PFItem<T> pi;
+            pi.pair = q;
+            pi.al = g.al;
+            pi.ar = g.ar;
+            pi.bl = g.bl;
+            pi.br = g.br;
+            pi.dw_start = g.dw_start + (int)dwbase[q];
+            pi.dw_count = g.dw_count;
+            pi.top = g.top;
+            hit[it++] = pi;
+        }
+    }
+    std::memset(H + S->off_ctrl, 0, 64);
+    // per pair: Boltzmann weights, scale factor and packed tables (disjoint
+    // staging regions, filled in parallel)
+    auto pack = [&](int q) {
+        const auto &p = prep[q];
+        const auto &t = pairs[q];
+        const PFLayout &L0 = S->lay[q];
+        PFLayout &L = S->lay[q];
+        const int n = p.n, m = p.m;
+        // Boltzmann weights exp(score / temperature) (scoring.hh:857-860),
+        // scores shifted by the continuous parameter offsets
+        const double *dl = o->param_delta;
+        const lcg_pf_grad_spec *sp = specs ? &specs[q] : nullptr;
+        std::vector<double> bm((size_t)(n + 1) * (m + 1), 0.0), gA(n + 1, 0.0), gB(m + 1, 0.0);
+        for (int i = 1; i <= n; ++i) {
+            const int x = sp && sp->code_a ? sp->code_a[i] : -1;
+            for (int j = 1; j <= m; ++j) {
+                const int y = sp && sp->code_b ? sp->code_b[j] : -1;
+                const double d = (x >= 0 && x < 4 && y >= 0 && y < 4) ? dl[3 + 4 * x + y] : 0.0;
+                bm[(size_t)i * (m + 1) + j] = std::exp(((double)t.sigma[(size_t)i * (m + 1) + j] + d) / temp);
+            }
+        }
+        for (int i = 1; i <= n; ++i) gA[i] = std::exp(((double)t.gap_a[i] + dl[0]) / temp);
+        for (int j = 1; j <= m; ++j) gB[j] = std::exp(((double)t.gap_b[j] + dl[0]) / temp);
+        const double ow = std::exp(((double)t.indel_opening + dl[1]) / temp);
+        double logc = 0.0;
+        if (sizeof(T) == 4) logc = seq_log_pf(t, bm, gA, gB, ow) / (double)(n + m);
+        const double c = std::exp(logc), c2 = c * c;
+        L.log_c_total = logc * (n + m);
+        std::memcpy(H + L0.rowinfo, p.rowinfo.data(), 16ull * (n + 2));
+        std::memcpy(H + L0.cre_start, p.cre_start.data(), 4ull * (p.bandcells + 1));
+        if (!p.cre.empty()) std::memcpy(H + L0.cre, p.cre.data(), 4ull * p.cre.size());
+        T *hbm = (T *)(H + L0.bm);
+        for (size_t k = 0; k < bm.size(); ++k) hbm[k] = (T)(bm[k] / c2);
+        T *hgA = (T *)(H + L0.gA);
+        for (int i = 0; i <= n; ++i) hgA[i] = (T)(gA[i] / c);
+        T *hgB = (T *)(H + L0.gB);
+        for (int j = 0; j <= m; ++j) hgB[j] = (T)(gB[j] / c);
+        T *hw = (T *)(H + L0.w);
+        T *hD = (T *)(H + L0.D);
+        for (int k = 0; k < L.na; ++k) {
+            const double dsw = (sp && sp->am_dscore_dsw) ? dl[2] * sp->am_dscore_dsw[k] : 0.0;
+            hw[k] = (T)std::exp(((double)t.am_score[k] + dsw) / temp);
+            if (p.Dinit[k] == NOT_READY) {
+                if (sizeof(T) == 8) {
+                    long long bits = PF_NOT_READY_F64;
+                    std::memcpy(&hD[k], &bits, 8);
+                } else {
+                    int bits = PF_NOT_READY_F32;
+                    std::memcpy(&hD[k], &bits, 4);
+                }
+            } else {
+                hD[k] = T(0);
+            }
+        }
+        PFPair<T> &d = hp[q];
+        std::memset(&d, 0, sizeof d);
+        d.n = n;
+        d.m = m;
+        d.num_am = L.na;
+        d.rowinfo = (const int4 *)(Dv + L0.rowinfo);
+        d.cre_start = (const int *)(Dv + L0.cre_start);
+        d.cre = (const int4 *)(Dv + L0.cre);
+        d.bm = (const T *)(Dv + L0.bm);
+        d.gA = (const T *)(Dv + L0.gA);
+        d.gB = (const T *)(Dv + L0.gB);
+        d.o = (T)ow;
+        d.inv_s = (T)(1.0 / pf_scale);
+        d.arcf = (T)(pf_scale / (c2 * c2));
+        d.w = (const T *)(Dv + L0.w);
+        d.D = (T *)(Dv + L0.D);
+        d.Dbar = (T *)(Dv + L.Dbar);
+        d.cnt = (int *)(Dv + L.cnt);
+        d.topM = (T *)(Dv + L.topM);
+        d.bmacc = (T *)(Dv + L.bmacc);
+        d.res = (double *)(Dv + L.res);
+    };
+    {
+        std::atomic<int> next(0);
+        int nth = (int)std::min<unsigned>(std::max(1u, std::thread::hardware_concurrency()), (unsigned)npairs);
+        nth = std::min(nth, 64);
+        auto work = [&]() {
+            for (int q; (q = next.fetch_add(1)) < npairs;) pack(q);
+        };
+        std::vector<std::thread> th;
+        for (int k = 1; k < nth; ++k) th.emplace_back(work);
+        work();
+        for (auto &x : th) x.join();
+    }
+    // scratch: forward one rectangle per warp, backward four
+    int bf = 0, bb = 0;
+    PF_TRY(pf_fwd_occupancy<T>(sw, &bf));
+    PF_TRY(pf_back_occupancy<T>(sw, &bb));
+    if (bf < 1 || bb < 1) return pf_fail(LCG_ERR_UNSUPPORTED, "PF kernels do not fit on an SM");
+    const long long stride = (long long)rows_max * sw;
+    const size_t fwd_slots = (size_t)e->sms * bf * pf_warps_per_block();
+    const size_t back_slots = (size_t)e->sms * bb * pf_warps_per_block() * 4;
+    const size_t need = std::max(fwd_slots, back_slots) * (size_t)stride * sizeof(T);
+    if (need > S->scratch_cap) {
+        if (S->d_scratch) cudaFree(S->d_scratch);
+        S->d_scratch = nullptr;
+        S->scratch_cap = 0;
+        if (cudaMalloc(&S->d_scratch, need) != cudaSuccess) return pf_fail(LCG_ERR_NOMEM, "PF scratch allocation failed");
+        S->scratch_cap = need;
+    }
+    cudaStream_t st = e->stream;
+    PF_TRY(cudaMemcpyAsync(Dv, H, zero_begin, cudaMemcpyHostToDevice, st));
+    PF_TRY(cudaMemsetAsync(Dv + zero_begin, 0, out_end - zero_begin, st));
+    unsigned int *qhead = (unsigned int *)(Dv + S->off_ctrl);
+    int *status = (int *)(Dv + S->off_ctrl + 4);
+    int *abort_flag = (int *)(Dv + S->off_ctrl + 8);
+    PF_TRY(cudaEventRecord(e->ev0, st));
+    PF_TRY(pf_launch_fwd<T>(Dv + S->off_pairs, Dv + S->off_items, (int)nitems, (const int4 *)(Dv + S->off_dw),
+                            S->d_scratch, stride, sw, qhead, status, abort_flag, e->sms * bf, true, st));
+    PF_TRY(cudaEventRecord(e->ev1, st));
+    PF_TRY(cudaMemcpyAsync(H + S->off_ctrl, Dv + S->off_ctrl, 64, cudaMemcpyDeviceToHost, st));
+    for (int q = 0; q < npairs; ++q)
+        PF_TRY(cudaMemcpyAsync(H + S->lay[q].res, Dv + S->lay[q].res, 8, cudaMemcpyDeviceToHost, st));
+    PF_TRY(cudaStreamSynchronize(st));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e->ev0, e->ev1);
+    S->fwd_ms = ms;
+    if (((int *)(H + S->off_ctrl))[1] & ST_TIMEOUT) return pf_fail(LCG_ERR_TIMEOUT, "a device wait timed out (PF forward)");
+    S->log_z.resize(npairs);
+    for (int q = 0; q < npairs; ++q) {
+        log_z[q] = ((double *)(H + S->lay[q].res))[0] + S->lay[q].log_c_total;
+        S->log_z[q] = log_z[q];
+    }
+    S->temperature = temp;
+    S->precision = sizeof(T) == 8 ? 64 : 32;
+    S->npairs = npairs;
+    S->nitems = nitems;
+    S->sw = sw;
+    S->stride = stride;
+    S->out_begin = out_begin;
+    S->out_end = out_end;
+    S->total = total;
+    S->have_forward = true;
+    (void)bb;
+    return LCG_OK;
+}
+
+template <typename T>
+lcg_status pf_backward_t(lcg_engine e, PFState *S, const lcg_pf_grad_spec *grads, lcg_pf_result *results) {
+    char *H = S->h_stage, *Dv = S->d_arena;
+    cudaStream_t st = e->stream;
+    int bb = 0;
+    PF_TRY(pf_back_occupancy<T>(S->sw, &bb));
+    PF_TRY(cudaMemsetAsync(Dv + S->off_ctrl, 0, 64, st));
+    unsigned int *qhead = (unsigned int *)(Dv + S->off_ctrl);
+    int *status = (int *)(Dv + S->off_ctrl + 4);
+    int *abort_flag = (int *)(Dv + S->off_ctrl + 8);
+    PF_TRY(cudaEventRecord(e->ev1, st));
+    PF_TRY(pf_launch_back<T>(Dv + S->off_pairs, Dv + S->off_items, (int)S->nitems, (const int4 *)(Dv + S->off_dw),
+                             S->d_scratch, S->stride, S->sw, qhead, status, abort_flag, e->sms * bb, st));
+    PF_TRY(cudaEventRecord(e->ev2, st));
+    PF_TRY(cudaMemcpyAsync(H + S->off_ctrl, Dv + S->off_ctrl, 64, cudaMemcpyDeviceToHost, st));
+    PF_TRY(cudaMemcpyAsync(H + S->out_begin, Dv + S->out_begin, S->out_end - S->out_begin, cudaMemcpyDeviceToHost, st));
+    // D values (for the arc-match probabilities)
+    for (int q = 0; q < S->npairs; ++q)
+        if (S->lay[q].na > 0)
+            PF_TRY(cudaMemcpyAsync(H + S->lay[q].D, Dv + S->lay[q].D, sizeof(T) * S->lay[q].na,
+                                   cudaMemcpyDeviceToHost, st));
+    PF_TRY(cudaStreamSynchronize(st));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e->ev1, e->ev2);
+    S->back_ms = ms;
+    if (((int *)(H + S->off_ctrl))[1] & ST_TIMEOUT) return pf_fail(LCG_ERR_TIMEOUT, "a device wait timed out (PF backward)");
+    const double invT = 1.0 / S->temperature;
+    for (int q = 0; q < S->npairs; ++q) {
+        const PFLayout &L = S->lay[q];
+        lcg_pf_result &r = results[q];
+        const double *res = (const double *)(H + L.res);
+        const double Zs = std::exp(res[0]);  // Z in the scaled frame
+        const T *D = (const T *)(H + L.D);
+        const T *Db = (const T *)(H + L.Dbar);
+        const T *acc = (const T *)(H + L.bmacc);
+        const int4 *rowinfo = (const int4 *)(H + L.rowinfo);
+        const lcg_pf_grad_spec *g = grads ? &grads[q] : nullptr;
+        r.log_z = S->log_z[q];
+        r.gap_ext_uses = res[1] / Zs;
+        r.gap_open_uses = res[2] / Zs;
+        r.dlogz_dindel = r.gap_ext_uses * invT;
+        r.dlogz_dindel_opening = r.gap_open_uses * invT;
+        r.dlogz_dstruct_weight = 0.0;
+        for (int k = 0; k < 16; ++k) r.dlogz_dbasematch[k] = 0.0;
+        const bool sw_grad = g && g->am_dscore_dsw;
+        if (r.am_prob || sw_grad) {
+            double dsw = 0.0;
+            for (int k = 0; k < L.na; ++k) {
+                const double p = (double)D[k] * (double)Db[k] / Zs;
+                if (r.am_prob) r.am_prob[k] = p;
+                if (sw_grad) dsw += p * g->am_dscore_dsw[k];
+            }
+            r.dlogz_dstruct_weight = dsw * invT;
+        }
+        const bool bm_grad = g && g->code_a && g->code_b;
+        if (r.bm_prob || bm_grad) {
+            const int n = L.n, m = L.m;
+            if (r.bm_prob) std::memset(r.bm_prob, 0, sizeof(double) * (size_t)(n + 1) * (m + 1));
+            double cnt[16] = {0};
+            for (int i = 1; i <= n; ++i) {
+                const int lo = std::max(1, rowinfo[i].x), hi = std::min(m, rowinfo[i].y);
+                for (int j = lo; j <= hi; ++j) {
+                    const double p = (double)acc[rowinfo[i].w + j - rowinfo[i].x] / Zs;
+                    if (r.bm_prob) r.bm_prob[(size_t)i * (m + 1) + j] = p;
+                    if (bm_grad && g->code_a[i] >= 0 && g->code_a[i] < 4 && g->code_b[j] >= 0 && g->code_b[j] < 4)
+                        cnt[4 * g->code_a[i] + g->code_b[j]] += p;
+                }
+            }
+            if (bm_grad)
+                for (int k = 0; k < 16; ++k) r.dlogz_dbasematch[k] = cnt[k] * invT;
+        }
+    }
+    return LCG_OK;
+}
+
+}  // namespace
+
+namespace lcg_host {
+void pf_release(lcg_engine_s *e) {
+    PFState *S = (PFState *)e->pf;
+    if (!S) return;
+    if (S->d_arena) cudaFree(S->d_arena);
+    if (S->h_stage) cudaFreeHost(S->h_stage);
+    if (S->d_scratch) cudaFree(S->d_scratch);
+    delete S;
+    e->pf = nullptr;
+}
+}  // namespace lcg_host
+
+extern "C" {
+
+void lcg_pf_opts_default(lcg_pf_opts *o) {
+    std::memset(o, 0, sizeof *o);
+    o->temperature = 300.0;
+    o->pf_scale = 1.0;
+    o->precision = 64;
+}
+
+lcg_status lcg_pf_forward(lcg_engine e, const lcg_pair_tables *pairs, int32_t npairs, const lcg_pf_opts *opts,
+                          const lcg_pf_grad_spec *specs, double *log_z) {
+    if (!e || !pairs || !opts || !log_z || npairs < 1) return pf_fail(LCG_ERR_ARG, "bad argument");
+    cudaError_t ce = cudaSetDevice(e->device);
+    if (ce != cudaSuccess) return pf_fail(LCG_ERR_CUDA, cudaGetErrorString(ce));
+    PFState *S = state_of(e);
+    S->have_forward = false;
+    if (opts->precision == 64) return pf_forward_t<double>(e, S, pairs, npairs, opts, specs, log_z);
+    if (opts->precision == 32) return pf_forward_t<float>(e, S, pairs, npairs, opts, specs, log_z);
+    return pf_fail(LCG_ERR_ARG, "precision must be 32 or 64");
+}
+
+lcg_status lcg_pf_backward(lcg_engine e, const lcg_pf_grad_spec *grads, lcg_pf_result *results) {
+    if (!e || !results) return pf_fail(LCG_ERR_ARG, "bad argument");
+    PFState *S = state_of(e);
+    if (!S->have_forward) return pf_fail(LCG_ERR_ARG, "lcg_pf_backward needs a preceding lcg_pf_forward");
+    cudaError_t ce = cudaSetDevice(e->device);
+    if (ce != cudaSuccess) return pf_fail(LCG_ERR_CUDA, cudaGetErrorString(ce));
+    lcg_status r = S->precision == 64 ? pf_backward_t<double>(e, S, grads, results)
+                                       : pf_backward_t<float>(e, S, grads, results);
+    S->have_forward = false;  // the backward consumes the use counters
+    return r;
+}
+
+lcg_status lcg_pf_last_timing(lcg_engine e, double *forward_ms, double *backward_ms) {
+    if (!e) return pf_fail(LCG_ERR_ARG, "engine is NULL");
+    PFState *S = state_of(e);
+    if (forward_ms) *forward_ms = S->fwd_ms;
+    if (backward_ms) *backward_ms = S->back_ms;
+    return LCG_OK;
+}
+
+}  // extern "C"

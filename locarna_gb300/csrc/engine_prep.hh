@@ -19,7 +19,7 @@ struct Prep {
     std::vector<int4> rowinfo;                   // n+2
     int maxband = 0;
     std::vector<int> cre_start;                  // bandcells+1
-    std::vector<int> cre;                        // 2 per entry
+    std::vector<int> cre;                        // 4 per entry: am, a.l-1, b.l-1, b.r
     std::vector<int> am_ends;                    // 4 per am
     std::vector<int> Dinit;                      // per am
     std::vector<lcg::GroupItem> groups;          // pair field filled later

@@ -1,0 +1,30 @@
+// State of an lcg_engine, shared by the alignment (engine.cu) and the
+// partition-function (engine_pf.cu) entry points.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstddef>
+
+struct lcg_engine_s {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int sms = 0;
+    char *d_arena = nullptr;
+    size_t arena_cap = 0;
+    char *h_stage = nullptr;
+    size_t stage_cap = 0;
+    int *d_scratch = nullptr;
+    size_t scratch_cap = 0;  // ints
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr;
+    double last_ms = 0, last_fill_ms = 0, last_trace_ms = 0;
+    long long last_launches = 0;
+    long long last_h2d = 0, last_d2h = 0;
+    long long last_groups = 0, last_cells = 0, last_terms = -1, last_visits = -1;
+    bool counting = false;
+    void *pf = nullptr;  // partition-function state (engine_pf.cu)
+};
+
+namespace lcg_host {
+void pf_release(lcg_engine_s *e);
+}

@@ -426,6 +426,8 @@ struct lcg_prepared_s {
     std::string seq_a, seq_b, name_a, name_b;
     std::vector<int32_t> sigma, gap_a, gap_b, arcs_a, arcs_b, am_arcs, am_score, min_col, max_col;
     std::vector<double> arc_p_a, arc_p_b;
+    std::vector<int8_t> code_a, code_b;  // 0..3 for A,C,G,U, -1 otherwise; index 1..len
+    std::vector<double> am_dsw;          // d am_score / d struct_weight, unrounded
     int32_t indel_opening = 0, exclusion = 0;
     int envelope_ok = 1;
 };
@@ -578,6 +580,7 @@ lcg_status lcg_prepare_pair(const char *pp_a, const char *pp_b, const lcg_prep_o
                 P->am_arcs.push_back((int32_t)ia);
                 P->am_arcs.push_back((int32_t)ib);
                 P->am_score.push_back((int32_t)s);
+                P->am_dsw.push_back((1 - log(a.p) / log(peA)) + (1 - log(b.p) / log(peB)));
             }
         }
         for (auto &a : A.arcs) {
@@ -590,6 +593,10 @@ lcg_status lcg_prepare_pair(const char *pp_a, const char *pp_b, const lcg_prep_o
             P->arcs_b.push_back(b.r);
             P->arc_p_b.push_back(b.p);
         }
+        P->code_a.assign(n + 1, -1);
+        P->code_b.assign(m + 1, -1);
+        for (int i = 1; i <= n; ++i) P->code_a[i] = (int8_t)idx_acgu(A.in.seq[i - 1]);
+        for (int j = 1; j <= m; ++j) P->code_b[j] = (int8_t)idx_acgu(B.in.seq[j - 1]);
         P->min_col.resize(n + 1);
         P->max_col.resize(n + 1);
         for (int i = 0; i <= n; ++i) {
@@ -648,6 +655,17 @@ const char *lcg_prepared_sequence(lcg_prepared p, int32_t which) {
 }
 
 int32_t lcg_prepared_envelope_ok(lcg_prepared p) { return p ? p->envelope_ok : 0; }
+
+lcg_status lcg_prepared_grad_spec(lcg_prepared p, lcg_pf_grad_spec *out) {
+    if (!p || !out) {
+        lcg_host::set_error("NULL argument");
+        return LCG_ERR_ARG;
+    }
+    out->code_a = p->code_a.data();
+    out->code_b = p->code_b.data();
+    out->am_dscore_dsw = p->am_dsw.data();
+    return LCG_OK;
+}
 
 lcg_status lcg_prepared_free(lcg_prepared p) {
     delete p;

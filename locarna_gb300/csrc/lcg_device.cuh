@@ -56,7 +56,7 @@ struct PairDev {
     const int4 *rowinfo;  // n+2: (min_col, max_col, gapA, bandoff) of row i
     const int *match_lo, *match_hi, *del_lo, *del_hi, *ins_lo, *ins_hi;
     const int *cre_start; // bandcells+1: arc matches with right ends at a band cell
-    const int2 *cre;      // (am index, (a.l<<16)|b.l), lex-greater-left-ends order
+    const int4 *cre;      // (am, a.l-1, b.l-1, b.r), lex-greater-left-ends order
     int *D;               // num_am
     const int4 *am_ends;  // per am: a.l, a.r, b.l, b.r
     const int *am_score;  // per am

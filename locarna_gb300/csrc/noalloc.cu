@@ -37,7 +37,7 @@ namespace lcg {
 cudaError_t launch_fill(const PairDev *, const GroupItem *, int, const int4 *, int *, long long, int,
                         unsigned int *, int *, int *, int, cudaStream_t, unsigned long long *);
 int fill_warps_per_block();
-cudaError_t fill_occupancy(int sw, int *blocks_per_sm);
+cudaError_t fill_occupancy(int sw, bool counting, int *blocks_per_sm);
 }  // namespace lcg
 
 using namespace lcg;
@@ -125,7 +125,7 @@ extern "C" lcg_status lcg_align_score_static(const lcg_pair_tables *pair, const 
     const size_t o_row = take(16ull * (n + 2));
     const size_t o_anc = anch ? take(4ull * (4 * (n + 1) + 2 * (m + 1))) : 0;
     const size_t o_cs = take(4ull * (p.bandcells + 1));
-    const size_t o_cre = take(4ull * std::max<size_t>(p.cre.size(), 2));
+    const size_t o_cre = take(4ull * std::max<size_t>(p.cre.size(), 4));
     const size_t o_ends = take(4ull * std::max<size_t>(p.am_ends.size(), 4));
     const size_t o_score = take(4ull * std::max(na, 1));
     const size_t o_D = take(4ull * std::max(na, 1));
@@ -133,7 +133,7 @@ extern "C" lcg_status lcg_align_score_static(const lcg_pair_tables *pair, const 
     const size_t fixed = off;
     const long long stride = (long long)rows_max * sw;  // ints per warp slot
     int blocks_per_sm = 0;
-    STATIC_TRY(fill_occupancy(sw, &blocks_per_sm));
+    STATIC_TRY(fill_occupancy(sw, false, &blocks_per_sm));
     int sms = 0;
     STATIC_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     const size_t per_block = (size_t)fill_warps_per_block() * (size_t)stride * sizeof(int);
@@ -178,7 +178,7 @@ extern "C" lcg_status lcg_align_score_static(const lcg_pair_tables *pair, const 
         d.ins_hi = a + 4 * (n + 1) + (m + 1);
     }
     d.cre_start = (const int *)(base + o_cs);
-    d.cre = (const int2 *)(base + o_cre);
+    d.cre = (const int4 *)(base + o_cre);
     d.D = (int *)(base + o_D);
     d.am_ends = (const int4 *)(base + o_ends);
     d.am_score = (const int *)(base + o_score);

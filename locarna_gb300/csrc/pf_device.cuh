@@ -1,0 +1,57 @@
+// Device-side records of the LocARNA-P engine shared by the kernels
+// (pf_kernels.cu) and the host side (engine_pf.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+namespace lcg {
+
+// NOT_READY pattern of a D entry that a group has yet to write (a NaN that no
+// arithmetic produces).
+constexpr long long PF_NOT_READY_F64 = 0x7ff4c0de00000000ll;
+constexpr int PF_NOT_READY_F32 = 0x7fa0c0de;
+
+template <typename T>
+struct PFPair {
+    int n, m;
+    int num_am;
+    const int4 *rowinfo;   // n+2: (min_col, max_col, -, band offset)
+    const int *cre_start;  // band cells + 1
+    const int4 *cre;       // (am, a.l-1, b.l-1, b.r)
+    const T *bm;           // (n+1)(m+1) scaled base-match weights
+    const T *gA, *gB;      // scaled gap weights
+    T o;                   // gap-opening weight
+    T inv_s;               // 1 / pf_scale
+    T arcf;                // pf_scale / c^4
+    const T *w;            // per am: arc-match weight
+    T *D;                  // per am, NOT_READY pattern until written
+    T *Dbar;               // per am: dZ'/dD (backward)
+    int *cnt;              // per am: number of uses still to be back-propagated
+    T *topM;               // (n+1)(m+1)
+    T *bmacc;              // per band cell (row offset rowinfo.w): sum of X_bar M(i-1,j-1) bm (backward)
+    double *res;           // [0] log Z', [1] gap-extension uses, [2] gap-opening uses
+};
+
+template <typename T>
+struct PFItem {
+    int pair;
+    int al, ar, bl, br;
+    int dw_start, dw_count;  // int4 (am, ar-1, br-1, -), ar ascending
+    int top;
+};
+
+
+template <typename T>
+cudaError_t pf_launch_fwd(const void *pairs, const void *items, int nitems, const int4 *dw, void *scratch,
+                          long long stride, int sw, unsigned int *qhead, int *status, int *abort_flag,
+                          int blocks, bool count_uses, cudaStream_t st);
+template <typename T>
+cudaError_t pf_launch_back(const void *pairs, const void *items, int nitems, const int4 *dw, void *scratch,
+                           long long stride, int sw, unsigned int *qhead, int *status, int *abort_flag,
+                           int blocks, cudaStream_t st);
+template <typename T>
+cudaError_t pf_fwd_occupancy(int sw, int *blocks_per_sm);
+template <typename T>
+cudaError_t pf_back_occupancy(int sw, int *blocks_per_sm);
+int pf_warps_per_block();
+
+}  // namespace lcg

@@ -68,7 +68,7 @@ __device__ __forceinline__ int wait_D(int *D, int k, int *status, volatile int *
 // until the first a.l <= al, one entry ahead.
 template <int NCH, bool TOP, bool WAIT, bool DWRITE, bool COUNT>
 __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, int *__restrict__ Mg,
-                            int pitch, int prev_o, int cur_o, int E_o, int gB_o,
+                            int pitch, int prev_o, int cur_o, int E_o, int gB_o, int A_o,
                             const int4 *__restrict__ dw, int ndw, bool globalA, bool globalB,
                             bool local_top, int *status, volatile int *abort_flag, TopOut *tout,
                             unsigned long long *counters) {
@@ -77,7 +77,7 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
     const int4 *__restrict__ rowinfo = P.rowinfo;
     const int *__restrict__ sigma = P.sigma;
     const int *__restrict__ cre_start = P.cre_start;
-    const int2 *__restrict__ cre = P.cre;
+    const int4 *__restrict__ cre = P.cre;
     int *const Dp = P.D;
     const bool anch = (P.flags & PF_ANCHORS) != 0;
     const int m1 = P.m + 1;
@@ -86,6 +86,7 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
     const int W = br - bl;
     int *const E = lcg_smem + E_o;
     int *const gBs = lcg_smem + gB_o;
+    int *const Aslot = lcg_smem + A_o;  // per-lane arc-term maxima of the current chunk
     int pv = prev_o, cu = cur_o;  // shared-memory offsets of the previous / current row
 #define PREV(c) lcg_smem[pv + (c)]
 #define CUR(c) lcg_smem[cu + (c)]
@@ -195,6 +196,7 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
                 q1 = cre_start[cb + j + 1];
             }
             int X = NEG;
+            const int qend = q1;
             if (act) {
                 const bool mok = !anch || a_match(P, i, j);
                 const bool dok = !anch || a_del(P, i, j);
@@ -203,27 +205,45 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
                 e = norm(e);
                 E[c] = e;
                 X = max(d, e);
-                if (!mok) q1 = q;
-            } else {
-                q1 = q;
             }
-            // arc-match terms: candidates (a,b) with right ends (i,j), sorted
-            // by a.l descending; valid while a.l > al, and when b.l > bl
-            int2 en = make_int2(0, 0);
-            if (q < q1) en = cre[q];
-            while (q < q1) {
-                const int2 cur_en = en;
-                if (q + 1 < q1) en = cre[q + 1];
-                ++q;
-                const int alq = cur_en.y >> 16, blq = cur_en.y & 0xffff;
-                if (COUNT) ++n_visits;
-                if (alq <= al) break;
-                if (blq <= bl) continue;
-                if (COUNT) ++n_terms;
-                int dv = WAIT ? ld_volatile(Dp + cur_en.x) : Dp[cur_en.x];
-                const int mv = Mg[(alq - 1 - al) * pitch + (blq - 1 - bl)];
-                if (WAIT && dv == NOT_READY) dv = wait_D(Dp, cur_en.x, status, abort_flag);
-                X = max(X, mv + dv);
+            // arc-match terms: max over candidates (a,b) with right ends (i,j),
+            // a.l > al, b.l > bl, of M(a.l-1,b.l-1) + D(a,b). The candidates of
+            // the chunk's cells are one contiguous range of the band-cell CSR;
+            // the warp reads it 32 entries at a time and reduces each term into
+            // its cell's slot with a shared-memory atomicMax.
+            {
+                const unsigned mokm = __ballot_sync(0xffffffffu, act && (!anch || a_match(P, i, j)));
+                const int last = min(base + 31, hi) - base;
+                const int Qs = __shfl_sync(0xffffffffu, q, 0);
+                int qe_l = __shfl_sync(0xffffffffu, act ? qend : 0, last);
+                Aslot[lane] = NEG;
+                __syncwarp();
+                for (int e0 = Qs; e0 < qe_l; e0 += 64) {
+                    int4 en[2];
+                    bool ok[2];
+#pragma unroll
+                    for (int u = 0; u < 2; ++u) {
+                        const int e = e0 + 32 * u + lane;
+                        en[u] = e < qe_l ? cre[e] : make_int4(0, -1, -1, base);
+                        ok[u] = e < qe_l && en[u].y >= al && en[u].z >= bl && ((mokm >> (en[u].w - base)) & 1u);
+                        if (COUNT && e < qe_l) ++n_visits;
+                        if (COUNT && ok[u]) ++n_terms;
+                    }
+                    int dv[2], mv[2];
+#pragma unroll
+                    for (int u = 0; u < 2; ++u) dv[u] = ok[u] ? (WAIT ? ld_volatile(Dp + en[u].x) : Dp[en[u].x]) : 0;
+#pragma unroll
+                    for (int u = 0; u < 2; ++u) mv[u] = ok[u] ? Mg[(en[u].y - al) * pitch + (en[u].z - bl)] : 0;
+#pragma unroll
+                    for (int u = 0; u < 2; ++u) {
+                        if (ok[u]) {
+                            if (WAIT && dv[u] == NOT_READY) dv[u] = wait_D(Dp, en[u].x, status, abort_flag);
+                            atomicMax(&Aslot[en[u].w - base], mv[u] + dv[u]);
+                        }
+                    }
+                }
+                __syncwarp();
+                X = max(X, Aslot[lane]);
             }
             if (TOP && local_top && act && i < la && j < lb) X = max(X, 0);
             // horizontal gaps: max-plus scan of F(j) = max(F(j-1)+a_j, b_j)
@@ -311,11 +331,11 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
 template <bool TOP, bool WAIT, bool DWRITE, bool COUNT = false>
 __device__ __forceinline__ void run_group(const PairDev &P, int cpl, int al, int ar, int bl, int br,
                                           int *__restrict__ Mg, int pitch, int prev, int cur,
-                                          int E, int gBs, const int4 *__restrict__ dw, int ndw,
+                                          int E, int gBs, int Aslot, const int4 *__restrict__ dw, int ndw,
                                           bool globalA, bool globalB, bool local_top, int *status,
                                           volatile int *abort_flag, TopOut *tout,
                                           unsigned long long *counters = nullptr) {
-    run_group_c<4, TOP, WAIT, DWRITE, COUNT>(P, al, ar, bl, br, Mg, pitch, prev, cur, E, gBs, dw, ndw,
+    run_group_c<4, TOP, WAIT, DWRITE, COUNT>(P, al, ar, bl, br, Mg, pitch, prev, cur, E, gBs, Aslot, dw, ndw,
                                              globalA, globalB, local_top, status, abort_flag, tout,
                                              counters);
 }
@@ -339,7 +359,7 @@ static __device__ __forceinline__ void warp_argmax(int &v, int &k1, int &k2) {
 // top level + final argmax: align_top_level_free_endgaps (aligner.cc:736-819)
 // and align_top_level_locally (aligner.cc:823-880)
 template <bool COUNT>
-__device__ __forceinline__ void run_top(const PairDev &P, int cpl, int prev, int cur, int E, int gBs,
+__device__ __forceinline__ void run_top(const PairDev &P, int cpl, int prev, int cur, int E, int gBs, int Aslot,
                                      int *status, volatile int *abort_flag,
                                      unsigned long long *counters) {
     const int lane = threadIdx.x & 31;
@@ -349,7 +369,7 @@ __device__ __forceinline__ void run_top(const PairDev &P, int cpl, int prev, int
     TopOut to;
     if (local) {
         run_group<true, true, false, COUNT>(P, cpl, 0, n + 1, 0, m + 1, P.topM, m1, prev, cur, E,
-                                            gBs, nullptr, 0, false, false, true, status, abort_flag,
+                                            gBs, Aslot, nullptr, 0, false, false, true, status, abort_flag,
                                             &to, counters);
         int v = to.best, i = to.bi, j = to.bj;
         if (v <= 0) {
@@ -371,7 +391,7 @@ __device__ __forceinline__ void run_top(const PairDev &P, int cpl, int prev, int
         return;
     }
     run_group<true, true, false, COUNT>(P, cpl, 0, n + 1, 0, m + 1, P.topM, m1, prev, cur, E, gBs,
-                                        nullptr, 0, !(fe & 4), !(fe & 1), false, status, abort_flag,
+                                        Aslot, nullptr, 0, !(fe & 4), !(fe & 1), false, status, abort_flag,
                                         &to, counters);
     __syncwarp();
     if (!(fe & (2 | 8))) {
@@ -521,8 +541,8 @@ static __device__ __noinline__ void walk(Walker &w, const int *Mg, int pitch, in
         if (!(a_match(P, i, j) && w.valid(i - 1, j - 1))) return;
         const int cell = P.bandoff[i] + j - P.min_col[i];
         for (int q = P.cre_start[cell]; q < P.cre_start[cell + 1]; ++q) {
-            const int2 ent = P.cre[q];
-            const int alq = ent.y >> 16, blq = ent.y & 0xffff;
+            const int4 ent = P.cre[q];
+            const int alq = ent.y + 1, blq = ent.z + 1;
             if (alq <= al || blq <= bl) continue;
             if (Mij == MM(alq - 1, blq - 1) + P.D[ent.x]) {
                 w.emit(i, j);

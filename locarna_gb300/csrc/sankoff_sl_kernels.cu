@@ -181,8 +181,8 @@ __device__ void run_group_sl(const PairDev &P, int al, int ar, int bl, int br, i
                     const int cell = cell0 + j;
                     const int q1 = P.cre_start[cell + 1];
                     for (int q = P.cre_start[cell]; q < q1; ++q) {
-                        const int2 ent = P.cre[q];
-                        const int alq = ent.y >> 16, blq = ent.y & 0xffff;
+                        const int4 ent = P.cre[q];
+                        const int alq = ent.y + 1, blq = ent.z + 1;
                         if (alq <= al) break;
                         if (blq <= bl) continue;
                         const int dv = WAIT ? wait_D(P.D, ent.x, status, abort_flag) : P.D[ent.x];
@@ -318,8 +318,8 @@ __global__ void __launch_bounds__(SL_FILL_WARPS * 32)
         const PairDev &P = pairs[it.pair];
         if (it.top) {
             const int base = (int)(sm - smem);
-            run_top<false>(P, it.cpl, base, base + sw, base + 2 * sw, base + 3 * sw, status, abort_flag,
-                           nullptr);
+            run_top<false>(P, it.cpl, base, base + sw, base + 2 * sw, base + 3 * sw, base + 4 * sw, status,
+                           abort_flag, nullptr);
         } else {
             run_group_sl<true, true, 4>(P, it.al, it.ar, it.bl, it.br, Mg, scratch_stride, sw, sm, sw,
                                         dw + it.dw_start, it.dw_count, status, abort_flag);
@@ -443,8 +443,8 @@ static __device__ __noinline__ void walk_sl(Walker &w, const int *Mg, long long 
         if (!(a_match(P, i, j) && w.valid(i - 1, j - 1))) return;
         const int cell = P.bandoff[i] + j - P.min_col[i];
         for (int q = P.cre_start[cell]; q < P.cre_start[cell + 1]; ++q) {
-            const int2 ent = P.cre[q];
-            const int alq = ent.y >> 16, blq = ent.y & 0xffff;
+            const int4 ent = P.cre[q];
+            const int alq = ent.y + 1, blq = ent.z + 1;
             if (alq <= al || blq <= bl) continue;
             if (Mij == MS(state, alq - 1, blq - 1) + P.D[ent.x]) {
                 w.emit(i, j);

@@ -7,8 +7,10 @@ This is a thin mirror of the C entry points: ``Engine.align_pairs`` is
 import ctypes as C
 import os
 
+import numpy as np
+
 from .abi import (ResultBuffers, lcg_align_opts, lcg_align_result, lcg_pair_tables,
-                  lcg_work_counts, make_opts)
+                  lcg_pf_grad_spec, lcg_pf_opts, lcg_pf_result, lcg_work_counts, make_opts)
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_build", "liblocarna_gb300.so")
@@ -51,6 +53,15 @@ def load_library(path=LIB_PATH):
     lib.lcg_engine_last_work.restype = C.c_int32
     lib.lcg_measure_int_peak.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_double)]
     lib.lcg_measure_int_peak.restype = C.c_int32
+    lib.lcg_pf_opts_default.argtypes = [C.POINTER(lcg_pf_opts)]
+    lib.lcg_pf_opts_default.restype = None
+    lib.lcg_pf_forward.argtypes = [C.c_void_p, C.POINTER(lcg_pair_tables), C.c_int32, C.POINTER(lcg_pf_opts),
+                                   C.POINTER(lcg_pf_grad_spec), C.POINTER(C.c_double)]
+    lib.lcg_pf_forward.restype = C.c_int32
+    lib.lcg_pf_backward.argtypes = [C.c_void_p, C.POINTER(lcg_pf_grad_spec), C.POINTER(lcg_pf_result)]
+    lib.lcg_pf_backward.restype = C.c_int32
+    lib.lcg_pf_last_timing.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    lib.lcg_pf_last_timing.restype = C.c_int32
     _lib = lib
     return lib
 
@@ -138,3 +149,79 @@ class Engine:
         g = C.c_double()
         _check(self.lib, self.lib.lcg_measure_int_peak(self.h, int(bool(dpx)), C.byref(g)))
         return g.value
+
+    # ------------------------------------------------------------ LocARNA-P
+
+    def pf_opts(self, temperature=300.0, pf_scale=1.0, precision=64, param_delta=None):
+        o = lcg_pf_opts()
+        self.lib.lcg_pf_opts_default(C.byref(o))
+        o.temperature, o.pf_scale, o.precision = float(temperature), float(pf_scale), int(precision)
+        if param_delta is not None:
+            for k, v in enumerate(param_delta):
+                o.param_delta[k] = float(v)
+        return o
+
+    @staticmethod
+    def _specs(tables):
+        """lcg_pf_grad_spec array from PairTables carrying code_a/code_b/am_dsw
+        (prepare_pair sets them); None when a table lacks them."""
+        if not all(hasattr(t, "code_a") for t in tables):
+            return None, None
+        keep = []
+        arr = (lcg_pf_grad_spec * len(tables))()
+        for k, t in enumerate(tables):
+            ca = np.ascontiguousarray(t.code_a, dtype=np.int8)
+            cb = np.ascontiguousarray(t.code_b, dtype=np.int8)
+            dsw = np.ascontiguousarray(t.am_dsw, dtype=np.float64) if getattr(t, "am_dsw", None) is not None else None
+            keep += [ca, cb, dsw]
+            arr[k].code_a = ca.ctypes.data_as(C.POINTER(C.c_int8))
+            arr[k].code_b = cb.ctypes.data_as(C.POINTER(C.c_int8))
+            arr[k].am_dscore_dsw = (dsw.ctypes.data_as(C.POINTER(C.c_double))
+                                    if dsw is not None and dsw.size else None)
+        return arr, keep
+
+    def pf_forward(self, tables, temperature=300.0, pf_scale=1.0, precision=64, param_delta=None):
+        """lcg_pf_forward: log Z of each pair (numpy float64 array)."""
+        o = self.pf_opts(temperature, pf_scale, precision, param_delta)
+        n = len(tables)
+        arr = (lcg_pair_tables * n)(*[t.to_c() for t in tables])
+        specs, keep = self._specs(tables)
+        out = np.zeros(n, dtype=np.float64)
+        self._pf_tables = (arr, tables, specs, keep)
+        _check(self.lib, self.lib.lcg_pf_forward(self.h, arr, n, C.byref(o), specs,
+                                                 out.ctypes.data_as(C.POINTER(C.c_double))))
+        return out
+
+    def pf_backward(self, probs=True):
+        """lcg_pf_backward for the last pf_forward: one dict per pair with
+        log_z, am_prob, bm_prob ((n+1) x (m+1)), expected gap counts and the
+        derivatives of log Z."""
+        arr, tables, specs, _ = self._pf_tables
+        n = len(tables)
+        res = (lcg_pf_result * n)()
+        bufs = []
+        for k, t in enumerate(tables):
+            am = np.zeros(max(1, t.num_arcmatches))
+            bm = np.zeros((t.len_a + 1) * (t.len_b + 1))
+            bufs.append((am, bm))
+            if probs:
+                res[k].am_prob = am.ctypes.data_as(C.POINTER(C.c_double))
+                res[k].bm_prob = bm.ctypes.data_as(C.POINTER(C.c_double))
+        _check(self.lib, self.lib.lcg_pf_backward(self.h, specs, res))
+        out = []
+        for k, t in enumerate(tables):
+            r = res[k]
+            d = dict(log_z=r.log_z, gap_ext_uses=r.gap_ext_uses, gap_open_uses=r.gap_open_uses,
+                     dlogz_dindel=r.dlogz_dindel, dlogz_dindel_opening=r.dlogz_dindel_opening,
+                     dlogz_dstruct_weight=r.dlogz_dstruct_weight,
+                     dlogz_dbasematch=np.array(list(r.dlogz_dbasematch)))
+            if probs:
+                d["am_prob"] = bufs[k][0][:t.num_arcmatches]
+                d["bm_prob"] = bufs[k][1].reshape(t.len_a + 1, t.len_b + 1)
+            out.append(d)
+        return out
+
+    def pf_last_timing(self):
+        a, b = C.c_double(), C.c_double()
+        _check(self.lib, self.lib.lcg_pf_last_timing(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value

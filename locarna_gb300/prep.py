@@ -7,7 +7,7 @@ import ctypes as C
 
 import numpy as np
 
-from .abi import LCG_FREE_LEFT_1, PairTables, lcg_pair_tables
+from .abi import LCG_FREE_LEFT_1, PairTables, lcg_pair_tables, lcg_pf_grad_spec
 from .engine import LcgError, load_library
 
 
@@ -41,6 +41,8 @@ def _lib():
         lib.lcg_prepared_envelope_ok.argtypes = [C.c_void_p]
         lib.lcg_prepared_envelope_ok.restype = C.c_int32
         lib.lcg_prepared_free.argtypes = [C.c_void_p]
+        lib.lcg_prepared_grad_spec.argtypes = [C.c_void_p, C.POINTER(lcg_pf_grad_spec)]
+        lib.lcg_prepared_grad_spec.restype = C.c_int32
         lib.lcg_prepared_free.restype = C.c_int32
         _ready = True
     return lib
@@ -94,6 +96,12 @@ def prepare_pair(pp_a, pp_b, **kw):
         pt.name_a = lib.lcg_prepared_sequence(h, 2).decode()
         pt.name_b = lib.lcg_prepared_sequence(h, 3).decode()
         pt.envelope_ok = bool(lib.lcg_prepared_envelope_ok(h))
+        g = lcg_pf_grad_spec()
+        if lib.lcg_prepared_grad_spec(h, C.byref(g)) == 0:
+            pt.code_a = np.ctypeslib.as_array(g.code_a, shape=(n + 1,)).copy()
+            pt.code_b = np.ctypeslib.as_array(g.code_b, shape=(m + 1,)).copy()
+            pt.am_dsw = (np.ctypeslib.as_array(g.am_dscore_dsw, shape=(nam,)).copy() if nam
+                         else np.zeros(0))
         return pt
     finally:
         lib.lcg_prepared_free(h)

@@ -36,3 +36,29 @@ def test_abi_version():
     lib = C.CDLL(build_engine())
     lib.lcg_abi_version.restype = C.c_int32
     assert lib.lcg_abi_version() == 1
+
+
+def test_ctypes_structs_match_c_layout(tmp_path):
+    """Every ctypes mirror in locarna_gb300.abi has the size and field offsets
+    the C compiler gives the header's struct of the same name."""
+    import subprocess
+
+    from locarna_gb300 import abi
+    structs = {name: cls for name, cls in vars(abi).items()
+               if name.startswith("lcg_") and isinstance(cls, type) and issubclass(cls, C.Structure)}
+    assert "lcg_pf_opts" in structs and "lcg_pair_tables" in structs
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "locarna_gb300.h"', "int main(void) {"]
+    for name, cls in sorted(structs.items()):
+        lines.append(f'printf("{name} %zu\\n", sizeof({name}));')
+        for f in cls._fields_:
+            lines.append(f'printf("{name}.{f[0]} %zu\\n", offsetof({name}, {f[0]}));')
+    lines.append("return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.check_call(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)])
+    got = dict(l.split() for l in subprocess.check_output([str(exe)], text=True).splitlines())
+    for name, cls in structs.items():
+        assert int(got[name]) == C.sizeof(cls), name
+        for f in cls._fields_:
+            assert int(got[f"{name}.{f[0]}"]) == getattr(cls, f[0]).offset, (name, f[0])
