@@ -185,6 +185,29 @@ lcg_status prep_pair(const lcg_pair_tables &t, const lcg_align_opts &o, Prep &p)
         p.cre[4 * q + 2] = p.am_ends[4 * k + 2] - 1;  // b.l - 1: column of the inner corner
         p.cre[4 * q + 3] = p.am_ends[4 * k + 3];      // b.r: the cell's column
     }
+    // the same candidates per row a.r: a.l descending, then b.l descending
+    // (within a row, the valid ones for a group (al,bl) with a.l > al are a prefix)
+    std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) {
+        const int *ex = &p.am_ends[4 * x], *ey = &p.am_ends[4 * y];
+        if (ex[1] != ey[1]) return ex[1] < ey[1];
+        if (ex[0] != ey[0]) return ex[0] > ey[0];
+        if (ex[2] != ey[2]) return ex[2] > ey[2];
+        return ex[3] < ey[3];
+    });
+    p.crow.resize(4 * ord.size());
+    p.rowarc.assign(2 * (size_t)(n + 2), 0);
+    for (size_t q = 0; q < ord.size(); ++q) {
+        int k = ord[q];
+        p.crow[4 * q] = k;
+        p.crow[4 * q + 1] = p.am_ends[4 * k] - 1;
+        p.crow[4 * q + 2] = p.am_ends[4 * k + 2] - 1;
+        p.crow[4 * q + 3] = p.am_ends[4 * k + 3];
+    }
+    for (size_t q = 0, r = 0; r <= (size_t)n + 1; ++r) {
+        p.rowarc[2 * r] = (int)q;
+        while (q < ord.size() && (size_t)p.am_ends[4 * ord[q] + 1] == r) ++q;
+        p.rowarc[2 * r + 1] = (int)q;
+    }
 
     // left-end groups (aligner.cc:660-732): bucket arc matches by (al,bl)
     std::vector<std::pair<long long, int>> byleft(na);
@@ -408,18 +431,7 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
 
     // ---- host preparation (threads over pairs)
     std::vector<Prep> prep(npairs);
-    {
-        std::atomic<int> next(0);
-        int nth = (int)std::min<unsigned>(std::max(1u, std::thread::hardware_concurrency()), (unsigned)npairs);
-        nth = std::min(nth, 64);
-        auto work = [&]() {
-            for (int q; (q = next.fetch_add(1)) < npairs;) prep_pair(pairs[q], *opts, prep[q]);
-        };
-        std::vector<std::thread> th;
-        for (int t = 1; t < nth; ++t) th.emplace_back(work);
-        work();
-        for (auto &t : th) t.join();
-    }
+    lcg_host::parallel_for(npairs, [&](int q) { prep_pair(pairs[q], *opts, prep[q]); });
     for (int q = 0; q < npairs; ++q)
         if (prep[q].code != LCG_OK) return fail(prep[q].code, "pair " + std::to_string(q) + ": " + prep[q].err);
 
@@ -430,7 +442,7 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
         rows_max = std::max(rows_max, p.rows_max + 1);
     }
     struct Off {
-        size_t sigma, gapA, gapB, minc, maxc, bandoff, rowinfo, anc, cre_start, cre, am_ends, am_score, D,
+        size_t sigma, gapA, gapB, minc, maxc, bandoff, rowinfo, anc, cre_start, cre, crow, rowarc, am_ends, am_score, D,
             topM, res, tok, tq, segs;
     };
     std::vector<Off> off(npairs);
@@ -463,6 +475,8 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
         o.anc = t.match_lo ? take(up, 4ull * (2 * (p.n + 1) + 2 * (p.n + 1) + 2 * (p.m + 1))) : 0;
         o.cre_start = take(up, 4ull * (p.bandcells + 1));
         o.cre = take(up, 4ull * std::max<size_t>(p.cre.size(), 4));
+        o.crow = take(up, 4ull * std::max<size_t>(p.crow.size(), 4));
+        o.rowarc = take(up, 4ull * p.rowarc.size());
         o.am_ends = take(up, 4ull * std::max<size_t>(p.am_ends.size(), 4));
         o.am_score = take(up, 4ull * std::max(t.num_arcmatches, 1));
         o.D = take(up, 4ull * std::max(t.num_arcmatches, 1));
@@ -535,7 +549,7 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
         }
     }
     std::memset(H + off_ctrl, 0, 64);
-    for (int q = 0; q < npairs; ++q) {
+    lcg_host::parallel_for(npairs, [&](int q) {
         const auto &p = prep[q];
         const auto &t = pairs[q];
         const Off &o = off[q];
@@ -557,6 +571,8 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
         }
         std::memcpy(H + o.cre_start, p.cre_start.data(), 4ull * (p.bandcells + 1));
         if (!p.cre.empty()) std::memcpy(H + o.cre, p.cre.data(), 4ull * p.cre.size());
+        if (!p.crow.empty()) std::memcpy(H + o.crow, p.crow.data(), 4ull * p.crow.size());
+        std::memcpy(H + o.rowarc, p.rowarc.data(), 4ull * p.rowarc.size());
         if (!p.am_ends.empty()) std::memcpy(H + o.am_ends, p.am_ends.data(), 4ull * p.am_ends.size());
         if (t.num_arcmatches) {
             std::memcpy(H + o.am_score, t.am_score, 4ull * t.num_arcmatches);
@@ -595,6 +611,8 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
         }
         d.cre_start = (const int *)(Dv + o.cre_start);
         d.cre = (const int4 *)(Dv + o.cre);
+        d.crow = (const int4 *)(Dv + o.crow);
+        d.rowarc = (const int2 *)(Dv + o.rowarc);
         d.D = (int *)(Dv + o.D);
         d.am_ends = (const int4 *)(Dv + o.am_ends);
         d.am_score = (const int *)(Dv + o.am_score);
@@ -605,7 +623,7 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
         d.tq = (int *)(Dv + o.tq);
         d.tq_cap = p.tq_cap;
         d.segs = (int4 *)(Dv + o.segs);
-    }
+    });
 
     // ---- scratch
     const bool sl = opts->struct_local != 0;

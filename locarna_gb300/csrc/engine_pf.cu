@@ -120,18 +120,7 @@ lcg_status pf_forward_t(lcg_engine e, PFState *S, const lcg_pair_tables *pairs, 
     const double pf_scale = o->pf_scale > 0 ? o->pf_scale : 1.0;
     lcg_align_opts ao{0, 0, 0, 0};
     std::vector<lcg_host::Prep> prep(npairs);
-    {
-        std::atomic<int> next(0);
-        int nth = (int)std::min<unsigned>(std::max(1u, std::thread::hardware_concurrency()), (unsigned)npairs);
-        nth = std::min(nth, 64);
-        auto work = [&]() {
-            for (int q; (q = next.fetch_add(1)) < npairs;) lcg_host::prep_pair(pairs[q], ao, prep[q]);
-        };
-        std::vector<std::thread> th;
-        for (int t = 1; t < nth; ++t) th.emplace_back(work);
-        work();
-        for (auto &t : th) t.join();
-    }
+    lcg_host::parallel_for(npairs, [&](int q) { lcg_host::prep_pair(pairs[q], ao, prep[q]); });
     bool need_spec = false;
     for (int k = 2; k < 19; ++k) need_spec |= o->param_delta[k] != 0.0;
     if (need_spec && !specs) return pf_fail(LCG_ERR_ARG, "param_delta[2..18] needs grad specs");
@@ -315,18 +304,7 @@ lcg_status pf_forward_t(lcg_engine e, PFState *S, const lcg_pair_tables *pairs, 
         d.bmacc = (T *)(Dv + L.bmacc);
         d.res = (double *)(Dv + L.res);
     };
-    {
-        std::atomic<int> next(0);
-        int nth = (int)std::min<unsigned>(std::max(1u, std::thread::hardware_concurrency()), (unsigned)npairs);
-        nth = std::min(nth, 64);
-        auto work = [&]() {
-            for (int q; (q = next.fetch_add(1)) < npairs;) pack(q);
-        };
-        std::vector<std::thread> th;
-        for (int k = 1; k < nth; ++k) th.emplace_back(work);
-        work();
-        for (auto &x : th) x.join();
-    }
+    lcg_host::parallel_for(npairs, pack);
     // scratch: forward one rectangle per warp, backward four
     int bf = 0, bb = 0;
     PF_TRY(pf_fwd_occupancy<T>(sw, &bf));

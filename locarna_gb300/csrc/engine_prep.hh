@@ -3,7 +3,10 @@
 // structures the kernels read (band offsets, candidate lists by right-end
 // cell, left-end groups in dependency order, D-write lists).
 #pragma once
+#include <algorithm>
+#include <atomic>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/locarna_gb300.h"
@@ -20,6 +23,8 @@ struct Prep {
     int maxband = 0;
     std::vector<int> cre_start;                  // bandcells+1
     std::vector<int> cre;                        // 4 per entry: am, a.l-1, b.l-1, b.r
+    std::vector<int> crow;                       // the same entries by row a.r, a.l desc, b.l desc
+    std::vector<int> rowarc;                     // 2 per row 0..n+1: [start, end) in crow
     std::vector<int> am_ends;                    // 4 per am
     std::vector<int> Dinit;                      // per am
     std::vector<lcg::GroupItem> groups;          // pair field filled later
@@ -36,5 +41,21 @@ struct Prep {
 lcg_status prep_pair(const lcg_pair_tables &t, const lcg_align_opts &o, Prep &p);
 
 void set_error(const std::string &msg);
+
+// fn(q) for q in [0, n) on up to 64 host threads (dynamic assignment)
+template <typename F>
+void parallel_for(int n, F &&fn) {
+    if (n <= 0) return;
+    std::atomic<int> next(0);
+    int nth = (int)std::min<unsigned>(std::max(1u, std::thread::hardware_concurrency()), (unsigned)n);
+    nth = std::min(nth, 64);
+    auto work = [&]() {
+        for (int q; (q = next.fetch_add(1)) < n;) fn(q);
+    };
+    std::vector<std::thread> th;
+    for (int t = 1; t < nth; ++t) th.emplace_back(work);
+    work();
+    for (auto &t : th) t.join();
+}
 
 }  // namespace lcg_host

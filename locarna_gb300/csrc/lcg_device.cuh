@@ -57,6 +57,8 @@ struct PairDev {
     const int *match_lo, *match_hi, *del_lo, *del_hi, *ins_lo, *ins_hi;
     const int *cre_start; // bandcells+1: arc matches with right ends at a band cell
     const int4 *cre;      // (am, a.l-1, b.l-1, b.r), lex-greater-left-ends order
+    const int4 *crow;     // the same entries by row a.r, then a.l descending, b.l descending
+    const int2 *rowarc;   // n+2: [start, end) of row i's entries in crow
     int *D;               // num_am
     const int4 *am_ends;  // per am: a.l, a.r, b.l, b.r
     const int *am_score;  // per am

@@ -126,6 +126,8 @@ extern "C" lcg_status lcg_align_score_static(const lcg_pair_tables *pair, const 
     const size_t o_anc = anch ? take(4ull * (4 * (n + 1) + 2 * (m + 1))) : 0;
     const size_t o_cs = take(4ull * (p.bandcells + 1));
     const size_t o_cre = take(4ull * std::max<size_t>(p.cre.size(), 4));
+    const size_t o_crow = take(4ull * std::max<size_t>(p.crow.size(), 4));
+    const size_t o_rowarc = take(4ull * p.rowarc.size());
     const size_t o_ends = take(4ull * std::max<size_t>(p.am_ends.size(), 4));
     const size_t o_score = take(4ull * std::max(na, 1));
     const size_t o_D = take(4ull * std::max(na, 1));
@@ -179,6 +181,8 @@ extern "C" lcg_status lcg_align_score_static(const lcg_pair_tables *pair, const 
     }
     d.cre_start = (const int *)(base + o_cs);
     d.cre = (const int4 *)(base + o_cre);
+    d.crow = (const int4 *)(base + o_crow);
+    d.rowarc = (const int2 *)(base + o_rowarc);
     d.D = (int *)(base + o_D);
     d.am_ends = (const int4 *)(base + o_ends);
     d.am_score = (const int *)(base + o_score);
@@ -213,6 +217,8 @@ extern "C" lcg_status lcg_align_score_static(const lcg_pair_tables *pair, const 
     }
     STATIC_TRY(h2d(o_cs, p.cre_start.data(), 4ull * (p.bandcells + 1)));
     STATIC_TRY(h2d(o_cre, p.cre.data(), 4ull * p.cre.size()));
+    STATIC_TRY(h2d(o_crow, p.crow.data(), 4ull * p.crow.size()));
+    STATIC_TRY(h2d(o_rowarc, p.rowarc.data(), 4ull * p.rowarc.size()));
     STATIC_TRY(h2d(o_ends, p.am_ends.data(), 4ull * p.am_ends.size()));
     STATIC_TRY(h2d(o_score, pair->am_score, 4ull * na));
     STATIC_TRY(h2d(o_D, p.Dinit.data(), 4ull * na));

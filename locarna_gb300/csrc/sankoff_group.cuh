@@ -58,15 +58,18 @@ __device__ __forceinline__ int wait_D(int *D, int k, int *status, volatile int *
 // (aligner.cc:424-437) with align_noex per cell. M of the rectangle is
 // written to Mg (row r = i-al, column c = j-bl, row pitch `pitch`).
 // Shared-memory rows (offsets into lcg_smem) hold the previous and current M
-// row, the E vector and the group's gap costs gapB, indexed by c = j-bl.
+// row, the E vector, the group's gap costs gapB and the arc-term maxima of
+// the current row, indexed by c = j-bl.
 //
-// Lanes own consecutive columns (lane-stride chunks of 32, so every shared
-// and global row access is unit-stride). Per row, the band metadata is read
-// as one int4 loaded a row ahead, and the sigma values and candidate-list
-// bounds of up to NCH chunks are loaded together before any cell of the row
-// is computed. Each cell walks its candidate list (sorted by a.l descending)
-// until the first a.l <= al, one entry ahead.
-template <int NCH, bool TOP, bool WAIT, bool DWRITE, bool COUNT>
+// Per row, the arc-match terms come first: the row's candidates (arc matches
+// with a.r = i, sorted by a.l descending) are read 32 at a time by the whole
+// warp until the first a.l <= al; each valid term M(a.l-1,b.l-1) + D(a,b) is
+// reduced into its column with a shared-memory atomicMax. Then lanes own
+// consecutive columns (chunks of 32) for the affine recursion; the horizontal
+// gap chain is a max-plus warp scan. ANCH = false drops every anchor test and
+// uses plain (non-saturating) adds: without anchors every gap term is finite,
+// so no sum can leave the int32 range.
+template <int NCH, bool ANCH, bool TOP, bool WAIT, bool DWRITE, bool COUNT>
 __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, int *__restrict__ Mg,
                             int pitch, int prev_o, int cur_o, int E_o, int gB_o, int A_o,
                             const int4 *__restrict__ dw, int ndw, bool globalA, bool globalB,
@@ -75,18 +78,17 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
     unsigned long long n_terms = 0, n_visits = 0;
     const int lane = threadIdx.x & 31;
     const int4 *__restrict__ rowinfo = P.rowinfo;
+    const int2 *__restrict__ rowarc = P.rowarc;
     const int *__restrict__ sigma = P.sigma;
-    const int *__restrict__ cre_start = P.cre_start;
-    const int4 *__restrict__ cre = P.cre;
+    const int4 *__restrict__ crow = P.crow;
     int *const Dp = P.D;
-    const bool anch = (P.flags & PF_ANCHORS) != 0;
     const int m1 = P.m + 1;
     const int go = P.go;
     const int gop = max(go, 0);
     const int W = br - bl;
     int *const E = lcg_smem + E_o;
     int *const gBs = lcg_smem + gB_o;
-    int *const Aslot = lcg_smem + A_o;  // per-lane arc-term maxima of the current chunk
+    int *const Arow = lcg_smem + A_o;  // arc-term maxima of the current row
     int pv = prev_o, cu = cur_o;  // shared-memory offsets of the previous / current row
 #define PREV(c) lcg_smem[pv + (c)]
 #define CUR(c) lcg_smem[cu + (c)]
@@ -103,7 +105,7 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
         for (int base = bl + 1; base < L0; base += 32) {
             int j = base + lane;
             bool act = j < L0;
-            bool blk = act && anch && !a_ins(P, al, j);
+            bool blk = ANCH && act && !a_ins(P, al, j);
             int s = (act && globalB) ? P.gapB[j] : 0;
             unsigned bm = __ballot_sync(0xffffffffu, blk);
 #pragma unroll
@@ -138,34 +140,56 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
     int best = TOP ? 0 : NEG, bi = 0, bj = 0;  // sequence-local argmax (aligner.cc:865-875)
     const int la = P.la, lb = P.lb, ra = P.ra, rb = P.rb;
     int4 rnxt = rowinfo[min(al + 1, P.n + 1)];
+    int2 anxt = rowarc[min(al + 1, P.n + 1)];
 
     for (int i = al + 1; i < ar; ++i) {
         const int4 rcur = rnxt;
+        const int2 acur = anxt;
         rnxt = rowinfo[min(i + 1, P.n + 1)];
+        anxt = rowarc[min(i + 1, P.n + 1)];
         const int minc = rcur.x;
         const int gAi = rcur.z;
         const int lo = max(bl + 1, minc);
         const int hi = min(br - 1, rcur.y);
         const int *srow = sigma + (size_t)i * m1;
-        const int cb = rcur.w - minc;  // band cell index of (i,j) = cb + j
-        // loads of the first NCH chunks of the row, issued before any use
-        int sgv[NCH], q0v[NCH], q1v[NCH];
+        // sigma of the first NCH chunks of the row, issued before any use
+        int sgv[NCH];
 #pragma unroll
         for (int k = 0; k < NCH; ++k) {
             const int j = lo + 32 * k + lane;
-            sgv[k] = 0;
-            q0v[k] = 0;
-            q1v[k] = 0;
-            if (j <= hi) {
-                sgv[k] = srow[j];
-                q0v[k] = cre_start[cb + j];
-                q1v[k] = cre_start[cb + j + 1];
-            }
+            sgv[k] = j <= hi ? srow[j] : 0;
         }
+        // ---- arc-match terms of row i into Arow[lo-bl .. hi-bl]
+        bool rowarcs = false;
+        for (int e0 = acur.x; e0 < acur.y; e0 += 32) {
+            const int e = e0 + lane;
+            const int4 en = e < acur.y ? crow[e] : make_int4(0, -1, -1, 0);
+            const bool okA = en.y >= al;  // a.l > al
+            const unsigned ballA = __ballot_sync(0xffffffffu, okA);
+            if (ballA == 0u) break;
+            if (!rowarcs) {
+                for (int c = lo - bl + lane; c <= hi - bl; c += 32) Arow[c] = NEG;
+                __syncwarp();
+                rowarcs = true;
+            }
+            const bool ok = okA && en.z >= bl && en.w >= lo && en.w <= hi;
+            if (COUNT) {
+                n_visits += okA;
+                n_terms += ok;
+            }
+            if (ok) {
+                int dv = WAIT ? ld_volatile(Dp + en.x) : Dp[en.x];
+                const int mv = Mg[(en.y - al) * pitch + (en.z - bl)];
+                if (WAIT && dv == NOT_READY) dv = wait_D(Dp, en.x, status, abort_flag);
+                atomicMax(&Arow[en.w - bl], mv + dv);
+            }
+            if (ballA != 0xffffffffu) break;
+        }
+        __syncwarp();
         int B;  // M(i, lo-1)
         if (minc <= bl) {
             if (!colblocked) {
-                if (anch && !a_del(P, i, bl)) colblocked = true;
+                if (ANCH && !a_del(P, i, bl)) colblocked = true;
                 else if (globalA) colval += gAi;
             }
             B = colblocked ? NEG : colval;
@@ -181,69 +205,21 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
             const int j = base + lane;
             const bool act = j <= hi;
             const int c = j - bl;
-            int sgx = 0, q = 0, q1 = 0;
+            int sgx = 0;
 #pragma unroll
-            for (int kk = 0; kk < NCH; ++kk) {
-                if (k == kk) {
-                    sgx = sgv[kk];
-                    q = q0v[kk];
-                    q1 = q1v[kk];
-                }
-            }
-            if (k >= NCH && act) {
-                sgx = srow[j];
-                q = cre_start[cb + j];
-                q1 = cre_start[cb + j + 1];
-            }
+            for (int kk = 0; kk < NCH; ++kk)
+                if (k == kk) sgx = sgv[kk];
+            if (k >= NCH && act) sgx = srow[j];
             int X = NEG;
-            const int qend = q1;
             if (act) {
-                const bool mok = !anch || a_match(P, i, j);
-                const bool dok = !anch || a_del(P, i, j);
-                int d = mok ? PREV(c - 1) + sgx : NEG;
-                int e = dok ? max(E[c] + gAi, PREV(c) + gAi + go) : NEG;
+                const bool mok = !ANCH || a_match(P, i, j);
+                const bool dok = !ANCH || a_del(P, i, j);
+                const int d = mok ? PREV(c - 1) + sgx : NEG;
+                int e = dok ? __viaddmax_s32(E[c], gAi, PREV(c) + gAi + go) : NEG;
                 e = norm(e);
                 E[c] = e;
                 X = max(d, e);
-            }
-            // arc-match terms: max over candidates (a,b) with right ends (i,j),
-            // a.l > al, b.l > bl, of M(a.l-1,b.l-1) + D(a,b). The candidates of
-            // the chunk's cells are one contiguous range of the band-cell CSR;
-            // the warp reads it 32 entries at a time and reduces each term into
-            // its cell's slot with a shared-memory atomicMax.
-            {
-                const unsigned mokm = __ballot_sync(0xffffffffu, act && (!anch || a_match(P, i, j)));
-                const int last = min(base + 31, hi) - base;
-                const int Qs = __shfl_sync(0xffffffffu, q, 0);
-                int qe_l = __shfl_sync(0xffffffffu, act ? qend : 0, last);
-                Aslot[lane] = NEG;
-                __syncwarp();
-                for (int e0 = Qs; e0 < qe_l; e0 += 64) {
-                    int4 en[2];
-                    bool ok[2];
-#pragma unroll
-                    for (int u = 0; u < 2; ++u) {
-                        const int e = e0 + 32 * u + lane;
-                        en[u] = e < qe_l ? cre[e] : make_int4(0, -1, -1, base);
-                        ok[u] = e < qe_l && en[u].y >= al && en[u].z >= bl && ((mokm >> (en[u].w - base)) & 1u);
-                        if (COUNT && e < qe_l) ++n_visits;
-                        if (COUNT && ok[u]) ++n_terms;
-                    }
-                    int dv[2], mv[2];
-#pragma unroll
-                    for (int u = 0; u < 2; ++u) dv[u] = ok[u] ? (WAIT ? ld_volatile(Dp + en[u].x) : Dp[en[u].x]) : 0;
-#pragma unroll
-                    for (int u = 0; u < 2; ++u) mv[u] = ok[u] ? Mg[(en[u].y - al) * pitch + (en[u].z - bl)] : 0;
-#pragma unroll
-                    for (int u = 0; u < 2; ++u) {
-                        if (ok[u]) {
-                            if (WAIT && dv[u] == NOT_READY) dv[u] = wait_D(Dp, en[u].x, status, abort_flag);
-                            atomicMax(&Aslot[en[u].w - base], mv[u] + dv[u]);
-                        }
-                    }
-                }
-                __syncwarp();
-                X = max(X, Aslot[lane]);
+                if (rowarcs && mok) X = max(X, Arow[c]);
             }
             if (TOP && local_top && act && i < la && j < lb) X = max(X, 0);
             // horizontal gaps: max-plus scan of F(j) = max(F(j-1)+a_j, b_j)
@@ -251,24 +227,29 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
             if (lane == 0) Xp = Xc;
             int a = 0, b = NEG;
             if (act) {
-                if (!anch || a_ins(P, i, j)) {
+                if (!ANCH || a_ins(P, i, j)) {
                     const int gb = gBs[c];
                     a = gb + gop;
-                    b = addc(Xp, gb + go);
+                    b = ANCH ? addc(Xp, gb + go) : Xp + gb + go;
                 } else {
                     a = NEG;
                 }
             }
 #pragma unroll
             for (int off = 1; off < 32; off <<= 1) {
-                int a1 = __shfl_up_sync(0xffffffffu, a, off);
-                int b1 = __shfl_up_sync(0xffffffffu, b, off);
+                const int a1 = __shfl_up_sync(0xffffffffu, a, off);
+                const int b1 = __shfl_up_sync(0xffffffffu, b, off);
                 if (lane >= off) {
-                    b = max(addc(b1, a), b);
-                    a = addc(a1, a);
+                    if (ANCH) {
+                        b = max(addc(b1, a), b);
+                        a = addc(a1, a);
+                    } else {
+                        b = __viaddmax_s32(b1, a, b);
+                        a = a1 + a;
+                    }
                 }
             }
-            const int F = max(addc(Fc, a), b);
+            const int F = ANCH ? max(addc(Fc, a), b) : __viaddmax_s32(Fc, a, b);
             const int M = norm(max(X, F));
             if (act) {
                 CUR(c) = M;
@@ -326,18 +307,24 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
     }
 }
 
-// All groups use the same routine; `cpl` (columns per lane in an earlier
-// design) is ignored.
+// All groups use the same routine, specialised for pairs without anchor
+// constraints; `cpl` (columns per lane in an earlier design) is ignored.
+// Shared memory per warp: 5 rows of sw ints from `prev`.
 template <bool TOP, bool WAIT, bool DWRITE, bool COUNT = false>
 __device__ __forceinline__ void run_group(const PairDev &P, int cpl, int al, int ar, int bl, int br,
                                           int *__restrict__ Mg, int pitch, int prev, int cur,
-                                          int E, int gBs, int Aslot, const int4 *__restrict__ dw, int ndw,
+                                          int E, int gBs, int Arow, const int4 *__restrict__ dw, int ndw,
                                           bool globalA, bool globalB, bool local_top, int *status,
                                           volatile int *abort_flag, TopOut *tout,
                                           unsigned long long *counters = nullptr) {
-    run_group_c<4, TOP, WAIT, DWRITE, COUNT>(P, al, ar, bl, br, Mg, pitch, prev, cur, E, gBs, Aslot, dw, ndw,
-                                             globalA, globalB, local_top, status, abort_flag, tout,
-                                             counters);
+    if (P.flags & PF_ANCHORS)
+        run_group_c<4, true, TOP, WAIT, DWRITE, COUNT>(P, al, ar, bl, br, Mg, pitch, prev, cur, E, gBs, Arow, dw,
+                                                       ndw, globalA, globalB, local_top, status, abort_flag, tout,
+                                                       counters);
+    else
+        run_group_c<4, false, TOP, WAIT, DWRITE, COUNT>(P, al, ar, bl, br, Mg, pitch, prev, cur, E, gBs, Arow, dw,
+                                                        ndw, globalA, globalB, local_top, status, abort_flag, tout,
+                                                        counters);
 }
 
 static __device__ __forceinline__ void warp_argmax(int &v, int &k1, int &k2) {

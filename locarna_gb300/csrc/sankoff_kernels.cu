@@ -43,7 +43,7 @@ __global__ void __launch_bounds__(FILL_WARPS * 32)
                         int *abort_flag_ptr, unsigned long long *counters) {
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
-    const int prev = warp * (4 * sw + 32), cur = prev + sw, E = cur + sw, gBs = E + sw, Aslot = gBs + sw;
+    const int prev = warp * 5 * sw, cur = prev + sw, E = cur + sw, gBs = E + sw, Arow = gBs + sw;
     int *Mg = scratch + ((long long)blockIdx.x * FILL_WARPS + warp) * scratch_stride;
     volatile int *abort_flag = abort_flag_ptr;
     while (true) {
@@ -54,10 +54,10 @@ __global__ void __launch_bounds__(FILL_WARPS * 32)
         const GroupItem it = items[idx];
         const PairDev &P = pairs[it.pair];
         if (it.top) {
-            run_top<COUNT>(P, it.cpl, prev, cur, E, gBs, Aslot, status, abort_flag, counters);
+            run_top<COUNT>(P, it.cpl, prev, cur, E, gBs, Arow, status, abort_flag, counters);
         } else {
             run_group<false, true, true, COUNT>(P, it.cpl, it.al, it.ar, it.bl, it.br, Mg, sw, prev,
-                                                cur, E, gBs, Aslot, dw + it.dw_start, it.dw_count, true,
+                                                cur, E, gBs, Arow, dw + it.dw_start, it.dw_count, true,
                                                 true, false, status, abort_flag, nullptr, counters);
         }
         __syncwarp();
@@ -73,7 +73,7 @@ __global__ void __launch_bounds__(TRACE_WARPS * 32)
     if (pair >= npairs) return;
     const PairDev &P = pairs[pair];
     if (!(P.flags & PF_TRACE)) return;
-    const int prev = warp * (4 * sw + 32), cur = prev + sw, E = cur + sw, gBs = E + sw, Aslot = gBs + sw;
+    const int prev = warp * 5 * sw, cur = prev + sw, E = cur + sw, gBs = E + sw, Arow = gBs + sw;
     int *Mg = scratch + (long long)pair * scratch_stride;
     int dummy_abort = 0;
     Walker w(P);
@@ -94,7 +94,7 @@ __global__ void __launch_bounds__(TRACE_WARPS * 32)
         if (k < 0) break;
         const int4 ends = P.am_ends[k];  // a.l, a.r, b.l, b.r
         const int cpl = min(4, max(1, (min(ends.w - ends.z, P.maxband) + 31) / 32));
-        run_group<false, false, false>(P, cpl, ends.x, ends.y, ends.z, ends.w, Mg, sw, prev, cur, E, gBs, Aslot,
+        run_group<false, false, false>(P, cpl, ends.x, ends.y, ends.z, ends.w, Mg, sw, prev, cur, E, gBs, Arow,
                                        nullptr, 0, true, true, false, status,
                                        (volatile int *)&dummy_abort, nullptr);
         __syncwarp();
@@ -120,7 +120,7 @@ cudaError_t launch_fill(const PairDev *pairs, const GroupItem *items, int nitems
                         int *scratch, long long scratch_stride, int sw, unsigned int *qhead,
                         int *status, int *abort_flag, int blocks, cudaStream_t st,
                         unsigned long long *counters) {
-    size_t smem = (size_t)FILL_WARPS * (4 * sw + 32) * sizeof(int);
+    size_t smem = (size_t)FILL_WARPS * 5 * sw * sizeof(int);
     if (counters)
         sankoff_fill_kernel<true><<<blocks, FILL_WARPS * 32, smem, st>>>(
             pairs, items, nitems, dw, scratch, scratch_stride, sw, qhead, status, abort_flag,
@@ -134,7 +134,7 @@ cudaError_t launch_fill(const PairDev *pairs, const GroupItem *items, int nitems
 
 cudaError_t launch_trace(const PairDev *pairs, int npairs, int *scratch,
                          long long scratch_stride, int sw, int *status, cudaStream_t st) {
-    size_t smem = (size_t)TRACE_WARPS * (4 * sw + 32) * sizeof(int);
+    size_t smem = (size_t)TRACE_WARPS * 5 * sw * sizeof(int);
     int blocks = (npairs + TRACE_WARPS - 1) / TRACE_WARPS;
     sankoff_trace_kernel<<<blocks, TRACE_WARPS * 32, smem, st>>>(pairs, npairs, scratch,
                                                                  scratch_stride, sw, status);
@@ -145,7 +145,7 @@ int fill_warps_per_block() { return FILL_WARPS; }
 int trace_warps_per_block() { return TRACE_WARPS; }
 
 cudaError_t fill_occupancy(int sw, bool counting, int *blocks_per_sm) {
-    size_t smem = (size_t)FILL_WARPS * (4 * sw + 32) * sizeof(int);
+    size_t smem = (size_t)FILL_WARPS * 5 * sw * sizeof(int);
     const void *k = counting ? (const void *)sankoff_fill_kernel<true> : (const void *)sankoff_fill_kernel<false>;
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -155,7 +155,7 @@ cudaError_t fill_occupancy(int sw, bool counting, int *blocks_per_sm) {
 }
 
 cudaError_t trace_prepare(int sw) {
-    size_t smem = (size_t)TRACE_WARPS * (4 * sw + 32) * sizeof(int);
+    size_t smem = (size_t)TRACE_WARPS * 5 * sw * sizeof(int);
     if (smem > 48 * 1024)
         return cudaFuncSetAttribute(sankoff_trace_kernel,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
