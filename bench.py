@@ -37,6 +37,7 @@ CPU_SAMPLE_SECONDS = 20.0
 PF_WORKLOAD = dict(count=128, len_lo=80, len_hi=500, seed=2025, q=0.05)
 PF_WORKLOAD_NAME = "locarna_p_allpairs_128rnas_80-500nt"
 PF_BUCKET = 1024
+PF_STRIDE = 32  # the timed LocARNA-P sample: every PF_STRIDE-th pair in size order
 PF_CPU_SECONDS = 20.0
 
 
@@ -187,12 +188,15 @@ class ClockSampler:
 # ---------------------------------------------------------------- LocARNA-P
 
 def run_pf(eng, tables, flush_l2, cpu):
-    """LocARNA-P: FP64 and FP32-scaled inside + adjoint outside over all pairs
-    in size-sorted buckets; device and end-to-end rates, FP32 error against
-    the FP64 run of the same kernels, and one 200-nt pair with gradients."""
+    """LocARNA-P: FP64 and FP32-scaled inside + adjoint outside over a
+    size-stratified sample of the pairs (every PF_STRIDE-th pair in size
+    order) in size-sorted buckets; device and end-to-end rates, FP32 error
+    against the FP64 run of the same kernels, and one 200-nt pair with
+    gradients."""
     import numpy as np
     order = sorted(range(len(tables)), key=lambda k: tables[k].len_a * tables[k].len_b)
-    buckets = [order[i:i + PF_BUCKET] for i in range(0, len(order), PF_BUCKET)]
+    sample = order[::PF_STRIDE]
+    buckets = [sample[i:i + PF_BUCKET] for i in range(0, len(sample), PF_BUCKET)]
     for prec in (64, 32):  # warm-up: the smallest bucket
         eng.pf_forward([tables[k] for k in buckets[0]], precision=prec)
         eng.pf_backward(probs=False)
@@ -219,10 +223,13 @@ def run_pf(eng, tables, flush_l2, cpu):
             err_am, err_bm = max(err_am, ea), max(err_bm, eb)
             pair_err.append(max(ea, eb))
         del res
-    n = len(tables)
+    n = len(sample)
     pair_err.sort()
     out = {
-        "workload": PF_WORKLOAD_NAME, "pairs": n, "buckets": len(buckets), "bucket_pairs": PF_BUCKET,
+        "workload": PF_WORKLOAD_NAME, "workload_pairs": len(tables), "pairs": n,
+        "sample": f"every {PF_STRIDE}th pair of the {len(tables)} in size order (rates are pairs of this "
+                  f"size mix per second)",
+        "buckets": len(buckets), "bucket_pairs": PF_BUCKET,
         "fp64": {"pairs_per_s": n / (dev[64] / 1e3), "device_ms": dev[64], "e2e_pairs_per_s": n / wall[64]},
         "fp32": {"pairs_per_s": n / (dev[32] / 1e3), "device_ms": dev[32], "e2e_pairs_per_s": n / wall[32]},
         "fp32_over_fp64_device": dev[64] / dev[32], "fp32_over_fp64_e2e": wall[64] / wall[32],
@@ -443,14 +450,19 @@ def run_reference(args):
 
 
 def run_small_case(args):
-    """A small batch of the same kind of work, one plain run, for profiling:
-    `--case small` aligns all pairs of 32 RNAs of 100-150 nt (496 pairs)."""
+    """A smaller batch of the same kind of work, one plain run, for profiling:
+    `--case small` aligns all pairs of 32 RNAs of 100-150 nt (496 pairs),
+    `--case large` all pairs of 16 RNAs of 300-400 nt (120 pairs, the long
+    end of the workload's length range)."""
     from concurrent.futures import ThreadPoolExecutor
 
     from locarna_gb300.engine import Engine
     from locarna_gb300.prep import prepare_pair
     from locarna_gb300.synth import make_family
-    fam = make_family(32, 100, 150, 77)
+    if args.case == "large":
+        fam = make_family(16, 300, 400, 78)
+    else:
+        fam = make_family(32, 100, 150, 77)
     pp = [r.to_pp() for r in fam]
     pairs = [(a, b) for a in range(len(fam)) for b in range(a + 1, len(fam))]
     with ThreadPoolExecutor(os.cpu_count() or 4) as ex:
@@ -462,14 +474,33 @@ def run_small_case(args):
             eng.run_call(call)
         ms, nl = eng.last_stats()
         f, t = eng.last_timing()
-        print(json.dumps({"case": "small", "mode": mode, "pairs": len(tables), "kernel_ms": ms,
+        print(json.dumps({"case": args.case, "mode": mode, "pairs": len(tables), "kernel_ms": ms,
                           "fill_ms": f, "trace_ms": t, "launches": nl}), flush=True)
+    eng.close()
+
+
+def run_pf_small_case(args):
+    """A small LocARNA-P batch for profiling: `--case pf-small` runs the
+    forward and the backward pass (FP32, then FP64) once on every 256th pair
+    of the LocARNA-P workload in size order (32 pairs of 80-500 nt)."""
+    from locarna_gb300.engine import Engine
+    tables = build_pf_tables()
+    order = sorted(range(len(tables)), key=lambda k: tables[k].len_a * tables[k].len_b)
+    tb = [tables[k] for k in order[::256]]
+    eng = Engine(0)
+    for prec in (32, 64):
+        for _ in range(max(1, args.warmup)):
+            eng.pf_forward(tb, precision=prec)
+            eng.pf_backward(probs=False)
+        f, b = eng.pf_last_timing()
+        print(json.dumps({"case": "pf-small", "precision": prec, "pairs": len(tb), "forward_ms": f,
+                          "backward_ms": b}), flush=True)
     eng.close()
 
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--case", default="full", choices=["full", "small"])
+    ap.add_argument("--case", default="full", choices=["full", "small", "large", "pf-small"])
     ap.add_argument("--struct-local", action="store_true", help="small case: also struct-local")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
@@ -486,8 +517,11 @@ def main():
     from locarna_gb300.build import build_engine, build_oracle
     build_engine()
     build_oracle()
-    if args.case == "small":
+    if args.case in ("small", "large"):
         run_small_case(args)
+        return
+    if args.case == "pf-small":
+        run_pf_small_case(args)
         return
     run_ours(args)
 

@@ -8,6 +8,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -19,20 +20,7 @@
 #include "engine_prep.hh"
 #include "engine_state.hh"
 
-namespace lcg {
-cudaError_t launch_fill(const PairDev *, const GroupItem *, int, const int4 *, int *, long long,
-                        int, unsigned int *, int *, int *, int, cudaStream_t, unsigned long long *);
-cudaError_t measure_int_peak(int sms, bool dpx, cudaStream_t st, double *gops);
-cudaError_t sl_prepare(int sw, int *blocks_per_sm);
-int sl_fill_warps_per_block();
-cudaError_t launch_sl_fill(const PairDev *, const GroupItem *, int, const int4 *, int *, long long, int,
-                           unsigned int *, int *, int *, int, cudaStream_t);
-cudaError_t launch_sl_trace(const PairDev *, int, int *, long long, int, int *, cudaStream_t);
-cudaError_t launch_trace(const PairDev *, int, int *, long long, int, int *, cudaStream_t);
-int fill_warps_per_block();
-cudaError_t fill_occupancy(int sw, bool counting, int *blocks_per_sm);
-cudaError_t trace_prepare(int sw);
-}  // namespace lcg
+#include "sankoff_launch.hh"
 
 using namespace lcg;
 using lcg_host::Prep;
@@ -113,6 +101,52 @@ lcg_status prep_pair(const lcg_pair_tables &t, const lcg_align_opts &o, Prep &p)
     for (int i = 0; i <= n + 1; ++i) {
         p.rowinfo[i] = make_int4(p.min_col[i], p.max_col[i], i <= n ? t.gap_a[i] : 0, p.bandoff[i]);
         if (i <= n) p.maxband = std::max(p.maxband, p.max_col[i] - p.min_col[i] + 1);
+    }
+    for (int i = 0; i < n; ++i) p.span = std::max(p.span, p.max_col[i + 1] - p.min_col[i] + 3);
+
+    // sigma classes: identical rows share a row class, identical columns a
+    // column class; with at most 16 of each, sigma is a 16x16 table lookup
+    {
+        const size_t m1 = (size_t)m + 1;
+        std::vector<int> rep_row, rep_col;
+        p.rcls.assign(n + 2, 0);
+        p.ccls.assign(m + 1, 0);
+        bool ok = true;
+        for (int i = 1; i <= n && ok; ++i) {
+            int c = -1;
+            for (size_t k = 0; k < rep_row.size() && c < 0; ++k)
+                if (std::memcmp(t.sigma + (size_t)i * m1 + 1, t.sigma + (size_t)rep_row[k] * m1 + 1, 4 * (size_t)m) == 0)
+                    c = (int)k;
+            if (c < 0) {
+                if (rep_row.size() == 16) ok = false;
+                c = (int)rep_row.size();
+                rep_row.push_back(i);
+            }
+            p.rcls[i] = c;
+        }
+        for (int j = 1; j <= m && ok; ++j) {
+            int c = -1;
+            for (size_t k = 0; k < rep_col.size() && c < 0; ++k) {
+                bool same = true;
+                for (size_t r = 0; r < rep_row.size() && same; ++r)
+                    same = t.sigma[(size_t)rep_row[r] * m1 + j] == t.sigma[(size_t)rep_row[r] * m1 + rep_col[k]];
+                if (same) c = (int)k;
+            }
+            if (c < 0) {
+                if (rep_col.size() == 16) ok = false;
+                c = (int)rep_col.size();
+                rep_col.push_back(j);
+            }
+            p.ccls[j] = c;
+        }
+        if (ok) {
+            p.scls.assign(256, 0);
+            for (size_t r = 0; r < rep_row.size(); ++r)
+                for (size_t k = 0; k < rep_col.size(); ++k)
+                    p.scls[r * 16 + k] = t.sigma[(size_t)rep_row[r] * m1 + rep_col[k]];
+            p.use_cls = true;
+            p.flags |= PF_SCLS;
+        }
     }
     if (cells > (1ll << 30)) return bad(LCG_ERR_UNSUPPORTED, "band too large");
     p.bandcells = (int)cells;
@@ -423,6 +457,14 @@ lcg_status lcg_measure_int_peak(lcg_engine e, int32_t dpx, double *gops) {
     return LCG_OK;
 }
 
+// Bytes of per-pair tables one wave of pairs may keep hot (default 48 MB of
+// the 126 MB L2); LCG_WAVE_MB overrides it for tuning runs.
+static double wave_budget_bytes() {
+    const char *v = std::getenv("LCG_WAVE_MB");
+    const double mb = v ? std::atof(v) : 48.0;
+    return (mb > 0 ? mb : 1e9) * 1048576.0;
+}
+
 lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t npairs,
                            const lcg_align_opts *opts, lcg_align_result *results) {
     if (!e || !pairs || !opts || !results || npairs < 0) return fail(LCG_ERR_ARG, "NULL argument");
@@ -436,13 +478,15 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
         if (prep[q].code != LCG_OK) return fail(prep[q].code, "pair " + std::to_string(q) + ": " + prep[q].err);
 
     // ---- arena layout
-    int sw = 0, rows_max = 1;
+    int sw = 0, rows_max = 1, span = 2;
     for (auto &p : prep) {
         sw = std::max(sw, std::max(p.width_max + 1, p.m + 2));
         rows_max = std::max(rows_max, p.rows_max + 1);
+        span = std::max(span, p.span);
     }
     struct Off {
-        size_t sigma, gapA, gapB, minc, maxc, bandoff, rowinfo, anc, cre_start, cre, crow, rowarc, am_ends, am_score, D,
+        size_t sigma, scls, rcls, ccls, gapA, gapB, minc, maxc, bandoff, rowinfo, anc, cre_start, cre, crow, rowarc,
+            am_ends, am_score, D,
             topM, res, tok, tq, segs;
     };
     std::vector<Off> off(npairs);
@@ -465,7 +509,11 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
         const auto &p = prep[q];
         const auto &t = pairs[q];
         Off &o = off[q];
-        o.sigma = take(up, 4ull * (p.n + 1) * (p.m + 1));
+        // sigma: the class table when it exists, else the dense table
+        o.sigma = p.use_cls ? 0 : take(up, 4ull * (p.n + 1) * (p.m + 1));
+        o.scls = p.use_cls ? take(up, 4ull * 256) : 0;
+        o.rcls = p.use_cls ? take(up, 4ull * (p.n + 2)) : 0;
+        o.ccls = p.use_cls ? take(up, 4ull * (p.m + 1)) : 0;
         o.gapA = take(up, 4ull * (p.n + 1));
         o.gapB = take(up, 4ull * (p.m + 1));
         o.minc = take(up, 4ull * (p.n + 2));
@@ -525,13 +573,26 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
     int4 *hdw = (int4 *)(H + off_dw);
     size_t it = 0, dwb = 0;
     {
-        // interleave the pairs' work lists so that every pair progresses
-        // proportionally; within a pair the order is kept
+        // pairs in waves whose per-pair tables (candidate lists, D, top
+        // level) together stay within a share of L2; inside a wave the
+        // pairs' work lists are interleaved so that every pair progresses
+        // proportionally; within a pair the order is kept. Waves follow each
+        // other in the queue without a barrier.
+        const double wave_bytes = wave_budget_bytes();
         std::vector<std::pair<double, std::pair<int, int>>> order;
         order.reserve(nitems);
+        double acc = 0.0;
+        int wave = 0;
         for (int q = 0; q < npairs; ++q) {
-            size_t G = prep[q].groups.size();
-            for (size_t g = 0; g < G; ++g) order.push_back({(double)(g + 1) / (double)G, {q, (int)g}});
+            const auto &p = prep[q];
+            const double fp = 20.0 * pairs[q].num_arcmatches + 4.0 * p.bandcells;
+            if (acc > 0.0 && acc + fp > wave_bytes) {
+                ++wave;
+                acc = 0.0;
+            }
+            acc += fp;
+            size_t G = p.groups.size();
+            for (size_t g = 0; g < G; ++g) order.push_back({wave + (double)(g + 1) / (double)G, {q, (int)g}});
         }
         std::stable_sort(order.begin(), order.end(), [](const auto &a, const auto &b) { return a.first < b.first; });
         std::vector<size_t> dwbase(npairs);
@@ -553,7 +614,13 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
         const auto &p = prep[q];
         const auto &t = pairs[q];
         const Off &o = off[q];
-        std::memcpy(H + o.sigma, t.sigma, 4ull * (p.n + 1) * (p.m + 1));
+        if (p.use_cls) {
+            std::memcpy(H + o.scls, p.scls.data(), 4ull * 256);
+            std::memcpy(H + o.rcls, p.rcls.data(), 4ull * (p.n + 2));
+            std::memcpy(H + o.ccls, p.ccls.data(), 4ull * (p.m + 1));
+        } else {
+            std::memcpy(H + o.sigma, t.sigma, 4ull * (p.n + 1) * (p.m + 1));
+        }
         std::memcpy(H + o.gapA, t.gap_a, 4ull * (p.n + 1));
         std::memcpy(H + o.gapB, t.gap_b, 4ull * (p.m + 1));
         std::memcpy(H + o.minc, p.min_col.data(), 4ull * (p.n + 2));
@@ -592,7 +659,12 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
         d.rb = t.match_lo ? t.right_anchor_b : 0;
         d.num_am = t.num_arcmatches;
         d.bandcells = p.bandcells;
-        d.sigma = (const int *)(Dv + o.sigma);
+        d.sigma = p.use_cls ? nullptr : (const int *)(Dv + o.sigma);
+        if (p.use_cls) {
+            d.scls = (const int *)(Dv + o.scls);
+            d.rcls = (const int *)(Dv + o.rcls);
+            d.ccls = (const int *)(Dv + o.ccls);
+        }
         d.gapA = (const int *)(Dv + o.gapA);
         d.gapB = (const int *)(Dv + o.gapB);
         d.min_col = (const int *)(Dv + o.minc);
@@ -627,12 +699,15 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
 
     // ---- scratch
     const bool sl = opts->struct_local != 0;
+    const int rb = lcg_host::ring_size(span);
+    bool fast = true;
+    for (auto &p : prep) fast = fast && (p.flags & PF_SCLS) && !(p.flags & PF_ANCHORS);
     int blocks_per_sm = 0;
     if (sl) {
-        CUDA_TRY(sl_prepare(sw, &blocks_per_sm));
+        CUDA_TRY(sl_prepare(sw, rb, &blocks_per_sm));
     } else {
-        CUDA_TRY(fill_occupancy(sw, e->counting, &blocks_per_sm));
-        CUDA_TRY(trace_prepare(sw));
+        CUDA_TRY(fill_occupancy(rb, e->counting, fast, &blocks_per_sm));
+        CUDA_TRY(trace_prepare(rb));
     }
     if (blocks_per_sm < 1) return fail(LCG_ERR_UNSUPPORTED, "fill kernel does not fit on an SM");
     int blocks = e->sms * blocks_per_sm;
@@ -662,11 +737,11 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
     if (sl) {
         if (counters) return fail(LCG_ERR_UNSUPPORTED, "work counting covers the plain mode only");
         CUDA_TRY(launch_sl_fill((const PairDev *)(Dv + off_pairs), (const GroupItem *)(Dv + off_items),
-                                (int)nitems, (const int4 *)(Dv + off_dw), e->d_scratch, stride, sw, qhead,
+                                (int)nitems, (const int4 *)(Dv + off_dw), e->d_scratch, stride, sw, rb, qhead,
                                 status, abort_flag, blocks, st));
     } else {
         CUDA_TRY(launch_fill((const PairDev *)(Dv + off_pairs), (const GroupItem *)(Dv + off_items),
-                             (int)nitems, (const int4 *)(Dv + off_dw), e->d_scratch, stride, sw, qhead,
+                             (int)nitems, (const int4 *)(Dv + off_dw), e->d_scratch, stride, sw, rb, fast, qhead,
                              status, abort_flag, blocks, st, counters));
     }
     CUDA_TRY(cudaEventRecord(e->ev1, st));
@@ -676,7 +751,7 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
             CUDA_TRY(launch_sl_trace((const PairDev *)(Dv + off_pairs), npairs, e->d_scratch, stride, sw,
                                      status, st));
         else
-            CUDA_TRY(launch_trace((const PairDev *)(Dv + off_pairs), npairs, e->d_scratch, stride, sw, status,
+            CUDA_TRY(launch_trace((const PairDev *)(Dv + off_pairs), npairs, e->d_scratch, stride, sw, rb, status,
                                   st));
         ++launches;
     }

@@ -40,7 +40,7 @@ size_t up16(size_t x) { return (x + 15) / 16 * 16; }
 
 struct PFLayout {
     int n, m, na, bandcells;
-    size_t rowinfo, cre_start, cre, bm, gA, gB, w, D, Dbar, cnt, bmacc, res, topM;
+    size_t rowinfo, crow, rowarc, bm, gA, gB, w, D, Dbar, cnt, bmacc, res, topM;
     double log_c_total;  // (n+m) log c
 };
 
@@ -56,7 +56,7 @@ struct PFState {
     std::vector<PFLayout> lay;
     size_t off_pairs = 0, off_items = 0, off_dw = 0, off_ctrl = 0, out_begin = 0, out_end = 0, total = 0;
     size_t nitems = 0;
-    int sw = 0;
+    int sw = 0, rb = 0;
     long long stride = 0;
     bool have_forward = false;
     double fwd_ms = 0, back_ms = 0;
@@ -137,12 +137,15 @@ lcg_status pf_forward_t(lcg_engine e, PFState *S, const lcg_pair_tables *pairs, 
         return r;
     };
     size_t nitems = 0, ndw = 0;
-    int sw = 0, rows_max = 1;
+    int sw = 0, rows_max = 1, span = 2;
     for (auto &p : prep) {
         nitems += p.groups.size();
         ndw += p.dw.size();
         sw = std::max(sw, std::max(p.width_max + 1, p.m + 2));
         rows_max = std::max(rows_max, std::max(p.rows_max + 1, p.n + 1));
+        // widest column range two consecutive band rows cover (plus the
+        // cell left of the band)
+        for (int i = 0; i < p.n; ++i) span = std::max(span, p.max_col[i + 1] - p.min_col[i] + 3);
     }
     S->off_pairs = take(up, sizeof(PFPair<T>) * npairs);
     S->off_items = take(up, sizeof(PFItem<T>) * nitems);
@@ -156,8 +159,8 @@ lcg_status pf_forward_t(lcg_engine e, PFState *S, const lcg_pair_tables *pairs, 
         L.na = pairs[q].num_arcmatches;
         L.bandcells = p.bandcells;
         L.rowinfo = take(up, 16ull * (p.n + 2));
-        L.cre_start = take(up, 4ull * (p.bandcells + 1));
-        L.cre = take(up, 4ull * std::max<size_t>(p.cre.size(), 4));
+        L.crow = take(up, 4ull * std::max<size_t>(p.crow.size(), 4));
+        L.rowarc = take(up, 4ull * p.rowarc.size());
         L.bm = take(up, sizeof(T) * (p.n + 1) * (p.m + 1));
         L.gA = take(up, sizeof(T) * (p.n + 1));
         L.gB = take(up, sizeof(T) * (p.m + 1));
@@ -171,8 +174,8 @@ lcg_status pf_forward_t(lcg_engine e, PFState *S, const lcg_pair_tables *pairs, 
     for (int q = 0; q < npairs; ++q) {
         PFLayout &L = S->lay[q];
         L.res = take(up, 8ull * 4);
-        L.Dbar = take(up, sizeof(T) * std::max(L.na, 1));
-        L.bmacc = take(up, sizeof(T) * std::max(L.bandcells, 1));
+        L.Dbar = take(up, sizeof(double) * std::max(L.na, 1));
+        L.bmacc = take(up, sizeof(double) * std::max(L.bandcells, 1));
     }
     const size_t out_end = up;
     for (int q = 0; q < npairs; ++q) S->lay[q].topM = take(up, sizeof(T) * (S->lay[q].n + 1) * (S->lay[q].m + 1));
@@ -257,8 +260,8 @@ lcg_status pf_forward_t(lcg_engine e, PFState *S, const lcg_pair_tables *pairs, 
         const double c = std::exp(logc), c2 = c * c;
         L.log_c_total = logc * (n + m);
         std::memcpy(H + L0.rowinfo, p.rowinfo.data(), 16ull * (n + 2));
-        std::memcpy(H + L0.cre_start, p.cre_start.data(), 4ull * (p.bandcells + 1));
-        if (!p.cre.empty()) std::memcpy(H + L0.cre, p.cre.data(), 4ull * p.cre.size());
+        if (!p.crow.empty()) std::memcpy(H + L0.crow, p.crow.data(), 4ull * p.crow.size());
+        std::memcpy(H + L0.rowarc, p.rowarc.data(), 4ull * p.rowarc.size());
         T *hbm = (T *)(H + L0.bm);
         for (size_t k = 0; k < bm.size(); ++k) hbm[k] = (T)(bm[k] / c2);
         T *hgA = (T *)(H + L0.gA);
@@ -288,8 +291,8 @@ lcg_status pf_forward_t(lcg_engine e, PFState *S, const lcg_pair_tables *pairs, 
         d.m = m;
         d.num_am = L.na;
         d.rowinfo = (const int4 *)(Dv + L0.rowinfo);
-        d.cre_start = (const int *)(Dv + L0.cre_start);
-        d.cre = (const int4 *)(Dv + L0.cre);
+        d.crow = (const int4 *)(Dv + L0.crow);
+        d.rowarc = (const int2 *)(Dv + L0.rowarc);
         d.bm = (const T *)(Dv + L0.bm);
         d.gA = (const T *)(Dv + L0.gA);
         d.gB = (const T *)(Dv + L0.gB);
@@ -298,17 +301,18 @@ lcg_status pf_forward_t(lcg_engine e, PFState *S, const lcg_pair_tables *pairs, 
         d.arcf = (T)(pf_scale / (c2 * c2));
         d.w = (const T *)(Dv + L0.w);
         d.D = (T *)(Dv + L0.D);
-        d.Dbar = (T *)(Dv + L.Dbar);
+        d.Dbar = (double *)(Dv + L.Dbar);
         d.cnt = (int *)(Dv + L.cnt);
         d.topM = (T *)(Dv + L.topM);
-        d.bmacc = (T *)(Dv + L.bmacc);
+        d.bmacc = (double *)(Dv + L.bmacc);
         d.res = (double *)(Dv + L.res);
     };
     lcg_host::parallel_for(npairs, pack);
     // scratch: forward one rectangle per warp, backward four
     int bf = 0, bb = 0;
-    PF_TRY(pf_fwd_occupancy<T>(sw, &bf));
-    PF_TRY(pf_back_occupancy<T>(sw, &bb));
+    const int rb = lcg_host::ring_size(span);
+    PF_TRY(pf_fwd_occupancy<T>(rb, &bf));
+    PF_TRY(pf_back_occupancy<T>(rb, &bb));
     if (bf < 1 || bb < 1) return pf_fail(LCG_ERR_UNSUPPORTED, "PF kernels do not fit on an SM");
     const long long stride = (long long)rows_max * sw;
     const size_t fwd_slots = (size_t)e->sms * bf * pf_warps_per_block();
@@ -329,7 +333,7 @@ lcg_status pf_forward_t(lcg_engine e, PFState *S, const lcg_pair_tables *pairs, 
     int *abort_flag = (int *)(Dv + S->off_ctrl + 8);
     PF_TRY(cudaEventRecord(e->ev0, st));
     PF_TRY(pf_launch_fwd<T>(Dv + S->off_pairs, Dv + S->off_items, (int)nitems, (const int4 *)(Dv + S->off_dw),
-                            S->d_scratch, stride, sw, qhead, status, abort_flag, e->sms * bf, true, st));
+                            S->d_scratch, stride, sw, rb, qhead, status, abort_flag, e->sms * bf, true, st));
     PF_TRY(cudaEventRecord(e->ev1, st));
     PF_TRY(cudaMemcpyAsync(H + S->off_ctrl, Dv + S->off_ctrl, 64, cudaMemcpyDeviceToHost, st));
     for (int q = 0; q < npairs; ++q)
@@ -349,6 +353,7 @@ lcg_status pf_forward_t(lcg_engine e, PFState *S, const lcg_pair_tables *pairs, 
     S->npairs = npairs;
     S->nitems = nitems;
     S->sw = sw;
+    S->rb = rb;
     S->stride = stride;
     S->out_begin = out_begin;
     S->out_end = out_end;
@@ -363,14 +368,14 @@ lcg_status pf_backward_t(lcg_engine e, PFState *S, const lcg_pf_grad_spec *grads
     char *H = S->h_stage, *Dv = S->d_arena;
     cudaStream_t st = e->stream;
     int bb = 0;
-    PF_TRY(pf_back_occupancy<T>(S->sw, &bb));
+    PF_TRY(pf_back_occupancy<T>(S->rb, &bb));
     PF_TRY(cudaMemsetAsync(Dv + S->off_ctrl, 0, 64, st));
     unsigned int *qhead = (unsigned int *)(Dv + S->off_ctrl);
     int *status = (int *)(Dv + S->off_ctrl + 4);
     int *abort_flag = (int *)(Dv + S->off_ctrl + 8);
     PF_TRY(cudaEventRecord(e->ev1, st));
     PF_TRY(pf_launch_back<T>(Dv + S->off_pairs, Dv + S->off_items, (int)S->nitems, (const int4 *)(Dv + S->off_dw),
-                             S->d_scratch, S->stride, S->sw, qhead, status, abort_flag, e->sms * bb, st));
+                             S->d_scratch, S->stride, S->sw, S->rb, qhead, status, abort_flag, e->sms * bb, st));
     PF_TRY(cudaEventRecord(e->ev2, st));
     PF_TRY(cudaMemcpyAsync(H + S->off_ctrl, Dv + S->off_ctrl, 64, cudaMemcpyDeviceToHost, st));
     PF_TRY(cudaMemcpyAsync(H + S->out_begin, Dv + S->out_begin, S->out_end - S->out_begin, cudaMemcpyDeviceToHost, st));
@@ -391,8 +396,8 @@ lcg_status pf_backward_t(lcg_engine e, PFState *S, const lcg_pf_grad_spec *grads
         const double *res = (const double *)(H + L.res);
         const double Zs = std::exp(res[0]);  // Z in the scaled frame
         const T *D = (const T *)(H + L.D);
-        const T *Db = (const T *)(H + L.Dbar);
-        const T *acc = (const T *)(H + L.bmacc);
+        const double *Db = (const double *)(H + L.Dbar);
+        const double *acc = (const double *)(H + L.bmacc);
         const int4 *rowinfo = (const int4 *)(H + L.rowinfo);
         const lcg_pf_grad_spec *g = grads ? &grads[q] : nullptr;
         r.log_z = S->log_z[q];

@@ -21,12 +21,18 @@ struct Prep {
     std::vector<int> min_col, max_col, bandoff;  // n+2
     std::vector<int4> rowinfo;                   // n+2
     int maxband = 0;
+    int span = 2;  // max over i of max_col[i+1] - min_col[i] + 3 (ring rows of the kernels)
     std::vector<int> cre_start;                  // bandcells+1
     std::vector<int> cre;                        // 4 per entry: am, a.l-1, b.l-1, b.r
     std::vector<int> crow;                       // the same entries by row a.r, a.l desc, b.l desc
     std::vector<int> rowarc;                     // 2 per row 0..n+1: [start, end) in crow
     std::vector<int> am_ends;                    // 4 per am
     std::vector<int> Dinit;                      // per am
+    // sigma as a class table when rows and columns fall into <= 16 classes
+    // each (single sequences: one class per base): sigma(i,j) =
+    // scls[rcls[i]*16 + ccls[j]]
+    bool use_cls = false;
+    std::vector<int> scls, rcls, ccls;
     std::vector<lcg::GroupItem> groups;          // pair field filled later
     std::vector<int4> dw;                        // dw_start relative to this pair
     int rows_max = 0, width_max = 0;             // over groups
@@ -41,6 +47,10 @@ struct Prep {
 lcg_status prep_pair(const lcg_pair_tables &t, const lcg_align_opts &o, Prep &p);
 
 void set_error(const std::string &msg);
+
+// ring size of the kernels' shared-memory rows for a set of pairs: the
+// smallest multiple of 32 >= every pair's span
+inline int ring_size(int span) { return (std::max(span, 32) + 31) / 32 * 32; }
 
 // fn(q) for q in [0, n) on up to 64 host threads (dynamic assignment)
 template <typename F>

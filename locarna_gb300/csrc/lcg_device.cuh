@@ -29,6 +29,7 @@ enum PairFlags : int {
     PF_SEQU_LOCAL = 2,
     PF_ANCHORS = 4,
     PF_TRACE = 8,
+    PF_SCLS = 16,  // sigma(i,j) = scls[rcls[i] * 16 + ccls[j]] (at most 16 row / column classes)
 };
 
 // status word bits (device -> host)
@@ -48,6 +49,9 @@ struct PairDev {
     int bandcells;
     int maxband;          // widest band row (columns)
     const int *sigma;     // (n+1)*(m+1)
+    const int *scls;      // PF_SCLS: 256-entry class table of sigma
+    const int *rcls;      // PF_SCLS: n+2 row classes
+    const int *ccls;      // PF_SCLS: m+1 column classes
     const int *gapA;      // n+1
     const int *gapB;      // m+1
     const int *min_col;   // n+2 (entry n+1 = m+1 sentinel)
@@ -70,6 +74,11 @@ struct PairDev {
     int tq_cap;
     int4 *segs;           // traceback segments: (am or -1, token start, token end, 0)
 };
+
+// Scoring::basematch(i,j) from the class table or the dense table
+__device__ __forceinline__ int sigma_at(const PairDev &P, int i, int j) {
+    return (P.flags & PF_SCLS) ? P.scls[P.rcls[i] * 16 + P.ccls[j]] : P.sigma[(size_t)i * (P.m + 1) + j];
+}
 
 enum Res : int {
     R_SCORE = 0, R_MAXI, R_MAXJ, R_MINI, R_MINJ, R_NTOK, R_NSEG, R_NWORDS

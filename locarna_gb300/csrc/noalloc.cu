@@ -33,12 +33,7 @@
 #include "engine_prep.hh"
 #include "lcg_device.cuh"
 
-namespace lcg {
-cudaError_t launch_fill(const PairDev *, const GroupItem *, int, const int4 *, int *, long long, int,
-                        unsigned int *, int *, int *, int, cudaStream_t, unsigned long long *);
-int fill_warps_per_block();
-cudaError_t fill_occupancy(int sw, bool counting, int *blocks_per_sm);
-}  // namespace lcg
+#include "sankoff_launch.hh"
 
 using namespace lcg;
 
@@ -116,7 +111,10 @@ extern "C" lcg_status lcg_align_score_static(const lcg_pair_tables *pair, const 
     const size_t o_dw = take(sizeof(int4) * std::max<size_t>(p.dw.size(), 1));
     const size_t o_ctrl = take(64);
     const size_t o_res = take(4ull * R_NWORDS);
-    const size_t o_sigma = take(4ull * (n + 1) * (m + 1));
+    const size_t o_sigma = p.use_cls ? 0 : take(4ull * (n + 1) * (m + 1));
+    const size_t o_scls = p.use_cls ? take(4ull * 256) : 0;
+    const size_t o_rcls = p.use_cls ? take(4ull * (n + 2)) : 0;
+    const size_t o_ccls = p.use_cls ? take(4ull * (m + 1)) : 0;
     const size_t o_gapA = take(4ull * (n + 1));
     const size_t o_gapB = take(4ull * (m + 1));
     const size_t o_minc = take(4ull * (n + 2));
@@ -135,7 +133,9 @@ extern "C" lcg_status lcg_align_score_static(const lcg_pair_tables *pair, const 
     const size_t fixed = off;
     const long long stride = (long long)rows_max * sw;  // ints per warp slot
     int blocks_per_sm = 0;
-    STATIC_TRY(fill_occupancy(sw, false, &blocks_per_sm));
+    const int rb = lcg_host::ring_size(p.span);
+    const bool fast = (p.flags & PF_SCLS) && !(p.flags & PF_ANCHORS);
+    STATIC_TRY(fill_occupancy(rb, false, fast, &blocks_per_sm));
     int sms = 0;
     STATIC_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     const size_t per_block = (size_t)fill_warps_per_block() * (size_t)stride * sizeof(int);
@@ -163,7 +163,13 @@ extern "C" lcg_status lcg_align_score_static(const lcg_pair_tables *pair, const 
     d.num_am = na;
     d.bandcells = p.bandcells;
     d.maxband = p.maxband;
-    d.sigma = (const int *)(base + o_sigma);
+    if (p.use_cls) {
+        d.scls = (const int *)(base + o_scls);
+        d.rcls = (const int *)(base + o_rcls);
+        d.ccls = (const int *)(base + o_ccls);
+    } else {
+        d.sigma = (const int *)(base + o_sigma);
+    }
     d.gapA = (const int *)(base + o_gapA);
     d.gapB = (const int *)(base + o_gapB);
     d.min_col = (const int *)(base + o_minc);
@@ -199,7 +205,13 @@ extern "C" lcg_status lcg_align_score_static(const lcg_pair_tables *pair, const 
     STATIC_TRY(h2d(o_dw, p.dw.data(), sizeof(int4) * p.dw.size()));
     STATIC_TRY(cudaMemsetAsync(base + o_ctrl, 0, 64, s));
     STATIC_TRY(cudaMemsetAsync(base + o_res, 0, 4ull * R_NWORDS, s));
-    STATIC_TRY(h2d(o_sigma, pair->sigma, 4ull * (n + 1) * (m + 1)));
+    if (p.use_cls) {
+        STATIC_TRY(h2d(o_scls, p.scls.data(), 4ull * 256));
+        STATIC_TRY(h2d(o_rcls, p.rcls.data(), 4ull * (n + 2)));
+        STATIC_TRY(h2d(o_ccls, p.ccls.data(), 4ull * (m + 1)));
+    } else {
+        STATIC_TRY(h2d(o_sigma, pair->sigma, 4ull * (n + 1) * (m + 1)));
+    }
     STATIC_TRY(h2d(o_gapA, pair->gap_a, 4ull * (n + 1)));
     STATIC_TRY(h2d(o_gapB, pair->gap_b, 4ull * (m + 1)));
     STATIC_TRY(h2d(o_minc, p.min_col.data(), 4ull * (n + 2)));
@@ -224,7 +236,7 @@ extern "C" lcg_status lcg_align_score_static(const lcg_pair_tables *pair, const 
     STATIC_TRY(h2d(o_D, p.Dinit.data(), 4ull * na));
 
     STATIC_TRY(launch_fill((const PairDev *)(base + o_pair), (const GroupItem *)(base + o_items),
-                           (int)p.groups.size(), (const int4 *)(base + o_dw), scratch, stride, sw,
+                           (int)p.groups.size(), (const int4 *)(base + o_dw), scratch, stride, sw, rb, fast,
                            (unsigned int *)(base + o_ctrl), (int *)(base + o_ctrl + 4),
                            (int *)(base + o_ctrl + 8), (int)blocks, s, nullptr));
     int ctrl[4] = {0, 0, 0, 0};

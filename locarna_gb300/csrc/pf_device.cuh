@@ -15,8 +15,8 @@ struct PFPair {
     int n, m;
     int num_am;
     const int4 *rowinfo;   // n+2: (min_col, max_col, -, band offset)
-    const int *cre_start;  // band cells + 1
-    const int4 *cre;       // (am, a.l-1, b.l-1, b.r)
+    const int4 *crow;      // (am, a.l-1, b.l-1, b.r) by row a.r, a.l descending
+    const int2 *rowarc;    // n+2: [start, end) of row i's entries in crow
     const T *bm;           // (n+1)(m+1) scaled base-match weights
     const T *gA, *gB;      // scaled gap weights
     T o;                   // gap-opening weight
@@ -24,10 +24,10 @@ struct PFPair {
     T arcf;                // pf_scale / c^4
     const T *w;            // per am: arc-match weight
     T *D;                  // per am, NOT_READY pattern until written
-    T *Dbar;               // per am: dZ'/dD (backward)
+    double *Dbar;          // per am: dZ'/dD (backward), accumulated in FP64
     int *cnt;              // per am: number of uses still to be back-propagated
     T *topM;               // (n+1)(m+1)
-    T *bmacc;              // per band cell (row offset rowinfo.w): sum of X_bar M(i-1,j-1) bm (backward)
+    double *bmacc;         // per band cell (row offset rowinfo.w): sum of X_bar M(i-1,j-1) bm, FP64
     double *res;           // [0] log Z', [1] gap-extension uses, [2] gap-opening uses
 };
 
@@ -42,16 +42,18 @@ struct PFItem {
 
 template <typename T>
 cudaError_t pf_launch_fwd(const void *pairs, const void *items, int nitems, const int4 *dw, void *scratch,
-                          long long stride, int sw, unsigned int *qhead, int *status, int *abort_flag,
+                          long long stride, int pitch, int rb, unsigned int *qhead, int *status, int *abort_flag,
                           int blocks, bool count_uses, cudaStream_t st);
 template <typename T>
 cudaError_t pf_launch_back(const void *pairs, const void *items, int nitems, const int4 *dw, void *scratch,
-                           long long stride, int sw, unsigned int *qhead, int *status, int *abort_flag,
+                           long long stride, int pitch, int rb, unsigned int *qhead, int *status, int *abort_flag,
                            int blocks, cudaStream_t st);
+// rb: ring size of the shared-memory rows (a power of two above the span of
+// any two consecutive band rows)
 template <typename T>
-cudaError_t pf_fwd_occupancy(int sw, int *blocks_per_sm);
+cudaError_t pf_fwd_occupancy(int rb, int *blocks_per_sm);
 template <typename T>
-cudaError_t pf_back_occupancy(int sw, int *blocks_per_sm);
+cudaError_t pf_back_occupancy(int rb, int *blocks_per_sm);
 int pf_warps_per_block();
 
 }  // namespace lcg

@@ -17,7 +17,13 @@ extern __shared__ int lcg_smem[];
 #ifndef LCG_FILL_WARPS
 #define LCG_FILL_WARPS 8
 #endif
+#ifndef LCG_FILL_MIN_BLOCKS
+#define LCG_FILL_MIN_BLOCKS 4
+#endif
 constexpr int FILL_WARPS = LCG_FILL_WARPS;  // warps per block of the fill kernel
+// shared ints per warp of the row sweep for ring size rb (see run_group)
+__host__ __device__ inline int smem_warp_ints(int rb) { return 5 * rb + 256; }
+constexpr int FILL_MIN_BLOCKS = LCG_FILL_MIN_BLOCKS;  // resident blocks per SM the register budget targets
 constexpr int TRACE_WARPS = 4;  // warps per block of the trace kernel
 constexpr long long SPIN_LIMIT = 1ll << 22;  // ~ seconds of polling, then ST_TIMEOUT
 
@@ -69,9 +75,9 @@ __device__ __forceinline__ int wait_D(int *D, int k, int *status, volatile int *
 // gap chain is a max-plus warp scan. ANCH = false drops every anchor test and
 // uses plain (non-saturating) adds: without anchors every gap term is finite,
 // so no sum can leave the int32 range.
-template <int NCH, bool ANCH, bool TOP, bool WAIT, bool DWRITE, bool COUNT>
+template <int NCH, bool ANCH, bool SCLS, bool TOP, bool WAIT, bool DWRITE, bool COUNT>
 __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, int *__restrict__ Mg,
-                            int pitch, int prev_o, int cur_o, int E_o, int gB_o, int A_o,
+                            int pitch, int sbase, int ringn,
                             const int4 *__restrict__ dw, int ndw, bool globalA, bool globalB,
                             bool local_top, int *status, volatile int *abort_flag, TopOut *tout,
                             unsigned long long *counters) {
@@ -85,17 +91,18 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
     const int m1 = P.m + 1;
     const int go = P.go;
     const int gop = max(go, 0);
-    const int W = br - bl;
-    int *const E = lcg_smem + E_o;
-    int *const gBs = lcg_smem + gB_o;
-    int *const Arow = lcg_smem + A_o;  // arc-term maxima of the current row
-    int pv = prev_o, cu = cur_o;  // shared-memory offsets of the previous / current row
-#define PREV(c) lcg_smem[pv + (c)]
-#define CUR(c) lcg_smem[cu + (c)]
-    for (int c = lane; c < W; c += 32) {
-        E[c] = NEG;
-        gBs[c] = P.gapB[bl + c];
-    }
+    const unsigned rmagic = 0xFFFFFFFFu / (unsigned)ringn + 1u;  // j / ringn = umulhi(j, rmagic), j < 2^20
+    int *const E = lcg_smem + sbase + 2 * ringn;
+    int *const gBs = lcg_smem + sbase + 3 * ringn;   // gapB(j) << 4 | sigma column class (SCLS)
+    int *const Arow = lcg_smem + sbase + 4 * ringn;  // arc-term maxima of the current row
+    int *const Stab = lcg_smem + sbase + 5 * ringn;  // SCLS: 16 x 16 sigma class table
+    int pv = sbase, cu = sbase + ringn;  // shared-memory offsets of the previous / current row
+#define RG(j) ((j) - ringn * (int)__umulhi((unsigned)(j), rmagic))
+#define PREV(j) lcg_smem[pv + RG(j)]
+#define CUR(j) lcg_smem[cu + RG(j)]
+    for (int c = lane; c < ringn; c += 32) E[c] = NEG;
+    if (SCLS)
+        for (int k = lane; k < 256; k += 32) Stab[k] = P.scls[k];
 
     // ---- row al: M(al,bl)=0, M(al,j) = prefix of gap costs, -inf once blocked
     const int L0 = min(br, rowinfo[al].y + 1);
@@ -106,7 +113,11 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
             int j = base + lane;
             bool act = j < L0;
             bool blk = ANCH && act && !a_ins(P, al, j);
-            int s = (act && globalB) ? P.gapB[j] : 0;
+            const int gbj = act ? P.gapB[j] : 0;
+            if (act) {
+                gBs[RG(j)] = gbj * 16 + (SCLS ? P.ccls[j] : 0);
+            }
+            int s = globalB ? gbj : 0;
             unsigned bm = __ballot_sync(0xffffffffu, blk);
 #pragma unroll
             for (int off = 1; off < 32; off <<= 1) {
@@ -116,20 +127,23 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
             bool anyblk = blocked_carry || (bm & (0xffffffffu >> (31 - lane)));
             int val = anyblk ? NEG : carry + s;
             if (act) {
-                PREV(j - bl) = val;
+                PREV(j) = val;
                 Mg[j - bl] = val;
             }
             carry += __shfl_sync(0xffffffffu, s, 31);
             blocked_carry = blocked_carry || bm != 0;
         }
         if (lane == 0) {
-            PREV(0) = 0;
+            PREV(bl) = 0;
             Mg[0] = 0;
         }
         // cells above the band of row al+1 (aligner.cc:361-367)
         if (al + 1 < ar) {
             int L1 = min(br, rowinfo[al + 1].y + 1);
-            for (int j = L0 + lane; j < L1; j += 32) PREV(j - bl) = NEG;
+            for (int j = L0 + lane; j < L1; j += 32) {
+                PREV(j) = NEG;
+                gBs[RG(j)] = P.gapB[j] * 16 + (SCLS ? P.ccls[j] : 0);
+            }
         }
     }
     __syncwarp();
@@ -141,23 +155,29 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
     const int la = P.la, lb = P.lb, ra = P.ra, rb = P.rb;
     int4 rnxt = rowinfo[min(al + 1, P.n + 1)];
     int2 anxt = rowarc[min(al + 1, P.n + 1)];
+    int cnxt = SCLS ? P.rcls[min(al + 1, P.n + 1)] : 0;
 
     for (int i = al + 1; i < ar; ++i) {
         const int4 rcur = rnxt;
         const int2 acur = anxt;
+        const int rcl16 = cnxt * 16;  // SCLS: row class of row i
         rnxt = rowinfo[min(i + 1, P.n + 1)];
         anxt = rowarc[min(i + 1, P.n + 1)];
+        if (SCLS) cnxt = P.rcls[min(i + 1, P.n + 1)];
         const int minc = rcur.x;
         const int gAi = rcur.z;
         const int lo = max(bl + 1, minc);
         const int hi = min(br - 1, rcur.y);
         const int *srow = sigma + (size_t)i * m1;
         // sigma of the first NCH chunks of the row, issued before any use
-        int sgv[NCH];
+        // (dense table only)
+        int sgv[SCLS ? 1 : NCH];
+        if (!SCLS) {
 #pragma unroll
-        for (int k = 0; k < NCH; ++k) {
-            const int j = lo + 32 * k + lane;
-            sgv[k] = j <= hi ? srow[j] : 0;
+            for (int k = 0; k < NCH; ++k) {
+                const int j = lo + 32 * k + lane;
+                sgv[k] = j <= hi ? srow[j] : 0;
+            }
         }
         // ---- arc-match terms of row i into Arow[lo-bl .. hi-bl]
         bool rowarcs = false;
@@ -168,7 +188,7 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
             const unsigned ballA = __ballot_sync(0xffffffffu, okA);
             if (ballA == 0u) break;
             if (!rowarcs) {
-                for (int c = lo - bl + lane; c <= hi - bl; c += 32) Arow[c] = NEG;
+                for (int j = lo + lane; j <= hi; j += 32) Arow[RG(j)] = NEG;
                 __syncwarp();
                 rowarcs = true;
             }
@@ -181,7 +201,7 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
                 int dv = WAIT ? ld_volatile(Dp + en.x) : Dp[en.x];
                 const int mv = Mg[(en.y - al) * pitch + (en.z - bl)];
                 if (WAIT && dv == NOT_READY) dv = wait_D(Dp, en.x, status, abort_flag);
-                atomicMax(&Arow[en.w - bl], mv + dv);
+                atomicMax(&Arow[RG(en.w)], mv + dv);
             }
             if (ballA != 0xffffffffu) break;
         }
@@ -197,29 +217,33 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
         } else {
             B = NEG;
         }
-        if (lane == 0 && lo - 1 - bl < W) CUR(lo - 1 - bl) = B;
+        if (lane == 0) CUR(lo - 1) = B;
         int *Mrow = Mg + (i - al) * pitch - bl;
         int Fc = NEG, Xc = B;
         int k = 0;
         for (int base = lo; base <= hi; base += 32, ++k) {
             const int j = base + lane;
             const bool act = j <= hi;
-            const int c = j - bl;
+            const int gbc = act ? gBs[RG(j)] : 0;  // gap cost << 4 | sigma column class
             int sgx = 0;
+            if (SCLS) {
+                if (act) sgx = Stab[rcl16 + (gbc & 15)];
+            } else {
 #pragma unroll
-            for (int kk = 0; kk < NCH; ++kk)
-                if (k == kk) sgx = sgv[kk];
-            if (k >= NCH && act) sgx = srow[j];
+                for (int kk = 0; kk < NCH; ++kk)
+                    if (k == kk) sgx = sgv[kk];
+                if (k >= NCH && act) sgx = srow[j];
+            }
             int X = NEG;
             if (act) {
                 const bool mok = !ANCH || a_match(P, i, j);
                 const bool dok = !ANCH || a_del(P, i, j);
-                const int d = mok ? PREV(c - 1) + sgx : NEG;
-                int e = dok ? __viaddmax_s32(E[c], gAi, PREV(c) + gAi + go) : NEG;
+                const int d = mok ? PREV(j - 1) + sgx : NEG;
+                int e = dok ? __viaddmax_s32(E[RG(j)], gAi, PREV(j) + gAi + go) : NEG;
                 e = norm(e);
-                E[c] = e;
+                E[RG(j)] = e;
                 X = max(d, e);
-                if (rowarcs && mok) X = max(X, Arow[c]);
+                if (rowarcs && mok) X = max(X, Arow[RG(j)]);
             }
             if (TOP && local_top && act && i < la && j < lb) X = max(X, 0);
             // horizontal gaps: max-plus scan of F(j) = max(F(j-1)+a_j, b_j)
@@ -228,7 +252,7 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
             int a = 0, b = NEG;
             if (act) {
                 if (!ANCH || a_ins(P, i, j)) {
-                    const int gb = gBs[c];
+                    const int gb = gbc >> 4;
                     a = gb + gop;
                     b = ANCH ? addc(Xp, gb + go) : Xp + gb + go;
                 } else {
@@ -252,7 +276,7 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
             const int F = ANCH ? max(addc(Fc, a), b) : __viaddmax_s32(Fc, a, b);
             const int M = norm(max(X, F));
             if (act) {
-                CUR(c) = M;
+                CUR(j) = M;
                 Mrow[j] = M;
                 if (TOP && local_top && i >= ra && j >= rb && M > best) {
                     best = M;
@@ -271,24 +295,32 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
                 int4 e = make_int4(0, -1, 0, 0);
                 if (q < ndw) e = dw[q];
                 const bool mine = q < ndw && e.y == i;
-                if (mine) st_volatile(Dp + e.x, norm(CUR(e.z - bl) + e.w));
+                if (mine) st_volatile(Dp + e.x, norm(CUR(e.z) + e.w));
                 const int cnt = __popc(__ballot_sync(0xffffffffu, mine));
                 dwp += cnt;
                 if (cnt < 32) break;
             }
         }
         if (i + 1 < ar) {
+            // columns entering the band with row i+1: M above them is -inf,
+            // their E starts at -inf, their gap cost is staged
             const int Ln = min(br, rnxt.y + 1);
-            for (int j = max(hi + 1, bl + 1) + lane; j < Ln; j += 32) CUR(j - bl) = NEG;
+            for (int j = max(hi + 1, bl + 1) + lane; j < Ln; j += 32) {
+                CUR(j) = NEG;
+                E[RG(j)] = NEG;
+                gBs[RG(j)] = P.gapB[j] * 16 + (SCLS ? P.ccls[j] : 0);
+            }
         }
         __syncwarp();
         const int tp = pv;
         pv = cu;
         cu = tp;
-        if (WAIT && *abort_flag) return;
+        // no per-row poll of the abort flag: every wait polls it, and the
+        // dequeue loop stops on it after the group
     }
 #undef PREV
 #undef CUR
+#undef RG
     if (TOP) {
         tout->best = best;
         tout->bi = bi;
@@ -309,22 +341,36 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
 
 // All groups use the same routine, specialised for pairs without anchor
 // constraints; `cpl` (columns per lane in an earlier design) is ignored.
-// Shared memory per warp: 5 rows of sw ints from `prev`.
-template <bool TOP, bool WAIT, bool DWRITE, bool COUNT = false>
+// Shared memory per warp (smem_warp_ints): 5 ring rows of `ringn` ints from
+// `sbase` (previous and current M row, E, gap cost << 4 | sigma column class,
+// arc-term maxima), indexed by column j mod ringn, and the 256-entry sigma
+// class table; ringn (a multiple of 32) exceeds the column span of any two
+// consecutive band rows. Gap costs stay below 2^27 (host check), so the
+// packed value does not overflow.
+// FAST: every pair of the launch has a sigma class table and no anchors.
+template <bool TOP, bool WAIT, bool DWRITE, bool COUNT = false, bool FAST = false>
 __device__ __forceinline__ void run_group(const PairDev &P, int cpl, int al, int ar, int bl, int br,
-                                          int *__restrict__ Mg, int pitch, int prev, int cur,
-                                          int E, int gBs, int Arow, const int4 *__restrict__ dw, int ndw,
+                                          int *__restrict__ Mg, int pitch, int sbase, int ringn,
+                                          const int4 *__restrict__ dw, int ndw,
                                           bool globalA, bool globalB, bool local_top, int *status,
                                           volatile int *abort_flag, TopOut *tout,
                                           unsigned long long *counters = nullptr) {
-    if (P.flags & PF_ANCHORS)
-        run_group_c<4, true, TOP, WAIT, DWRITE, COUNT>(P, al, ar, bl, br, Mg, pitch, prev, cur, E, gBs, Arow, dw,
-                                                       ndw, globalA, globalB, local_top, status, abort_flag, tout,
-                                                       counters);
+    if (FAST)
+        run_group_c<4, false, true, TOP, WAIT, DWRITE, COUNT>(P, al, ar, bl, br, Mg, pitch, sbase, ringn, dw, ndw,
+                                                              globalA, globalB, local_top, status, abort_flag,
+                                                              tout, counters);
+    else if (P.flags & PF_ANCHORS)
+        run_group_c<4, true, false, TOP, WAIT, DWRITE, COUNT>(P, al, ar, bl, br, Mg, pitch, sbase, ringn, dw, ndw,
+                                                              globalA, globalB, local_top, status, abort_flag,
+                                                              tout, counters);
+    else if (P.flags & PF_SCLS)
+        run_group_c<4, false, true, TOP, WAIT, DWRITE, COUNT>(P, al, ar, bl, br, Mg, pitch, sbase, ringn, dw, ndw,
+                                                              globalA, globalB, local_top, status, abort_flag,
+                                                              tout, counters);
     else
-        run_group_c<4, false, TOP, WAIT, DWRITE, COUNT>(P, al, ar, bl, br, Mg, pitch, prev, cur, E, gBs, Arow, dw,
-                                                        ndw, globalA, globalB, local_top, status, abort_flag, tout,
-                                                        counters);
+        run_group_c<4, false, false, TOP, WAIT, DWRITE, COUNT>(P, al, ar, bl, br, Mg, pitch, sbase, ringn, dw, ndw,
+                                                               globalA, globalB, local_top, status, abort_flag,
+                                                               tout, counters);
 }
 
 static __device__ __forceinline__ void warp_argmax(int &v, int &k1, int &k2) {
@@ -345,8 +391,8 @@ static __device__ __forceinline__ void warp_argmax(int &v, int &k1, int &k2) {
 
 // top level + final argmax: align_top_level_free_endgaps (aligner.cc:736-819)
 // and align_top_level_locally (aligner.cc:823-880)
-template <bool COUNT>
-__device__ __forceinline__ void run_top(const PairDev &P, int cpl, int prev, int cur, int E, int gBs, int Aslot,
+template <bool COUNT, bool FAST = false>
+__device__ __forceinline__ void run_top(const PairDev &P, int cpl, int sbase, int ringn,
                                      int *status, volatile int *abort_flag,
                                      unsigned long long *counters) {
     const int lane = threadIdx.x & 31;
@@ -355,8 +401,8 @@ __device__ __forceinline__ void run_top(const PairDev &P, int cpl, int prev, int
     const int fe = P.free_endgaps;
     TopOut to;
     if (local) {
-        run_group<true, true, false, COUNT>(P, cpl, 0, n + 1, 0, m + 1, P.topM, m1, prev, cur, E,
-                                            gBs, Aslot, nullptr, 0, false, false, true, status, abort_flag,
+        run_group<true, true, false, COUNT, FAST>(P, cpl, 0, n + 1, 0, m + 1, P.topM, m1, sbase, ringn,
+                                            nullptr, 0, false, false, true, status, abort_flag,
                                             &to, counters);
         int v = to.best, i = to.bi, j = to.bj;
         if (v <= 0) {
@@ -377,8 +423,8 @@ __device__ __forceinline__ void run_top(const PairDev &P, int cpl, int prev, int
         }
         return;
     }
-    run_group<true, true, false, COUNT>(P, cpl, 0, n + 1, 0, m + 1, P.topM, m1, prev, cur, E, gBs,
-                                        Aslot, nullptr, 0, !(fe & 4), !(fe & 1), false, status, abort_flag,
+    run_group<true, true, false, COUNT, FAST>(P, cpl, 0, n + 1, 0, m + 1, P.topM, m1, sbase, ringn,
+                                        nullptr, 0, !(fe & 4), !(fe & 1), false, status, abort_flag,
                                         &to, counters);
     __syncwarp();
     if (!(fe & (2 | 8))) {
@@ -481,7 +527,7 @@ static __device__ __noinline__ void walk(Walker &w, const int *Mg, int pitch, in
             return;
         }
         if (a_match(P, i, j) && w.valid(i - 1, j - 1) &&
-            Mij == MM(i - 1, j - 1) + P.sigma[(size_t)i * m1 + j]) {
+            Mij == MM(i - 1, j - 1) + sigma_at(P, i, j)) {
             w.emit(i, j);
             --i;
             --j;

@@ -35,15 +35,15 @@
 
 namespace lcg {
 
-template <bool COUNT>
-__global__ void __launch_bounds__(FILL_WARPS * 32)
+template <bool COUNT, bool FAST>
+__global__ void __launch_bounds__(FILL_WARPS * 32, FILL_MIN_BLOCKS)
     sankoff_fill_kernel(const PairDev *__restrict__ pairs, const GroupItem *__restrict__ items,
                         int nitems, const int4 *__restrict__ dw, int *scratch,
-                        long long scratch_stride, int sw, unsigned int *qhead, int *status,
+                        long long scratch_stride, int sw, int rb, unsigned int *qhead, int *status,
                         int *abort_flag_ptr, unsigned long long *counters) {
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
-    const int prev = warp * 5 * sw, cur = prev + sw, E = cur + sw, gBs = E + sw, Arow = gBs + sw;
+    const int sbase = warp * smem_warp_ints(rb);
     int *Mg = scratch + ((long long)blockIdx.x * FILL_WARPS + warp) * scratch_stride;
     volatile int *abort_flag = abort_flag_ptr;
     while (true) {
@@ -54,11 +54,11 @@ __global__ void __launch_bounds__(FILL_WARPS * 32)
         const GroupItem it = items[idx];
         const PairDev &P = pairs[it.pair];
         if (it.top) {
-            run_top<COUNT>(P, it.cpl, prev, cur, E, gBs, Arow, status, abort_flag, counters);
+            run_top<COUNT, FAST>(P, it.cpl, sbase, rb, status, abort_flag, counters);
         } else {
-            run_group<false, true, true, COUNT>(P, it.cpl, it.al, it.ar, it.bl, it.br, Mg, sw, prev,
-                                                cur, E, gBs, Arow, dw + it.dw_start, it.dw_count, true,
-                                                true, false, status, abort_flag, nullptr, counters);
+            run_group<false, true, true, COUNT, FAST>(P, it.cpl, it.al, it.ar, it.bl, it.br, Mg, sw, sbase, rb,
+                                                dw + it.dw_start, it.dw_count, true, true, false, status,
+                                                abort_flag, nullptr, counters);
         }
         __syncwarp();
     }
@@ -66,14 +66,14 @@ __global__ void __launch_bounds__(FILL_WARPS * 32)
 
 __global__ void __launch_bounds__(TRACE_WARPS * 32)
     sankoff_trace_kernel(const PairDev *__restrict__ pairs, int npairs, int *scratch,
-                         long long scratch_stride, int sw, int *status) {
+                         long long scratch_stride, int sw, int rb, int *status) {
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
     const int pair = blockIdx.x * TRACE_WARPS + warp;
     if (pair >= npairs) return;
     const PairDev &P = pairs[pair];
     if (!(P.flags & PF_TRACE)) return;
-    const int prev = warp * 5 * sw, cur = prev + sw, E = cur + sw, gBs = E + sw, Arow = gBs + sw;
+    const int sbase = warp * smem_warp_ints(rb);
     int *Mg = scratch + (long long)pair * scratch_stride;
     int dummy_abort = 0;
     Walker w(P);
@@ -94,9 +94,8 @@ __global__ void __launch_bounds__(TRACE_WARPS * 32)
         if (k < 0) break;
         const int4 ends = P.am_ends[k];  // a.l, a.r, b.l, b.r
         const int cpl = min(4, max(1, (min(ends.w - ends.z, P.maxband) + 31) / 32));
-        run_group<false, false, false>(P, cpl, ends.x, ends.y, ends.z, ends.w, Mg, sw, prev, cur, E, gBs, Arow,
-                                       nullptr, 0, true, true, false, status,
-                                       (volatile int *)&dummy_abort, nullptr);
+        run_group<false, false, false>(P, cpl, ends.x, ends.y, ends.z, ends.w, Mg, sw, sbase, rb, nullptr, 0,
+                                       true, true, false, status, (volatile int *)&dummy_abort, nullptr);
         __syncwarp();
         if (lane == 0) {
             const int start = w.ntok;
@@ -116,37 +115,47 @@ __global__ void __launch_bounds__(TRACE_WARPS * 32)
 
 // ---------------------------------------------------------------- launchers
 
+template <bool COUNT, bool FAST>
+static const void *fill_fn() {
+    return (const void *)sankoff_fill_kernel<COUNT, FAST>;
+}
+
 cudaError_t launch_fill(const PairDev *pairs, const GroupItem *items, int nitems, const int4 *dw,
-                        int *scratch, long long scratch_stride, int sw, unsigned int *qhead,
+                        int *scratch, long long scratch_stride, int sw, int rb, bool fast, unsigned int *qhead,
                         int *status, int *abort_flag, int blocks, cudaStream_t st,
                         unsigned long long *counters) {
-    size_t smem = (size_t)FILL_WARPS * 5 * sw * sizeof(int);
-    if (counters)
-        sankoff_fill_kernel<true><<<blocks, FILL_WARPS * 32, smem, st>>>(
-            pairs, items, nitems, dw, scratch, scratch_stride, sw, qhead, status, abort_flag,
-            counters);
+    size_t smem = (size_t)FILL_WARPS * smem_warp_ints(rb) * sizeof(int);
+    if (counters && fast)
+        sankoff_fill_kernel<true, true><<<blocks, FILL_WARPS * 32, smem, st>>>(
+            pairs, items, nitems, dw, scratch, scratch_stride, sw, rb, qhead, status, abort_flag, counters);
+    else if (counters)
+        sankoff_fill_kernel<true, false><<<blocks, FILL_WARPS * 32, smem, st>>>(
+            pairs, items, nitems, dw, scratch, scratch_stride, sw, rb, qhead, status, abort_flag, counters);
+    else if (fast)
+        sankoff_fill_kernel<false, true><<<blocks, FILL_WARPS * 32, smem, st>>>(
+            pairs, items, nitems, dw, scratch, scratch_stride, sw, rb, qhead, status, abort_flag, counters);
     else
-        sankoff_fill_kernel<false><<<blocks, FILL_WARPS * 32, smem, st>>>(
-            pairs, items, nitems, dw, scratch, scratch_stride, sw, qhead, status, abort_flag,
-            counters);
+        sankoff_fill_kernel<false, false><<<blocks, FILL_WARPS * 32, smem, st>>>(
+            pairs, items, nitems, dw, scratch, scratch_stride, sw, rb, qhead, status, abort_flag, counters);
     return cudaGetLastError();
 }
 
 cudaError_t launch_trace(const PairDev *pairs, int npairs, int *scratch,
-                         long long scratch_stride, int sw, int *status, cudaStream_t st) {
-    size_t smem = (size_t)TRACE_WARPS * 5 * sw * sizeof(int);
+                         long long scratch_stride, int sw, int rb, int *status, cudaStream_t st) {
+    size_t smem = (size_t)TRACE_WARPS * smem_warp_ints(rb) * sizeof(int);
     int blocks = (npairs + TRACE_WARPS - 1) / TRACE_WARPS;
     sankoff_trace_kernel<<<blocks, TRACE_WARPS * 32, smem, st>>>(pairs, npairs, scratch,
-                                                                 scratch_stride, sw, status);
+                                                                 scratch_stride, sw, rb, status);
     return cudaGetLastError();
 }
 
 int fill_warps_per_block() { return FILL_WARPS; }
 int trace_warps_per_block() { return TRACE_WARPS; }
 
-cudaError_t fill_occupancy(int sw, bool counting, int *blocks_per_sm) {
-    size_t smem = (size_t)FILL_WARPS * 5 * sw * sizeof(int);
-    const void *k = counting ? (const void *)sankoff_fill_kernel<true> : (const void *)sankoff_fill_kernel<false>;
+cudaError_t fill_occupancy(int rb, bool counting, bool fast, int *blocks_per_sm) {
+    size_t smem = (size_t)FILL_WARPS * smem_warp_ints(rb) * sizeof(int);
+    const void *k = counting ? (fast ? fill_fn<true, true>() : fill_fn<true, false>())
+                             : (fast ? fill_fn<false, true>() : fill_fn<false, false>());
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
@@ -154,8 +163,8 @@ cudaError_t fill_occupancy(int sw, bool counting, int *blocks_per_sm) {
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k, FILL_WARPS * 32, smem);
 }
 
-cudaError_t trace_prepare(int sw) {
-    size_t smem = (size_t)TRACE_WARPS * 5 * sw * sizeof(int);
+cudaError_t trace_prepare(int rb) {
+    size_t smem = (size_t)TRACE_WARPS * smem_warp_ints(rb) * sizeof(int);
     if (smem > 48 * 1024)
         return cudaFuncSetAttribute(sankoff_trace_kernel,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

@@ -1,0 +1,29 @@
+// Host-side entry points of the Sankoff kernels (sankoff_kernels.cu,
+// sankoff_sl_kernels.cu, microbench.cu) used by engine.cu and noalloc.cu.
+// sw: scratch row pitch (ints); rb: ring size of the shared-memory rows (a
+// power of two above the column span of any two consecutive band rows).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "lcg_device.cuh"
+
+namespace lcg {
+// fast: every pair has a sigma class table and no anchor constraints
+cudaError_t launch_fill(const PairDev *pairs, const GroupItem *items, int nitems, const int4 *dw, int *scratch,
+                        long long scratch_stride, int sw, int rb, bool fast, unsigned int *qhead, int *status,
+                        int *abort_flag, int blocks, cudaStream_t st, unsigned long long *counters);
+cudaError_t launch_trace(const PairDev *pairs, int npairs, int *scratch, long long scratch_stride, int sw, int rb,
+                         int *status, cudaStream_t st);
+cudaError_t fill_occupancy(int rb, bool counting, bool fast, int *blocks_per_sm);
+cudaError_t trace_prepare(int rb);
+int fill_warps_per_block();
+int trace_warps_per_block();
+cudaError_t sl_prepare(int sw, int rb, int *blocks_per_sm);
+int sl_fill_warps_per_block();
+cudaError_t launch_sl_fill(const PairDev *pairs, const GroupItem *items, int nitems, const int4 *dw, int *scratch,
+                           long long scratch_stride, int sw, int rb, unsigned int *qhead, int *status,
+                           int *abort_flag, int blocks, cudaStream_t st);
+cudaError_t launch_sl_trace(const PairDev *pairs, int npairs, int *scratch, long long scratch_stride, int sw,
+                            int *status, cudaStream_t st);
+cudaError_t measure_int_peak(int sms, bool dpx, cudaStream_t st, double *gops);
+}  // namespace lcg

@@ -31,6 +31,11 @@ enum { S_NO_NO = 0, S_X_NO = 1, S_NO_X = 2, S_X_X = 3, S_OP_NO = 4, S_NO_OP = 5,
 constexpr int SL_FILL_WARPS = 4;
 // shared-memory rows per warp: prev/cur of states 0,1,2,3,4,6 and E of 0..3
 constexpr int SL_ROWS = 16;
+// shared ints per warp of the fill kernel: SL_ROWS rows of sw for the group
+// states, and room for the plain row sweep of the top level (smem_warp_ints)
+__host__ __device__ inline int sl_warp_ints(int sw, int rb) {
+    return SL_ROWS * sw > smem_warp_ints(rb) ? SL_ROWS * sw : smem_warp_ints(rb);
+}
 
 // slot of a state's prev row in shared memory (states 5 and 7 keep no row)
 __device__ __forceinline__ int sl_slot(int s) { return s < 4 ? s : (s == 4 ? 4 : 5); }
@@ -157,7 +162,6 @@ __device__ void run_group_sl(const PairDev &P, int al, int ar, int bl, int br, i
             cur[4][lo - 1 - bl] = Bs[4];
             cur[5][lo - 1 - bl] = Bs[6];
         }
-        const int *sig_row = P.sigma + (size_t)i * m1;
         const long long roff = (long long)(i - al) * pitch - bl;
         const int cell0 = P.bandoff[i] - minc;
         // carries across chunks: F of states 0..3, X' of states 0..3, NO_OP, X_OP
@@ -175,7 +179,7 @@ __device__ void run_group_sl(const PairDev &P, int al, int ar, int bl, int br, i
                 mok = a_match(P, i, j);
                 dok = a_del(P, i, j);
                 iok = a_ins(P, i, j);
-                sg = sig_row[j];
+                sg = sigma_at(P, i, j);
                 gb = P.gapB[j];
                 if (mok) {
                     const int cell = cell0 + j;
@@ -300,12 +304,12 @@ __device__ void run_group_sl(const PairDev &P, int al, int ar, int bl, int br, i
 __global__ void __launch_bounds__(SL_FILL_WARPS * 32)
     sankoff_sl_fill_kernel(const PairDev *__restrict__ pairs, const GroupItem *__restrict__ items,
                            int nitems, const int4 *__restrict__ dw, int *scratch,
-                           long long scratch_stride, int sw, unsigned int *qhead, int *status,
+                           long long scratch_stride, int sw, int rb, unsigned int *qhead, int *status,
                            int *abort_flag_ptr) {
     extern __shared__ int smem[];
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
-    int *sm = smem + warp * SL_ROWS * sw;
+    int *sm = smem + warp * sl_warp_ints(sw, rb);
     // 4 state matrices per warp slot
     int *Mg = scratch + ((long long)blockIdx.x * SL_FILL_WARPS + warp) * scratch_stride * 4;
     volatile int *abort_flag = abort_flag_ptr;
@@ -318,8 +322,7 @@ __global__ void __launch_bounds__(SL_FILL_WARPS * 32)
         const PairDev &P = pairs[it.pair];
         if (it.top) {
             const int base = (int)(sm - smem);
-            run_top<false>(P, it.cpl, base, base + sw, base + 2 * sw, base + 3 * sw, base + 4 * sw, status,
-                           abort_flag, nullptr);
+            run_top<false>(P, it.cpl, base, rb, status, abort_flag, nullptr);
         } else {
             run_group_sl<true, true, 4>(P, it.al, it.ar, it.bl, it.br, Mg, scratch_stride, sw, sm, sw,
                                         dw + it.dw_start, it.dw_count, status, abort_flag);
@@ -396,7 +399,7 @@ static __device__ __noinline__ void walk_sl(Walker &w, const int *Mg, long long 
         if (!noex) return;
         // trace_noex (aligner.cc:1082-1229) in `state`
         if (a_match(P, i, j) && w.valid(i - 1, j - 1) &&
-            Mij == MS(state, i - 1, j - 1) + P.sigma[(size_t)i * m1 + j]) {
+            Mij == MS(state, i - 1, j - 1) + sigma_at(P, i, j)) {
             w.emit(i, j);
             --i;
             --j;
@@ -526,8 +529,8 @@ __global__ void __launch_bounds__(TRACE_WARPS * 32)
 
 // ---------------------------------------------------------------- launchers
 
-cudaError_t sl_prepare(int sw, int *blocks_per_sm) {
-    size_t smem = (size_t)SL_FILL_WARPS * SL_ROWS * sw * sizeof(int);
+cudaError_t sl_prepare(int sw, int rb, int *blocks_per_sm) {
+    size_t smem = (size_t)SL_FILL_WARPS * sl_warp_ints(sw, rb) * sizeof(int);
     size_t smem_t = (size_t)TRACE_WARPS * SL_ROWS * sw * sizeof(int);
     cudaError_t e = cudaFuncSetAttribute(sankoff_sl_fill_kernel,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -542,11 +545,11 @@ cudaError_t sl_prepare(int sw, int *blocks_per_sm) {
 int sl_fill_warps_per_block() { return SL_FILL_WARPS; }
 
 cudaError_t launch_sl_fill(const PairDev *pairs, const GroupItem *items, int nitems, const int4 *dw,
-                           int *scratch, long long scratch_stride, int sw, unsigned int *qhead,
+                           int *scratch, long long scratch_stride, int sw, int rb, unsigned int *qhead,
                            int *status, int *abort_flag, int blocks, cudaStream_t st) {
-    size_t smem = (size_t)SL_FILL_WARPS * SL_ROWS * sw * sizeof(int);
+    size_t smem = (size_t)SL_FILL_WARPS * sl_warp_ints(sw, rb) * sizeof(int);
     sankoff_sl_fill_kernel<<<blocks, SL_FILL_WARPS * 32, smem, st>>>(
-        pairs, items, nitems, dw, scratch, scratch_stride, sw, qhead, status, abort_flag);
+        pairs, items, nitems, dw, scratch, scratch_stride, sw, rb, qhead, status, abort_flag);
     return cudaGetLastError();
 }
 
