@@ -325,6 +325,7 @@ def run_ours(args):
     sampler = ClockSampler()
     sampler.start()
     kern_ms, fill_ms, wall_s = 0.0, 0.0, 0.0
+    phases = [0.0, 0.0, 0.0, 0.0]
     launches = 0
     for _ in range(args.steps):
         flush_l2()
@@ -333,6 +334,7 @@ def run_ours(args):
         wall_s += time.perf_counter() - s0
         ms, nl = eng.last_stats()
         f, _ = eng.last_timing()
+        phases = [a + b for a, b in zip(phases, eng.last_phases())]
         kern_ms += ms
         fill_ms += f
         launches += nl
@@ -394,7 +396,9 @@ def run_ours(args):
                    "l2": "flushed between steps (256 MB write)"},
         "gcups": work["cells"] / T / 1e9,
         "e2e": {"value": npairs / We, "unit": "aligns/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h, "ms_per_step": We * 1e3},
+                "d2h_bytes_per_step": d2h, "ms_per_step": We * 1e3,
+                "phases_ms_per_step": dict(zip(("host_prep", "pack", "copies_and_kernels", "results"),
+                                               (x / args.steps for x in phases)))},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": alg_bytes / Tf / 1e9, "peak": hbm_peak, "unit": "GB/s",
                      "frac": alg_bytes / Tf / 1e9 / hbm_peak, "traffic": None,

@@ -165,6 +165,12 @@ lcg_status lcg_engine_last_stats(lcg_engine eng, double *kernel_ms,
 /* Device time (ms) of the last call's D-fill kernel and traceback kernel. */
 lcg_status lcg_engine_last_timing(lcg_engine eng, double *fill_ms, double *trace_ms);
 
+/* Wall-clock phases (ms) of the last lcg_align_pairs call: host preparation of
+ * the pairs' index structures, packing of the upload, copies + kernels until
+ * the results are on the host, and assembly of the alignments. */
+lcg_status lcg_engine_last_phases(lcg_engine eng, double *prep_ms, double *pack_ms,
+                                  double *device_ms, double *results_ms);
+
 /* Bytes the last lcg_align_pairs call copied host->device and device->host. */
 lcg_status lcg_engine_last_transfer(lcg_engine eng, int64_t *h2d_bytes,
                                     int64_t *d2h_bytes);

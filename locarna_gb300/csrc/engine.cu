@@ -8,6 +8,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cstdio>
+#include <chrono>
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
@@ -212,36 +213,41 @@ lcg_status prep_pair(const lcg_pair_tables &t, const lcg_align_opts &o, Prep &p)
                 return p.am_ends[4 * x + 2] > p.am_ends[4 * y + 2];
             });
     }
-    for (size_t q = 0; q < ord.size(); ++q) {
-        int k = ord[q];
-        p.cre[4 * q] = k;
-        p.cre[4 * q + 1] = p.am_ends[4 * k] - 1;      // a.l - 1: row of the inner corner
-        p.cre[4 * q + 2] = p.am_ends[4 * k + 2] - 1;  // b.l - 1: column of the inner corner
-        p.cre[4 * q + 3] = p.am_ends[4 * k + 3];      // b.r: the cell's column
-    }
     // the same candidates per row a.r: a.l descending, then b.l descending
-    // (within a row, the valid ones for a group (al,bl) with a.l > al are a prefix)
-    std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) {
+    // (within a row, the valid ones for a group (al,bl) with a.l > al are a
+    // prefix). The position of an arc match in this order is also the index
+    // of its D entry, so a row's D values are contiguous.
+    std::vector<int> ordr(ord);
+    std::stable_sort(ordr.begin(), ordr.end(), [&](int x, int y) {
         const int *ex = &p.am_ends[4 * x], *ey = &p.am_ends[4 * y];
         if (ex[1] != ey[1]) return ex[1] < ey[1];
         if (ex[0] != ey[0]) return ex[0] > ey[0];
         if (ex[2] != ey[2]) return ex[2] > ey[2];
         return ex[3] < ey[3];
     });
-    p.crow.resize(4 * ord.size());
+    p.am_pos.assign(na, -1);
+    p.crow.resize(2 * ordr.size());
     p.rowarc.assign(2 * (size_t)(n + 2), 0);
-    for (size_t q = 0; q < ord.size(); ++q) {
-        int k = ord[q];
-        p.crow[4 * q] = k;
-        p.crow[4 * q + 1] = p.am_ends[4 * k] - 1;
-        p.crow[4 * q + 2] = p.am_ends[4 * k + 2] - 1;
-        p.crow[4 * q + 3] = p.am_ends[4 * k + 3];
+    for (size_t q = 0; q < ordr.size(); ++q) {
+        int k = ordr[q];
+        p.am_pos[k] = (int)q;
+        // (a.l-1) | (b.l-1) << 16: the inner corner; positions are < 2^15
+        p.crow[2 * q] = (p.am_ends[4 * k] - 1) | ((p.am_ends[4 * k + 2] - 1) << 16);
+        p.crow[2 * q + 1] = p.am_ends[4 * k + 3];  // b.r: the cell's column
     }
     for (size_t q = 0, r = 0; r <= (size_t)n + 1; ++r) {
         p.rowarc[2 * r] = (int)q;
-        while (q < ord.size() && (size_t)p.am_ends[4 * ord[q] + 1] == r) ++q;
+        while (q < ordr.size() && (size_t)p.am_ends[4 * ordr[q] + 1] == r) ++q;
         p.rowarc[2 * r + 1] = (int)q;
     }
+    for (size_t q = 0; q < ord.size(); ++q) {
+        int k = ord[q];
+        p.cre[4 * q] = p.am_pos[k];                   // D entry
+        p.cre[4 * q + 1] = p.am_ends[4 * k] - 1;      // a.l - 1: row of the inner corner
+        p.cre[4 * q + 2] = p.am_ends[4 * k + 2] - 1;  // b.l - 1: column of the inner corner
+        p.cre[4 * q + 3] = k;                         // the arc match
+    }
+    p.num_pos = (int)ordr.size();
 
     // left-end groups (aligner.cc:660-732): bucket arc matches by (al,bl)
     std::vector<std::pair<long long, int>> byleft(na);
@@ -249,7 +255,7 @@ lcg_status prep_pair(const lcg_pair_tables &t, const lcg_align_opts &o, Prep &p)
         byleft[k] = {(long long)p.am_ends[4 * k] * (m + 1) + p.am_ends[4 * k + 2], k};
     std::stable_sort(byleft.begin(), byleft.end(),
                      [](const auto &x, const auto &y) { return x.first > y.first; });
-    p.Dinit.assign(na, NEG);
+    p.Dinit.assign(p.num_pos, NEG);
     p.rows_max = 0;
     p.width_max = 0;
     for (size_t s = 0; s < byleft.size();) {
@@ -277,9 +283,10 @@ lcg_status prep_pair(const lcg_pair_tables &t, const lcg_align_opts &o, Prep &p)
             for (int k : ks) {
                 int ar = p.am_ends[4 * k + 1], br = p.am_ends[4 * k + 3];
                 // the inner corner (ar-1,br-1) is computed by this group iff it is in the band
-                if (ar - 1 > al && br - 1 > bl && in_band(ar - 1, br - 1)) {
-                    p.dw.push_back(make_int4(k, ar - 1, br - 1, t.am_score[k]));
-                    p.Dinit[k] = NOT_READY;
+                // (only arc matches whose right ends are a band cell are ever read)
+                if (ar - 1 > al && br - 1 > bl && in_band(ar - 1, br - 1) && p.am_pos[k] >= 0) {
+                    p.dw.push_back(make_int4(p.am_pos[k], ar - 1, br - 1, t.am_score[k]));
+                    p.Dinit[p.am_pos[k]] = NOT_READY;
                 }
             }
             g.dw_count = (int)p.dw.size() - g.dw_start;
@@ -457,25 +464,23 @@ lcg_status lcg_measure_int_peak(lcg_engine e, int32_t dpx, double *gops) {
     return LCG_OK;
 }
 
-// Bytes of per-pair tables one wave of pairs may keep hot (default 48 MB of
-// the 126 MB L2); LCG_WAVE_MB overrides it for tuning runs.
-static double wave_budget_bytes() {
-    const char *v = std::getenv("LCG_WAVE_MB");
-    const double mb = v ? std::atof(v) : 48.0;
-    return (mb > 0 ? mb : 1e9) * 1048576.0;
-}
-
 lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t npairs,
                            const lcg_align_opts *opts, lcg_align_result *results) {
     if (!e || !pairs || !opts || !results || npairs < 0) return fail(LCG_ERR_ARG, "NULL argument");
     if (npairs == 0) return LCG_OK;
     CUDA_TRY(cudaSetDevice(e->device));
+    using clk = std::chrono::steady_clock;
+    const auto t0 = clk::now();
+    auto ms_since = [](clk::time_point a, clk::time_point b) {
+        return std::chrono::duration<double, std::milli>(b - a).count();
+    };
 
     // ---- host preparation (threads over pairs)
     std::vector<Prep> prep(npairs);
     lcg_host::parallel_for(npairs, [&](int q) { prep_pair(pairs[q], *opts, prep[q]); });
     for (int q = 0; q < npairs; ++q)
         if (prep[q].code != LCG_OK) return fail(prep[q].code, "pair " + std::to_string(q) + ": " + prep[q].err);
+    const auto t1 = clk::now();
 
     // ---- arena layout
     int sw = 0, rows_max = 1, span = 2;
@@ -486,7 +491,7 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
     }
     struct Off {
         size_t sigma, scls, rcls, ccls, gapA, gapB, minc, maxc, bandoff, rowinfo, anc, cre_start, cre, crow, rowarc,
-            am_ends, am_score, D,
+            am_pos, am_ends, am_score, D,
             topM, res, tok, tq, segs;
     };
     std::vector<Off> off(npairs);
@@ -526,8 +531,9 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
         o.crow = take(up, 4ull * std::max<size_t>(p.crow.size(), 4));
         o.rowarc = take(up, 4ull * p.rowarc.size());
         o.am_ends = take(up, 4ull * std::max<size_t>(p.am_ends.size(), 4));
+        o.am_pos = take(up, 4ull * std::max(t.num_arcmatches, 1));
         o.am_score = take(up, 4ull * std::max(t.num_arcmatches, 1));
-        o.D = take(up, 4ull * std::max(t.num_arcmatches, 1));
+        o.D = take(up, 4ull * std::max(p.num_pos, 1));
     }
     size_t down_begin = up;
     size_t dn = up;
@@ -578,14 +584,14 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
         // pairs' work lists are interleaved so that every pair progresses
         // proportionally; within a pair the order is kept. Waves follow each
         // other in the queue without a barrier.
-        const double wave_bytes = wave_budget_bytes();
+        const double wave_bytes = lcg_host::wave_budget_bytes();
         std::vector<std::pair<double, std::pair<int, int>>> order;
         order.reserve(nitems);
         double acc = 0.0;
         int wave = 0;
         for (int q = 0; q < npairs; ++q) {
             const auto &p = prep[q];
-            const double fp = 20.0 * pairs[q].num_arcmatches + 4.0 * p.bandcells;
+            const double fp = 12.0 * p.num_pos + 4.0 * p.bandcells;
             if (acc > 0.0 && acc + fp > wave_bytes) {
                 ++wave;
                 acc = 0.0;
@@ -641,9 +647,10 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
         if (!p.crow.empty()) std::memcpy(H + o.crow, p.crow.data(), 4ull * p.crow.size());
         std::memcpy(H + o.rowarc, p.rowarc.data(), 4ull * p.rowarc.size());
         if (!p.am_ends.empty()) std::memcpy(H + o.am_ends, p.am_ends.data(), 4ull * p.am_ends.size());
+        if (p.num_pos) std::memcpy(H + o.D, p.Dinit.data(), 4ull * p.num_pos);
         if (t.num_arcmatches) {
+            std::memcpy(H + o.am_pos, p.am_pos.data(), 4ull * t.num_arcmatches);
             std::memcpy(H + o.am_score, t.am_score, 4ull * t.num_arcmatches);
-            std::memcpy(H + o.D, p.Dinit.data(), 4ull * t.num_arcmatches);
         }
         PairDev &d = hp[q];
         std::memset(&d, 0, sizeof d);
@@ -683,7 +690,9 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
         }
         d.cre_start = (const int *)(Dv + o.cre_start);
         d.cre = (const int4 *)(Dv + o.cre);
-        d.crow = (const int4 *)(Dv + o.crow);
+        d.crow = (const int2 *)(Dv + o.crow);
+        d.am_pos = (const int *)(Dv + o.am_pos);
+        d.num_pos = p.num_pos;
         d.rowarc = (const int2 *)(Dv + o.rowarc);
         d.D = (int *)(Dv + o.D);
         d.am_ends = (const int4 *)(Dv + o.am_ends);
@@ -697,6 +706,7 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
         d.segs = (int4 *)(Dv + o.segs);
     });
 
+    const auto t2 = clk::now();
     // ---- scratch
     const bool sl = opts->struct_local != 0;
     const int rb = lcg_host::ring_size(span);
@@ -759,6 +769,7 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
     CUDA_TRY(cudaMemcpyAsync(H + off_ctrl, Dv + off_ctrl, 64, cudaMemcpyDeviceToHost, st));
     CUDA_TRY(cudaMemcpyAsync(H + down_begin, Dv + down_begin, down_end - down_begin, cudaMemcpyDeviceToHost, st));
     CUDA_TRY(cudaStreamSynchronize(st));
+    const auto t3 = clk::now();
     float ms = 0, ms1 = 0;
     cudaEventElapsedTime(&ms, e->ev0, e->ev2);
     cudaEventElapsedTime(&ms1, e->ev0, e->ev1);
@@ -820,6 +831,21 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
         r.num_edges = as.nedges;
         r.num_traced_am = as.ntam;
     }
+    const auto t4 = clk::now();
+    e->last_phase_ms[0] = ms_since(t0, t1);
+    e->last_phase_ms[1] = ms_since(t1, t2);
+    e->last_phase_ms[2] = ms_since(t2, t3);
+    e->last_phase_ms[3] = ms_since(t3, t4);
+    return LCG_OK;
+}
+
+lcg_status lcg_engine_last_phases(lcg_engine e, double *prep_ms, double *pack_ms, double *device_ms,
+                                  double *results_ms) {
+    if (!e) return fail(LCG_ERR_ARG, "engine is NULL");
+    if (prep_ms) *prep_ms = e->last_phase_ms[0];
+    if (pack_ms) *pack_ms = e->last_phase_ms[1];
+    if (device_ms) *device_ms = e->last_phase_ms[2];
+    if (results_ms) *results_ms = e->last_phase_ms[3];
     return LCG_OK;
 }
 

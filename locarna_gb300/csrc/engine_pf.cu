@@ -39,7 +39,7 @@ lcg_status pf_fail(lcg_status c, const std::string &m) {
 size_t up16(size_t x) { return (x + 15) / 16 * 16; }
 
 struct PFLayout {
-    int n, m, na, bandcells;
+    int n, m, na, npos, bandcells;  // npos: D entries (arc matches with a band cell as right ends)
     size_t rowinfo, crow, rowarc, bm, gA, gB, w, D, Dbar, cnt, bmacc, res, topM;
     double log_c_total;  // (n+m) log c
 };
@@ -62,6 +62,7 @@ struct PFState {
     double fwd_ms = 0, back_ms = 0;
     double temperature = 300.0;
     std::vector<double> log_z;
+    std::vector<std::vector<int>> am_pos;  // per pair: D position of each arc match
 };
 
 PFState *state_of(lcg_engine e) {
@@ -130,6 +131,7 @@ lcg_status pf_forward_t(lcg_engine e, PFState *S, const lcg_pair_tables *pairs, 
     }
     // layout
     S->lay.assign(npairs, PFLayout{});
+    S->am_pos.assign(npairs, std::vector<int>());
     size_t up = 0;
     auto take = [](size_t &cur, size_t bytes) {
         size_t r = cur;
@@ -157,6 +159,7 @@ lcg_status pf_forward_t(lcg_engine e, PFState *S, const lcg_pair_tables *pairs, 
         L.n = p.n;
         L.m = p.m;
         L.na = pairs[q].num_arcmatches;
+        L.npos = p.num_pos;
         L.bandcells = p.bandcells;
         L.rowinfo = take(up, 16ull * (p.n + 2));
         L.crow = take(up, 4ull * std::max<size_t>(p.crow.size(), 4));
@@ -164,17 +167,17 @@ lcg_status pf_forward_t(lcg_engine e, PFState *S, const lcg_pair_tables *pairs, 
         L.bm = take(up, sizeof(T) * (p.n + 1) * (p.m + 1));
         L.gA = take(up, sizeof(T) * (p.n + 1));
         L.gB = take(up, sizeof(T) * (p.m + 1));
-        L.w = take(up, sizeof(T) * std::max(L.na, 1));
-        L.D = take(up, sizeof(T) * std::max(L.na, 1));
+        L.w = take(up, sizeof(T) * std::max(L.npos, 1));
+        L.D = take(up, sizeof(T) * std::max(L.npos, 1));
     }
     // zero-initialised device section, then the output section
     const size_t zero_begin = up;
-    for (int q = 0; q < npairs; ++q) S->lay[q].cnt = take(up, 4ull * std::max(S->lay[q].na, 1));
+    for (int q = 0; q < npairs; ++q) S->lay[q].cnt = take(up, 4ull * std::max(S->lay[q].npos, 1));
     const size_t out_begin = up;
     for (int q = 0; q < npairs; ++q) {
         PFLayout &L = S->lay[q];
         L.res = take(up, 8ull * 4);
-        L.Dbar = take(up, sizeof(double) * std::max(L.na, 1));
+        L.Dbar = take(up, sizeof(double) * std::max(L.npos, 1));
         L.bmacc = take(up, sizeof(double) * std::max(L.bandcells, 1));
     }
     const size_t out_end = up;
@@ -200,11 +203,22 @@ lcg_status pf_forward_t(lcg_engine e, PFState *S, const lcg_pair_tables *pairs, 
     PFItem<T> *hit = (PFItem<T> *)(H + S->off_items);
     int4 *hdw = (int4 *)(H + S->off_dw);
     {
+        // waves of pairs whose tables fit a share of L2, interleaved by
+        // progress inside a wave (as for lcg_align_pairs)
+        const double wave_bytes = lcg_host::wave_budget_bytes();
         std::vector<std::pair<double, std::pair<int, int>>> order;
         order.reserve(nitems);
+        double acc = 0.0;
+        int wave = 0;
         for (int q = 0; q < npairs; ++q) {
+            const double fp = (12.0 + 3.0 * sizeof(T)) * prep[q].num_pos + 3.0 * sizeof(T) * prep[q].bandcells;
+            if (acc > 0.0 && acc + fp > wave_bytes) {
+                ++wave;
+                acc = 0.0;
+            }
+            acc += fp;
             size_t G = prep[q].groups.size();
-            for (size_t g = 0; g < G; ++g) order.push_back({(double)(g + 1) / (double)G, {q, (int)g}});
+            for (size_t g = 0; g < G; ++g) order.push_back({wave + (double)(g + 1) / (double)G, {q, (int)g}});
         }
         std::stable_sort(order.begin(), order.end(), [](const auto &a, const auto &b) { return a.first < b.first; });
         std::vector<size_t> dwbase(npairs);
@@ -271,27 +285,30 @@ lcg_status pf_forward_t(lcg_engine e, PFState *S, const lcg_pair_tables *pairs, 
         T *hw = (T *)(H + L0.w);
         T *hD = (T *)(H + L0.D);
         for (int k = 0; k < L.na; ++k) {
+            const int pos = p.am_pos[k];
+            if (pos < 0) continue;  // never a term: its right ends are not a band cell
             const double dsw = (sp && sp->am_dscore_dsw) ? dl[2] * sp->am_dscore_dsw[k] : 0.0;
-            hw[k] = (T)std::exp(((double)t.am_score[k] + dsw) / temp);
-            if (p.Dinit[k] == NOT_READY) {
+            hw[pos] = (T)std::exp(((double)t.am_score[k] + dsw) / temp);
+            if (p.Dinit[pos] == NOT_READY) {
                 if (sizeof(T) == 8) {
                     long long bits = PF_NOT_READY_F64;
-                    std::memcpy(&hD[k], &bits, 8);
+                    std::memcpy(&hD[pos], &bits, 8);
                 } else {
                     int bits = PF_NOT_READY_F32;
-                    std::memcpy(&hD[k], &bits, 4);
+                    std::memcpy(&hD[pos], &bits, 4);
                 }
             } else {
-                hD[k] = T(0);
+                hD[pos] = T(0);
             }
         }
+        S->am_pos[q] = p.am_pos;
         PFPair<T> &d = hp[q];
         std::memset(&d, 0, sizeof d);
         d.n = n;
         d.m = m;
         d.num_am = L.na;
         d.rowinfo = (const int4 *)(Dv + L0.rowinfo);
-        d.crow = (const int4 *)(Dv + L0.crow);
+        d.crow = (const int2 *)(Dv + L0.crow);
         d.rowarc = (const int2 *)(Dv + L0.rowarc);
         d.bm = (const T *)(Dv + L0.bm);
         d.gA = (const T *)(Dv + L0.gA);
@@ -381,8 +398,8 @@ lcg_status pf_backward_t(lcg_engine e, PFState *S, const lcg_pf_grad_spec *grads
     PF_TRY(cudaMemcpyAsync(H + S->out_begin, Dv + S->out_begin, S->out_end - S->out_begin, cudaMemcpyDeviceToHost, st));
     // D values (for the arc-match probabilities)
     for (int q = 0; q < S->npairs; ++q)
-        if (S->lay[q].na > 0)
-            PF_TRY(cudaMemcpyAsync(H + S->lay[q].D, Dv + S->lay[q].D, sizeof(T) * S->lay[q].na,
+        if (S->lay[q].npos > 0)
+            PF_TRY(cudaMemcpyAsync(H + S->lay[q].D, Dv + S->lay[q].D, sizeof(T) * S->lay[q].npos,
                                    cudaMemcpyDeviceToHost, st));
     PF_TRY(cudaStreamSynchronize(st));
     float ms = 0;
@@ -410,8 +427,9 @@ lcg_status pf_backward_t(lcg_engine e, PFState *S, const lcg_pf_grad_spec *grads
         const bool sw_grad = g && g->am_dscore_dsw;
         if (r.am_prob || sw_grad) {
             double dsw = 0.0;
+            const std::vector<int> &pos = S->am_pos[q];
             for (int k = 0; k < L.na; ++k) {
-                const double p = (double)D[k] * (double)Db[k] / Zs;
+                const double p = pos[k] >= 0 ? (double)D[pos[k]] * Db[pos[k]] / Zs : 0.0;
                 if (r.am_prob) r.am_prob[k] = p;
                 if (sw_grad) dsw += p * g->am_dscore_dsw[k];
             }

@@ -4,6 +4,7 @@
 // cell, left-end groups in dependency order, D-write lists).
 #pragma once
 #include <algorithm>
+#include <cstdlib>
 #include <atomic>
 #include <string>
 #include <thread>
@@ -23,11 +24,14 @@ struct Prep {
     int maxband = 0;
     int span = 2;  // max over i of max_col[i+1] - min_col[i] + 3 (ring rows of the kernels)
     std::vector<int> cre_start;                  // bandcells+1
-    std::vector<int> cre;                        // 4 per entry: am, a.l-1, b.l-1, b.r
-    std::vector<int> crow;                       // the same entries by row a.r, a.l desc, b.l desc
+    std::vector<int> cre;                        // 4 per entry: D position, a.l-1, b.l-1, am
+    std::vector<int> crow;                       // 2 per entry by row a.r, a.l desc, b.l desc:
+                                                 //   (a.l-1) | (b.l-1) << 16, b.r
     std::vector<int> rowarc;                     // 2 per row 0..n+1: [start, end) in crow
+    std::vector<int> am_pos;                     // per am: its crow position = D index (-1: right ends off the band)
+    int num_pos = 0;                             // crow entries = D entries
     std::vector<int> am_ends;                    // 4 per am
-    std::vector<int> Dinit;                      // per am
+    std::vector<int> Dinit;                      // per D position
     // sigma as a class table when rows and columns fall into <= 16 classes
     // each (single sequences: one class per base): sigma(i,j) =
     // scls[rcls[i]*16 + ccls[j]]
@@ -51,6 +55,15 @@ void set_error(const std::string &msg);
 // ring size of the kernels' shared-memory rows for a set of pairs: the
 // smallest multiple of 32 >= every pair's span
 inline int ring_size(int span) { return (std::max(span, 32) + 31) / 32 * 32; }
+
+// Bytes of per-pair tables one wave of pairs in the work queue may keep hot
+// (default 16 MB of the 126 MB L2); LCG_WAVE_MB overrides it for tuning runs
+// (0 = one wave).
+inline double wave_budget_bytes() {
+    const char *v = std::getenv("LCG_WAVE_MB");
+    const double mb = v ? std::atof(v) : 16.0;
+    return (mb > 0 ? mb : 1e9) * 1048576.0;
+}
 
 // fn(q) for q in [0, n) on up to 64 host threads (dynamic assignment)
 template <typename F>

@@ -22,6 +22,9 @@ struct lcg_engine_s {
     long long last_h2d = 0, last_d2h = 0;
     long long last_groups = 0, last_cells = 0, last_terms = -1, last_visits = -1;
     bool counting = false;
+    // wall-clock phases of the last lcg_align_pairs call (ms): host preparation,
+    // packing, copies + kernels (until the results are on the host), result assembly
+    double last_phase_ms[4] = {0, 0, 0, 0};
     void *pf = nullptr;  // partition-function state (engine_pf.cu)
 };
 

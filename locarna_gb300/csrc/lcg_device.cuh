@@ -60,10 +60,13 @@ struct PairDev {
     const int4 *rowinfo;  // n+2: (min_col, max_col, gapA, bandoff) of row i
     const int *match_lo, *match_hi, *del_lo, *del_hi, *ins_lo, *ins_hi;
     const int *cre_start; // bandcells+1: arc matches with right ends at a band cell
-    const int4 *cre;      // (am, a.l-1, b.l-1, b.r), lex-greater-left-ends order
-    const int4 *crow;     // the same entries by row a.r, then a.l descending, b.l descending
+    const int4 *cre;      // (D index, a.l-1, b.l-1, am), lex-greater-left-ends order
+    const int2 *crow;     // the same arc matches by row a.r, then a.l descending, b.l descending:
+                          // ((a.l-1) | (b.l-1) << 16, b.r); the position is the D index
     const int2 *rowarc;   // n+2: [start, end) of row i's entries in crow
-    int *D;               // num_am
+    int *D;               // num_pos, by crow position
+    const int *am_pos;    // num_am: crow position (D index) of each arc match, -1 if none
+    int num_pos;
     const int4 *am_ends;  // per am: a.l, a.r, b.l, b.r
     const int *am_score;  // per am
     int *topM;            // (n+1)*(m+1), top-level M

@@ -15,17 +15,18 @@ struct PFPair {
     int n, m;
     int num_am;
     const int4 *rowinfo;   // n+2: (min_col, max_col, -, band offset)
-    const int4 *crow;      // (am, a.l-1, b.l-1, b.r) by row a.r, a.l descending
+    const int2 *crow;      // ((a.l-1) | (b.l-1) << 16, b.r) by row a.r, a.l descending
     const int2 *rowarc;    // n+2: [start, end) of row i's entries in crow
     const T *bm;           // (n+1)(m+1) scaled base-match weights
     const T *gA, *gB;      // scaled gap weights
     T o;                   // gap-opening weight
     T inv_s;               // 1 / pf_scale
     T arcf;                // pf_scale / c^4
-    const T *w;            // per am: arc-match weight
-    T *D;                  // per am, NOT_READY pattern until written
-    double *Dbar;          // per am: dZ'/dD (backward), accumulated in FP64
-    int *cnt;              // per am: number of uses still to be back-propagated
+    // per D position (the arc match's position in crow):
+    const T *w;            // arc-match weight
+    T *D;                  // NOT_READY pattern until written
+    double *Dbar;          // dZ'/dD (backward), accumulated in FP64
+    int *cnt;              // number of uses still to be back-propagated
     T *topM;               // (n+1)(m+1)
     double *bmacc;         // per band cell (row offset rowinfo.w): sum of X_bar M(i-1,j-1) bm, FP64
     double *res;           // [0] log Z', [1] gap-extension uses, [2] gap-opening uses

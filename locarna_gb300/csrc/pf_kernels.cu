@@ -165,8 +165,9 @@ __device__ void pf_group_sweep(const PFPair<T> &P, int al, int ar, int bl, int b
         bool rowarcs = false;
         for (int e0 = ra.x; e0 < ra.y; e0 += 32) {
             const int e = e0 + lane;
-            const int4 en = e < ra.y ? P.crow[e] : make_int4(0, -1, -1, 0);
-            const bool okA = en.y >= al;  // a.l > al
+            const int2 en = e < ra.y ? P.crow[e] : make_int2(0xffff, 0);
+            const int ca = en.x & 0xffff, cbl = en.x >> 16;  // inner corner (a.l-1, b.l-1)
+            const bool okA = ca >= al && ca != 0xffff;        // a.l > al
             const unsigned ballA = __ballot_sync(0xffffffffu, okA);
             if (ballA == 0u) break;
             if (!rowarcs) {
@@ -174,12 +175,12 @@ __device__ void pf_group_sweep(const PFPair<T> &P, int al, int ar, int bl, int b
                 __syncwarp();
                 rowarcs = true;
             }
-            if (okA && en.z >= bl && en.w >= lo && en.w <= hi) {
-                T dv = pf_ld(P.D + en.x);
-                if (WAIT && pf_not_ready(dv)) dv = pf_wait(P.D + en.x, status, abort_flag);
-                const T mv = Mg[(size_t)(en.y - al) * pitch + (en.z - bl)];
-                atomicAdd(&R.Ar[RG(en.w)], mv * dv * arcf);
-                if (COUNTU) atomicAdd(P.cnt + en.x, 1);
+            if (okA && cbl >= bl && en.y >= lo && en.y <= hi) {
+                T dv = pf_ld(P.D + e);
+                if (WAIT && pf_not_ready(dv)) dv = pf_wait(P.D + e, status, abort_flag);
+                const T mv = Mg[(size_t)(ca - al) * pitch + (cbl - bl)];
+                atomicAdd(&R.Ar[RG(en.y)], mv * dv * arcf);
+                if (COUNTU) atomicAdd(P.cnt + e, 1);
             }
             if (ballA != 0xffffffffu) break;
         }
@@ -452,17 +453,18 @@ __device__ void pf_group_back(const PFPair<T> &P, int al, int ar, int bl, int br
         // arc terms of row i: M_bar(corner) += X_bar D s', D_bar(am) += X_bar M(corner) s'
         for (int e0 = ra.x; e0 < ra.y; e0 += 32) {
             const int e = e0 + lane;
-            const int4 en = e < ra.y ? P.crow[e] : make_int4(0, -1, -1, 0);
-            const bool okA = en.y >= al;
+            const int2 en = e < ra.y ? P.crow[e] : make_int2(0xffff, 0);
+            const int ca = en.x & 0xffff, cbl = en.x >> 16;
+            const bool okA = ca >= al && ca != 0xffff;
             const unsigned ballA = __ballot_sync(0xffffffffu, okA);
             if (ballA == 0u) break;
-            if (okA && en.z >= bl && en.w >= lo && en.w <= hi) {
-                const T xb = Xb[RG(en.w)];
-                const size_t co = (size_t)(en.y - al) * pitch + (en.z - bl);
-                atomicAdd(Mb + co, xb * P.D[en.x] * arcf);
-                atomicAdd(P.Dbar + en.x, (double)(xb * Mg[co] * arcf));
+            if (okA && cbl >= bl && en.y >= lo && en.y <= hi) {
+                const T xb = Xb[RG(en.y)];
+                const size_t co = (size_t)(ca - al) * pitch + (cbl - bl);
+                atomicAdd(Mb + co, xb * P.D[e] * arcf);
+                atomicAdd(P.Dbar + e, (double)(xb * Mg[co] * arcf));
                 __threadfence();
-                atomicSub(P.cnt + en.x, 1);
+                atomicSub(P.cnt + e, 1);
             }
             if (ballA != 0xffffffffu) break;
         }

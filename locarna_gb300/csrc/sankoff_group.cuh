@@ -86,7 +86,7 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
     const int4 *__restrict__ rowinfo = P.rowinfo;
     const int2 *__restrict__ rowarc = P.rowarc;
     const int *__restrict__ sigma = P.sigma;
-    const int4 *__restrict__ crow = P.crow;
+    const int2 *__restrict__ crow = P.crow;
     int *const Dp = P.D;
     const int m1 = P.m + 1;
     const int go = P.go;
@@ -183,8 +183,9 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
         bool rowarcs = false;
         for (int e0 = acur.x; e0 < acur.y; e0 += 32) {
             const int e = e0 + lane;
-            const int4 en = e < acur.y ? crow[e] : make_int4(0, -1, -1, 0);
-            const bool okA = en.y >= al;  // a.l > al
+            const int2 en = e < acur.y ? crow[e] : make_int2(0xffff, 0);
+            const int ca = en.x & 0xffff, cbl = en.x >> 16;  // inner corner (a.l-1, b.l-1)
+            const bool okA = ca >= al && ca != 0xffff;        // a.l > al
             const unsigned ballA = __ballot_sync(0xffffffffu, okA);
             if (ballA == 0u) break;
             if (!rowarcs) {
@@ -192,16 +193,16 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
                 __syncwarp();
                 rowarcs = true;
             }
-            const bool ok = okA && en.z >= bl && en.w >= lo && en.w <= hi;
+            const bool ok = okA && cbl >= bl && en.y >= lo && en.y <= hi;
             if (COUNT) {
                 n_visits += okA;
                 n_terms += ok;
             }
             if (ok) {
-                int dv = WAIT ? ld_volatile(Dp + en.x) : Dp[en.x];
-                const int mv = Mg[(en.y - al) * pitch + (en.z - bl)];
-                if (WAIT && dv == NOT_READY) dv = wait_D(Dp, en.x, status, abort_flag);
-                atomicMax(&Arow[RG(en.w)], mv + dv);
+                int dv = WAIT ? ld_volatile(Dp + e) : Dp[e];
+                const int mv = Mg[(ca - al) * pitch + (cbl - bl)];
+                if (WAIT && dv == NOT_READY) dv = wait_D(Dp, e, status, abort_flag);
+                atomicMax(&Arow[RG(en.y)], mv + dv);
             }
             if (ballA != 0xffffffffu) break;
         }
@@ -579,9 +580,9 @@ static __device__ __noinline__ void walk(Walker &w, const int *Mg, int pitch, in
             if (alq <= al || blq <= bl) continue;
             if (Mij == MM(alq - 1, blq - 1) + P.D[ent.x]) {
                 w.emit(i, j);
-                w.emit(-2, ent.x);
+                w.emit(-2, ent.w);
                 w.emit(alq, blq);
-                if (w.qtail < P.tq_cap) P.tq[w.qtail] = ent.x;
+                if (w.qtail < P.tq_cap) P.tq[w.qtail] = ent.w;
                 else w.ok = false;
                 ++w.qtail;
                 i = alq - 1;

@@ -451,9 +451,9 @@ static __device__ __noinline__ void walk_sl(Walker &w, const int *Mg, long long 
             if (alq <= al || blq <= bl) continue;
             if (Mij == MS(state, alq - 1, blq - 1) + P.D[ent.x]) {
                 w.emit(i, j);
-                w.emit(-2, ent.x);
+                w.emit(-2, ent.w);
                 w.emit(alq, blq);
-                if (w.qtail < P.tq_cap) P.tq[w.qtail] = ent.x;
+                if (w.qtail < P.tq_cap) P.tq[w.qtail] = ent.w;
                 else w.ok = false;
                 ++w.qtail;
                 i = alq - 1;
@@ -506,7 +506,7 @@ __global__ void __launch_bounds__(TRACE_WARPS * 32)
             // non-open state whose value explains D(am)
             const int ar = ends.y, br = ends.w;
             const long long o = (long long)(ar - 1 - ends.x) * sw + (br - 1 - ends.z);
-            const int dv = P.D[k], sc = P.am_score[k];
+            const int dv = P.D[P.am_pos[k]], sc = P.am_score[k];
             const int start = w.ntok;
             for (int s2 = 0; s2 < 4; ++s2) {
                 if (dv == Mg[s2 * scratch_stride + o] + sc) {

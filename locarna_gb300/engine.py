@@ -45,6 +45,8 @@ def load_library(path=LIB_PATH):
     lib.lcg_engine_last_stats.restype = C.c_int32
     lib.lcg_engine_last_timing.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]
     lib.lcg_engine_last_timing.restype = C.c_int32
+    lib.lcg_engine_last_phases.argtypes = [C.c_void_p] + [C.POINTER(C.c_double)] * 4
+    lib.lcg_engine_last_phases.restype = C.c_int32
     lib.lcg_engine_last_transfer.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
     lib.lcg_engine_last_transfer.restype = C.c_int32
     lib.lcg_engine_set_counting.argtypes = [C.c_void_p, C.c_int32]
@@ -131,6 +133,12 @@ class Engine:
         a, b = C.c_double(), C.c_double()
         _check(self.lib, self.lib.lcg_engine_last_timing(self.h, C.byref(a), C.byref(b)))
         return a.value, b.value
+
+    def last_phases(self):
+        """(prep, pack, copies + kernels, results) wall ms of the last call."""
+        v = [C.c_double() for _ in range(4)]
+        _check(self.lib, self.lib.lcg_engine_last_phases(self.h, *[C.byref(x) for x in v]))
+        return tuple(x.value for x in v)
 
     def last_transfer(self):
         a, b = C.c_int64(), C.c_int64()
