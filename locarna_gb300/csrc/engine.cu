@@ -204,27 +204,43 @@ lcg_status prep_pair(const lcg_pair_tables &t, const lcg_align_opts &o, Prep &p)
     for (int k = 0; k < na; ++k)
         if (cell_of[k] >= 0) ord[fillp[cell_of[k]]++] = k;
     p.cre.resize(4 * ord.size());
+    // (arc matches in the reference's index order come per cell already in
+    // this order; sort only where they do not)
+    auto lex_greater_left = [&](int x, int y) {
+        int alx = p.am_ends[4 * x], aly = p.am_ends[4 * y];
+        if (alx != aly) return alx > aly;
+        return p.am_ends[4 * x + 2] > p.am_ends[4 * y + 2];
+    };
     for (int c = 0; c < p.bandcells; ++c) {
         auto b = ord.begin() + p.cre_start[c], e = ord.begin() + p.cre_start[c + 1];
-        if (e - b > 1)
-            std::sort(b, e, [&](int x, int y) {
-                int alx = p.am_ends[4 * x], aly = p.am_ends[4 * y];
-                if (alx != aly) return alx > aly;
-                return p.am_ends[4 * x + 2] > p.am_ends[4 * y + 2];
-            });
+        if (e - b > 1 && !std::is_sorted(b, e, lex_greater_left)) std::sort(b, e, lex_greater_left);
     }
     // the same candidates per row a.r: a.l descending, then b.l descending
     // (within a row, the valid ones for a group (al,bl) with a.l > al are a
     // prefix). The position of an arc match in this order is also the index
     // of its D entry, so a row's D values are contiguous.
-    std::vector<int> ordr(ord);
-    std::stable_sort(ordr.begin(), ordr.end(), [&](int x, int y) {
-        const int *ex = &p.am_ends[4 * x], *ey = &p.am_ends[4 * y];
-        if (ex[1] != ey[1]) return ex[1] < ey[1];
-        if (ex[0] != ey[0]) return ex[0] > ey[0];
-        if (ex[2] != ey[2]) return ex[2] > ey[2];
-        return ex[3] < ey[3];
-    });
+    // bucket by a.r (counting sort of the arc matches in index order), then
+    // order each row where the index order does not already give it
+    std::vector<int> ordr(ord.size());
+    {
+        std::vector<int> rstart(n + 2, 0);
+        for (int k = 0; k < na; ++k)
+            if (cell_of[k] >= 0) rstart[p.am_ends[4 * k + 1] + 1]++;
+        for (int r = 0; r <= n; ++r) rstart[r + 1] += rstart[r];
+        std::vector<int> fill(rstart.begin(), rstart.end() - 1);
+        for (int k = 0; k < na; ++k)
+            if (cell_of[k] >= 0) ordr[fill[p.am_ends[4 * k + 1]]++] = k;
+        auto row_less = [&](int x, int y) {
+            const int *ex = &p.am_ends[4 * x], *ey = &p.am_ends[4 * y];
+            if (ex[0] != ey[0]) return ex[0] > ey[0];
+            if (ex[2] != ey[2]) return ex[2] > ey[2];
+            return ex[3] < ey[3];
+        };
+        for (int r = 0; r <= n; ++r) {
+            auto b = ordr.begin() + rstart[r], e = ordr.begin() + rstart[r + 1];
+            if (e - b > 1 && !std::is_sorted(b, e, row_less)) std::sort(b, e, row_less);
+        }
+    }
     p.am_pos.assign(na, -1);
     p.crow.resize(2 * ordr.size());
     p.rowarc.assign(2 * (size_t)(n + 2), 0);
@@ -250,12 +266,43 @@ lcg_status prep_pair(const lcg_pair_tables &t, const lcg_align_opts &o, Prep &p)
     p.num_pos = (int)ordr.size();
 
     // left-end groups (aligner.cc:660-732): bucket arc matches by (al,bl)
+    // ordered by (al, bl) descending, index order within equal left ends:
+    // two stable counting sorts (by bl descending, then by al descending)
     std::vector<std::pair<long long, int>> byleft(na);
-    for (int k = 0; k < na; ++k)
-        byleft[k] = {(long long)p.am_ends[4 * k] * (m + 1) + p.am_ends[4 * k + 2], k};
-    std::stable_sort(byleft.begin(), byleft.end(),
-                     [](const auto &x, const auto &y) { return x.first > y.first; });
+    {
+        std::vector<int> tmp(na), cntb(m + 2, 0), cnta(n + 2, 0);
+        for (int k = 0; k < na; ++k) cntb[m - p.am_ends[4 * k + 2] + 1]++;
+        for (int j = 0; j <= m; ++j) cntb[j + 1] += cntb[j];
+        for (int k = 0; k < na; ++k) tmp[cntb[m - p.am_ends[4 * k + 2]]++] = k;
+        for (int k = 0; k < na; ++k) cnta[n - p.am_ends[4 * k] + 1]++;
+        for (int i = 0; i <= n; ++i) cnta[i + 1] += cnta[i];
+        for (int q = 0; q < na; ++q) {
+            const int k = tmp[q];
+            byleft[cnta[n - p.am_ends[4 * k]]++] = {(long long)p.am_ends[4 * k] * (m + 1) + p.am_ends[4 * k + 2], k};
+        }
+    }
     p.Dinit.assign(p.num_pos, NEG);
+    std::vector<int> ks;
+    // band cells of rows [r0, r1) inside columns [A, B], in O(log n) from
+    // prefix sums (min_col and max_col are nondecreasing)
+    std::vector<long long> psmin(n + 2, 0), psmax(n + 2, 0);
+    for (int i = 0; i <= n; ++i) {
+        psmin[i + 1] = psmin[i] + p.min_col[i];
+        psmax[i + 1] = psmax[i] + p.max_col[i];
+    }
+    auto rect_cells = [&](int r0, int r1, int A, int B) -> long long {
+        if (r0 >= r1 || A > B) return 0;
+        const int *mn = p.min_col.data(), *mx = p.max_col.data();
+        // rows whose band lies left of A (max_col < A) or right of B (min_col > B) are empty
+        const int u = (int)(std::lower_bound(mx + r0, mx + r1, A) - mx);
+        const int v = (int)(std::upper_bound(mn + r0, mn + r1, B) - mn);
+        if (u >= v) return 0;
+        const int x = (int)(std::upper_bound(mx + u, mx + v, B) - mx);  // rows [u,x): max_col <= B
+        const int y = (int)(std::upper_bound(mn + u, mn + v, A) - mn);  // rows [u,y): min_col <= A
+        const long long shi = (psmax[x] - psmax[u]) + (long long)B * (v - x);
+        const long long slo = (long long)A * (y - u) + (psmin[v] - psmin[y]);
+        return shi - slo + (v - u);
+    };
     p.rows_max = 0;
     p.width_max = 0;
     for (size_t s = 0; s < byleft.size();) {
@@ -277,9 +324,10 @@ lcg_status prep_pair(const lcg_pair_tables &t, const lcg_align_opts &o, Prep &p)
             g.br = max_br;
             g.dw_start = (int)p.dw.size();
             g.top = 0;
-            std::vector<int> ks;
+            ks.clear();
             for (size_t q = s; q < e; ++q) ks.push_back(byleft[q].second);
-            std::stable_sort(ks.begin(), ks.end(), [&](int x, int y) { return p.am_ends[4 * x + 1] < p.am_ends[4 * y + 1]; });
+            auto ar_less = [&](int x, int y) { return p.am_ends[4 * x + 1] < p.am_ends[4 * y + 1]; };
+            if (!std::is_sorted(ks.begin(), ks.end(), ar_less)) std::stable_sort(ks.begin(), ks.end(), ar_less);
             for (int k : ks) {
                 int ar = p.am_ends[4 * k + 1], br = p.am_ends[4 * k + 3];
                 // the inner corner (ar-1,br-1) is computed by this group iff it is in the band
@@ -290,15 +338,8 @@ lcg_status prep_pair(const lcg_pair_tables &t, const lcg_align_opts &o, Prep &p)
                 }
             }
             g.dw_count = (int)p.dw.size() - g.dw_start;
-            int wmax = 1;
-            for (int i = al + 1; i < max_ar; ++i) {
-                int lo = std::max(bl + 1, p.min_col[i]), hi = std::min(max_br - 1, p.max_col[i]);
-                if (hi >= lo) {
-                    p.cells += hi - lo + 1;
-                    wmax = std::max(wmax, hi - lo + 1);
-                }
-            }
-            g.cpl = std::min(4, (wmax + 31) / 32);
+            p.cells += rect_cells(al + 1, max_ar, bl + 1, max_br - 1);
+            g.cpl = 1;
             p.groups.push_back(g);
             p.rows_max = std::max(p.rows_max, max_ar - al);
             p.width_max = std::max(p.width_max, max_br - bl + 1);
@@ -491,7 +532,7 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
     }
     struct Off {
         size_t sigma, scls, rcls, ccls, gapA, gapB, minc, maxc, bandoff, rowinfo, anc, cre_start, cre, crow, rowarc,
-            am_pos, am_ends, am_score, D,
+            am_score, D,
             topM, res, tok, tq, segs;
     };
     std::vector<Off> off(npairs);
@@ -530,8 +571,6 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
         o.cre = take(up, 4ull * std::max<size_t>(p.cre.size(), 4));
         o.crow = take(up, 4ull * std::max<size_t>(p.crow.size(), 4));
         o.rowarc = take(up, 4ull * p.rowarc.size());
-        o.am_ends = take(up, 4ull * std::max<size_t>(p.am_ends.size(), 4));
-        o.am_pos = take(up, 4ull * std::max(t.num_arcmatches, 1));
         o.am_score = take(up, 4ull * std::max(t.num_arcmatches, 1));
         o.D = take(up, 4ull * std::max(p.num_pos, 1));
     }
@@ -549,7 +588,7 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
     for (int q = 0; q < npairs; ++q) {
         const auto &p = prep[q];
         Off &o = off[q];
-        o.tq = take(dev_only, 4ull * p.tq_cap);
+        o.tq = take(dev_only, 16ull * p.tq_cap);
         o.topM = take(dev_only, 4ull * (p.n + 1) * (p.m + 1));
     }
     size_t total = dev_only;
@@ -584,23 +623,10 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
         // pairs' work lists are interleaved so that every pair progresses
         // proportionally; within a pair the order is kept. Waves follow each
         // other in the queue without a barrier.
-        const double wave_bytes = lcg_host::wave_budget_bytes();
-        std::vector<std::pair<double, std::pair<int, int>>> order;
-        order.reserve(nitems);
-        double acc = 0.0;
-        int wave = 0;
-        for (int q = 0; q < npairs; ++q) {
-            const auto &p = prep[q];
-            const double fp = 12.0 * p.num_pos + 4.0 * p.bandcells;
-            if (acc > 0.0 && acc + fp > wave_bytes) {
-                ++wave;
-                acc = 0.0;
-            }
-            acc += fp;
-            size_t G = p.groups.size();
-            for (size_t g = 0; g < G; ++g) order.push_back({wave + (double)(g + 1) / (double)G, {q, (int)g}});
-        }
-        std::stable_sort(order.begin(), order.end(), [](const auto &a, const auto &b) { return a.first < b.first; });
+        std::vector<size_t> ng(npairs);
+        for (int q = 0; q < npairs; ++q) ng[q] = prep[q].groups.size();
+        const std::vector<std::pair<int, int>> order = lcg_host::queue_order(
+            ng, [&](int q) { return 12.0 * prep[q].num_pos + 4.0 * prep[q].bandcells; });
         std::vector<size_t> dwbase(npairs);
         for (int q = 0; q < npairs; ++q) {
             dwbase[q] = dwb;
@@ -608,8 +634,8 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
             dwb += prep[q].dw.size();
         }
         for (auto &x : order) {
-            int q = x.second.first;
-            GroupItem g = prep[q].groups[x.second.second];
+            int q = x.first;
+            GroupItem g = prep[q].groups[x.second];
             g.pair = q;
             g.dw_start += (int)dwbase[q];
             hitems[it++] = g;
@@ -646,10 +672,8 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
         if (!p.cre.empty()) std::memcpy(H + o.cre, p.cre.data(), 4ull * p.cre.size());
         if (!p.crow.empty()) std::memcpy(H + o.crow, p.crow.data(), 4ull * p.crow.size());
         std::memcpy(H + o.rowarc, p.rowarc.data(), 4ull * p.rowarc.size());
-        if (!p.am_ends.empty()) std::memcpy(H + o.am_ends, p.am_ends.data(), 4ull * p.am_ends.size());
         if (p.num_pos) std::memcpy(H + o.D, p.Dinit.data(), 4ull * p.num_pos);
         if (t.num_arcmatches) {
-            std::memcpy(H + o.am_pos, p.am_pos.data(), 4ull * t.num_arcmatches);
             std::memcpy(H + o.am_score, t.am_score, 4ull * t.num_arcmatches);
         }
         PairDev &d = hp[q];
@@ -691,17 +715,15 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
         d.cre_start = (const int *)(Dv + o.cre_start);
         d.cre = (const int4 *)(Dv + o.cre);
         d.crow = (const int2 *)(Dv + o.crow);
-        d.am_pos = (const int *)(Dv + o.am_pos);
         d.num_pos = p.num_pos;
         d.rowarc = (const int2 *)(Dv + o.rowarc);
         d.D = (int *)(Dv + o.D);
-        d.am_ends = (const int4 *)(Dv + o.am_ends);
         d.am_score = (const int *)(Dv + o.am_score);
         d.topM = (int *)(Dv + o.topM);
         d.res = (int *)(Dv + o.res);
         d.tokens = (int2 *)(Dv + o.tok);
         d.token_cap = p.token_cap;
-        d.tq = (int *)(Dv + o.tq);
+        d.tq = (int4 *)(Dv + o.tq);
         d.tq_cap = p.tq_cap;
         d.segs = (int4 *)(Dv + o.segs);
     });

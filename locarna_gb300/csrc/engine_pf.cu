@@ -205,22 +205,11 @@ lcg_status pf_forward_t(lcg_engine e, PFState *S, const lcg_pair_tables *pairs, 
     {
         // waves of pairs whose tables fit a share of L2, interleaved by
         // progress inside a wave (as for lcg_align_pairs)
-        const double wave_bytes = lcg_host::wave_budget_bytes();
-        std::vector<std::pair<double, std::pair<int, int>>> order;
-        order.reserve(nitems);
-        double acc = 0.0;
-        int wave = 0;
-        for (int q = 0; q < npairs; ++q) {
-            const double fp = (12.0 + 3.0 * sizeof(T)) * prep[q].num_pos + 3.0 * sizeof(T) * prep[q].bandcells;
-            if (acc > 0.0 && acc + fp > wave_bytes) {
-                ++wave;
-                acc = 0.0;
-            }
-            acc += fp;
-            size_t G = prep[q].groups.size();
-            for (size_t g = 0; g < G; ++g) order.push_back({wave + (double)(g + 1) / (double)G, {q, (int)g}});
-        }
-        std::stable_sort(order.begin(), order.end(), [](const auto &a, const auto &b) { return a.first < b.first; });
+        std::vector<size_t> ng(npairs);
+        for (int q = 0; q < npairs; ++q) ng[q] = prep[q].groups.size();
+        const std::vector<std::pair<int, int>> order = lcg_host::queue_order(ng, [&](int q) {
+            return (12.0 + 3.0 * sizeof(T)) * prep[q].num_pos + 3.0 * sizeof(T) * prep[q].bandcells;
+        });
         std::vector<size_t> dwbase(npairs);
         size_t dwb = 0;
         for (int q = 0; q < npairs; ++q) {
@@ -230,8 +219,8 @@ lcg_status pf_forward_t(lcg_engine e, PFState *S, const lcg_pair_tables *pairs, 
         }
         size_t it = 0;
         for (auto &x : order) {
-            const int q = x.second.first;
-            const GroupItem &g = prep[q].groups[x.second.second];
+            const int q = x.first;
+            const GroupItem &g = prep[q].groups[x.second];
             PFItem<T> pi;
             pi.pair = q;
             pi.al = g.al;

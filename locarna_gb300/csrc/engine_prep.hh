@@ -65,6 +65,42 @@ inline double wave_budget_bytes() {
     return (mb > 0 ? mb : 1e9) * 1048576.0;
 }
 
+// Work-queue order of the groups of a batch: pairs in waves whose tables
+// (bytes(q)) fit wave_budget_bytes(); inside a wave, the pairs' lists are
+// interleaved by progress, quantised to 4096 steps; each pair's own order is
+// kept. Returns (pair, group index) in queue order; a counting sort, O(items).
+template <typename BytesOf>
+std::vector<std::pair<int, int>> queue_order(const std::vector<size_t> &ngroups, BytesOf bytes) {
+    const int npairs = (int)ngroups.size();
+    constexpr int NB = 4096;
+    const double budget = wave_budget_bytes();
+    std::vector<int> wave(npairs);
+    double acc = 0.0;
+    int w = 0;
+    for (int q = 0; q < npairs; ++q) {
+        const double fp = bytes(q);
+        if (acc > 0.0 && acc + fp > budget) {
+            ++w;
+            acc = 0.0;
+        }
+        acc += fp;
+        wave[q] = w;
+    }
+    const size_t nkeys = (size_t)(w + 1) * NB;
+    std::vector<size_t> start(nkeys + 1, 0);
+    auto key = [&](int q, size_t g) {
+        const size_t G = ngroups[q];
+        return (size_t)wave[q] * NB + ((g + 1) * NB - 1) / G;  // nondecreasing in g, < NB
+    };
+    for (int q = 0; q < npairs; ++q)
+        for (size_t g = 0; g < ngroups[q]; ++g) ++start[key(q, g) + 1];
+    for (size_t k = 0; k < nkeys; ++k) start[k + 1] += start[k];
+    std::vector<std::pair<int, int>> out(start[nkeys]);
+    for (int q = 0; q < npairs; ++q)
+        for (size_t g = 0; g < ngroups[q]; ++g) out[start[key(q, g)]++] = {q, (int)g};
+    return out;
+}
+
 // fn(q) for q in [0, n) on up to 64 host threads (dynamic assignment)
 template <typename F>
 void parallel_for(int n, F &&fn) {

@@ -65,15 +65,14 @@ struct PairDev {
                           // ((a.l-1) | (b.l-1) << 16, b.r); the position is the D index
     const int2 *rowarc;   // n+2: [start, end) of row i's entries in crow
     int *D;               // num_pos, by crow position
-    const int *am_pos;    // num_am: crow position (D index) of each arc match, -1 if none
     int num_pos;
-    const int4 *am_ends;  // per am: a.l, a.r, b.l, b.r
     const int *am_score;  // per am
     int *topM;            // (n+1)*(m+1), top-level M
     int *res;             // result words, see Res
     int2 *tokens;         // traceback tokens
     int token_cap;
-    int *tq;              // traceback queue of arc matches (capacity tq_cap)
+    int4 *tq;             // traceback queue of arc matches (capacity tq_cap):
+                          // (am, D index, a.l | b.l << 16, a.r | b.r << 16)
     int tq_cap;
     int4 *segs;           // traceback segments: (am or -1, token start, token end, 0)
 };

@@ -126,10 +126,8 @@ extern "C" lcg_status lcg_align_score_static(const lcg_pair_tables *pair, const 
     const size_t o_cre = take(4ull * std::max<size_t>(p.cre.size(), 4));
     const size_t o_crow = take(4ull * std::max<size_t>(p.crow.size(), 4));
     const size_t o_rowarc = take(4ull * p.rowarc.size());
-    const size_t o_ends = take(4ull * std::max<size_t>(p.am_ends.size(), 4));
     const size_t o_score = take(4ull * std::max(na, 1));
     const size_t o_D = take(4ull * std::max(p.num_pos, 1));
-    const size_t o_pos = take(4ull * std::max(na, 1));
     const size_t o_top = take(4ull * (n + 1) * (m + 1));
     const size_t fixed = off;
     const long long stride = (long long)rows_max * sw;  // ints per warp slot
@@ -189,11 +187,9 @@ extern "C" lcg_status lcg_align_score_static(const lcg_pair_tables *pair, const 
     d.cre_start = (const int *)(base + o_cs);
     d.cre = (const int4 *)(base + o_cre);
     d.crow = (const int2 *)(base + o_crow);
-    d.am_pos = (const int *)(base + o_pos);
     d.num_pos = p.num_pos;
     d.rowarc = (const int2 *)(base + o_rowarc);
     d.D = (int *)(base + o_D);
-    d.am_ends = (const int4 *)(base + o_ends);
     d.am_score = (const int *)(base + o_score);
     d.topM = (int *)(base + o_top);
     d.res = (int *)(base + o_res);
@@ -234,10 +230,8 @@ extern "C" lcg_status lcg_align_score_static(const lcg_pair_tables *pair, const 
     STATIC_TRY(h2d(o_cre, p.cre.data(), 4ull * p.cre.size()));
     STATIC_TRY(h2d(o_crow, p.crow.data(), 4ull * p.crow.size()));
     STATIC_TRY(h2d(o_rowarc, p.rowarc.data(), 4ull * p.rowarc.size()));
-    STATIC_TRY(h2d(o_ends, p.am_ends.data(), 4ull * p.am_ends.size()));
     STATIC_TRY(h2d(o_score, pair->am_score, 4ull * na));
     STATIC_TRY(h2d(o_D, p.Dinit.data(), 4ull * p.num_pos));
-    STATIC_TRY(h2d(o_pos, p.am_pos.data(), 4ull * na));
 
     STATIC_TRY(launch_fill((const PairDev *)(base + o_pair), (const GroupItem *)(base + o_items),
                            (int)p.groups.size(), (const int4 *)(base + o_dw), scratch, stride, sw, rb, fast,

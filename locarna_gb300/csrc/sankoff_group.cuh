@@ -507,7 +507,6 @@ static __device__ __noinline__ void walk(Walker &w, const int *Mg, int pitch, in
     const PairDev &P = w.P;
     const bool local = P.flags & PF_SEQU_LOCAL;
     const int fe = P.free_endgaps;
-    const int m1 = P.m + 1;
     const int go = P.go;
 #define MM(x, y) Mg[(size_t)((x) - al) * pitch + ((y) - bl)]
     for (int guard = 0; guard < 4 * (P.n + P.m + 4); ++guard) {
@@ -582,7 +581,7 @@ static __device__ __noinline__ void walk(Walker &w, const int *Mg, int pitch, in
                 w.emit(i, j);
                 w.emit(-2, ent.w);
                 w.emit(alq, blq);
-                if (w.qtail < P.tq_cap) P.tq[w.qtail] = ent.w;
+                if (w.qtail < P.tq_cap) P.tq[w.qtail] = make_int4(ent.w, ent.x, alq | (blq << 16), i | (j << 16));
                 else w.ok = false;
                 ++w.qtail;
                 i = alq - 1;

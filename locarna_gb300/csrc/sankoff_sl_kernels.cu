@@ -63,7 +63,6 @@ __device__ void run_group_sl(const PairDev &P, int al, int ar, int bl, int br, i
                              const int4 *__restrict__ dw, int ndw, int *status,
                              volatile int *abort_flag) {
     const int lane = threadIdx.x & 31;
-    const int m1 = P.m + 1;
     const int go = P.go, X = P.excl;
     const int W = br - bl;
     int *prev[6], *cur[6];
@@ -341,7 +340,6 @@ static __device__ __noinline__ void walk_sl(Walker &w, const int *Mg, long long 
     const PairDev &P = w.P;
     const bool local = P.flags & PF_SEQU_LOCAL;
     const int fe = P.free_endgaps;
-    const int m1 = P.m + 1;
     const int go = P.go, X = P.excl;
 #define MS(s, x, y) Mg[(long long)(s) * mstride + (long long)((x) - al) * pitch + ((y) - bl)]
     for (int guard = 0; guard < 8 * (P.n + P.m + 4); ++guard) {
@@ -453,7 +451,7 @@ static __device__ __noinline__ void walk_sl(Walker &w, const int *Mg, long long 
                 w.emit(i, j);
                 w.emit(-2, ent.w);
                 w.emit(alq, blq);
-                if (w.qtail < P.tq_cap) P.tq[w.qtail] = ent.w;
+                if (w.qtail < P.tq_cap) P.tq[w.qtail] = make_int4(ent.w, ent.x, alq | (blq << 16), i | (j << 16));
                 else w.ok = false;
                 ++w.qtail;
                 i = alq - 1;
@@ -492,12 +490,13 @@ __global__ void __launch_bounds__(TRACE_WARPS * 32)
     }
     int qtail = __shfl_sync(0xffffffffu, w.qtail, 0);
     while (qhead < qtail) {
-        int k = 0;
-        if (lane == 0) k = qhead < P.tq_cap ? P.tq[qhead] : -1;
-        k = __shfl_sync(0xffffffffu, k, 0);
+        int4 qe = make_int4(-1, 0, 0, 0);
+        if (lane == 0 && qhead < P.tq_cap) qe = P.tq[qhead];
+        const int k = __shfl_sync(0xffffffffu, qe.x, 0), kpos = __shfl_sync(0xffffffffu, qe.y, 0);
+        const int lefts = __shfl_sync(0xffffffffu, qe.z, 0), rights = __shfl_sync(0xffffffffu, qe.w, 0);
         ++qhead;
         if (k < 0) break;
-        const int4 ends = P.am_ends[k];  // a.l, a.r, b.l, b.r
+        const int4 ends = make_int4(lefts & 0xffff, rights & 0xffff, lefts >> 16, rights >> 16);  // a.l, a.r, b.l, b.r
         run_group_sl<false, false, 8>(P, ends.x, ends.y, ends.z, ends.w, Mg, scratch_stride, sw, sm, sw,
                                       nullptr, 0, status, (volatile int *)&dummy_abort);
         __syncwarp();
@@ -506,7 +505,7 @@ __global__ void __launch_bounds__(TRACE_WARPS * 32)
             // non-open state whose value explains D(am)
             const int ar = ends.y, br = ends.w;
             const long long o = (long long)(ar - 1 - ends.x) * sw + (br - 1 - ends.z);
-            const int dv = P.D[P.am_pos[k]], sc = P.am_score[k];
+            const int dv = P.D[kpos], sc = P.am_score[k];
             const int start = w.ntok;
             for (int s2 = 0; s2 < 4; ++s2) {
                 if (dv == Mg[s2 * scratch_stride + o] + sc) {
