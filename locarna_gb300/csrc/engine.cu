@@ -533,7 +533,7 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
     struct Off {
         size_t sigma, scls, rcls, ccls, gapA, gapB, minc, maxc, bandoff, rowinfo, anc, cre_start, cre, crow, rowarc,
             am_score, D,
-            topM, res, tok, tq, segs;
+            topM, res, tok, tq, segs, groups, dw;
     };
     std::vector<Off> off(npairs);
     size_t up = 0;  // upload section (bytes)
@@ -543,18 +543,16 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
         return o;
     };
     size_t off_pairs = take(up, sizeof(PairDev) * npairs);
-    size_t nitems = 0, ndw = 0;
-    for (auto &p : prep) {
-        nitems += p.groups.size();
-        ndw += p.dw.size();
-    }
-    size_t off_items = take(up, sizeof(GroupItem) * nitems);
-    size_t off_dw = take(up, sizeof(int4) * std::max<size_t>(ndw, 1));
+    size_t nitems = 0;
+    for (auto &p : prep) nitems += p.groups.size();
+    size_t off_queue = take(up, sizeof(int2) * nitems);  // (pair, group) work items
     size_t off_ctrl = take(up, 64);  // qhead, status, abort, pad, 2 x u64 counters
     for (int q = 0; q < npairs; ++q) {
         const auto &p = prep[q];
         const auto &t = pairs[q];
         Off &o = off[q];
+        o.groups = take(up, sizeof(GroupItem) * p.groups.size());
+        o.dw = take(up, sizeof(int4) * std::max<size_t>(p.dw.size(), 1));
         // sigma: the class table when it exists, else the dense table
         o.sigma = p.use_cls ? 0 : take(up, 4ull * (p.n + 1) * (p.m + 1));
         o.scls = p.use_cls ? take(up, 4ull * 256) : 0;
@@ -614,9 +612,6 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
 
     // ---- pack the upload
     PairDev *hp = (PairDev *)(H + off_pairs);
-    GroupItem *hitems = (GroupItem *)(H + off_items);
-    int4 *hdw = (int4 *)(H + off_dw);
-    size_t it = 0, dwb = 0;
     {
         // pairs in waves whose per-pair tables (candidate lists, D, top
         // level) together stay within a share of L2; inside a wave the
@@ -625,21 +620,9 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
         // other in the queue without a barrier.
         std::vector<size_t> ng(npairs);
         for (int q = 0; q < npairs; ++q) ng[q] = prep[q].groups.size();
-        const std::vector<std::pair<int, int>> order = lcg_host::queue_order(
-            ng, [&](int q) { return 12.0 * prep[q].num_pos + 4.0 * prep[q].bandcells; });
-        std::vector<size_t> dwbase(npairs);
-        for (int q = 0; q < npairs; ++q) {
-            dwbase[q] = dwb;
-            std::memcpy(hdw + dwb, prep[q].dw.data(), sizeof(int4) * prep[q].dw.size());
-            dwb += prep[q].dw.size();
-        }
-        for (auto &x : order) {
-            int q = x.first;
-            GroupItem g = prep[q].groups[x.second];
-            g.pair = q;
-            g.dw_start += (int)dwbase[q];
-            hitems[it++] = g;
-        }
+        lcg_host::queue_order(
+            ng, [&](int q) { return 12.0 * prep[q].num_pos + 4.0 * prep[q].bandcells; }, (int2 *)(H + off_queue),
+            [](int n, auto fn) { lcg_host::parallel_for(n, fn); });
     }
     std::memset(H + off_ctrl, 0, 64);
     lcg_host::parallel_for(npairs, [&](int q) {
@@ -676,6 +659,12 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
         if (t.num_arcmatches) {
             std::memcpy(H + o.am_score, t.am_score, 4ull * t.num_arcmatches);
         }
+        GroupItem *hg = (GroupItem *)(H + o.groups);
+        for (size_t g = 0; g < p.groups.size(); ++g) {
+            hg[g] = p.groups[g];
+            hg[g].pair = q;
+        }
+        if (!p.dw.empty()) std::memcpy(H + o.dw, p.dw.data(), sizeof(int4) * p.dw.size());
         PairDev &d = hp[q];
         std::memset(&d, 0, sizeof d);
         d.n = p.n;
@@ -726,6 +715,8 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
         d.tq = (int4 *)(Dv + o.tq);
         d.tq_cap = p.tq_cap;
         d.segs = (int4 *)(Dv + o.segs);
+        d.groups = (const GroupItem *)(Dv + o.groups);
+        d.dw = (const int4 *)(Dv + o.dw);
     });
 
     const auto t2 = clk::now();
@@ -768,12 +759,12 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
     unsigned long long *counters = e->counting ? (unsigned long long *)(Dv + off_ctrl + 16) : nullptr;
     if (sl) {
         if (counters) return fail(LCG_ERR_UNSUPPORTED, "work counting covers the plain mode only");
-        CUDA_TRY(launch_sl_fill((const PairDev *)(Dv + off_pairs), (const GroupItem *)(Dv + off_items),
-                                (int)nitems, (const int4 *)(Dv + off_dw), e->d_scratch, stride, sw, rb, qhead,
+        CUDA_TRY(launch_sl_fill((const PairDev *)(Dv + off_pairs), (const int2 *)(Dv + off_queue),
+                                (int)nitems, e->d_scratch, stride, sw, rb, qhead,
                                 status, abort_flag, blocks, st));
     } else {
-        CUDA_TRY(launch_fill((const PairDev *)(Dv + off_pairs), (const GroupItem *)(Dv + off_items),
-                             (int)nitems, (const int4 *)(Dv + off_dw), e->d_scratch, stride, sw, rb, fast, qhead,
+        CUDA_TRY(launch_fill((const PairDev *)(Dv + off_pairs), (const int2 *)(Dv + off_queue),
+                             (int)nitems, e->d_scratch, stride, sw, rb, fast, qhead,
                              status, abort_flag, blocks, st, counters));
     }
     CUDA_TRY(cudaEventRecord(e->ev1, st));

@@ -40,7 +40,7 @@ size_t up16(size_t x) { return (x + 15) / 16 * 16; }
 
 struct PFLayout {
     int n, m, na, npos, bandcells;  // npos: D entries (arc matches with a band cell as right ends)
-    size_t rowinfo, crow, rowarc, bm, gA, gB, w, D, Dbar, cnt, bmacc, res, topM;
+    size_t rowinfo, crow, rowarc, groups, dw, bm, gA, gB, w, D, Dbar, cnt, bmacc, res, topM;
     double log_c_total;  // (n+m) log c
 };
 
@@ -54,7 +54,7 @@ struct PFState {
     char *d_scratch = nullptr;
     size_t scratch_cap = 0;
     std::vector<PFLayout> lay;
-    size_t off_pairs = 0, off_items = 0, off_dw = 0, off_ctrl = 0, out_begin = 0, out_end = 0, total = 0;
+    size_t off_pairs = 0, off_queue = 0, off_ctrl = 0, out_begin = 0, out_end = 0, total = 0;
     size_t nitems = 0;
     int sw = 0, rb = 0;
     long long stride = 0;
@@ -138,11 +138,10 @@ lcg_status pf_forward_t(lcg_engine e, PFState *S, const lcg_pair_tables *pairs, 
         cur = up16(cur + bytes);
         return r;
     };
-    size_t nitems = 0, ndw = 0;
+    size_t nitems = 0;
     int sw = 0, rows_max = 1, span = 2;
     for (auto &p : prep) {
         nitems += p.groups.size();
-        ndw += p.dw.size();
         sw = std::max(sw, std::max(p.width_max + 1, p.m + 2));
         rows_max = std::max(rows_max, std::max(p.rows_max + 1, p.n + 1));
         // widest column range two consecutive band rows cover (plus the
@@ -150,8 +149,7 @@ lcg_status pf_forward_t(lcg_engine e, PFState *S, const lcg_pair_tables *pairs, 
         for (int i = 0; i < p.n; ++i) span = std::max(span, p.max_col[i + 1] - p.min_col[i] + 3);
     }
     S->off_pairs = take(up, sizeof(PFPair<T>) * npairs);
-    S->off_items = take(up, sizeof(PFItem<T>) * nitems);
-    S->off_dw = take(up, sizeof(int4) * std::max<size_t>(ndw, 1));
+    S->off_queue = take(up, sizeof(int2) * nitems);
     S->off_ctrl = take(up, 64);
     for (int q = 0; q < npairs; ++q) {
         const auto &p = prep[q];
@@ -164,6 +162,8 @@ lcg_status pf_forward_t(lcg_engine e, PFState *S, const lcg_pair_tables *pairs, 
         L.rowinfo = take(up, 16ull * (p.n + 2));
         L.crow = take(up, 4ull * std::max<size_t>(p.crow.size(), 4));
         L.rowarc = take(up, 4ull * p.rowarc.size());
+        L.groups = take(up, sizeof(GroupItem) * p.groups.size());
+        L.dw = take(up, sizeof(int4) * std::max<size_t>(p.dw.size(), 1));
         L.bm = take(up, sizeof(T) * (p.n + 1) * (p.m + 1));
         L.gA = take(up, sizeof(T) * (p.n + 1));
         L.gB = take(up, sizeof(T) * (p.m + 1));
@@ -200,38 +200,17 @@ lcg_status pf_forward_t(lcg_engine e, PFState *S, const lcg_pair_tables *pairs, 
     char *H = S->h_stage, *Dv = S->d_arena;
     // pack
     PFPair<T> *hp = (PFPair<T> *)(H + S->off_pairs);
-    PFItem<T> *hit = (PFItem<T> *)(H + S->off_items);
-    int4 *hdw = (int4 *)(H + S->off_dw);
     {
         // waves of pairs whose tables fit a share of L2, interleaved by
         // progress inside a wave (as for lcg_align_pairs)
         std::vector<size_t> ng(npairs);
         for (int q = 0; q < npairs; ++q) ng[q] = prep[q].groups.size();
-        const std::vector<std::pair<int, int>> order = lcg_host::queue_order(ng, [&](int q) {
-            return (12.0 + 3.0 * sizeof(T)) * prep[q].num_pos + 3.0 * sizeof(T) * prep[q].bandcells;
-        });
-        std::vector<size_t> dwbase(npairs);
-        size_t dwb = 0;
-        for (int q = 0; q < npairs; ++q) {
-            dwbase[q] = dwb;
-            for (size_t k = 0; k < prep[q].dw.size(); ++k) hdw[dwb + k] = prep[q].dw[k];
-            dwb += prep[q].dw.size();
-        }
-        size_t it = 0;
-        for (auto &x : order) {
-            const int q = x.first;
-            const GroupItem &g = prep[q].groups[x.second];
-            PFItem<T> pi;
-            pi.pair = q;
-            pi.al = g.al;
-            pi.ar = g.ar;
-            pi.bl = g.bl;
-            pi.br = g.br;
-            pi.dw_start = g.dw_start + (int)dwbase[q];
-            pi.dw_count = g.dw_count;
-            pi.top = g.top;
-            hit[it++] = pi;
-        }
+        lcg_host::queue_order(
+            ng,
+            [&](int q) {
+                return (12.0 + 3.0 * sizeof(T)) * prep[q].num_pos + 3.0 * sizeof(T) * prep[q].bandcells;
+            },
+            (int2 *)(H + S->off_queue), [](int n, auto fn) { lcg_host::parallel_for(n, fn); });
     }
     std::memset(H + S->off_ctrl, 0, 64);
     // per pair: Boltzmann weights, scale factor and packed tables (disjoint
@@ -264,6 +243,8 @@ lcg_status pf_forward_t(lcg_engine e, PFState *S, const lcg_pair_tables *pairs, 
         L.log_c_total = logc * (n + m);
         std::memcpy(H + L0.rowinfo, p.rowinfo.data(), 16ull * (n + 2));
         if (!p.crow.empty()) std::memcpy(H + L0.crow, p.crow.data(), 4ull * p.crow.size());
+        std::memcpy(H + L0.groups, p.groups.data(), sizeof(GroupItem) * p.groups.size());
+        if (!p.dw.empty()) std::memcpy(H + L0.dw, p.dw.data(), sizeof(int4) * p.dw.size());
         std::memcpy(H + L0.rowarc, p.rowarc.data(), 4ull * p.rowarc.size());
         T *hbm = (T *)(H + L0.bm);
         for (size_t k = 0; k < bm.size(); ++k) hbm[k] = (T)(bm[k] / c2);
@@ -298,6 +279,8 @@ lcg_status pf_forward_t(lcg_engine e, PFState *S, const lcg_pair_tables *pairs, 
         d.num_am = L.na;
         d.rowinfo = (const int4 *)(Dv + L0.rowinfo);
         d.crow = (const int2 *)(Dv + L0.crow);
+        d.groups = (const GroupItem *)(Dv + L0.groups);
+        d.dw = (const int4 *)(Dv + L0.dw);
         d.rowarc = (const int2 *)(Dv + L0.rowarc);
         d.bm = (const T *)(Dv + L0.bm);
         d.gA = (const T *)(Dv + L0.gA);
@@ -338,7 +321,7 @@ lcg_status pf_forward_t(lcg_engine e, PFState *S, const lcg_pair_tables *pairs, 
     int *status = (int *)(Dv + S->off_ctrl + 4);
     int *abort_flag = (int *)(Dv + S->off_ctrl + 8);
     PF_TRY(cudaEventRecord(e->ev0, st));
-    PF_TRY(pf_launch_fwd<T>(Dv + S->off_pairs, Dv + S->off_items, (int)nitems, (const int4 *)(Dv + S->off_dw),
+    PF_TRY(pf_launch_fwd<T>(Dv + S->off_pairs, (const int2 *)(Dv + S->off_queue), (int)nitems,
                             S->d_scratch, stride, sw, rb, qhead, status, abort_flag, e->sms * bf, true, st));
     PF_TRY(cudaEventRecord(e->ev1, st));
     PF_TRY(cudaMemcpyAsync(H + S->off_ctrl, Dv + S->off_ctrl, 64, cudaMemcpyDeviceToHost, st));
@@ -380,7 +363,7 @@ lcg_status pf_backward_t(lcg_engine e, PFState *S, const lcg_pf_grad_spec *grads
     int *status = (int *)(Dv + S->off_ctrl + 4);
     int *abort_flag = (int *)(Dv + S->off_ctrl + 8);
     PF_TRY(cudaEventRecord(e->ev1, st));
-    PF_TRY(pf_launch_back<T>(Dv + S->off_pairs, Dv + S->off_items, (int)S->nitems, (const int4 *)(Dv + S->off_dw),
+    PF_TRY(pf_launch_back<T>(Dv + S->off_pairs, (const int2 *)(Dv + S->off_queue), (int)S->nitems,
                              S->d_scratch, S->stride, S->sw, S->rb, qhead, status, abort_flag, e->sms * bb, st));
     PF_TRY(cudaEventRecord(e->ev2, st));
     PF_TRY(cudaMemcpyAsync(H + S->off_ctrl, Dv + S->off_ctrl, 64, cudaMemcpyDeviceToHost, st));

@@ -68,37 +68,39 @@ inline double wave_budget_bytes() {
 // Work-queue order of the groups of a batch: pairs in waves whose tables
 // (bytes(q)) fit wave_budget_bytes(); inside a wave, the pairs' lists are
 // interleaved by progress, quantised to 4096 steps; each pair's own order is
-// kept. Returns (pair, group index) in queue order; a counting sort, O(items).
-template <typename BytesOf>
-std::vector<std::pair<int, int>> queue_order(const std::vector<size_t> &ngroups, BytesOf bytes) {
+// kept. Writes (pair, group index) in queue order to out[0 .. total); one
+// counting sort per wave, waves in parallel.
+template <typename BytesOf, typename ParallelFor>
+void queue_order(const std::vector<size_t> &ngroups, BytesOf bytes, int2 *out, ParallelFor pfor) {
     const int npairs = (int)ngroups.size();
-    constexpr int NB = 4096;
+    constexpr size_t NB = 4096;
     const double budget = wave_budget_bytes();
-    std::vector<int> wave(npairs);
+    std::vector<int> wave_first;  // first pair of each wave
+    std::vector<size_t> wave_off;  // first output slot of each wave
     double acc = 0.0;
-    int w = 0;
+    size_t items = 0;
     for (int q = 0; q < npairs; ++q) {
         const double fp = bytes(q);
-        if (acc > 0.0 && acc + fp > budget) {
-            ++w;
+        if (q == 0 || (acc > 0.0 && acc + fp > budget)) {
+            wave_first.push_back(q);
+            wave_off.push_back(items);
             acc = 0.0;
         }
         acc += fp;
-        wave[q] = w;
+        items += ngroups[q];
     }
-    const size_t nkeys = (size_t)(w + 1) * NB;
-    std::vector<size_t> start(nkeys + 1, 0);
-    auto key = [&](int q, size_t g) {
-        const size_t G = ngroups[q];
-        return (size_t)wave[q] * NB + ((g + 1) * NB - 1) / G;  // nondecreasing in g, < NB
-    };
-    for (int q = 0; q < npairs; ++q)
-        for (size_t g = 0; g < ngroups[q]; ++g) ++start[key(q, g) + 1];
-    for (size_t k = 0; k < nkeys; ++k) start[k + 1] += start[k];
-    std::vector<std::pair<int, int>> out(start[nkeys]);
-    for (int q = 0; q < npairs; ++q)
-        for (size_t g = 0; g < ngroups[q]; ++g) out[start[key(q, g)]++] = {q, (int)g};
-    return out;
+    wave_first.push_back(npairs);
+    const int nw = (int)wave_first.size() - 1;
+    pfor(nw, [&](int w) {
+        std::vector<size_t> start(NB + 1, 0);
+        auto key = [&](int q, size_t g) { return ((g + 1) * NB - 1) / ngroups[q]; };  // nondecreasing in g
+        for (int q = wave_first[w]; q < wave_first[w + 1]; ++q)
+            for (size_t g = 0; g < ngroups[q]; ++g) ++start[key(q, g) + 1];
+        for (size_t k = 0; k < NB; ++k) start[k + 1] += start[k];
+        int2 *o = out + wave_off[w];
+        for (int q = wave_first[w]; q < wave_first[w + 1]; ++q)
+            for (size_t g = 0; g < ngroups[q]; ++g) o[start[key(q, g)]++] = make_int2(q, (int)g);
+    });
 }
 
 // fn(q) for q in [0, n) on up to 64 host threads (dynamic assignment)

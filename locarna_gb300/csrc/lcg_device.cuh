@@ -39,6 +39,8 @@ enum StatusBits : int {
     ST_INTERNAL = 4,    // traceback found no predecessor
 };
 
+struct GroupItem;
+
 struct PairDev {
     int n, m;
     int go, excl;
@@ -75,6 +77,8 @@ struct PairDev {
                           // (am, D index, a.l | b.l << 16, a.r | b.r << 16)
     int tq_cap;
     int4 *segs;           // traceback segments: (am or -1, token start, token end, 0)
+    const GroupItem *groups;  // the pair's left-end groups (work items) in dependency order
+    const int4 *dw;           // the pair's D writes; GroupItem::dw_start indexes it
 };
 
 // Scoring::basematch(i,j) from the class table or the dense table

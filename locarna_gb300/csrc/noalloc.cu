@@ -109,6 +109,7 @@ extern "C" lcg_status lcg_align_score_static(const lcg_pair_tables *pair, const 
     const size_t o_pair = take(sizeof(PairDev));
     const size_t o_items = take(sizeof(GroupItem) * p.groups.size());
     const size_t o_dw = take(sizeof(int4) * std::max<size_t>(p.dw.size(), 1));
+    const size_t o_queue = take(sizeof(int2) * p.groups.size());
     const size_t o_ctrl = take(64);
     const size_t o_res = take(4ull * R_NWORDS);
     const size_t o_sigma = p.use_cls ? 0 : take(4ull * (n + 1) * (m + 1));
@@ -194,6 +195,10 @@ extern "C" lcg_status lcg_align_score_static(const lcg_pair_tables *pair, const 
     d.topM = (int *)(base + o_top);
     d.res = (int *)(base + o_res);
     for (auto &g : p.groups) g.pair = 0;
+    d.groups = (const GroupItem *)(base + o_items);
+    d.dw = (const int4 *)(base + o_dw);
+    std::vector<int2> queue(p.groups.size());  // one pair: the groups in their own order
+    for (size_t g = 0; g < queue.size(); ++g) queue[g] = make_int2(0, (int)g);
 
     // inputs (pageable host memory; no staging buffer), cleared control words
     auto h2d = [&](size_t o, const void *src, size_t bytes) {
@@ -202,6 +207,7 @@ extern "C" lcg_status lcg_align_score_static(const lcg_pair_tables *pair, const 
     STATIC_TRY(h2d(o_pair, &d, sizeof d));
     STATIC_TRY(h2d(o_items, p.groups.data(), sizeof(GroupItem) * p.groups.size()));
     STATIC_TRY(h2d(o_dw, p.dw.data(), sizeof(int4) * p.dw.size()));
+    STATIC_TRY(h2d(o_queue, queue.data(), sizeof(int2) * queue.size()));
     STATIC_TRY(cudaMemsetAsync(base + o_ctrl, 0, 64, s));
     STATIC_TRY(cudaMemsetAsync(base + o_res, 0, 4ull * R_NWORDS, s));
     if (p.use_cls) {
@@ -233,8 +239,8 @@ extern "C" lcg_status lcg_align_score_static(const lcg_pair_tables *pair, const 
     STATIC_TRY(h2d(o_score, pair->am_score, 4ull * na));
     STATIC_TRY(h2d(o_D, p.Dinit.data(), 4ull * p.num_pos));
 
-    STATIC_TRY(launch_fill((const PairDev *)(base + o_pair), (const GroupItem *)(base + o_items),
-                           (int)p.groups.size(), (const int4 *)(base + o_dw), scratch, stride, sw, rb, fast,
+    STATIC_TRY(launch_fill((const PairDev *)(base + o_pair), (const int2 *)(base + o_queue),
+                           (int)p.groups.size(), scratch, stride, sw, rb, fast,
                            (unsigned int *)(base + o_ctrl), (int *)(base + o_ctrl + 4),
                            (int *)(base + o_ctrl + 8), (int)blocks, s, nullptr));
     int ctrl[4] = {0, 0, 0, 0};

@@ -30,23 +30,19 @@ struct PFPair {
     T *topM;               // (n+1)(m+1)
     double *bmacc;         // per band cell (row offset rowinfo.w): sum of X_bar M(i-1,j-1) bm, FP64
     double *res;           // [0] log Z', [1] gap-extension uses, [2] gap-opening uses
-};
-
-template <typename T>
-struct PFItem {
-    int pair;
-    int al, ar, bl, br;
-    int dw_start, dw_count;  // int4 (am, ar-1, br-1, -), ar ascending
-    int top;
+    const GroupItem *groups;  // left-end groups (work items) in dependency order, top level last
+    const int4 *dw;           // D writes: (D index, ar-1, br-1, -), by group, ar ascending
 };
 
 
+
 template <typename T>
-cudaError_t pf_launch_fwd(const void *pairs, const void *items, int nitems, const int4 *dw, void *scratch,
+// queue: (pair, group) work items in dependency-respecting order
+cudaError_t pf_launch_fwd(const void *pairs, const int2 *queue, int nitems, void *scratch,
                           long long stride, int pitch, int rb, unsigned int *qhead, int *status, int *abort_flag,
                           int blocks, bool count_uses, cudaStream_t st);
 template <typename T>
-cudaError_t pf_launch_back(const void *pairs, const void *items, int nitems, const int4 *dw, void *scratch,
+cudaError_t pf_launch_back(const void *pairs, const int2 *queue, int nitems, void *scratch,
                            long long stride, int pitch, int rb, unsigned int *qhead, int *status, int *abort_flag,
                            int blocks, cudaStream_t st);
 // rb: ring size of the shared-memory rows (a power of two above the span of

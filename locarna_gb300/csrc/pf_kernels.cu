@@ -287,8 +287,8 @@ __device__ void pf_group_sweep(const PFPair<T> &P, int al, int ar, int bl, int b
 
 template <typename T, bool COUNTU>
 __global__ void __launch_bounds__(PF_WARPS * 32)
-    pf_fwd_kernel(const PFPair<T> *__restrict__ pairs, const PFItem<T> *__restrict__ items, int nitems,
-                  const int4 *__restrict__ dw, T *scratch, long long stride, int pitch, int rb,
+    pf_fwd_kernel(const PFPair<T> *__restrict__ pairs, const int2 *__restrict__ queue, int nitems,
+                  T *scratch, long long stride, int pitch, int rb,
                   unsigned int *qhead, int *status, int *abort_ptr) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     PFRows<T> R = pf_rows<T>(warp, rb);
@@ -299,8 +299,9 @@ __global__ void __launch_bounds__(PF_WARPS * 32)
         if (lane == 0) idx = (int)atomicAdd(qhead, 1u);
         idx = __shfl_sync(0xffffffffu, idx, 0);
         if (idx >= nitems || *abort_flag) break;
-        const PFItem<T> it = items[idx];
-        const PFPair<T> &P = pairs[it.pair];
+        const int2 qi = queue[idx];  // (pair, group)
+        const PFPair<T> &P = pairs[qi.x];
+        const GroupItem it = P.groups[qi.y];
         if (it.top) {
             pf_group_sweep<T, true, false, COUNTU, false>(P, 0, P.n + 1, 0, P.m + 1, P.topM, nullptr, nullptr,
                                                           P.m + 1, R, nullptr, 0, status, abort_flag);
@@ -311,7 +312,7 @@ __global__ void __launch_bounds__(PF_WARPS * 32)
             }
         } else {
             pf_group_sweep<T, true, true, COUNTU, false>(P, it.al, it.ar, it.bl, it.br, Mg, nullptr, nullptr,
-                                                         pitch, R, dw + it.dw_start, it.dw_count, status,
+                                                         pitch, R, P.dw + it.dw_start, it.dw_count, status,
                                                          abort_flag);
         }
         __syncwarp();
@@ -505,8 +506,8 @@ __device__ void pf_group_back(const PFPair<T> &P, int al, int ar, int bl, int br
 
 template <typename T>
 __global__ void __launch_bounds__(PF_WARPS * 32)
-    pf_back_kernel(const PFPair<T> *__restrict__ pairs, const PFItem<T> *__restrict__ items, int nitems,
-                   const int4 *__restrict__ dw, T *scratch, long long stride, int pitch, int rb,
+    pf_back_kernel(const PFPair<T> *__restrict__ pairs, const int2 *__restrict__ queue, int nitems,
+                   T *scratch, long long stride, int pitch, int rb,
                    unsigned int *qhead, int *status, int *abort_ptr) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     PFRows<T> R = pf_rows<T>(warp, rb);
@@ -519,15 +520,16 @@ __global__ void __launch_bounds__(PF_WARPS * 32)
         idx = __shfl_sync(0xffffffffu, idx, 0);
         if (idx >= nitems || *abort_flag) break;
         // items in reverse: the consumers of a group's D entries come first
-        const PFItem<T> it = items[nitems - 1 - idx];
-        const PFPair<T> &P = pairs[it.pair];
+        const int2 qi = queue[nitems - 1 - idx];
+        const PFPair<T> &P = pairs[qi.x];
+        const GroupItem it = P.groups[qi.y];
         const int al = it.top ? 0 : it.al, ar = it.top ? P.n + 1 : it.ar;
         const int bl = it.top ? 0 : it.bl, br = it.top ? P.m + 1 : it.br;
         pf_group_sweep<T, false, false, false, true>(P, al, ar, bl, br, Mg, Eg, Fg, pitch, R, nullptr, 0, status,
                                                      abort_flag);
         __syncwarp();
         pf_group_back<T>(P, al, ar, bl, br, it.top != 0, Mg, Eg, Fg, Mb, pitch, R,
-                         it.top ? nullptr : dw + it.dw_start, it.top ? 0 : it.dw_count, status, abort_flag,
+                         it.top ? nullptr : P.dw + it.dw_start, it.top ? 0 : it.dw_count, status, abort_flag,
                          P.res + 1, P.res + 2);
         __syncwarp();
     }
@@ -541,7 +543,7 @@ static size_t pf_smem(int rb) {
 }
 
 template <typename T>
-cudaError_t pf_launch_fwd(const void *pairs, const void *items, int nitems, const int4 *dw, void *scratch,
+cudaError_t pf_launch_fwd(const void *pairs, const int2 *queue, int nitems, void *scratch,
                           long long stride, int pitch, int rb, unsigned int *qhead, int *status, int *abort_flag,
                           int blocks, bool count_uses, cudaStream_t st) {
     const size_t smem = pf_smem<T>(rb);
@@ -550,13 +552,13 @@ cudaError_t pf_launch_fwd(const void *pairs, const void *items, int nitems, cons
         e = cudaFuncSetAttribute(pf_fwd_kernel<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         pf_fwd_kernel<T, true><<<blocks, PF_WARPS * 32, smem, st>>>(
-            (const PFPair<T> *)pairs, (const PFItem<T> *)items, nitems, dw, (T *)scratch, stride, pitch, rb, qhead,
+            (const PFPair<T> *)pairs, queue, nitems, (T *)scratch, stride, pitch, rb, qhead,
             status, abort_flag);
     } else {
         e = cudaFuncSetAttribute(pf_fwd_kernel<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         pf_fwd_kernel<T, false><<<blocks, PF_WARPS * 32, smem, st>>>(
-            (const PFPair<T> *)pairs, (const PFItem<T> *)items, nitems, dw, (T *)scratch, stride, pitch, rb, qhead,
+            (const PFPair<T> *)pairs, queue, nitems, (T *)scratch, stride, pitch, rb, qhead,
             status, abort_flag);
     }
     return cudaGetLastError();
@@ -571,14 +573,14 @@ cudaError_t pf_fwd_occupancy(int rb, int *blocks_per_sm) {
 }
 
 template <typename T>
-cudaError_t pf_launch_back(const void *pairs, const void *items, int nitems, const int4 *dw, void *scratch,
+cudaError_t pf_launch_back(const void *pairs, const int2 *queue, int nitems, void *scratch,
                            long long stride, int pitch, int rb, unsigned int *qhead, int *status, int *abort_flag,
                            int blocks, cudaStream_t st) {
     const size_t smem = pf_smem<T>(rb);
     cudaError_t e = cudaFuncSetAttribute(pf_back_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    pf_back_kernel<T><<<blocks, PF_WARPS * 32, smem, st>>>((const PFPair<T> *)pairs, (const PFItem<T> *)items,
-                                                             nitems, dw, (T *)scratch, stride, pitch, rb, qhead,
+    pf_back_kernel<T><<<blocks, PF_WARPS * 32, smem, st>>>((const PFPair<T> *)pairs, queue,
+                                                             nitems, (T *)scratch, stride, pitch, rb, qhead,
                                                              status, abort_flag);
     return cudaGetLastError();
 }
@@ -593,15 +595,15 @@ cudaError_t pf_back_occupancy(int rb, int *blocks_per_sm) {
 
 int pf_warps_per_block() { return PF_WARPS; }
 
-template cudaError_t pf_launch_fwd<double>(const void *, const void *, int, const int4 *, void *, long long, int,
+template cudaError_t pf_launch_fwd<double>(const void *, const int2 *, int, void *, long long, int,
                                            int, unsigned int *, int *, int *, int, bool, cudaStream_t);
-template cudaError_t pf_launch_fwd<float>(const void *, const void *, int, const int4 *, void *, long long, int,
+template cudaError_t pf_launch_fwd<float>(const void *, const int2 *, int, void *, long long, int,
                                           int, unsigned int *, int *, int *, int, bool, cudaStream_t);
 template cudaError_t pf_fwd_occupancy<double>(int, int *);
 template cudaError_t pf_fwd_occupancy<float>(int, int *);
-template cudaError_t pf_launch_back<double>(const void *, const void *, int, const int4 *, void *, long long, int,
+template cudaError_t pf_launch_back<double>(const void *, const int2 *, int, void *, long long, int,
                                             int, unsigned int *, int *, int *, int, cudaStream_t);
-template cudaError_t pf_launch_back<float>(const void *, const void *, int, const int4 *, void *, long long, int,
+template cudaError_t pf_launch_back<float>(const void *, const int2 *, int, void *, long long, int,
                                            int, unsigned int *, int *, int *, int, cudaStream_t);
 template cudaError_t pf_back_occupancy<double>(int, int *);
 template cudaError_t pf_back_occupancy<float>(int, int *);

@@ -179,32 +179,52 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
                 sgv[k] = j <= hi ? srow[j] : 0;
             }
         }
-        // ---- arc-match terms of row i into Arow[lo-bl .. hi-bl]
+        // ---- arc-match terms of row i into Arow[lo .. hi]: two batches of 32
+        // entries per step, their loads issued together
         bool rowarcs = false;
-        for (int e0 = acur.x; e0 < acur.y; e0 += 32) {
-            const int e = e0 + lane;
-            const int2 en = e < acur.y ? crow[e] : make_int2(0xffff, 0);
-            const int ca = en.x & 0xffff, cbl = en.x >> 16;  // inner corner (a.l-1, b.l-1)
-            const bool okA = ca >= al && ca != 0xffff;        // a.l > al
-            const unsigned ballA = __ballot_sync(0xffffffffu, okA);
-            if (ballA == 0u) break;
+        for (int e0 = acur.x; e0 < acur.y; e0 += 64) {
+            int2 en[2];
+            bool okA[2];
+            unsigned ball[2];
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                const int e = e0 + 32 * u + lane;
+                en[u] = e < acur.y ? crow[e] : make_int2(0xffff, 0);
+            }
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                const int ca = en[u].x & 0xffff;  // a.l - 1 (0xffff: no entry)
+                okA[u] = ca >= al && ca != 0xffff;  // a.l > al
+                ball[u] = __ballot_sync(0xffffffffu, okA[u]);
+            }
+            if (ball[0] == 0u) break;
             if (!rowarcs) {
                 for (int j = lo + lane; j <= hi; j += 32) Arow[RG(j)] = NEG;
                 __syncwarp();
                 rowarcs = true;
             }
-            const bool ok = okA && cbl >= bl && en.y >= lo && en.y <= hi;
-            if (COUNT) {
-                n_visits += okA;
-                n_terms += ok;
+            bool ok[2];
+            int dv[2], mv[2];
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                const int ca = en[u].x & 0xffff, cbl = en[u].x >> 16;  // inner corner (a.l-1, b.l-1)
+                ok[u] = okA[u] && cbl >= bl && en[u].y >= lo && en[u].y <= hi;
+                if (COUNT) {
+                    n_visits += okA[u];
+                    n_terms += ok[u];
+                }
+                const int e = e0 + 32 * u + lane;
+                dv[u] = ok[u] ? (WAIT ? ld_volatile(Dp + e) : Dp[e]) : 0;
+                mv[u] = ok[u] ? Mg[(ca - al) * pitch + (cbl - bl)] : 0;
             }
-            if (ok) {
-                int dv = WAIT ? ld_volatile(Dp + e) : Dp[e];
-                const int mv = Mg[(ca - al) * pitch + (cbl - bl)];
-                if (WAIT && dv == NOT_READY) dv = wait_D(Dp, e, status, abort_flag);
-                atomicMax(&Arow[RG(en.y)], mv + dv);
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                if (ok[u]) {
+                    if (WAIT && dv[u] == NOT_READY) dv[u] = wait_D(Dp, e0 + 32 * u + lane, status, abort_flag);
+                    atomicMax(&Arow[RG(en[u].y)], mv[u] + dv[u]);
+                }
             }
-            if (ballA != 0xffffffffu) break;
+            if (ball[0] != 0xffffffffu || ball[1] != 0xffffffffu) break;
         }
         __syncwarp();
         int B;  // M(i, lo-1)

@@ -37,8 +37,8 @@ namespace lcg {
 
 template <bool COUNT, bool FAST>
 __global__ void __launch_bounds__(FILL_WARPS * 32, FILL_MIN_BLOCKS)
-    sankoff_fill_kernel(const PairDev *__restrict__ pairs, const GroupItem *__restrict__ items,
-                        int nitems, const int4 *__restrict__ dw, int *scratch,
+    sankoff_fill_kernel(const PairDev *__restrict__ pairs, const int2 *__restrict__ queue,
+                        int nitems, int *scratch,
                         long long scratch_stride, int sw, int rb, unsigned int *qhead, int *status,
                         int *abort_flag_ptr, unsigned long long *counters) {
     const int warp = threadIdx.x >> 5;
@@ -51,8 +51,10 @@ __global__ void __launch_bounds__(FILL_WARPS * 32, FILL_MIN_BLOCKS)
         if (lane == 0) idx = (int)atomicAdd(qhead, 1u);
         idx = __shfl_sync(0xffffffffu, idx, 0);
         if (idx >= nitems || *abort_flag) break;
-        const GroupItem it = items[idx];
-        const PairDev &P = pairs[it.pair];
+        const int2 qi = queue[idx];  // (pair, group)
+        const PairDev &P = pairs[qi.x];
+        const GroupItem it = P.groups[qi.y];
+        const int4 *__restrict__ dw = P.dw;
         if (it.top) {
             run_top<COUNT, FAST>(P, it.cpl, sbase, rb, status, abort_flag, counters);
         } else {
@@ -121,23 +123,23 @@ static const void *fill_fn() {
     return (const void *)sankoff_fill_kernel<COUNT, FAST>;
 }
 
-cudaError_t launch_fill(const PairDev *pairs, const GroupItem *items, int nitems, const int4 *dw,
+cudaError_t launch_fill(const PairDev *pairs, const int2 *queue, int nitems,
                         int *scratch, long long scratch_stride, int sw, int rb, bool fast, unsigned int *qhead,
                         int *status, int *abort_flag, int blocks, cudaStream_t st,
                         unsigned long long *counters) {
     size_t smem = (size_t)FILL_WARPS * smem_warp_ints(rb) * sizeof(int);
     if (counters && fast)
         sankoff_fill_kernel<true, true><<<blocks, FILL_WARPS * 32, smem, st>>>(
-            pairs, items, nitems, dw, scratch, scratch_stride, sw, rb, qhead, status, abort_flag, counters);
+            pairs, queue, nitems, scratch, scratch_stride, sw, rb, qhead, status, abort_flag, counters);
     else if (counters)
         sankoff_fill_kernel<true, false><<<blocks, FILL_WARPS * 32, smem, st>>>(
-            pairs, items, nitems, dw, scratch, scratch_stride, sw, rb, qhead, status, abort_flag, counters);
+            pairs, queue, nitems, scratch, scratch_stride, sw, rb, qhead, status, abort_flag, counters);
     else if (fast)
         sankoff_fill_kernel<false, true><<<blocks, FILL_WARPS * 32, smem, st>>>(
-            pairs, items, nitems, dw, scratch, scratch_stride, sw, rb, qhead, status, abort_flag, counters);
+            pairs, queue, nitems, scratch, scratch_stride, sw, rb, qhead, status, abort_flag, counters);
     else
         sankoff_fill_kernel<false, false><<<blocks, FILL_WARPS * 32, smem, st>>>(
-            pairs, items, nitems, dw, scratch, scratch_stride, sw, rb, qhead, status, abort_flag, counters);
+            pairs, queue, nitems, scratch, scratch_stride, sw, rb, qhead, status, abort_flag, counters);
     return cudaGetLastError();
 }
 

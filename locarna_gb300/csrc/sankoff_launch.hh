@@ -9,7 +9,8 @@
 
 namespace lcg {
 // fast: every pair has a sigma class table and no anchor constraints
-cudaError_t launch_fill(const PairDev *pairs, const GroupItem *items, int nitems, const int4 *dw, int *scratch,
+// queue: (pair, group) work items in dependency-respecting order
+cudaError_t launch_fill(const PairDev *pairs, const int2 *queue, int nitems, int *scratch,
                         long long scratch_stride, int sw, int rb, bool fast, unsigned int *qhead, int *status,
                         int *abort_flag, int blocks, cudaStream_t st, unsigned long long *counters);
 cudaError_t launch_trace(const PairDev *pairs, int npairs, int *scratch, long long scratch_stride, int sw, int rb,
@@ -20,7 +21,7 @@ int fill_warps_per_block();
 int trace_warps_per_block();
 cudaError_t sl_prepare(int sw, int rb, int *blocks_per_sm);
 int sl_fill_warps_per_block();
-cudaError_t launch_sl_fill(const PairDev *pairs, const GroupItem *items, int nitems, const int4 *dw, int *scratch,
+cudaError_t launch_sl_fill(const PairDev *pairs, const int2 *queue, int nitems, int *scratch,
                            long long scratch_stride, int sw, int rb, unsigned int *qhead, int *status,
                            int *abort_flag, int blocks, cudaStream_t st);
 cudaError_t launch_sl_trace(const PairDev *pairs, int npairs, int *scratch, long long scratch_stride, int sw,

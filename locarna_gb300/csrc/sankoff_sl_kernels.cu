@@ -301,8 +301,8 @@ __device__ void run_group_sl(const PairDev &P, int al, int ar, int bl, int br, i
 }
 
 __global__ void __launch_bounds__(SL_FILL_WARPS * 32)
-    sankoff_sl_fill_kernel(const PairDev *__restrict__ pairs, const GroupItem *__restrict__ items,
-                           int nitems, const int4 *__restrict__ dw, int *scratch,
+    sankoff_sl_fill_kernel(const PairDev *__restrict__ pairs, const int2 *__restrict__ queue,
+                           int nitems, int *scratch,
                            long long scratch_stride, int sw, int rb, unsigned int *qhead, int *status,
                            int *abort_flag_ptr) {
     extern __shared__ int smem[];
@@ -317,8 +317,10 @@ __global__ void __launch_bounds__(SL_FILL_WARPS * 32)
         if (lane == 0) idx = (int)atomicAdd(qhead, 1u);
         idx = __shfl_sync(0xffffffffu, idx, 0);
         if (idx >= nitems || *abort_flag) break;
-        const GroupItem it = items[idx];
-        const PairDev &P = pairs[it.pair];
+        const int2 qi = queue[idx];  // (pair, group)
+        const PairDev &P = pairs[qi.x];
+        const GroupItem it = P.groups[qi.y];
+        const int4 *__restrict__ dw = P.dw;
         if (it.top) {
             const int base = (int)(sm - smem);
             run_top<false>(P, it.cpl, base, rb, status, abort_flag, nullptr);
@@ -543,12 +545,12 @@ cudaError_t sl_prepare(int sw, int rb, int *blocks_per_sm) {
 
 int sl_fill_warps_per_block() { return SL_FILL_WARPS; }
 
-cudaError_t launch_sl_fill(const PairDev *pairs, const GroupItem *items, int nitems, const int4 *dw,
+cudaError_t launch_sl_fill(const PairDev *pairs, const int2 *queue, int nitems,
                            int *scratch, long long scratch_stride, int sw, int rb, unsigned int *qhead,
                            int *status, int *abort_flag, int blocks, cudaStream_t st) {
     size_t smem = (size_t)SL_FILL_WARPS * sl_warp_ints(sw, rb) * sizeof(int);
     sankoff_sl_fill_kernel<<<blocks, SL_FILL_WARPS * 32, smem, st>>>(
-        pairs, items, nitems, dw, scratch, scratch_stride, sw, rb, qhead, status, abort_flag);
+        pairs, queue, nitems, scratch, scratch_stride, sw, rb, qhead, status, abort_flag);
     return cudaGetLastError();
 }
 
