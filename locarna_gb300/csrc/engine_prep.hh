@@ -57,11 +57,11 @@ void set_error(const std::string &msg);
 inline int ring_size(int span) { return (std::max(span, 32) + 31) / 32 * 32; }
 
 // Bytes of per-pair tables one wave of pairs in the work queue may keep hot
-// (default 16 MB of the 126 MB L2); LCG_WAVE_MB overrides it for tuning runs
+// (default 8 MB of the 126 MB L2); LCG_WAVE_MB overrides it for tuning runs
 // (0 = one wave).
 inline double wave_budget_bytes() {
     const char *v = std::getenv("LCG_WAVE_MB");
-    const double mb = v ? std::atof(v) : 16.0;
+    const double mb = v ? std::atof(v) : 8.0;
     return (mb > 0 ? mb : 1e9) * 1048576.0;
 }
 

@@ -34,6 +34,12 @@
 namespace lcg {
 
 constexpr int PF_WARPS = 4;
+// resident blocks per SM the register budget targets: 8 (32 warps) in FP32;
+// FP64 rows take twice the shared memory, 5 blocks fit
+template <typename T>
+__host__ __device__ constexpr int pf_min_blocks() {
+    return sizeof(T) == 4 ? 8 : 5;
+}
 constexpr long long PF_SPIN_LIMIT = 1ll << 22;
 
 __device__ __forceinline__ bool pf_not_ready(double v) {
@@ -161,28 +167,50 @@ __device__ void pf_group_sweep(const PFPair<T> &P, int al, int ar, int bl, int b
         const int minc = ri.x;
         const int lo = max(bl + 1, minc), hi = min(br - 1, ri.y);
         const T gAi = P.gA[i];
-        // ---- arc-match terms of row i into Ar[lo..hi]
+        // ---- arc-match terms of row i into Ar[lo..hi]: two batches of 32
+        // entries per step, their loads issued together
         bool rowarcs = false;
-        for (int e0 = ra.x; e0 < ra.y; e0 += 32) {
-            const int e = e0 + lane;
-            const int2 en = e < ra.y ? P.crow[e] : make_int2(0xffff, 0);
-            const int ca = en.x & 0xffff, cbl = en.x >> 16;  // inner corner (a.l-1, b.l-1)
-            const bool okA = ca >= al && ca != 0xffff;        // a.l > al
-            const unsigned ballA = __ballot_sync(0xffffffffu, okA);
-            if (ballA == 0u) break;
+        for (int e0 = ra.x; e0 < ra.y; e0 += 64) {
+            int2 en[2];
+            bool okA[2];
+            unsigned ball[2];
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                const int e = e0 + 32 * u + lane;
+                en[u] = e < ra.y ? P.crow[e] : make_int2(0xffff, 0);
+            }
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                const int ca = en[u].x & 0xffff;
+                okA[u] = ca >= al && ca != 0xffff;  // a.l > al
+                ball[u] = __ballot_sync(0xffffffffu, okA[u]);
+            }
+            if (ball[0] == 0u) break;
             if (!rowarcs) {
                 for (int j = lo + lane; j <= hi; j += 32) R.Ar[RG(j)] = T(0);
                 __syncwarp();
                 rowarcs = true;
             }
-            if (okA && cbl >= bl && en.y >= lo && en.y <= hi) {
-                T dv = pf_ld(P.D + e);
-                if (WAIT && pf_not_ready(dv)) dv = pf_wait(P.D + e, status, abort_flag);
-                const T mv = Mg[(size_t)(ca - al) * pitch + (cbl - bl)];
-                atomicAdd(&R.Ar[RG(en.y)], mv * dv * arcf);
-                if (COUNTU) atomicAdd(P.cnt + e, 1);
+            bool ok[2];
+            T dv[2], mv[2];
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                const int ca = en[u].x & 0xffff, cbl = en[u].x >> 16;  // inner corner (a.l-1, b.l-1)
+                ok[u] = okA[u] && cbl >= bl && en[u].y >= lo && en[u].y <= hi;
+                const int e = e0 + 32 * u + lane;
+                dv[u] = ok[u] ? pf_ld(P.D + e) : T(0);
+                mv[u] = ok[u] ? Mg[(size_t)(ca - al) * pitch + (cbl - bl)] : T(0);
             }
-            if (ballA != 0xffffffffu) break;
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                if (ok[u]) {
+                    const int e = e0 + 32 * u + lane;
+                    if (WAIT && pf_not_ready(dv[u])) dv[u] = pf_wait(P.D + e, status, abort_flag);
+                    atomicAdd(&R.Ar[RG(en[u].y)], mv[u] * dv[u] * arcf);
+                    if (COUNTU) atomicAdd(P.cnt + e, 1);
+                }
+            }
+            if (ball[0] != 0xffffffffu || ball[1] != 0xffffffffu) break;
         }
         __syncwarp();
         T B = T(0);
@@ -286,7 +314,7 @@ __device__ void pf_group_sweep(const PFPair<T> &P, int al, int ar, int bl, int b
 }
 
 template <typename T, bool COUNTU>
-__global__ void __launch_bounds__(PF_WARPS * 32)
+__global__ void __launch_bounds__(PF_WARPS * 32, pf_min_blocks<T>())
     pf_fwd_kernel(const PFPair<T> *__restrict__ pairs, const int2 *__restrict__ queue, int nitems,
                   T *scratch, long long stride, int pitch, int rb,
                   unsigned int *qhead, int *status, int *abort_ptr) {
@@ -452,22 +480,44 @@ __device__ void pf_group_back(const PFPair<T> &P, int al, int ar, int bl, int br
         }
         __syncwarp();
         // arc terms of row i: M_bar(corner) += X_bar D s', D_bar(am) += X_bar M(corner) s'
-        for (int e0 = ra.x; e0 < ra.y; e0 += 32) {
-            const int e = e0 + lane;
-            const int2 en = e < ra.y ? P.crow[e] : make_int2(0xffff, 0);
-            const int ca = en.x & 0xffff, cbl = en.x >> 16;
-            const bool okA = ca >= al && ca != 0xffff;
-            const unsigned ballA = __ballot_sync(0xffffffffu, okA);
-            if (ballA == 0u) break;
-            if (okA && cbl >= bl && en.y >= lo && en.y <= hi) {
-                const T xb = Xb[RG(en.y)];
-                const size_t co = (size_t)(ca - al) * pitch + (cbl - bl);
-                atomicAdd(Mb + co, xb * P.D[e] * arcf);
-                atomicAdd(P.Dbar + e, (double)(xb * Mg[co] * arcf));
-                __threadfence();
-                atomicSub(P.cnt + e, 1);
+        // (two batches of 32 entries per step, loads issued together)
+        for (int e0 = ra.x; e0 < ra.y; e0 += 64) {
+            int2 en[2];
+            bool okA[2];
+            unsigned ball[2];
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                const int e = e0 + 32 * u + lane;
+                en[u] = e < ra.y ? P.crow[e] : make_int2(0xffff, 0);
+                const int ca = en[u].x & 0xffff;
+                okA[u] = ca >= al && ca != 0xffff;
+                ball[u] = __ballot_sync(0xffffffffu, okA[u]);
             }
-            if (ballA != 0xffffffffu) break;
+            if (ball[0] == 0u) break;
+            bool ok[2];
+            T dv[2], mv[2], xb[2];
+            size_t co[2];
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                const int ca = en[u].x & 0xffff, cbl = en[u].x >> 16;
+                ok[u] = okA[u] && cbl >= bl && en[u].y >= lo && en[u].y <= hi;
+                const int e = e0 + 32 * u + lane;
+                co[u] = ok[u] ? (size_t)(ca - al) * pitch + (cbl - bl) : 0;
+                xb[u] = ok[u] ? Xb[RG(en[u].y)] : T(0);
+                dv[u] = ok[u] ? P.D[e] : T(0);
+                mv[u] = ok[u] ? Mg[co[u]] : T(0);
+            }
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                if (ok[u]) {
+                    const int e = e0 + 32 * u + lane;
+                    atomicAdd(Mb + co[u], xb[u] * dv[u] * arcf);
+                    atomicAdd(P.Dbar + e, (double)(xb[u] * mv[u] * arcf));
+                    __threadfence();
+                    atomicSub(P.cnt + e, 1);
+                }
+            }
+            if (ball[0] != 0xffffffffu || ball[1] != 0xffffffffu) break;
         }
         // E_bar of row i at columns row i-1 has but row i does not is zero
         if (i - 1 > al) {
@@ -505,7 +555,7 @@ __device__ void pf_group_back(const PFPair<T> &P, int al, int ar, int bl, int br
 }
 
 template <typename T>
-__global__ void __launch_bounds__(PF_WARPS * 32)
+__global__ void __launch_bounds__(PF_WARPS * 32, pf_min_blocks<T>())
     pf_back_kernel(const PFPair<T> *__restrict__ pairs, const int2 *__restrict__ queue, int nitems,
                    T *scratch, long long stride, int pitch, int rb,
                    unsigned int *qhead, int *status, int *abort_ptr) {

@@ -6,6 +6,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <climits>
+
 #include "lcg_device.cuh"
 
 namespace lcg {
@@ -100,6 +102,8 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
 #define RG(j) ((j) - ringn * (int)__umulhi((unsigned)(j), rmagic))
 #define PREV(j) lcg_smem[pv + RG(j)]
 #define CUR(j) lcg_smem[cu + RG(j)]
+#define PREVR(r) lcg_smem[pv + (r)]  // by ring index
+#define CURR(r) lcg_smem[cu + (r)]
     for (int c = lane; c < ringn; c += 32) E[c] = NEG;
     if (SCLS)
         for (int k = lane; k < 256; k += 32) Stab[k] = P.scls[k];
@@ -151,6 +155,7 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
     int colval = globalA ? go : 0;
     bool colblocked = false;
     int dwp = 0;
+    int dw_row = (DWRITE && ndw > 0) ? dw[0].y : INT_MAX;  // D-write lists are by row ascending
     int best = TOP ? 0 : NEG, bi = 0, bj = 0;  // sequence-local argmax (aligner.cc:865-875)
     const int la = P.la, lb = P.lb, ra = P.ra, rb = P.rb;
     int4 rnxt = rowinfo[min(al + 1, P.n + 1)];
@@ -242,10 +247,16 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
         int *Mrow = Mg + (i - al) * pitch - bl;
         int Fc = NEG, Xc = B;
         int k = 0;
+        int rbase = RG(lo);  // ring index of column base, advanced by 32 per chunk
         for (int base = lo; base <= hi; base += 32, ++k) {
             const int j = base + lane;
             const bool act = j <= hi;
-            const int gbc = act ? gBs[RG(j)] : 0;  // gap cost << 4 | sigma column class
+            int rj = rbase + lane;  // ring index of column j
+            if (rj >= ringn) rj -= ringn;
+            const int rjm = rj == 0 ? ringn - 1 : rj - 1;  // of column j-1
+            rbase += 32;
+            if (rbase >= ringn) rbase -= ringn;
+            const int gbc = act ? gBs[rj] : 0;  // gap cost << 4 | sigma column class
             int sgx = 0;
             if (SCLS) {
                 if (act) sgx = Stab[rcl16 + (gbc & 15)];
@@ -259,12 +270,12 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
             if (act) {
                 const bool mok = !ANCH || a_match(P, i, j);
                 const bool dok = !ANCH || a_del(P, i, j);
-                const int d = mok ? PREV(j - 1) + sgx : NEG;
-                int e = dok ? __viaddmax_s32(E[RG(j)], gAi, PREV(j) + gAi + go) : NEG;
+                const int d = mok ? PREVR(rjm) + sgx : NEG;
+                int e = dok ? __viaddmax_s32(E[rj], gAi, PREVR(rj) + gAi + go) : NEG;
                 e = norm(e);
-                E[RG(j)] = e;
+                E[rj] = e;
                 X = max(d, e);
-                if (rowarcs && mok) X = max(X, Arow[RG(j)]);
+                if (rowarcs && mok) X = max(X, Arow[rj]);
             }
             if (TOP && local_top && act && i < la && j < lb) X = max(X, 0);
             // horizontal gaps: max-plus scan of F(j) = max(F(j-1)+a_j, b_j)
@@ -297,7 +308,7 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
             const int F = ANCH ? max(addc(Fc, a), b) : __viaddmax_s32(Fc, a, b);
             const int M = norm(max(X, F));
             if (act) {
-                CUR(j) = M;
+                CURR(rj) = M;
                 Mrow[j] = M;
                 if (TOP && local_top && i >= ra && j >= rb && M > best) {
                     best = M;
@@ -309,7 +320,7 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
             Xc = __shfl_sync(0xffffffffu, X, 31);
         }
         __syncwarp();
-        if (DWRITE) {
+        if (DWRITE && i == dw_row) {
             // fill_D_entries for arc matches whose inner corner is in row i
             while (dwp < ndw) {
                 const int q = dwp + lane;
@@ -321,6 +332,7 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
                 dwp += cnt;
                 if (cnt < 32) break;
             }
+            dw_row = dwp < ndw ? dw[dwp].y : INT_MAX;  // next row with D writes
         }
         if (i + 1 < ar) {
             // columns entering the band with row i+1: M above them is -inf,
@@ -341,6 +353,8 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
     }
 #undef PREV
 #undef CUR
+#undef PREVR
+#undef CURR
 #undef RG
     if (TOP) {
         tout->best = best;
