@@ -148,6 +148,8 @@ lcg_status prep_pair(const lcg_pair_tables &t, const lcg_align_opts &o, Prep &p)
             p.use_cls = true;
             p.flags |= PF_SCLS;
         }
+        p.gbc.assign(m + 1, 0);
+        for (int j = 0; j <= m; ++j) p.gbc[j] = t.gap_b[j] * 16 + (p.use_cls ? p.ccls[j] : 0);
     }
     if (cells > (1ll << 30)) return bad(LCG_ERR_UNSUPPORTED, "band too large");
     p.bandcells = (int)cells;
@@ -533,7 +535,7 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
     struct Off {
         size_t sigma, scls, rcls, ccls, gapA, gapB, minc, maxc, bandoff, rowinfo, anc, cre_start, cre, crow, rowarc,
             am_score, D,
-            topM, res, tok, tq, segs, groups, dw;
+            topM, res, tok, tq, segs, groups, dw, gbc;
     };
     std::vector<Off> off(npairs);
     size_t up = 0;  // upload section (bytes)
@@ -551,6 +553,7 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
         const auto &p = prep[q];
         const auto &t = pairs[q];
         Off &o = off[q];
+        o.gbc = take(up, 4ull * (p.m + 1));
         o.groups = take(up, sizeof(GroupItem) * p.groups.size());
         o.dw = take(up, sizeof(int4) * std::max<size_t>(p.dw.size(), 1));
         // sigma: the class table when it exists, else the dense table
@@ -659,6 +662,7 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
         if (t.num_arcmatches) {
             std::memcpy(H + o.am_score, t.am_score, 4ull * t.num_arcmatches);
         }
+        std::memcpy(H + o.gbc, p.gbc.data(), 4ull * (p.m + 1));
         GroupItem *hg = (GroupItem *)(H + o.groups);
         for (size_t g = 0; g < p.groups.size(); ++g) {
             hg[g] = p.groups[g];
@@ -715,6 +719,7 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
         d.tq = (int4 *)(Dv + o.tq);
         d.tq_cap = p.tq_cap;
         d.segs = (int4 *)(Dv + o.segs);
+        d.gbc = (const int *)(Dv + o.gbc);
         d.groups = (const GroupItem *)(Dv + o.groups);
         d.dw = (const int4 *)(Dv + o.dw);
     });

@@ -37,6 +37,7 @@ struct Prep {
     // scls[rcls[i]*16 + ccls[j]]
     bool use_cls = false;
     std::vector<int> scls, rcls, ccls;
+    std::vector<int> gbc;  // m+1: gapB(j) * 16 + sigma column class (0 without classes)
     std::vector<lcg::GroupItem> groups;          // pair field filled later
     std::vector<int4> dw;                        // dw_start relative to this pair
     int rows_max = 0, width_max = 0;             // over groups

@@ -429,14 +429,31 @@ __device__ void pf_group_back(const PFPair<T> &P, int al, int ar, int bl, int br
             const int j = base + lane;
             const bool act = j <= hi;
             const int c = j - bl;
-            T Mbar = T(0), Nbar = T(0), Ebn = T(0), g = T(0), gn = T(0);
+            // every load of the chunk first (none depends on the scan); left
+            // neighbours and gB(j+1) come from the adjacent lanes
+            T Mbar = T(0), Ebn = T(0), g = T(0), Ev = T(0), Fv = T(0), Mv = T(0), Mup = T(0), Eup = T(0),
+              bmj = T(0);
             if (act) {
                 Mbar = ld_cg(Mb + roff + c);
-                Ebn = Eb[RG(j)];             // E_bar(i+1, j)
-                Nbar = Ebn * gAn * o;        // N(i,j) feeds E(i+1,j)
+                Ebn = Eb[RG(j)];  // E_bar(i+1, j)
                 g = P.gB[j];
-                gn = (j + 1 <= hi) ? P.gB[j + 1] : T(0);
+                Ev = Eg[roff + c];
+                Fv = Fg[roff + c];
+                Mv = Mg[roff + c];
+                Mup = Mg[roff - pitch + c];
+                Eup = Eg[roff - pitch + c];
+                bmj = bmrow[j];
             }
+            T gn = __shfl_down_sync(0xffffffffu, g, 1);  // gB(j+1); 0 past the row's end
+            T Ml = __shfl_up_sync(0xffffffffu, Mv, 1), Fl = __shfl_up_sync(0xffffffffu, Fv, 1);
+            T Md = __shfl_up_sync(0xffffffffu, Mup, 1);
+            if (lane == 31 && act) gn = (j + 1 <= hi) ? P.gB[j + 1] : T(0);
+            if (lane == 0 && act) {
+                Ml = Mg[roff + c - 1];
+                Fl = Fg[roff + c - 1];
+                Md = Mg[roff - pitch + c - 1];
+            }
+            const T Nbar = act ? Ebn * gAn * o : T(0);  // N(i,j) feeds E(i+1,j)
             // F_bar(j) = gB(j+1) F_bar(j+1) + (M_bar + N_bar)(j), right to left
             T a = T(1), b = T(0);
             if (act) {
@@ -462,15 +479,11 @@ __device__ void pf_group_back(const PFPair<T> &P, int al, int ar, int bl, int br
                 Eb[RG(j)] = Ebar;
                 Xb[RG(j)] = Xbar;
                 // gap derivatives: E(i,j) = gA(i) (E(i-1,j) + N(i-1,j) o)
-                const T Ev = Eg[roff + c], Fv = Fg[roff + c];
                 ext += (double)(Ebar * Ev + Fb * Fv);
-                const T Mup = Mg[roff - pitch + c], Eup = Eg[roff - pitch + c];
-                const T Ml = Mg[roff + c - 1], Fl = Fg[roff + c - 1];
                 opn += (double)(Ebar * (Mup - Eup) * gAi * o + Fb * (Ml - Fl) * g * o);
                 // diagonal
-                const T Md = Mg[roff - pitch + c - 1];
-                atomicAdd(Mb + roff - pitch + c - 1, Xbar * bmrow[j]);
-                atomicAdd(P.bmacc + cb + j, (double)(Xbar * Md * bmrow[j]));
+                atomicAdd(Mb + roff - pitch + c - 1, Xbar * bmj);
+                atomicAdd(P.bmacc + cb + j, (double)(Xbar * Md * bmj));
                 // E(i,j) reads N(i-1,j) = M(i-1,j) - E(i-1,j); F(i,j) reads Q(i,j-1)
                 if (i - 1 == al || P.rowinfo[i - 1].x > j || P.rowinfo[i - 1].y < j)
                     atomicAdd(Mb + roff - pitch + c, Ebar * gAi * o);
@@ -510,13 +523,15 @@ __device__ void pf_group_back(const PFPair<T> &P, int al, int ar, int bl, int br
 #pragma unroll
             for (int u = 0; u < 2; ++u) {
                 if (ok[u]) {
-                    const int e = e0 + 32 * u + lane;
                     atomicAdd(Mb + co[u], xb[u] * dv[u] * arcf);
-                    atomicAdd(P.Dbar + e, (double)(xb[u] * mv[u] * arcf));
-                    __threadfence();
-                    atomicSub(P.cnt + e, 1);
+                    atomicAdd(P.Dbar + e0 + 32 * u + lane, (double)(xb[u] * mv[u] * arcf));
                 }
             }
+            // the D_bar updates are visible before their use counters drop
+            if (ok[0] || ok[1]) __threadfence();
+#pragma unroll
+            for (int u = 0; u < 2; ++u)
+                if (ok[u]) atomicSub(P.cnt + e0 + 32 * u + lane, 1);
             if (ball[0] != 0xffffffffu || ball[1] != 0xffffffffu) break;
         }
         // E_bar of row i at columns row i-1 has but row i does not is zero

@@ -117,11 +117,9 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
             int j = base + lane;
             bool act = j < L0;
             bool blk = ANCH && act && !a_ins(P, al, j);
-            const int gbj = act ? P.gapB[j] : 0;
-            if (act) {
-                gBs[RG(j)] = gbj * 16 + (SCLS ? P.ccls[j] : 0);
-            }
-            int s = globalB ? gbj : 0;
+            const int gbcj = act ? P.gbc[j] : 0;  // gapB(j) << 4 | sigma column class
+            if (act) gBs[RG(j)] = gbcj;
+            int s = globalB ? gbcj >> 4 : 0;
             unsigned bm = __ballot_sync(0xffffffffu, blk);
 #pragma unroll
             for (int off = 1; off < 32; off <<= 1) {
@@ -146,7 +144,7 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
             int L1 = min(br, rowinfo[al + 1].y + 1);
             for (int j = L0 + lane; j < L1; j += 32) {
                 PREV(j) = NEG;
-                gBs[RG(j)] = P.gapB[j] * 16 + (SCLS ? P.ccls[j] : 0);
+                gBs[RG(j)] = P.gbc[j];
             }
         }
     }
@@ -341,7 +339,7 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
             for (int j = max(hi + 1, bl + 1) + lane; j < Ln; j += 32) {
                 CUR(j) = NEG;
                 E[RG(j)] = NEG;
-                gBs[RG(j)] = P.gapB[j] * 16 + (SCLS ? P.ccls[j] : 0);
+                gBs[RG(j)] = P.gbc[j];
             }
         }
         __syncwarp();
