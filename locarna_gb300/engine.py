@@ -6,6 +6,7 @@ This is a thin mirror of the C entry points: ``Engine.align_pairs`` is
 """
 import ctypes as C
 import os
+import threading
 
 import numpy as np
 
@@ -16,6 +17,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_build", "liblocarna_gb300.so")
 
 _lib = None
+_lib_lock = threading.Lock()
 
 
 class LcgError(RuntimeError):
@@ -26,6 +28,13 @@ class LcgError(RuntimeError):
 
 def load_library(path=LIB_PATH):
     """Load the engine library; raises if it has not been built."""
+    if _lib is not None:
+        return _lib
+    with _lib_lock:
+        return _load_locked(path)
+
+
+def _load_locked(path):
     global _lib
     if _lib is not None:
         return _lib

@@ -4,6 +4,7 @@ Mirror of the reference locarna driver's input side (src/locarna.cc:398-703):
 the options have the command line's names and defaults.
 """
 import ctypes as C
+import threading
 
 import numpy as np
 
@@ -24,12 +25,20 @@ class lcg_prep_opts(C.Structure):
 
 
 _ready = False
+_ready_lock = threading.Lock()
 
 
 def _lib():
+    # ctypes caches a function object per attribute on first access; two
+    # threads that race on that first access can each cache their own object,
+    # so the signatures are declared once, under a lock.
     global _ready
     lib = load_library()
-    if not _ready:
+    if _ready:
+        return lib
+    with _ready_lock:
+        if _ready:
+            return lib
         lib.lcg_prep_opts_default.argtypes = [C.POINTER(lcg_prep_opts)]
         lib.lcg_prep_opts_default.restype = None
         lib.lcg_prepare_pair.argtypes = [C.c_char_p, C.c_char_p, C.POINTER(lcg_prep_opts), C.POINTER(C.c_void_p)]
