@@ -152,22 +152,33 @@ lcg_status lcg_engine_destroy(lcg_engine eng);
  * LocARNA::Aligner per pair and calling align() (+ trace()) on each
  * (reference: src/locarna.cc:727-785, aligner.cc:924-957,1345-1358).
  * Host tables in, host results out; all device traffic is inside the call.
+ * Large batches run as a pipeline of chunks of pairs on two streams: the host
+ * prepares chunk k+1 while the device aligns chunk k (see
+ * lcg_engine_set_chunk_pairs).
  */
 lcg_status lcg_align_pairs(lcg_engine eng, const lcg_pair_tables *pairs,
                            int32_t npairs, const lcg_align_opts *opts,
                            lcg_align_result *results);
 
-/* Device time (ms) of the last lcg_align_pairs call's kernels, and the number
- * of kernel launches it made. */
+/* Pairs per chunk of lcg_align_pairs' pipeline: 0 (default) chooses by batch
+ * size (one chunk below 256 pairs, else up to 8 chunks); n > 0 caps a chunk
+ * at n pairs (n >= npairs: one chunk, one fill and one traceback launch). */
+lcg_status lcg_engine_set_chunk_pairs(lcg_engine eng, int32_t pairs_per_chunk);
+
+/* Device time (ms) of the last lcg_align_pairs call's kernels (summed over its
+ * chunks, whose kernels may overlap on the two streams), and the number of
+ * kernel launches it made. */
 lcg_status lcg_engine_last_stats(lcg_engine eng, double *kernel_ms,
                                  int64_t *launches);
 
-/* Device time (ms) of the last call's D-fill kernel and traceback kernel. */
+/* Device time (ms) of the last call's D-fill kernels and traceback kernels
+ * (summed over chunks). */
 lcg_status lcg_engine_last_timing(lcg_engine eng, double *fill_ms, double *trace_ms);
 
 /* Wall-clock phases (ms) of the last lcg_align_pairs call: host preparation of
- * the pairs' index structures, packing of the upload, copies + kernels until
- * the results are on the host, and assembly of the alignments. */
+ * the pairs' index structures, packing of the upload, time the host waited for
+ * copies + kernels, and assembly of the alignments (summed over chunks; with
+ * several chunks the device works during the host phases). */
 lcg_status lcg_engine_last_phases(lcg_engine eng, double *prep_ms, double *pack_ms,
                                   double *device_ms, double *results_ms);
 

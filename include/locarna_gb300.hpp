@@ -49,6 +49,8 @@ public:
     Engine(const Engine &) = delete;
     Engine &operator=(const Engine &) = delete;
     lcg_engine get() const { return e_; }
+    // pairs per chunk of the batched call's host/device pipeline (0: automatic)
+    void set_chunk_pairs(int n) { check(lcg_engine_set_chunk_pairs(e_, n)); }
 };
 
 // Tables of one pair built from two PP 2.0 texts (lcg_prepare_pair).

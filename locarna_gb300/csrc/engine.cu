@@ -148,8 +148,20 @@ lcg_status prep_pair(const lcg_pair_tables &t, const lcg_align_opts &o, Prep &p)
             p.use_cls = true;
             p.flags |= PF_SCLS;
         }
+        // per column: the horizontal gap term << 4 | sigma column class. With
+        // anchors the term is gapB(j); without, the prefix sum
+        // PA(j) = sum_{t=1..j} (gapB(t) + max(go, 0)), from which the fill
+        // takes F by a prefix maximum (sankoff_group.cuh)
         p.gbc.assign(m + 1, 0);
-        for (int j = 0; j <= m; ++j) p.gbc[j] = t.gap_b[j] * 16 + (p.use_cls ? p.ccls[j] : 0);
+        const bool prefix = !(p.flags & PF_ANCHORS);
+        const long long gop = std::max(t.indel_opening, 0);
+        long long pa = 0;
+        for (int j = 0; j <= m; ++j) {
+            if (j > 0) pa += t.gap_b[j] + gop;
+            if (prefix && (pa >= (1ll << 26) || pa <= -(1ll << 26)))
+                return bad(LCG_ERR_RANGE, "gap cost prefix sums exceed the device range");
+            p.gbc[j] = (int)(prefix ? pa : t.gap_b[j]) * 16 + (p.use_cls ? p.ccls[j] : 0);
+        }
     }
     if (cells > (1ll << 30)) return bad(LCG_ERR_UNSUPPORTED, "band too large");
     p.bandcells = (int)cells;
@@ -412,132 +424,74 @@ struct Assembler {
 
 size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
-}  // namespace
+// One buffer set of the engine, by reference: set 0 is the engine's own
+// fields, set 1 the second set of the pipeline.
+struct Slot {
+    cudaStream_t st;
+    char **d_arena;
+    size_t *arena_cap;
+    char **h_stage;
+    size_t *stage_cap;
+    int **d_scratch;
+    size_t *scratch_cap;
+    cudaEvent_t ev0, ev1, ev2;
+};
 
-// ------------------------------------------------------------------ engine
-
-extern "C" {
-
-const char *lcg_last_error(void) { return g_last_error.c_str(); }
-
-int32_t lcg_abi_version(void) { return LCG_ABI_VERSION; }
-
-lcg_status lcg_engine_create(int32_t device, void *stream, lcg_engine *out) {
-    if (!out) return fail(LCG_ERR_ARG, "out is NULL");
-    *out = nullptr;
-    int ndev = 0;
-    CUDA_TRY(cudaGetDeviceCount(&ndev));
-    if (device < 0 || device >= ndev) return fail(LCG_ERR_ARG, "no such CUDA device");
-    CUDA_TRY(cudaSetDevice(device));
-    auto *e = new lcg_engine_s();
-    e->device = device;
-    if (stream) {
-        e->stream = (cudaStream_t)stream;
-    } else {
-        if (cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) != cudaSuccess) {
-            delete e;
-            return fail(LCG_ERR_CUDA, "cudaStreamCreate failed");
-        }
-        e->own_stream = true;
-    }
-    cudaDeviceGetAttribute(&e->sms, cudaDevAttrMultiProcessorCount, device);
-    cudaEventCreate(&e->ev0);
-    cudaEventCreate(&e->ev1);
-    cudaEventCreate(&e->ev2);
-    *out = e;
-    return LCG_OK;
+Slot slot_of(lcg_engine e, int k) {
+    if (k == 0)
+        return Slot{e->stream, &e->d_arena, &e->arena_cap, &e->h_stage, &e->stage_cap,
+                    &e->d_scratch, &e->scratch_cap, e->ev0, e->ev1, e->ev2};
+    lcg_buffer_set &b = e->alt;
+    return Slot{b.stream, &b.d_arena, &b.arena_cap, &b.h_stage, &b.stage_cap,
+                &b.d_scratch, &b.scratch_cap, b.ev0, b.ev1, b.ev2};
 }
 
-lcg_status lcg_engine_destroy(lcg_engine e) {
-    if (!e) return LCG_OK;
-    cudaSetDevice(e->device);
-    if (e->stream) cudaStreamSynchronize(e->stream);
-    if (e->d_arena) cudaFree(e->d_arena);
-    if (e->d_scratch) cudaFree(e->d_scratch);
-    if (e->h_stage) cudaFreeHost(e->h_stage);
-    if (e->ev0) cudaEventDestroy(e->ev0);
-    if (e->ev1) cudaEventDestroy(e->ev1);
-    if (e->ev2) cudaEventDestroy(e->ev2);
-    if (e->own_stream) cudaStreamDestroy(e->stream);
-    lcg_host::pf_release(e);
-    delete e;
-    return LCG_OK;
+// byte offsets of one pair's tables in the arena
+struct PairOff {
+    size_t sigma, scls, rcls, ccls, gapA, gapB, minc, maxc, bandoff, rowinfo, anc, cre_start, cre, crow, rowarc,
+        am_score, D, topM, res, tok, tq, segs, groups, dw, gbc;
+};
+
+// One chunk of an lcg_align_pairs call: pairs [q0, q0 + nq) of the batch.
+struct Chunk {
+    int q0 = 0, nq = 0;
+    std::vector<Prep> prep;
+    std::vector<PairOff> off;
+    size_t off_ctrl = 0, down_begin = 0, down_end = 0;
+    long long launches = 0;
+    bool in_flight = false;
+};
+
+// pairs per chunk: one chunk for small batches, else up to 8 chunks of at
+// least 128 pairs (the first chunk's host preparation is not overlapped)
+int chunk_size(int npairs, int setting) {
+    if (setting > 0) return setting;
+    if (npairs < 256) return npairs;
+    const int k = std::min(8, npairs / 128);
+    return (npairs + k - 1) / k;
 }
 
-lcg_status lcg_engine_last_stats(lcg_engine e, double *kernel_ms, int64_t *launches) {
-    if (!e) return fail(LCG_ERR_ARG, "engine is NULL");
-    if (kernel_ms) *kernel_ms = e->last_ms;
-    if (launches) *launches = e->last_launches;
-    return LCG_OK;
+double ms_between(std::chrono::steady_clock::time_point a, std::chrono::steady_clock::time_point b) {
+    return std::chrono::duration<double, std::milli>(b - a).count();
 }
 
-lcg_status lcg_engine_last_transfer(lcg_engine e, int64_t *h2d_bytes, int64_t *d2h_bytes) {
-    if (!e) return fail(LCG_ERR_ARG, "engine is NULL");
-    if (h2d_bytes) *h2d_bytes = e->last_h2d;
-    if (d2h_bytes) *d2h_bytes = e->last_d2h;
-    return LCG_OK;
-}
-
-lcg_status lcg_engine_last_timing(lcg_engine e, double *fill_ms, double *trace_ms) {
-    if (!e) return fail(LCG_ERR_ARG, "engine is NULL");
-    if (fill_ms) *fill_ms = e->last_fill_ms;
-    if (trace_ms) *trace_ms = e->last_trace_ms;
-    return LCG_OK;
-}
-
-lcg_status lcg_engine_set_counting(lcg_engine e, int32_t on) {
-    if (!e) return fail(LCG_ERR_ARG, "engine is NULL");
-    e->counting = on != 0;
-    return LCG_OK;
-}
-
-lcg_status lcg_engine_last_work(lcg_engine e, lcg_work_counts *w) {
-    if (!e || !w) return fail(LCG_ERR_ARG, "NULL argument");
-    w->groups = e->last_groups;
-    w->cells = e->last_cells;
-    w->arc_terms = e->last_visits;
-    w->valid_arc_terms = e->last_terms;
-    return LCG_OK;
-}
-
-lcg_status lcg_measure_int_peak(lcg_engine e, int32_t dpx, double *gops) {
-    if (!e || !gops) return fail(LCG_ERR_ARG, "NULL argument");
-    CUDA_TRY(cudaSetDevice(e->device));
-    CUDA_TRY(measure_int_peak(e->sms, dpx != 0, e->stream, gops));
-    return LCG_OK;
-}
-
-lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t npairs,
-                           const lcg_align_opts *opts, lcg_align_result *results) {
-    if (!e || !pairs || !opts || !results || npairs < 0) return fail(LCG_ERR_ARG, "NULL argument");
-    if (npairs == 0) return LCG_OK;
-    CUDA_TRY(cudaSetDevice(e->device));
-    using clk = std::chrono::steady_clock;
-    const auto t0 = clk::now();
-    auto ms_since = [](clk::time_point a, clk::time_point b) {
-        return std::chrono::duration<double, std::milli>(b - a).count();
-    };
-
-    // ---- host preparation (threads over pairs)
-    std::vector<Prep> prep(npairs);
-    lcg_host::parallel_for(npairs, [&](int q) { prep_pair(pairs[q], *opts, prep[q]); });
-    for (int q = 0; q < npairs; ++q)
-        if (prep[q].code != LCG_OK) return fail(prep[q].code, "pair " + std::to_string(q) + ": " + prep[q].err);
-    const auto t1 = clk::now();
-
-    // ---- arena layout
+// Lay out, pack and enqueue one prepared chunk on its buffer set: one
+// host->device copy, the fill (and traceback) launch, one device->host copy.
+// Returns without waiting.
+lcg_status chunk_launch(lcg_engine e, const Slot &s, const lcg_pair_tables *all, const lcg_align_opts *opts,
+                        Chunk &c, double *pack_ms) {
+    const auto tp0 = std::chrono::steady_clock::now();
+    const lcg_pair_tables *pairs = all + c.q0;
+    const int npairs = c.nq;
+    std::vector<Prep> &prep = c.prep;
     int sw = 0, rows_max = 1, span = 2;
     for (auto &p : prep) {
         sw = std::max(sw, std::max(p.width_max + 1, p.m + 2));
         rows_max = std::max(rows_max, p.rows_max + 1);
         span = std::max(span, p.span);
     }
-    struct Off {
-        size_t sigma, scls, rcls, ccls, gapA, gapB, minc, maxc, bandoff, rowinfo, anc, cre_start, cre, crow, rowarc,
-            am_score, D,
-            topM, res, tok, tq, segs, groups, dw, gbc;
-    };
-    std::vector<Off> off(npairs);
+    c.off.assign(npairs, PairOff{});
+    std::vector<PairOff> &off = c.off;
     size_t up = 0;  // upload section (bytes)
     auto take = [](size_t &cur, size_t bytes) {
         size_t o = cur;
@@ -548,11 +502,12 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
     size_t nitems = 0;
     for (auto &p : prep) nitems += p.groups.size();
     size_t off_queue = take(up, sizeof(int2) * nitems);  // (pair, group) work items
-    size_t off_ctrl = take(up, 64);  // qhead, status, abort, pad, 2 x u64 counters
+    c.off_ctrl = take(up, 64);  // qhead, status, abort, pad, 2 x u64 counters
+    const size_t off_ctrl = c.off_ctrl;
     for (int q = 0; q < npairs; ++q) {
         const auto &p = prep[q];
         const auto &t = pairs[q];
-        Off &o = off[q];
+        PairOff &o = off[q];
         o.gbc = take(up, 4ull * (p.m + 1));
         o.groups = take(up, sizeof(GroupItem) * p.groups.size());
         o.dw = take(up, sizeof(int4) * std::max<size_t>(p.dw.size(), 1));
@@ -575,43 +530,44 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
         o.am_score = take(up, 4ull * std::max(t.num_arcmatches, 1));
         o.D = take(up, 4ull * std::max(p.num_pos, 1));
     }
-    size_t down_begin = up;
+    c.down_begin = up;
     size_t dn = up;
     for (int q = 0; q < npairs; ++q) {
         const auto &p = prep[q];
-        Off &o = off[q];
+        PairOff &o = off[q];
         o.res = take(dn, 4ull * R_NWORDS);
         o.tok = take(dn, 8ull * p.token_cap);
         o.segs = take(dn, 16ull * (p.tq_cap + 1));
     }
-    size_t down_end = dn;
+    c.down_end = dn;
+    const size_t down_begin = c.down_begin, down_end = c.down_end;
     size_t dev_only = dn;
     for (int q = 0; q < npairs; ++q) {
         const auto &p = prep[q];
-        Off &o = off[q];
+        PairOff &o = off[q];
         o.tq = take(dev_only, 16ull * p.tq_cap);
         o.topM = take(dev_only, 4ull * (p.n + 1) * (p.m + 1));
     }
     size_t total = dev_only;
 
-    if (total > e->arena_cap) {
-        if (e->d_arena) cudaFree(e->d_arena);
-        e->d_arena = nullptr;
-        e->arena_cap = 0;
+    if (total > *s.arena_cap) {
+        if (*s.d_arena) cudaFree(*s.d_arena);
+        *s.d_arena = nullptr;
+        *s.arena_cap = 0;
         size_t cap = total + total / 4;
-        if (cudaMalloc(&e->d_arena, cap) != cudaSuccess) return fail(LCG_ERR_NOMEM, "device arena allocation failed");
-        e->arena_cap = cap;
+        if (cudaMalloc(s.d_arena, cap) != cudaSuccess) return fail(LCG_ERR_NOMEM, "device arena allocation failed");
+        *s.arena_cap = cap;
     }
-    if (down_end > e->stage_cap) {
-        if (e->h_stage) cudaFreeHost(e->h_stage);
-        e->h_stage = nullptr;
-        e->stage_cap = 0;
+    if (down_end > *s.stage_cap) {
+        if (*s.h_stage) cudaFreeHost(*s.h_stage);
+        *s.h_stage = nullptr;
+        *s.stage_cap = 0;
         size_t cap = down_end + down_end / 4;
-        if (cudaMallocHost(&e->h_stage, cap) != cudaSuccess) return fail(LCG_ERR_NOMEM, "pinned staging allocation failed");
-        e->stage_cap = cap;
+        if (cudaMallocHost(s.h_stage, cap) != cudaSuccess) return fail(LCG_ERR_NOMEM, "pinned staging allocation failed");
+        *s.stage_cap = cap;
     }
-    char *H = e->h_stage;
-    char *Dv = e->d_arena;
+    char *H = *s.h_stage;
+    char *Dv = *s.d_arena;
 
     // ---- pack the upload
     PairDev *hp = (PairDev *)(H + off_pairs);
@@ -631,7 +587,7 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
     lcg_host::parallel_for(npairs, [&](int q) {
         const auto &p = prep[q];
         const auto &t = pairs[q];
-        const Off &o = off[q];
+        const PairOff &o = off[q];
         if (p.use_cls) {
             std::memcpy(H + o.scls, p.scls.data(), 4ull * 256);
             std::memcpy(H + o.rcls, p.rcls.data(), 4ull * (p.n + 2));
@@ -723,8 +679,8 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
         d.groups = (const GroupItem *)(Dv + o.groups);
         d.dw = (const int4 *)(Dv + o.dw);
     });
+    *pack_ms += ms_between(tp0, std::chrono::steady_clock::now());
 
-    const auto t2 = clk::now();
     // ---- scratch
     const bool sl = opts->struct_local != 0;
     const int rb = lcg_host::ring_size(span);
@@ -744,83 +700,90 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
     size_t fill_slots = (size_t)blocks * (sl ? sl_fill_warps_per_block() * 4 : fill_warps_per_block());
     size_t trace_slots = (size_t)npairs * (sl ? 8 : 1);
     size_t need = std::max(fill_slots, trace_slots) * (size_t)stride;
-    if (need > e->scratch_cap) {
-        if (e->d_scratch) cudaFree(e->d_scratch);
-        e->d_scratch = nullptr;
-        e->scratch_cap = 0;
-        if (cudaMalloc(&e->d_scratch, need * sizeof(int)) != cudaSuccess)
+    if (need > *s.scratch_cap) {
+        if (*s.d_scratch) cudaFree(*s.d_scratch);
+        *s.d_scratch = nullptr;
+        *s.scratch_cap = 0;
+        if (cudaMalloc(s.d_scratch, need * sizeof(int)) != cudaSuccess)
             return fail(LCG_ERR_NOMEM, "device scratch allocation failed");
-        e->scratch_cap = need;
+        *s.scratch_cap = need;
     }
+    int *scratch = *s.d_scratch;
 
     // ---- transfer + launch + transfer
-    cudaStream_t st = e->stream;
+    cudaStream_t st = s.st;
     CUDA_TRY(cudaMemcpyAsync(Dv, H, down_begin, cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaMemsetAsync(Dv + down_begin, 0, down_end - down_begin, st));
     unsigned int *qhead = (unsigned int *)(Dv + off_ctrl);
     int *status = (int *)(Dv + off_ctrl + 4);
     int *abort_flag = (int *)(Dv + off_ctrl + 8);
-    CUDA_TRY(cudaEventRecord(e->ev0, st));
+    CUDA_TRY(cudaEventRecord(s.ev0, st));
     unsigned long long *counters = e->counting ? (unsigned long long *)(Dv + off_ctrl + 16) : nullptr;
     if (sl) {
         if (counters) return fail(LCG_ERR_UNSUPPORTED, "work counting covers the plain mode only");
         CUDA_TRY(launch_sl_fill((const PairDev *)(Dv + off_pairs), (const int2 *)(Dv + off_queue),
-                                (int)nitems, e->d_scratch, stride, sw, rb, qhead,
+                                (int)nitems, scratch, stride, sw, rb, qhead,
                                 status, abort_flag, blocks, st));
     } else {
         CUDA_TRY(launch_fill((const PairDev *)(Dv + off_pairs), (const int2 *)(Dv + off_queue),
-                             (int)nitems, e->d_scratch, stride, sw, rb, fast, qhead,
+                             (int)nitems, scratch, stride, sw, rb, fast, qhead,
                              status, abort_flag, blocks, st, counters));
     }
-    CUDA_TRY(cudaEventRecord(e->ev1, st));
-    long long launches = 1;
+    CUDA_TRY(cudaEventRecord(s.ev1, st));
+    c.launches = 1;
     if (opts->do_trace) {
         if (sl)
-            CUDA_TRY(launch_sl_trace((const PairDev *)(Dv + off_pairs), npairs, e->d_scratch, stride, sw,
+            CUDA_TRY(launch_sl_trace((const PairDev *)(Dv + off_pairs), npairs, scratch, stride, sw,
                                      status, st));
         else
-            CUDA_TRY(launch_trace((const PairDev *)(Dv + off_pairs), npairs, e->d_scratch, stride, sw, rb, status,
+            CUDA_TRY(launch_trace((const PairDev *)(Dv + off_pairs), npairs, scratch, stride, sw, rb, status,
                                   st));
-        ++launches;
+        ++c.launches;
     }
-    CUDA_TRY(cudaEventRecord(e->ev2, st));
+    CUDA_TRY(cudaEventRecord(s.ev2, st));
     CUDA_TRY(cudaMemcpyAsync(H + off_ctrl, Dv + off_ctrl, 64, cudaMemcpyDeviceToHost, st));
     CUDA_TRY(cudaMemcpyAsync(H + down_begin, Dv + down_begin, down_end - down_begin, cudaMemcpyDeviceToHost, st));
-    CUDA_TRY(cudaStreamSynchronize(st));
-    const auto t3 = clk::now();
+    c.in_flight = true;
+    e->last_h2d += (long long)down_begin;
+    e->last_d2h += 64 + (long long)(down_end - down_begin);
+    return LCG_OK;
+}
+
+// Wait for a launched chunk, check its status and assemble its alignments.
+lcg_status chunk_finish(lcg_engine e, const Slot &s, const lcg_align_opts *opts, Chunk &c,
+                        lcg_align_result *all_results, double *wait_ms, double *results_ms) {
+    const auto t0 = std::chrono::steady_clock::now();
+    c.in_flight = false;
+    CUDA_TRY(cudaStreamSynchronize(s.st));
+    const auto t1 = std::chrono::steady_clock::now();
+    *wait_ms += ms_between(t0, t1);
+    const char *H = *s.h_stage;
     float ms = 0, ms1 = 0;
-    cudaEventElapsedTime(&ms, e->ev0, e->ev2);
-    cudaEventElapsedTime(&ms1, e->ev0, e->ev1);
-    e->last_ms = ms;
-    e->last_fill_ms = ms1;
-    e->last_trace_ms = ms - ms1;
-    e->last_launches = launches;
-    e->last_h2d = (long long)down_begin;
-    e->last_d2h = 64 + (long long)(down_end - down_begin);
-    e->last_groups = 0;
-    e->last_cells = 0;
-    for (auto &p : prep) {
+    cudaEventElapsedTime(&ms, s.ev0, s.ev2);
+    cudaEventElapsedTime(&ms1, s.ev0, s.ev1);
+    e->last_ms += ms;
+    e->last_fill_ms += ms1;
+    e->last_trace_ms += ms - ms1;
+    e->last_launches += c.launches;
+    for (auto &p : c.prep) {
         e->last_groups += (long long)p.groups.size() - 1;
         e->last_cells += p.cells;
     }
     if (e->counting) {
-        const unsigned long long *cn = (const unsigned long long *)(H + off_ctrl + 16);
-        e->last_terms = (long long)cn[0];
-        e->last_visits = (long long)cn[1];
-    } else {
-        e->last_terms = e->last_visits = -1;
+        const unsigned long long *cn = (const unsigned long long *)(H + c.off_ctrl + 16);
+        e->last_terms = std::max(e->last_terms, 0ll) + (long long)cn[0];
+        e->last_visits = std::max(e->last_visits, 0ll) + (long long)cn[1];
     }
-    int hstatus = ((int *)(H + off_ctrl))[1];
+    int hstatus = ((const int *)(H + c.off_ctrl))[1];
     if (hstatus & ST_TIMEOUT) return fail(LCG_ERR_TIMEOUT, "a device wait for an arc-match entry timed out");
     if (hstatus & ST_OVERFLOW) return fail(LCG_ERR_DEVICE, "traceback buffer overflow");
     if (hstatus & ST_INTERNAL) return fail(LCG_ERR_DEVICE, "traceback found no predecessor");
 
-    // ---- results
-    for (int q = 0; q < npairs; ++q) {
-        const auto &p = prep[q];
-        const Off &o = off[q];
+    for (int q = 0; q < c.nq; ++q) {
+        const auto &p = c.prep[q];
+        const PairOff &o = c.off[q];
         const int *res = (const int *)(H + o.res);
-        lcg_align_result &r = results[q];
+        lcg_align_result &r = all_results[c.q0 + q];
         int sc = res[R_SCORE];
         r.score = sc < MIN_FINITE ? LCG_NEG_INF : (int64_t)sc;
         r.max_i = res[R_MAXI];
@@ -835,10 +798,10 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
         int nseg = res[R_NSEG];
         const int4 *segs = (const int4 *)(H + o.segs);
         if (nseg < 1 || nseg > p.tq_cap + 1) return fail(LCG_ERR_DEVICE, "bad traceback segment count");
-        for (int s = 0; s < nseg; ++s) {
-            as.seg_am.push_back(segs[s].x);
-            as.seg_start.push_back(segs[s].y);
-            as.seg_end.push_back(segs[s].z);
+        for (int sg = 0; sg < nseg; ++sg) {
+            as.seg_am.push_back(segs[sg].x);
+            as.seg_start.push_back(segs[sg].y);
+            as.seg_end.push_back(segs[sg].z);
         }
         as.edges = r.edges;
         as.edge_cap = r.edges ? p.n + p.m : 0;
@@ -849,11 +812,201 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
         r.num_edges = as.nedges;
         r.num_traced_am = as.ntam;
     }
-    const auto t4 = clk::now();
-    e->last_phase_ms[0] = ms_since(t0, t1);
-    e->last_phase_ms[1] = ms_since(t1, t2);
-    e->last_phase_ms[2] = ms_since(t2, t3);
-    e->last_phase_ms[3] = ms_since(t3, t4);
+    *results_ms += ms_between(t1, std::chrono::steady_clock::now());
+    return LCG_OK;
+}
+
+// the second buffer set: its stream and events
+lcg_status ensure_alt(lcg_engine e) {
+    lcg_buffer_set &b = e->alt;
+    if (b.stream) return LCG_OK;
+    CUDA_TRY(cudaStreamCreateWithFlags(&b.stream, cudaStreamNonBlocking));
+    b.own_stream = true;
+    CUDA_TRY(cudaEventCreate(&b.ev0));
+    CUDA_TRY(cudaEventCreate(&b.ev1));
+    CUDA_TRY(cudaEventCreate(&b.ev2));
+    return LCG_OK;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ engine
+
+extern "C" {
+
+const char *lcg_last_error(void) { return g_last_error.c_str(); }
+
+int32_t lcg_abi_version(void) { return LCG_ABI_VERSION; }
+
+lcg_status lcg_engine_create(int32_t device, void *stream, lcg_engine *out) {
+    if (!out) return fail(LCG_ERR_ARG, "out is NULL");
+    *out = nullptr;
+    int ndev = 0;
+    CUDA_TRY(cudaGetDeviceCount(&ndev));
+    if (device < 0 || device >= ndev) return fail(LCG_ERR_ARG, "no such CUDA device");
+    CUDA_TRY(cudaSetDevice(device));
+    auto *e = new lcg_engine_s();
+    e->device = device;
+    if (stream) {
+        e->stream = (cudaStream_t)stream;
+    } else {
+        if (cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) != cudaSuccess) {
+            delete e;
+            return fail(LCG_ERR_CUDA, "cudaStreamCreate failed");
+        }
+        e->own_stream = true;
+    }
+    cudaDeviceGetAttribute(&e->sms, cudaDevAttrMultiProcessorCount, device);
+    cudaEventCreate(&e->ev0);
+    cudaEventCreate(&e->ev1);
+    cudaEventCreate(&e->ev2);
+    *out = e;
+    return LCG_OK;
+}
+
+lcg_status lcg_engine_destroy(lcg_engine e) {
+    if (!e) return LCG_OK;
+    cudaSetDevice(e->device);
+    if (e->stream) cudaStreamSynchronize(e->stream);
+    if (e->d_arena) cudaFree(e->d_arena);
+    if (e->d_scratch) cudaFree(e->d_scratch);
+    if (e->h_stage) cudaFreeHost(e->h_stage);
+    if (e->ev0) cudaEventDestroy(e->ev0);
+    if (e->ev1) cudaEventDestroy(e->ev1);
+    if (e->ev2) cudaEventDestroy(e->ev2);
+    if (e->own_stream) cudaStreamDestroy(e->stream);
+    lcg_buffer_set &b = e->alt;
+    if (b.stream) cudaStreamSynchronize(b.stream);
+    if (b.d_arena) cudaFree(b.d_arena);
+    if (b.d_scratch) cudaFree(b.d_scratch);
+    if (b.h_stage) cudaFreeHost(b.h_stage);
+    if (b.ev0) cudaEventDestroy(b.ev0);
+    if (b.ev1) cudaEventDestroy(b.ev1);
+    if (b.ev2) cudaEventDestroy(b.ev2);
+    if (b.own_stream) cudaStreamDestroy(b.stream);
+    lcg_host::pf_release(e);
+    delete e;
+    return LCG_OK;
+}
+
+lcg_status lcg_engine_last_stats(lcg_engine e, double *kernel_ms, int64_t *launches) {
+    if (!e) return fail(LCG_ERR_ARG, "engine is NULL");
+    if (kernel_ms) *kernel_ms = e->last_ms;
+    if (launches) *launches = e->last_launches;
+    return LCG_OK;
+}
+
+lcg_status lcg_engine_last_transfer(lcg_engine e, int64_t *h2d_bytes, int64_t *d2h_bytes) {
+    if (!e) return fail(LCG_ERR_ARG, "engine is NULL");
+    if (h2d_bytes) *h2d_bytes = e->last_h2d;
+    if (d2h_bytes) *d2h_bytes = e->last_d2h;
+    return LCG_OK;
+}
+
+lcg_status lcg_engine_last_timing(lcg_engine e, double *fill_ms, double *trace_ms) {
+    if (!e) return fail(LCG_ERR_ARG, "engine is NULL");
+    if (fill_ms) *fill_ms = e->last_fill_ms;
+    if (trace_ms) *trace_ms = e->last_trace_ms;
+    return LCG_OK;
+}
+
+lcg_status lcg_engine_set_counting(lcg_engine e, int32_t on) {
+    if (!e) return fail(LCG_ERR_ARG, "engine is NULL");
+    e->counting = on != 0;
+    return LCG_OK;
+}
+
+lcg_status lcg_engine_last_work(lcg_engine e, lcg_work_counts *w) {
+    if (!e || !w) return fail(LCG_ERR_ARG, "NULL argument");
+    w->groups = e->last_groups;
+    w->cells = e->last_cells;
+    w->arc_terms = e->last_visits;
+    w->valid_arc_terms = e->last_terms;
+    return LCG_OK;
+}
+
+lcg_status lcg_measure_int_peak(lcg_engine e, int32_t dpx, double *gops) {
+    if (!e || !gops) return fail(LCG_ERR_ARG, "NULL argument");
+    CUDA_TRY(cudaSetDevice(e->device));
+    CUDA_TRY(measure_int_peak(e->sms, dpx != 0, e->stream, gops));
+    return LCG_OK;
+}
+
+lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t npairs,
+                           const lcg_align_opts *opts, lcg_align_result *results) {
+    if (!e || !pairs || !opts || !results || npairs < 0) return fail(LCG_ERR_ARG, "NULL argument");
+    if (npairs == 0) return LCG_OK;
+    CUDA_TRY(cudaSetDevice(e->device));
+    using clk = std::chrono::steady_clock;
+    const int per = std::max(1, std::min<int>(npairs, chunk_size(npairs, e->chunk_pairs)));
+    const int nchunks = (npairs + per - 1) / per;
+    if (nchunks > 1) {
+        lcg_status st = ensure_alt(e);
+        if (st != LCG_OK) return st;
+    }
+    e->last_ms = e->last_fill_ms = e->last_trace_ms = 0;
+    e->last_launches = 0;
+    e->last_h2d = e->last_d2h = 0;
+    e->last_groups = e->last_cells = 0;
+    e->last_terms = e->last_visits = -1;
+    double t_prep = 0, t_pack = 0, t_wait = 0, t_res = 0;
+
+    // Pipeline over chunks of pairs on two buffer sets: the host prepares
+    // chunk k while the device runs chunks k-1 (other set) and k-2 (this
+    // set, finished just before its buffers are reused).
+    Chunk ch[2];
+    std::vector<Prep> next;
+    lcg_status rc = LCG_OK;
+    for (int k = 0; k < nchunks && rc == LCG_OK; ++k) {
+        const int q0 = k * per, nq = std::min(per, npairs - q0);
+        const auto a = clk::now();
+        next.clear();
+        next.resize(nq);
+        lcg_host::parallel_for(nq, [&](int q) { prep_pair(pairs[q0 + q], *opts, next[q]); });
+        t_prep += ms_between(a, clk::now());
+        for (int q = 0; q < nq && rc == LCG_OK; ++q)
+            if (next[q].code != LCG_OK)
+                rc = fail(next[q].code, "pair " + std::to_string(q0 + q) + ": " + next[q].err);
+        if (rc != LCG_OK) break;
+        Chunk &c = ch[k & 1];
+        const Slot s = slot_of(e, k & 1);
+        if (c.in_flight) {
+            rc = chunk_finish(e, s, opts, c, results, &t_wait, &t_res);
+            if (rc != LCG_OK) break;
+        }
+        c.prep.swap(next);
+        c.q0 = q0;
+        c.nq = nq;
+        rc = chunk_launch(e, s, pairs, opts, c, &t_pack);
+    }
+    // the chunks still in flight, in batch order; after an error only wait
+    // for them (nothing of the call stays in flight)
+    const int first = ch[0].q0 <= ch[1].q0 ? 0 : 1;
+    for (int u = 0; u < 2; ++u) {
+        const int k = u == 0 ? first : 1 - first;
+        const Slot s = slot_of(e, k);
+        if (!s.st) continue;
+        if (ch[k].in_flight && rc == LCG_OK) {
+            rc = chunk_finish(e, s, opts, ch[k], results, &t_wait, &t_res);
+        } else {
+            cudaStreamSynchronize(s.st);
+            ch[k].in_flight = false;
+        }
+    }
+    if (rc != LCG_OK)
+        for (int k = 0; k < 2; ++k)
+            if (slot_of(e, k).st) cudaStreamSynchronize(slot_of(e, k).st);
+    e->last_phase_ms[0] = t_prep;
+    e->last_phase_ms[1] = t_pack;
+    e->last_phase_ms[2] = t_wait;
+    e->last_phase_ms[3] = t_res;
+    return rc;
+}
+
+lcg_status lcg_engine_set_chunk_pairs(lcg_engine e, int32_t pairs_per_chunk) {
+    if (!e) return fail(LCG_ERR_ARG, "engine is NULL");
+    if (pairs_per_chunk < 0) return fail(LCG_ERR_ARG, "pairs_per_chunk < 0");
+    e->chunk_pairs = pairs_per_chunk;
     return LCG_OK;
 }
 

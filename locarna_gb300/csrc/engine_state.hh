@@ -5,6 +5,21 @@
 
 #include <cstddef>
 
+// Device arena, pinned staging, fill scratch, stream and events of one
+// in-flight chunk of an lcg_align_pairs call. The engine's own fields are
+// the first set; `alt` is the second one of the double-buffered pipeline.
+struct lcg_buffer_set {
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    char *d_arena = nullptr;
+    size_t arena_cap = 0;
+    char *h_stage = nullptr;
+    size_t stage_cap = 0;
+    int *d_scratch = nullptr;
+    size_t scratch_cap = 0;  // ints
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr;
+};
+
 struct lcg_engine_s {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -26,6 +41,10 @@ struct lcg_engine_s {
     // packing, copies + kernels (until the results are on the host), result assembly
     double last_phase_ms[4] = {0, 0, 0, 0};
     void *pf = nullptr;  // partition-function state (engine_pf.cu)
+    // pipeline of lcg_align_pairs: pairs per chunk (0 = automatic) and the
+    // second buffer set (created on first use)
+    int chunk_pairs = 0;
+    lcg_buffer_set alt;
 };
 
 namespace lcg_host {

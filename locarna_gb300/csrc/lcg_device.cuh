@@ -54,7 +54,8 @@ struct PairDev {
     const int *scls;      // PF_SCLS: 256-entry class table of sigma
     const int *rcls;      // PF_SCLS: n+2 row classes
     const int *ccls;      // PF_SCLS: m+1 column classes
-    const int *gbc;       // m+1: gapB(j) << 4 | sigma column class (0 without PF_SCLS)
+    const int *gbc;       // m+1: gap term << 4 | sigma column class (0 without PF_SCLS); the gap
+                          // term is gapB(j) with anchors, else the prefix sum sum_{t<=j} (gapB(t) + max(go,0))
     const int *gapA;      // n+1
     const int *gapB;      // m+1
     const int *min_col;   // n+2 (entry n+1 = m+1 sentinel)

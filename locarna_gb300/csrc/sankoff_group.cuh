@@ -95,7 +95,7 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
     const int gop = max(go, 0);
     const unsigned rmagic = 0xFFFFFFFFu / (unsigned)ringn + 1u;  // j / ringn = umulhi(j, rmagic), j < 2^20
     int *const E = lcg_smem + sbase + 2 * ringn;
-    int *const gBs = lcg_smem + sbase + 3 * ringn;   // gapB(j) << 4 | sigma column class (SCLS)
+    int *const gBs = lcg_smem + sbase + 3 * ringn;   // gap term (PairDev::gbc) << 4 | sigma column class
     int *const Arow = lcg_smem + sbase + 4 * ringn;  // arc-term maxima of the current row
     int *const Stab = lcg_smem + sbase + 5 * ringn;  // SCLS: 16 x 16 sigma class table
     int pv = sbase, cu = sbase + ringn;  // shared-memory offsets of the previous / current row
@@ -110,30 +110,40 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
 
     // ---- row al: M(al,bl)=0, M(al,j) = prefix of gap costs, -inf once blocked
     const int L0 = min(br, rowinfo[al].y + 1);
+    // without anchors the column table holds the prefix sums
+    // PA(j) = sum_{t<=j} (gapB(t) + gop); PA(bl) anchors the group's sums
+    const int PAbl = ANCH ? 0 : (P.gbc[bl] >> 4);
+    const int gdel = go - gop;
     {
         int carry = globalB ? go : 0;
         bool blocked_carry = false;
         for (int base = bl + 1; base < L0; base += 32) {
             int j = base + lane;
             bool act = j < L0;
-            bool blk = ANCH && act && !a_ins(P, al, j);
-            const int gbcj = act ? P.gbc[j] : 0;  // gapB(j) << 4 | sigma column class
+            const int gbcj = act ? P.gbc[j] : 0;  // gap term << 4 | sigma column class
             if (act) gBs[RG(j)] = gbcj;
-            int s = globalB ? gbcj >> 4 : 0;
-            unsigned bm = __ballot_sync(0xffffffffu, blk);
+            int val;
+            if (ANCH) {
+                bool blk = act && !a_ins(P, al, j);
+                int s = globalB ? gbcj >> 4 : 0;
+                unsigned bm = __ballot_sync(0xffffffffu, blk);
 #pragma unroll
-            for (int off = 1; off < 32; off <<= 1) {
-                int t = __shfl_up_sync(0xffffffffu, s, off);
-                if (lane >= off) s += t;
+                for (int off = 1; off < 32; off <<= 1) {
+                    int t = __shfl_up_sync(0xffffffffu, s, off);
+                    if (lane >= off) s += t;
+                }
+                bool anyblk = blocked_carry || (bm & (0xffffffffu >> (31 - lane)));
+                val = anyblk ? NEG : carry + s;
+                carry += __shfl_sync(0xffffffffu, s, 31);
+                blocked_carry = blocked_carry || bm != 0;
+            } else {
+                // go + sum_{bl<t<=j} gapB(t)
+                val = globalB ? go + (gbcj >> 4) - PAbl - (j - bl) * gop : 0;
             }
-            bool anyblk = blocked_carry || (bm & (0xffffffffu >> (31 - lane)));
-            int val = anyblk ? NEG : carry + s;
             if (act) {
                 PREV(j) = val;
                 Mg[j - bl] = val;
             }
-            carry += __shfl_sync(0xffffffffu, s, 31);
-            blocked_carry = blocked_carry || bm != 0;
         }
         if (lane == 0) {
             PREV(bl) = 0;
@@ -244,6 +254,11 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
         if (lane == 0) CUR(lo - 1) = B;
         int *Mrow = Mg + (i - al) * pitch - bl;
         int Fc = NEG, Xc = B;
+        // without anchors: Pc = max over k < base of M-open terms X(k) - PA(k),
+        // starting with k = lo-1 (column lo-1 > bl is in the ring: it is in
+        // the band of an earlier row of the group)
+        int Pc = 0;
+        if (!ANCH) Pc = B - (lo - 1 == bl ? PAbl : (gBs[RG(lo - 1)] >> 4));
         int k = 0;
         int rbase = RG(lo);  // ring index of column base, advanced by 32 per chunk
         for (int base = lo; base <= hi; base += 32, ++k) {
@@ -276,34 +291,46 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
                 if (rowarcs && mok) X = max(X, Arow[rj]);
             }
             if (TOP && local_top && act && i < la && j < lb) X = max(X, 0);
-            // horizontal gaps: max-plus scan of F(j) = max(F(j-1)+a_j, b_j)
-            int Xp = __shfl_up_sync(0xffffffffu, X, 1);
-            if (lane == 0) Xp = Xc;
-            int a = 0, b = NEG;
-            if (act) {
-                if (!ANCH || a_ins(P, i, j)) {
-                    const int gb = gbc >> 4;
-                    a = gb + gop;
-                    b = ANCH ? addc(Xp, gb + go) : Xp + gb + go;
-                } else {
-                    a = NEG;
-                }
-            }
-#pragma unroll
-            for (int off = 1; off < 32; off <<= 1) {
-                const int a1 = __shfl_up_sync(0xffffffffu, a, off);
-                const int b1 = __shfl_up_sync(0xffffffffu, b, off);
-                if (lane >= off) {
-                    if (ANCH) {
-                        b = max(addc(b1, a), b);
-                        a = addc(a1, a);
+            int F;
+            if (ANCH) {
+                // horizontal gaps: max-plus scan of F(j) = max(F(j-1)+a_j, b_j)
+                int Xp = __shfl_up_sync(0xffffffffu, X, 1);
+                if (lane == 0) Xp = Xc;
+                int a = 0, b = NEG;
+                if (act) {
+                    if (a_ins(P, i, j)) {
+                        const int gb = gbc >> 4;
+                        a = gb + gop;
+                        b = addc(Xp, gb + go);
                     } else {
-                        b = __viaddmax_s32(b1, a, b);
-                        a = a1 + a;
+                        a = NEG;
                     }
                 }
+#pragma unroll
+                for (int off = 1; off < 32; off <<= 1) {
+                    const int a1 = __shfl_up_sync(0xffffffffu, a, off);
+                    const int b1 = __shfl_up_sync(0xffffffffu, b, off);
+                    if (lane >= off) {
+                        b = max(addc(b1, a), b);
+                        a = addc(a1, a);
+                    }
+                }
+                F = max(addc(Fc, a), b);
+                Fc = __shfl_sync(0xffffffffu, F, 31);
+                Xc = __shfl_sync(0xffffffffu, X, 31);
+            } else {
+                // F(j) = max_{k<j} X(k) + go + sum_{k<t<=j} gapB(t)
+                //      = PA(j) + (go - gop) + max_{k<j} (X(k) - PA(k)),
+                // a prefix maximum over the lanes (inactive lanes: X = NEG)
+                const int pa = gbc >> 4;
+                const int v = X - pa;
+                int w = __shfl_up_sync(0xffffffffu, v, 1);
+                if (lane == 0) w = Pc;
+#pragma unroll
+                for (int off = 1; off < 32; off <<= 1) w = max(w, __shfl_up_sync(0xffffffffu, w, off));
+                F = w + pa + gdel;
+                Pc = __shfl_sync(0xffffffffu, max(w, v), 31);
             }
-            const int F = ANCH ? max(addc(Fc, a), b) : __viaddmax_s32(Fc, a, b);
             const int M = norm(max(X, F));
             if (act) {
                 CURR(rj) = M;
@@ -314,8 +341,6 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
                     bj = j;
                 }
             }
-            Fc = __shfl_sync(0xffffffffu, F, 31);
-            Xc = __shfl_sync(0xffffffffu, X, 31);
         }
         __syncwarp();
         if (DWRITE && i == dw_row) {

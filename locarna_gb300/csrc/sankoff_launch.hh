@@ -1,7 +1,7 @@
 // Host-side entry points of the Sankoff kernels (sankoff_kernels.cu,
 // sankoff_sl_kernels.cu, microbench.cu) used by engine.cu and noalloc.cu.
 // sw: scratch row pitch (ints); rb: ring size of the shared-memory rows (a
-// power of two above the column span of any two consecutive band rows).
+// multiple of 32 above the column span of any two consecutive band rows).
 #pragma once
 #include <cuda_runtime.h>
 

@@ -58,6 +58,8 @@ def _load_locked(path):
     lib.lcg_engine_last_phases.restype = C.c_int32
     lib.lcg_engine_last_transfer.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
     lib.lcg_engine_last_transfer.restype = C.c_int32
+    lib.lcg_engine_set_chunk_pairs.argtypes = [C.c_void_p, C.c_int32]
+    lib.lcg_engine_set_chunk_pairs.restype = C.c_int32
     lib.lcg_engine_set_counting.argtypes = [C.c_void_p, C.c_int32]
     lib.lcg_engine_set_counting.restype = C.c_int32
     lib.lcg_engine_last_work.argtypes = [C.c_void_p, C.POINTER(lcg_work_counts)]
@@ -153,6 +155,10 @@ class Engine:
         a, b = C.c_int64(), C.c_int64()
         _check(self.lib, self.lib.lcg_engine_last_transfer(self.h, C.byref(a), C.byref(b)))
         return a.value, b.value
+
+    def set_chunk_pairs(self, n):
+        """Pairs per chunk of lcg_align_pairs' pipeline (0: automatic)."""
+        _check(self.lib, self.lib.lcg_engine_set_chunk_pairs(self.h, int(n)))
 
     def set_counting(self, on):
         _check(self.lib, self.lib.lcg_engine_set_counting(self.h, int(bool(on))))

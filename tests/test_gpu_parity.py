@@ -31,3 +31,38 @@ def test_gpu_batch_matches_oracle(engine):
         for k, r in enumerate(res):
             g = group[k % len(group)]
             assert_same_result(r, oracle_align(g.tables, **kw), g.name)
+
+
+@pytest.mark.gpu
+def test_gpu_chunk_pipeline_matches_oracle(engine):
+    """lcg_align_pairs' chunk pipeline (two buffer sets, host preparation of
+    chunk k+1 during the device work of chunk k): automatic chunks for a
+    300-pair batch, then 7-pair chunks, equal the oracle pair by pair and the
+    one-chunk call bit for bit."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    from locarna_gb300.prep import prepare_pair
+    from locarna_gb300.synth import make_family
+    fam = make_family(25, 50, 110, 77, q=0.05)
+    pp = [r.to_pp() for r in fam]
+    pairs = [(a, b) for a in range(len(fam)) for b in range(a + 1, len(fam))]
+    with ThreadPoolExecutor(8) as ex:
+        tables = list(ex.map(lambda ab: prepare_pair(pp[ab[0]], pp[ab[1]]), pairs))
+    assert len(tables) == 300
+    try:
+        engine.set_chunk_pairs(len(tables))
+        one = engine.align_pairs(tables)
+        assert engine.last_stats()[1] == 2
+        engine.set_chunk_pairs(0)
+        auto = engine.align_pairs(tables)
+        assert engine.last_stats()[1] == 4  # two chunks of 150 pairs
+        engine.set_chunk_pairs(7)
+        small = engine.align_pairs(tables)
+        assert engine.last_stats()[1] == 2 * 43
+    finally:
+        engine.set_chunk_pairs(0)
+    for k, t in enumerate(tables):
+        ref = oracle_align(t)
+        assert_same_result(one[k], ref, f"pair {k}")
+        assert_same_result(auto[k], ref, f"pair {k} (automatic chunks)")
+        assert_same_result(small[k], ref, f"pair {k} (7-pair chunks)")
