@@ -26,6 +26,10 @@
 // Z = Z' c^(n+m); probabilities are unchanged. The FP32 path uses c from a
 // host estimate so values stay well inside the float range; FP64 uses c = 1.
 #include <cuda_runtime.h>
+
+#include <algorithm>
+#include <climits>
+#include <cstdlib>
 #include <stdint.h>
 
 #include "lcg_device.cuh"
@@ -369,6 +373,11 @@ __device__ void pf_group_back(const PFPair<T> &P, int al, int ar, int bl, int br
     const T o = P.o, arcf = P.arcf;
     T *const Eb = R.E;
     T *const Xb = R.Ar;
+    // diagonal adjoint contributions X_bar(i,j) bm(i,j) to M_bar(i-1,j-1):
+    // row i writes them into one ring (each target column once), row i-1
+    // reads them (and clears the entry) from it; the two rings alternate.
+    // Targets outside row i-1's columns, and row al, take the global atomic.
+    T *Dn = R.Mp, *Dc = R.Mc;
 #define RG(j) ((j) - R.rb * (int)__umulhi((unsigned)(j), R.magic))
     const int rows = ar - al;
     // clear the adjoint rectangle (band cells and boundaries)
@@ -379,7 +388,11 @@ __device__ void pf_group_back(const PFPair<T> &P, int al, int ar, int bl, int br
         for (int j = lo + lane; j <= hi; j += 32) Mb[(size_t)r * pitch + (j - bl)] = T(0);
         if (lane == 0) Mb[(size_t)r * pitch] = T(0);
     }
-    for (int c = lane; c < R.rb; c += 32) Eb[c] = T(0);
+    for (int c = lane; c < R.rb; c += 32) {
+        Eb[c] = T(0);
+        Dn[c] = T(0);
+        Dc[c] = T(0);
+    }
     __syncwarp();
     if (top && lane == 0) Mb[(size_t)(P.n - al) * pitch + (P.m - bl)] = T(1);
     __syncwarp();
@@ -421,6 +434,10 @@ __device__ void pf_group_back(const PFPair<T> &P, int al, int ar, int bl, int br
         const T *bmrow = P.bm + (size_t)i * m1;
         const size_t roff = (size_t)(i - al) * pitch;
         const int cb = ri.w - minc;
+        // columns of row i-1 whose diagonal contributions go through the ring
+        const int4 rup = P.rowinfo[i - 1];
+        const int dlo = i - 1 > al ? max(bl + 1, rup.x) : INT_MAX;
+        const int dhi = min(br - 1, rup.y);
         // chunks right to left
         const int nchunks = hi >= lo ? (hi - lo) / 32 + 1 : 0;
         T Fbc = T(0);  // F_bar(i, base+32) carried from the chunk to the right
@@ -434,7 +451,8 @@ __device__ void pf_group_back(const PFPair<T> &P, int al, int ar, int bl, int br
             T Mbar = T(0), Ebn = T(0), g = T(0), Ev = T(0), Fv = T(0), Mv = T(0), Mup = T(0), Eup = T(0),
               bmj = T(0);
             if (act) {
-                Mbar = ld_cg(Mb + roff + c);
+                Mbar = ld_cg(Mb + roff + c) + Dc[RG(j)];
+                Dc[RG(j)] = T(0);
                 Ebn = Eb[RG(j)];  // E_bar(i+1, j)
                 g = P.gB[j];
                 Ev = Eg[roff + c];
@@ -482,10 +500,13 @@ __device__ void pf_group_back(const PFPair<T> &P, int al, int ar, int bl, int br
                 ext += (double)(Ebar * Ev + Fb * Fv);
                 opn += (double)(Ebar * (Mup - Eup) * gAi * o + Fb * (Ml - Fl) * g * o);
                 // diagonal
-                atomicAdd(Mb + roff - pitch + c - 1, Xbar * bmj);
+                if (j - 1 >= dlo && j - 1 <= dhi)
+                    Dn[RG(j - 1)] = Xbar * bmj;
+                else
+                    atomicAdd(Mb + roff - pitch + c - 1, Xbar * bmj);
                 atomicAdd(P.bmacc + cb + j, (double)(Xbar * Md * bmj));
                 // E(i,j) reads N(i-1,j) = M(i-1,j) - E(i-1,j); F(i,j) reads Q(i,j-1)
-                if (i - 1 == al || P.rowinfo[i - 1].x > j || P.rowinfo[i - 1].y < j)
+                if (i - 1 == al || rup.x > j || rup.y < j)
                     atomicAdd(Mb + roff - pitch + c, Ebar * gAi * o);
                 if (j == lo) atomicAdd(Mb + roff + c - 1, Fb * g * o);
             }
@@ -493,8 +514,27 @@ __device__ void pf_group_back(const PFPair<T> &P, int al, int ar, int bl, int br
         }
         __syncwarp();
         // arc terms of row i: M_bar(corner) += X_bar D s', D_bar(am) += X_bar M(corner) s'
-        // (two batches of 32 entries per step, loads issued together)
-        for (int e0 = ra.x; e0 < ra.y; e0 += 64) {
+        // (two batches of 32 entries per step, loads issued together). The
+        // use counters of the row's entries drop after one fence per row:
+        // bit 2k+u of `pend` stands for entry ebase + 64k + 32u + lane.
+        unsigned long long pend = 0;
+        int ebase = ra.x, kb = 0;
+        auto drop_uses = [&]() {
+            if (pend) {
+                __threadfence();  // the D_bar updates are visible before the counters drop
+                do {
+                    const int b = __ffsll((long long)pend) - 1;
+                    pend &= pend - 1;
+                    atomicSub(P.cnt + ebase + 64 * (b >> 1) + 32 * (b & 1) + lane, 1);
+                } while (pend);
+            }
+        };
+        for (int e0 = ra.x; e0 < ra.y; e0 += 64, ++kb) {
+            if (kb == 32) {
+                drop_uses();
+                ebase = e0;
+                kb = 0;
+            }
             int2 en[2];
             bool okA[2];
             unsigned ball[2];
@@ -527,19 +567,21 @@ __device__ void pf_group_back(const PFPair<T> &P, int al, int ar, int bl, int br
                     atomicAdd(P.Dbar + e0 + 32 * u + lane, (double)(xb[u] * mv[u] * arcf));
                 }
             }
-            // the D_bar updates are visible before their use counters drop
-            if (ok[0] || ok[1]) __threadfence();
 #pragma unroll
             for (int u = 0; u < 2; ++u)
-                if (ok[u]) atomicSub(P.cnt + e0 + 32 * u + lane, 1);
+                if (ok[u]) pend |= 1ull << (2 * kb + u);
             if (ball[0] != 0xffffffffu || ball[1] != 0xffffffffu) break;
         }
+        drop_uses();
         // E_bar of row i at columns row i-1 has but row i does not is zero
         if (i - 1 > al) {
             const int lp = max(bl + 1, P.rowinfo[i - 1].x);
             for (int j = lp + lane; j < lo; j += 32) Eb[RG(j)] = T(0);
         }
         __syncwarp();
+        T *const dt = Dn;  // row i-1 reads what row i wrote
+        Dn = Dc;
+        Dc = dt;
         if (*abort_flag) return;
     }
     // boundary values: M(al,j) = (o/s) prod gB, M(i,bl) = (o/s) prod gA
@@ -629,12 +671,33 @@ cudaError_t pf_launch_fwd(const void *pairs, const int2 *queue, int nitems, void
     return cudaGetLastError();
 }
 
+// Resident blocks per SM for a kernel that could hold `occ`: the cap from
+// the environment variable `var` (tuning runs), else `occ`. A cap below occ
+// also asks for a shared-memory carveout that fits only the capped blocks, so
+// that the rest of the SM's unified memory serves as L1 cache.
+template <typename K>
+static cudaError_t pf_cap_blocks(K kernel, const char *var, size_t smem, int *blocks_per_sm) {
+    const char *v = std::getenv(var);
+    const int cap = v ? std::atoi(v) : 0;
+    cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, -1);
+    if (cap <= 0 || cap >= *blocks_per_sm) return cudaSuccess;
+    *blocks_per_sm = cap;
+    int dev = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    const size_t want = (size_t)cap * (smem + 1024);
+    const int pct = (int)std::min<size_t>(100, (want * 100 + per_sm - 1) / (size_t)std::max(per_sm, 1));
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, pct);
+}
+
 template <typename T>
 cudaError_t pf_fwd_occupancy(int rb, int *blocks_per_sm) {
     const size_t smem = pf_smem<T>(rb);
     cudaError_t e = cudaFuncSetAttribute(pf_fwd_kernel<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, pf_fwd_kernel<T, true>, PF_WARPS * 32, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, pf_fwd_kernel<T, true>, PF_WARPS * 32, smem);
+    if (e != cudaSuccess) return e;
+    return pf_cap_blocks(pf_fwd_kernel<T, true>, "LCG_PF_FWD_BPS", smem, blocks_per_sm);
 }
 
 template <typename T>
@@ -655,7 +718,9 @@ cudaError_t pf_back_occupancy(int rb, int *blocks_per_sm) {
     const size_t smem = pf_smem<T>(rb);
     cudaError_t e = cudaFuncSetAttribute(pf_back_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, pf_back_kernel<T>, PF_WARPS * 32, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, pf_back_kernel<T>, PF_WARPS * 32, smem);
+    if (e != cudaSuccess) return e;
+    return pf_cap_blocks(pf_back_kernel<T>, "LCG_PF_BACK_BPS", smem, blocks_per_sm);
 }
 
 int pf_warps_per_block() { return PF_WARPS; }
