@@ -330,6 +330,20 @@ void lcg_prep_opts_default(lcg_prep_opts *opts);
 /* Parse two PP 2.0 texts and build the pair's tables (opts NULL = defaults). */
 lcg_status lcg_prepare_pair(const char *pp_a, const char *pp_b, const lcg_prep_opts *opts,
                             lcg_prepared *out);
+
+/* Batched lcg_prepare_pair: the tables of npairs pairs (pp_a[q], pp_b[q]),
+ * identical to lcg_prepare_pair's, with the sequence envelope of all pairs
+ * computed on the engine's GPU (PFGotoh / PFTraceProbs, edge_probs.icc:76-268,
+ * in FP64 with per-row power-of-two scaling). A pair whose edge probability
+ * lies within 1e-7 relative of min_trace_probability where it could move a
+ * band row, or whose values would leave the range of the reference's float
+ * type (or whose lengths sum above 1000 for double, 16000 for long double),
+ * gets its envelope from the host path in the reference's precision; their
+ * number goes to *host_envelopes (may be NULL). Parsing and table building
+ * run on the host threads. out[q] are freed with lcg_prepared_free. */
+lcg_status lcg_prepare_pairs(lcg_engine eng, const char *const *pp_a, const char *const *pp_b,
+                             int32_t npairs, const lcg_prep_opts *opts, lcg_prepared *out,
+                             int32_t *host_envelopes);
 /* Views into the prepared tables; valid until lcg_prepared_free. */
 lcg_status lcg_prepared_tables(lcg_prepared p, lcg_pair_tables *out);
 /* which: 0 sequence A, 1 sequence B, 2 name A, 3 name B */

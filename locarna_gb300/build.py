@@ -25,7 +25,7 @@ GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 EXTRA_DEFS = os.environ.get("LCG_NVCC_DEFS", "").split()
 
 CUDA_SOURCES = ["engine.cu", "sankoff_kernels.cu", "sankoff_sl_kernels.cu", "microbench.cu", "noalloc.cu",
-                "pf_kernels.cu", "engine_pf.cu"]
+                "pf_kernels.cu", "engine_pf.cu", "envelope.cu"]
 HOST_SOURCES = ["host_prep.cpp"]  # C++ host-only translation units
 
 

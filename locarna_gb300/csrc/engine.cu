@@ -884,6 +884,8 @@ lcg_status lcg_engine_destroy(lcg_engine e) {
     if (b.ev1) cudaEventDestroy(b.ev1);
     if (b.ev2) cudaEventDestroy(b.ev2);
     if (b.own_stream) cudaStreamDestroy(b.stream);
+    if (e->env_dev) cudaFree(e->env_dev);
+    if (e->env_host) cudaFreeHost(e->env_host);
     lcg_host::pf_release(e);
     delete e;
     return LCG_OK;

@@ -45,6 +45,11 @@ struct lcg_engine_s {
     // second buffer set (created on first use)
     int chunk_pairs = 0;
     lcg_buffer_set alt;
+    // batched table preparation (envelope.cu): device arena and pinned staging
+    char *env_dev = nullptr;
+    size_t env_dev_cap = 0;
+    char *env_host = nullptr;
+    size_t env_host_cap = 0;
 };
 
 namespace lcg_host {

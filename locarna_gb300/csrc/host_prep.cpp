@@ -20,6 +20,7 @@
 // in the reference, so that thresholds (p >= min_prob, envelope >= 1e-4) and
 // rounded integer scores come out identical on the same host.
 #include <algorithm>
+#include <atomic>
 #include <cctype>
 #include <cmath>
 #include <cstdio>
@@ -29,9 +30,11 @@
 #include <memory>
 #include <sstream>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/locarna_gb300.h"
+#include "envelope.hh"
 
 namespace {
 
@@ -330,6 +333,9 @@ int reverse_fe(int fe) {
     return r;
 }
 
+template <class I>
+void apply_envelope_rows(Band &tc, const I *nmin, const I *nmax);
+
 // PFTraceProbs (edge_probs.icc:212-268) followed by
 // TraceController::restrict_by_trace_probabilities (trace_controller.cc:565-597)
 template <class T>
@@ -378,6 +384,7 @@ bool restrict_by_envelope(Band &tc, const Side &A, const Side &B, const lcg_prep
         }
     }
     const double min_prob = o.min_trace_probability;
+    std::vector<long> nmin(n + 1), nmax(n + 1);
     for (int i = 0; i <= n; ++i) {
         long new_min = tc.maxc[i], new_max = tc.minc[i];
         for (long j = tc.minc[i]; j <= tc.maxc[i]; ++j) {
@@ -386,8 +393,21 @@ bool restrict_by_envelope(Band &tc, const Side &A, const Side &B, const lcg_prep
                 new_max = std::max(new_max, j);
             }
         }
-        tc.minc[i] = std::max(tc.minc[i], new_min);
-        tc.maxc[i] = std::min(tc.maxc[i], new_max);
+        nmin[i] = new_min;
+        nmax[i] = new_max;
+    }
+    apply_envelope_rows(tc, nmin.data(), nmax.data());
+    return !failed;
+}
+
+// the band update of TraceController::restrict_by_trace_probabilities
+// (trace_controller.cc:576-597) from each row's first and last kept column
+template <class I>
+void apply_envelope_rows(Band &tc, const I *nmin, const I *nmax) {
+    const int n = (int)tc.minc.size() - 1;
+    for (int i = 0; i <= n; ++i) {
+        tc.minc[i] = std::max(tc.minc[i], (long)nmin[i]);
+        tc.maxc[i] = std::min(tc.maxc[i], (long)nmax[i]);
     }
     long mx = 0;
     for (int i = 0; i <= n; ++i) {
@@ -400,7 +420,6 @@ bool restrict_by_envelope(Band &tc, const Side &A, const Side &B, const lcg_prep
         tc.minc[i] = std::min(tc.minc[i], mn);
         mn = tc.minc[i];
     }
-    return !failed;
 }
 
 // TraceController::constrain_wo_ref (trace_controller.cc:360-390)
@@ -469,6 +488,158 @@ namespace lcg_host {
 void set_error(const std::string &msg);
 }
 
+namespace {
+
+// One pair between the stages of the preparation: inputs read, band before
+// the envelope, then the tables.
+struct Staged {
+    lcg_prep_opts o;
+    Side A, B;
+    Band tc;
+    std::unique_ptr<lcg_prepared_s> P;
+    lcg_status code = LCG_OK;
+    std::string err;
+};
+
+// PP reading, arcs, the max-diff band (locarna.cc:398-560)
+void stage_inputs(const char *pp_a, const char *pp_b, Staged &S) {
+    const lcg_prep_opts &o = S.o;
+    S.P = std::make_unique<lcg_prepared_s>();
+    Side &A = S.A, &B = S.B;
+    A.in = read_pp(pp_a, o.min_prob);
+    B.in = read_pp(pp_b, o.min_prob);
+    make_arcs(A, o.min_prob);
+    make_arcs(B, o.min_prob);
+    const int n = A.len, m = B.len;
+    lcg_prepared_s *P = S.P.get();
+    P->n = n;
+    P->m = m;
+    P->seq_a = A.in.seq;
+    P->seq_b = B.in.seq;
+    P->name_a = A.in.name;
+    P->name_b = B.in.name;
+    // trace controller (no reference alignment, no anchors)
+    S.tc.minc.assign(n + 1, 0);
+    S.tc.maxc.assign(n + 1, m);
+    if (o.max_diff >= 0) constrain_wo_ref(S.tc, n, m, (size_t)o.max_diff);
+}
+
+// the envelope in the reference's precision (edge_probs.icc, trace_controller.cc:565-597)
+void stage_envelope_host(Staged &S) {
+    bool ok;
+    if (S.o.pf_precision == 0) ok = restrict_by_envelope<double>(S.tc, S.A, S.B, S.o);
+    else ok = restrict_by_envelope<long double>(S.tc, S.A, S.B, S.o);
+    S.P->envelope_ok = ok ? 1 : 0;
+}
+
+// scoring tables and arc matches on the final band (locarna.cc:560-703)
+void stage_tables(Staged &S) {
+    const lcg_prep_opts &o = S.o;
+    Side &A = S.A, &B = S.B;
+    const Band &tc = S.tc;
+    lcg_prepared_s *P = S.P.get();
+    const int n = A.len, m = B.len;
+    // scoring tables
+    P->sigma.assign((size_t)(n + 1) * (m + 1), 0);
+    long tab[256][256];
+    bool have[256][256];
+    std::memset(have, 0, sizeof have);
+    for (int i = 1; i <= n; ++i) {
+        unsigned char ca = (unsigned char)A.in.seq[i - 1];
+        for (int j = 1; j <= m; ++j) {
+            unsigned char cb = (unsigned char)B.in.seq[j - 1];
+            if (!have[ca][cb]) {
+                tab[ca][cb] = sigma_single(o, (char)ca, (char)cb);
+                have[ca][cb] = true;
+            }
+            P->sigma[(size_t)i * (m + 1) + j] = (int32_t)tab[ca][cb];
+        }
+    }
+    // Scoring::precompute_gapcost (scoring.cc:271-311) for gap-free rows
+    P->gap_a.assign(n + 1, 0);
+    P->gap_b.assign(m + 1, 0);
+    for (int i = 1; i <= n; ++i) {
+        float gf = A.in.seq[i - 1] == '-' ? 1.0f : 0.0f;
+        P->gap_a[i] = (int32_t)round2score((1 - gf) * o.indel);
+    }
+    for (int j = 1; j <= m; ++j) {
+        float gf = B.in.seq[j - 1] == '-' ? 1.0f : 0.0f;
+        P->gap_b[j] = (int32_t)round2score((1 - gf) * o.indel);
+    }
+    P->indel_opening = o.indel_opening;
+    P->exclusion = o.exclusion;
+    double peA = o.exp_prob > 0 ? o.exp_prob : 1.0 / (2.0 * n);
+    double peB = o.exp_prob > 0 ? o.exp_prob : 1.0 / (2.0 * m);
+    for (auto &a : A.arcs) A.weights.push_back(prob_to_weight(a.p, peA, o.struct_weight));
+    for (auto &b : B.arcs) B.weights.push_back(prob_to_weight(b.p, peB, o.struct_weight));
+
+    // arc matches (arc_matches.cc:130-188), A index outer, B index inner
+    const size_t mdam = o.max_diff_am != -1 ? (size_t)o.max_diff_am : (size_t)std::max(n, m);
+    const size_t mdaam = o.max_diff_at_am != -1 ? (size_t)o.max_diff_at_am : (size_t)std::max(n, m);
+    auto valid = [&](long i, long j) { return i >= 0 && i <= n && tc.minc[i] <= j && j <= tc.maxc[i]; };
+    auto valid_match = [&](long i, long j) { return valid(i, j) && valid(i - 1, j - 1); };
+    long ribo_cache[4][4][4][4];
+    bool ribo_have[4][4][4][4];
+    std::memset(ribo_have, 0, sizeof ribo_have);
+    for (size_t ia = 0; ia < A.arcs.size(); ++ia) {
+        const Arc &a = A.arcs[ia];
+        for (size_t ib = 0; ib < B.arcs.size(); ++ib) {
+            const Arc &b = B.arcs[ib];
+            bool ok = valid_match(a.l, b.l) && valid_match(a.r, b.r) &&
+                      (size_t)std::abs((a.r - a.l) - (b.r - b.l)) <= mdam &&
+                      (size_t)a.l <= b.l + mdaam && (size_t)b.l <= a.l + mdaam &&
+                      (size_t)a.r <= b.r + mdaam && (size_t)b.r <= a.r + mdaam;
+            if (!ok) continue;
+            long seqc = 0;
+            if (o.tau != 0) {
+                if (o.use_ribosum) {
+                    char c1 = A.in.seq[a.l - 1], c2 = A.in.seq[a.r - 1];
+                    char c3 = B.in.seq[b.l - 1], c4 = B.in.seq[b.r - 1];
+                    int x1 = idx_acgu(c1), x2 = idx_acgu(c2), x3 = idx_acgu(c3), x4 = idx_acgu(c4);
+                    if (x1 >= 0 && x2 >= 0 && x3 >= 0 && x4 >= 0) {
+                        if (!ribo_have[x1][x2][x3][x4]) {
+                            ribo_cache[x1][x2][x3][x4] = riboX_single(c1, c2, c3, c4);
+                            ribo_have[x1][x2][x3][x4] = true;
+                        }
+                        seqc = ribo_cache[x1][x2][x3][x4];
+                    } else {
+                        seqc = riboX_single(c1, c2, c3, c4);
+                    }
+                } else {
+                    seqc = P->sigma[(size_t)a.l * (m + 1) + b.l] + P->sigma[(size_t)a.r * (m + 1) + b.r];
+                }
+            }
+            long s = ((long)o.tau * seqc) / 100 + (A.weights[ia] + B.weights[ib]);
+            P->am_arcs.push_back((int32_t)ia);
+            P->am_arcs.push_back((int32_t)ib);
+            P->am_score.push_back((int32_t)s);
+            P->am_dsw.push_back((1 - log(a.p) / log(peA)) + (1 - log(b.p) / log(peB)));
+        }
+    }
+    for (auto &a : A.arcs) {
+        P->arcs_a.push_back(a.l);
+        P->arcs_a.push_back(a.r);
+        P->arc_p_a.push_back(a.p);
+    }
+    for (auto &b : B.arcs) {
+        P->arcs_b.push_back(b.l);
+        P->arcs_b.push_back(b.r);
+        P->arc_p_b.push_back(b.p);
+    }
+    P->code_a.assign(n + 1, -1);
+    P->code_b.assign(m + 1, -1);
+    for (int i = 1; i <= n; ++i) P->code_a[i] = (int8_t)idx_acgu(A.in.seq[i - 1]);
+    for (int j = 1; j <= m; ++j) P->code_b[j] = (int8_t)idx_acgu(B.in.seq[j - 1]);
+    P->min_col.resize(n + 1);
+    P->max_col.resize(n + 1);
+    for (int i = 0; i <= n; ++i) {
+        P->min_col[i] = (int32_t)tc.minc[i];
+        P->max_col[i] = (int32_t)tc.maxc[i];
+    }
+}
+
+}  // namespace
+
 lcg_status lcg_prepare_pair(const char *pp_a, const char *pp_b, const lcg_prep_opts *opts,
                             lcg_prepared *out) {
     if (!pp_a || !pp_b || !out) {
@@ -476,134 +647,14 @@ lcg_status lcg_prepare_pair(const char *pp_a, const char *pp_b, const lcg_prep_o
         return LCG_ERR_ARG;
     }
     *out = nullptr;
-    lcg_prep_opts o;
-    if (opts) o = *opts;
-    else lcg_prep_opts_default(&o);
+    Staged S;
+    if (opts) S.o = *opts;
+    else lcg_prep_opts_default(&S.o);
     try {
-        auto P = std::make_unique<lcg_prepared_s>();
-        Side A, B;
-        A.in = read_pp(pp_a, o.min_prob);
-        B.in = read_pp(pp_b, o.min_prob);
-        make_arcs(A, o.min_prob);
-        make_arcs(B, o.min_prob);
-        const int n = A.len, m = B.len;
-        P->n = n;
-        P->m = m;
-        P->seq_a = A.in.seq;
-        P->seq_b = B.in.seq;
-        P->name_a = A.in.name;
-        P->name_b = B.in.name;
-
-        // trace controller (no reference alignment, no anchors)
-        Band tc;
-        tc.minc.assign(n + 1, 0);
-        tc.maxc.assign(n + 1, m);
-        if (o.max_diff >= 0) constrain_wo_ref(tc, n, m, (size_t)o.max_diff);
-        if (o.min_trace_probability > 0.0) {
-            bool ok;
-            if (o.pf_precision == 0) ok = restrict_by_envelope<double>(tc, A, B, o);
-            else ok = restrict_by_envelope<long double>(tc, A, B, o);
-            P->envelope_ok = ok ? 1 : 0;
-        }
-
-        // scoring tables
-        P->sigma.assign((size_t)(n + 1) * (m + 1), 0);
-        long tab[256][256];
-        bool have[256][256];
-        std::memset(have, 0, sizeof have);
-        for (int i = 1; i <= n; ++i) {
-            unsigned char ca = (unsigned char)A.in.seq[i - 1];
-            for (int j = 1; j <= m; ++j) {
-                unsigned char cb = (unsigned char)B.in.seq[j - 1];
-                if (!have[ca][cb]) {
-                    tab[ca][cb] = sigma_single(o, (char)ca, (char)cb);
-                    have[ca][cb] = true;
-                }
-                P->sigma[(size_t)i * (m + 1) + j] = (int32_t)tab[ca][cb];
-            }
-        }
-        // Scoring::precompute_gapcost (scoring.cc:271-311) for gap-free rows
-        P->gap_a.assign(n + 1, 0);
-        P->gap_b.assign(m + 1, 0);
-        for (int i = 1; i <= n; ++i) {
-            float gf = A.in.seq[i - 1] == '-' ? 1.0f : 0.0f;
-            P->gap_a[i] = (int32_t)round2score((1 - gf) * o.indel);
-        }
-        for (int j = 1; j <= m; ++j) {
-            float gf = B.in.seq[j - 1] == '-' ? 1.0f : 0.0f;
-            P->gap_b[j] = (int32_t)round2score((1 - gf) * o.indel);
-        }
-        P->indel_opening = o.indel_opening;
-        P->exclusion = o.exclusion;
-        double peA = o.exp_prob > 0 ? o.exp_prob : 1.0 / (2.0 * n);
-        double peB = o.exp_prob > 0 ? o.exp_prob : 1.0 / (2.0 * m);
-        for (auto &a : A.arcs) A.weights.push_back(prob_to_weight(a.p, peA, o.struct_weight));
-        for (auto &b : B.arcs) B.weights.push_back(prob_to_weight(b.p, peB, o.struct_weight));
-
-        // arc matches (arc_matches.cc:130-188), A index outer, B index inner
-        const size_t mdam = o.max_diff_am != -1 ? (size_t)o.max_diff_am : (size_t)std::max(n, m);
-        const size_t mdaam = o.max_diff_at_am != -1 ? (size_t)o.max_diff_at_am : (size_t)std::max(n, m);
-        auto valid = [&](long i, long j) { return i >= 0 && i <= n && tc.minc[i] <= j && j <= tc.maxc[i]; };
-        auto valid_match = [&](long i, long j) { return valid(i, j) && valid(i - 1, j - 1); };
-        long ribo_cache[4][4][4][4];
-        bool ribo_have[4][4][4][4];
-        std::memset(ribo_have, 0, sizeof ribo_have);
-        for (size_t ia = 0; ia < A.arcs.size(); ++ia) {
-            const Arc &a = A.arcs[ia];
-            for (size_t ib = 0; ib < B.arcs.size(); ++ib) {
-                const Arc &b = B.arcs[ib];
-                bool ok = valid_match(a.l, b.l) && valid_match(a.r, b.r) &&
-                          (size_t)std::abs((a.r - a.l) - (b.r - b.l)) <= mdam &&
-                          (size_t)a.l <= b.l + mdaam && (size_t)b.l <= a.l + mdaam &&
-                          (size_t)a.r <= b.r + mdaam && (size_t)b.r <= a.r + mdaam;
-                if (!ok) continue;
-                long seqc = 0;
-                if (o.tau != 0) {
-                    if (o.use_ribosum) {
-                        char c1 = A.in.seq[a.l - 1], c2 = A.in.seq[a.r - 1];
-                        char c3 = B.in.seq[b.l - 1], c4 = B.in.seq[b.r - 1];
-                        int x1 = idx_acgu(c1), x2 = idx_acgu(c2), x3 = idx_acgu(c3), x4 = idx_acgu(c4);
-                        if (x1 >= 0 && x2 >= 0 && x3 >= 0 && x4 >= 0) {
-                            if (!ribo_have[x1][x2][x3][x4]) {
-                                ribo_cache[x1][x2][x3][x4] = riboX_single(c1, c2, c3, c4);
-                                ribo_have[x1][x2][x3][x4] = true;
-                            }
-                            seqc = ribo_cache[x1][x2][x3][x4];
-                        } else {
-                            seqc = riboX_single(c1, c2, c3, c4);
-                        }
-                    } else {
-                        seqc = P->sigma[(size_t)a.l * (m + 1) + b.l] + P->sigma[(size_t)a.r * (m + 1) + b.r];
-                    }
-                }
-                long s = ((long)o.tau * seqc) / 100 + (A.weights[ia] + B.weights[ib]);
-                P->am_arcs.push_back((int32_t)ia);
-                P->am_arcs.push_back((int32_t)ib);
-                P->am_score.push_back((int32_t)s);
-                P->am_dsw.push_back((1 - log(a.p) / log(peA)) + (1 - log(b.p) / log(peB)));
-            }
-        }
-        for (auto &a : A.arcs) {
-            P->arcs_a.push_back(a.l);
-            P->arcs_a.push_back(a.r);
-            P->arc_p_a.push_back(a.p);
-        }
-        for (auto &b : B.arcs) {
-            P->arcs_b.push_back(b.l);
-            P->arcs_b.push_back(b.r);
-            P->arc_p_b.push_back(b.p);
-        }
-        P->code_a.assign(n + 1, -1);
-        P->code_b.assign(m + 1, -1);
-        for (int i = 1; i <= n; ++i) P->code_a[i] = (int8_t)idx_acgu(A.in.seq[i - 1]);
-        for (int j = 1; j <= m; ++j) P->code_b[j] = (int8_t)idx_acgu(B.in.seq[j - 1]);
-        P->min_col.resize(n + 1);
-        P->max_col.resize(n + 1);
-        for (int i = 0; i <= n; ++i) {
-            P->min_col[i] = (int32_t)tc.minc[i];
-            P->max_col[i] = (int32_t)tc.maxc[i];
-        }
-        *out = P.release();
+        stage_inputs(pp_a, pp_b, S);
+        if (S.o.min_trace_probability > 0.0) stage_envelope_host(S);
+        stage_tables(S);
+        *out = S.P.release();
         return LCG_OK;
     } catch (const PrepError &e) {
         lcg_host::set_error(e.msg);
@@ -612,6 +663,157 @@ lcg_status lcg_prepare_pair(const char *pp_a, const char *pp_b, const lcg_prep_o
         lcg_host::set_error(e.what());
         return LCG_ERR_NOMEM;
     }
+}
+
+namespace {
+
+// fn(q) for q in [0, n) on the host's threads
+template <typename F>
+void host_parallel(int n, F &&fn) {
+    if (n <= 0) return;
+    std::atomic<int> next(0);
+    const int nth = (int)std::min<unsigned>(std::max(1u, std::thread::hardware_concurrency()), (unsigned)std::min(n, 64));
+    auto work = [&]() {
+        for (int q; (q = next.fetch_add(1)) < n;) fn(q);
+    };
+    std::vector<std::thread> th;
+    for (int t = 1; t < nth; ++t) th.emplace_back(work);
+    work();
+    for (auto &t : th) t.join();
+}
+
+template <typename F>
+void guarded(Staged &S, F &&fn) {
+    if (S.code != LCG_OK) return;
+    try {
+        fn();
+    } catch (const PrepError &e) {
+        S.code = e.code;
+        S.err = e.msg;
+    } catch (const std::exception &e) {
+        S.code = LCG_ERR_NOMEM;
+        S.err = e.what();
+    }
+}
+
+}  // namespace
+
+lcg_status lcg_prepare_pairs(lcg_engine eng, const char *const *pp_a, const char *const *pp_b, int32_t npairs,
+                             const lcg_prep_opts *opts, lcg_prepared *out, int32_t *host_envelopes) {
+    if (!eng || !pp_a || !pp_b || !out || npairs < 0) {
+        lcg_host::set_error("NULL argument");
+        return LCG_ERR_ARG;
+    }
+    if (host_envelopes) *host_envelopes = 0;
+    for (int q = 0; q < npairs; ++q) out[q] = nullptr;
+    if (npairs == 0) return LCG_OK;
+    lcg_prep_opts o;
+    if (opts) o = *opts;
+    else lcg_prep_opts_default(&o);
+    std::vector<Staged> st(npairs);
+    for (auto &S : st) S.o = o;
+    host_parallel(npairs, [&](int q) {
+        guarded(st[q], [&]() {
+            if (!pp_a[q] || !pp_b[q]) throw PrepError{LCG_ERR_ARG, "NULL PP text"};
+            stage_inputs(pp_a[q], pp_b[q], st[q]);
+        });
+    });
+    for (int q = 0; q < npairs; ++q)
+        if (st[q].code != LCG_OK) {
+            lcg_host::set_error("pair " + std::to_string(q) + ": " + st[q].err);
+            return st[q].code;
+        }
+    if (o.min_trace_probability > 0.0) {
+        // per-position inputs of the GPU envelope
+        lcg_env::Params ep;
+        ep.sw = o.struct_weight / 100.0;
+        ep.temp = o.temperature_alipf / 100.0;
+        ep.g_open = exp((o.indel_opening / 100.0) / ep.temp);
+        ep.g_ext = exp((o.indel / 100.0) / ep.temp);
+        ep.min_prob = o.min_trace_probability;
+        for (int a = 0; a < 4; ++a)
+            for (int b = 0; b < 4; ++b)
+                ep.score[a * 4 + b] = o.use_ribosum ? kBmScore[a * 4 + b] : (a == b ? (double)o.match : (double)o.mismatch);
+        ep.local = o.sequ_local != 0;
+        ep.fe = o.free_endgaps & 15;
+        // |log2| range of the reference's float type, and the sequence
+        // lengths up to which no value of the recursions comes near its
+        // subnormal range; longer pairs take the host path
+        const bool dbl = o.pf_precision == 0;
+        ep.exp_limit = dbl ? 1000 : 16000;
+        const int max_len_sum = dbl ? 1000 : 16000;
+        struct Buf {
+            std::vector<int8_t> ca, cb;
+            std::vector<double> sdA, suA, sdB, suB;
+            std::vector<int32_t> minc, maxc, nmin, nmax;
+        };
+        std::vector<Buf> buf(npairs);
+        std::vector<lcg_env::PairIn> in;
+        std::vector<lcg_env::PairOut> res;
+        std::vector<int> gpu_q;
+        for (int q = 0; q < npairs; ++q)
+            if (st[q].A.len + st[q].B.len <= max_len_sum) gpu_q.push_back(q);
+        in.resize(gpu_q.size());
+        res.resize(gpu_q.size());
+        host_parallel((int)gpu_q.size(), [&](int k) {
+            const int q = gpu_q[k];
+            const Staged &S = st[q];
+            Buf &b = buf[q];
+            const int n = S.A.len, m = S.B.len;
+            b.ca.assign(n + 1, -1);
+            b.cb.assign(m + 1, -1);
+            b.sdA.assign(n + 1, 0.0);
+            b.suA.assign(n + 1, 0.0);
+            b.sdB.assign(m + 1, 0.0);
+            b.suB.assign(m + 1, 0.0);
+            for (int i = 1; i <= n; ++i) {
+                b.ca[i] = (int8_t)idx_acgu(S.A.in.seq[i - 1]);
+                b.sdA[i] = std::sqrt(S.A.p_down[i]);
+                b.suA[i] = std::sqrt(S.A.p_up[i]);
+            }
+            for (int j = 1; j <= m; ++j) {
+                b.cb[j] = (int8_t)idx_acgu(S.B.in.seq[j - 1]);
+                b.sdB[j] = std::sqrt(S.B.p_down[j]);
+                b.suB[j] = std::sqrt(S.B.p_up[j]);
+            }
+            b.minc.assign(S.tc.minc.begin(), S.tc.minc.end());
+            b.maxc.assign(S.tc.maxc.begin(), S.tc.maxc.end());
+            b.nmin.assign(n + 1, 0);
+            b.nmax.assign(n + 1, 0);
+            in[k] = lcg_env::PairIn{n, m, b.ca.data(), b.cb.data(), b.sdA.data(), b.suA.data(),
+                                   b.sdB.data(), b.suB.data(), b.minc.data(), b.maxc.data()};
+            res[k] = lcg_env::PairOut{b.nmin.data(), b.nmax.data(), 0};
+        });
+        std::string err;
+        lcg_status rc = lcg_env::compute(eng, ep, (int)gpu_q.size(), in.data(), res.data(), err);
+        if (rc != LCG_OK) {
+            lcg_host::set_error(err);
+            return rc;
+        }
+        std::vector<char> on_gpu(npairs, 0);
+        for (size_t k = 0; k < gpu_q.size(); ++k) on_gpu[gpu_q[k]] = res[k].flag == 0;
+        int fallbacks = 0;
+        for (int q = 0; q < npairs; ++q) fallbacks += !on_gpu[q];
+        if (host_envelopes) *host_envelopes = fallbacks;
+        host_parallel(npairs, [&](int q) {
+            guarded(st[q], [&]() {
+                if (on_gpu[q]) {
+                    apply_envelope_rows(st[q].tc, buf[q].nmin.data(), buf[q].nmax.data());
+                    st[q].P->envelope_ok = 1;
+                } else {
+                    stage_envelope_host(st[q]);
+                }
+            });
+        });
+    }
+    host_parallel(npairs, [&](int q) { guarded(st[q], [&]() { stage_tables(st[q]); }); });
+    for (int q = 0; q < npairs; ++q)
+        if (st[q].code != LCG_OK) {
+            lcg_host::set_error("pair " + std::to_string(q) + ": " + st[q].err);
+            return st[q].code;
+        }
+    for (int q = 0; q < npairs; ++q) out[q] = st[q].P.release();
+    return LCG_OK;
 }
 
 lcg_status lcg_prepared_tables(lcg_prepared p, lcg_pair_tables *t) {

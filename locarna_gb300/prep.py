@@ -53,6 +53,9 @@ def _lib():
         lib.lcg_prepared_grad_spec.argtypes = [C.c_void_p, C.POINTER(lcg_pf_grad_spec)]
         lib.lcg_prepared_grad_spec.restype = C.c_int32
         lib.lcg_prepared_free.restype = C.c_int32
+        lib.lcg_prepare_pairs.argtypes = [C.c_void_p, C.POINTER(C.c_char_p), C.POINTER(C.c_char_p), C.c_int32,
+                                          C.POINTER(lcg_prep_opts), C.POINTER(C.c_void_p), C.POINTER(C.c_int32)]
+        lib.lcg_prepare_pairs.restype = C.c_int32
         _ready = True
     return lib
 
@@ -93,24 +96,53 @@ def prepare_pair(pp_a, pp_b, **kw):
     if rc != 0:
         raise LcgError(rc, lib.lcg_last_error().decode())
     try:
-        t = lcg_pair_tables()
-        lib.lcg_prepared_tables(h, C.byref(t))
-        n, m = t.len_a, t.len_b
-        na, nb, nam = t.num_arcs_a, t.num_arcs_b, t.num_arcmatches
-        pt = PairTables(
-            n, m, _arr(t.sigma, (n + 1) * (m + 1)), _arr(t.gap_a, n + 1), _arr(t.gap_b, m + 1),
-            t.indel_opening, t.exclusion, _arr(t.arcs_a, 2 * na), _arr(t.arcs_b, 2 * nb),
-            _arr(t.am_arcs, 2 * nam), _arr(t.am_score, nam), _arr(t.min_col, n + 1), _arr(t.max_col, n + 1),
-            seq_a=lib.lcg_prepared_sequence(h, 0).decode(), seq_b=lib.lcg_prepared_sequence(h, 1).decode())
-        pt.name_a = lib.lcg_prepared_sequence(h, 2).decode()
-        pt.name_b = lib.lcg_prepared_sequence(h, 3).decode()
-        pt.envelope_ok = bool(lib.lcg_prepared_envelope_ok(h))
-        g = lcg_pf_grad_spec()
-        if lib.lcg_prepared_grad_spec(h, C.byref(g)) == 0:
-            pt.code_a = np.ctypeslib.as_array(g.code_a, shape=(n + 1,)).copy()
-            pt.code_b = np.ctypeslib.as_array(g.code_b, shape=(m + 1,)).copy()
-            pt.am_dsw = (np.ctypeslib.as_array(g.am_dscore_dsw, shape=(nam,)).copy() if nam
-                         else np.zeros(0))
-        return pt
+        return _tables_of(lib, h)
     finally:
         lib.lcg_prepared_free(h)
+
+
+def prepare_pairs(engine, pp_pairs, **kw):
+    """lcg_prepare_pairs: the tables of many pairs [(pp_a, pp_b), ...] with the
+    sequence envelopes computed on the engine's GPU. Returns (tables, number of
+    pairs whose envelope took the host path)."""
+    lib = _lib()
+    o = prep_options(**kw)
+    n = len(pp_pairs)
+    enc_a = [a.encode() for a, _ in pp_pairs]
+    enc_b = [b.encode() for _, b in pp_pairs]
+    arr_a = (C.c_char_p * n)(*enc_a)
+    arr_b = (C.c_char_p * n)(*enc_b)
+    hs = (C.c_void_p * n)()
+    nhost = C.c_int32()
+    rc = lib.lcg_prepare_pairs(engine.h, arr_a, arr_b, n, C.byref(o), hs, C.byref(nhost))
+    if rc != 0:
+        raise LcgError(rc, lib.lcg_last_error().decode())
+    try:
+        return [_tables_of(lib, C.c_void_p(h)) for h in hs], nhost.value
+    finally:
+        for h in hs:
+            if h:
+                lib.lcg_prepared_free(C.c_void_p(h))
+
+
+def _tables_of(lib, h):
+    """PairTables of a prepared handle (copies)."""
+    t = lcg_pair_tables()
+    lib.lcg_prepared_tables(h, C.byref(t))
+    n, m = t.len_a, t.len_b
+    na, nb, nam = t.num_arcs_a, t.num_arcs_b, t.num_arcmatches
+    pt = PairTables(
+        n, m, _arr(t.sigma, (n + 1) * (m + 1)), _arr(t.gap_a, n + 1), _arr(t.gap_b, m + 1),
+        t.indel_opening, t.exclusion, _arr(t.arcs_a, 2 * na), _arr(t.arcs_b, 2 * nb),
+        _arr(t.am_arcs, 2 * nam), _arr(t.am_score, nam), _arr(t.min_col, n + 1), _arr(t.max_col, n + 1),
+        seq_a=lib.lcg_prepared_sequence(h, 0).decode(), seq_b=lib.lcg_prepared_sequence(h, 1).decode())
+    pt.name_a = lib.lcg_prepared_sequence(h, 2).decode()
+    pt.name_b = lib.lcg_prepared_sequence(h, 3).decode()
+    pt.envelope_ok = bool(lib.lcg_prepared_envelope_ok(h))
+    g = lcg_pf_grad_spec()
+    if lib.lcg_prepared_grad_spec(h, C.byref(g)) == 0:
+        pt.code_a = np.ctypeslib.as_array(g.code_a, shape=(n + 1,)).copy()
+        pt.code_b = np.ctypeslib.as_array(g.code_b, shape=(m + 1,)).copy()
+        pt.am_dsw = (np.ctypeslib.as_array(g.am_dscore_dsw, shape=(nam,)).copy() if nam
+                     else np.zeros(0))
+    return pt
