@@ -45,19 +45,49 @@ def log(*a):
     print(*a, file=sys.stderr, flush=True)
 
 
-def build_tables(threads=None):
-    from concurrent.futures import ThreadPoolExecutor
-
-    from locarna_gb300.prep import prepare_pair
+def workload_pp():
+    """PP texts of the all-pairs workload and its pairs (index pairs)."""
     from locarna_gb300.synth import make_family
     fam = make_family(WORKLOAD["count"], WORKLOAD["len_lo"], WORKLOAD["len_hi"], WORKLOAD["seed"],
                       q=WORKLOAD["q"])
     pp = [r.to_pp() for r in fam]
     pairs = [(a, b) for a in range(len(fam)) for b in range(a + 1, len(fam))]
+    return pp, pairs
+
+
+def build_tables(threads=None):
+    """Tables of the workload from the host path (lcg_prepare_pair on every
+    host thread; the envelope in long double as locarna computes it)."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    from locarna_gb300.prep import prepare_pair
+    pp, pairs = workload_pp()
     threads = threads or os.cpu_count() or 4
     with ThreadPoolExecutor(threads) as ex:
         tables = list(ex.map(lambda ab: prepare_pair(pp[ab[0]], pp[ab[1]]), pairs))
     return tables, pairs
+
+
+def table_prep_gpu(eng, host_tables, host_s):
+    """The same tables through lcg_prepare_pairs (envelopes on the GPU),
+    timed once and checked against the host path's tables."""
+    import numpy as np
+
+    from locarna_gb300.prep import prepare_pairs
+    pp, pairs = workload_pp()
+    pp_pairs = [(pp[a], pp[b]) for a, b in pairs]
+    prepare_pairs(eng, pp_pairs[:64])  # first-call set-up outside the timing
+    t0 = time.perf_counter()
+    tables, nhost = prepare_pairs(eng, pp_pairs)
+    gpu_s = time.perf_counter() - t0
+    for k, (t, r) in enumerate(zip(tables, host_tables)):
+        for f in ("min_col", "max_col", "am_arcs", "am_score", "sigma"):
+            if not np.array_equal(getattr(t, f), getattr(r, f)):
+                raise RuntimeError(f"pair {k}: lcg_prepare_pairs {f} differs from lcg_prepare_pair")
+    return {"pairs": len(pairs), "host_s": host_s, "host_threads": os.cpu_count() or 1,
+            "gpu_envelope_s": gpu_s, "host_envelopes": nhost, "speedup": host_s / gpu_s,
+            "what": "PP texts -> lcg_pair_tables (parsing, arcs, scoring, envelope 1e-4, arc matches): "
+                    "lcg_prepare_pair on every host thread vs lcg_prepare_pairs (envelopes on the GPU)"}
 
 
 def build_pf_tables(threads=None):
@@ -278,7 +308,8 @@ def run_ours(args):
         os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
     t0 = time.time()
     tables, pairs = build_tables()
-    log(f"host preparation of {len(tables)} pairs: {time.time() - t0:.1f} s")
+    host_prep_s = time.time() - t0
+    log(f"host preparation of {len(tables)} pairs: {host_prep_s:.1f} s")
     npairs = len(tables)
     # CPU baseline first (forked workers must start before the first GPU call):
     # the oracle restatement of the reference's Aligner on a bounded sample
@@ -297,6 +328,9 @@ def run_ours(args):
                             f"core, {PF_CPU_SECONDS:.0f} s per process; the oracle restatement of AlignerP "
                             f"(inside, outside, arc-match and base-match probabilities)"}
     eng = Engine(0)
+    table_prep = table_prep_gpu(eng, tables, host_prep_s)
+    log(f"table preparation with GPU envelopes: {table_prep['gpu_envelope_s']:.2f} s "
+        f"({table_prep['host_envelopes']} host envelopes)")
     call = eng.prepare_call(tables)
 
     # measurement-only runs (outside the timed region): work counts
@@ -435,6 +469,7 @@ def run_ours(args):
                          "sample": f"{cpu_done} of the {npairs} pairs (seeded permutation), one process "
                                    f"per core, {CPU_SAMPLE_SECONDS:.0f} s per process"},
         "clocks": clocks,
+        "table_prep": table_prep,
     }
     if pf_tables is not None:
         out["locarna_p"] = run_pf(eng, pf_tables, flush_l2, pf_cpu)

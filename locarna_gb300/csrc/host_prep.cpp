@@ -30,7 +30,9 @@
 #include <memory>
 #include <sstream>
 #include <string>
+#include <string_view>
 #include <thread>
+#include <unordered_map>
 #include <vector>
 
 #include "../../include/locarna_gb300.h"
@@ -180,19 +182,22 @@ struct Side {
     int len = 0;
     std::vector<Arc> arcs;        // reference index order
     std::vector<long> weights;    // probToWeight per arc
+    std::vector<double> dsw;      // d weight / d struct_weight per arc, unrounded: 1 - ln p / ln pe
     std::vector<double> p_up, p_down;  // prob_paired_upstream / downstream
+    std::vector<int> left_start;  // len+2: arcs with left end l are [left_start[l+1], left_start[l]) (index order)
 };
 
-// BasePairs::generateBPLists: i from len-3 down to 1, j ascending from i+3
+// BasePairs::generateBPLists: i from len-3 down to 1, j ascending from i+3,
+// keeping p >= min_prob (the sparse matrix in that order)
 void make_arcs(Side &s, double min_prob) {
     s.len = (int)s.in.seq.size();
-    for (int i = s.len - 3; i >= 1; --i) {
-        for (int j = i + 3; j <= s.len; ++j) {
-            auto it = s.in.arc_probs.find({i, j});
-            double p = it == s.in.arc_probs.end() ? 0.0 : it->second;
-            if (p >= min_prob) s.arcs.push_back({i, j, p});
-        }
+    for (auto &kv : s.in.arc_probs) {
+        const int i = kv.first.first, j = kv.first.second;
+        if (i >= 1 && i <= s.len - 3 && j >= i + 3 && j <= s.len && kv.second >= min_prob)
+            s.arcs.push_back({i, j, kv.second});
     }
+    std::stable_sort(s.arcs.begin(), s.arcs.end(),
+                     [](const Arc &x, const Arc &y) { return x.l != y.l ? x.l > y.l : x.r < y.r; });
     // RnaData::prob_paired_upstream / downstream (rna_data.cc:713-732):
     // ascending sums over the sparse probability matrix
     s.p_up.assign(s.len + 1, 0.0);
@@ -494,30 +499,50 @@ namespace {
 // the envelope, then the tables.
 struct Staged {
     lcg_prep_opts o;
-    Side A, B;
+    std::shared_ptr<const Side> pa, pb;  // shared by the pairs of a batch that use the same input
     Band tc;
     std::unique_ptr<lcg_prepared_s> P;
     lcg_status code = LCG_OK;
     std::string err;
 };
 
-// PP reading, arcs, the max-diff band (locarna.cc:398-560)
-void stage_inputs(const char *pp_a, const char *pp_b, Staged &S) {
+// One input: PP reading, arcs (basepairs.cc:155-205), pairing probabilities,
+// arc weights Scoring::probToWeight (scoring.cc:250-265) with
+// pe = prob_exp_f(len) (aux.hh:216-220), and the arcs by left end.
+std::shared_ptr<const Side> make_side(const char *pp, const lcg_prep_opts &o) {
+    auto s = std::make_shared<Side>();
+    s->in = read_pp(pp, o.min_prob);
+    make_arcs(*s, o.min_prob);
+    const double pe = o.exp_prob > 0 ? o.exp_prob : 1.0 / (2.0 * s->len);
+    for (auto &a : s->arcs) {
+        s->weights.push_back(prob_to_weight(a.p, pe, o.struct_weight));
+        s->dsw.push_back(1 - log(a.p) / log(pe));
+    }
+    // arcs are ordered by left end descending: [left_start[l+1], left_start[l])
+    s->left_start.assign(s->len + 2, 0);
+    size_t k = s->arcs.size();
+    for (int l = 0; l <= s->len + 1; ++l) {
+        while (k > 0 && s->arcs[k - 1].l < l) --k;
+        s->left_start[l] = (int)k;
+    }
+    return s;
+}
+
+// the pair's record and the max-diff band (locarna.cc:398-560)
+void stage_inputs(std::shared_ptr<const Side> A, std::shared_ptr<const Side> B, Staged &S) {
     const lcg_prep_opts &o = S.o;
     S.P = std::make_unique<lcg_prepared_s>();
-    Side &A = S.A, &B = S.B;
-    A.in = read_pp(pp_a, o.min_prob);
-    B.in = read_pp(pp_b, o.min_prob);
-    make_arcs(A, o.min_prob);
-    make_arcs(B, o.min_prob);
-    const int n = A.len, m = B.len;
+    S.pa = std::move(A);
+    S.pb = std::move(B);
+    const Side &sa = *S.pa, &sb = *S.pb;
+    const int n = sa.len, m = sb.len;
     lcg_prepared_s *P = S.P.get();
     P->n = n;
     P->m = m;
-    P->seq_a = A.in.seq;
-    P->seq_b = B.in.seq;
-    P->name_a = A.in.name;
-    P->name_b = B.in.name;
+    P->seq_a = sa.in.seq;
+    P->seq_b = sb.in.seq;
+    P->name_a = sa.in.name;
+    P->name_b = sb.in.name;
     // trace controller (no reference alignment, no anchors)
     S.tc.minc.assign(n + 1, 0);
     S.tc.maxc.assign(n + 1, m);
@@ -527,15 +552,15 @@ void stage_inputs(const char *pp_a, const char *pp_b, Staged &S) {
 // the envelope in the reference's precision (edge_probs.icc, trace_controller.cc:565-597)
 void stage_envelope_host(Staged &S) {
     bool ok;
-    if (S.o.pf_precision == 0) ok = restrict_by_envelope<double>(S.tc, S.A, S.B, S.o);
-    else ok = restrict_by_envelope<long double>(S.tc, S.A, S.B, S.o);
+    if (S.o.pf_precision == 0) ok = restrict_by_envelope<double>(S.tc, *S.pa, *S.pb, S.o);
+    else ok = restrict_by_envelope<long double>(S.tc, *S.pa, *S.pb, S.o);
     S.P->envelope_ok = ok ? 1 : 0;
 }
 
 // scoring tables and arc matches on the final band (locarna.cc:560-703)
 void stage_tables(Staged &S) {
     const lcg_prep_opts &o = S.o;
-    Side &A = S.A, &B = S.B;
+    const Side &A = *S.pa, &B = *S.pb;
     const Band &tc = S.tc;
     lcg_prepared_s *P = S.P.get();
     const int n = A.len, m = B.len;
@@ -568,12 +593,11 @@ void stage_tables(Staged &S) {
     }
     P->indel_opening = o.indel_opening;
     P->exclusion = o.exclusion;
-    double peA = o.exp_prob > 0 ? o.exp_prob : 1.0 / (2.0 * n);
-    double peB = o.exp_prob > 0 ? o.exp_prob : 1.0 / (2.0 * m);
-    for (auto &a : A.arcs) A.weights.push_back(prob_to_weight(a.p, peA, o.struct_weight));
-    for (auto &b : B.arcs) B.weights.push_back(prob_to_weight(b.p, peB, o.struct_weight));
 
-    // arc matches (arc_matches.cc:130-188), A index outer, B index inner
+    // arc matches (arc_matches.cc:130-188), A index outer, B index inner;
+    // for arc a only the B arcs whose left end b.l passes
+    // is_valid_match(a.l, b.l) are visited (by left end descending = B index
+    // ascending)
     const size_t mdam = o.max_diff_am != -1 ? (size_t)o.max_diff_am : (size_t)std::max(n, m);
     const size_t mdaam = o.max_diff_at_am != -1 ? (size_t)o.max_diff_at_am : (size_t)std::max(n, m);
     auto valid = [&](long i, long j) { return i >= 0 && i <= n && tc.minc[i] <= j && j <= tc.maxc[i]; };
@@ -583,7 +607,11 @@ void stage_tables(Staged &S) {
     std::memset(ribo_have, 0, sizeof ribo_have);
     for (size_t ia = 0; ia < A.arcs.size(); ++ia) {
         const Arc &a = A.arcs[ia];
-        for (size_t ib = 0; ib < B.arcs.size(); ++ib) {
+        const long llo = std::max({tc.minc[a.l], tc.minc[a.l - 1] + 1, 1L});
+        const long lhi = std::min({tc.maxc[a.l], tc.maxc[a.l - 1] + 1, (long)m});
+        const size_t ib0 = lhi >= llo ? (size_t)B.left_start[lhi + 1] : 0;
+        const size_t ib1 = lhi >= llo ? (size_t)B.left_start[llo] : 0;
+        for (size_t ib = ib0; ib < ib1; ++ib) {
             const Arc &b = B.arcs[ib];
             bool ok = valid_match(a.l, b.l) && valid_match(a.r, b.r) &&
                       (size_t)std::abs((a.r - a.l) - (b.r - b.l)) <= mdam &&
@@ -613,7 +641,7 @@ void stage_tables(Staged &S) {
             P->am_arcs.push_back((int32_t)ia);
             P->am_arcs.push_back((int32_t)ib);
             P->am_score.push_back((int32_t)s);
-            P->am_dsw.push_back((1 - log(a.p) / log(peA)) + (1 - log(b.p) / log(peB)));
+            P->am_dsw.push_back(A.dsw[ia] + B.dsw[ib]);
         }
     }
     for (auto &a : A.arcs) {
@@ -651,7 +679,7 @@ lcg_status lcg_prepare_pair(const char *pp_a, const char *pp_b, const lcg_prep_o
     if (opts) S.o = *opts;
     else lcg_prep_opts_default(&S.o);
     try {
-        stage_inputs(pp_a, pp_b, S);
+        stage_inputs(make_side(pp_a, S.o), make_side(pp_b, S.o), S);
         if (S.o.min_trace_probability > 0.0) stage_envelope_host(S);
         stage_tables(S);
         *out = S.P.release();
@@ -712,12 +740,34 @@ lcg_status lcg_prepare_pairs(lcg_engine eng, const char *const *pp_a, const char
     else lcg_prep_opts_default(&o);
     std::vector<Staged> st(npairs);
     for (auto &S : st) S.o = o;
-    host_parallel(npairs, [&](int q) {
-        guarded(st[q], [&]() {
-            if (!pp_a[q] || !pp_b[q]) throw PrepError{LCG_ERR_ARG, "NULL PP text"};
-            stage_inputs(pp_a[q], pp_b[q], st[q]);
-        });
-    });
+    for (int q = 0; q < npairs; ++q)
+        if (!pp_a[q] || !pp_b[q]) {
+            lcg_host::set_error("pair " + std::to_string(q) + ": NULL PP text");
+            return LCG_ERR_ARG;
+        }
+    // every distinct input is read once (all-pairs batches repeat each input)
+    std::unordered_map<std::string_view, int> text_id;
+    std::vector<const char *> texts;
+    std::vector<int> ida(npairs), idb(npairs);
+    for (int q = 0; q < npairs; ++q)
+        for (int w = 0; w < 2; ++w) {
+            const char *t = w ? pp_b[q] : pp_a[q];
+            auto it = text_id.emplace(std::string_view(t), (int)texts.size());
+            if (it.second) texts.push_back(t);
+            (w ? idb : ida)[q] = it.first->second;
+        }
+    std::vector<std::shared_ptr<const Side>> sides(texts.size());
+    std::vector<Staged> side_err(texts.size());
+    host_parallel((int)texts.size(), [&](int k) { guarded(side_err[k], [&]() { sides[k] = make_side(texts[k], o); }); });
+    for (int q = 0; q < npairs; ++q) {
+        const Staged &ea = side_err[ida[q]], &eb = side_err[idb[q]];
+        if (ea.code != LCG_OK || eb.code != LCG_OK) {
+            const Staged &e = ea.code != LCG_OK ? ea : eb;
+            lcg_host::set_error("pair " + std::to_string(q) + ": " + e.err);
+            return e.code;
+        }
+    }
+    host_parallel(npairs, [&](int q) { guarded(st[q], [&]() { stage_inputs(sides[ida[q]], sides[idb[q]], st[q]); }); });
     for (int q = 0; q < npairs; ++q)
         if (st[q].code != LCG_OK) {
             lcg_host::set_error("pair " + std::to_string(q) + ": " + st[q].err);
@@ -752,14 +802,15 @@ lcg_status lcg_prepare_pairs(lcg_engine eng, const char *const *pp_a, const char
         std::vector<lcg_env::PairOut> res;
         std::vector<int> gpu_q;
         for (int q = 0; q < npairs; ++q)
-            if (st[q].A.len + st[q].B.len <= max_len_sum) gpu_q.push_back(q);
+            if (st[q].pa->len + st[q].pb->len <= max_len_sum) gpu_q.push_back(q);
         in.resize(gpu_q.size());
         res.resize(gpu_q.size());
         host_parallel((int)gpu_q.size(), [&](int k) {
             const int q = gpu_q[k];
+            const Side &SA = *st[q].pa, &SB = *st[q].pb;
             const Staged &S = st[q];
             Buf &b = buf[q];
-            const int n = S.A.len, m = S.B.len;
+            const int n = SA.len, m = SB.len;
             b.ca.assign(n + 1, -1);
             b.cb.assign(m + 1, -1);
             b.sdA.assign(n + 1, 0.0);
@@ -767,14 +818,14 @@ lcg_status lcg_prepare_pairs(lcg_engine eng, const char *const *pp_a, const char
             b.sdB.assign(m + 1, 0.0);
             b.suB.assign(m + 1, 0.0);
             for (int i = 1; i <= n; ++i) {
-                b.ca[i] = (int8_t)idx_acgu(S.A.in.seq[i - 1]);
-                b.sdA[i] = std::sqrt(S.A.p_down[i]);
-                b.suA[i] = std::sqrt(S.A.p_up[i]);
+                b.ca[i] = (int8_t)idx_acgu(SA.in.seq[i - 1]);
+                b.sdA[i] = std::sqrt(SA.p_down[i]);
+                b.suA[i] = std::sqrt(SA.p_up[i]);
             }
             for (int j = 1; j <= m; ++j) {
-                b.cb[j] = (int8_t)idx_acgu(S.B.in.seq[j - 1]);
-                b.sdB[j] = std::sqrt(S.B.p_down[j]);
-                b.suB[j] = std::sqrt(S.B.p_up[j]);
+                b.cb[j] = (int8_t)idx_acgu(SB.in.seq[j - 1]);
+                b.sdB[j] = std::sqrt(SB.p_down[j]);
+                b.suB[j] = std::sqrt(SB.p_up[j]);
             }
             b.minc.assign(S.tc.minc.begin(), S.tc.minc.end());
             b.maxc.assign(S.tc.maxc.begin(), S.tc.maxc.end());
