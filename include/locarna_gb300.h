@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define LCG_ABI_VERSION 1
+#define LCG_ABI_VERSION 2
 
 typedef int32_t lcg_status;
 #define LCG_OK 0
@@ -100,6 +100,13 @@ typedef struct lcg_align_opts {
     int32_t sequ_local;    /* AlignerParams::sequ_local */
     int32_t free_endgaps;  /* LCG_FREE_* bits */
     int32_t do_trace;      /* run Aligner::trace() after align() */
+    /* AlignerParams::no_lonely_pairs (locarna --noLP): every arc match must
+     * enclose an inner arc match (left ends +1, right ends -1); D is filled
+     * by fill_D_entries_noLP (aligner.cc:612-657), groups are chosen by
+     * get_max_right_ends(.., true) (arc_matches.cc:313-355) and the
+     * traceback follows trace_arcmatch_noLP (aligner.cc:1030-1079). No
+     * stacking terms. */
+    int32_t no_lonely_pairs;
 } lcg_align_opts;
 
 /*

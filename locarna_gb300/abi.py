@@ -34,7 +34,8 @@ class lcg_pair_tables(C.Structure):
 
 class lcg_align_opts(C.Structure):
     _fields_ = [("struct_local", C.c_int32), ("sequ_local", C.c_int32),
-                ("free_endgaps", C.c_int32), ("do_trace", C.c_int32)]
+                ("free_endgaps", C.c_int32), ("do_trace", C.c_int32),
+                ("no_lonely_pairs", C.c_int32)]
 
 
 class lcg_align_result(C.Structure):
@@ -179,7 +180,8 @@ class ResultBuffers:
                            [tuple(map(int, x)) for x in e], [int(x) for x in self.tam[:nt]])
 
 
-def make_opts(struct_local=False, sequ_local=False, free_endgaps="----", do_trace=True):
+def make_opts(struct_local=False, sequ_local=False, free_endgaps="----", do_trace=True,
+              no_lonely_pairs=False):
     fe = 0
     if isinstance(free_endgaps, str):
         for k, ch in enumerate(free_endgaps[:4]):
@@ -187,4 +189,5 @@ def make_opts(struct_local=False, sequ_local=False, free_endgaps="----", do_trac
                 fe |= 1 << k
     else:
         fe = int(free_endgaps)
-    return lcg_align_opts(int(bool(struct_local)), int(bool(sequ_local)), fe, int(bool(do_trace)))
+    return lcg_align_opts(int(bool(struct_local)), int(bool(sequ_local)), fe, int(bool(do_trace)),
+                          int(bool(no_lonely_pairs)))

@@ -75,8 +75,9 @@ lcg_status prep_pair(const lcg_pair_tables &t, const lcg_align_opts &o, Prep &p)
     p.n = n;
     p.m = m;
     p.fe = o.free_endgaps & 15;
+    const bool nolp = o.no_lonely_pairs != 0;
     p.flags = (o.sequ_local ? PF_SEQU_LOCAL : 0) | (anchors ? PF_ANCHORS : 0) |
-              (o.do_trace ? PF_TRACE : 0) | (o.struct_local ? PF_STRUCT_LOCAL : 0);
+              (o.do_trace ? PF_TRACE : 0) | (o.struct_local ? PF_STRUCT_LOCAL : 0) | (nolp ? PF_NOLP : 0);
     if (o.sequ_local && p.fe) return bad(LCG_ERR_ARG, "free end gaps cannot be combined with local alignment");
 
     // band: monotone, inside [0,m], rows non-empty and connected
@@ -180,13 +181,16 @@ lcg_status prep_pair(const lcg_pair_tables &t, const lcg_align_opts &o, Prep &p)
                       (long long)(std::min(n, m) / 2 + 1) * mam;
     if (bound >= (1ll << 27)) return bad(LCG_ERR_RANGE, "scores may exceed the int32 device range");
 
+    // arcs span at least 3 positions, as BasePairs makes them
+    // (basepairs.cc:162-163: j from i+3), so every corner cell (ar-1,br-1)
+    // lies below its group's first row
     for (int k = 0; k < t.num_arcs_a; ++k) {
         int l = t.arcs_a[2 * k], r = t.arcs_a[2 * k + 1];
-        if (l < 1 || r > n || l >= r) return bad(LCG_ERR_ARG, "arc of A out of range");
+        if (l < 1 || r > n || r - l < 3) return bad(LCG_ERR_ARG, "arc of A out of range (1 <= l, l+3 <= r <= len)");
     }
     for (int k = 0; k < t.num_arcs_b; ++k) {
         int l = t.arcs_b[2 * k], r = t.arcs_b[2 * k + 1];
-        if (l < 1 || r > m || l >= r) return bad(LCG_ERR_ARG, "arc of B out of range");
+        if (l < 1 || r > m || r - l < 3) return bad(LCG_ERR_ARG, "arc of B out of range (1 <= l, l+3 <= r <= len)");
     }
     const int na = t.num_arcmatches;
     p.am_ends.resize(4 * (size_t)na);
@@ -295,6 +299,30 @@ lcg_status prep_pair(const lcg_pair_tables &t, const lcg_align_opts &o, Prep &p)
             byleft[cnta[n - p.am_ends[4 * k]]++] = {(long long)p.am_ends[4 * k] * (m + 1) + p.am_ends[4 * k + 2], k};
         }
     }
+    // no lonely pairs: the inner arc match of each arc match, the first one in
+    // index order with left ends (a.l+1,b.l+1) and right ends (a.r-1,b.r-1)
+    // (ArcMatches::init_inner_arc_matchs, arc_matches.cc:50-74); byleft
+    // holds each left-end bucket in index order
+    std::vector<int> inner;
+    if (nolp) {
+        inner.assign(na, -1);
+        p.inner.assign(std::max(na, 1), make_int2(-1, -1));
+        for (int k = 0; k < na; ++k) {
+            const int *ek = &p.am_ends[4 * k];
+            if (ek[0] + 1 > n || ek[2] + 1 > m) continue;
+            const long long key = (long long)(ek[0] + 1) * (m + 1) + (ek[2] + 1);
+            auto it = std::lower_bound(byleft.begin(), byleft.end(), key,
+                                       [](const std::pair<long long, int> &x, long long v) { return x.first > v; });
+            for (; it != byleft.end() && it->first == key; ++it) {
+                const int x = it->second;
+                if (p.am_ends[4 * x + 1] == ek[1] - 1 && p.am_ends[4 * x + 3] == ek[3] - 1) {
+                    inner[k] = x;
+                    p.inner[k] = make_int2(x, p.am_pos[x]);
+                    break;
+                }
+            }
+        }
+    }
     p.Dinit.assign(p.num_pos, NEG);
     std::vector<int> ks;
     // band cells of rows [r0, r1) inside columns [A, B], in O(log n) from
@@ -323,13 +351,24 @@ lcg_status prep_pair(const lcg_pair_tables &t, const lcg_align_opts &o, Prep &p)
         size_t e = s;
         while (e < byleft.size() && byleft[e].first == byleft[s].first) ++e;
         int k0 = byleft[s].second;
-        int al = p.am_ends[4 * k0], bl = p.am_ends[4 * k0 + 2];
-        if (allowed_match(t, al, bl) && in_band(al, bl) && in_band(al - 1, bl - 1)) {
+        // the group's left ends: those of the bucket's arc matches, or, without
+        // lonely pairs, one inside them (align_D, aligner.cc:660-732, with
+        // get_max_right_ends(.., no_lonely_pairs), arc_matches.cc:313-355:
+        // the bucket's arc matches that enclose an inner arc match, right
+        // ends minus one)
+        const int sh = nolp ? 1 : 0;
+        int al = p.am_ends[4 * k0] + sh, bl = p.am_ends[4 * k0 + 2] + sh;
+        if (al <= n && bl <= m && allowed_match(t, al, bl) && in_band(al, bl) && in_band(al - 1, bl - 1)) {
             int max_ar = al, max_br = bl;
             for (size_t q = s; q < e; ++q) {
                 int k = byleft[q].second;
-                max_ar = std::max(max_ar, p.am_ends[4 * k + 1]);
-                max_br = std::max(max_br, p.am_ends[4 * k + 3]);
+                if (nolp && inner[k] < 0) continue;
+                max_ar = std::max(max_ar, p.am_ends[4 * k + 1] - sh);
+                max_br = std::max(max_br, p.am_ends[4 * k + 3] - sh);
+            }
+            if (max_ar == al || max_br == bl) {
+                s = e;
+                continue;
             }
             GroupItem g{};
             g.al = al;
@@ -343,11 +382,20 @@ lcg_status prep_pair(const lcg_pair_tables &t, const lcg_align_opts &o, Prep &p)
             auto ar_less = [&](int x, int y) { return p.am_ends[4 * x + 1] < p.am_ends[4 * y + 1]; };
             if (!std::is_sorted(ks.begin(), ks.end(), ar_less)) std::stable_sort(ks.begin(), ks.end(), ar_less);
             for (int k : ks) {
-                int ar = p.am_ends[4 * k + 1], br = p.am_ends[4 * k + 3];
-                // the inner corner (ar-1,br-1) is computed by this group iff it is in the band
+                if (nolp && inner[k] < 0) continue;
+                // the corner: (ar-1,br-1) inside the arc match, or, without
+                // lonely pairs, inside its inner arc match
+                int ar = p.am_ends[4 * k + 1] - sh, br = p.am_ends[4 * k + 3] - sh;
+                // the corner is computed by this group iff it is in the band
                 // (only arc matches whose right ends are a band cell are ever read)
                 if (ar - 1 > al && br - 1 > bl && in_band(ar - 1, br - 1) && p.am_pos[k] >= 0) {
-                    p.dw.push_back(make_int4(p.am_pos[k], ar - 1, br - 1, t.am_score[k]));
+                    if (nolp) {
+                        const int in = inner[k];
+                        p.dw.push_back(make_int4(p.am_pos[k], ar - 1, br - 1, t.am_score[k] + t.am_score[in]));
+                        p.dwn.push_back(make_int2(p.am_pos[in], t.am_score[k]));
+                    } else {
+                        p.dw.push_back(make_int4(p.am_pos[k], ar - 1, br - 1, t.am_score[k]));
+                    }
                     p.Dinit[p.am_pos[k]] = NOT_READY;
                 }
             }
@@ -449,7 +497,7 @@ Slot slot_of(lcg_engine e, int k) {
 // byte offsets of one pair's tables in the arena
 struct PairOff {
     size_t sigma, scls, rcls, ccls, gapA, gapB, minc, maxc, bandoff, rowinfo, anc, cre_start, cre, crow, rowarc,
-        am_score, D, topM, res, tok, tq, segs, groups, dw, gbc;
+        am_score, D, topM, res, tok, tq, segs, groups, dw, gbc, dwn, inner;
 };
 
 // One chunk of an lcg_align_pairs call: pairs [q0, q0 + nq) of the batch.
@@ -511,6 +559,8 @@ lcg_status chunk_launch(lcg_engine e, const Slot &s, const lcg_pair_tables *all,
         o.gbc = take(up, 4ull * (p.m + 1));
         o.groups = take(up, sizeof(GroupItem) * p.groups.size());
         o.dw = take(up, sizeof(int4) * std::max<size_t>(p.dw.size(), 1));
+        o.dwn = p.inner.empty() ? 0 : take(up, sizeof(int2) * std::max<size_t>(p.dwn.size(), 1));
+        o.inner = p.inner.empty() ? 0 : take(up, sizeof(int2) * p.inner.size());
         // sigma: the class table when it exists, else the dense table
         o.sigma = p.use_cls ? 0 : take(up, 4ull * (p.n + 1) * (p.m + 1));
         o.scls = p.use_cls ? take(up, 4ull * 256) : 0;
@@ -625,6 +675,8 @@ lcg_status chunk_launch(lcg_engine e, const Slot &s, const lcg_pair_tables *all,
             hg[g].pair = q;
         }
         if (!p.dw.empty()) std::memcpy(H + o.dw, p.dw.data(), sizeof(int4) * p.dw.size());
+        if (!p.dwn.empty()) std::memcpy(H + o.dwn, p.dwn.data(), sizeof(int2) * p.dwn.size());
+        if (!p.inner.empty()) std::memcpy(H + o.inner, p.inner.data(), sizeof(int2) * p.inner.size());
         PairDev &d = hp[q];
         std::memset(&d, 0, sizeof d);
         d.n = p.n;
@@ -678,6 +730,8 @@ lcg_status chunk_launch(lcg_engine e, const Slot &s, const lcg_pair_tables *all,
         d.gbc = (const int *)(Dv + o.gbc);
         d.groups = (const GroupItem *)(Dv + o.groups);
         d.dw = (const int4 *)(Dv + o.dw);
+        d.dwn = p.inner.empty() ? nullptr : (const int2 *)(Dv + o.dwn);
+        d.inner = p.inner.empty() ? nullptr : (const int2 *)(Dv + o.inner);
     });
     *pack_ms += ms_between(tp0, std::chrono::steady_clock::now());
 

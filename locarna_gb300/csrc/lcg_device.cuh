@@ -30,6 +30,7 @@ enum PairFlags : int {
     PF_ANCHORS = 4,
     PF_TRACE = 8,
     PF_SCLS = 16,  // sigma(i,j) = scls[rcls[i] * 16 + ccls[j]] (at most 16 row / column classes)
+    PF_NOLP = 32,  // no lonely pairs (AlignerParams::no_lonely_pairs)
 };
 
 // status word bits (device -> host)
@@ -81,6 +82,14 @@ struct PairDev {
     int4 *segs;           // traceback segments: (am or -1, token start, token end, 0)
     const GroupItem *groups;  // the pair's left-end groups (work items) in dependency order
     const int4 *dw;           // the pair's D writes; GroupItem::dw_start indexes it
+    // PF_NOLP only (else nullptr): per D write, (D index of the inner arc
+    // match or -1, score of the outer arc match), parallel to dw; the write is
+    // D = max(M(corner) + dw.w, D(inner) + score) (fill_D_entries_noLP,
+    // aligner.cc:612-657) with dw.w = score(outer) + score(inner)
+    const int2 *dwn;
+    // PF_NOLP only: per arc match, (inner arc match or -1, its D index or -1)
+    // (ArcMatches::inner_arc_match, arc_matches.hh:466-476)
+    const int2 *inner;
 };
 
 // Scoring::basematch(i,j) from the class table or the dense table
@@ -95,7 +104,7 @@ enum Res : int {
 struct GroupItem {
     int pair;
     int al, ar, bl, br;
-    int dw_start, dw_count;  // D writes: int4 (am, ar-1, br-1, score), ar ascending
+    int dw_start, dw_count;  // D writes: int4 (D index, corner row, corner column, score), rows ascending
     int top;                 // 1 for the top-level item
     int cpl;                 // columns per lane: ceil(widest band row of the group / 32), <= 4
 };

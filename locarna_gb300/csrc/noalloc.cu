@@ -109,6 +109,7 @@ extern "C" lcg_status lcg_align_score_static(const lcg_pair_tables *pair, const 
     const size_t o_pair = take(sizeof(PairDev));
     const size_t o_items = take(sizeof(GroupItem) * p.groups.size());
     const size_t o_dw = take(sizeof(int4) * std::max<size_t>(p.dw.size(), 1));
+    const size_t o_dwn = take(sizeof(int2) * std::max<size_t>(p.dwn.size(), 1));  // no lonely pairs
     const size_t o_queue = take(sizeof(int2) * p.groups.size());
     const size_t o_gbc = take(4ull * (m + 1));
     const size_t o_ctrl = take(64);
@@ -198,6 +199,7 @@ extern "C" lcg_status lcg_align_score_static(const lcg_pair_tables *pair, const 
     for (auto &g : p.groups) g.pair = 0;
     d.groups = (const GroupItem *)(base + o_items);
     d.dw = (const int4 *)(base + o_dw);
+    d.dwn = (p.flags & PF_NOLP) ? (const int2 *)(base + o_dwn) : nullptr;
     d.gbc = (const int *)(base + o_gbc);
     std::vector<int2> queue(p.groups.size());  // one pair: the groups in their own order
     for (size_t g = 0; g < queue.size(); ++g) queue[g] = make_int2(0, (int)g);
@@ -209,6 +211,7 @@ extern "C" lcg_status lcg_align_score_static(const lcg_pair_tables *pair, const 
     STATIC_TRY(h2d(o_pair, &d, sizeof d));
     STATIC_TRY(h2d(o_items, p.groups.data(), sizeof(GroupItem) * p.groups.size()));
     STATIC_TRY(h2d(o_dw, p.dw.data(), sizeof(int4) * p.dw.size()));
+    STATIC_TRY(h2d(o_dwn, p.dwn.data(), sizeof(int2) * p.dwn.size()));
     STATIC_TRY(h2d(o_queue, queue.data(), sizeof(int2) * queue.size()));
     STATIC_TRY(h2d(o_gbc, p.gbc.data(), 4ull * (m + 1)));
     STATIC_TRY(cudaMemsetAsync(base + o_ctrl, 0, 64, s));

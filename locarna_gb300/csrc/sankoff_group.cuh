@@ -61,6 +61,15 @@ __device__ __forceinline__ int wait_D(int *D, int k, int *status, volatile int *
     return v;
 }
 
+// No lonely pairs: D(inner) + score(outer) for the D write *e of a group
+// (PairDev::dwn, parallel to PairDev::dw); kept out of line, it is rare.
+template <bool WAIT>
+__device__ __noinline__ int inner_term(const PairDev &P, const int4 *e, int *status, volatile int *abort_flag) {
+    const int2 x = P.dwn[e - P.dw];
+    const int din = x.x < 0 ? NEG : (WAIT ? wait_D(P.D, x.x, status, abort_flag) : P.D[x.x]);
+    return din + x.y;
+}
+
 // One left-end group (or the top level) in state E_NO_NO:
 // init_state (aligner.cc:264-368) + the row sweep of align_in_arcmatch
 // (aligner.cc:424-437) with align_noex per cell. M of the rectangle is
@@ -344,13 +353,19 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
         }
         __syncwarp();
         if (DWRITE && i == dw_row) {
-            // fill_D_entries for arc matches whose inner corner is in row i
+            // fill_D_entries for arc matches whose inner corner is in row i;
+            // without lonely pairs (P.dwn set) fill_D_entries_noLP: the
+            // better of the corner and the inner arc match's own D
             while (dwp < ndw) {
                 const int q = dwp + lane;
                 int4 e = make_int4(0, -1, 0, 0);
                 if (q < ndw) e = dw[q];
                 const bool mine = q < ndw && e.y == i;
-                if (mine) st_volatile(Dp + e.x, norm(CUR(e.z) + e.w));
+                if (mine) {
+                    int v = CUR(e.z) + e.w;
+                    if (P.flags & PF_NOLP) v = max(v, inner_term<WAIT>(P, dw + q, status, abort_flag));
+                    st_volatile(Dp + e.x, norm(v));
+                }
                 const int cnt = __popc(__ballot_sync(0xffffffffu, mine));
                 dwp += cnt;
                 if (cnt < 32) break;
@@ -556,6 +571,52 @@ struct Walker {
     }
 };
 
+// Traceback queue entries: (am, aux, a.l | b.l << 16 | mode, a.r | b.r << 16).
+// Mode TQ_CHAIN (no lonely pairs): trace_arcmatch_noLP of am, aux = its D
+// index. Otherwise the interior of am is recomputed and walked; aux = its D
+// index, or, for the inner arc match of a no-lonely-pairs stack, the value
+// its interior's corner must have (D(outer) - score(outer) - score(am)).
+constexpr int TQ_CHAIN = INT32_MIN;
+__device__ __forceinline__ int4 trace_entry(const PairDev &P, int am, int dpos, int al, int ar, int bl, int br) {
+    return make_int4(am, dpos, al | (bl << 16) | ((P.flags & PF_NOLP) ? TQ_CHAIN : 0), ar | (br << 16));
+}
+// (a.l, a.r, b.l, b.r) of a queue entry
+__device__ __forceinline__ int4 trace_ends(int lefts, int rights) {
+    return make_int4(lefts & 0xffff, rights & 0xffff, (lefts >> 16) & 0x7fff, rights >> 16);
+}
+
+// trace_arcmatch_noLP (aligner.cc:1030-1079) for arc match k (D index kpos):
+// the inner arc match's two edges and its arc-match token form k's segment;
+// the inner arc match is queued to continue the stack (TQ_CHAIN) when
+// D(k) == D(inner) + score(k), else to have its interior recomputed and
+// walked (aligner.cc:1057-1075).
+static __device__ __noinline__ void trace_chain(Walker &w, int k, int kpos, int4 ends, int &nseg,
+                                                int *status) {
+    const PairDev &P = w.P;
+    const int2 in = P.inner[k];
+    const int start = w.ntok;
+    if (in.x < 0) {
+        atomicOr(status, ST_INTERNAL);
+    } else {
+        const int ial = ends.x + 1, iar = ends.y - 1, ibl = ends.z + 1, ibr = ends.w - 1;
+        w.emit(iar, ibr);
+        w.emit(-2, in.x);
+        w.emit(ial, ibl);
+        const int dk = P.D[kpos], sk = P.am_score[k];
+        const int din = in.y >= 0 ? P.D[in.y] : NEG;
+        int4 e;
+        if (in.y >= 0 && dk == din + sk)
+            e = make_int4(in.x, in.y, ial | (ibl << 16) | TQ_CHAIN, iar | (ibr << 16));
+        else
+            e = make_int4(in.x, dk - sk - P.am_score[in.x], ial | (ibl << 16), iar | (ibr << 16));
+        if (w.qtail < P.tq_cap) P.tq[w.qtail] = e;
+        else w.ok = false;
+        ++w.qtail;
+    }
+    if (nseg < P.tq_cap + 1) P.segs[nseg] = make_int4(k, start, w.ntok, 0);
+    ++nseg;
+}
+
 // Walk back from (i,j) inside the rectangle with origin (al,bl) whose M is
 // Mg (pitch), emitting tokens in reverse append order. Arc-match tokens are
 // (-2, am); each traced arc match is queued for its own walk.
@@ -638,7 +699,7 @@ static __device__ __noinline__ void walk(Walker &w, const int *Mg, int pitch, in
                 w.emit(i, j);
                 w.emit(-2, ent.w);
                 w.emit(alq, blq);
-                if (w.qtail < P.tq_cap) P.tq[w.qtail] = make_int4(ent.w, ent.x, alq | (blq << 16), i | (j << 16));
+                if (w.qtail < P.tq_cap) P.tq[w.qtail] = trace_entry(P, ent.w, ent.x, alq, i, blq, j);
                 else w.ok = false;
                 ++w.qtail;
                 i = alq - 1;

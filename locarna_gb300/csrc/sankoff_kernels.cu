@@ -91,11 +91,17 @@ __global__ void __launch_bounds__(TRACE_WARPS * 32)
     while (qhead < qtail) {
         int4 qe = make_int4(-1, 0, 0, 0);
         if (lane == 0 && qhead < P.tq_cap) qe = P.tq[qhead];
-        const int k = __shfl_sync(0xffffffffu, qe.x, 0);
+        const int k = __shfl_sync(0xffffffffu, qe.x, 0), kaux = __shfl_sync(0xffffffffu, qe.y, 0);
         const int lefts = __shfl_sync(0xffffffffu, qe.z, 0), rights = __shfl_sync(0xffffffffu, qe.w, 0);
         ++qhead;
         if (k < 0) break;
-        const int4 ends = make_int4(lefts & 0xffff, rights & 0xffff, lefts >> 16, rights >> 16);  // a.l, a.r, b.l, b.r
+        const int4 ends = trace_ends(lefts, rights);  // a.l, a.r, b.l, b.r
+        if (lefts & TQ_CHAIN) {
+            if (lane == 0) trace_chain(w, k, kaux, ends, nseg, status);
+            __syncwarp();
+            qtail = __shfl_sync(0xffffffffu, w.qtail, 0);
+            continue;
+        }
         const int cpl = min(4, max(1, (min(ends.w - ends.z, P.maxband) + 31) / 32));
         run_group<false, false, false>(P, cpl, ends.x, ends.y, ends.z, ends.w, Mg, sw, sbase, rb, nullptr, 0,
                                        true, true, false, status, (volatile int *)&dummy_abort, nullptr);

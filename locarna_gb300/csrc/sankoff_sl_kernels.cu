@@ -267,6 +267,8 @@ __device__ void run_group_sl(const PairDev &P, int al, int ar, int bl, int br, i
         }
         __syncwarp();
         if (DWRITE) {
+            // fill_D_entries (struct-local: maximum over the non-open
+            // states); without lonely pairs (P.dwn set) fill_D_entries_noLP
             while (dwp < ndw) {
                 const int q = dwp + lane;
                 int4 e = make_int4(0, -1, 0, 0);
@@ -275,7 +277,9 @@ __device__ void run_group_sl(const PairDev &P, int al, int ar, int bl, int br, i
                 if (mine) {
                     const int c2 = e.z - bl;
                     const int mv = max(max(cur[0][c2], cur[1][c2]), max(cur[2][c2], cur[3][c2]));
-                    st_volatile(P.D + e.x, norm(mv + e.w));
+                    int v = mv + e.w;
+                    if (P.flags & PF_NOLP) v = max(v, inner_term<WAIT>(P, dw + q, status, abort_flag));
+                    st_volatile(P.D + e.x, norm(v));
                 }
                 const int cnt = __popc(__ballot_sync(0xffffffffu, mine));
                 dwp += cnt;
@@ -453,7 +457,7 @@ static __device__ __noinline__ void walk_sl(Walker &w, const int *Mg, long long 
                 w.emit(i, j);
                 w.emit(-2, ent.w);
                 w.emit(alq, blq);
-                if (w.qtail < P.tq_cap) P.tq[w.qtail] = make_int4(ent.w, ent.x, alq | (blq << 16), i | (j << 16));
+                if (w.qtail < P.tq_cap) P.tq[w.qtail] = trace_entry(P, ent.w, ent.x, alq, i, blq, j);
                 else w.ok = false;
                 ++w.qtail;
                 i = alq - 1;
@@ -498,16 +502,25 @@ __global__ void __launch_bounds__(TRACE_WARPS * 32)
         const int lefts = __shfl_sync(0xffffffffu, qe.z, 0), rights = __shfl_sync(0xffffffffu, qe.w, 0);
         ++qhead;
         if (k < 0) break;
-        const int4 ends = make_int4(lefts & 0xffff, rights & 0xffff, lefts >> 16, rights >> 16);  // a.l, a.r, b.l, b.r
+        const int4 ends = trace_ends(lefts, rights);  // a.l, a.r, b.l, b.r
+        if (lefts & TQ_CHAIN) {
+            if (lane == 0) trace_chain(w, k, kpos, ends, nseg, status);
+            __syncwarp();
+            qtail = __shfl_sync(0xffffffffu, w.qtail, 0);
+            continue;
+        }
         run_group_sl<false, false, 8>(P, ends.x, ends.y, ends.z, ends.w, Mg, scratch_stride, sw, sm, sw,
                                       nullptr, 0, status, (volatile int *)&dummy_abort);
         __syncwarp();
         if (lane == 0) {
             // trace_arcmatch, struct-local branch (aligner.cc:1014-1026): first
-            // non-open state whose value explains D(am)
+            // non-open state whose value explains D(am); for the inner arc
+            // match of a no-lonely-pairs stack (aligner.cc:1062-1074) the
+            // queue entry carries D(outer) - score(outer) - score(am)
             const int ar = ends.y, br = ends.w;
             const long long o = (long long)(ar - 1 - ends.x) * sw + (br - 1 - ends.z);
-            const int dv = P.D[kpos], sc = P.am_score[k];
+            const bool nolp = P.flags & PF_NOLP;
+            const int dv = nolp ? kpos : P.D[kpos], sc = nolp ? 0 : P.am_score[k];
             const int start = w.ntok;
             for (int s2 = 0; s2 < 4; ++s2) {
                 if (dv == Mg[s2 * scratch_stride + o] + sc) {

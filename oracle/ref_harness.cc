@@ -13,7 +13,7 @@
 // bench uses the timing line as the reference's own CPU baseline.
 //
 // Usage: ref_harness A.pp B.pp [key=value ...]
-//   struct_local=0|1 sequ_local=0|1 free_endgaps=---- min_trace_prob=1e-4
+//   struct_local=0|1 sequ_local=0|1 no_lonely_pairs=0|1 free_endgaps=---- min_trace_prob=1e-4
 //   max_diff=-1 min_prob=0.001 indel=-150 indel_opening=-750 struct_weight=200
 //   tau=50 exclusion=0 dump_tables=1 repeat=1
 #include <chrono>
@@ -46,7 +46,7 @@
 using namespace LocARNA;
 
 struct Opts {
-    bool struct_local = false, sequ_local = false;
+    bool struct_local = false, sequ_local = false, no_lonely_pairs = false;
     std::string free_endgaps = "----";
     double min_trace_prob = 1e-4, min_prob = 0.001;
     int max_diff = -1, indel = -150, indel_opening = -750, struct_weight = 200,
@@ -62,6 +62,7 @@ static void parse(Opts &o, const char *kv) {
     std::string k = s.substr(0, p), v = s.substr(p + 1);
     if (k == "struct_local") o.struct_local = std::atoi(v.c_str());
     else if (k == "sequ_local") o.sequ_local = std::atoi(v.c_str());
+    else if (k == "no_lonely_pairs") o.no_lonely_pairs = std::atoi(v.c_str());
     else if (k == "free_endgaps") o.free_endgaps = v;
     else if (k == "min_trace_prob") o.min_trace_prob = std::atof(v.c_str());
     else if (k == "min_prob") o.min_prob = std::atof(v.c_str());
@@ -183,7 +184,7 @@ int main(int argc, char **argv) {
         auto t0 = std::chrono::steady_clock::now();
         Aligner aligner(AlignerParams(
             AlignerParams::seqA(&seqA), AlignerParams::seqB(&seqB),
-            AlignerParams::scoring(&scoring), AlignerParams::no_lonely_pairs(false),
+            AlignerParams::scoring(&scoring), AlignerParams::no_lonely_pairs(o.no_lonely_pairs),
             AlignerParams::struct_local(o.struct_local), AlignerParams::sequ_local(o.sequ_local),
             AlignerParams::free_endgaps(FreeEndgaps(o.free_endgaps)),
             AlignerParams::max_diff_am(o.max_diff_am), AlignerParams::max_diff_at_am(o.max_diff_at_am),

@@ -45,6 +45,7 @@ typedef struct {
      * (sorted lex greater left ends), CSR over (n+1)*(m+1) */
     int *cle_start, *cle;
     int *cre_start, *cre;
+    int *inner;    /* per arc match: the inner arc match, or -1 */
     sc_t *D;       /* |arcsA| x |arcsB| */
     sc_t *M[8];    /* (n+1) x (m+1) */
     sc_t *E[4];    /* m+1 */
@@ -312,24 +313,76 @@ static void fill_D_entries(Ctx *c, int al, int bl) {
     }
 }
 
-/* AlignerImpl::align_D, aligner.cc:660-732 */
+/* AlignerImpl::fill_D_entries_noLP, aligner.cc:612-657 (no stacking): the
+ * arc matches with left ends (al-1,bl-1) that enclose an inner arc match
+ * (left ends (al,bl), right ends one less) take the better of the inner arc
+ * match's own D and the inner interior plus the inner arc-match score */
+static void fill_D_entries_noLP(Ctx *c, int al, int bl) {
+    size_t q = (size_t)(al - 1) * (c->m + 1) + (bl - 1);
+    for (int p = c->cle_start[q]; p < c->cle_start[q + 1]; ++p) {
+        int k = c->cle[p];
+        int in = c->inner[k];
+        if (in < 0) continue;
+        int a = c->t->am_arcs[2 * k], b = c->t->am_arcs[2 * k + 1];
+        int ar = arcR(c->t->arcs_a, a) - 1, br = arcR(c->t->arcs_b, b) - 1;
+        sc_t mv = MM(c, 0, ar - 1, br - 1);
+        if (c->o->struct_local)
+            for (int s = 1; s < 4; ++s) mv = smax(mv, MM(c, s, ar - 1, br - 1));
+        int ia = c->t->am_arcs[2 * in], ib = c->t->am_arcs[2 * in + 1];
+        DD(c, a, b) = norm(smax(mv + c->t->am_score[in], DD(c, ia, ib)) + c->t->am_score[k]);
+    }
+}
+
+/* ArcMatches::init_inner_arc_matchs, arc_matches.cc:50-74: the first arc
+ * match (in creation order) with left ends (a.l+1,b.l+1) and right ends
+ * (a.r-1,b.r-1), or -1 */
+static void init_inner(Ctx *c) {
+    int na = c->t->num_arcmatches;
+    c->inner = malloc((na > 0 ? na : 1) * sizeof(int));
+    for (int k = 0; k < na; ++k) {
+        int a = c->t->am_arcs[2 * k], b = c->t->am_arcs[2 * k + 1];
+        int al = arcL(c->t->arcs_a, a), ar = arcR(c->t->arcs_a, a);
+        int bl = arcL(c->t->arcs_b, b), br = arcR(c->t->arcs_b, b);
+        c->inner[k] = -1;
+        if (al + 1 > c->n || bl + 1 > c->m) continue;
+        size_t q = (size_t)(al + 1) * (c->m + 1) + (bl + 1);
+        for (int p = c->cle_start[q]; p < c->cle_start[q + 1]; ++p) {
+            int x = c->cle[p];
+            if (arcR(c->t->arcs_a, c->t->am_arcs[2 * x]) == ar - 1 &&
+                arcR(c->t->arcs_b, c->t->am_arcs[2 * x + 1]) == br - 1) {
+                c->inner[k] = x;
+                break;
+            }
+        }
+    }
+}
+
+/* AlignerImpl::align_D, aligner.cc:660-732; group extents by
+ * ArcMatches::get_max_right_ends, arc_matches.cc:313-355 */
 static void align_D(Ctx *c) {
+    const int nolp = c->o->no_lonely_pairs;
     for (int al = c->n; al >= 1; --al) {
         int max_bl = imin(c->m, maxc(c, al));
         int min_bl = imax(1, minc(c, al));
         for (int bl = max_bl; bl >= min_bl; --bl) {
             if (!(a_match(c, al, bl) && valid_match(c, al, bl))) continue;
             int max_ar = al, max_br = bl;
-            size_t q = (size_t)al * (c->m + 1) + bl;
+            /* without lonely pairs: the arc matches that start at
+             * (al-1,bl-1) and enclose an inner arc match, right ends minus one */
+            size_t q = nolp ? (size_t)(al - 1) * (c->m + 1) + (bl - 1) : (size_t)al * (c->m + 1) + bl;
+            if (nolp) { max_ar++; max_br++; }
             for (int p = c->cle_start[q]; p < c->cle_start[q + 1]; ++p) {
                 int k = c->cle[p];
+                if (nolp && c->inner[k] < 0) continue;
                 max_ar = imax(max_ar, arcR(c->t->arcs_a, c->t->am_arcs[2 * k]));
                 max_br = imax(max_br, arcR(c->t->arcs_b, c->t->am_arcs[2 * k + 1]));
             }
+            if (nolp) { max_ar--; max_br--; }
             if (al == max_ar || bl == max_br) continue;
             if (c->cnt) c->cnt->groups++;
             align_in_arcmatch(c, al, max_ar, bl, max_br, c->o->struct_local, 1);
-            fill_D_entries(c, al, bl);
+            if (nolp) fill_D_entries_noLP(c, al, bl);
+            else fill_D_entries(c, al, bl);
         }
     }
 }
@@ -414,6 +467,37 @@ static void trace_arcmatch(Ctx *c, int k) {
     }
 }
 
+/* AlignerImpl::trace_arcmatch_noLP, aligner.cc:1030-1079 (no stacking):
+ * the inner arc match is part of the alignment; below it, either the inner
+ * arc match's own stack continues (D(am) = D(inner) + score(am)) or its
+ * interior is recomputed and traced */
+static void trace_arcmatch_noLP(Ctx *c, int k) {
+    int in = c->inner[k];
+    int a = c->t->am_arcs[2 * k], b = c->t->am_arcs[2 * k + 1];
+    int ia = c->t->am_arcs[2 * in], ib = c->t->am_arcs[2 * in + 1];
+    int ial = arcL(c->t->arcs_a, ia), iar = arcR(c->t->arcs_a, ia);
+    int ibl = arcL(c->t->arcs_b, ib), ibr = arcR(c->t->arcs_b, ib);
+    if (c->ntam < c->tam_cap) c->tam[c->ntam] = in;
+    c->ntam++;
+    append(c, ial, ibl);
+    if (DD(c, a, b) == DD(c, ia, ib) + c->t->am_score[k]) {
+        trace_arcmatch_noLP(c, in);
+    } else {
+        align_in_arcmatch(c, ial, iar, ibl, ibr, c->o->struct_local, 0);
+        if (!c->o->struct_local) {
+            trace_in_arcmatch(c, 0, ial, iar - 1, ibl, ibr - 1, 0);
+        } else {
+            for (int s = 0; s < 4; ++s) {
+                if (DD(c, a, b) == MM(c, s, iar - 1, ibr - 1) + c->t->am_score[k] + c->t->am_score[in]) {
+                    trace_in_arcmatch(c, s, ial, iar - 1, ibl, ibr - 1, 0);
+                    break;
+                }
+            }
+        }
+    }
+    append(c, iar, ibr);
+}
+
 /* AlignerImpl::trace_noex, aligner.cc:1082-1229 */
 static void trace_noex(Ctx *c, int state, int oal, int i, int obl, int j, int tl) {
     sc_t Mij = MM(c, state, i, j);
@@ -467,7 +551,8 @@ static void trace_noex(Ctx *c, int state, int oal, int i, int obl, int j, int tl
             if (c->ntam < c->tam_cap) c->tam[c->ntam] = k;
             c->ntam++;
             append(c, al, bl);
-            trace_arcmatch(c, k);
+            if (c->o->no_lonely_pairs) trace_arcmatch_noLP(c, k);
+            else trace_arcmatch(c, k);
             append(c, i, j);
             return;
         }
@@ -533,7 +618,7 @@ static void trace_in_arcmatch(Ctx *c, int state, int al, int i, int bl, int j, i
 static void ctx_free(Ctx *c) {
     free(c->radjA_start); free(c->radjA); free(c->radjB_start); free(c->radjB);
     free(c->cle_start); free(c->cle); free(c->cre_start); free(c->cre);
-    free(c->D);
+    free(c->D); free(c->inner);
     for (int s = 0; s < 8; ++s) free(c->M[s]);
     for (int s = 0; s < 4; ++s) free(c->E[s]);
 }
@@ -552,6 +637,7 @@ int lcg_oracle_align(const lcg_pair_tables *t, const lcg_align_opts *o,
     build_radj(t->arcs_a, t->num_arcs_a, c.n, &c.radjA_start, &c.radjA);
     build_radj(t->arcs_b, t->num_arcs_b, c.m, &c.radjB_start, &c.radjB);
     build_am_lists(&c);
+    init_inner(&c);
     size_t nd = (size_t)t->num_arcs_a * t->num_arcs_b;
     c.D = malloc((nd > 0 ? nd : 1) * sizeof(sc_t));
     for (size_t q = 0; q < nd; ++q) c.D[q] = NEG_INF;

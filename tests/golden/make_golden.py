@@ -40,6 +40,14 @@ CASES = {
     "c60_short": (60, 41, 70, 42, {}, True),
     "c200_global": (200, 5, 200, 6, {}, True),
     "c400_global": (400, 3, 400, 4, {}, True),
+    # locarna --noLP: no lonely base pairs in the aligned structure
+    "c150_nolp": (150, 1, 150, 2, {"no_lonely_pairs": "1"}, True),
+    "c150_nolp_b": (150, 11, 140, 12, {"no_lonely_pairs": "1"}, True),
+    "c150_nolp_seqlocal": (150, 1, 150, 2, {"no_lonely_pairs": "1", "sequ_local": "1"}, True),
+    "c150_nolp_structlocal": (150, 1, 150, 2, {"no_lonely_pairs": "1", "struct_local": "1"}, True),
+    "c150_nolp_freeall": (150, 1, 150, 2, {"no_lonely_pairs": "1", "free_endgaps": "++++"}, True),
+    "c120_nolp_opening0": (120, 21, 130, 22, {"no_lonely_pairs": "1", "indel_opening": "0"}, True),
+    "c300_nolp": (300, 61, 280, 62, {"no_lonely_pairs": "1"}, True),
 }
 
 

@@ -52,9 +52,16 @@ class Golden:
     def free_endgaps(self):
         return self.opts.get("free_endgaps", "----")
 
+    @property
+    def no_lonely_pairs(self):
+        return self.opts.get("no_lonely_pairs") == "1"
+
     def align_kwargs(self):
-        return dict(struct_local=self.struct_local, sequ_local=self.sequ_local,
-                    free_endgaps=self.free_endgaps)
+        kw = dict(struct_local=self.struct_local, sequ_local=self.sequ_local,
+                  free_endgaps=self.free_endgaps)
+        if self.no_lonely_pairs:
+            kw["no_lonely_pairs"] = True
+        return kw
 
 
 class GoldenPF:

@@ -66,3 +66,25 @@ def test_gpu_chunk_pipeline_matches_oracle(engine):
         assert_same_result(one[k], ref, f"pair {k}")
         assert_same_result(auto[k], ref, f"pair {k} (automatic chunks)")
         assert_same_result(small[k], ref, f"pair {k} (7-pair chunks)")
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", [{}, {"struct_local": True}, {"sequ_local": True},
+                                  {"free_endgaps": "+-+-"}])
+def test_gpu_no_lonely_pairs_matches_oracle(engine, mode):
+    """locarna --noLP (fill_D_entries_noLP, trace_arcmatch_noLP): a batch of
+    synthetic pairs with planted stems, every pair bit-exact against the
+    oracle (score, end cells, edges, traced arc matches)."""
+    from locarna_gb300.prep import prepare_pair
+    from locarna_gb300.synth import make_family
+    fam = make_family(9, 60, 170, 91, q=0.05)
+    pp = [r.to_pp() for r in fam]
+    tables = [prepare_pair(pp[a], pp[b]) for a in range(len(fam)) for b in range(a + 1, len(fam))]
+    kw = dict(mode, no_lonely_pairs=True)
+    res = engine.align_pairs(tables, **kw)
+    stacked = 0
+    for k, t in enumerate(tables):
+        ref = oracle_align(t, **kw)
+        assert_same_result(res[k], ref, f"pair {k}")
+        stacked += len(ref.traced_am)
+    assert stacked > 0
