@@ -422,6 +422,32 @@ def run_ours(args):
         dev_ms_single += eng.last_stats()[0]
     wall_single = time.perf_counter() - t1
 
+    # the same workload with locarna --noLP (no lonely pairs): device time of
+    # the one-chunk call and wall time of the default call
+    ncall = eng.prepare_call(tables, no_lonely_pairs=True)
+    eng.set_chunk_pairs(npairs)
+    eng.run_call(ncall)
+    nolp_ms = []
+    for _ in range(max(1, args.steps // 2)):
+        flush_l2()
+        eng.run_call(ncall)
+        nolp_ms.append(eng.last_stats()[0])
+    eng.set_chunk_pairs(0)
+    eng.run_call(ncall)
+    nolp_wall = []
+    for _ in range(max(1, args.steps // 2)):
+        flush_l2()
+        s0 = time.perf_counter()
+        eng.run_call(ncall)
+        nolp_wall.append(time.perf_counter() - s0)
+    nres = Engine.decode_call(ncall)
+    for k in range(0, npairs, max(1, npairs // 6)):
+        assert_same_result(nres[k], oracle_align(tables[k], no_lonely_pairs=True), f"pair {k} (noLP)")
+    nolp = {"mode": "global, --noLP (no lonely pairs)", "pairs": npairs,
+            "aligns_per_s": npairs / (sum(nolp_ms) / len(nolp_ms) / 1e3),
+            "e2e_aligns_per_s": npairs / (sum(nolp_wall) / len(nolp_wall)),
+            "stacked_arc_matches_traced": sum(len(r.traced_am) for r in nres)}
+
     T = kern_ms / 1e3 / args.steps
     Tf = fill_ms / 1e3 / args.steps
     We = wall_s / args.steps
@@ -470,6 +496,7 @@ def run_ours(args):
                                    f"per core, {CPU_SAMPLE_SECONDS:.0f} s per process"},
         "clocks": clocks,
         "table_prep": table_prep,
+        "nolp": nolp,
     }
     if pf_tables is not None:
         out["locarna_p"] = run_pf(eng, pf_tables, flush_l2, pf_cpu)

@@ -92,7 +92,20 @@ typedef struct lcg_pair_tables {
      * without anchors (0,0) and (len_a+1,len_b+1) */
     int32_t right_anchor_a, right_anchor_b;
     int32_t left_anchor_a, left_anchor_b;
+    /* Stacking (locarna --stacking / --new-stacking; Scoring::stacking(),
+     * scoring.hh:653): both NULL = off. am_stack_score[k] =
+     * Scoring::arcmatch(am_k, true) (scoring.cc:440-480), the score of am_k
+     * stacked on its inner arc match; values <= LCG_STACK_NONE stand for
+     * scores outside the int32 range, which the reference only produces from
+     * zero stacking probabilities (undefined weights) and which never explain
+     * an alignment. am_stackable[k] = Scoring::is_stackable_am(am_k)
+     * (scoring.cc:567-569). Used by fill_D_entries (aligner.cc:600-608),
+     * fill_D_entries_noLP (:629-650) and trace_arcmatch (:986-1006). */
+    const int32_t *am_stack_score;
+    const uint8_t *am_stackable;
 } lcg_pair_tables;
+
+#define LCG_STACK_NONE (-(1 << 29))
 
 /* AlignerParams subset (aligner_params.hh:51-64) */
 typedef struct lcg_align_opts {
@@ -327,6 +340,11 @@ typedef struct lcg_prep_opts {
     int32_t free_endgaps;         /* LCG_FREE_* bits for the envelope */
     int32_t pf_precision;         /* envelope float type: 0 double, 1 long double (locarna's default) */
     double exp_prob;              /* --exp-prob; <= 0 means 1/(2 len) per sequence */
+    /* --stacking (needs --exp-prob, else off as in src/locarna.cc:407-414)
+     * and --new-stacking: read the joint probabilities of the PP input's
+     * #STACK section and fill lcg_pair_tables.am_stack_score/am_stackable */
+    int32_t stacking;
+    int32_t new_stacking;
 } lcg_prep_opts;
 
 typedef struct lcg_prepared_s *lcg_prepared;

@@ -9,6 +9,7 @@ import ctypes as C
 import numpy as np
 
 LCG_NEG_INF = -(1 << 40)
+LCG_STACK_NONE = -(1 << 29)
 LCG_FREE_LEFT_1, LCG_FREE_RIGHT_1, LCG_FREE_LEFT_2, LCG_FREE_RIGHT_2 = 1, 2, 4, 8
 
 _P32 = C.POINTER(C.c_int32)
@@ -29,6 +30,7 @@ class lcg_pair_tables(C.Structure):
         ("ins_lo", _P32), ("ins_hi", _P32),
         ("right_anchor_a", C.c_int32), ("right_anchor_b", C.c_int32),
         ("left_anchor_a", C.c_int32), ("left_anchor_b", C.c_int32),
+        ("am_stack_score", _P32), ("am_stackable", C.POINTER(C.c_uint8)),
     ]
 
 
@@ -93,7 +95,7 @@ class PairTables:
     def __init__(self, len_a, len_b, sigma, gap_a, gap_b, indel_opening,
                  exclusion, arcs_a, arcs_b, am_arcs, am_score, min_col,
                  max_col, anchors=None, right_anchor=(0, 0), left_anchor=None,
-                 seq_a="", seq_b=""):
+                 seq_a="", seq_b="", am_stack_score=None, am_stackable=None):
         self.len_a, self.len_b = int(len_a), int(len_b)
         self.sigma = _i32(sigma).reshape(-1)
         self.gap_a, self.gap_b = _i32(gap_a), _i32(gap_b)
@@ -109,6 +111,10 @@ class PairTables:
         self.right_anchor = tuple(right_anchor)
         self.left_anchor = tuple(left_anchor) if left_anchor else (self.len_a + 1, self.len_b + 1)
         self.seq_a, self.seq_b = seq_a, seq_b
+        # stacking (both None = off): Scoring::arcmatch(am, true) and is_stackable_am
+        self.am_stack_score = None if am_stack_score is None else _i32(am_stack_score)
+        self.am_stackable = (None if am_stackable is None else
+                             np.ascontiguousarray(np.asarray(am_stackable, dtype=np.uint8)))
         self._check()
 
     def _check(self):
@@ -117,6 +123,9 @@ class PairTables:
         assert self.gap_a.size == n + 1 and self.gap_b.size == m + 1
         assert self.min_col.size == n + 1 and self.max_col.size == n + 1
         assert self.am_arcs.size == 2 * self.am_score.size
+        assert (self.am_stack_score is None) == (self.am_stackable is None)
+        if self.am_stack_score is not None:
+            assert self.am_stack_score.size == self.am_stackable.size == self.am_score.size
 
     @property
     def num_arcs_a(self):
@@ -145,6 +154,10 @@ class PairTables:
                 setattr(t, k, _ptr(self.anchors[k]))
         t.right_anchor_a, t.right_anchor_b = self.right_anchor
         t.left_anchor_a, t.left_anchor_b = self.left_anchor
+        if self.am_stack_score is not None:
+            # numpy gives even an empty array a non-NULL data pointer
+            t.am_stack_score = _ptr(self.am_stack_score)
+            t.am_stackable = self.am_stackable.ctypes.data_as(C.POINTER(C.c_uint8))
         return t
 
 

@@ -76,8 +76,12 @@ lcg_status prep_pair(const lcg_pair_tables &t, const lcg_align_opts &o, Prep &p)
     p.m = m;
     p.fe = o.free_endgaps & 15;
     const bool nolp = o.no_lonely_pairs != 0;
+    const bool stack = t.am_stack_score != nullptr;
+    if (stack != (t.am_stackable != nullptr))
+        return bad(LCG_ERR_ARG, "am_stack_score and am_stackable must be both set or both NULL");
     p.flags = (o.sequ_local ? PF_SEQU_LOCAL : 0) | (anchors ? PF_ANCHORS : 0) |
-              (o.do_trace ? PF_TRACE : 0) | (o.struct_local ? PF_STRUCT_LOCAL : 0) | (nolp ? PF_NOLP : 0);
+              (o.do_trace ? PF_TRACE : 0) | (o.struct_local ? PF_STRUCT_LOCAL : 0) | (nolp ? PF_NOLP : 0) |
+              (stack ? PF_STACK : 0);
     if (o.sequ_local && p.fe) return bad(LCG_ERR_ARG, "free end gaps cannot be combined with local alignment");
 
     // band: monotone, inside [0,m], rows non-empty and connected
@@ -177,6 +181,9 @@ lcg_status prep_pair(const lcg_pair_tables &t, const lcg_align_opts &o, Prep &p)
     for (int i = 0; i <= n; ++i) mg = std::max(mg, (long long)std::llabs(t.gap_a[i]));
     for (int j = 0; j <= m; ++j) mg = std::max(mg, (long long)std::llabs(t.gap_b[j]));
     for (int k = 0; k < t.num_arcmatches; ++k) mam = std::max(mam, (long long)std::llabs(t.am_score[k]));
+    if (stack)
+        for (int k = 0; k < t.num_arcmatches; ++k)
+            if (t.am_stack_score[k] > LCG_STACK_NONE) mam = std::max(mam, (long long)std::llabs(t.am_stack_score[k]));
     long long bound = (long long)(n + m) * (ms + mg + std::llabs(t.indel_opening) + std::llabs(t.exclusion)) +
                       (long long)(std::min(n, m) / 2 + 1) * mam;
     if (bound >= (1ll << 27)) return bad(LCG_ERR_RANGE, "scores may exceed the int32 device range");
@@ -304,7 +311,11 @@ lcg_status prep_pair(const lcg_pair_tables &t, const lcg_align_opts &o, Prep &p)
     // (ArcMatches::init_inner_arc_matchs, arc_matches.cc:50-74); byleft
     // holds each left-end bucket in index order
     std::vector<int> inner;
-    if (nolp) {
+    if (stack) {
+        p.sscore.assign(std::max(na, 1), NEG);
+        for (int k = 0; k < na; ++k) p.sscore[k] = t.am_stack_score[k] <= LCG_STACK_NONE ? NEG : t.am_stack_score[k];
+    }
+    if (nolp || stack) {
         inner.assign(na, -1);
         p.inner.assign(std::max(na, 1), make_int2(-1, -1));
         for (int k = 0; k < na; ++k) {
@@ -382,7 +393,9 @@ lcg_status prep_pair(const lcg_pair_tables &t, const lcg_align_opts &o, Prep &p)
             auto ar_less = [&](int x, int y) { return p.am_ends[4 * x + 1] < p.am_ends[4 * y + 1]; };
             if (!std::is_sorted(ks.begin(), ks.end(), ar_less)) std::stable_sort(ks.begin(), ks.end(), ar_less);
             for (int k : ks) {
-                if (nolp && inner[k] < 0) continue;
+                // fill_D_entries_noLP: only arc matches with an inner arc
+                // match, with stacking only stackable ones (aligner.cc:629-630)
+                if (nolp && (inner[k] < 0 || (stack && !t.am_stackable[k]))) continue;
                 // the corner: (ar-1,br-1) inside the arc match, or, without
                 // lonely pairs, inside its inner arc match
                 int ar = p.am_ends[4 * k + 1] - sh, br = p.am_ends[4 * k + 3] - sh;
@@ -391,10 +404,17 @@ lcg_status prep_pair(const lcg_pair_tables &t, const lcg_align_opts &o, Prep &p)
                 if (ar - 1 > al && br - 1 > bl && in_band(ar - 1, br - 1) && p.am_pos[k] >= 0) {
                     if (nolp) {
                         const int in = inner[k];
-                        p.dw.push_back(make_int4(p.am_pos[k], ar - 1, br - 1, t.am_score[k] + t.am_score[in]));
-                        p.dwn.push_back(make_int2(p.am_pos[in], t.am_score[k]));
+                        const int sk = stack ? p.sscore[k] : t.am_score[k];  // arcmatch(am, stacking)
+                        p.dw.push_back(make_int4(p.am_pos[k], ar - 1, br - 1, sk + t.am_score[in]));
+                        p.dwn.push_back(make_int2(p.am_pos[in], sk));
                     } else {
                         p.dw.push_back(make_int4(p.am_pos[k], ar - 1, br - 1, t.am_score[k]));
+                        if (stack) {
+                            // fill_D_entries with stacking (aligner.cc:600-608)
+                            const int in = inner[k];
+                            if (in >= 0 && t.am_stackable[k]) p.dwn.push_back(make_int2(p.am_pos[in], p.sscore[k]));
+                            else p.dwn.push_back(make_int2(-1, 0));
+                        }
                     }
                     p.Dinit[p.am_pos[k]] = NOT_READY;
                 }
@@ -497,7 +517,7 @@ Slot slot_of(lcg_engine e, int k) {
 // byte offsets of one pair's tables in the arena
 struct PairOff {
     size_t sigma, scls, rcls, ccls, gapA, gapB, minc, maxc, bandoff, rowinfo, anc, cre_start, cre, crow, rowarc,
-        am_score, D, topM, res, tok, tq, segs, groups, dw, gbc, dwn, inner;
+        am_score, D, topM, res, tok, tq, segs, groups, dw, gbc, dwn, inner, sscore;
 };
 
 // One chunk of an lcg_align_pairs call: pairs [q0, q0 + nq) of the batch.
@@ -561,6 +581,7 @@ lcg_status chunk_launch(lcg_engine e, const Slot &s, const lcg_pair_tables *all,
         o.dw = take(up, sizeof(int4) * std::max<size_t>(p.dw.size(), 1));
         o.dwn = p.inner.empty() ? 0 : take(up, sizeof(int2) * std::max<size_t>(p.dwn.size(), 1));
         o.inner = p.inner.empty() ? 0 : take(up, sizeof(int2) * p.inner.size());
+        o.sscore = p.sscore.empty() ? 0 : take(up, 4ull * p.sscore.size());
         // sigma: the class table when it exists, else the dense table
         o.sigma = p.use_cls ? 0 : take(up, 4ull * (p.n + 1) * (p.m + 1));
         o.scls = p.use_cls ? take(up, 4ull * 256) : 0;
@@ -677,6 +698,7 @@ lcg_status chunk_launch(lcg_engine e, const Slot &s, const lcg_pair_tables *all,
         if (!p.dw.empty()) std::memcpy(H + o.dw, p.dw.data(), sizeof(int4) * p.dw.size());
         if (!p.dwn.empty()) std::memcpy(H + o.dwn, p.dwn.data(), sizeof(int2) * p.dwn.size());
         if (!p.inner.empty()) std::memcpy(H + o.inner, p.inner.data(), sizeof(int2) * p.inner.size());
+        if (!p.sscore.empty()) std::memcpy(H + o.sscore, p.sscore.data(), 4ull * p.sscore.size());
         PairDev &d = hp[q];
         std::memset(&d, 0, sizeof d);
         d.n = p.n;
@@ -732,6 +754,7 @@ lcg_status chunk_launch(lcg_engine e, const Slot &s, const lcg_pair_tables *all,
         d.dw = (const int4 *)(Dv + o.dw);
         d.dwn = p.inner.empty() ? nullptr : (const int2 *)(Dv + o.dwn);
         d.inner = p.inner.empty() ? nullptr : (const int2 *)(Dv + o.inner);
+        d.am_sscore = p.sscore.empty() ? nullptr : (const int *)(Dv + o.sscore);
     });
     *pack_ms += ms_between(tp0, std::chrono::steady_clock::now());
 

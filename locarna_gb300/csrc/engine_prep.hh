@@ -40,8 +40,9 @@ struct Prep {
     std::vector<int> gbc;  // m+1: gapB(j) * 16 + sigma column class (0 without classes)
     std::vector<lcg::GroupItem> groups;          // pair field filled later
     std::vector<int4> dw;                        // dw_start relative to this pair
-    std::vector<int2> dwn;                       // no lonely pairs: parallel to dw (PairDev::dwn)
-    std::vector<int2> inner;                     // no lonely pairs: per am (PairDev::inner)
+    std::vector<int2> dwn;                       // no lonely pairs / stacking: parallel to dw (PairDev::dwn)
+    std::vector<int2> inner;                     // no lonely pairs / stacking: per am (PairDev::inner)
+    std::vector<int> sscore;                     // stacking: per am (PairDev::am_sscore)
     int rows_max = 0, width_max = 0;             // over groups
     int token_cap = 0, tq_cap = 0;
     long long cells = 0;                         // M cells of all groups + top level

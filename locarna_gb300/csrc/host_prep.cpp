@@ -22,6 +22,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cctype>
+#include <climits>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -55,6 +56,8 @@ struct RnaInput {
     std::string name;
     std::string seq;                  // normalised (upper case, T -> U), 1-based via seq[i-1]
     std::map<std::pair<int, int>, double> arc_probs;  // (i,j) -> p, i<j (sparse matrix)
+    // joint probabilities of (i,j) and (i+1,j-1) (the p2 column, read only with stacking)
+    std::map<std::pair<int, int>, double> arc2_probs;
     std::string anchors;
 };
 
@@ -82,7 +85,7 @@ bool next_line(std::istream &in, std::string &line) {
 
 bool has_prefix(const std::string &s, const std::string &p) { return s.compare(0, p.size(), p) == 0; }
 
-RnaInput read_pp(const std::string &text, double p_bpcut) {
+RnaInput read_pp(const std::string &text, double p_bpcut, bool stacking) {
     std::istringstream in(text);
     std::string line;
     RnaInput r;
@@ -133,6 +136,7 @@ RnaInput read_pp(const std::string &text, double p_bpcut) {
     // base pair section
     if (!next_line(in, line) || line != "#SECTION BASEPAIRS") perr(LCG_ERR_PARSE, "Expected base pair section header.");
     const size_t len = r.seq.size();
+    bool contains_stacking = false;
     while (next_line(in, line)) {
         if (line[0] == '#') {
             if (has_prefix(line, "#END")) break;
@@ -143,6 +147,8 @@ RnaInput read_pp(const std::string &text, double p_bpcut) {
                 ls >> dummy >> p;
                 if (ls.fail()) perr(LCG_ERR_PARSE, "Cannot parse line \"" + line + "\" in base pairs section.");
                 p_bpcut = std::max(p, p_bpcut);
+            } else if (has_prefix(line, "#STACK")) {
+                contains_stacking = true;
             }
             continue;
         }
@@ -154,7 +160,12 @@ RnaInput read_pp(const std::string &text, double p_bpcut) {
         if (!(1 <= i && i < j && j <= len)) perr(LCG_ERR_PARSE, "Invalid indices in PP input line \"" + line + "\".");
         if (p <= p_bpcut) continue;
         r.arc_probs[{(int)i, (int)j}] = p;
+        // rna_data.cc:1085-1094: the joint probability of (i,j) and (i+1,j-1)
+        double p2;
+        if (stacking && (ls >> p2) && p2 > p_bpcut) r.arc2_probs[{(int)i, (int)j}] = p2;
     }
+    if (!contains_stacking && !r.arc2_probs.empty())
+        perr(LCG_ERR_PARSE, "Stacking probabilties found but stack keyword is missing.");
     return r;
 }
 
@@ -182,6 +193,10 @@ struct Side {
     int len = 0;
     std::vector<Arc> arcs;        // reference index order
     std::vector<long> weights;    // probToWeight per arc
+    // stacking: Scoring::stack_weightsX per arc (scoring.cc:200-237) in the
+    // reference's 64-bit arithmetic, and is_stackable_arcX (joint probability > 0)
+    std::vector<long> stack_w;
+    std::vector<uint8_t> stackable;
     std::vector<double> dsw;      // d weight / d struct_weight per arc, unrounded: 1 - ln p / ln pe
     std::vector<double> p_up, p_down;  // prob_paired_upstream / downstream
     std::vector<int> left_start;  // len+2: arcs with left end l are [left_start[l+1], left_start[l]) (index order)
@@ -250,6 +265,21 @@ long prob_to_weight(double p, double pe, int struct_weight) {
     // Scoring::probToWeight (scoring.cc:250-265)
     return round2score(round(struct_weight * (1 - log(p) / log(pe))));
 }
+
+// probToWeight for stack weights, where p may be 0: the weight is then
+// -infinity, which the reference converts to its integer score type; both of
+// its targets (x86-64 and arm64) give LONG_MIN for that conversion, which is
+// what this returns instead of converting -infinity (undefined in C++)
+long stack_prob_to_weight(double p, double pe, int struct_weight) {
+    const double x = round(struct_weight * (1 - log(p) / log(pe)));
+    const double d = x < 0 ? x - 0.5 : x + 0.5;
+    if (!(d > -9.2e18)) return LONG_MIN;
+    return (long)d;
+}
+
+// a + b with 64-bit two's-complement wrap-around, as the reference's sums of
+// such weights come out on its targets
+long wrap_add(long a, long b) { return (long)((unsigned long)a + (unsigned long)b); }
 
 // ---------------------------------------------------------------- envelope
 
@@ -452,8 +482,11 @@ struct lcg_prepared_s {
     std::vector<double> arc_p_a, arc_p_b;
     std::vector<int8_t> code_a, code_b;  // 0..3 for A,C,G,U, -1 otherwise; index 1..len
     std::vector<double> am_dsw;          // d am_score / d struct_weight, unrounded
+    std::vector<int32_t> am_stack_score; // stacking: Scoring::arcmatch(am, true) (LCG_STACK_NONE: out of range)
+    std::vector<uint8_t> am_stackable;   // stacking: Scoring::is_stackable_am
     int32_t indel_opening = 0, exclusion = 0;
     int envelope_ok = 1;
+    bool stacking = false;
 };
 
 extern "C" {
@@ -511,12 +544,37 @@ struct Staged {
 // pe = prob_exp_f(len) (aux.hh:216-220), and the arcs by left end.
 std::shared_ptr<const Side> make_side(const char *pp, const lcg_prep_opts &o) {
     auto s = std::make_shared<Side>();
-    s->in = read_pp(pp, o.min_prob);
+    // locarna turns the (old) stacking off unless --exp-prob is given
+    // (src/locarna.cc:407-414); the PP reader reads the joint probabilities
+    // when either stacking is on (locarna.cc:462)
+    const bool old_stacking = o.stacking && o.exp_prob > 0;
+    const bool stacking = old_stacking || o.new_stacking;
+    s->in = read_pp(pp, o.min_prob, stacking);
     make_arcs(*s, o.min_prob);
     const double pe = o.exp_prob > 0 ? o.exp_prob : 1.0 / (2.0 * s->len);
     for (auto &a : s->arcs) {
         s->weights.push_back(prob_to_weight(a.p, pe, o.struct_weight));
         s->dsw.push_back(1 - log(a.p) / log(pe));
+    }
+    if (stacking) {
+        // Scoring::precompute_weights (scoring.cc:200-237)
+        auto prob = [](const std::map<std::pair<int, int>, double> &mp, int i, int j) {
+            auto it = mp.find({i, j});
+            return it == mp.end() ? 0.0 : it->second;
+        };
+        for (size_t k = 0; k < s->arcs.size(); ++k) {
+            const Arc &a = s->arcs[k];
+            const double p_in = prob(s->in.arc_probs, a.l + 1, a.r - 1);
+            const double joint = prob(s->in.arc2_probs, a.l, a.r);
+            long w = 0;
+            if (old_stacking && p_in > 0) w = stack_prob_to_weight(joint / p_in, pe, o.struct_weight);
+            if (o.new_stacking) {
+                if (!old_stacking) w = s->weights[k];
+                if (p_in > 0) w = wrap_add(w, stack_prob_to_weight(joint, pe, o.struct_weight));
+            }
+            s->stack_w.push_back(w);
+            s->stackable.push_back(joint > 0 ? 1 : 0);
+        }
     }
     // arcs are ordered by left end descending: [left_start[l+1], left_start[l])
     s->left_start.assign(s->len + 2, 0);
@@ -564,6 +622,7 @@ void stage_tables(Staged &S) {
     const Band &tc = S.tc;
     lcg_prepared_s *P = S.P.get();
     const int n = A.len, m = B.len;
+    P->stacking = (o.stacking && o.exp_prob > 0) || o.new_stacking;
     // scoring tables
     P->sigma.assign((size_t)(n + 1) * (m + 1), 0);
     long tab[256][256];
@@ -642,6 +701,15 @@ void stage_tables(Staged &S) {
             P->am_arcs.push_back((int32_t)ib);
             P->am_score.push_back((int32_t)s);
             P->am_dsw.push_back(A.dsw[ia] + B.dsw[ib]);
+            if (!A.stack_w.empty()) {
+                // Scoring::arcmatch(am, true) (scoring.cc:440-480) in the
+                // reference's 64-bit arithmetic; values that leave the int32
+                // tables' range only arise from undefined (zero-probability)
+                // stack weights and never explain an alignment
+                const long st = wrap_add(((long)o.tau * seqc) / 100, wrap_add(A.stack_w[ia], B.stack_w[ib]));
+                P->am_stack_score.push_back(st > -(1L << 29) && st < (1L << 29) ? (int32_t)st : LCG_STACK_NONE);
+                P->am_stackable.push_back(A.stackable[ia] && B.stackable[ib]);
+            }
         }
     }
     for (auto &a : A.arcs) {
@@ -889,6 +957,10 @@ lcg_status lcg_prepared_tables(lcg_prepared p, lcg_pair_tables *t) {
     t->am_score = p->am_score.data();
     t->min_col = p->min_col.data();
     t->max_col = p->max_col.data();
+    if (p->stacking) {
+        t->am_stack_score = p->am_stack_score.data();
+        t->am_stackable = p->am_stackable.data();
+    }
     t->right_anchor_a = 0;
     t->right_anchor_b = 0;
     t->left_anchor_a = p->n + 1;

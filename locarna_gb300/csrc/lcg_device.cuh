@@ -31,6 +31,7 @@ enum PairFlags : int {
     PF_TRACE = 8,
     PF_SCLS = 16,  // sigma(i,j) = scls[rcls[i] * 16 + ccls[j]] (at most 16 row / column classes)
     PF_NOLP = 32,  // no lonely pairs (AlignerParams::no_lonely_pairs)
+    PF_STACK = 64, // stacking terms (Scoring::stacking())
 };
 
 // status word bits (device -> host)
@@ -82,14 +83,20 @@ struct PairDev {
     int4 *segs;           // traceback segments: (am or -1, token start, token end, 0)
     const GroupItem *groups;  // the pair's left-end groups (work items) in dependency order
     const int4 *dw;           // the pair's D writes; GroupItem::dw_start indexes it
-    // PF_NOLP only (else nullptr): per D write, (D index of the inner arc
-    // match or -1, score of the outer arc match), parallel to dw; the write is
-    // D = max(M(corner) + dw.w, D(inner) + score) (fill_D_entries_noLP,
-    // aligner.cc:612-657) with dw.w = score(outer) + score(inner)
+    // PF_NOLP or PF_STACK (else nullptr): per D write, (D index of the inner
+    // arc match or -1, a score), parallel to dw; the write is
+    // D = max(M(corner) + dw.w, D(inner) + score). No lonely pairs
+    // (fill_D_entries_noLP, aligner.cc:612-657): dw.w = score'(outer) +
+    // score(inner), score = score'(outer), score' the stacked score with
+    // PF_STACK; stacking alone (fill_D_entries, :600-608): dw.w =
+    // score(outer), score = its stacked score (inner -1 unless stackable)
     const int2 *dwn;
-    // PF_NOLP only: per arc match, (inner arc match or -1, its D index or -1)
-    // (ArcMatches::inner_arc_match, arc_matches.hh:466-476)
+    // PF_NOLP or PF_STACK: per arc match, (inner arc match or -1, its D index
+    // or -1) (ArcMatches::inner_arc_match, arc_matches.hh:466-476)
     const int2 *inner;
+    // PF_STACK: per arc match Scoring::arcmatch(am, true), NEG where the
+    // tables give LCG_STACK_NONE
+    const int *am_sscore;
 };
 
 // Scoring::basematch(i,j) from the class table or the dense table

@@ -199,7 +199,7 @@ extern "C" lcg_status lcg_align_score_static(const lcg_pair_tables *pair, const 
     for (auto &g : p.groups) g.pair = 0;
     d.groups = (const GroupItem *)(base + o_items);
     d.dw = (const int4 *)(base + o_dw);
-    d.dwn = (p.flags & PF_NOLP) ? (const int2 *)(base + o_dwn) : nullptr;
+    d.dwn = (p.flags & (PF_NOLP | PF_STACK)) ? (const int2 *)(base + o_dwn) : nullptr;
     d.gbc = (const int *)(base + o_gbc);
     std::vector<int2> queue(p.groups.size());  // one pair: the groups in their own order
     for (size_t g = 0; g < queue.size(); ++g) queue[g] = make_int2(0, (int)g);

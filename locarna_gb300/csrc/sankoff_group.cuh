@@ -61,8 +61,8 @@ __device__ __forceinline__ int wait_D(int *D, int k, int *status, volatile int *
     return v;
 }
 
-// No lonely pairs: D(inner) + score(outer) for the D write *e of a group
-// (PairDev::dwn, parallel to PairDev::dw); kept out of line, it is rare.
+// No lonely pairs or stacking: D(inner) + score for the D write *e of a
+// group (PairDev::dwn, parallel to PairDev::dw); kept out of line, it is rare.
 template <bool WAIT>
 __device__ __noinline__ int inner_term(const PairDev &P, const int4 *e, int *status, volatile int *abort_flag) {
     const int2 x = P.dwn[e - P.dw];
@@ -363,7 +363,7 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
                 const bool mine = q < ndw && e.y == i;
                 if (mine) {
                     int v = CUR(e.z) + e.w;
-                    if (P.flags & PF_NOLP) v = max(v, inner_term<WAIT>(P, dw + q, status, abort_flag));
+                    if (P.flags & (PF_NOLP | PF_STACK)) v = max(v, inner_term<WAIT>(P, dw + q, status, abort_flag));
                     st_volatile(Dp + e.x, norm(v));
                 }
                 const int cnt = __popc(__ballot_sync(0xffffffffu, mine));
@@ -585,11 +585,19 @@ __device__ __forceinline__ int4 trace_ends(int lefts, int rights) {
     return make_int4(lefts & 0xffff, rights & 0xffff, (lefts >> 16) & 0x7fff, rights >> 16);
 }
 
+// Arc match k's segment when k is traced through its inner arc match:
+// the inner arc match's two edges around its arc-match token
+__device__ __forceinline__ void emit_inner(Walker &w, int in, int4 ends) {
+    w.emit(ends.y - 1, ends.w - 1);
+    w.emit(-2, in);
+    w.emit(ends.x + 1, ends.z + 1);
+}
+
 // trace_arcmatch_noLP (aligner.cc:1030-1079) for arc match k (D index kpos):
 // the inner arc match's two edges and its arc-match token form k's segment;
 // the inner arc match is queued to continue the stack (TQ_CHAIN) when
-// D(k) == D(inner) + score(k), else to have its interior recomputed and
-// walked (aligner.cc:1057-1075).
+// D(k) == D(inner) + score'(k), else to have its interior recomputed and
+// walked (aligner.cc:1057-1075); score' is the stacked score with stacking.
 static __device__ __noinline__ void trace_chain(Walker &w, int k, int kpos, int4 ends, int &nseg,
                                                 int *status) {
     const PairDev &P = w.P;
@@ -599,10 +607,8 @@ static __device__ __noinline__ void trace_chain(Walker &w, int k, int kpos, int4
         atomicOr(status, ST_INTERNAL);
     } else {
         const int ial = ends.x + 1, iar = ends.y - 1, ibl = ends.z + 1, ibr = ends.w - 1;
-        w.emit(iar, ibr);
-        w.emit(-2, in.x);
-        w.emit(ial, ibl);
-        const int dk = P.D[kpos], sk = P.am_score[k];
+        emit_inner(w, in.x, ends);
+        const int dk = P.D[kpos], sk = (P.flags & PF_STACK) ? P.am_sscore[k] : P.am_score[k];
         const int din = in.y >= 0 ? P.D[in.y] : NEG;
         int4 e;
         if (in.y >= 0 && dk == din + sk)
@@ -615,6 +621,27 @@ static __device__ __noinline__ void trace_chain(Walker &w, int k, int kpos, int4
     }
     if (nseg < P.tq_cap + 1) P.segs[nseg] = make_int4(k, start, w.ntok, 0);
     ++nseg;
+}
+
+// trace_arcmatch with stacking (aligner.cc:986-1006): if arc match k (D index
+// kpos) is explained by its inner arc match, D(k) == D(inner) + stacked
+// score(k), k's segment is the inner arc match's edges and token, the inner
+// arc match is queued in the same mode, and this returns true; else k's
+// interior is traced as without stacking.
+static __device__ __noinline__ bool trace_stack(Walker &w, int k, int kpos, int4 ends, int &nseg) {
+    const PairDev &P = w.P;
+    const int2 in = P.inner[k];
+    if (in.x < 0 || in.y < 0 || P.D[kpos] != P.D[in.y] + P.am_sscore[k]) return false;
+    const int start = w.ntok;
+    emit_inner(w, in.x, ends);
+    if (w.qtail < P.tq_cap)
+        P.tq[w.qtail] = make_int4(in.x, in.y, (ends.x + 1) | ((ends.z + 1) << 16), (ends.y - 1) | ((ends.w - 1) << 16));
+    else
+        w.ok = false;
+    ++w.qtail;
+    if (nseg < P.tq_cap + 1) P.segs[nseg] = make_int4(k, start, w.ntok, 0);
+    ++nseg;
+    return true;
 }
 
 // Walk back from (i,j) inside the rectangle with origin (al,bl) whose M is

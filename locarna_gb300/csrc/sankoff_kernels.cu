@@ -102,6 +102,14 @@ __global__ void __launch_bounds__(TRACE_WARPS * 32)
             qtail = __shfl_sync(0xffffffffu, w.qtail, 0);
             continue;
         }
+        if ((P.flags & (PF_STACK | PF_NOLP)) == PF_STACK) {
+            int stacked = 0;
+            if (lane == 0) stacked = trace_stack(w, k, kaux, ends, nseg);
+            if (__shfl_sync(0xffffffffu, stacked, 0)) {
+                qtail = __shfl_sync(0xffffffffu, w.qtail, 0);
+                continue;
+            }
+        }
         const int cpl = min(4, max(1, (min(ends.w - ends.z, P.maxband) + 31) / 32));
         run_group<false, false, false>(P, cpl, ends.x, ends.y, ends.z, ends.w, Mg, sw, sbase, rb, nullptr, 0,
                                        true, true, false, status, (volatile int *)&dummy_abort, nullptr);

@@ -278,7 +278,7 @@ __device__ void run_group_sl(const PairDev &P, int al, int ar, int bl, int br, i
                     const int c2 = e.z - bl;
                     const int mv = max(max(cur[0][c2], cur[1][c2]), max(cur[2][c2], cur[3][c2]));
                     int v = mv + e.w;
-                    if (P.flags & PF_NOLP) v = max(v, inner_term<WAIT>(P, dw + q, status, abort_flag));
+                    if (P.flags & (PF_NOLP | PF_STACK)) v = max(v, inner_term<WAIT>(P, dw + q, status, abort_flag));
                     st_volatile(P.D + e.x, norm(v));
                 }
                 const int cnt = __popc(__ballot_sync(0xffffffffu, mine));
@@ -508,6 +508,14 @@ __global__ void __launch_bounds__(TRACE_WARPS * 32)
             __syncwarp();
             qtail = __shfl_sync(0xffffffffu, w.qtail, 0);
             continue;
+        }
+        if ((P.flags & (PF_STACK | PF_NOLP)) == PF_STACK) {
+            int stacked = 0;
+            if (lane == 0) stacked = trace_stack(w, k, kpos, ends, nseg);
+            if (__shfl_sync(0xffffffffu, stacked, 0)) {
+                qtail = __shfl_sync(0xffffffffu, w.qtail, 0);
+                continue;
+            }
         }
         run_group_sl<false, false, 8>(P, ends.x, ends.y, ends.z, ends.w, Mg, scratch_stride, sw, sm, sw,
                                       nullptr, 0, status, (volatile int *)&dummy_abort);

@@ -21,6 +21,7 @@ class lcg_prep_opts(C.Structure):
         ("max_diff_am", C.c_int32), ("max_diff_at_am", C.c_int32),
         ("temperature_alipf", C.c_int32), ("sequ_local", C.c_int32),
         ("free_endgaps", C.c_int32), ("pf_precision", C.c_int32), ("exp_prob", C.c_double),
+        ("stacking", C.c_int32), ("new_stacking", C.c_int32),
     ]
 
 
@@ -135,7 +136,10 @@ def _tables_of(lib, h):
         n, m, _arr(t.sigma, (n + 1) * (m + 1)), _arr(t.gap_a, n + 1), _arr(t.gap_b, m + 1),
         t.indel_opening, t.exclusion, _arr(t.arcs_a, 2 * na), _arr(t.arcs_b, 2 * nb),
         _arr(t.am_arcs, 2 * nam), _arr(t.am_score, nam), _arr(t.min_col, n + 1), _arr(t.max_col, n + 1),
-        seq_a=lib.lcg_prepared_sequence(h, 0).decode(), seq_b=lib.lcg_prepared_sequence(h, 1).decode())
+        seq_a=lib.lcg_prepared_sequence(h, 0).decode(), seq_b=lib.lcg_prepared_sequence(h, 1).decode(),
+        am_stack_score=_arr(t.am_stack_score, nam) if t.am_stack_score else None,
+        am_stackable=(np.ctypeslib.as_array(t.am_stackable, shape=(nam,)).copy() if nam else np.zeros(0, np.uint8))
+        if t.am_stack_score else None)
     pt.name_a = lib.lcg_prepared_sequence(h, 2).decode()
     pt.name_b = lib.lcg_prepared_sequence(h, 3).decode()
     pt.envelope_ok = bool(lib.lcg_prepared_envelope_ok(h))

@@ -33,15 +33,44 @@ def _randint(rng, lo, hi):
 class RnaRecord:
     """One synthetic RNA: name, sequence and sparse base-pair probabilities."""
 
-    def __init__(self, name, seq, pairs):
+    def __init__(self, name, seq, pairs, seed=0):
         self.name = name
         self.seq = seq
         self.pairs = pairs  # dict (i, j) -> p, 1-based, i < j
+        self.seed = seed
 
-    def to_pp(self):
-        lines = ["#PP 2.0", "", f"{self.name} {self.seq}", "", "#END", "", "#SECTION BASEPAIRS", ""]
+    def stack_probs(self):
+        """Joint probabilities p2 of (i,j) and (i+1,j-1) for the pairs whose
+        inner pair is listed (the fourth column of a PP base-pair line,
+        rna_data.cc:1085-1094): p2 = min(p, p_inner) * U(0.2, 1); one pair in
+        ten gets a p2 below the default cutoff (dropped by the reader) and one
+        in ten none at all. Drawn from a generator of its own, so the
+        sequence and the pairs do not depend on it."""
+        rng = random.Random(self.seed * 7919 + 17)
+        out = {}
         for (i, j) in sorted(self.pairs):
-            lines.append(f"{i} {j} {self.pairs[(i, j)]:.6f}")
+            pin = self.pairs.get((i + 1, j - 1))
+            u = rng.random()
+            if pin is None or u < 0.1:
+                continue
+            if u < 0.2:
+                out[(i, j)] = 0.0005
+            else:
+                out[(i, j)] = round(min(self.pairs[(i, j)], pin) * (0.2 + 0.8 * rng.random()), 6)
+        return out
+
+    def to_pp(self, stacking=False):
+        """PP 2.0 text; with ``stacking`` the base-pair section carries the
+        #STACK keyword and p2 columns (stack_probs)."""
+        lines = ["#PP 2.0", "", f"{self.name} {self.seq}", "", "#END", "", "#SECTION BASEPAIRS", ""]
+        st = self.stack_probs() if stacking else {}
+        if stacking:
+            lines.append("#STACK")
+        for (i, j) in sorted(self.pairs):
+            if (i, j) in st:
+                lines.append(f"{i} {j} {self.pairs[(i, j)]:.6f} {st[(i, j)]:.6f}")
+            else:
+                lines.append(f"{i} {j} {self.pairs[(i, j)]:.6f}")
         lines += ["", "#END", ""]
         return "\n".join(lines)
 
@@ -102,7 +131,37 @@ def make_rna(length, seed, name=None, q=0.05, stems=None, min_prob=0.001):
             pairs[(i, j)] = round(p, 6)
 
     pairs = {k: v for k, v in pairs.items() if v > min_prob}
-    return RnaRecord(name or f"rna{seed}", "".join(seq), pairs)
+    return RnaRecord(name or f"rna{seed}", "".join(seq), pairs, seed=seed)
+
+
+def make_homolog(rec, seed, sub_rate=0.1, name=None):
+    """A related RNA: ``rec`` with point substitutions (rate ``sub_rate``;
+    both bases of a paired position are redrawn as a canonical pair, so the
+    structure is kept) and every pair probability scaled by U(0.7, 1.3),
+    capped at 0.99. Pairs whose written value drops to <= 0.001 are left out."""
+    rng = random.Random(seed)
+    seq = list(rec.seq)
+    partner = {}
+    for (i, j), p in rec.pairs.items():
+        if p >= 0.5:
+            partner[i], partner[j] = j, i
+    for pos in range(1, len(seq) + 1):
+        if rng.random() >= sub_rate:
+            continue
+        if pos in partner:
+            a, b = min(pos, partner[pos]), max(pos, partner[pos])
+            x, y = _CANON_LIST[_randint(rng, 0, 5)]
+            seq[a - 1], seq[b - 1] = x, y
+        else:
+            seq[pos - 1] = ("A", "C", "G", "U")[_randint(rng, 0, 3)]
+    pairs = {}
+    for (i, j) in sorted(rec.pairs):
+        if (seq[i - 1], seq[j - 1]) not in CANONICAL:
+            continue
+        p = round(min(0.99, rec.pairs[(i, j)] * (0.7 + 0.6 * rng.random())), 6)
+        if p > 0.001:
+            pairs[(i, j)] = p
+    return RnaRecord(name or f"{rec.name}_h{seed}", "".join(seq), pairs, seed=seed)
 
 
 def make_family(count, len_lo, len_hi, seed, q=0.05):

@@ -15,7 +15,7 @@
 // Usage: ref_harness A.pp B.pp [key=value ...]
 //   struct_local=0|1 sequ_local=0|1 no_lonely_pairs=0|1 free_endgaps=---- min_trace_prob=1e-4
 //   max_diff=-1 min_prob=0.001 indel=-150 indel_opening=-750 struct_weight=200
-//   tau=50 exclusion=0 dump_tables=1 repeat=1
+//   tau=50 exclusion=0 stacking=0|1 new_stacking=0|1 exp_prob=P dump_tables=1 repeat=1
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -51,6 +51,8 @@ struct Opts {
     double min_trace_prob = 1e-4, min_prob = 0.001;
     int max_diff = -1, indel = -150, indel_opening = -750, struct_weight = 200,
         tau = 50, exclusion = 0, max_diff_am = -1, max_diff_at_am = -1;
+    bool stacking = false, new_stacking = false;
+    double exp_prob = -1;  // --exp-prob; < 0: not given
     bool dump_tables = true;
     int repeat = 1;
 };
@@ -75,6 +77,9 @@ static void parse(Opts &o, const char *kv) {
     else if (k == "tau") o.tau = std::atoi(v.c_str());
     else if (k == "exclusion") o.exclusion = std::atoi(v.c_str());
     else if (k == "dump_tables") o.dump_tables = std::atoi(v.c_str());
+    else if (k == "stacking") o.stacking = std::atoi(v.c_str());
+    else if (k == "new_stacking") o.new_stacking = std::atoi(v.c_str());
+    else if (k == "exp_prob") o.exp_prob = std::atof(v.c_str());
     else if (k == "repeat") o.repeat = std::atoi(v.c_str());
     else { std::cerr << "unknown option " << k << "\n"; std::exit(2); }
 }
@@ -91,8 +96,12 @@ int main(int argc, char **argv) {
 
     // ribosum as in MainHelper::init_ribo_matrix (main_helper.icc:251-279)
     auto ribosum = std::make_unique<Ribosum85_60>();
+    // locarna turns the (old) stacking off unless --exp-prob is given
+    // (src/locarna.cc:407-414)
+    if (o.stacking && o.exp_prob < 0) o.stacking = false;
+    const bool stacking = o.stacking || o.new_stacking;
     PFoldParams pfoldparams(PFoldParams::args::noLP(false),
-                            PFoldParams::args::stacking(false),
+                            PFoldParams::args::stacking(stacking),
                             PFoldParams::args::max_bp_span(-1));
     RnaData rnaA(argv[1], o.min_prob, 0.0, pfoldparams);
     RnaData rnaB(argv[2], o.min_prob, 0.0, pfoldparams);
@@ -128,9 +137,10 @@ int main(int argc, char **argv) {
         ScoringParams::ribosum(ribosum.get()), ScoringParams::ribofit(nullptr),
         ScoringParams::unpaired_penalty(0), ScoringParams::struct_weight(o.struct_weight),
         ScoringParams::tau_factor(o.tau), ScoringParams::exclusion(o.exclusion),
-        ScoringParams::exp_probA(prob_exp_f(lenA)), ScoringParams::exp_probB(prob_exp_f(lenB)),
-        ScoringParams::temperature_alipf(300), ScoringParams::stacking(false),
-        ScoringParams::new_stacking(false), ScoringParams::mea_scoring(false),
+        ScoringParams::exp_probA(o.exp_prob >= 0 ? o.exp_prob : prob_exp_f(lenA)),
+        ScoringParams::exp_probB(o.exp_prob >= 0 ? o.exp_prob : prob_exp_f(lenB)),
+        ScoringParams::temperature_alipf(300), ScoringParams::stacking(o.stacking),
+        ScoringParams::new_stacking(o.new_stacking), ScoringParams::mea_scoring(false),
         ScoringParams::mea_alpha(0), ScoringParams::mea_beta(200),
         ScoringParams::mea_gamma(100), ScoringParams::probability_scale(10000));
     Scoring scoring(seqA, seqB, rnaA, rnaB, am, nullptr, sp);
@@ -167,6 +177,14 @@ int main(int argc, char **argv) {
             const ArcMatch &x = am.arcmatch(k);
             std::printf(" %zu:%zu:%ld", x.arcA().idx(), x.arcB().idx(), (long)scoring.arcmatch(x));
         }
+        if (stacking) {
+            // Scoring::arcmatch(am, true) and Scoring::is_stackable_am per arc match
+            std::printf("\namstack");
+            for (size_t k = 0; k < am.num_arc_matches(); ++k) {
+                const ArcMatch &x = am.arcmatch(k);
+                std::printf(" %ld:%d", (long)scoring.arcmatch(x, true), (int)scoring.is_stackable_am(x));
+            }
+        }
         std::printf("\nanchor_match");
         for (size_t i = 1; i <= lenA; ++i) {
             long lo = -1, hi = -2;
@@ -188,7 +206,7 @@ int main(int argc, char **argv) {
             AlignerParams::struct_local(o.struct_local), AlignerParams::sequ_local(o.sequ_local),
             AlignerParams::free_endgaps(FreeEndgaps(o.free_endgaps)),
             AlignerParams::max_diff_am(o.max_diff_am), AlignerParams::max_diff_at_am(o.max_diff_at_am),
-            AlignerParams::trace_controller(&tc), AlignerParams::stacking(false),
+            AlignerParams::trace_controller(&tc), AlignerParams::stacking(stacking),
             AlignerParams::constraints(&anchors)));
         score = aligner.align();
         aligner.trace();

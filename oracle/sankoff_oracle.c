@@ -79,6 +79,16 @@ static inline int a_ins(const Ctx *c, int i, int j) {
     return !c->t->ins_lo || (c->t->ins_lo[j] <= i && i <= c->t->ins_hi[j]);
 }
 static inline sc_t sigma(const Ctx *c, int i, int j) { return c->t->sigma[(size_t)i * (c->m + 1) + j]; }
+/* Scoring::stacking() (scoring.hh:653) */
+static inline int stacking(const Ctx *c) { return c->t->am_stack_score != NULL; }
+/* Scoring::arcmatch(am, true); LCG_STACK_NONE (a score outside the table
+ * range, only from an undefined zero-probability weight) as -infinity */
+static inline sc_t stack_score(const Ctx *c, int k) {
+    int32_t v = c->t->am_stack_score[k];
+    return v <= LCG_STACK_NONE ? NEG_INF : v;
+}
+/* Scoring::arcmatch(am, scoring->stacking()) */
+static inline sc_t am_score_st(const Ctx *c, int k) { return stacking(c) ? stack_score(c, k) : c->t->am_score[k]; }
 
 /* ---------------------------------------------------------------- setup */
 
@@ -299,7 +309,8 @@ static void align_in_arcmatch(Ctx *c, int al, int ar, int bl, int br, int excl, 
 #undef ROWS_END
 }
 
-/* AlignerImpl::fill_D_entries, aligner.cc:574-610 (no stacking) */
+/* AlignerImpl::fill_D_entries, aligner.cc:574-610; with stacking the arc
+ * match may also stack on its inner arc match (:600-608) */
 static void fill_D_entries(Ctx *c, int al, int bl) {
     size_t q = (size_t)al * (c->m + 1) + bl;
     for (int p = c->cle_start[q]; p < c->cle_start[q + 1]; ++p) {
@@ -309,27 +320,34 @@ static void fill_D_entries(Ctx *c, int al, int bl) {
         sc_t mv = MM(c, 0, ar - 1, br - 1);
         if (c->o->struct_local)
             for (int s = 1; s < 4; ++s) mv = smax(mv, MM(c, s, ar - 1, br - 1));
-        DD(c, a, b) = norm(mv + c->t->am_score[k]);
+        sc_t d = mv + c->t->am_score[k];
+        int in = c->inner ? c->inner[k] : -1;
+        if (stacking(c) && in >= 0 && c->t->am_stackable[k]) {
+            int ia = c->t->am_arcs[2 * in], ib = c->t->am_arcs[2 * in + 1];
+            d = smax(d, DD(c, ia, ib) + stack_score(c, k));
+        }
+        DD(c, a, b) = norm(d);
     }
 }
 
-/* AlignerImpl::fill_D_entries_noLP, aligner.cc:612-657 (no stacking): the
- * arc matches with left ends (al-1,bl-1) that enclose an inner arc match
- * (left ends (al,bl), right ends one less) take the better of the inner arc
- * match's own D and the inner interior plus the inner arc-match score */
+/* AlignerImpl::fill_D_entries_noLP, aligner.cc:612-657: the arc matches
+ * with left ends (al-1,bl-1) that enclose an inner arc match (left ends
+ * (al,bl), right ends one less; with stacking, only stackable ones) take the
+ * better of the inner arc match's own D and the inner interior plus the
+ * inner arc-match score, plus their own (stacked) score */
 static void fill_D_entries_noLP(Ctx *c, int al, int bl) {
     size_t q = (size_t)(al - 1) * (c->m + 1) + (bl - 1);
     for (int p = c->cle_start[q]; p < c->cle_start[q + 1]; ++p) {
         int k = c->cle[p];
         int in = c->inner[k];
-        if (in < 0) continue;
+        if (in < 0 || (stacking(c) && !c->t->am_stackable[k])) continue;
         int a = c->t->am_arcs[2 * k], b = c->t->am_arcs[2 * k + 1];
         int ar = arcR(c->t->arcs_a, a) - 1, br = arcR(c->t->arcs_b, b) - 1;
         sc_t mv = MM(c, 0, ar - 1, br - 1);
         if (c->o->struct_local)
             for (int s = 1; s < 4; ++s) mv = smax(mv, MM(c, s, ar - 1, br - 1));
         int ia = c->t->am_arcs[2 * in], ib = c->t->am_arcs[2 * in + 1];
-        DD(c, a, b) = norm(smax(mv + c->t->am_score[in], DD(c, ia, ib)) + c->t->am_score[k]);
+        DD(c, a, b) = norm(smax(mv + c->t->am_score[in], DD(c, ia, ib)) + am_score_st(c, k));
     }
 }
 
@@ -449,11 +467,24 @@ static void append(Ctx *c, int a, int b) {
 
 static void trace_in_arcmatch(Ctx *c, int state, int al, int i, int bl, int j, int tl);
 
-/* AlignerImpl::trace_arcmatch, aligner.cc:967-1028 (no stacking) */
+/* AlignerImpl::trace_arcmatch, aligner.cc:967-1028 */
 static void trace_arcmatch(Ctx *c, int k) {
     int a = c->t->am_arcs[2 * k], b = c->t->am_arcs[2 * k + 1];
     int al = arcL(c->t->arcs_a, a), ar = arcR(c->t->arcs_a, a);
     int bl = arcL(c->t->arcs_b, b), br = arcR(c->t->arcs_b, b);
+    int in = c->inner ? c->inner[k] : -1;
+    if (stacking(c) && in >= 0) {
+        /* stacked on the inner arc match (aligner.cc:986-1006) */
+        int ia = c->t->am_arcs[2 * in], ib = c->t->am_arcs[2 * in + 1];
+        if (DD(c, a, b) == DD(c, ia, ib) + stack_score(c, k)) {
+            if (c->ntam < c->tam_cap) c->tam[c->ntam] = in;
+            c->ntam++;
+            append(c, arcL(c->t->arcs_a, ia), arcL(c->t->arcs_b, ib));
+            trace_arcmatch(c, in);
+            append(c, arcR(c->t->arcs_a, ia), arcR(c->t->arcs_b, ib));
+            return;
+        }
+    }
     align_in_arcmatch(c, al, ar, bl, br, c->o->struct_local, 0);
     if (!c->o->struct_local) {
         trace_in_arcmatch(c, 0, al, ar - 1, bl, br - 1, 0);
@@ -467,7 +498,7 @@ static void trace_arcmatch(Ctx *c, int k) {
     }
 }
 
-/* AlignerImpl::trace_arcmatch_noLP, aligner.cc:1030-1079 (no stacking):
+/* AlignerImpl::trace_arcmatch_noLP, aligner.cc:1030-1079:
  * the inner arc match is part of the alignment; below it, either the inner
  * arc match's own stack continues (D(am) = D(inner) + score(am)) or its
  * interior is recomputed and traced */
@@ -480,7 +511,7 @@ static void trace_arcmatch_noLP(Ctx *c, int k) {
     if (c->ntam < c->tam_cap) c->tam[c->ntam] = in;
     c->ntam++;
     append(c, ial, ibl);
-    if (DD(c, a, b) == DD(c, ia, ib) + c->t->am_score[k]) {
+    if (DD(c, a, b) == DD(c, ia, ib) + am_score_st(c, k)) {
         trace_arcmatch_noLP(c, in);
     } else {
         align_in_arcmatch(c, ial, iar, ibl, ibr, c->o->struct_local, 0);
@@ -488,7 +519,7 @@ static void trace_arcmatch_noLP(Ctx *c, int k) {
             trace_in_arcmatch(c, 0, ial, iar - 1, ibl, ibr - 1, 0);
         } else {
             for (int s = 0; s < 4; ++s) {
-                if (DD(c, a, b) == MM(c, s, iar - 1, ibr - 1) + c->t->am_score[k] + c->t->am_score[in]) {
+                if (DD(c, a, b) == MM(c, s, iar - 1, ibr - 1) + am_score_st(c, k) + c->t->am_score[in]) {
                     trace_in_arcmatch(c, s, ial, iar - 1, ibl, ibr - 1, 0);
                     break;
                 }
@@ -637,7 +668,7 @@ int lcg_oracle_align(const lcg_pair_tables *t, const lcg_align_opts *o,
     build_radj(t->arcs_a, t->num_arcs_a, c.n, &c.radjA_start, &c.radjA);
     build_radj(t->arcs_b, t->num_arcs_b, c.m, &c.radjB_start, &c.radjB);
     build_am_lists(&c);
-    init_inner(&c);
+    if (o->no_lonely_pairs || t->am_stack_score) init_inner(&c);
     size_t nd = (size_t)t->num_arcs_a * t->num_arcs_b;
     c.D = malloc((nd > 0 ? nd : 1) * sizeof(sc_t));
     for (size_t q = 0; q < nd; ++q) c.D[q] = NEG_INF;

@@ -20,12 +20,13 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.dirname(HERE))
 
-from locarna_gb300.synth import make_rna  # noqa: E402
+from locarna_gb300.synth import make_homolog, make_rna  # noqa: E402
 from refdump import parse_ref  # noqa: E402
 
 HARNESS = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
 
-# name: (lenA, seedA, lenB, seedB, options, keep_tables)
+# name: (lenA, seedA, lenB, seedB, options, keep_tables); lenB = "h" makes B a
+# homolog of A (make_homolog with seed seedB)
 CASES = {
     "c150_global": (150, 1, 150, 2, {}, True),
     "c150_seqlocal": (150, 1, 150, 2, {"sequ_local": "1"}, True),
@@ -48,23 +49,48 @@ CASES = {
     "c150_nolp_freeall": (150, 1, 150, 2, {"no_lonely_pairs": "1", "free_endgaps": "++++"}, True),
     "c120_nolp_opening0": (120, 21, 130, 22, {"no_lonely_pairs": "1", "indel_opening": "0"}, True),
     "c300_nolp": (300, 61, 280, 62, {"no_lonely_pairs": "1"}, True),
+    # locarna --stacking / --new-stacking: PP inputs with #STACK joint probabilities
+    "c150_stack": (150, 1, 150, 2, {"stacking": "1", "exp_prob": "0.005"}, True),
+    "c150_newstack": (150, 1, 150, 2, {"new_stacking": "1"}, True),
+    "c150_bothstack": (150, 1, 150, 2, {"stacking": "1", "new_stacking": "1", "exp_prob": "0.005"}, True),
+    "c150_stack_noexp": (150, 1, 150, 2, {"stacking": "1"}, True),
+    "c150_stack_nolp": (150, 1, 150, 2, {"stacking": "1", "exp_prob": "0.005", "no_lonely_pairs": "1"}, True),
+    "c150_stack_structlocal": (150, 1, 150, 2, {"stacking": "1", "exp_prob": "0.005", "struct_local": "1"}, True),
+    "c150_newstack_nolp_sl": (150, 11, 140, 12, {"new_stacking": "1", "no_lonely_pairs": "1",
+                                                 "struct_local": "1"}, True),
+    "c120_stack_seqlocal": (120, 21, 130, 22, {"stacking": "1", "exp_prob": "0.01", "sequ_local": "1"}, True),
+    "c250_newstack_b": (250, 71, 240, 72, {"new_stacking": "1"}, True),
+    # homologous pairs (shared stems): most of the structure is aligned
+    "h150_global": (150, 81, "h", 82, {}, True),
+    "h150_nolp": (150, 81, "h", 82, {"no_lonely_pairs": "1"}, True),
+    "h150_stack": (150, 81, "h", 82, {"stacking": "1", "exp_prob": "0.005"}, True),
+    "h150_newstack_nolp": (150, 81, "h", 82, {"new_stacking": "1", "no_lonely_pairs": "1"}, True),
+    "h200_bothstack_sl": (200, 83, "h", 84, {"stacking": "1", "new_stacking": "1", "exp_prob": "0.004",
+                                             "struct_local": "1"}, True),
+    "h180_nolp_sl": (180, 85, "h", 86, {"no_lonely_pairs": "1", "struct_local": "1"}, True),
+    "h160_stack_nolp_seqlocal": (160, 87, "h", 88, {"stacking": "1", "exp_prob": "0.006",
+                                                    "no_lonely_pairs": "1", "sequ_local": "1"}, True),
 }
+
+STACK_KEYS = ("stacking", "new_stacking")
 
 
 def make_case(name, spec, workdir):
     la, sa, lb, sb, opts, keep = spec
-    ra, rb = make_rna(la, sa), make_rna(lb, sb)
+    ra = make_rna(la, sa)
+    rb = make_homolog(ra, sb) if lb == "h" else make_rna(lb, sb)
+    st = any(k in opts for k in STACK_KEYS)  # inputs with joint (stacking) probabilities
     pa, pb = os.path.join(workdir, name + "_A.pp"), os.path.join(workdir, name + "_B.pp")
     with open(pa, "w") as f:
-        f.write(ra.to_pp())
+        f.write(ra.to_pp(stacking=st))
     with open(pb, "w") as f:
-        f.write(rb.to_pp())
+        f.write(rb.to_pp(stacking=st))
     args = [HARNESS, pa, pb] + [f"{k}={v}" for k, v in opts.items()]
     txt = subprocess.run(args, capture_output=True, text=True, check=True).stdout
     ref = parse_ref(txt)
     t = ref["tables"]
     out = {
-        "pp_a": ra.to_pp(), "pp_b": rb.to_pp(), "opts": json.dumps(opts),
+        "pp_a": ra.to_pp(stacking=st), "pp_b": rb.to_pp(stacking=st), "opts": json.dumps(opts),
         "score": ref["score"], "edges": np.array(ref["edges"], dtype=np.int32),
         "struct_a": ref["struct_a"], "struct_b": ref["struct_b"],
         "min_col": np.array(ref["min_col"], dtype=np.int32),
@@ -78,6 +104,9 @@ def make_case(name, spec, workdir):
         "am_arcs": t.am_arcs, "am_score": t.am_score,
         "sigma": t.sigma.astype(np.int16) if np.abs(t.sigma).max() < 32000 else t.sigma,
     }
+    if t.am_stack_score is not None:
+        out["am_stack_score"] = t.am_stack_score
+        out["am_stackable"] = t.am_stackable
     np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
     return ref
 
@@ -140,7 +169,7 @@ def make_pf_case(name, spec, workdir):
     ref, Z, am, bm = parse_pf(txt)
     t = ref["tables"]
     out = {
-        "pp_a": ra.to_pp(), "pp_b": rb.to_pp(), "opts": json.dumps(opts), "Z": Z,
+        "pp_a": ra.to_pp(stacking=st), "pp_b": rb.to_pp(stacking=st), "opts": json.dumps(opts), "Z": Z,
         "am": np.array([x[:4] for x in am], dtype=np.int32).reshape(-1, 4),
         "am_p": np.array([x[4] for x in am], dtype=np.float64),
         "bm": np.array([x[:2] for x in bm], dtype=np.int32).reshape(-1, 2),

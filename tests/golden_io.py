@@ -38,7 +38,9 @@ class Golden:
             n, m, z["sigma"].astype(np.int32), z["gap_a"], z["gap_b"],
             int(z["indel_opening"]), int(z["exclusion"]), z["arcs_a"], z["arcs_b"],
             z["am_arcs"], z["am_score"], self.min_col, self.max_col,
-            seq_a=self.seq_a, seq_b=self.seq_b)
+            seq_a=self.seq_a, seq_b=self.seq_b,
+            am_stack_score=z["am_stack_score"] if "am_stack_score" in z else None,
+            am_stackable=z["am_stackable"] if "am_stackable" in z else None)
 
     @property
     def struct_local(self):
@@ -83,7 +85,9 @@ class GoldenPF:
             n, m, z["sigma"].astype(np.int32), z["gap_a"], z["gap_b"],
             int(z["indel_opening"]), int(z["exclusion"]), z["arcs_a"], z["arcs_b"],
             z["am_arcs"], z["am_score"], self.min_col, self.max_col,
-            seq_a=self.seq_a, seq_b=self.seq_b)
+            seq_a=self.seq_a, seq_b=self.seq_b,
+            am_stack_score=z["am_stack_score"] if "am_stack_score" in z else None,
+            am_stackable=z["am_stackable"] if "am_stackable" in z else None)
 
     def am_by_ends(self):
         return {tuple(int(v) for v in e): float(p) for e, p in zip(self.am_ends, self.am_p)}

@@ -5,7 +5,7 @@ tables (``PairTables``) plus the reference's results.
 """
 import numpy as np
 
-from locarna_gb300.abi import PairTables
+from locarna_gb300.abi import LCG_STACK_NONE, PairTables
 
 
 def _pairs(tokens, conv=int):
@@ -38,9 +38,16 @@ def parse_ref(text):
         arcs_a = np.array(_pairs(rec["arcsA"]), dtype=np.int32).reshape(-1, 2)
         arcs_b = np.array(_pairs(rec["arcsB"]), dtype=np.int32).reshape(-1, 2)
         am = np.array(_pairs(rec["am"]), dtype=np.int32).reshape(-1, 3)
+        st = sst = None
+        if "amstack" in rec:
+            # the reference's 64-bit stacked scores; values outside the int32
+            # tables' range become LCG_STACK_NONE
+            raw = [tuple(int(x) for x in t.split(":")) for t in rec["amstack"]]
+            st = np.array([v if -(1 << 29) < v < (1 << 29) else LCG_STACK_NONE for v, _ in raw], dtype=np.int32)
+            sst = np.array([f for _, f in raw], dtype=np.uint8)
         out["tables"] = PairTables(
             n, m, sig, [int(x) for x in rec["gapA"]], [int(x) for x in rec["gapB"]],
             io, ex, arcs_a, arcs_b, am[:, :2], am[:, 2], out["min_col"], out["max_col"],
-            seq_a=rec["seqA"], seq_b=rec["seqB"])
+            seq_a=rec["seqA"], seq_b=rec["seqB"], am_stack_score=st, am_stackable=sst)
         out["anchor_match"] = _pairs(rec["anchor_match"])
     return out

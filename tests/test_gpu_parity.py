@@ -88,3 +88,39 @@ def test_gpu_no_lonely_pairs_matches_oracle(engine, mode):
         assert_same_result(res[k], ref, f"pair {k}")
         stacked += len(ref.traced_am)
     assert stacked > 0
+
+
+def _homolog_tables(prep_kw, count=4, length=140, seed=301):
+    """All pairs of a few RNAs and their homologs (shared stems), with #STACK
+    joint probabilities in the inputs."""
+    from locarna_gb300.prep import prepare_pair
+    from locarna_gb300.synth import make_homolog, make_rna
+    recs = []
+    for k in range(count):
+        r = make_rna(length + 7 * k, seed + k)
+        recs += [r, make_homolog(r, seed + 100 + k)]
+    pp = [r.to_pp(stacking=True) for r in recs]
+    return [prepare_pair(pp[a], pp[b], **prep_kw) for a in range(len(pp)) for b in range(a + 1, len(pp))]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prep_kw,mode", [
+    ({"stacking": 1, "exp_prob": 0.005}, {}),
+    ({"new_stacking": 1}, {"no_lonely_pairs": True}),
+    ({"stacking": 1, "new_stacking": 1, "exp_prob": 0.004}, {"struct_local": True}),
+    ({"stacking": 1, "exp_prob": 0.006}, {"sequ_local": True, "no_lonely_pairs": True}),
+    ({"new_stacking": 1}, {"struct_local": True, "no_lonely_pairs": True}),
+])
+def test_gpu_stacking_matches_oracle(engine, prep_kw, mode):
+    """locarna --stacking / --new-stacking (stacked arc-match scores in
+    fill_D_entries, fill_D_entries_noLP and trace_arcmatch): homologous pairs,
+    every pair bit-exact against the oracle."""
+    tables = _homolog_tables(prep_kw)
+    assert all(t.am_stack_score is not None for t in tables)
+    res = engine.align_pairs(tables, **mode)
+    traced = 0
+    for k, t in enumerate(tables):
+        ref = oracle_align(t, **mode)
+        assert_same_result(res[k], ref, f"pair {k}")
+        traced += len(ref.traced_am)
+    assert traced > 50

@@ -7,7 +7,8 @@ from golden_io import Golden, sankoff_golden_names as golden_names
 
 _OPT_MAP = {"sequ_local": ("sequ_local", int), "free_endgaps": ("free_endgaps", str),
             "min_trace_prob": ("min_trace_probability", float), "indel_opening": ("indel_opening", int),
-            "struct_local": None, "no_lonely_pairs": None}
+            "struct_local": None, "no_lonely_pairs": None, "stacking": ("stacking", int),
+            "new_stacking": ("new_stacking", int), "exp_prob": ("exp_prob", float)}
 
 
 def prep_kwargs(g):
@@ -36,3 +37,7 @@ def test_prep_matches_reference_tables(name):
     assert np.array_equal(t.arcs_a, r.arcs_a) and np.array_equal(t.arcs_b, r.arcs_b), "arcs differ"
     assert np.array_equal(t.am_arcs, r.am_arcs), "arc match list differs"
     assert np.array_equal(t.am_score, r.am_score), "arc match scores differ"
+    assert (t.am_stack_score is None) == (r.am_stack_score is None), "stacking on/off differs"
+    if r.am_stack_score is not None:
+        assert np.array_equal(t.am_stack_score, r.am_stack_score), "stacked arc match scores differ"
+        assert np.array_equal(t.am_stackable, r.am_stackable), "stackable flags differ"

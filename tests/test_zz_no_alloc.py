@@ -15,7 +15,8 @@ import pytest
 from golden_io import Golden
 from locarna_gb300.abi import lcg_align_opts, lcg_pair_tables, make_opts
 
-CASES = ["c150_global", "c120_opening0", "c200_global", "c150_freeright", "c150_nolp"]
+CASES = ["c150_global", "c120_opening0", "c200_global", "c150_freeright", "c150_nolp", "h150_stack",
+         "h150_newstack_nolp"]
 
 
 def _static_fn():
