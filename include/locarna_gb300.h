@@ -120,6 +120,18 @@ typedef struct lcg_align_opts {
      * traceback follows trace_arcmatch_noLP (aligner.cc:1030-1079). No
      * stacking terms. */
     int32_t no_lonely_pairs;
+    /* locarna --normalized L (Aligner::normalized_align, aligner.cc:1521-1588):
+     * sequence-local alignment maximising score / (length + L) by
+     * Dinkelbach iterations over the top level with every position penalised
+     * by the current ratio; the result score is that ratio (integer) and the
+     * traceback the last iteration's. Needs sequ_local, not struct_local. */
+    int32_t normalized;
+    int32_t normalized_L;
+    /* locarna --penalized PP (Aligner::penalized_align, aligner.cc:1590-1617):
+     * the top level with every position penalised by PP; the result score is
+     * the penalised score. Not with normalized. */
+    int32_t penalized;
+    int32_t position_penalty;
 } lcg_align_opts;
 
 /*

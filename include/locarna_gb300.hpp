@@ -87,17 +87,23 @@ struct AlignerParams {
     std::string free_endgaps = "----";  // FreeEndgaps("abcd")
     bool do_trace = true;               // DO_TRACE
     bool no_lonely_pairs = false;       // no_lonely_pairs (locarna --noLP)
+    int normalized = -1;                // locarna --normalized L (-1 = off)
+    int penalized = -1;                 // locarna --penalized PP (-1 = off)
     AlignerParams &with_tables(const lcg_pair_tables *t) { tables = t; return *this; }
     AlignerParams &with_struct_local(bool v) { struct_local = v; return *this; }
     AlignerParams &with_sequ_local(bool v) { sequ_local = v; return *this; }
     AlignerParams &with_free_endgaps(const std::string &v) { free_endgaps = v; return *this; }
     AlignerParams &with_do_trace(bool v) { do_trace = v; return *this; }
     AlignerParams &with_no_lonely_pairs(bool v) { no_lonely_pairs = v; return *this; }
+    AlignerParams &with_normalized(int L) { normalized = L; return *this; }
+    AlignerParams &with_penalized(int pp) { penalized = pp; return *this; }
     lcg_align_opts opts() const {
         int fe = 0;
         for (int k = 0; k < 4 && k < (int)free_endgaps.size(); ++k)
             if (free_endgaps[k] == '+') fe |= 1 << k;
-        return lcg_align_opts{struct_local, sequ_local, fe, do_trace, no_lonely_pairs};
+        return lcg_align_opts{struct_local, sequ_local, fe, do_trace, no_lonely_pairs,
+                              normalized >= 0, normalized >= 0 ? normalized : 0,
+                              penalized >= 0, penalized >= 0 ? penalized : 0};
     }
 };
 

@@ -37,7 +37,8 @@ class lcg_pair_tables(C.Structure):
 class lcg_align_opts(C.Structure):
     _fields_ = [("struct_local", C.c_int32), ("sequ_local", C.c_int32),
                 ("free_endgaps", C.c_int32), ("do_trace", C.c_int32),
-                ("no_lonely_pairs", C.c_int32)]
+                ("no_lonely_pairs", C.c_int32), ("normalized", C.c_int32), ("normalized_L", C.c_int32),
+                ("penalized", C.c_int32), ("position_penalty", C.c_int32)]
 
 
 class lcg_align_result(C.Structure):
@@ -194,7 +195,9 @@ class ResultBuffers:
 
 
 def make_opts(struct_local=False, sequ_local=False, free_endgaps="----", do_trace=True,
-              no_lonely_pairs=False):
+              no_lonely_pairs=False, normalized=None, penalized=None):
+    """lcg_align_opts; normalized = L of --normalized, penalized = PP of
+    --penalized (None = off)."""
     fe = 0
     if isinstance(free_endgaps, str):
         for k, ch in enumerate(free_endgaps[:4]):
@@ -203,4 +206,5 @@ def make_opts(struct_local=False, sequ_local=False, free_endgaps="----", do_trac
     else:
         fe = int(free_endgaps)
     return lcg_align_opts(int(bool(struct_local)), int(bool(sequ_local)), fe, int(bool(do_trace)),
-                          int(bool(no_lonely_pairs)))
+                          int(bool(no_lonely_pairs)), int(normalized is not None), int(normalized or 0),
+                          int(penalized is not None), int(penalized or 0))

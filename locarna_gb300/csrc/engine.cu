@@ -79,9 +79,18 @@ lcg_status prep_pair(const lcg_pair_tables &t, const lcg_align_opts &o, Prep &p)
     const bool stack = t.am_stack_score != nullptr;
     if (stack != (t.am_stackable != nullptr))
         return bad(LCG_ERR_ARG, "am_stack_score and am_stackable must be both set or both NULL");
+    // normalized and penalized alignment always trace (aligner.cc:1564,1614)
+    const bool traced = o.do_trace || o.normalized || o.penalized;
     p.flags = (o.sequ_local ? PF_SEQU_LOCAL : 0) | (anchors ? PF_ANCHORS : 0) |
-              (o.do_trace ? PF_TRACE : 0) | (o.struct_local ? PF_STRUCT_LOCAL : 0) | (nolp ? PF_NOLP : 0) |
+              (traced ? PF_TRACE : 0) | (o.struct_local ? PF_STRUCT_LOCAL : 0) | (nolp ? PF_NOLP : 0) |
               (stack ? PF_STACK : 0);
+    // src/locarna.cc:369-373, 428-446
+    if (o.normalized && o.penalized) return bad(LCG_ERR_ARG, "normalized and penalized alignment cannot be combined");
+    if (o.normalized && (!o.sequ_local || o.struct_local))
+        return bad(LCG_ERR_ARG, "normalized alignment needs sequ_local and no struct_local");
+    if (o.normalized && o.normalized_L < 0) return bad(LCG_ERR_ARG, "normalized alignment needs L >= 0");
+    if (o.penalized && (long long)std::llabs(o.position_penalty) * (n + m) >= (1ll << 26))
+        return bad(LCG_ERR_RANGE, "position penalty times (lenA + lenB) exceeds the device range");
     if (o.sequ_local && p.fe) return bad(LCG_ERR_ARG, "free end gaps cannot be combined with local alignment");
 
     // band: monotone, inside [0,m], rows non-empty and connected
@@ -528,6 +537,7 @@ struct Chunk {
     size_t off_ctrl = 0, down_begin = 0, down_end = 0;
     long long launches = 0;
     bool in_flight = false;
+    std::vector<long long> ratio;  // normalized alignment: the final score ratio per pair
 };
 
 // pairs per chunk: one chunk for small batches, else up to 8 chunks of at
@@ -541,6 +551,76 @@ int chunk_size(int npairs, int setting) {
 
 double ms_between(std::chrono::steady_clock::time_point a, std::chrono::steady_clock::time_point b) {
     return std::chrono::duration<double, std::milli>(b - a).count();
+}
+
+// Top levels of normalized and penalized alignment after the fill
+// (Aligner::normalized_align / penalized_align, aligner.cc:1527-1617): the top
+// level of every pair under the scoring modified by its penalty lam
+// (sankoff_top_kernel). Penalized: one pass with lam = PP. Normalized:
+// Dinkelbach iterations per pair, lam <- (score + length lam) / (length + L)
+// with length = (max_i - min_i + 1) + (max_j - min_j + 1) from a top-level
+// walk, until lam repeats; each iteration runs the pairs whose lam changed,
+// and the host reads their result words once per iteration. On return the
+// device holds each pair's final lam and top level, and *sel selects the
+// final traceback's penalties. Synchronises the stream once per iteration.
+lcg_status mod_top_levels(const lcg_align_opts *opts, Chunk &c, const PairDev *dpairs, int *dmod, int npairs,
+                          int *scratch, long long stride, int sw, int rb, bool sl, int *status, cudaStream_t st,
+                          TraceSel *sel) {
+    int *d_lam = dmod, *d_items = dmod + npairs, *d_res = dmod + 2 * npairs;
+    std::vector<int> lam(npairs, 0), items(npairs);
+    for (int q = 0; q < npairs; ++q) items[q] = q;
+    sel->lam = d_lam;
+    if (opts->penalized) {
+        std::fill(lam.begin(), lam.end(), opts->position_penalty);
+        CUDA_TRY(cudaMemcpyAsync(d_lam, lam.data(), 4ull * npairs, cudaMemcpyHostToDevice, st));
+        CUDA_TRY(cudaMemcpyAsync(d_items, items.data(), 4ull * npairs, cudaMemcpyHostToDevice, st));
+        CUDA_TRY(launch_top(dpairs, d_items, npairs, d_lam, rb, status, st));
+        c.launches += 1;
+        return LCG_OK;
+    }
+    const long long L = opts->normalized_L;
+    std::vector<long long> lambda(npairs, -1), nl(npairs, 0);
+    std::vector<int> res(5ull * npairs);
+    for (int iter = 0; !items.empty(); ++iter) {
+        if (iter > 100000) return fail(LCG_ERR_DEVICE, "normalized alignment: Dinkelbach iterations do not converge");
+        for (int q : items) {
+            lambda[q] = nl[q];
+            if (std::llabs(lambda[q]) * (c.prep[q].n + c.prep[q].m) >= (1ll << 26))
+                return fail(LCG_ERR_RANGE, "normalized alignment: score ratio times length exceeds the device range");
+            lam[q] = (int)lambda[q];
+        }
+        const int ni = (int)items.size();
+        CUDA_TRY(cudaMemcpyAsync(d_lam, lam.data(), 4ull * npairs, cudaMemcpyHostToDevice, st));
+        CUDA_TRY(cudaMemcpyAsync(d_items, items.data(), 4ull * ni, cudaMemcpyHostToDevice, st));
+        CUDA_TRY(launch_top(dpairs, d_items, ni, d_lam, rb, status, st));
+        TraceSel ts;
+        ts.items = d_items;
+        ts.nitems = ni;
+        ts.lam = d_lam;
+        ts.flags = TRACE_TOP_ONLY | (iter ? TRACE_KEEP_MIN : 0);
+        if (sl) CUDA_TRY(launch_sl_trace(dpairs, npairs, scratch, stride, sw, status, st, ts));
+        else CUDA_TRY(launch_trace(dpairs, npairs, scratch, stride, sw, rb, status, st, ts));
+        CUDA_TRY(launch_gather_res(dpairs, d_items, ni, d_res, st));
+        c.launches += 3;
+        CUDA_TRY(cudaMemcpyAsync(res.data(), d_res, 20ull * ni, cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaStreamSynchronize(st));
+        std::vector<int> still;
+        for (int k = 0; k < ni; ++k) {
+            const int q = items[k];
+            const int *r = &res[5ull * k];
+            if (r[R_SCORE] < MIN_FINITE) return fail(LCG_ERR_DEVICE, "normalized alignment: -inf top level");
+            const long long length = (long long)(r[R_MAXI] - r[R_MINI] + 1) + (r[R_MAXJ] - r[R_MINJ] + 1);
+            const long long score = (long long)r[R_SCORE] + length * lambda[q];
+            if (length + L <= 0)
+                return fail(LCG_ERR_ARG, "normalized alignment: empty alignment with L = 0 (division by zero)");
+            nl[q] = score / (length + L);
+            if (nl[q] != lambda[q]) still.push_back(q);
+        }
+        items.swap(still);
+    }
+    c.ratio.assign(lambda.begin(), lambda.end());
+    sel->flags = TRACE_KEEP_MIN;
+    return LCG_OK;
 }
 
 // Lay out, pack and enqueue one prepared chunk on its buffer set: one
@@ -619,6 +699,10 @@ lcg_status chunk_launch(lcg_engine e, const Slot &s, const lcg_pair_tables *all,
         o.tq = take(dev_only, 16ull * p.tq_cap);
         o.topM = take(dev_only, 4ull * (p.n + 1) * (p.m + 1));
     }
+    // normalized / penalized alignment: per pair its penalty, the selected
+    // pairs and their gathered result words
+    const bool modv = opts->normalized || opts->penalized;
+    const size_t off_mod = modv ? take(dev_only, 4ull * 7 * npairs) : 0;
     size_t total = dev_only;
 
     if (total > *s.arena_cap) {
@@ -808,13 +892,19 @@ lcg_status chunk_launch(lcg_engine e, const Slot &s, const lcg_pair_tables *all,
     }
     CUDA_TRY(cudaEventRecord(s.ev1, st));
     c.launches = 1;
-    if (opts->do_trace) {
+    TraceSel sel;
+    if (modv) {
+        lcg_status ms = mod_top_levels(opts, c, (const PairDev *)(Dv + off_pairs), (int *)(Dv + off_mod), npairs,
+                                       scratch, stride, sw, rb, sl, status, st, &sel);
+        if (ms != LCG_OK) return ms;
+    }
+    if (opts->do_trace || modv) {
         if (sl)
             CUDA_TRY(launch_sl_trace((const PairDev *)(Dv + off_pairs), npairs, scratch, stride, sw,
-                                     status, st));
+                                     status, st, sel));
         else
             CUDA_TRY(launch_trace((const PairDev *)(Dv + off_pairs), npairs, scratch, stride, sw, rb, status,
-                                  st));
+                                  st, sel));
         ++c.launches;
     }
     CUDA_TRY(cudaEventRecord(s.ev2, st));
@@ -863,13 +953,15 @@ lcg_status chunk_finish(lcg_engine e, const Slot &s, const lcg_align_opts *opts,
         lcg_align_result &r = all_results[c.q0 + q];
         int sc = res[R_SCORE];
         r.score = sc < MIN_FINITE ? LCG_NEG_INF : (int64_t)sc;
+        if (opts->normalized) r.score = c.ratio[q];  // the normalized score (aligner.cc:1587)
+        const bool traced = opts->do_trace || opts->normalized || opts->penalized;
         r.max_i = res[R_MAXI];
         r.max_j = res[R_MAXJ];
-        r.min_i = opts->do_trace ? res[R_MINI] : 1;
-        r.min_j = opts->do_trace ? res[R_MINJ] : 1;
+        r.min_i = traced ? res[R_MINI] : 1;
+        r.min_j = traced ? res[R_MINJ] : 1;
         r.num_edges = 0;
         r.num_traced_am = 0;
-        if (!opts->do_trace) continue;
+        if (!traced) continue;
         Assembler as;
         as.tok = (const int2 *)(H + o.tok);
         int nseg = res[R_NSEG];
@@ -1017,7 +1109,10 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
     if (npairs == 0) return LCG_OK;
     CUDA_TRY(cudaSetDevice(e->device));
     using clk = std::chrono::steady_clock;
-    const int per = std::max(1, std::min<int>(npairs, chunk_size(npairs, e->chunk_pairs)));
+    // normalized / penalized alignment: one chunk (their top levels iterate
+    // with the host between launches)
+    const bool modv = opts->normalized || opts->penalized;
+    const int per = modv ? npairs : std::max(1, std::min<int>(npairs, chunk_size(npairs, e->chunk_pairs)));
     const int nchunks = (npairs + per - 1) / per;
     if (nchunks > 1) {
         lcg_status st = ensure_alt(e);

@@ -104,6 +104,20 @@ __device__ __forceinline__ int sigma_at(const PairDev &P, int i, int j) {
     return (P.flags & PF_SCLS) ? P.scls[P.rcls[i] * 16 + P.ccls[j]] : P.sigma[(size_t)i * (P.m + 1) + j];
 }
 
+// Selection and options of a traceback launch: items (NULL = every pair)
+// lists the pairs to trace; lam[pair] (NULL = 0) is the top level's penalty of
+// normalized / penalized alignment; TRACE_KEEP_MIN keeps the result words
+// min_i/min_j unless the walk sets them (the reference's members carry over
+// between the traces of Dinkelbach iterations); TRACE_TOP_ONLY walks the top
+// level only (enough for the end cells).
+enum TraceFlags : int { TRACE_KEEP_MIN = 1, TRACE_TOP_ONLY = 2 };
+struct TraceSel {
+    const int *items = nullptr;
+    int nitems = 0;
+    const int *lam = nullptr;
+    int flags = 0;
+};
+
 enum Res : int {
     R_SCORE = 0, R_MAXI, R_MAXJ, R_MINI, R_MINJ, R_NTOK, R_NSEG, R_NWORDS
 };

@@ -84,6 +84,8 @@ extern "C" lcg_status lcg_align_score_static(const lcg_pair_tables *pair, const 
     if (!pair || !opts || !score) return static_fail(LCG_ERR_ARG, "NULL argument");
     if (opts->struct_local) return static_fail(LCG_ERR_UNSUPPORTED, "static entry point: plain (non struct-local) mode only");
     if (opts->do_trace) return static_fail(LCG_ERR_UNSUPPORTED, "static entry point computes the score only (do_trace must be 0)");
+    if (opts->normalized || opts->penalized)
+        return static_fail(LCG_ERR_UNSUPPORTED, "static entry point: no normalized or penalized alignment");
     int dev = 0;
     STATIC_TRY(cudaGetDevice(&dev));
     char *base = nullptr;

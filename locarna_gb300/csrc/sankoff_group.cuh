@@ -85,13 +85,16 @@ __device__ __noinline__ int inner_term(const PairDev &P, const int4 *e, int *sta
 // consecutive columns (chunks of 32) for the affine recursion; the horizontal
 // gap chain is a max-plus warp scan. ANCH = false drops every anchor test and
 // uses plain (non-saturating) adds: without anchors every gap term is finite,
-// so no sum can leave the int32 range.
-template <int NCH, bool ANCH, bool SCLS, bool TOP, bool WAIT, bool DWRITE, bool COUNT>
+// so no sum can leave the int32 range. MOD: the scoring view of normalized and
+// penalized alignment (ModifiedScoringView, aligner_impl.hh:190-275) with
+// every position penalised by lam: sigma - 2 lam, gap costs - lam, arc-match
+// terms D(a,b) - lam (|a| + |b|) (the host bounds lam (n+m) below 2^27).
+template <int NCH, bool ANCH, bool SCLS, bool TOP, bool WAIT, bool DWRITE, bool COUNT, bool MOD = false>
 __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, int *__restrict__ Mg,
                             int pitch, int sbase, int ringn,
                             const int4 *__restrict__ dw, int ndw, bool globalA, bool globalB,
                             bool local_top, int *status, volatile int *abort_flag, TopOut *tout,
-                            unsigned long long *counters) {
+                            unsigned long long *counters, int lam = 0) {
     unsigned long long n_terms = 0, n_visits = 0;
     const int lane = threadIdx.x & 31;
     const int4 *__restrict__ rowinfo = P.rowinfo;
@@ -121,7 +124,9 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
     const int L0 = min(br, rowinfo[al].y + 1);
     // without anchors the column table holds the prefix sums
     // PA(j) = sum_{t<=j} (gapB(t) + gop); PA(bl) anchors the group's sums
-    const int PAbl = ANCH ? 0 : (P.gbc[bl] >> 4);
+    // MOD: the prefix sums of the penalised gap costs, PA(j) - lam j
+#define PAX(gbcv, jj) (((gbcv) >> 4) - (MOD ? lam * (jj) : 0))
+    const int PAbl = ANCH ? 0 : PAX(P.gbc[bl], bl);
     const int gdel = go - gop;
     {
         int carry = globalB ? go : 0;
@@ -134,7 +139,7 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
             int val;
             if (ANCH) {
                 bool blk = act && !a_ins(P, al, j);
-                int s = globalB ? gbcj >> 4 : 0;
+                int s = globalB ? (gbcj >> 4) - (MOD ? lam : 0) : 0;
                 unsigned bm = __ballot_sync(0xffffffffu, blk);
 #pragma unroll
                 for (int off = 1; off < 32; off <<= 1) {
@@ -147,7 +152,7 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
                 blocked_carry = blocked_carry || bm != 0;
             } else {
                 // go + sum_{bl<t<=j} gapB(t)
-                val = globalB ? go + (gbcj >> 4) - PAbl - (j - bl) * gop : 0;
+                val = globalB ? go + PAX(gbcj, j) - PAbl - (j - bl) * gop : 0;
             }
             if (act) {
                 PREV(j) = val;
@@ -187,7 +192,7 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
         anxt = rowarc[min(i + 1, P.n + 1)];
         if (SCLS) cnxt = P.rcls[min(i + 1, P.n + 1)];
         const int minc = rcur.x;
-        const int gAi = rcur.z;
+        const int gAi = rcur.z - (MOD ? lam : 0);
         const int lo = max(bl + 1, minc);
         const int hi = min(br - 1, rcur.y);
         const int *srow = sigma + (size_t)i * m1;
@@ -243,7 +248,9 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
             for (int u = 0; u < 2; ++u) {
                 if (ok[u]) {
                     if (WAIT && dv[u] == NOT_READY) dv[u] = wait_D(Dp, e0 + 32 * u + lane, status, abort_flag);
-                    atomicMax(&Arow[RG(en[u].y)], mv[u] + dv[u]);
+                    int term = mv[u] + dv[u];
+                    if (MOD) term -= lam * ((i - (en[u].x & 0xffff)) + (en[u].y - (en[u].x >> 16)));
+                    atomicMax(&Arow[RG(en[u].y)], term);
                 }
             }
             if (ball[0] != 0xffffffffu || ball[1] != 0xffffffffu) break;
@@ -267,7 +274,7 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
         // starting with k = lo-1 (column lo-1 > bl is in the ring: it is in
         // the band of an earlier row of the group)
         int Pc = 0;
-        if (!ANCH) Pc = B - (lo - 1 == bl ? PAbl : (gBs[RG(lo - 1)] >> 4));
+        if (!ANCH) Pc = B - (lo - 1 == bl ? PAbl : PAX(gBs[RG(lo - 1)], lo - 1));
         int k = 0;
         int rbase = RG(lo);  // ring index of column base, advanced by 32 per chunk
         for (int base = lo; base <= hi; base += 32, ++k) {
@@ -288,6 +295,7 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
                     if (k == kk) sgx = sgv[kk];
                 if (k >= NCH && act) sgx = srow[j];
             }
+            if (MOD) sgx -= 2 * lam;
             int X = NEG;
             if (act) {
                 const bool mok = !ANCH || a_match(P, i, j);
@@ -308,7 +316,7 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
                 int a = 0, b = NEG;
                 if (act) {
                     if (a_ins(P, i, j)) {
-                        const int gb = gbc >> 4;
+                        const int gb = (gbc >> 4) - (MOD ? lam : 0);
                         a = gb + gop;
                         b = addc(Xp, gb + go);
                     } else {
@@ -331,7 +339,7 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
                 // F(j) = max_{k<j} X(k) + go + sum_{k<t<=j} gapB(t)
                 //      = PA(j) + (go - gop) + max_{k<j} (X(k) - PA(k)),
                 // a prefix maximum over the lanes (inactive lanes: X = NEG)
-                const int pa = gbc >> 4;
+                const int pa = PAX(gbc, j);
                 const int v = X - pa;
                 int w = __shfl_up_sync(0xffffffffu, v, 1);
                 if (lane == 0) w = Pc;
@@ -394,6 +402,7 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
 #undef PREVR
 #undef CURR
 #undef RG
+#undef PAX
     if (TOP) {
         tout->best = best;
         tout->bi = bi;
@@ -421,29 +430,29 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
 // consecutive band rows. Gap costs stay below 2^27 (host check), so the
 // packed value does not overflow.
 // FAST: every pair of the launch has a sigma class table and no anchors.
-template <bool TOP, bool WAIT, bool DWRITE, bool COUNT = false, bool FAST = false>
+template <bool TOP, bool WAIT, bool DWRITE, bool COUNT = false, bool FAST = false, bool MOD = false>
 __device__ __forceinline__ void run_group(const PairDev &P, int cpl, int al, int ar, int bl, int br,
                                           int *__restrict__ Mg, int pitch, int sbase, int ringn,
                                           const int4 *__restrict__ dw, int ndw,
                                           bool globalA, bool globalB, bool local_top, int *status,
                                           volatile int *abort_flag, TopOut *tout,
-                                          unsigned long long *counters = nullptr) {
+                                          unsigned long long *counters = nullptr, int lam = 0) {
     if (FAST)
-        run_group_c<4, false, true, TOP, WAIT, DWRITE, COUNT>(P, al, ar, bl, br, Mg, pitch, sbase, ringn, dw, ndw,
+        run_group_c<4, false, true, TOP, WAIT, DWRITE, COUNT, MOD>(P, al, ar, bl, br, Mg, pitch, sbase, ringn, dw, ndw,
                                                               globalA, globalB, local_top, status, abort_flag,
-                                                              tout, counters);
+                                                              tout, counters, lam);
     else if (P.flags & PF_ANCHORS)
-        run_group_c<4, true, false, TOP, WAIT, DWRITE, COUNT>(P, al, ar, bl, br, Mg, pitch, sbase, ringn, dw, ndw,
+        run_group_c<4, true, false, TOP, WAIT, DWRITE, COUNT, MOD>(P, al, ar, bl, br, Mg, pitch, sbase, ringn, dw, ndw,
                                                               globalA, globalB, local_top, status, abort_flag,
-                                                              tout, counters);
+                                                              tout, counters, lam);
     else if (P.flags & PF_SCLS)
-        run_group_c<4, false, true, TOP, WAIT, DWRITE, COUNT>(P, al, ar, bl, br, Mg, pitch, sbase, ringn, dw, ndw,
+        run_group_c<4, false, true, TOP, WAIT, DWRITE, COUNT, MOD>(P, al, ar, bl, br, Mg, pitch, sbase, ringn, dw, ndw,
                                                               globalA, globalB, local_top, status, abort_flag,
-                                                              tout, counters);
+                                                              tout, counters, lam);
     else
-        run_group_c<4, false, false, TOP, WAIT, DWRITE, COUNT>(P, al, ar, bl, br, Mg, pitch, sbase, ringn, dw, ndw,
+        run_group_c<4, false, false, TOP, WAIT, DWRITE, COUNT, MOD>(P, al, ar, bl, br, Mg, pitch, sbase, ringn, dw, ndw,
                                                                globalA, globalB, local_top, status, abort_flag,
-                                                               tout, counters);
+                                                               tout, counters, lam);
 }
 
 static __device__ __forceinline__ void warp_argmax(int &v, int &k1, int &k2) {
@@ -464,19 +473,19 @@ static __device__ __forceinline__ void warp_argmax(int &v, int &k1, int &k2) {
 
 // top level + final argmax: align_top_level_free_endgaps (aligner.cc:736-819)
 // and align_top_level_locally (aligner.cc:823-880)
-template <bool COUNT, bool FAST = false>
+template <bool COUNT, bool FAST = false, bool MOD = false>
 __device__ __forceinline__ void run_top(const PairDev &P, int cpl, int sbase, int ringn,
                                      int *status, volatile int *abort_flag,
-                                     unsigned long long *counters) {
+                                     unsigned long long *counters, int lam = 0) {
     const int lane = threadIdx.x & 31;
     const int n = P.n, m = P.m, m1 = m + 1;
     const bool local = P.flags & PF_SEQU_LOCAL;
     const int fe = P.free_endgaps;
     TopOut to;
     if (local) {
-        run_group<true, true, false, COUNT, FAST>(P, cpl, 0, n + 1, 0, m + 1, P.topM, m1, sbase, ringn,
-                                            nullptr, 0, false, false, true, status, abort_flag,
-                                            &to, counters);
+        run_group<true, !MOD, false, COUNT, FAST, MOD>(P, cpl, 0, n + 1, 0, m + 1, P.topM, m1, sbase, ringn,
+                                                      nullptr, 0, false, false, true, status, abort_flag,
+                                                      &to, counters, lam);
         int v = to.best, i = to.bi, j = to.bj;
         if (v <= 0) {
             v = 0;
@@ -496,9 +505,9 @@ __device__ __forceinline__ void run_top(const PairDev &P, int cpl, int sbase, in
         }
         return;
     }
-    run_group<true, true, false, COUNT, FAST>(P, cpl, 0, n + 1, 0, m + 1, P.topM, m1, sbase, ringn,
-                                        nullptr, 0, !(fe & 4), !(fe & 1), false, status, abort_flag,
-                                        &to, counters);
+    run_group<true, !MOD, false, COUNT, FAST, MOD>(P, cpl, 0, n + 1, 0, m + 1, P.topM, m1, sbase, ringn,
+                                                  nullptr, 0, !(fe & 4), !(fe & 1), false, status, abort_flag,
+                                                  &to, counters, lam);
     __syncwarp();
     if (!(fe & (2 | 8))) {
         if (lane == 0) {
@@ -646,10 +655,13 @@ static __device__ __noinline__ bool trace_stack(Walker &w, int k, int kpos, int4
 
 // Walk back from (i,j) inside the rectangle with origin (al,bl) whose M is
 // Mg (pitch), emitting tokens in reverse append order. Arc-match tokens are
-// (-2, am); each traced arc match is queued for its own walk.
+// (-2, am); each traced arc match is queued for its own walk. On the top level
+// (tl) lam is the penalty of the modified scoring view of normalized and
+// penalized alignment (0 otherwise).
 static __device__ __noinline__ void walk(Walker &w, const int *Mg, int pitch, int al, int bl, int i, int j, bool tl,
-                     int *status) {
+                     int *status, int lam = 0) {
     const PairDev &P = w.P;
+    const int tlam = tl ? lam : 0;
     const bool local = P.flags & PF_SEQU_LOCAL;
     const int fe = P.free_endgaps;
     const int go = P.go;
@@ -672,7 +684,7 @@ static __device__ __noinline__ void walk(Walker &w, const int *Mg, int pitch, in
             return;
         }
         if (a_match(P, i, j) && w.valid(i - 1, j - 1) &&
-            Mij == MM(i - 1, j - 1) + sigma_at(P, i, j)) {
+            Mij == MM(i - 1, j - 1) + sigma_at(P, i, j) - 2 * tlam) {
             w.emit(i, j);
             --i;
             --j;
@@ -680,12 +692,12 @@ static __device__ __noinline__ void walk(Walker &w, const int *Mg, int pitch, in
         }
         bool found = false;
         if (go == 0) {
-            if (a_del(P, i, j) && w.valid(i - 1, j) && Mij == MM(i - 1, j) + P.gapA[i]) {
+            if (a_del(P, i, j) && w.valid(i - 1, j) && Mij == MM(i - 1, j) + P.gapA[i] - tlam) {
                 w.emit(i, -1);
                 --i;
                 continue;
             }
-            if (a_ins(P, i, j) && w.valid(i, j - 1) && Mij == MM(i, j - 1) + P.gapB[j]) {
+            if (a_ins(P, i, j) && w.valid(i, j - 1) && Mij == MM(i, j - 1) + P.gapB[j] - tlam) {
                 w.emit(-1, j);
                 --j;
                 continue;
@@ -694,7 +706,7 @@ static __device__ __noinline__ void walk(Walker &w, const int *Mg, int pitch, in
             int gap = go;
             for (int k = 1; i >= al + k && a_del(P, i - k + 1, j); ++k) {
                 if (!w.valid(i - k, j)) break;
-                gap += P.gapA[i - k + 1];
+                gap += P.gapA[i - k + 1] - tlam;
                 if (Mij == MM(i - k, j) + gap) {
                     for (int l = 1; l <= k; ++l) w.emit(i - l + 1, -1);
                     i -= k;
@@ -706,7 +718,7 @@ static __device__ __noinline__ void walk(Walker &w, const int *Mg, int pitch, in
             gap = go;
             for (int k = 1; j >= bl + k && a_ins(P, i, j - k + 1); ++k) {
                 if (!w.valid(i, j - k)) break;
-                gap += P.gapB[j - k + 1];
+                gap += P.gapB[j - k + 1] - tlam;
                 if (Mij == MM(i, j - k) + gap) {
                     for (int l = 1; l <= k; ++l) w.emit(-1, j - l + 1);
                     j -= k;
@@ -722,7 +734,7 @@ static __device__ __noinline__ void walk(Walker &w, const int *Mg, int pitch, in
             const int4 ent = P.cre[q];
             const int alq = ent.y + 1, blq = ent.z + 1;
             if (alq <= al || blq <= bl) continue;
-            if (Mij == MM(alq - 1, blq - 1) + P.D[ent.x]) {
+            if (Mij == MM(alq - 1, blq - 1) + P.D[ent.x] - tlam * ((i - alq + 1) + (j - blq + 1))) {
                 w.emit(i, j);
                 w.emit(-2, ent.w);
                 w.emit(alq, blq);

@@ -68,13 +68,15 @@ __global__ void __launch_bounds__(FILL_WARPS * 32, FILL_MIN_BLOCKS)
 
 __global__ void __launch_bounds__(TRACE_WARPS * 32)
     sankoff_trace_kernel(const PairDev *__restrict__ pairs, int npairs, int *scratch,
-                         long long scratch_stride, int sw, int rb, int *status) {
+                         long long scratch_stride, int sw, int rb, int *status, TraceSel sel) {
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
-    const int pair = blockIdx.x * TRACE_WARPS + warp;
-    if (pair >= npairs) return;
+    const int wi = blockIdx.x * TRACE_WARPS + warp;
+    if (wi >= (sel.items ? sel.nitems : npairs)) return;
+    const int pair = sel.items ? sel.items[wi] : wi;
     const PairDev &P = pairs[pair];
     if (!(P.flags & PF_TRACE)) return;
+    const int lam = sel.lam ? sel.lam[pair] : 0;
     const int sbase = warp * smem_warp_ints(rb);
     int *Mg = scratch + (long long)pair * scratch_stride;
     int dummy_abort = 0;
@@ -82,11 +84,14 @@ __global__ void __launch_bounds__(TRACE_WARPS * 32)
     int nseg = 0;
     int qhead = 0;
     if (lane == 0) {
-        P.res[R_MINI] = 1;
-        P.res[R_MINJ] = 1;
-        walk(w, P.topM, P.m + 1, 0, 0, P.res[R_MAXI], P.res[R_MAXJ], true, status);
+        if (!(sel.flags & TRACE_KEEP_MIN)) {
+            P.res[R_MINI] = 1;
+            P.res[R_MINJ] = 1;
+        }
+        walk(w, P.topM, P.m + 1, 0, 0, P.res[R_MAXI], P.res[R_MAXJ], true, status, lam);
         P.segs[nseg++] = make_int4(-1, 0, w.ntok, 0);
     }
+    if (sel.flags & TRACE_TOP_ONLY) return;
     int qtail = __shfl_sync(0xffffffffu, w.qtail, 0);
     while (qhead < qtail) {
         int4 qe = make_int4(-1, 0, 0, 0);
@@ -158,11 +163,62 @@ cudaError_t launch_fill(const PairDev *pairs, const int2 *queue, int nitems,
 }
 
 cudaError_t launch_trace(const PairDev *pairs, int npairs, int *scratch,
-                         long long scratch_stride, int sw, int rb, int *status, cudaStream_t st) {
+                         long long scratch_stride, int sw, int rb, int *status, cudaStream_t st, TraceSel sel) {
     size_t smem = (size_t)TRACE_WARPS * smem_warp_ints(rb) * sizeof(int);
-    int blocks = (npairs + TRACE_WARPS - 1) / TRACE_WARPS;
+    const int nw = sel.items ? sel.nitems : npairs;
+    if (nw <= 0) return cudaSuccess;
+    int blocks = (nw + TRACE_WARPS - 1) / TRACE_WARPS;
     sankoff_trace_kernel<<<blocks, TRACE_WARPS * 32, smem, st>>>(pairs, npairs, scratch,
-                                                                 scratch_stride, sw, rb, status);
+                                                                 scratch_stride, sw, rb, status, sel);
+    return cudaGetLastError();
+}
+
+// The top level alone under the modified scoring view of normalized and
+// penalized alignment (every position penalised by lam[pair]), one warp per
+// selected pair, after the fill kernel has made D final
+// (align_top_level_locally / _free_endgaps with a ModifiedScoringView,
+// aligner.cc:1561-1562, 1606-1610). Writes the pair's top-level matrix and
+// result words like the fill kernel's top item.
+__global__ void __launch_bounds__(TRACE_WARPS * 32)
+    sankoff_top_kernel(const PairDev *__restrict__ pairs, const int *__restrict__ items, int nitems,
+                       const int *__restrict__ lam, int rb, int *status) {
+    const int warp = threadIdx.x >> 5;
+    const int wi = blockIdx.x * TRACE_WARPS + warp;
+    if (wi >= nitems) return;
+    const int pair = items[wi];
+    const PairDev &P = pairs[pair];
+    int dummy_abort = 0;
+    run_top<false, false, true>(P, 1, warp * smem_warp_ints(rb), rb, status, (volatile int *)&dummy_abort,
+                                nullptr, lam[pair]);
+}
+
+// result words of the selected pairs, gathered for one device->host copy:
+// out[5 q + k] = res[k] of items[q], k = score, max_i, max_j, min_i, min_j
+__global__ void gather_res_kernel(const PairDev *__restrict__ pairs, const int *__restrict__ items, int nitems,
+                                  int *__restrict__ out) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nitems) return;
+    const int *r = pairs[items[q]].res;
+    for (int k = 0; k < 5; ++k) out[5 * q + k] = r[k];
+}
+
+cudaError_t launch_top(const PairDev *pairs, const int *items, int nitems, const int *lam, int rb, int *status,
+                       cudaStream_t st) {
+    if (nitems <= 0) return cudaSuccess;
+    size_t smem = (size_t)TRACE_WARPS * smem_warp_ints(rb) * sizeof(int);
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(sankoff_top_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    int blocks = (nitems + TRACE_WARPS - 1) / TRACE_WARPS;
+    sankoff_top_kernel<<<blocks, TRACE_WARPS * 32, smem, st>>>(pairs, items, nitems, lam, rb, status);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gather_res(const PairDev *pairs, const int *items, int nitems, int *out, cudaStream_t st) {
+    if (nitems <= 0) return cudaSuccess;
+    gather_res_kernel<<<(nitems + 127) / 128, 128, 0, st>>>(pairs, items, nitems, out);
     return cudaGetLastError();
 }
 

@@ -14,7 +14,12 @@ cudaError_t launch_fill(const PairDev *pairs, const int2 *queue, int nitems, int
                         long long scratch_stride, int sw, int rb, bool fast, unsigned int *qhead, int *status,
                         int *abort_flag, int blocks, cudaStream_t st, unsigned long long *counters);
 cudaError_t launch_trace(const PairDev *pairs, int npairs, int *scratch, long long scratch_stride, int sw, int rb,
-                         int *status, cudaStream_t st);
+                         int *status, cudaStream_t st, TraceSel sel = TraceSel());
+// the top level of the selected pairs under the scoring modified by lam[pair]
+cudaError_t launch_top(const PairDev *pairs, const int *items, int nitems, const int *lam, int rb, int *status,
+                       cudaStream_t st);
+// out[5 q + k] = result word k (score, max_i, max_j, min_i, min_j) of pair items[q]
+cudaError_t launch_gather_res(const PairDev *pairs, const int *items, int nitems, int *out, cudaStream_t st);
 cudaError_t fill_occupancy(int rb, bool counting, bool fast, int *blocks_per_sm);
 cudaError_t trace_prepare(int rb);
 int fill_warps_per_block();
@@ -25,6 +30,6 @@ cudaError_t launch_sl_fill(const PairDev *pairs, const int2 *queue, int nitems, 
                            long long scratch_stride, int sw, int rb, unsigned int *qhead, int *status,
                            int *abort_flag, int blocks, cudaStream_t st);
 cudaError_t launch_sl_trace(const PairDev *pairs, int npairs, int *scratch, long long scratch_stride, int sw,
-                            int *status, cudaStream_t st);
+                            int *status, cudaStream_t st, TraceSel sel = TraceSel());
 cudaError_t measure_int_peak(int sms, bool dpx, cudaStream_t st, double *gops);
 }  // namespace lcg

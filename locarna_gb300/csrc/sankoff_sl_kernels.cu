@@ -342,8 +342,9 @@ __global__ void __launch_bounds__(SL_FILL_WARPS * 32)
 // M of state s is Mg + s*mstride (the top level has only state NO_NO).
 static __device__ __noinline__ void walk_sl(Walker &w, const int *Mg, long long mstride, int pitch,
                                             int al, int bl, int state, int i, int j, bool tl,
-                                            int *status) {
+                                            int *status, int lam = 0) {
     const PairDev &P = w.P;
+    const int tlam = tl ? lam : 0;  // top level of normalized / penalized alignment
     const bool local = P.flags & PF_SEQU_LOCAL;
     const int fe = P.free_endgaps;
     const int go = P.go, X = P.excl;
@@ -403,7 +404,7 @@ static __device__ __noinline__ void walk_sl(Walker &w, const int *Mg, long long 
         if (!noex) return;
         // trace_noex (aligner.cc:1082-1229) in `state`
         if (a_match(P, i, j) && w.valid(i - 1, j - 1) &&
-            Mij == MS(state, i - 1, j - 1) + sigma_at(P, i, j)) {
+            Mij == MS(state, i - 1, j - 1) + sigma_at(P, i, j) - 2 * tlam) {
             w.emit(i, j);
             --i;
             --j;
@@ -411,12 +412,12 @@ static __device__ __noinline__ void walk_sl(Walker &w, const int *Mg, long long 
         }
         bool found = false;
         if (go == 0) {
-            if (a_del(P, i, j) && w.valid(i - 1, j) && Mij == MS(state, i - 1, j) + P.gapA[i]) {
+            if (a_del(P, i, j) && w.valid(i - 1, j) && Mij == MS(state, i - 1, j) + P.gapA[i] - tlam) {
                 w.emit(i, -1);
                 --i;
                 continue;
             }
-            if (a_ins(P, i, j) && w.valid(i, j - 1) && Mij == MS(state, i, j - 1) + P.gapB[j]) {
+            if (a_ins(P, i, j) && w.valid(i, j - 1) && Mij == MS(state, i, j - 1) + P.gapB[j] - tlam) {
                 w.emit(-1, j);
                 --j;
                 continue;
@@ -425,7 +426,7 @@ static __device__ __noinline__ void walk_sl(Walker &w, const int *Mg, long long 
             int gap = go;
             for (int k = 1; i >= al + k && a_del(P, i - k + 1, j); ++k) {
                 if (!w.valid(i - k, j)) break;
-                gap += P.gapA[i - k + 1];
+                gap += P.gapA[i - k + 1] - tlam;
                 if (Mij == MS(state, i - k, j) + gap) {
                     for (int l = 1; l <= k; ++l) w.emit(i - l + 1, -1);
                     i -= k;
@@ -437,7 +438,7 @@ static __device__ __noinline__ void walk_sl(Walker &w, const int *Mg, long long 
             gap = go;
             for (int k = 1; j >= bl + k && a_ins(P, i, j - k + 1); ++k) {
                 if (!w.valid(i, j - k)) break;
-                gap += P.gapB[j - k + 1];
+                gap += P.gapB[j - k + 1] - tlam;
                 if (Mij == MS(state, i, j - k) + gap) {
                     for (int l = 1; l <= k; ++l) w.emit(-1, j - l + 1);
                     j -= k;
@@ -453,7 +454,7 @@ static __device__ __noinline__ void walk_sl(Walker &w, const int *Mg, long long 
             const int4 ent = P.cre[q];
             const int alq = ent.y + 1, blq = ent.z + 1;
             if (alq <= al || blq <= bl) continue;
-            if (Mij == MS(state, alq - 1, blq - 1) + P.D[ent.x]) {
+            if (Mij == MS(state, alq - 1, blq - 1) + P.D[ent.x] - tlam * ((i - alq + 1) + (j - blq + 1))) {
                 w.emit(i, j);
                 w.emit(-2, ent.w);
                 w.emit(alq, blq);
@@ -474,14 +475,16 @@ static __device__ __noinline__ void walk_sl(Walker &w, const int *Mg, long long 
 
 __global__ void __launch_bounds__(TRACE_WARPS * 32)
     sankoff_sl_trace_kernel(const PairDev *__restrict__ pairs, int npairs, int *scratch,
-                            long long scratch_stride, int sw, int *status) {
+                            long long scratch_stride, int sw, int *status, TraceSel sel) {
     extern __shared__ int smem[];
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
-    const int pair = blockIdx.x * TRACE_WARPS + warp;
-    if (pair >= npairs) return;
+    const int wi = blockIdx.x * TRACE_WARPS + warp;
+    if (wi >= (sel.items ? sel.nitems : npairs)) return;
+    const int pair = sel.items ? sel.items[wi] : wi;
     const PairDev &P = pairs[pair];
     if (!(P.flags & PF_TRACE)) return;
+    const int lam = sel.lam ? sel.lam[pair] : 0;
     int *sm = smem + warp * SL_ROWS * sw;
     int *Mg = scratch + (long long)pair * scratch_stride * 8;
     int dummy_abort = 0;
@@ -489,11 +492,14 @@ __global__ void __launch_bounds__(TRACE_WARPS * 32)
     int nseg = 0;
     int qhead = 0;
     if (lane == 0) {
-        P.res[R_MINI] = 1;
-        P.res[R_MINJ] = 1;
-        walk_sl(w, P.topM, 0, P.m + 1, 0, 0, S_NO_NO, P.res[R_MAXI], P.res[R_MAXJ], true, status);
+        if (!(sel.flags & TRACE_KEEP_MIN)) {
+            P.res[R_MINI] = 1;
+            P.res[R_MINJ] = 1;
+        }
+        walk_sl(w, P.topM, 0, P.m + 1, 0, 0, S_NO_NO, P.res[R_MAXI], P.res[R_MAXJ], true, status, lam);
         P.segs[nseg++] = make_int4(-1, 0, w.ntok, 0);
     }
+    if (sel.flags & TRACE_TOP_ONLY) return;
     int qtail = __shfl_sync(0xffffffffu, w.qtail, 0);
     while (qhead < qtail) {
         int4 qe = make_int4(-1, 0, 0, 0);
@@ -576,11 +582,13 @@ cudaError_t launch_sl_fill(const PairDev *pairs, const int2 *queue, int nitems,
 }
 
 cudaError_t launch_sl_trace(const PairDev *pairs, int npairs, int *scratch,
-                            long long scratch_stride, int sw, int *status, cudaStream_t st) {
+                            long long scratch_stride, int sw, int *status, cudaStream_t st, TraceSel sel) {
     size_t smem = (size_t)TRACE_WARPS * SL_ROWS * sw * sizeof(int);
-    int blocks = (npairs + TRACE_WARPS - 1) / TRACE_WARPS;
+    const int nw = sel.items ? sel.nitems : npairs;
+    if (nw <= 0) return cudaSuccess;
+    int blocks = (nw + TRACE_WARPS - 1) / TRACE_WARPS;
     sankoff_sl_trace_kernel<<<blocks, TRACE_WARPS * 32, smem, st>>>(pairs, npairs, scratch,
-                                                                    scratch_stride, sw, status);
+                                                                    scratch_stride, sw, status, sel);
     return cudaGetLastError();
 }
 

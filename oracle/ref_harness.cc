@@ -15,7 +15,8 @@
 // Usage: ref_harness A.pp B.pp [key=value ...]
 //   struct_local=0|1 sequ_local=0|1 no_lonely_pairs=0|1 free_endgaps=---- min_trace_prob=1e-4
 //   max_diff=-1 min_prob=0.001 indel=-150 indel_opening=-750 struct_weight=200
-//   tau=50 exclusion=0 stacking=0|1 new_stacking=0|1 exp_prob=P dump_tables=1 repeat=1
+//   tau=50 exclusion=0 stacking=0|1 new_stacking=0|1 exp_prob=P normalized=L penalized=PP
+//   dump_tables=1 repeat=1
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -53,6 +54,7 @@ struct Opts {
         tau = 50, exclusion = 0, max_diff_am = -1, max_diff_at_am = -1;
     bool stacking = false, new_stacking = false;
     double exp_prob = -1;  // --exp-prob; < 0: not given
+    int normalized = -1, penalized = -1;  // --normalized L / --penalized PP (-1: off)
     bool dump_tables = true;
     int repeat = 1;
 };
@@ -80,6 +82,8 @@ static void parse(Opts &o, const char *kv) {
     else if (k == "stacking") o.stacking = std::atoi(v.c_str());
     else if (k == "new_stacking") o.new_stacking = std::atoi(v.c_str());
     else if (k == "exp_prob") o.exp_prob = std::atof(v.c_str());
+    else if (k == "normalized") o.normalized = std::atoi(v.c_str());
+    else if (k == "penalized") o.penalized = std::atoi(v.c_str());
     else if (k == "repeat") o.repeat = std::atoi(v.c_str());
     else { std::cerr << "unknown option " << k << "\n"; std::exit(2); }
 }
@@ -208,8 +212,16 @@ int main(int argc, char **argv) {
             AlignerParams::max_diff_am(o.max_diff_am), AlignerParams::max_diff_at_am(o.max_diff_at_am),
             AlignerParams::trace_controller(&tc), AlignerParams::stacking(stacking),
             AlignerParams::constraints(&anchors)));
-        score = aligner.align();
-        aligner.trace();
+        // src/locarna.cc:751-783: normalized and penalized alignment trace
+        // inside their own calls
+        if (o.normalized >= 0) {
+            score = aligner.normalized_align(o.normalized, false);
+        } else if (o.penalized >= 0) {
+            score = aligner.penalized_align(o.penalized);
+        } else {
+            score = aligner.align();
+            aligner.trace();
+        }
         auto t1 = std::chrono::steady_clock::now();
         best = std::min(best, std::chrono::duration<double>(t1 - t0).count());
         aln = std::make_unique<Alignment>(aligner.get_alignment());

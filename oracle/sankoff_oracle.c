@@ -46,6 +46,12 @@ typedef struct {
     int *cle_start, *cle;
     int *cre_start, *cre;
     int *inner;    /* per arc match: the inner arc match, or -1 */
+    /* ModifiedScoringView (aligner_impl.hh:190-275): with mod set, sigma -
+     * 2 lam, gaps - lam and D(a,b) - lam (|a| + |b|) (Scoring::
+     * modify_by_parameter, scoring.cc:77-90); used by the top level of
+     * normalized and penalized alignment */
+    sc_t lam;
+    int lam_on, mod;
     sc_t *D;       /* |arcsA| x |arcsB| */
     sc_t *M[8];    /* (n+1) x (m+1) */
     sc_t *E[4];    /* m+1 */
@@ -79,6 +85,12 @@ static inline int a_ins(const Ctx *c, int i, int j) {
     return !c->t->ins_lo || (c->t->ins_lo[j] <= i && i <= c->t->ins_hi[j]);
 }
 static inline sc_t sigma(const Ctx *c, int i, int j) { return c->t->sigma[(size_t)i * (c->m + 1) + j]; }
+static inline sc_t sigma_v(const Ctx *c, int i, int j) { return sigma(c, i, j) - (c->mod ? 2 * c->lam : 0); }
+static inline sc_t gapA_v(const Ctx *c, int i) { return c->t->gap_a[i] - (c->mod ? c->lam : 0); }
+static inline sc_t gapB_v(const Ctx *c, int j) { return c->t->gap_b[j] - (c->mod ? c->lam : 0); }
+/* the scoring view of the current trace level: modified on the top level */
+static inline void set_view(Ctx *c, int tl) { c->mod = tl && c->lam_on; }
+
 /* Scoring::stacking() (scoring.hh:653) */
 static inline int stacking(const Ctx *c) { return c->t->am_stack_score != NULL; }
 /* Scoring::arcmatch(am, true); LCG_STACK_NONE (a score outside the table
@@ -179,15 +191,15 @@ static void build_am_lists(Ctx *c) {
 static sc_t align_noex(Ctx *c, int state, int al, int bl, int i, int j) {
     sc_t *E = c->E[state];
     sc_t max_score = NEG_INF;
-    if (a_match(c, i, j)) max_score = MM(c, state, i - 1, j - 1) + sigma(c, i, j);
+    if (a_match(c, i, j)) max_score = MM(c, state, i - 1, j - 1) + sigma_v(c, i, j);
     if (a_del(c, i, j)) {
-        E[j] = norm(smax(E[j] + c->t->gap_a[i], MM(c, state, i - 1, j) + c->t->gap_a[i] + c->t->indel_opening));
+        E[j] = norm(smax(E[j] + gapA_v(c, i), MM(c, state, i - 1, j) + gapA_v(c, i) + c->t->indel_opening));
         max_score = smax(max_score, E[j]);
     } else {
         E[j] = NEG_INF;
     }
     if (a_ins(c, i, j)) {
-        c->F[state] = norm(smax(c->F[state] + c->t->gap_b[j], MM(c, state, i, j - 1) + c->t->gap_b[j] + c->t->indel_opening));
+        c->F[state] = norm(smax(c->F[state] + gapB_v(c, j), MM(c, state, i, j - 1) + gapB_v(c, j) + c->t->indel_opening));
         max_score = smax(max_score, c->F[state]);
     } else {
         c->F[state] = NEG_INF;
@@ -204,6 +216,7 @@ static sc_t align_noex(Ctx *c, int state, int al, int bl, int i, int j) {
             const sc_t *Mrow = Ms + (size_t)(la[1] - 1) * mp - 1;
             for (const int *lb = lb0; lb[1] > bl; lb += 2) {
                 sc_t d = Drow[lb[0]];
+                if (c->mod) d -= c->lam * ((i - la[1] + 1) + (j - lb[1] + 1));
                 if (c->cnt) {
                     c->cnt->arc_terms++;
                     if (d != NEG_INF) c->cnt->valid_arc_terms++;
@@ -232,7 +245,7 @@ static void init_state(Ctx *c, int state, int al, int ar, int bl, int br,
         if (minc(c, i) > bl) break;
         if (indel != NEG_INF) {
             if (!a_del(c, i, bl)) indel = NEG_INF;
-            else if (!exclA && globalA) indel = norm(indel + c->t->gap_a[i]);
+            else if (!exclA && globalA) indel = norm(indel + gapA_v(c, i));
         }
         MM(c, state, i, bl) = indel;
     }
@@ -246,7 +259,7 @@ static void init_state(Ctx *c, int state, int al, int ar, int bl, int br,
     for (j = bl + 1; j < lim; ++j) {
         if (indel != NEG_INF) {
             if (!a_ins(c, al, j)) indel = NEG_INF;
-            else if (!exclB && globalB) indel = norm(indel + c->t->gap_b[j]);
+            else if (!exclB && globalB) indel = norm(indel + gapB_v(c, j));
         }
         MM(c, state, al, j) = indel;
     }
@@ -469,6 +482,7 @@ static void trace_in_arcmatch(Ctx *c, int state, int al, int i, int bl, int j, i
 
 /* AlignerImpl::trace_arcmatch, aligner.cc:967-1028 */
 static void trace_arcmatch(Ctx *c, int k) {
+    c->mod = 0;
     int a = c->t->am_arcs[2 * k], b = c->t->am_arcs[2 * k + 1];
     int al = arcL(c->t->arcs_a, a), ar = arcR(c->t->arcs_a, a);
     int bl = arcL(c->t->arcs_b, b), br = arcR(c->t->arcs_b, b);
@@ -503,6 +517,7 @@ static void trace_arcmatch(Ctx *c, int k) {
  * arc match's own stack continues (D(am) = D(inner) + score(am)) or its
  * interior is recomputed and traced */
 static void trace_arcmatch_noLP(Ctx *c, int k) {
+    c->mod = 0;
     int in = c->inner[k];
     int a = c->t->am_arcs[2 * k], b = c->t->am_arcs[2 * k + 1];
     int ia = c->t->am_arcs[2 * in], ib = c->t->am_arcs[2 * in + 1];
@@ -531,19 +546,20 @@ static void trace_arcmatch_noLP(Ctx *c, int k) {
 
 /* AlignerImpl::trace_noex, aligner.cc:1082-1229 */
 static void trace_noex(Ctx *c, int state, int oal, int i, int obl, int j, int tl) {
+    set_view(c, tl);
     sc_t Mij = MM(c, state, i, j);
-    if (a_match(c, i, j) && valid(c, i - 1, j - 1) && Mij == MM(c, state, i - 1, j - 1) + sigma(c, i, j)) {
+    if (a_match(c, i, j) && valid(c, i - 1, j - 1) && Mij == MM(c, state, i - 1, j - 1) + sigma_v(c, i, j)) {
         trace_in_arcmatch(c, state, oal, i - 1, obl, j - 1, tl);
         append(c, i, j);
         return;
     }
     if (c->t->indel_opening == 0) {
-        if (a_del(c, i, j) && valid(c, i - 1, j) && Mij == MM(c, state, i - 1, j) + c->t->gap_a[i]) {
+        if (a_del(c, i, j) && valid(c, i - 1, j) && Mij == MM(c, state, i - 1, j) + gapA_v(c, i)) {
             trace_in_arcmatch(c, state, oal, i - 1, obl, j, tl);
             append(c, i, -1);
             return;
         }
-        if (a_ins(c, i, j) && valid(c, i, j - 1) && Mij == MM(c, state, i, j - 1) + c->t->gap_b[j]) {
+        if (a_ins(c, i, j) && valid(c, i, j - 1) && Mij == MM(c, state, i, j - 1) + gapB_v(c, j)) {
             trace_in_arcmatch(c, state, oal, i, obl, j - 1, tl);
             append(c, -1, j);
             return;
@@ -552,7 +568,7 @@ static void trace_noex(Ctx *c, int state, int oal, int i, int obl, int j, int tl
         sc_t gap = c->t->indel_opening;
         for (int k = 1; i >= oal + k && a_del(c, i - k + 1, j); ++k) {
             if (!valid(c, i - k, j)) break;
-            gap += c->t->gap_a[i - k + 1];
+            gap += gapA_v(c, i - k + 1);
             if (Mij == MM(c, state, i - k, j) + gap) {
                 trace_in_arcmatch(c, state, oal, i - k, obl, j, tl);
                 for (int l = k; l > 0; --l) append(c, i - l + 1, -1);
@@ -562,7 +578,7 @@ static void trace_noex(Ctx *c, int state, int oal, int i, int obl, int j, int tl
         gap = c->t->indel_opening;
         for (int k = 1; j >= obl + k && a_ins(c, i, j - k + 1); ++k) {
             if (!valid(c, i, j - k)) break;
-            gap += c->t->gap_b[j - k + 1];
+            gap += gapB_v(c, j - k + 1);
             if (Mij == MM(c, state, i, j - k) + gap) {
                 trace_in_arcmatch(c, state, oal, i, obl, j - k, tl);
                 for (int l = k; l > 0; --l) append(c, -1, j - l + 1);
@@ -577,7 +593,8 @@ static void trace_noex(Ctx *c, int state, int oal, int i, int obl, int j, int tl
         int a = c->t->am_arcs[2 * k], b = c->t->am_arcs[2 * k + 1];
         int al = arcL(c->t->arcs_a, a), bl = arcL(c->t->arcs_b, b);
         if (al <= oal || bl <= obl) continue;
-        if (Mij == MM(c, state, al - 1, bl - 1) + DD(c, a, b)) {
+        sc_t dv = DD(c, a, b) - (c->mod ? c->lam * ((i - al + 1) + (j - bl + 1)) : 0);
+        if (Mij == MM(c, state, al - 1, bl - 1) + dv) {
             trace_in_arcmatch(c, state, oal, al - 1, obl, bl - 1, tl);
             if (c->ntam < c->tam_cap) c->tam[c->ntam] = k;
             c->ntam++;
@@ -592,6 +609,7 @@ static void trace_noex(Ctx *c, int state, int oal, int i, int obl, int j, int tl
 
 /* AlignerImpl::trace_in_arcmatch, aligner.cc:1233-1343 */
 static void trace_in_arcmatch(Ctx *c, int state, int al, int i, int bl, int j, int tl) {
+    set_view(c, tl);
     sc_t Mij = MM(c, state, i, j);
     if (tl && c->o->sequ_local && Mij == 0) { c->min_i = i; c->min_j = j; return; }
     int fe = c->o->free_endgaps;
@@ -681,15 +699,45 @@ int lcg_oracle_align(const lcg_pair_tables *t, const lcg_align_opts *o,
     c.min_i = 1; c.min_j = 1; c.max_i = c.n; c.max_j = c.m;
 
     align_D(&c);
-    sc_t score = o->sequ_local ? top_locally(&c) : top_free_endgaps(&c);
+    c.edges = r->edges; c.edge_cap = r->edges ? c.n + c.m : 0;
+    c.tam = r->traced_am; c.tam_cap = r->traced_am ? (c.n < c.m ? c.n : c.m) : 0;
+    sc_t score;
+    int traced = 0;
+    if (o->normalized) {
+        /* AlignerImpl::normalized_align, aligner.cc:1527-1588: Dinkelbach
+         * iterations; each traces (min_i/min_j carry over when a trace does
+         * not reach a zero cell, as the reference's members do) */
+        sc_t lambda = -1, new_lambda = 0;
+        c.lam_on = 1;
+        while (lambda != new_lambda) {
+            lambda = new_lambda;
+            c.lam = lambda;
+            c.mod = 1;
+            sc_t s = top_locally(&c);
+            c.nedges = 0; c.ntam = 0;
+            trace_in_arcmatch(&c, E_NO_NO, 0, c.max_i, 0, c.max_j, 1);
+            sc_t length = (sc_t)(c.max_i - c.min_i + 1) + (c.max_j - c.min_j + 1);
+            s += length * lambda;
+            if (length + o->normalized_L <= 0) { ctx_free(&c); return -2; }
+            new_lambda = s / (length + o->normalized_L);
+        }
+        score = new_lambda;
+        traced = 1;
+    } else if (o->penalized) {
+        /* AlignerImpl::penalized_align, aligner.cc:1597-1617 */
+        c.lam_on = 1;
+        c.lam = o->position_penalty;
+        c.mod = 1;
+        score = o->sequ_local ? top_locally(&c) : top_free_endgaps(&c);
+        trace_in_arcmatch(&c, E_NO_NO, 0, c.max_i, 0, c.max_j, 1);
+        traced = 1;
+    } else {
+        score = o->sequ_local ? top_locally(&c) : top_free_endgaps(&c);
+    }
     r->score = score < MIN_FINITY ? LCG_NEG_INF : score;
     r->num_edges = 0; r->num_traced_am = 0;
-    if (o->do_trace) {
-        c.edges = r->edges; c.edge_cap = r->edges ? c.n + c.m : 0;
-        c.tam = r->traced_am; c.tam_cap = r->traced_am ? (c.n < c.m ? c.n : c.m) : 0;
-        trace_in_arcmatch(&c, E_NO_NO, 0, c.max_i, 0, c.max_j, 1);
-        r->num_edges = c.nedges; r->num_traced_am = c.ntam;
-    }
+    if (o->do_trace && !traced) trace_in_arcmatch(&c, E_NO_NO, 0, c.max_i, 0, c.max_j, 1);
+    if (o->do_trace || traced) { r->num_edges = c.nedges; r->num_traced_am = c.ntam; }
     r->max_i = c.max_i; r->max_j = c.max_j; r->min_i = c.min_i; r->min_j = c.min_j;
     ctx_free(&c);
     return 0;

@@ -70,6 +70,15 @@ CASES = {
     "h180_nolp_sl": (180, 85, "h", 86, {"no_lonely_pairs": "1", "struct_local": "1"}, True),
     "h160_stack_nolp_seqlocal": (160, 87, "h", 88, {"stacking": "1", "exp_prob": "0.006",
                                                     "no_lonely_pairs": "1", "sequ_local": "1"}, True),
+    # locarna --normalized L / --penalized PP (sequence-local top level, modified scoring)
+    "h150_normalized": (150, 81, "h", 82, {"sequ_local": "1", "normalized": "100"}, True),
+    "c150_normalized": (150, 1, 150, 2, {"sequ_local": "1", "normalized": "50"}, True),
+    "h180_normalized_nolp": (180, 85, "h", 86, {"sequ_local": "1", "normalized": "300",
+                                                "no_lonely_pairs": "1"}, True),
+    "h150_penalized": (150, 81, "h", 82, {"sequ_local": "1", "penalized": "40"}, True),
+    "c150_penalized": (150, 1, 150, 2, {"sequ_local": "1", "penalized": "20"}, True),
+    "h200_penalized_global": (200, 83, "h", 84, {"penalized": "30", "free_endgaps": "++++"}, True),
+    "h180_penalized_sl": (180, 85, "h", 86, {"sequ_local": "1", "penalized": "25", "struct_local": "1"}, True),
 }
 
 STACK_KEYS = ("stacking", "new_stacking")

@@ -63,6 +63,9 @@ class Golden:
                   free_endgaps=self.free_endgaps)
         if self.no_lonely_pairs:
             kw["no_lonely_pairs"] = True
+        for k in ("normalized", "penalized"):
+            if k in self.opts:
+                kw[k] = int(self.opts[k])
         return kw
 
 

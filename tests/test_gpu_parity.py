@@ -124,3 +124,35 @@ def test_gpu_stacking_matches_oracle(engine, prep_kw, mode):
         assert_same_result(res[k], ref, f"pair {k}")
         traced += len(ref.traced_am)
     assert traced > 50
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prep_kw,mode", [
+    ({}, {"sequ_local": True, "normalized": 100}),
+    ({}, {"sequ_local": True, "normalized": 0, "no_lonely_pairs": True}),
+    ({"stacking": 1, "exp_prob": 0.005}, {"sequ_local": True, "normalized": 400}),
+    ({}, {"sequ_local": True, "penalized": 30}),
+    ({}, {"penalized": 15, "free_endgaps": "++++"}),
+    ({"new_stacking": 1}, {"sequ_local": True, "penalized": 20, "struct_local": True}),
+])
+def test_gpu_normalized_penalized_matches_oracle(engine, prep_kw, mode):
+    """locarna --normalized L (Dinkelbach iterations of the top level) and
+    --penalized PP: homologous and unrelated pairs in one batch, every pair
+    bit-exact against the oracle (score, end cells, edges, traced arc
+    matches)."""
+    tables = _homolog_tables(prep_kw, count=3, length=120, seed=401)
+    res = engine.align_pairs(tables, **mode)
+    for k, t in enumerate(tables):
+        ref = oracle_align(t, **mode)
+        assert_same_result(res[k], ref, f"pair {k}")
+        assert res[k].min_ij == ref.min_ij, (k, res[k].min_ij, ref.min_ij)
+
+
+@pytest.mark.gpu
+def test_gpu_normalized_rejects_global_mode(engine):
+    from locarna_gb300.engine import LcgError
+    g = Golden("c60_short")
+    with pytest.raises(LcgError):
+        engine.align_pairs([g.tables], normalized=100)
+    with pytest.raises(LcgError):
+        engine.align_pairs([g.tables], sequ_local=True, normalized=100, penalized=10)
