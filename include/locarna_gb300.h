@@ -192,6 +192,23 @@ lcg_status lcg_align_pairs(lcg_engine eng, const lcg_pair_tables *pairs,
                            int32_t npairs, const lcg_align_opts *opts,
                            lcg_align_result *results);
 
+/*
+ * The k best alignments of each pair by interval splitting (locarna --kbest k
+ * --better t; Aligner::suboptimal, aligner.cc:1384-1512): the best
+ * alignment, then repeatedly the best remaining task of a queue of
+ * (interval, score), whose alignment is a hit and whose interval is split in
+ * the middle of that alignment along the longer sequence into two new tasks.
+ * Ends after k hits, when the best task scores below threshold + 1 or is -inf,
+ * or when the queue is empty (where the reference's behaviour is undefined).
+ * Empty alignments are not hits. results[q*k + h] (h < num_hits[q]) is hit h
+ * of pair q, its score the task's score; each needs edge and arc-match
+ * buffers as in lcg_align_pairs. opts->normalized / penalized must be 0;
+ * opts->do_trace is ignored (hits are always traced).
+ */
+lcg_status lcg_align_kbest(lcg_engine eng, const lcg_pair_tables *pairs, int32_t npairs,
+                           const lcg_align_opts *opts, int32_t k, int64_t threshold,
+                           lcg_align_result *results, int32_t *num_hits);
+
 /* Pairs per chunk of lcg_align_pairs' pipeline: 0 (default) chooses by batch
  * size (one chunk below 256 pairs, else up to 8 chunks); n > 0 caps a chunk
  * at n pairs (n >= npairs: one chunk, one fill and one traceback launch). */

@@ -78,11 +78,18 @@ def build_oracle():
     out = os.path.join(ORACLE, "_build")
     os.makedirs(out, exist_ok=True)
     hdr = os.path.join(ROOT, "include", "locarna_gb300.h")
-    for src, name in (("sankoff_oracle.c", "liboracle.so"), ("pf_oracle.c", "libpforacle.so")):
-        lib = os.path.join(out, name)
-        s = os.path.join(ORACLE, src)
-        if _newer(lib, [s, hdr]):
-            _run(["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-ffp-contract=off", s, "-o", lib, "-lm"])
+    # the Sankoff oracle: the C restatement plus the k-best driver (C++, for
+    # std::priority_queue's order of equal scores)
+    lib = os.path.join(out, "liboracle.so")
+    srcs = [os.path.join(ORACLE, "sankoff_oracle.c"), os.path.join(ORACLE, "kbest_oracle.cc")]
+    if _newer(lib, srcs + [hdr]):
+        obj = os.path.join(out, "sankoff_oracle.o")
+        _run(["gcc", "-O2", "-std=c11", "-fPIC", "-ffp-contract=off", "-c", srcs[0], "-o", obj])
+        _run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", srcs[1], obj, "-o", lib, "-lm"])
+    lib = os.path.join(out, "libpforacle.so")
+    s = os.path.join(ORACLE, "pf_oracle.c")
+    if _newer(lib, [s, hdr]):
+        _run(["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-ffp-contract=off", s, "-o", lib, "-lm"])
     return os.path.join(out, "liboracle.so")
 
 

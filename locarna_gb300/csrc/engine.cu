@@ -12,6 +12,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
+#include <queue>
 #include <string>
 #include <thread>
 #include <vector>
@@ -538,6 +539,14 @@ struct Chunk {
     long long launches = 0;
     bool in_flight = false;
     std::vector<long long> ratio;  // normalized alignment: the final score ratio per pair
+    // k-best alignment: the fill only (the top levels and traces follow per
+    // round), and what the rounds need of the launch
+    bool kbest = false;
+    size_t off_pairs = 0, off_mod = 0;
+    int sw = 0, rb = 0;
+    long long stride = 0;
+    bool sl = false;
+    int *scratch = nullptr;
 };
 
 // pairs per chunk: one chunk for small batches, else up to 8 chunks of at
@@ -574,7 +583,7 @@ lcg_status mod_top_levels(const lcg_align_opts *opts, Chunk &c, const PairDev *d
         std::fill(lam.begin(), lam.end(), opts->position_penalty);
         CUDA_TRY(cudaMemcpyAsync(d_lam, lam.data(), 4ull * npairs, cudaMemcpyHostToDevice, st));
         CUDA_TRY(cudaMemcpyAsync(d_items, items.data(), 4ull * npairs, cudaMemcpyHostToDevice, st));
-        CUDA_TRY(launch_top(dpairs, d_items, npairs, d_lam, rb, status, st));
+        CUDA_TRY(launch_top(dpairs, d_items, npairs, d_lam, nullptr, rb, status, st));
         c.launches += 1;
         return LCG_OK;
     }
@@ -592,7 +601,7 @@ lcg_status mod_top_levels(const lcg_align_opts *opts, Chunk &c, const PairDev *d
         const int ni = (int)items.size();
         CUDA_TRY(cudaMemcpyAsync(d_lam, lam.data(), 4ull * npairs, cudaMemcpyHostToDevice, st));
         CUDA_TRY(cudaMemcpyAsync(d_items, items.data(), 4ull * ni, cudaMemcpyHostToDevice, st));
-        CUDA_TRY(launch_top(dpairs, d_items, ni, d_lam, rb, status, st));
+        CUDA_TRY(launch_top(dpairs, d_items, ni, d_lam, nullptr, rb, status, st));
         TraceSel ts;
         ts.items = d_items;
         ts.nitems = ni;
@@ -702,7 +711,8 @@ lcg_status chunk_launch(lcg_engine e, const Slot &s, const lcg_pair_tables *all,
     // normalized / penalized alignment: per pair its penalty, the selected
     // pairs and their gathered result words
     const bool modv = opts->normalized || opts->penalized;
-    const size_t off_mod = modv ? take(dev_only, 4ull * 7 * npairs) : 0;
+    // k-best: penalties, items, two gathered result sets, restrictions
+    const size_t off_mod = (modv || c.kbest) ? take(dev_only, 4ull * 16 * npairs) : 0;
     size_t total = dev_only;
 
     if (total > *s.arena_cap) {
@@ -898,7 +908,14 @@ lcg_status chunk_launch(lcg_engine e, const Slot &s, const lcg_pair_tables *all,
                                        scratch, stride, sw, rb, sl, status, st, &sel);
         if (ms != LCG_OK) return ms;
     }
-    if (opts->do_trace || modv) {
+    c.off_pairs = off_pairs;
+    c.off_mod = off_mod;
+    c.sw = sw;
+    c.rb = rb;
+    c.stride = stride;
+    c.sl = sl;
+    c.scratch = scratch;
+    if ((opts->do_trace || modv) && !c.kbest) {
         if (sl)
             CUDA_TRY(launch_sl_trace((const PairDev *)(Dv + off_pairs), npairs, scratch, stride, sw,
                                      status, st, sel));
@@ -913,6 +930,31 @@ lcg_status chunk_launch(lcg_engine e, const Slot &s, const lcg_pair_tables *all,
     c.in_flight = true;
     e->last_h2d += (long long)down_begin;
     e->last_d2h += 64 + (long long)(down_end - down_begin);
+    return LCG_OK;
+}
+
+// The traced alignment of one pair from the staged download: the edges in
+// the reference's append order and the traced arc matches into r.
+lcg_status assemble(const Prep &p, const PairOff &o, const char *H, lcg_align_result &r) {
+    const int *res = (const int *)(H + o.res);
+    Assembler as;
+    as.tok = (const int2 *)(H + o.tok);
+    int nseg = res[R_NSEG];
+    const int4 *segs = (const int4 *)(H + o.segs);
+    if (nseg < 1 || nseg > p.tq_cap + 1) return fail(LCG_ERR_DEVICE, "bad traceback segment count");
+    for (int sg = 0; sg < nseg; ++sg) {
+        as.seg_am.push_back(segs[sg].x);
+        as.seg_start.push_back(segs[sg].y);
+        as.seg_end.push_back(segs[sg].z);
+    }
+    as.edges = r.edges;
+    as.edge_cap = r.edges ? p.n + p.m : 0;
+    as.tam = r.traced_am;
+    as.tam_cap = r.traced_am ? std::min(p.n, p.m) : 0;
+    as.expand(0, 0);
+    if (!as.ok) return fail(LCG_ERR_DEVICE, "traceback assembly failed");
+    r.num_edges = as.nedges;
+    r.num_traced_am = as.ntam;
     return LCG_OK;
 }
 
@@ -962,24 +1004,8 @@ lcg_status chunk_finish(lcg_engine e, const Slot &s, const lcg_align_opts *opts,
         r.num_edges = 0;
         r.num_traced_am = 0;
         if (!traced) continue;
-        Assembler as;
-        as.tok = (const int2 *)(H + o.tok);
-        int nseg = res[R_NSEG];
-        const int4 *segs = (const int4 *)(H + o.segs);
-        if (nseg < 1 || nseg > p.tq_cap + 1) return fail(LCG_ERR_DEVICE, "bad traceback segment count");
-        for (int sg = 0; sg < nseg; ++sg) {
-            as.seg_am.push_back(segs[sg].x);
-            as.seg_start.push_back(segs[sg].y);
-            as.seg_end.push_back(segs[sg].z);
-        }
-        as.edges = r.edges;
-        as.edge_cap = r.edges ? p.n + p.m : 0;
-        as.tam = r.traced_am;
-        as.tam_cap = r.traced_am ? std::min(p.n, p.m) : 0;
-        as.expand(0, 0);
-        if (!as.ok) return fail(LCG_ERR_DEVICE, "traceback assembly failed");
-        r.num_edges = as.nedges;
-        r.num_traced_am = as.ntam;
+        lcg_status as = assemble(p, o, H, r);
+        if (as != LCG_OK) return as;
     }
     *results_ms += ms_between(t1, std::chrono::steady_clock::now());
     return LCG_OK;
@@ -1175,6 +1201,190 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
     e->last_phase_ms[2] = t_wait;
     e->last_phase_ms[3] = t_res;
     return rc;
+}
+
+lcg_status lcg_align_kbest(lcg_engine e, const lcg_pair_tables *pairs, int32_t npairs, const lcg_align_opts *opts,
+                           int32_t k, int64_t threshold, lcg_align_result *results, int32_t *num_hits) {
+    if (!e || !pairs || !opts || !results || !num_hits || npairs < 0) return fail(LCG_ERR_ARG, "NULL argument");
+    if (k < 1) return fail(LCG_ERR_ARG, "k must be >= 1");
+    if (opts->normalized || opts->penalized)
+        return fail(LCG_ERR_UNSUPPORTED, "k-best alignment with normalized or penalized scores is not supported");
+    for (int q = 0; q < npairs; ++q) num_hits[q] = 0;
+    if (npairs == 0) return LCG_OK;
+    CUDA_TRY(cudaSetDevice(e->device));
+    e->last_ms = e->last_fill_ms = e->last_trace_ms = 0;
+    e->last_launches = 0;
+    e->last_h2d = e->last_d2h = 0;
+    e->last_groups = e->last_cells = 0;
+    e->last_terms = e->last_visits = -1;
+    // the fill and the whole-sequence top levels: one chunk, traced pairs
+    // (PF_TRACE) but no traceback launch
+    lcg_align_opts o = *opts;
+    o.do_trace = 1;
+    Chunk c;
+    c.q0 = 0;
+    c.nq = npairs;
+    c.kbest = true;
+    c.prep.resize(npairs);
+    lcg_host::parallel_for(npairs, [&](int q) { prep_pair(pairs[q], o, c.prep[q]); });
+    for (int q = 0; q < npairs; ++q)
+        if (c.prep[q].code != LCG_OK) return fail(c.prep[q].code, "pair " + std::to_string(q) + ": " + c.prep[q].err);
+    const Slot sl0 = slot_of(e, 0);
+    double t_pack = 0, t_wait = 0, t_res = 0;
+    lcg_status rc = chunk_launch(e, sl0, pairs, &o, c, &t_pack);
+    if (rc != LCG_OK) return rc;
+    std::vector<lcg_align_result> first(npairs);
+    for (auto &r : first) std::memset(&r, 0, sizeof r);
+    lcg_align_opts o_score = o;
+    o_score.do_trace = 0;
+    rc = chunk_finish(e, sl0, &o_score, c, first.data(), &t_wait, &t_res);
+    if (rc != LCG_OK) return rc;
+
+    // Aligner::suboptimal (aligner.cc:1384-1512) per pair: a task queue of
+    // (interval, score) with the reference's comparator (greater_second,
+    // aligner.hh:32-44); each round pops one task per pair, aligns and traces
+    // its interval, and scores the two halves of the split
+    struct Task {
+        int4 r;  // (sA, sB, eA, eB)
+        long long score;
+    };
+    struct ScoreLess {
+        bool operator()(const Task &a, const Task &b) const { return a.score < b.score; }
+    };
+    std::vector<std::priority_queue<Task, std::vector<Task>, ScoreLess>> tasks(npairs);
+    std::vector<int> count(npairs, 1);  // i of the reference's loop
+    std::vector<bool> done(npairs, false);
+    std::vector<Task> cur(npairs);
+    for (int q = 0; q < npairs; ++q) tasks[q].push(Task{make_int4(1, 1, c.prep[q].n, c.prep[q].m), first[q].score});
+    char *Dv = *sl0.d_arena;
+    char *H = *sl0.h_stage;
+    const PairDev *dpairs = (const PairDev *)(Dv + c.off_pairs);
+    int *dmod = (int *)(Dv + c.off_mod);
+    int *d_items = dmod + npairs, *d_res1 = dmod + 2 * npairs, *d_res2 = dmod + 7 * npairs;
+    int4 *d_rst = (int4 *)(dmod + 12 * npairs);
+    int *status = (int *)(Dv + c.off_ctrl + 4);
+    cudaStream_t st = sl0.st;
+    std::vector<int> items, split_items;
+    std::vector<int4> rst(npairs), r1(npairs), r2(npairs);
+    std::vector<int> g1(5ull * npairs), g2(5ull * npairs);
+    // an interval the top level can align (the reference leaves others undefined)
+    auto valid_r = [&](int q, int4 r) {
+        return r.x >= 1 && r.y >= 1 && r.z <= c.prep[q].n && r.w <= c.prep[q].m && r.z >= r.x - 1 && r.w >= r.y - 1;
+    };
+    const auto t0 = std::chrono::steady_clock::now();
+    for (int round = 0;; ++round) {
+        items.clear();
+        for (int q = 0; q < npairs; ++q) {
+            if (done[q]) continue;
+            // the reference reads top() of an empty queue here (undefined);
+            // the enumeration ends instead
+            if (tasks[q].empty()) {
+                done[q] = true;
+                continue;
+            }
+            cur[q] = tasks[q].top();
+            tasks[q].pop();
+            if (cur[q].score == LCG_NEG_INF || cur[q].score < (long long)threshold + 1) {
+                done[q] = true;
+                continue;
+            }
+            rst[q] = cur[q].r;
+            items.push_back(q);
+        }
+        if (items.empty()) break;
+        const int ni = (int)items.size();
+        CUDA_TRY(cudaMemcpyAsync(d_rst, rst.data(), sizeof(int4) * npairs, cudaMemcpyHostToDevice, st));
+        CUDA_TRY(cudaMemcpyAsync(d_items, items.data(), 4ull * ni, cudaMemcpyHostToDevice, st));
+        CUDA_TRY(launch_top(dpairs, d_items, ni, nullptr, d_rst, c.rb, status, st));
+        TraceSel ts;
+        ts.items = d_items;
+        ts.nitems = ni;
+        ts.rst = d_rst;
+        ts.flags = round ? TRACE_KEEP_MIN : 0;  // the reference's min_i_/min_j_ carry over between traces
+        if (c.sl) CUDA_TRY(launch_sl_trace(dpairs, npairs, c.scratch, c.stride, c.sw, status, st, ts));
+        else CUDA_TRY(launch_trace(dpairs, npairs, c.scratch, c.stride, c.sw, c.rb, status, st, ts));
+        CUDA_TRY(cudaMemcpyAsync(H + c.down_begin, Dv + c.down_begin, c.down_end - c.down_begin,
+                                 cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaMemcpyAsync(H + c.off_ctrl, Dv + c.off_ctrl, 64, cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaStreamSynchronize(st));
+        e->last_launches += 2;
+        e->last_d2h += (long long)(c.down_end - c.down_begin) + 64;
+        const int hstatus = ((const int *)(H + c.off_ctrl))[1];
+        if (hstatus & ST_OVERFLOW) return fail(LCG_ERR_DEVICE, "traceback buffer overflow");
+        if (hstatus & ST_INTERNAL) return fail(LCG_ERR_DEVICE, "traceback found no predecessor");
+        split_items.clear();
+        for (int q : items) {
+            lcg_align_result &r = results[(size_t)q * k + num_hits[q]];
+            const int *res = (const int *)(H + c.off[q].res);
+            rc = assemble(c.prep[q], c.off[q], H, r);
+            if (rc != LCG_OK) return rc;
+            if (r.num_edges == 0) continue;  // empty alignment: no hit, the count stays
+            r.score = cur[q].score;
+            r.max_i = res[R_MAXI];
+            r.max_j = res[R_MAXJ];
+            r.min_i = res[R_MINI];
+            r.min_j = res[R_MINJ];
+            ++num_hits[q];
+            if (count[q] == k) {
+                done[q] = true;
+                continue;
+            }
+            if (!r.edges) return fail(LCG_ERR_ARG, "k-best alignment needs edge buffers");
+            // Alignment::start_positions / end_positions (alignment.cc:169-195)
+            int sa = c.prep[q].n, sb = c.prep[q].m, ea = 0, eb = 0;
+            const int ne = std::min(r.num_edges, c.prep[q].n + c.prep[q].m);
+            for (int t = 0; t < ne; ++t) if (r.edges[2 * t] >= 0) { sa = r.edges[2 * t]; break; }
+            for (int t = 0; t < ne; ++t) if (r.edges[2 * t + 1] >= 0) { sb = r.edges[2 * t + 1]; break; }
+            for (int t = ne - 1; t >= 0; --t) if (r.edges[2 * t] >= 0) { ea = r.edges[2 * t]; break; }
+            for (int t = ne - 1; t >= 0; --t) if (r.edges[2 * t + 1] >= 0) { eb = r.edges[2 * t + 1]; break; }
+            const int4 tr = cur[q].r;
+            r1[q] = tr;
+            r2[q] = tr;
+            // the reference's interval lengths are size_t differences
+            if ((unsigned long)(long)(tr.z - tr.x) > (unsigned long)(long)(tr.w - tr.y)) {
+                const int split = (sa + ea) / 2;
+                r1[q].z = split;
+                r2[q].x = split;
+            } else {
+                const int split = (sb + eb) / 2;
+                r1[q].w = split;
+                r2[q].y = split;
+            }
+            split_items.push_back(q);
+        }
+        if (split_items.empty()) continue;
+        // the scores of both halves (two restricted top levels)
+        std::vector<int> run1, run2;
+        for (int q : split_items) {
+            if (valid_r(q, r1[q])) run1.push_back(q);
+            if (valid_r(q, r2[q])) run2.push_back(q);
+        }
+        const int n1 = (int)run1.size(), n2 = (int)run2.size();
+        CUDA_TRY(cudaMemcpyAsync(d_rst, r1.data(), sizeof(int4) * npairs, cudaMemcpyHostToDevice, st));
+        CUDA_TRY(cudaMemcpyAsync(d_items, run1.data(), 4ull * n1, cudaMemcpyHostToDevice, st));
+        CUDA_TRY(launch_top(dpairs, d_items, n1, nullptr, d_rst, c.rb, status, st));
+        CUDA_TRY(launch_gather_res(dpairs, d_items, n1, d_res1, st));
+        CUDA_TRY(cudaMemcpyAsync(d_rst, r2.data(), sizeof(int4) * npairs, cudaMemcpyHostToDevice, st));
+        CUDA_TRY(cudaMemcpyAsync(d_items, run2.data(), 4ull * n2, cudaMemcpyHostToDevice, st));
+        CUDA_TRY(launch_top(dpairs, d_items, n2, nullptr, d_rst, c.rb, status, st));
+        CUDA_TRY(launch_gather_res(dpairs, d_items, n2, d_res2, st));
+        CUDA_TRY(cudaMemcpyAsync(g1.data(), d_res1, 20ull * n1, cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaMemcpyAsync(g2.data(), d_res2, 20ull * n2, cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaStreamSynchronize(st));
+        e->last_launches += 4;
+        std::vector<long long> s1(npairs, LCG_NEG_INF), s2(npairs, LCG_NEG_INF);
+        for (int t = 0; t < n1; ++t) s1[run1[t]] = g1[5 * t] < MIN_FINITE ? LCG_NEG_INF : g1[5 * t];
+        for (int t = 0; t < n2; ++t) s2[run2[t]] = g2[5 * t] < MIN_FINITE ? LCG_NEG_INF : g2[5 * t];
+        for (int q : split_items) {
+            tasks[q].push(Task{r1[q], s1[q]});
+            tasks[q].push(Task{r2[q], s2[q]});
+            ++count[q];
+        }
+    }
+    e->last_trace_ms = ms_between(t0, std::chrono::steady_clock::now());
+    const int hstatus = ((const int *)(H + c.off_ctrl))[1];
+    if (hstatus & ST_TIMEOUT) return fail(LCG_ERR_TIMEOUT, "a device wait for an arc-match entry timed out");
+    return LCG_OK;
 }
 
 lcg_status lcg_engine_set_chunk_pairs(lcg_engine e, int32_t pairs_per_chunk) {

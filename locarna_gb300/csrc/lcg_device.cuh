@@ -116,6 +116,7 @@ struct TraceSel {
     int nitems = 0;
     const int *lam = nullptr;
     int flags = 0;
+    const int4 *rst = nullptr;  // per pair (sA, sB, eA, eB) of k-best alignment; NULL = whole sequences
 };
 
 enum Res : int {

@@ -476,28 +476,35 @@ static __device__ __forceinline__ void warp_argmax(int &v, int &k1, int &k2) {
 template <bool COUNT, bool FAST = false, bool MOD = false>
 __device__ __forceinline__ void run_top(const PairDev &P, int cpl, int sbase, int ringn,
                                      int *status, volatile int *abort_flag,
-                                     unsigned long long *counters, int lam = 0) {
+                                     unsigned long long *counters, int lam = 0,
+                                     const int4 *rst = nullptr) {
     const int lane = threadIdx.x & 31;
-    const int n = P.n, m = P.m, m1 = m + 1;
+    const int m1 = P.m + 1;
+    // AlignerRestriction (aligner_restriction.hh): the top level aligns
+    // A[sA..n] with B[sB..m]; the whole sequences unless rst is given (the
+    // intervals of k-best alignment, checked on the host)
+    const int sA = rst ? rst->x : 1, sB = rst ? rst->y : 1;
+    const int n = rst ? rst->z : P.n, m = rst ? rst->w : P.m;
+    int *const Mg = P.topM + (size_t)(sA - 1) * m1 + (sB - 1);  // M(sA-1, sB-1)
     const bool local = P.flags & PF_SEQU_LOCAL;
     const int fe = P.free_endgaps;
     TopOut to;
     if (local) {
-        run_group<true, !MOD, false, COUNT, FAST, MOD>(P, cpl, 0, n + 1, 0, m + 1, P.topM, m1, sbase, ringn,
+        run_group<true, !MOD, false, COUNT, FAST, MOD>(P, cpl, sA - 1, n + 1, sB - 1, m + 1, Mg, m1, sbase, ringn,
                                                       nullptr, 0, false, false, true, status, abort_flag,
                                                       &to, counters, lam);
         int v = to.best, i = to.bi, j = to.bj;
         if (v <= 0) {
             v = 0;
-            i = 0;
-            j = 0;
+            i = sA - 1;
+            j = sB - 1;
         }
         warp_argmax(v, i, j);
         if (lane == 0) {
             if (v <= 0) {
                 v = 0;
-                i = 0;
-                j = 0;
+                i = sA - 1;
+                j = sB - 1;
             }
             P.res[R_SCORE] = v;
             P.res[R_MAXI] = i;
@@ -505,13 +512,19 @@ __device__ __forceinline__ void run_top(const PairDev &P, int cpl, int sbase, in
         }
         return;
     }
-    run_group<true, !MOD, false, COUNT, FAST, MOD>(P, cpl, 0, n + 1, 0, m + 1, P.topM, m1, sbase, ringn,
+    run_group<true, !MOD, false, COUNT, FAST, MOD>(P, cpl, sA - 1, n + 1, sB - 1, m + 1, Mg, m1, sbase, ringn,
                                                   nullptr, 0, !(fe & 4), !(fe & 1), false, status, abort_flag,
                                                   &to, counters, lam);
     __syncwarp();
+    // The argmax reads M(n,m) and, with free right end gaps, column m of the
+    // rows whose band reaches m (aligner.cc:771-799). On an interval of
+    // k-best alignment such a cell can lie outside the band, where the
+    // reference reads whatever its reused matrix holds; here it counts as
+    // -inf. On the whole sequences every cell read is in the band.
     if (!(fe & (2 | 8))) {
         if (lane == 0) {
-            P.res[R_SCORE] = P.topM[(size_t)n * m1 + m];
+            const bool inb = (P.min_col[n] <= m && m <= P.max_col[n]) || (n == sA - 1 && m == sB - 1);
+            P.res[R_SCORE] = inb ? P.topM[(size_t)n * m1 + m] : NEG;
             P.res[R_MAXI] = n;
             P.res[R_MAXJ] = m;
         }
@@ -521,8 +534,8 @@ __device__ __forceinline__ void run_top(const PairDev &P, int cpl, int sbase, in
     // then over row n (j ascending); order key = position in that scan
     int v = NEG, k1 = INT32_MAX, k2 = 0;
     if (fe & 8) {
-        for (int i = max(P.ra + 1, 1) + lane; i <= n; i += 32) {
-            if (P.max_col[i] >= m) {
+        for (int i = max(P.ra + 1, sA) + lane; i <= n; i += 32) {
+            if (P.max_col[i] >= m && P.min_col[i] <= m) {
                 int x = P.topM[(size_t)i * m1 + m];
                 if (x > v) {
                     v = x;
@@ -533,7 +546,7 @@ __device__ __forceinline__ void run_top(const PairDev &P, int cpl, int sbase, in
         }
     }
     if (fe & 2) {
-        int lo = max(max(P.rb + 1, 1), P.min_col[n]), hi = min(m, P.max_col[n]);
+        int lo = max(max(P.rb + 1, sB), P.min_col[n]), hi = min(m, P.max_col[n]);
         for (int j = lo + lane; j <= hi; j += 32) {
             int x = P.topM[(size_t)n * m1 + j];
             if (x > v) {
@@ -545,7 +558,7 @@ __device__ __forceinline__ void run_top(const PairDev &P, int cpl, int sbase, in
     }
     warp_argmax(v, k1, k2);
     if (lane == 0) {
-        int mi = 0, mj = 0;
+        int mi = sA - 1, mj = sB - 1;
         if (v > NEG) {
             if (k1 <= n) {
                 mi = k1;

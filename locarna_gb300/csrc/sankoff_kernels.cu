@@ -88,7 +88,9 @@ __global__ void __launch_bounds__(TRACE_WARPS * 32)
             P.res[R_MINI] = 1;
             P.res[R_MINJ] = 1;
         }
-        walk(w, P.topM, P.m + 1, 0, 0, P.res[R_MAXI], P.res[R_MAXJ], true, status, lam);
+        const int sA = sel.rst ? sel.rst[pair].x : 1, sB = sel.rst ? sel.rst[pair].y : 1;
+        walk(w, P.topM + (size_t)(sA - 1) * (P.m + 1) + (sB - 1), P.m + 1, sA - 1, sB - 1, P.res[R_MAXI],
+             P.res[R_MAXJ], true, status, lam);
         P.segs[nseg++] = make_int4(-1, 0, w.ntok, 0);
     }
     if (sel.flags & TRACE_TOP_ONLY) return;
@@ -173,15 +175,16 @@ cudaError_t launch_trace(const PairDev *pairs, int npairs, int *scratch,
     return cudaGetLastError();
 }
 
-// The top level alone under the modified scoring view of normalized and
-// penalized alignment (every position penalised by lam[pair]), one warp per
-// selected pair, after the fill kernel has made D final
-// (align_top_level_locally / _free_endgaps with a ModifiedScoringView,
-// aligner.cc:1561-1562, 1606-1610). Writes the pair's top-level matrix and
-// result words like the fill kernel's top item.
+// The top level alone, one warp per selected pair, after the fill kernel has
+// made D final: under the modified scoring view of normalized and penalized
+// alignment (every position penalised by lam[pair]; align_top_level_locally /
+// _free_endgaps with a ModifiedScoringView, aligner.cc:1561-1562, 1606-1610)
+// and/or restricted to the interval rst[pair] of k-best alignment
+// (Aligner::suboptimal, aligner.cc:1384-1512). Writes the pair's top-level
+// matrix and result words like the fill kernel's top item.
 __global__ void __launch_bounds__(TRACE_WARPS * 32)
     sankoff_top_kernel(const PairDev *__restrict__ pairs, const int *__restrict__ items, int nitems,
-                       const int *__restrict__ lam, int rb, int *status) {
+                       const int *__restrict__ lam, const int4 *__restrict__ rst, int rb, int *status) {
     const int warp = threadIdx.x >> 5;
     const int wi = blockIdx.x * TRACE_WARPS + warp;
     if (wi >= nitems) return;
@@ -189,7 +192,7 @@ __global__ void __launch_bounds__(TRACE_WARPS * 32)
     const PairDev &P = pairs[pair];
     int dummy_abort = 0;
     run_top<false, false, true>(P, 1, warp * smem_warp_ints(rb), rb, status, (volatile int *)&dummy_abort,
-                                nullptr, lam[pair]);
+                                nullptr, lam ? lam[pair] : 0, rst ? rst + pair : nullptr);
 }
 
 // result words of the selected pairs, gathered for one device->host copy:
@@ -202,8 +205,8 @@ __global__ void gather_res_kernel(const PairDev *__restrict__ pairs, const int *
     for (int k = 0; k < 5; ++k) out[5 * q + k] = r[k];
 }
 
-cudaError_t launch_top(const PairDev *pairs, const int *items, int nitems, const int *lam, int rb, int *status,
-                       cudaStream_t st) {
+cudaError_t launch_top(const PairDev *pairs, const int *items, int nitems, const int *lam, const int4 *rst, int rb,
+                       int *status, cudaStream_t st) {
     if (nitems <= 0) return cudaSuccess;
     size_t smem = (size_t)TRACE_WARPS * smem_warp_ints(rb) * sizeof(int);
     if (smem > 48 * 1024) {
@@ -212,7 +215,7 @@ cudaError_t launch_top(const PairDev *pairs, const int *items, int nitems, const
         if (e != cudaSuccess) return e;
     }
     int blocks = (nitems + TRACE_WARPS - 1) / TRACE_WARPS;
-    sankoff_top_kernel<<<blocks, TRACE_WARPS * 32, smem, st>>>(pairs, items, nitems, lam, rb, status);
+    sankoff_top_kernel<<<blocks, TRACE_WARPS * 32, smem, st>>>(pairs, items, nitems, lam, rst, rb, status);
     return cudaGetLastError();
 }
 

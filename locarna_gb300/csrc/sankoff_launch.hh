@@ -16,8 +16,9 @@ cudaError_t launch_fill(const PairDev *pairs, const int2 *queue, int nitems, int
 cudaError_t launch_trace(const PairDev *pairs, int npairs, int *scratch, long long scratch_stride, int sw, int rb,
                          int *status, cudaStream_t st, TraceSel sel = TraceSel());
 // the top level of the selected pairs under the scoring modified by lam[pair]
-cudaError_t launch_top(const PairDev *pairs, const int *items, int nitems, const int *lam, int rb, int *status,
-                       cudaStream_t st);
+// (NULL: 0) and restricted to rst[pair] (NULL: whole sequences)
+cudaError_t launch_top(const PairDev *pairs, const int *items, int nitems, const int *lam, const int4 *rst, int rb,
+                       int *status, cudaStream_t st);
 // out[5 q + k] = result word k (score, max_i, max_j, min_i, min_j) of pair items[q]
 cudaError_t launch_gather_res(const PairDev *pairs, const int *items, int nitems, int *out, cudaStream_t st);
 cudaError_t fill_occupancy(int rb, bool counting, bool fast, int *blocks_per_sm);

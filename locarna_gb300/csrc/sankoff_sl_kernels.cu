@@ -496,7 +496,9 @@ __global__ void __launch_bounds__(TRACE_WARPS * 32)
             P.res[R_MINI] = 1;
             P.res[R_MINJ] = 1;
         }
-        walk_sl(w, P.topM, 0, P.m + 1, 0, 0, S_NO_NO, P.res[R_MAXI], P.res[R_MAXJ], true, status, lam);
+        const int sA = sel.rst ? sel.rst[pair].x : 1, sB = sel.rst ? sel.rst[pair].y : 1;
+        walk_sl(w, P.topM + (size_t)(sA - 1) * (P.m + 1) + (sB - 1), 0, P.m + 1, sA - 1, sB - 1, S_NO_NO,
+                P.res[R_MAXI], P.res[R_MAXJ], true, status, lam);
         P.segs[nseg++] = make_int4(-1, 0, w.ntok, 0);
     }
     if (sel.flags & TRACE_TOP_ONLY) return;

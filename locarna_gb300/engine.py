@@ -50,6 +50,9 @@ def _load_locked(path):
     lib.lcg_align_pairs.argtypes = [C.c_void_p, C.POINTER(lcg_pair_tables), C.c_int32,
                                     C.POINTER(lcg_align_opts), C.POINTER(lcg_align_result)]
     lib.lcg_align_pairs.restype = C.c_int32
+    lib.lcg_align_kbest.argtypes = [C.c_void_p, C.POINTER(lcg_pair_tables), C.c_int32, C.POINTER(lcg_align_opts),
+                                    C.c_int32, C.c_int64, C.POINTER(lcg_align_result), C.POINTER(C.c_int32)]
+    lib.lcg_align_kbest.restype = C.c_int32
     lib.lcg_engine_last_stats.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int64)]
     lib.lcg_engine_last_stats.restype = C.c_int32
     lib.lcg_engine_last_timing.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]
@@ -133,6 +136,26 @@ class Engine:
         call = self.prepare_call(tables, opts, **kw)
         self.run_call(call)
         return self.decode_call(call)
+
+    def align_kbest(self, tables, k, threshold=-1000000, **kw):
+        """lcg_align_kbest: per pair the list of its (up to k) hits, each an
+        AlignResult whose score is the hit's score."""
+        opts = make_opts(**kw)
+        n = len(tables)
+        arr = (lcg_pair_tables * n)(*[t.to_c() for t in tables])
+        bufs = [ResultBuffers(t.len_a, t.len_b) for t in tables for _ in range(k)]
+        res = (lcg_align_result * (n * k))(*[b.c for b in bufs])
+        hits = (C.c_int32 * n)()
+        _check(self.lib, self.lib.lcg_align_kbest(self.h, arr, n, C.byref(opts), int(k), int(threshold), res, hits))
+        out = []
+        for q in range(n):
+            row = []
+            for h in range(hits[q]):
+                b = bufs[q * k + h]
+                b.c = res[q * k + h]
+                row.append(b.decode())
+            out.append(row)
+        return out
 
     def last_stats(self):
         ms = C.c_double()

@@ -24,10 +24,12 @@
 #include <cstring>
 #include <iostream>
 #include <memory>
+#include <queue>
 #include <string>
 #include <vector>
 
 #include "LocARNA/aligner.hh"
+#include "LocARNA/aligner_restriction.hh"
 #include "LocARNA/aligner_params.hh"
 #include "LocARNA/alignment.hh"
 #include "LocARNA/anchor_constraints.hh"
@@ -55,6 +57,8 @@ struct Opts {
     bool stacking = false, new_stacking = false;
     double exp_prob = -1;  // --exp-prob; < 0: not given
     int normalized = -1, penalized = -1;  // --normalized L / --penalized PP (-1: off)
+    int kbest = 0;                          // --kbest k (0: off)
+    long better = -1000000;                 // --better t
     bool dump_tables = true;
     int repeat = 1;
 };
@@ -84,6 +88,8 @@ static void parse(Opts &o, const char *kv) {
     else if (k == "exp_prob") o.exp_prob = std::atof(v.c_str());
     else if (k == "normalized") o.normalized = std::atoi(v.c_str());
     else if (k == "penalized") o.penalized = std::atoi(v.c_str());
+    else if (k == "kbest") o.kbest = std::atoi(v.c_str());
+    else if (k == "better") o.better = std::atol(v.c_str());
     else if (k == "repeat") o.repeat = std::atoi(v.c_str());
     else { std::cerr << "unknown option " << k << "\n"; std::exit(2); }
 }
@@ -197,6 +203,75 @@ int main(int argc, char **argv) {
             std::printf(" %ld:%ld", lo, hi);
         }
         std::printf("\n");
+    }
+
+    auto make_aligner = [&]() {
+        return std::make_unique<Aligner>(AlignerParams(
+            AlignerParams::seqA(&seqA), AlignerParams::seqB(&seqB),
+            AlignerParams::scoring(&scoring), AlignerParams::no_lonely_pairs(o.no_lonely_pairs),
+            AlignerParams::struct_local(o.struct_local), AlignerParams::sequ_local(o.sequ_local),
+            AlignerParams::free_endgaps(FreeEndgaps(o.free_endgaps)),
+            AlignerParams::max_diff_am(o.max_diff_am), AlignerParams::max_diff_at_am(o.max_diff_at_am),
+            AlignerParams::trace_controller(&tc), AlignerParams::stacking(stacking),
+            AlignerParams::constraints(&anchors)));
+    };
+    if (o.kbest > 0) {
+        // (1) the reference's own enumeration (Aligner::suboptimal), which
+        // prints "HIT score startA startA endB endB" per hit
+        std::fflush(stdout);
+        make_aligner()->suboptimal(o.kbest, o.better, false, 0, 120, false, false, true, false);
+        std::cout.flush();
+        // (2) the same enumeration through the public Aligner API
+        // (aligner.cc:1384-1512), printing each hit's full alignment
+        auto a = make_aligner();
+        typedef std::pair<AlignerRestriction, infty_score_t> task_t;
+        std::priority_queue<task_t, std::vector<task_t>, greater_second<task_t>> tasks;
+        infty_score_t s0 = a->align();
+        tasks.push(task_t(a->get_restriction(), s0));
+        for (size_t i = 1; i <= (size_t)o.kbest && !tasks.empty();) {
+            task_t task = tasks.top();
+            tasks.pop();
+            AlignerRestriction r = task.first;
+            if (task.second < (infty_score_t)o.better + 1) break;
+            a->set_restriction(r);
+            a->align();
+            a->trace();
+            Alignment alignment = a->get_alignment();
+            if (alignment.empty()) continue;
+            std::printf("khit %ld", score_val(task.second));
+            for (auto &e : alignment.alignment_edges(false)) {
+                int x = e.first.is_pos() ? (int)(size_t)e.first : -1 - (int)e.first.gap();
+                int y = e.second.is_pos() ? (int)(size_t)e.second : -1 - (int)e.second.gap();
+                std::printf(" %d:%d", x, y);
+            }
+            std::printf("\nklocal");
+            for (auto &e : alignment.alignment_edges(true)) {
+                int x = e.first.is_pos() ? (int)(size_t)e.first : -1 - (int)e.first.gap();
+                int y = e.second.is_pos() ? (int)(size_t)e.second : -1 - (int)e.second.gap();
+                std::printf(" %d:%d", x, y);
+            }
+            std::printf("\nkstruct %s %s\n", alignment.dot_bracket_structureA(false).c_str(),
+                        alignment.dot_bracket_structureB(false).c_str());
+            if (i == (size_t)o.kbest) break;
+            size_t lenA = r.endA() - r.startA(), lenB = r.endB() - r.startB();
+            AlignerRestriction r1(r), r2(r);
+            if (lenA > lenB) {
+                int split = (alignment.start_positions().first + alignment.end_positions().first) / 2;
+                r1.set_endA(split);
+                r2.set_startA(split);
+            } else {
+                int split = (alignment.start_positions().second + alignment.end_positions().second) / 2;
+                r1.set_endB(split);
+                r2.set_startB(split);
+            }
+            a->set_restriction(r1);
+            infty_score_t s1 = a->align();
+            a->set_restriction(r2);
+            infty_score_t s2 = a->align();
+            tasks.push(task_t(r1, s1));
+            tasks.push(task_t(r2, s2));
+            ++i;
+        }
     }
 
     double best = 1e30;

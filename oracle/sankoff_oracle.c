@@ -52,6 +52,13 @@ typedef struct {
      * normalized and penalized alignment */
     sc_t lam;
     int lam_on, mod;
+    /* AlignerRestriction (aligner_restriction.hh): the top level aligns
+     * A[rsA..reA] with B[rsB..reB] (default: the whole sequences) */
+    int rsA, rsB, reA, reB;
+    /* restricted top levels read M cells outside the band in their final
+     * argmax (see top_free_endgaps); count of reads where that changed the
+     * result, which then follows the defined rule */
+    int stale_argmax;
     sc_t *D;       /* |arcsA| x |arcsB| */
     sc_t *M[8];    /* (n+1) x (m+1) */
     sc_t *E[4];    /* m+1 */
@@ -421,47 +428,65 @@ static void align_D(Ctx *c) {
 /* align_top_level_free_endgaps, aligner.cc:736-819 */
 static sc_t top_free_endgaps(Ctx *c) {
     int fe = c->o->free_endgaps;
-    int n = c->n, m = c->m;
-    init_state(c, E_NO_NO, 0, n + 1, 0, m + 1, !(fe & LCG_FREE_LEFT_2), 0, !(fe & LCG_FREE_LEFT_1), 0);
-    for (int i = 1; i <= n; ++i) {
+    int sA = c->rsA, sB = c->rsB, n = c->reA, m = c->reB;  /* the restriction */
+    init_state(c, E_NO_NO, sA - 1, n + 1, sB - 1, m + 1, !(fe & LCG_FREE_LEFT_2), 0, !(fe & LCG_FREE_LEFT_1), 0);
+    for (int i = sA; i <= n; ++i) {
         c->F[E_NO_NO] = NEG_INF;
-        int lo = imax(1, minc(c, i)), hi = imin(m, maxc(c, i));
+        int lo = imax(sB, minc(c, i)), hi = imin(m, maxc(c, i));
         for (int j = lo; j <= hi; ++j) {
-            MM(c, E_NO_NO, i, j) = norm(align_noex(c, E_NO_NO, 0, 0, i, j));
+            MM(c, E_NO_NO, i, j) = norm(align_noex(c, E_NO_NO, sA - 1, sB - 1, i, j));
             if (c->cnt) c->cnt->cells++;
         }
     }
-    sc_t best = MM(c, E_NO_NO, n, m);
+    /* The final argmax reads M(n,m) and, with free right end gaps, column m
+     * of every row whose band reaches m (aligner.cc:771-799). For an interval
+     * of k-best alignment these cells can lie outside the band, where the
+     * reference's reused M holds whatever earlier computations left
+     * (aligner.cc:118-131). Such a cell counts as -inf here (the rule the GPU
+     * follows); the reference's value is still evaluated, and a difference in
+     * the outcome is counted in stale_argmax. On the whole sequences every
+     * cell read is in the band. */
+    int origin_nm = (n == sA - 1 && m == sB - 1);
+    sc_t best = (valid(c, n, m) || origin_nm) ? MM(c, E_NO_NO, n, m) : NEG_INF;
+    sc_t best_ref = MM(c, E_NO_NO, n, m);
     c->max_i = n; c->max_j = m;
+    int ri = n, rj = m;
     if (fe & (LCG_FREE_RIGHT_1 | LCG_FREE_RIGHT_2)) {
-        best = NEG_INF; c->max_i = 0; c->max_j = 0;
+        best = NEG_INF; c->max_i = sA - 1; c->max_j = sB - 1;
+        best_ref = NEG_INF; ri = sA - 1; rj = sB - 1;
     }
     int ra = c->t->right_anchor_a, rb = c->t->right_anchor_b;
     if (fe & LCG_FREE_RIGHT_2) {
-        for (int i = imax(ra + 1, 1); i <= n; ++i)
-            if (maxc(c, i) >= m && MM(c, E_NO_NO, i, m) > best) { best = MM(c, E_NO_NO, i, m); c->max_i = i; c->max_j = m; }
+        for (int i = imax(ra + 1, sA); i <= n; ++i) {
+            if (maxc(c, i) < m) continue;
+            if (minc(c, i) <= m && MM(c, E_NO_NO, i, m) > best) { best = MM(c, E_NO_NO, i, m); c->max_i = i; c->max_j = m; }
+            if (MM(c, E_NO_NO, i, m) > best_ref) { best_ref = MM(c, E_NO_NO, i, m); ri = i; rj = m; }
+        }
     }
     if (fe & LCG_FREE_RIGHT_1) {
-        int lo = imax(imax(rb + 1, 1), minc(c, n)), hi = imin(m, maxc(c, n));
-        for (int j = lo; j <= hi; ++j)
+        int lo = imax(imax(rb + 1, sB), minc(c, n)), hi = imin(m, maxc(c, n));
+        for (int j = lo; j <= hi; ++j) {
             if (MM(c, E_NO_NO, n, j) > best) { best = MM(c, E_NO_NO, n, j); c->max_i = n; c->max_j = j; }
+            if (MM(c, E_NO_NO, n, j) > best_ref) { best_ref = MM(c, E_NO_NO, n, j); ri = n; rj = j; }
+        }
     }
+    if (norm(best_ref) != norm(best) || ri != c->max_i || rj != c->max_j) c->stale_argmax++;
     return best;
 }
 
 /* align_top_level_locally, aligner.cc:823-880 */
 static sc_t top_locally(Ctx *c) {
-    int n = c->n, m = c->m;
+    int sA = c->rsA, sB = c->rsB, n = c->reA, m = c->reB;  /* the restriction */
     sc_t best = 0;
-    c->max_i = 0; c->max_j = 0;
-    init_state(c, E_NO_NO, 0, n + 1, 0, m + 1, 0, 0, 0, 0);
+    c->max_i = sA - 1; c->max_j = sB - 1;
+    init_state(c, E_NO_NO, sA - 1, n + 1, sB - 1, m + 1, 0, 0, 0, 0);
     int ra = c->t->right_anchor_a, rb = c->t->right_anchor_b;
     int la = c->t->left_anchor_a, lb = c->t->left_anchor_b;
-    for (int i = 1; i <= n; ++i) {
+    for (int i = sA; i <= n; ++i) {
         c->F[E_NO_NO] = NEG_INF;
-        int lo = imax(1, minc(c, i)), hi = imin(m, maxc(c, i));
+        int lo = imax(sB, minc(c, i)), hi = imin(m, maxc(c, i));
         for (int j = lo; j <= hi; ++j) {
-            sc_t v = norm(align_noex(c, E_NO_NO, 0, 0, i, j));
+            sc_t v = norm(align_noex(c, E_NO_NO, sA - 1, sB - 1, i, j));
             if (i < la && j < lb) v = smax(0, v);
             MM(c, E_NO_NO, i, j) = v;
             if (c->cnt) c->cnt->cells++;
@@ -697,6 +722,7 @@ int lcg_oracle_align(const lcg_pair_tables *t, const lcg_align_opts *o,
     for (int s = 0; s < 8; ++s) if (!c.M[s]) c.M[s] = NULL;
     if (!c.D || !c.M[0]) { ctx_free(&c); return -1; }
     c.min_i = 1; c.min_j = 1; c.max_i = c.n; c.max_j = c.m;
+    c.rsA = 1; c.rsB = 1; c.reA = c.n; c.reB = c.m;
 
     align_D(&c);
     c.edges = r->edges; c.edge_cap = r->edges ? c.n + c.m : 0;
@@ -715,7 +741,7 @@ int lcg_oracle_align(const lcg_pair_tables *t, const lcg_align_opts *o,
             c.mod = 1;
             sc_t s = top_locally(&c);
             c.nedges = 0; c.ntam = 0;
-            trace_in_arcmatch(&c, E_NO_NO, 0, c.max_i, 0, c.max_j, 1);
+            trace_in_arcmatch(&c, E_NO_NO, c.rsA - 1, c.max_i, c.rsB - 1, c.max_j, 1);
             sc_t length = (sc_t)(c.max_i - c.min_i + 1) + (c.max_j - c.min_j + 1);
             s += length * lambda;
             if (length + o->normalized_L <= 0) { ctx_free(&c); return -2; }
@@ -729,16 +755,73 @@ int lcg_oracle_align(const lcg_pair_tables *t, const lcg_align_opts *o,
         c.lam = o->position_penalty;
         c.mod = 1;
         score = o->sequ_local ? top_locally(&c) : top_free_endgaps(&c);
-        trace_in_arcmatch(&c, E_NO_NO, 0, c.max_i, 0, c.max_j, 1);
+        trace_in_arcmatch(&c, E_NO_NO, c.rsA - 1, c.max_i, c.rsB - 1, c.max_j, 1);
         traced = 1;
     } else {
         score = o->sequ_local ? top_locally(&c) : top_free_endgaps(&c);
     }
     r->score = score < MIN_FINITY ? LCG_NEG_INF : score;
     r->num_edges = 0; r->num_traced_am = 0;
-    if (o->do_trace && !traced) trace_in_arcmatch(&c, E_NO_NO, 0, c.max_i, 0, c.max_j, 1);
+    if (o->do_trace && !traced) trace_in_arcmatch(&c, E_NO_NO, c.rsA - 1, c.max_i, c.rsB - 1, c.max_j, 1);
     if (o->do_trace || traced) { r->num_edges = c.nedges; r->num_traced_am = c.ntam; }
     r->max_i = c.max_i; r->max_j = c.max_j; r->min_i = c.min_i; r->min_j = c.min_j;
     ctx_free(&c);
     return 0;
+}
+
+/* ---------------------------------------------------------------- k-best
+ *
+ * A context for Aligner::suboptimal (aligner.cc:1384-1512, driven by
+ * oracle/kbest_oracle.cc): D is filled once for the whole sequences (the
+ * first align() of an Aligner), then the top level and its trace run again
+ * per restriction, as set_restriction() + align() + trace() do.
+ */
+void *lcg_oracle_ctx_new(const lcg_pair_tables *t, const lcg_align_opts *o) {
+    Ctx *c = calloc(1, sizeof(Ctx));
+    if (!c) return NULL;
+    c->t = t; c->o = o; c->n = t->len_a; c->m = t->len_b;
+    build_radj(t->arcs_a, t->num_arcs_a, c->n, &c->radjA_start, &c->radjA);
+    build_radj(t->arcs_b, t->num_arcs_b, c->m, &c->radjB_start, &c->radjB);
+    build_am_lists(c);
+    if (o->no_lonely_pairs || t->am_stack_score) init_inner(c);
+    size_t nd = (size_t)t->num_arcs_a * t->num_arcs_b;
+    c->D = malloc((nd > 0 ? nd : 1) * sizeof(sc_t));
+    for (size_t q = 0; q < nd; ++q) c->D[q] = NEG_INF;
+    size_t cells = (size_t)(c->n + 1) * (c->m + 1);
+    for (int s = 0; s < (o->struct_local ? 8 : 1); ++s) c->M[s] = calloc(cells, sizeof(sc_t));
+    for (int s = 0; s < (o->struct_local ? 4 : 1); ++s) c->E[s] = calloc(c->m + 1, sizeof(sc_t));
+    c->min_i = 1; c->min_j = 1; c->max_i = c->n; c->max_j = c->m;
+    c->rsA = 1; c->rsB = 1; c->reA = c->n; c->reB = c->m;
+    align_D(c);
+    return c;
+}
+
+/* Aligner::set_restriction + align(): the score of the top level restricted
+ * to A[sA..eA], B[sB..eB] (LCG_NEG_INF for -inf) */
+long long lcg_oracle_ctx_top(void *ctx, int sA, int sB, int eA, int eB) {
+    Ctx *c = ctx;
+    c->rsA = sA; c->rsB = sB; c->reA = eA; c->reB = eB;
+    sc_t s = c->o->sequ_local ? top_locally(c) : top_free_endgaps(c);
+    return s < MIN_FINITY ? LCG_NEG_INF : s;
+}
+
+/* Aligner::trace() of the last top level: edges, traced arc matches and end
+ * cells into r (capacities as for lcg_oracle_align) */
+void lcg_oracle_ctx_trace(void *ctx, lcg_align_result *r) {
+    Ctx *c = ctx;
+    c->edges = r->edges; c->edge_cap = r->edges ? c->n + c->m : 0; c->nedges = 0;
+    c->tam = r->traced_am; c->tam_cap = r->traced_am ? (c->n < c->m ? c->n : c->m) : 0; c->ntam = 0;
+    trace_in_arcmatch(c, E_NO_NO, c->rsA - 1, c->max_i, c->rsB - 1, c->max_j, 1);
+    r->num_edges = c->nedges; r->num_traced_am = c->ntam;
+    r->max_i = c->max_i; r->max_j = c->max_j; r->min_i = c->min_i; r->min_j = c->min_j;
+}
+
+/* number of restricted top levels whose argmax the reference would have
+ * taken from a cell outside the band (see top_free_endgaps) */
+int lcg_oracle_ctx_stale(void *ctx) { return ((Ctx *)ctx)->stale_argmax; }
+
+void lcg_oracle_ctx_free(void *ctx) {
+    if (!ctx) return;
+    ctx_free((Ctx *)ctx);
+    free(ctx);
 }

@@ -29,3 +29,17 @@ def assert_same_result(a, b, name=""):
     assert a.max_ij == b.max_ij, (name, a.max_ij, b.max_ij)
     assert a.edges == b.edges, (name, "raw edges differ")
     assert a.traced_am == b.traced_am, (name, "traced arc matches differ")
+
+
+def assert_kbest_matches_golden(g, hits):
+    """k-best hits (Aligner::suboptimal) against the reference's: score,
+    full edges and structure strings of every hit, in order."""
+    t = g.tables
+    ref = g.kbest_hits()
+    assert len(hits) == len(ref), (g.name, len(hits), len(ref))
+    for h, (res, (sc, edges, (sa, sb))) in enumerate(zip(hits, ref)):
+        assert res.score == sc, (g.name, h, res.score, sc)
+        e = full_edges(t, res)
+        assert e == edges, (g.name, h, "edges differ")
+        ga, gb = structure_strings(e, t.len_a, t.len_b, traced_arcs(t, res.traced_am))
+        assert (ga, gb) == (sa, sb), (g.name, h, "structure strings differ")

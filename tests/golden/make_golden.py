@@ -79,6 +79,12 @@ CASES = {
     "c150_penalized": (150, 1, 150, 2, {"sequ_local": "1", "penalized": "20"}, True),
     "h200_penalized_global": (200, 83, "h", 84, {"penalized": "30", "free_endgaps": "++++"}, True),
     "h180_penalized_sl": (180, 85, "h", 86, {"sequ_local": "1", "penalized": "25", "struct_local": "1"}, True),
+    # locarna --kbest k [--better t] (Aligner::suboptimal: k best local alignments by interval splitting)
+    "c150_kbest": (150, 1, 150, 2, {"sequ_local": "1", "kbest": "6"}, True),
+    "h200_kbest": (200, 83, "h", 84, {"sequ_local": "1", "kbest": "8"}, True),
+    "h180_kbest_nolp_better": (180, 85, "h", 86, {"sequ_local": "1", "kbest": "10", "no_lonely_pairs": "1",
+                                                  "better": "3000"}, True),
+    "c150_kbest_global": (150, 11, 140, 12, {"kbest": "4", "free_endgaps": "++++"}, True),
 }
 
 STACK_KEYS = ("stacking", "new_stacking")
@@ -116,6 +122,19 @@ def make_case(name, spec, workdir):
     if t.am_stack_score is not None:
         out["am_stack_score"] = t.am_stack_score
         out["am_stackable"] = t.am_stackable
+    if ref["khits"]:
+        # the harness's enumeration must give the reference's own hits
+        # (score, first position in A, last position in B)
+        mine = []
+        for sc, _, local in ref["khits"]:
+            pa = [a for a, _ in local if a > 0]
+            pb = [b for _, b in local if b > 0]
+            mine.append((sc, pa[0] if pa else 0, pb[-1] if pb else 0))
+        assert mine == ref["hits"], (name, mine, ref["hits"])
+        out["kbest_scores"] = np.array([h[0] for h in ref["khits"]], dtype=np.int64)  # hit scores
+        out["kbest_edges"] = np.concatenate([np.array(h[1], dtype=np.int32) for h in ref["khits"]])
+        out["kbest_nedges"] = np.array([len(h[1]) for h in ref["khits"]], dtype=np.int32)
+        out["kbest_struct"] = "|".join(a + " " + b for a, b in ref["kstruct"])
     np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
     return ref
 

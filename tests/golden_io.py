@@ -55,6 +55,24 @@ class Golden:
         return self.opts.get("free_endgaps", "----")
 
     @property
+    def kbest(self):
+        """(k, threshold) of --kbest k --better t, or None"""
+        if "kbest" not in self.opts:
+            return None
+        return int(self.opts["kbest"]), int(self.opts.get("better", -1000000))
+
+    def kbest_hits(self):
+        """The reference's k-best hits: [(score, full edges, (structA, structB))]"""
+        z = np.load(os.path.join(GOLDEN_DIR, self.name + ".npz"))
+        out, pos = [], 0
+        structs = str(z["kbest_struct"]).split("|")
+        for sc, ne, st in zip(z["kbest_scores"], z["kbest_nedges"], structs):
+            e = [tuple(int(v) for v in x) for x in z["kbest_edges"][pos:pos + ne]]
+            pos += ne
+            out.append((int(sc), e, tuple(st.split(" "))))
+        return out
+
+    @property
     def no_lonely_pairs(self):
         return self.opts.get("no_lonely_pairs") == "1"
 

@@ -22,6 +22,31 @@ def load_oracle():
     return _lib
 
 
+def oracle_kbest(tables, k, threshold=-1000000, stale=False, **kw):
+    """Aligner::suboptimal restated (oracle/kbest_oracle.cc): up to k hits,
+    each an AlignResult whose score is the hit's score. With stale=True also
+    the number of interval top levels whose argmax the reference takes from a
+    cell outside the band."""
+    lib = load_oracle()
+    if not getattr(lib, "_kbest_ready", False):
+        lib.lcg_oracle_kbest.argtypes = [C.POINTER(lcg_pair_tables), C.POINTER(lcg_align_opts), C.c_int,
+                                         C.c_longlong, C.POINTER(lcg_align_result), C.POINTER(C.c_int)]
+        lib.lcg_oracle_kbest.restype = C.c_int
+        lib._kbest_ready = True
+    o = make_opts(**kw)
+    bufs = [ResultBuffers(tables.len_a, tables.len_b) for _ in range(k)]
+    arr = (lcg_align_result * k)(*[b.c for b in bufs])
+    ct = tables.to_c()
+    ns = C.c_int(0)
+    nh = lib.lcg_oracle_kbest(C.byref(ct), C.byref(o), k, threshold, arr, C.byref(ns))
+    assert nh >= 0
+    out = []
+    for h in range(nh):
+        bufs[h].c = arr[h]
+        out.append(bufs[h].decode())
+    return (out, ns.value) if stale else out
+
+
 def oracle_align(tables, counts=False, **kw):
     lib = load_oracle()
     o = make_opts(**kw)

@@ -14,10 +14,27 @@ def _pairs(tokens, conv=int):
 
 def parse_ref(text):
     rec = {}
+    hits, khits, kstruct = [], [], []
     for line in text.splitlines():
         if not line.strip():
             continue
         key, _, rest = line.partition(" ")
+        # k-best: "HIT score startA startA endB endB" (Aligner::suboptimal's own
+        # output), "khit score edges..." / "kstruct A B" (the harness's hits)
+        if key == "HIT":
+            v = [int(x) for x in rest.split()]
+            hits.append((v[0], v[1], v[3]))
+            continue
+        if key == "khit":
+            t = rest.split()
+            khits.append((int(t[0]), _pairs(t[1:])))
+            continue
+        if key == "klocal":
+            khits[-1] = khits[-1] + (_pairs(rest.split()),)
+            continue
+        if key == "kstruct":
+            kstruct.append(tuple(rest.split()))
+            continue
         rec[key] = rest.split() if key not in ("seqA", "seqB", "structA", "structB") else rest.strip()
     n, m = (int(x) for x in rec["lens"])
     out = {"len_a": n, "len_b": m, "seq_a": rec["seqA"], "seq_b": rec["seqB"]}
@@ -32,6 +49,7 @@ def parse_ref(text):
     out["struct_a"] = rec["structA"]
     out["struct_b"] = rec["structB"]
     out["align_seconds"] = float(rec["align_seconds"][0])
+    out["hits"], out["khits"], out["kstruct"] = hits, khits, kstruct
     if "sigma" in rec:
         sig = np.zeros((n + 1, m + 1), dtype=np.int32)
         sig[1:, 1:] = np.array([int(x) for x in rec["sigma"]], dtype=np.int32).reshape(n, m)

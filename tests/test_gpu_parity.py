@@ -156,3 +156,41 @@ def test_gpu_normalized_rejects_global_mode(engine):
         engine.align_pairs([g.tables], normalized=100)
     with pytest.raises(LcgError):
         engine.align_pairs([g.tables], sequ_local=True, normalized=100, penalized=10)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", [n for n in GPU_CASES if "kbest" in n])
+def test_gpu_kbest_matches_reference(engine, name):
+    """locarna --kbest k (Aligner::suboptimal, interval splitting): every hit
+    of the reference's enumeration, in order, bit-exact through
+    lcg_align_kbest."""
+    from checks import assert_kbest_matches_golden
+    g = Golden(name)
+    hits = engine.align_kbest([g.tables], *g.kbest, **g.align_kwargs())[0]
+    assert_kbest_matches_golden(g, hits)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prep_kw,mode,k,thr", [
+    ({}, {"sequ_local": True}, 7, -1000000),
+    ({}, {"sequ_local": True, "no_lonely_pairs": True}, 5, 800),
+    ({"stacking": 1, "exp_prob": 0.005}, {"sequ_local": True, "struct_local": True}, 4, -1000000),
+    ({}, {"free_endgaps": "++++"}, 3, -1000000),
+    ({}, {}, 4, -1000000),
+])
+def test_gpu_kbest_matches_oracle(engine, prep_kw, mode, k, thr):
+    """k-best hits of a batch of homologous and unrelated pairs against the
+    oracle's restatement of Aligner::suboptimal, pair by pair and hit by hit.
+    (Global intervals can end on cells outside the band, which both count as
+    -inf; the reference reads stale matrix cells there.)"""
+    from oracle_ffi import oracle_kbest
+    tables = _homolog_tables(prep_kw, count=3, length=110, seed=501)
+    got = engine.align_kbest(tables, k, thr, **mode)
+    total = 0
+    for q, t in enumerate(tables):
+        ref = oracle_kbest(t, k, thr, **mode)
+        assert len(got[q]) == len(ref), (q, len(got[q]), len(ref))
+        for h, (a, b) in enumerate(zip(got[q], ref)):
+            assert_same_result(a, b, f"pair {q} hit {h}")
+        total += len(ref)
+    assert total > len(tables)

@@ -9,7 +9,7 @@ _OPT_MAP = {"sequ_local": ("sequ_local", int), "free_endgaps": ("free_endgaps", 
             "min_trace_prob": ("min_trace_probability", float), "indel_opening": ("indel_opening", int),
             "struct_local": None, "no_lonely_pairs": None, "stacking": ("stacking", int),
             "new_stacking": ("new_stacking", int), "exp_prob": ("exp_prob", float),
-            "normalized": None, "penalized": None}
+            "normalized": None, "penalized": None, "kbest": None, "better": None}
 
 
 def prep_kwargs(g):
