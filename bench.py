@@ -217,6 +217,47 @@ class ClockSampler:
 
 # ---------------------------------------------------------------- LocARNA-P
 
+MODES_SAMPLE = 256  # pairs of the workload (every 8th) for the alignment-mode lines
+
+
+def run_modes(eng, tables, flush_l2):
+    """Sequence-local alignment modes on a sample of the workload's pairs
+    (every 8th of the 2,016): plain local, --normalized 100 (Dinkelbach
+    iterations), --penalized 50 and --kbest 5; pairs per second of the public
+    calls (wall, host tables in and results out) and their device time, each
+    checked against the oracle on a few pairs."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from checks import assert_same_result
+    from oracle_ffi import oracle_align, oracle_kbest
+    sample = tables[::max(1, len(tables) // MODES_SAMPLE)][:MODES_SAMPLE]
+    out = {"sample": f"{len(sample)} pairs (every {max(1, len(tables) // MODES_SAMPLE)}th of the workload)"}
+    specs = [("local", dict(sequ_local=True)), ("normalized_100", dict(sequ_local=True, normalized=100)),
+             ("penalized_50", dict(sequ_local=True, penalized=50))]
+    for name, kw in specs:
+        eng.align_pairs(sample[:8], **kw)
+        flush_l2()
+        t0 = time.perf_counter()
+        res = eng.align_pairs(sample, **kw)
+        wall = time.perf_counter() - t0
+        dev_ms = eng.last_stats()[0]
+        for k in range(0, len(sample), 64):
+            assert_same_result(res[k], oracle_align(sample[k], **kw), f"{name} pair {k}")
+        out[name] = {"pairs_per_s": len(sample) / wall, "device_ms": dev_ms, "launches": eng.last_stats()[1]}
+    eng.align_kbest(sample[:8], 5, sequ_local=True)
+    flush_l2()
+    t0 = time.perf_counter()
+    hits = eng.align_kbest(sample, 5, sequ_local=True)
+    wall = time.perf_counter() - t0
+    for k in range(0, len(sample), 64):
+        ref = oracle_kbest(sample[k], 5, sequ_local=True)
+        assert len(ref) == len(hits[k])
+        for a, b in zip(hits[k], ref):
+            assert_same_result(a, b, f"kbest pair {k}")
+    out["kbest_5"] = {"pairs_per_s": len(sample) / wall, "hits": sum(len(h) for h in hits),
+                      "launches": eng.last_stats()[1]}
+    return out
+
+
 def run_pf(eng, tables, flush_l2, cpu):
     """LocARNA-P: FP64 and FP32-scaled inside + adjoint outside over a
     size-stratified sample of the pairs (every PF_STRIDE-th pair in size
@@ -448,6 +489,8 @@ def run_ours(args):
             "e2e_aligns_per_s": npairs / (sum(nolp_wall) / len(nolp_wall)),
             "stacked_arc_matches_traced": sum(len(r.traced_am) for r in nres)}
 
+    modes = run_modes(eng, tables, flush_l2)
+
     T = kern_ms / 1e3 / args.steps
     Tf = fill_ms / 1e3 / args.steps
     We = wall_s / args.steps
@@ -497,6 +540,7 @@ def run_ours(args):
         "clocks": clocks,
         "table_prep": table_prep,
         "nolp": nolp,
+        "modes": modes,
     }
     if pf_tables is not None:
         out["locarna_p"] = run_pf(eng, pf_tables, flush_l2, pf_cpu)

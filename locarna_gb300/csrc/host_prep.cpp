@@ -54,7 +54,10 @@ struct PrepError {
 
 struct RnaInput {
     std::string name;
-    std::string seq;                  // normalised (upper case, T -> U), 1-based via seq[i-1]
+    std::string seq;                  // normalised (upper case, T -> U), 1-based via seq[i-1]; the first row
+    // all rows (a multiple alignment: a profile of equal-length rows,
+    // MultipleAlignment of the PP sequence section); rows[0] == seq
+    std::vector<std::string> rows;
     std::map<std::pair<int, int>, double> arc_probs;  // (i,j) -> p, i<j (sparse matrix)
     // joint probabilities of (i,j) and (i+1,j-1) (the p2 column, read only with stacking)
     std::map<std::pair<int, int>, double> arc2_probs;
@@ -124,15 +127,23 @@ RnaInput read_pp(const std::string &text, double p_bpcut, bool stacking) {
         }
     } while (next_line(in, line));
     if (names.empty()) perr(LCG_ERR_PARSE, "PP file without sequence");
-    if (names.size() > 1) perr(LCG_ERR_UNSUPPORTED, "multiple-sequence (alignment) PP input is not supported yet");
     if (!anchors.empty()) perr(LCG_ERR_UNSUPPORTED, "anchor constraints (#A lines) are not supported yet");
     r.name = names[0];
-    r.seq = seqs[names[0]];
-    if (r.seq.empty()) perr(LCG_ERR_PARSE, "empty sequence");
-    for (auto &c : r.seq) {
-        c = (char)std::toupper((unsigned char)c);
-        if (c == 'T') c = 'U';
+    // MultipleAlignment::normalize_rna_symbols (multiple_alignment.cc:577-584,
+    // aux.cc:65-70) on every row; the rows of an alignment must have equal
+    // lengths (MultipleAlignment::is_proper)
+    for (auto &nm : names) {
+        std::string row = seqs[nm];
+        for (auto &c : row) {
+            c = (char)std::toupper((unsigned char)c);
+            if (c == 'T') c = 'U';
+        }
+        if (!r.rows.empty() && row.size() != r.rows[0].size())
+            perr(LCG_ERR_PARSE, "alignment rows of different lengths in the sequence section");
+        r.rows.push_back(row);
     }
+    r.seq = r.rows[0];
+    if (r.seq.empty()) perr(LCG_ERR_PARSE, "empty sequence");
     // base pair section
     if (!next_line(in, line) || line != "#SECTION BASEPAIRS") perr(LCG_ERR_PARSE, "Expected base pair section header.");
     const size_t len = r.seq.size();
@@ -261,6 +272,45 @@ long riboX_single(char al, char ar, char bl, char br) {
     return round2score(100.0 * score / 1);
 }
 
+// One row pair's term of Scoring::sigma_ (scoring.cc:155-193): the RIBOSUM
+// base-match score for two bases, else match / mismatch unless one is 'N'
+long sigma_term(const lcg_prep_opts &o, char ca, char cb) {
+    int a = idx_acgu(ca), b = idx_acgu(cb);
+    if (o.use_ribosum && a >= 0 && b >= 0) return round2score(100.0 * basematch_score_corrected(a, b));
+    if (ca != 'N' && cb != 'N') return (ca == cb) ? o.match : o.mismatch;
+    return 0;
+}
+
+// Scoring::riboX_arcmatch_score (scoring.cc:368-438) for profiles: the average
+// over the row pairs whose four ends are bases
+long riboX_profile(const RnaInput &A, int al, int ar, const RnaInput &B, int bl, int br) {
+    double score = 0;
+    int considered = 0;
+    for (const auto &ra : A.rows) {
+        for (const auto &rb : B.rows) {
+            const char c1 = ra[al - 1], c2 = ra[ar - 1], c3 = rb[bl - 1], c4 = rb[br - 1];
+            if (c1 == '-' || c2 == '-' || c3 == '-' || c4 == '-') continue;
+            const int a1 = idx_acgu(c1), a2 = idx_acgu(c2), b1 = idx_acgu(c3), b2 = idx_acgu(c4);
+            if (a1 < 0 || a2 < 0 || b1 < 0 || b2 < 0) continue;
+            considered++;
+            score += log(kArcmatchProbs[(a1 * 4 + a2) * 16 + (b1 * 4 + b2)] /
+                         (kBasepairProbs[a1 * 4 + a2] * kBasepairProbs[b1 * 4 + b2])) /
+                     log(2);
+        }
+    }
+    if (considered == 0) return 0;
+    return round2score(100.0 * score / considered);
+}
+
+// Scoring::precompute_gapcost (scoring.cc:271-311): the gap cost of a column
+// scaled by its fraction of non-gap rows (in float, as the reference)
+int32_t column_gapcost(const RnaInput &in, int i, int indel) {
+    float gf = 0;
+    for (const auto &r : in.rows) gf += (r[i - 1] == '-') ? 1 : 0;
+    gf /= (float)in.rows.size();
+    return (int32_t)round2score((1 - gf) * indel);
+}
+
 long prob_to_weight(double p, double pe, int struct_weight) {
     // Scoring::probToWeight (scoring.cc:250-265)
     return round2score(round(struct_weight * (1 - log(p) / log(pe))));
@@ -287,7 +337,7 @@ struct Band {
     std::vector<long> minc, maxc;  // size_t in the reference; all values >= 0
 };
 
-// StralScore::sigma (stral_score.cc:29-60) for single sequences; `rev`
+// StralScore::sigma (stral_score.cc:29-60) for sequences or profiles; `rev`
 // evaluates the reversed object (StralScore::reverse, :78-100), whose
 // up/down vectors are swapped and reversed.
 struct Stral {
@@ -301,12 +351,18 @@ struct Stral {
         int ia = rev ? n + 1 - i : i, jb = rev ? m + 1 - j : j;
         double seq_score = 0;
         int pairs = 0;
-        int a = idx_acgu(A->in.seq[ia - 1]), b = idx_acgu(B->in.seq[jb - 1]);
-        if (a >= 0 && b >= 0) {
-            // sim_mat: ribosum base-match scores, or match/mismatch
-            // (MainHelper::select_basematch_scores, main_helper.icc:281-306)
-            seq_score += ribosum ? kBmScore[a * 4 + b] : (a == b ? match : mismatch);
-            pairs++;
+        // the average over the row pairs of the two columns whose characters
+        // are both in the alphabet (one pair for single sequences)
+        for (const auto &ra : A->in.rows) {
+            for (const auto &rb : B->in.rows) {
+                int a = idx_acgu(ra[ia - 1]), b = idx_acgu(rb[jb - 1]);
+                if (a >= 0 && b >= 0) {
+                    // sim_mat: ribosum base-match scores, or match/mismatch
+                    // (MainHelper::select_basematch_scores, main_helper.icc:281-306)
+                    seq_score += ribosum ? kBmScore[a * 4 + b] : (a == b ? match : mismatch);
+                    pairs++;
+                }
+            }
         }
         if (pairs != 0) seq_score /= pairs;
         double dA = rev ? A->p_up[ia] : A->p_down[ia];
@@ -625,10 +681,49 @@ void stage_tables(Staged &S) {
     P->stacking = (o.stacking && o.exp_prob > 0) || o.new_stacking;
     // scoring tables
     P->sigma.assign((size_t)(n + 1) * (m + 1), 0);
+    const bool profiles = A.in.rows.size() > 1 || B.in.rows.size() > 1;
     long tab[256][256];
     bool have[256][256];
     std::memset(have, 0, sizeof have);
-    for (int i = 1; i <= n; ++i) {
+    if (profiles) {
+        // Scoring::sigma_ (scoring.cc:140-198): the sum over the row pairs of
+        // the two columns, divided (in integers) by their number; summed per
+        // column by the counts of its distinct characters
+        auto hist = [](const RnaInput &in, int len) {
+            std::vector<std::vector<std::pair<unsigned char, long>>> h(len + 1);
+            for (int i = 1; i <= len; ++i) {
+                for (const auto &r : in.rows) {
+                    const unsigned char c = (unsigned char)r[i - 1];
+                    bool found = false;
+                    for (auto &x : h[i])
+                        if (x.first == c) {
+                            x.second++;
+                            found = true;
+                        }
+                    if (!found) h[i].push_back({c, 1});
+                }
+            }
+            return h;
+        };
+        const auto hA = hist(A.in, n), hB = hist(B.in, m);
+        const long npairs_rows = (long)(A.in.rows.size() * B.in.rows.size());
+        for (int i = 1; i <= n; ++i) {
+            for (int j = 1; j <= m; ++j) {
+                long score = 0;
+                for (const auto &x : hA[i]) {
+                    for (const auto &y : hB[j]) {
+                        if (!have[x.first][y.first]) {
+                            tab[x.first][y.first] = sigma_term(o, (char)x.first, (char)y.first);
+                            have[x.first][y.first] = true;
+                        }
+                        score += x.second * y.second * tab[x.first][y.first];
+                    }
+                }
+                P->sigma[(size_t)i * (m + 1) + j] = (int32_t)round2score((double)(score / (int)npairs_rows));
+            }
+        }
+    }
+    for (int i = 1; i <= n && !profiles; ++i) {
         unsigned char ca = (unsigned char)A.in.seq[i - 1];
         for (int j = 1; j <= m; ++j) {
             unsigned char cb = (unsigned char)B.in.seq[j - 1];
@@ -642,14 +737,8 @@ void stage_tables(Staged &S) {
     // Scoring::precompute_gapcost (scoring.cc:271-311) for gap-free rows
     P->gap_a.assign(n + 1, 0);
     P->gap_b.assign(m + 1, 0);
-    for (int i = 1; i <= n; ++i) {
-        float gf = A.in.seq[i - 1] == '-' ? 1.0f : 0.0f;
-        P->gap_a[i] = (int32_t)round2score((1 - gf) * o.indel);
-    }
-    for (int j = 1; j <= m; ++j) {
-        float gf = B.in.seq[j - 1] == '-' ? 1.0f : 0.0f;
-        P->gap_b[j] = (int32_t)round2score((1 - gf) * o.indel);
-    }
+    for (int i = 1; i <= n; ++i) P->gap_a[i] = column_gapcost(A.in, i, o.indel);
+    for (int j = 1; j <= m; ++j) P->gap_b[j] = column_gapcost(B.in, j, o.indel);
     P->indel_opening = o.indel_opening;
     P->exclusion = o.exclusion;
 
@@ -679,7 +768,9 @@ void stage_tables(Staged &S) {
             if (!ok) continue;
             long seqc = 0;
             if (o.tau != 0) {
-                if (o.use_ribosum) {
+                if (o.use_ribosum && profiles) {
+                    seqc = riboX_profile(A.in, a.l, a.r, B.in, b.l, b.r);
+                } else if (o.use_ribosum) {
                     char c1 = A.in.seq[a.l - 1], c2 = A.in.seq[a.r - 1];
                     char c3 = B.in.seq[b.l - 1], c4 = B.in.seq[b.r - 1];
                     int x1 = idx_acgu(c1), x2 = idx_acgu(c2), x3 = idx_acgu(c3), x4 = idx_acgu(c4);
@@ -724,8 +815,10 @@ void stage_tables(Staged &S) {
     }
     P->code_a.assign(n + 1, -1);
     P->code_b.assign(m + 1, -1);
-    for (int i = 1; i <= n; ++i) P->code_a[i] = (int8_t)idx_acgu(A.in.seq[i - 1]);
-    for (int j = 1; j <= m; ++j) P->code_b[j] = (int8_t)idx_acgu(B.in.seq[j - 1]);
+    // base codes for the base-match gradients of LocARNA-P: single sequences
+    // only (a profile column is no single base)
+    for (int i = 1; i <= n && A.in.rows.size() == 1; ++i) P->code_a[i] = (int8_t)idx_acgu(A.in.seq[i - 1]);
+    for (int j = 1; j <= m && B.in.rows.size() == 1; ++j) P->code_b[j] = (int8_t)idx_acgu(B.in.seq[j - 1]);
     P->min_col.resize(n + 1);
     P->max_col.resize(n + 1);
     for (int i = 0; i <= n; ++i) {
@@ -869,8 +962,11 @@ lcg_status lcg_prepare_pairs(lcg_engine eng, const char *const *pp_a, const char
         std::vector<lcg_env::PairIn> in;
         std::vector<lcg_env::PairOut> res;
         std::vector<int> gpu_q;
+        // the kernel scores single sequences; profiles take the host path
         for (int q = 0; q < npairs; ++q)
-            if (st[q].pa->len + st[q].pb->len <= max_len_sum) gpu_q.push_back(q);
+            if (st[q].pa->len + st[q].pb->len <= max_len_sum && st[q].pa->in.rows.size() == 1 &&
+                st[q].pb->in.rows.size() == 1)
+                gpu_q.push_back(q);
         in.resize(gpu_q.size());
         res.resize(gpu_q.size());
         host_parallel((int)gpu_q.size(), [&](int k) {

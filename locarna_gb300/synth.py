@@ -164,6 +164,53 @@ def make_homolog(rec, seed, sub_rate=0.1, name=None):
     return RnaRecord(name or f"{rec.name}_h{seed}", "".join(seq), pairs, seed=seed)
 
 
+class ProfileRecord:
+    """A multiple alignment (equal-length rows with '-' gaps) and the base-pair
+    probabilities of its columns: the input of progressive alignment."""
+
+    def __init__(self, name, rows, pairs, seed=0):
+        self.name = name
+        self.rows = rows  # list of (name, aligned row)
+        self.pairs = pairs  # dict (i, j) -> p over columns
+        self.seed = seed
+
+    def to_pp(self):
+        lines = ["#PP 2.0", ""] + [f"{nm} {row}" for nm, row in self.rows] + ["", "#END", "",
+                                                                             "#SECTION BASEPAIRS", ""]
+        for (i, j) in sorted(self.pairs):
+            lines.append(f"{i} {j} {self.pairs[(i, j)]:.6f}")
+        lines += ["", "#END", ""]
+        return "\n".join(lines)
+
+
+def make_profile(length, seed, nrows=3, gap_rate=0.08, name=None):
+    """A profile of ``nrows`` homologs of one synthetic RNA (make_homolog):
+    gaps are placed in each row except the first at unpaired positions (rate
+    ``gap_rate``) and in runs; the column pair probabilities are the root's."""
+    root = make_rna(length, seed)
+    rng = random.Random(seed * 31 + 7)
+    paired = set()
+    for (i, j), p in root.pairs.items():
+        if p >= 0.5:
+            paired.update((i, j))
+    rows = [(f"{name or 'p' + str(seed)}_0", root.seq)]
+    for r in range(1, nrows):
+        h = make_homolog(root, seed * 1000 + r, sub_rate=0.1)
+        row = list(h.seq)
+        pos = 1
+        while pos <= length:
+            if pos not in paired and rng.random() < gap_rate:
+                run = 1 + min(3, int(rng.random() * 4))
+                for t in range(pos, min(length, pos + run - 1) + 1):
+                    if t not in paired:
+                        row[t - 1] = "-"
+                pos += run
+            else:
+                pos += 1
+        rows.append((f"{name or 'p' + str(seed)}_{r}", "".join(row)))
+    return ProfileRecord(name or f"prof{seed}", rows, dict(root.pairs), seed=seed)
+
+
 def make_family(count, len_lo, len_hi, seed, q=0.05):
     """``count`` RNAs with lengths uniform in [len_lo, len_hi]."""
     rng = random.Random(seed)

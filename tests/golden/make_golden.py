@@ -20,13 +20,14 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.dirname(HERE))
 
-from locarna_gb300.synth import make_homolog, make_rna  # noqa: E402
+from locarna_gb300.synth import make_homolog, make_profile, make_rna  # noqa: E402
 from refdump import parse_ref  # noqa: E402
 
 HARNESS = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
 
 # name: (lenA, seedA, lenB, seedB, options, keep_tables); lenB = "h" makes B a
-# homolog of A (make_homolog with seed seedB)
+# homolog of A (make_homolog with seed seedB); a length ("p", L, rows) makes a
+# profile (make_profile: an alignment of rows homologs of one RNA)
 CASES = {
     "c150_global": (150, 1, 150, 2, {}, True),
     "c150_seqlocal": (150, 1, 150, 2, {"sequ_local": "1"}, True),
@@ -85,6 +86,15 @@ CASES = {
     "h180_kbest_nolp_better": (180, 85, "h", 86, {"sequ_local": "1", "kbest": "10", "no_lonely_pairs": "1",
                                                   "better": "3000"}, True),
     "c150_kbest_global": (150, 11, 140, 12, {"kbest": "4", "free_endgaps": "++++"}, True),
+    # profile (multiple alignment) inputs, as in mlocarna's progressive stage
+    "p120_global": (("p", 120, 3), 5, ("p", 110, 2), 6, {}, True),
+    "p150_vs_seq": (("p", 150, 4), 91, 140, 92, {}, True),
+    "p140_seqlocal": (("p", 140, 3), 95, ("p", 130, 3), 96, {"sequ_local": "1"}, True),
+    "p140_structlocal": (("p", 140, 3), 95, ("p", 130, 3), 96, {"struct_local": "1"}, True),
+    "p140_nolp_free": (("p", 140, 3), 97, ("p", 150, 2), 98, {"no_lonely_pairs": "1", "free_endgaps": "++++"},
+                       True),
+    "p130_noenv": (("p", 130, 5), 99, ("p", 120, 3), 100, {"min_trace_prob": "0"}, True),
+    "p250_global": (("p", 250, 3), 101, ("p", 240, 3), 102, {}, True),
 }
 
 STACK_KEYS = ("stacking", "new_stacking")
@@ -92,20 +102,25 @@ STACK_KEYS = ("stacking", "new_stacking")
 
 def make_case(name, spec, workdir):
     la, sa, lb, sb, opts, keep = spec
-    ra = make_rna(la, sa)
-    rb = make_homolog(ra, sb) if lb == "h" else make_rna(lb, sb)
+    ra = make_profile(la[1], sa, la[2]) if isinstance(la, tuple) else make_rna(la, sa)
+    if lb == "h":
+        rb = make_homolog(ra, sb)
+    else:
+        rb = make_profile(lb[1], sb, lb[2]) if isinstance(lb, tuple) else make_rna(lb, sb)
     st = any(k in opts for k in STACK_KEYS)  # inputs with joint (stacking) probabilities
     pa, pb = os.path.join(workdir, name + "_A.pp"), os.path.join(workdir, name + "_B.pp")
+    pp_a = ra.to_pp(stacking=st) if st else ra.to_pp()
+    pp_b = rb.to_pp(stacking=st) if st else rb.to_pp()
     with open(pa, "w") as f:
-        f.write(ra.to_pp(stacking=st))
+        f.write(pp_a)
     with open(pb, "w") as f:
-        f.write(rb.to_pp(stacking=st))
+        f.write(pp_b)
     args = [HARNESS, pa, pb] + [f"{k}={v}" for k, v in opts.items()]
     txt = subprocess.run(args, capture_output=True, text=True, check=True).stdout
     ref = parse_ref(txt)
     t = ref["tables"]
     out = {
-        "pp_a": ra.to_pp(stacking=st), "pp_b": rb.to_pp(stacking=st), "opts": json.dumps(opts),
+        "pp_a": pp_a, "pp_b": pp_b, "opts": json.dumps(opts),
         "score": ref["score"], "edges": np.array(ref["edges"], dtype=np.int32),
         "struct_a": ref["struct_a"], "struct_b": ref["struct_b"],
         "min_col": np.array(ref["min_col"], dtype=np.int32),
@@ -197,7 +212,7 @@ def make_pf_case(name, spec, workdir):
     ref, Z, am, bm = parse_pf(txt)
     t = ref["tables"]
     out = {
-        "pp_a": ra.to_pp(stacking=st), "pp_b": rb.to_pp(stacking=st), "opts": json.dumps(opts), "Z": Z,
+        "pp_a": ra.to_pp(), "pp_b": rb.to_pp(), "opts": json.dumps(opts), "Z": Z,
         "am": np.array([x[:4] for x in am], dtype=np.int32).reshape(-1, 4),
         "am_p": np.array([x[4] for x in am], dtype=np.float64),
         "bm": np.array([x[:2] for x in bm], dtype=np.int32).reshape(-1, 2),

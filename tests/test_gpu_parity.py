@@ -194,3 +194,23 @@ def test_gpu_kbest_matches_oracle(engine, prep_kw, mode, k, thr):
             assert_same_result(a, b, f"pair {q} hit {h}")
         total += len(ref)
     assert total > len(tables)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", [{}, {"sequ_local": True}, {"struct_local": True},
+                                  {"no_lonely_pairs": True, "free_endgaps": "++++"}])
+def test_gpu_profiles_match_oracle(engine, mode):
+    """Profile (multiple alignment) inputs as in progressive alignment:
+    profiles of 2-4 rows and single sequences, all pairs, prepared by
+    lcg_prepare_pairs (profiles take the host envelope), bit-exact against
+    the oracle."""
+    from locarna_gb300.prep import prepare_pairs
+    from locarna_gb300.synth import make_profile, make_rna
+    recs = [make_profile(90 + 13 * k, 700 + k, 2 + k % 3) for k in range(5)] + [make_rna(100, 790)]
+    pp = [r.to_pp() for r in recs]
+    pairs = [(pp[a], pp[b]) for a in range(len(pp)) for b in range(a + 1, len(pp))]
+    tables, nhost = prepare_pairs(engine, pairs)
+    assert nhost == len(pairs)  # every pair has a profile
+    res = engine.align_pairs(tables, **mode)
+    for k, t in enumerate(tables):
+        assert_same_result(res[k], oracle_align(t, **mode), f"pair {k}")
