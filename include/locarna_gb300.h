@@ -202,8 +202,10 @@ lcg_status lcg_align_pairs(lcg_engine eng, const lcg_pair_tables *pairs,
  * or when the queue is empty (where the reference's behaviour is undefined).
  * Empty alignments are not hits. results[q*k + h] (h < num_hits[q]) is hit h
  * of pair q, its score the task's score; each needs edge and arc-match
- * buffers as in lcg_align_pairs. opts->normalized / penalized must be 0;
- * opts->do_trace is ignored (hits are always traced).
+ * buffers as in lcg_align_pairs. With opts->normalized every interval is
+ * scored by normalized alignment (as suboptimal(.., normalized = true, L));
+ * opts->penalized must be 0; opts->do_trace is ignored (hits are always
+ * traced).
  */
 lcg_status lcg_align_kbest(lcg_engine eng, const lcg_pair_tables *pairs, int32_t npairs,
                            const lcg_align_opts *opts, int32_t k, int64_t threshold,

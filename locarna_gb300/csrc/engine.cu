@@ -1207,8 +1207,7 @@ lcg_status lcg_align_kbest(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
                            int32_t k, int64_t threshold, lcg_align_result *results, int32_t *num_hits) {
     if (!e || !pairs || !opts || !results || !num_hits || npairs < 0) return fail(LCG_ERR_ARG, "NULL argument");
     if (k < 1) return fail(LCG_ERR_ARG, "k must be >= 1");
-    if (opts->normalized || opts->penalized)
-        return fail(LCG_ERR_UNSUPPORTED, "k-best alignment with normalized or penalized scores is not supported");
+    if (opts->penalized) return fail(LCG_ERR_UNSUPPORTED, "k-best alignment with penalized scores is not supported");
     for (int q = 0; q < npairs; ++q) num_hits[q] = 0;
     if (npairs == 0) return LCG_OK;
     CUDA_TRY(cudaSetDevice(e->device));
@@ -1217,16 +1216,19 @@ lcg_status lcg_align_kbest(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
     e->last_h2d = e->last_d2h = 0;
     e->last_groups = e->last_cells = 0;
     e->last_terms = e->last_visits = -1;
-    // the fill and the whole-sequence top levels: one chunk, traced pairs
-    // (PF_TRACE) but no traceback launch
+    const bool norm = opts->normalized != 0;
+    // the fill (and the whole-sequence top levels): one chunk, traced pairs
+    // (PF_TRACE) but no traceback launch; normalized alignment is iterated
+    // below, per interval
     lcg_align_opts o = *opts;
     o.do_trace = 1;
+    o.normalized = 0;
     Chunk c;
     c.q0 = 0;
     c.nq = npairs;
     c.kbest = true;
     c.prep.resize(npairs);
-    lcg_host::parallel_for(npairs, [&](int q) { prep_pair(pairs[q], o, c.prep[q]); });
+    lcg_host::parallel_for(npairs, [&](int q) { prep_pair(pairs[q], *opts, c.prep[q]); });
     for (int q = 0; q < npairs; ++q)
         if (c.prep[q].code != LCG_OK) return fail(c.prep[q].code, "pair " + std::to_string(q) + ": " + c.prep[q].err);
     const Slot sl0 = slot_of(e, 0);
@@ -1239,6 +1241,92 @@ lcg_status lcg_align_kbest(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
     o_score.do_trace = 0;
     rc = chunk_finish(e, sl0, &o_score, c, first.data(), &t_wait, &t_res);
     if (rc != LCG_OK) return rc;
+
+    char *Dv = *sl0.d_arena;
+    char *H = *sl0.h_stage;
+    const PairDev *dpairs = (const PairDev *)(Dv + c.off_pairs);
+    int *dmod = (int *)(Dv + c.off_mod);
+    int *d_lam = dmod, *d_items = dmod + npairs, *d_res1 = dmod + 2 * npairs, *d_res2 = dmod + 7 * npairs;
+    int4 *d_rst = (int4 *)(dmod + 12 * npairs);
+    int *status = (int *)(Dv + c.off_ctrl + 4);
+    cudaStream_t st = sl0.st;
+    std::vector<int> lam(npairs, 0);
+    bool first_trace = true;  // the reference's min_i_/min_j_ start at 1 and then carry over between traces
+    auto trace_flags = [&](int f) {
+        const int r = f | (first_trace ? 0 : TRACE_KEEP_MIN);
+        first_trace = false;
+        return r;
+    };
+    auto trace_launch = [&](const TraceSel &ts) -> lcg_status {
+        if (c.sl) CUDA_TRY(launch_sl_trace(dpairs, npairs, c.scratch, c.stride, c.sw, status, st, ts));
+        else CUDA_TRY(launch_trace(dpairs, npairs, c.scratch, c.stride, c.sw, c.rb, status, st, ts));
+        return LCG_OK;
+    };
+    // The score of each listed pair's interval rr[q] (Aligner::align() or,
+    // normalized, Aligner::normalized_align(), aligner.cc:1527-1588, with its
+    // Dinkelbach iterations: top level with penalty lam, top-level walk for
+    // the end cells, lam <- (score + length lam) / (length + L) until it
+    // repeats). Afterwards the device holds each listed pair's last top level
+    // and, normalized, its final lam in d_lam.
+    auto evaluate = [&](const std::vector<int> &its, const std::vector<int4> &rr, int *d_res,
+                        std::vector<long long> &score) -> lcg_status {
+        if (its.empty()) return LCG_OK;
+        std::vector<int> g(5 * its.size());
+        CUDA_TRY(cudaMemcpyAsync(d_rst, rr.data(), sizeof(int4) * npairs, cudaMemcpyHostToDevice, st));
+        if (!norm) {
+            const int ni = (int)its.size();
+            CUDA_TRY(cudaMemcpyAsync(d_items, its.data(), 4ull * ni, cudaMemcpyHostToDevice, st));
+            CUDA_TRY(launch_top(dpairs, d_items, ni, nullptr, d_rst, c.rb, status, st));
+            CUDA_TRY(launch_gather_res(dpairs, d_items, ni, d_res, st));
+            CUDA_TRY(cudaMemcpyAsync(g.data(), d_res, 20ull * ni, cudaMemcpyDeviceToHost, st));
+            CUDA_TRY(cudaStreamSynchronize(st));
+            e->last_launches += 2;
+            for (int t = 0; t < ni; ++t) score[its[t]] = g[5 * t] < MIN_FINITE ? LCG_NEG_INF : g[5 * t];
+            return LCG_OK;
+        }
+        const long long L = opts->normalized_L;
+        std::vector<long long> lambda(npairs, -1), nl(npairs, 0);
+        std::vector<int> act = its;
+        for (int iter = 0; !act.empty(); ++iter) {
+            if (iter > 100000) return fail(LCG_ERR_DEVICE, "normalized alignment: Dinkelbach iterations do not converge");
+            for (int q : act) {
+                lambda[q] = nl[q];
+                if (std::llabs(lambda[q]) * (c.prep[q].n + c.prep[q].m) >= (1ll << 26))
+                    return fail(LCG_ERR_RANGE, "normalized alignment: score ratio times length exceeds the device range");
+                lam[q] = (int)lambda[q];
+            }
+            const int ni = (int)act.size();
+            CUDA_TRY(cudaMemcpyAsync(d_lam, lam.data(), 4ull * npairs, cudaMemcpyHostToDevice, st));
+            CUDA_TRY(cudaMemcpyAsync(d_items, act.data(), 4ull * ni, cudaMemcpyHostToDevice, st));
+            CUDA_TRY(launch_top(dpairs, d_items, ni, d_lam, d_rst, c.rb, status, st));
+            TraceSel ts;
+            ts.items = d_items;
+            ts.nitems = ni;
+            ts.lam = d_lam;
+            ts.rst = d_rst;
+            ts.flags = trace_flags(TRACE_TOP_ONLY);
+            lcg_status tr = trace_launch(ts);
+            if (tr != LCG_OK) return tr;
+            CUDA_TRY(launch_gather_res(dpairs, d_items, ni, d_res, st));
+            CUDA_TRY(cudaMemcpyAsync(g.data(), d_res, 20ull * ni, cudaMemcpyDeviceToHost, st));
+            CUDA_TRY(cudaStreamSynchronize(st));
+            e->last_launches += 3;
+            std::vector<int> still;
+            for (int t = 0; t < ni; ++t) {
+                const int q = act[t];
+                const int *r = &g[5 * t];
+                if (r[R_SCORE] < MIN_FINITE) return fail(LCG_ERR_DEVICE, "normalized alignment: -inf top level");
+                const long long length = (long long)(r[R_MAXI] - r[R_MINI] + 1) + (r[R_MAXJ] - r[R_MINJ] + 1);
+                if (length + L <= 0)
+                    return fail(LCG_ERR_ARG, "normalized alignment: empty alignment with L = 0 (division by zero)");
+                nl[q] = ((long long)r[R_SCORE] + length * lambda[q]) / (length + L);
+                if (nl[q] != lambda[q]) still.push_back(q);
+            }
+            act.swap(still);
+        }
+        for (int q : its) score[q] = lambda[q];
+        return LCG_OK;
+    };
 
     // Aligner::suboptimal (aligner.cc:1384-1512) per pair: a task queue of
     // (interval, score) with the reference's comparator (greater_second,
@@ -1255,23 +1343,24 @@ lcg_status lcg_align_kbest(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
     std::vector<int> count(npairs, 1);  // i of the reference's loop
     std::vector<bool> done(npairs, false);
     std::vector<Task> cur(npairs);
-    for (int q = 0; q < npairs; ++q) tasks[q].push(Task{make_int4(1, 1, c.prep[q].n, c.prep[q].m), first[q].score});
-    char *Dv = *sl0.d_arena;
-    char *H = *sl0.h_stage;
-    const PairDev *dpairs = (const PairDev *)(Dv + c.off_pairs);
-    int *dmod = (int *)(Dv + c.off_mod);
-    int *d_items = dmod + npairs, *d_res1 = dmod + 2 * npairs, *d_res2 = dmod + 7 * npairs;
-    int4 *d_rst = (int4 *)(dmod + 12 * npairs);
-    int *status = (int *)(Dv + c.off_ctrl + 4);
-    cudaStream_t st = sl0.st;
-    std::vector<int> items, split_items;
+    std::vector<int> items, split_items, all(npairs);
     std::vector<int4> rst(npairs), r1(npairs), r2(npairs);
-    std::vector<int> g1(5ull * npairs), g2(5ull * npairs);
+    std::vector<long long> s0(npairs, LCG_NEG_INF), s1(npairs, LCG_NEG_INF), s2(npairs, LCG_NEG_INF);
+    for (int q = 0; q < npairs; ++q) {
+        all[q] = q;
+        rst[q] = make_int4(1, 1, c.prep[q].n, c.prep[q].m);
+        s0[q] = first[q].score;
+    }
+    const auto t0 = std::chrono::steady_clock::now();
+    if (norm) {
+        rc = evaluate(all, rst, d_res1, s0);
+        if (rc != LCG_OK) return rc;
+    }
+    for (int q = 0; q < npairs; ++q) tasks[q].push(Task{rst[q], s0[q]});
     // an interval the top level can align (the reference leaves others undefined)
     auto valid_r = [&](int q, int4 r) {
         return r.x >= 1 && r.y >= 1 && r.z <= c.prep[q].n && r.w <= c.prep[q].m && r.z >= r.x - 1 && r.w >= r.y - 1;
     };
-    const auto t0 = std::chrono::steady_clock::now();
     for (int round = 0;; ++round) {
         items.clear();
         for (int q = 0; q < npairs; ++q) {
@@ -1293,16 +1382,25 @@ lcg_status lcg_align_kbest(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
         }
         if (items.empty()) break;
         const int ni = (int)items.size();
-        CUDA_TRY(cudaMemcpyAsync(d_rst, rst.data(), sizeof(int4) * npairs, cudaMemcpyHostToDevice, st));
-        CUDA_TRY(cudaMemcpyAsync(d_items, items.data(), 4ull * ni, cudaMemcpyHostToDevice, st));
-        CUDA_TRY(launch_top(dpairs, d_items, ni, nullptr, d_rst, c.rb, status, st));
+        // the task's alignment: its top level (normalized: its Dinkelbach
+        // iterations) and the traceback
         TraceSel ts;
+        if (norm) {
+            rc = evaluate(items, rst, d_res1, s0);
+            if (rc != LCG_OK) return rc;
+            ts.lam = d_lam;
+        } else {
+            CUDA_TRY(cudaMemcpyAsync(d_rst, rst.data(), sizeof(int4) * npairs, cudaMemcpyHostToDevice, st));
+            CUDA_TRY(cudaMemcpyAsync(d_items, items.data(), 4ull * ni, cudaMemcpyHostToDevice, st));
+            CUDA_TRY(launch_top(dpairs, d_items, ni, nullptr, d_rst, c.rb, status, st));
+        }
+        CUDA_TRY(cudaMemcpyAsync(d_items, items.data(), 4ull * ni, cudaMemcpyHostToDevice, st));
         ts.items = d_items;
         ts.nitems = ni;
         ts.rst = d_rst;
-        ts.flags = round ? TRACE_KEEP_MIN : 0;  // the reference's min_i_/min_j_ carry over between traces
-        if (c.sl) CUDA_TRY(launch_sl_trace(dpairs, npairs, c.scratch, c.stride, c.sw, status, st, ts));
-        else CUDA_TRY(launch_trace(dpairs, npairs, c.scratch, c.stride, c.sw, c.rb, status, st, ts));
+        ts.flags = trace_flags(0);
+        rc = trace_launch(ts);
+        if (rc != LCG_OK) return rc;
         CUDA_TRY(cudaMemcpyAsync(H + c.down_begin, Dv + c.down_begin, c.down_end - c.down_begin,
                                  cudaMemcpyDeviceToHost, st));
         CUDA_TRY(cudaMemcpyAsync(H + c.off_ctrl, Dv + c.off_ctrl, 64, cudaMemcpyDeviceToHost, st));
@@ -1353,28 +1451,17 @@ lcg_status lcg_align_kbest(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
             split_items.push_back(q);
         }
         if (split_items.empty()) continue;
-        // the scores of both halves (two restricted top levels)
+        // the scores of both halves, r1 first (the reference's order)
         std::vector<int> run1, run2;
         for (int q : split_items) {
+            s1[q] = s2[q] = LCG_NEG_INF;
             if (valid_r(q, r1[q])) run1.push_back(q);
             if (valid_r(q, r2[q])) run2.push_back(q);
         }
-        const int n1 = (int)run1.size(), n2 = (int)run2.size();
-        CUDA_TRY(cudaMemcpyAsync(d_rst, r1.data(), sizeof(int4) * npairs, cudaMemcpyHostToDevice, st));
-        CUDA_TRY(cudaMemcpyAsync(d_items, run1.data(), 4ull * n1, cudaMemcpyHostToDevice, st));
-        CUDA_TRY(launch_top(dpairs, d_items, n1, nullptr, d_rst, c.rb, status, st));
-        CUDA_TRY(launch_gather_res(dpairs, d_items, n1, d_res1, st));
-        CUDA_TRY(cudaMemcpyAsync(d_rst, r2.data(), sizeof(int4) * npairs, cudaMemcpyHostToDevice, st));
-        CUDA_TRY(cudaMemcpyAsync(d_items, run2.data(), 4ull * n2, cudaMemcpyHostToDevice, st));
-        CUDA_TRY(launch_top(dpairs, d_items, n2, nullptr, d_rst, c.rb, status, st));
-        CUDA_TRY(launch_gather_res(dpairs, d_items, n2, d_res2, st));
-        CUDA_TRY(cudaMemcpyAsync(g1.data(), d_res1, 20ull * n1, cudaMemcpyDeviceToHost, st));
-        CUDA_TRY(cudaMemcpyAsync(g2.data(), d_res2, 20ull * n2, cudaMemcpyDeviceToHost, st));
-        CUDA_TRY(cudaStreamSynchronize(st));
-        e->last_launches += 4;
-        std::vector<long long> s1(npairs, LCG_NEG_INF), s2(npairs, LCG_NEG_INF);
-        for (int t = 0; t < n1; ++t) s1[run1[t]] = g1[5 * t] < MIN_FINITE ? LCG_NEG_INF : g1[5 * t];
-        for (int t = 0; t < n2; ++t) s2[run2[t]] = g2[5 * t] < MIN_FINITE ? LCG_NEG_INF : g2[5 * t];
+        rc = evaluate(run1, r1, d_res1, s1);
+        if (rc != LCG_OK) return rc;
+        rc = evaluate(run2, r2, d_res2, s2);
+        if (rc != LCG_OK) return rc;
         for (int q : split_items) {
             tasks[q].push(Task{r1[q], s1[q]});
             tasks[q].push(Task{r2[q], s2[q]});

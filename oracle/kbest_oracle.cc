@@ -2,8 +2,9 @@
 // bench.py's CPU-baseline leg may load this file's library, and only as the
 // checker, never as the product path.
 //
-// Restatement of Aligner::suboptimal (src/LocARNA/aligner.cc:1384-1512,
-// non-normalized): k best alignments by interval splitting. The tasks are
+// Restatement of Aligner::suboptimal (src/LocARNA/aligner.cc:1384-1512): k
+// best alignments by interval splitting, scored by align() or, normalized,
+// by normalized_align(). The tasks are
 // kept in a std::priority_queue ordered by score with the reference's
 // comparator (greater_second, aligner.hh:32-44), so that equal scores leave
 // the queue in the same order as in the reference.
@@ -18,6 +19,7 @@ long long lcg_oracle_ctx_top(void *ctx, int sA, int sB, int eA, int eB);
 void lcg_oracle_ctx_trace(void *ctx, lcg_align_result *r);
 void lcg_oracle_ctx_free(void *ctx);
 int lcg_oracle_ctx_stale(void *ctx);
+int lcg_oracle_ctx_normalized(void *ctx, int sA, int sB, int eA, int eB, lcg_align_result *r, long long *score);
 }
 
 namespace {
@@ -62,9 +64,18 @@ extern "C" int lcg_oracle_kbest(const lcg_pair_tables *t, const lcg_align_opts *
     void *ctx = lcg_oracle_ctx_new(t, o);
     if (!ctx) return -1;
     const int n = t->len_a, m = t->len_b;
+    const bool norm = o->normalized != 0;
+    // the score of an interval: Aligner::align() or normalized_align() (whose
+    // last trace goes to res when given)
+    auto eval = [&](const Restriction &r, lcg_align_result *res) -> long long {
+        if (!norm) return lcg_oracle_ctx_top(ctx, r.sA, r.sB, r.eA, r.eB);
+        long long sc = LCG_NEG_INF;
+        if (lcg_oracle_ctx_normalized(ctx, r.sA, r.sB, r.eA, r.eB, res, &sc) != 0) return LCG_NEG_INF;
+        return sc;
+    };
     std::priority_queue<task_t, std::vector<task_t>, score_less> tasks;
     Restriction full{1, 1, n, m};
-    tasks.push(task_t(full, lcg_oracle_ctx_top(ctx, 1, 1, n, m)));
+    tasks.push(task_t(full, eval(full, nullptr)));
     int hits = 0;
     for (int i = 1; k < 0 || i <= k;) {
         // the reference reads top() of an empty queue here (undefined); the
@@ -75,9 +86,13 @@ extern "C" int lcg_oracle_kbest(const lcg_pair_tables *t, const lcg_align_opts *
         const Restriction r = task.first;
         // InftyInt comparison: -inf is below every threshold
         if (task.second == LCG_NEG_INF || task.second < threshold + 1) break;
-        lcg_oracle_ctx_top(ctx, r.sA, r.sB, r.eA, r.eB);
         lcg_align_result &res = results[hits];
-        lcg_oracle_ctx_trace(ctx, &res);
+        if (norm) {
+            eval(r, &res);
+        } else {
+            lcg_oracle_ctx_top(ctx, r.sA, r.sB, r.eA, r.eB);
+            lcg_oracle_ctx_trace(ctx, &res);
+        }
         if (res.num_edges == 0) continue;  // empty alignment: no hit, i unchanged
         res.score = task.second;
         ++hits;
@@ -95,8 +110,8 @@ extern "C" int lcg_oracle_kbest(const lcg_pair_tables *t, const lcg_align_opts *
             r1.eB = split;
             r2.sB = split;
         }
-        const long long s1 = lcg_oracle_ctx_top(ctx, r1.sA, r1.sB, r1.eA, r1.eB);
-        const long long s2 = lcg_oracle_ctx_top(ctx, r2.sA, r2.sB, r2.eA, r2.eB);
+        const long long s1 = eval(r1, nullptr);
+        const long long s2 = eval(r2, nullptr);
         tasks.push(task_t(r1, s1));
         tasks.push(task_t(r2, s2));
         ++i;

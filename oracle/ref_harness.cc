@@ -219,14 +219,16 @@ int main(int argc, char **argv) {
         // (1) the reference's own enumeration (Aligner::suboptimal), which
         // prints "HIT score startA startA endB endB" per hit
         std::fflush(stdout);
-        make_aligner()->suboptimal(o.kbest, o.better, false, 0, 120, false, false, true, false);
+        make_aligner()->suboptimal(o.kbest, o.better, o.normalized >= 0, std::max(o.normalized, 0), 120, false,
+                                   false, true, false);
         std::cout.flush();
         // (2) the same enumeration through the public Aligner API
         // (aligner.cc:1384-1512), printing each hit's full alignment
         auto a = make_aligner();
         typedef std::pair<AlignerRestriction, infty_score_t> task_t;
         std::priority_queue<task_t, std::vector<task_t>, greater_second<task_t>> tasks;
-        infty_score_t s0 = a->align();
+        const bool norm = o.normalized >= 0;
+        infty_score_t s0 = norm ? a->normalized_align(o.normalized, false) : a->align();
         tasks.push(task_t(a->get_restriction(), s0));
         for (size_t i = 1; i <= (size_t)o.kbest && !tasks.empty();) {
             task_t task = tasks.top();
@@ -234,8 +236,12 @@ int main(int argc, char **argv) {
             AlignerRestriction r = task.first;
             if (task.second < (infty_score_t)o.better + 1) break;
             a->set_restriction(r);
-            a->align();
-            a->trace();
+            if (norm) {
+                a->normalized_align(o.normalized, false);
+            } else {
+                a->align();
+                a->trace();
+            }
             Alignment alignment = a->get_alignment();
             if (alignment.empty()) continue;
             std::printf("khit %ld", score_val(task.second));
@@ -265,9 +271,9 @@ int main(int argc, char **argv) {
                 r2.set_startB(split);
             }
             a->set_restriction(r1);
-            infty_score_t s1 = a->align();
+            infty_score_t s1 = norm ? a->normalized_align(o.normalized, false) : a->align();
             a->set_restriction(r2);
-            infty_score_t s2 = a->align();
+            infty_score_t s2 = norm ? a->normalized_align(o.normalized, false) : a->align();
             tasks.push(task_t(r1, s1));
             tasks.push(task_t(r2, s2));
             ++i;

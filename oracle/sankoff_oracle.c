@@ -687,6 +687,32 @@ static void trace_in_arcmatch(Ctx *c, int state, int al, int i, int bl, int j, i
     }
 }
 
+/* AlignerImpl::normalized_align, aligner.cc:1527-1588: Dinkelbach iterations
+ * of the top level (under the current restriction); each traces, and
+ * min_i/min_j carry over when a trace does not reach a zero cell, as the
+ * reference's members do. The score is the final ratio; the edges of the last
+ * trace stay in the context's buffers. Returns -2 on a zero denominator. */
+static int normalized_align(Ctx *c, sc_t *score) {
+    sc_t lambda = -1, new_lambda = 0;
+    c->lam_on = 1;
+    while (lambda != new_lambda) {
+        lambda = new_lambda;
+        c->lam = lambda;
+        c->mod = 1;
+        sc_t s = top_locally(c);
+        c->nedges = 0; c->ntam = 0;
+        trace_in_arcmatch(c, E_NO_NO, c->rsA - 1, c->max_i, c->rsB - 1, c->max_j, 1);
+        sc_t length = (sc_t)(c->max_i - c->min_i + 1) + (c->max_j - c->min_j + 1);
+        s += length * lambda;
+        if (length + c->o->normalized_L <= 0) return -2;
+        new_lambda = s / (length + c->o->normalized_L);
+    }
+    c->lam_on = 0;
+    c->mod = 0;
+    *score = new_lambda;
+    return 0;
+}
+
 /* ---------------------------------------------------------------- entry */
 
 static void ctx_free(Ctx *c) {
@@ -730,24 +756,7 @@ int lcg_oracle_align(const lcg_pair_tables *t, const lcg_align_opts *o,
     sc_t score;
     int traced = 0;
     if (o->normalized) {
-        /* AlignerImpl::normalized_align, aligner.cc:1527-1588: Dinkelbach
-         * iterations; each traces (min_i/min_j carry over when a trace does
-         * not reach a zero cell, as the reference's members do) */
-        sc_t lambda = -1, new_lambda = 0;
-        c.lam_on = 1;
-        while (lambda != new_lambda) {
-            lambda = new_lambda;
-            c.lam = lambda;
-            c.mod = 1;
-            sc_t s = top_locally(&c);
-            c.nedges = 0; c.ntam = 0;
-            trace_in_arcmatch(&c, E_NO_NO, c.rsA - 1, c.max_i, c.rsB - 1, c.max_j, 1);
-            sc_t length = (sc_t)(c.max_i - c.min_i + 1) + (c.max_j - c.min_j + 1);
-            s += length * lambda;
-            if (length + o->normalized_L <= 0) { ctx_free(&c); return -2; }
-            new_lambda = s / (length + o->normalized_L);
-        }
-        score = new_lambda;
+        if (normalized_align(&c, &score) != 0) { ctx_free(&c); return -2; }
         traced = 1;
     } else if (o->penalized) {
         /* AlignerImpl::penalized_align, aligner.cc:1597-1617 */
@@ -803,6 +812,24 @@ long long lcg_oracle_ctx_top(void *ctx, int sA, int sB, int eA, int eB) {
     c->rsA = sA; c->rsB = sB; c->reA = eA; c->reB = eB;
     sc_t s = c->o->sequ_local ? top_locally(c) : top_free_endgaps(c);
     return s < MIN_FINITY ? LCG_NEG_INF : s;
+}
+
+/* Aligner::set_restriction + normalized_align(L): the ratio of the interval;
+ * its last trace goes to r as in lcg_oracle_ctx_trace. -2 on a zero
+ * denominator. */
+int lcg_oracle_ctx_normalized(void *ctx, int sA, int sB, int eA, int eB, lcg_align_result *r, long long *score) {
+    Ctx *c = ctx;
+    c->rsA = sA; c->rsB = sB; c->reA = eA; c->reB = eB;
+    c->edges = r ? r->edges : NULL; c->edge_cap = (r && r->edges) ? c->n + c->m : 0;
+    c->tam = r ? r->traced_am : NULL; c->tam_cap = (r && r->traced_am) ? (c->n < c->m ? c->n : c->m) : 0;
+    sc_t s;
+    if (normalized_align(c, &s) != 0) return -2;
+    *score = s;
+    if (r) {
+        r->num_edges = c->nedges; r->num_traced_am = c->ntam;
+        r->max_i = c->max_i; r->max_j = c->max_j; r->min_i = c->min_i; r->min_j = c->min_j;
+    }
+    return 0;
 }
 
 /* Aligner::trace() of the last top level: edges, traced arc matches and end

@@ -86,6 +86,9 @@ CASES = {
     "h180_kbest_nolp_better": (180, 85, "h", 86, {"sequ_local": "1", "kbest": "10", "no_lonely_pairs": "1",
                                                   "better": "3000"}, True),
     "c150_kbest_global": (150, 11, 140, 12, {"kbest": "4", "free_endgaps": "++++"}, True),
+    "h200_kbest_normalized": (200, 83, "h", 84, {"sequ_local": "1", "kbest": "5", "normalized": "100"}, True),
+    "c150_kbest_normalized_nolp": (150, 1, 150, 2, {"sequ_local": "1", "kbest": "4", "normalized": "50",
+                                                    "no_lonely_pairs": "1"}, True),
     # profile (multiple alignment) inputs, as in mlocarna's progressive stage
     "p120_global": (("p", 120, 3), 5, ("p", 110, 2), 6, {}, True),
     "p150_vs_seq": (("p", 150, 4), 91, 140, 92, {}, True),
@@ -178,6 +181,8 @@ PF_CASES = {
     "pf150": (150, 1, 150, 2, {}),
     "pf200": (200, 5, 200, 6, {}),
     "pf90_b": (90, 51, 110, 52, {}),
+    # profile inputs (alignment rows)
+    "pf_p100": (("p", 100, 3), 61, ("p", 90, 2), 62, {}),
 }
 
 
@@ -201,7 +206,8 @@ def parse_pf(txt):
 
 def make_pf_case(name, spec, workdir):
     la, sa, lb, sb, opts = spec
-    ra, rb = make_rna(la, sa), make_rna(lb, sb)
+    ra = make_profile(la[1], sa, la[2]) if isinstance(la, tuple) else make_rna(la, sa)
+    rb = make_profile(lb[1], sb, lb[2]) if isinstance(lb, tuple) else make_rna(lb, sb)
     pa, pb = os.path.join(workdir, name + "_A.pp"), os.path.join(workdir, name + "_B.pp")
     with open(pa, "w") as f:
         f.write(ra.to_pp())
@@ -231,8 +237,8 @@ def make_pf_case(name, spec, workdir):
 def main_pf():
     work = os.path.join(ROOT, "_work", "golden_pp")
     os.makedirs(work, exist_ok=True)
-    for name, spec in PF_CASES.items():
-        print(name, *make_pf_case(name, spec, work))
+    for name in sys.argv[1:] or list(PF_CASES):
+        print(name, *make_pf_case(name, PF_CASES[name], work))
 
 
 if __name__ == "__main__" and os.environ.get("LCG_GOLDEN_PF"):

@@ -214,3 +214,18 @@ def test_gpu_profiles_match_oracle(engine, mode):
     res = engine.align_pairs(tables, **mode)
     for k, t in enumerate(tables):
         assert_same_result(res[k], oracle_align(t, **mode), f"pair {k}")
+
+
+@pytest.mark.gpu
+def test_gpu_kbest_normalized_matches_oracle(engine):
+    """--kbest with --normalized: every interval scored by its Dinkelbach
+    iterations; hits against the oracle, pair by pair."""
+    from oracle_ffi import oracle_kbest
+    tables = _homolog_tables({}, count=2, length=100, seed=601)
+    mode = {"sequ_local": True, "normalized": 80}
+    got = engine.align_kbest(tables, 4, -1000000, **mode)
+    for q, t in enumerate(tables):
+        ref = oracle_kbest(t, 4, -1000000, **mode)
+        assert len(got[q]) == len(ref), (q, len(got[q]), len(ref))
+        for h, (a, b) in enumerate(zip(got[q], ref)):
+            assert_same_result(a, b, f"pair {q} hit {h}")
