@@ -452,6 +452,17 @@ def run_ours(args):
         eng.run_call(pcall)
         single_ms.append(eng.last_stats()[0])
     single_ms.sort()
+    # the same pair in structure-local mode
+    scall = eng.prepare_call([pt], struct_local=True)
+    for _ in range(2):
+        eng.run_call(scall)
+    sl_ms = []
+    for _ in range(3):
+        flush_l2()
+        eng.run_call(scall)
+        sl_ms.append(eng.last_stats()[0])
+    sl_ms.sort()
+    assert_same_result(Engine.decode_call(scall)[0], oracle_align(pt, struct_local=True), "400x400 struct-local")
     sample = list(range(0, npairs, 16))
     per_calls = [eng.prepare_call([tables[k]]) for k in sample]
     for c in per_calls[:4]:
@@ -531,6 +542,7 @@ def run_ours(args):
                     "arc_terms": work["arc_terms"], "groups": work["groups"]},
         "per_pair": {"workload": "one 400x400 nt pair, global", "device_ms": single_ms[len(single_ms) // 2],
                      "aligns_per_s": 1e3 / single_ms[len(single_ms) // 2],
+                     "struct_local_device_ms": sl_ms[len(sl_ms) // 2],
                      "per_pair_launch_aligns_per_s_device": len(sample) / (dev_ms_single / 1e3),
                      "per_pair_launch_aligns_per_s_wall": len(sample) / wall_single,
                      "batched_over_per_pair_launch": value / (len(sample) / (dev_ms_single / 1e3))},

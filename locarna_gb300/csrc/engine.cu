@@ -856,7 +856,8 @@ lcg_status chunk_launch(lcg_engine e, const Slot &s, const lcg_pair_tables *all,
     const bool sl = opts->struct_local != 0;
     const int rb = lcg_host::ring_size(span);
     bool fast = true;
-    for (auto &p : prep) fast = fast && (p.flags & PF_SCLS) && !(p.flags & PF_ANCHORS);
+    for (auto &p : prep)
+        fast = fast && (p.flags & PF_SCLS) && !(p.flags & (PF_ANCHORS | PF_NOLP | PF_STACK));
     int blocks_per_sm = 0;
     if (sl) {
         CUDA_TRY(sl_prepare(sw, rb, &blocks_per_sm));

@@ -138,7 +138,7 @@ extern "C" lcg_status lcg_align_score_static(const lcg_pair_tables *pair, const 
     const long long stride = (long long)rows_max * sw;  // ints per warp slot
     int blocks_per_sm = 0;
     const int rb = lcg_host::ring_size(p.span);
-    const bool fast = (p.flags & PF_SCLS) && !(p.flags & PF_ANCHORS);
+    const bool fast = (p.flags & PF_SCLS) && !(p.flags & (PF_ANCHORS | PF_NOLP | PF_STACK));
     STATIC_TRY(fill_occupancy(rb, false, fast, &blocks_per_sm));
     int sms = 0;
     STATIC_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));

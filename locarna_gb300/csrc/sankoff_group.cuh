@@ -89,7 +89,8 @@ __device__ __noinline__ int inner_term(const PairDev &P, const int4 *e, int *sta
 // penalized alignment (ModifiedScoringView, aligner_impl.hh:190-275) with
 // every position penalised by lam: sigma - 2 lam, gap costs - lam, arc-match
 // terms D(a,b) - lam (|a| + |b|) (the host bounds lam (n+m) below 2^27).
-template <int NCH, bool ANCH, bool SCLS, bool TOP, bool WAIT, bool DWRITE, bool COUNT, bool MOD = false>
+template <int NCH, bool ANCH, bool SCLS, bool TOP, bool WAIT, bool DWRITE, bool COUNT, bool MOD = false,
+          bool INNER = true>
 __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, int *__restrict__ Mg,
                             int pitch, int sbase, int ringn,
                             const int4 *__restrict__ dw, int ndw, bool globalA, bool globalB,
@@ -371,7 +372,8 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
                 const bool mine = q < ndw && e.y == i;
                 if (mine) {
                     int v = CUR(e.z) + e.w;
-                    if (P.flags & (PF_NOLP | PF_STACK)) v = max(v, inner_term<WAIT>(P, dw + q, status, abort_flag));
+                    if (INNER && (P.flags & (PF_NOLP | PF_STACK)))
+                        v = max(v, inner_term<WAIT>(P, dw + q, status, abort_flag));
                     st_volatile(Dp + e.x, norm(v));
                 }
                 const int cnt = __popc(__ballot_sync(0xffffffffu, mine));
@@ -429,7 +431,9 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
 // class table; ringn (a multiple of 32) exceeds the column span of any two
 // consecutive band rows. Gap costs stay below 2^27 (host check), so the
 // packed value does not overflow.
-// FAST: every pair of the launch has a sigma class table and no anchors.
+// FAST: every pair of the launch has a sigma class table, no anchors, no
+// lonely-pair or stacking terms (INNER = false: the D writes are the plain
+// fill_D_entries, so this hot instantiation carries no inner-term code).
 template <bool TOP, bool WAIT, bool DWRITE, bool COUNT = false, bool FAST = false, bool MOD = false>
 __device__ __forceinline__ void run_group(const PairDev &P, int cpl, int al, int ar, int bl, int br,
                                           int *__restrict__ Mg, int pitch, int sbase, int ringn,
@@ -438,9 +442,9 @@ __device__ __forceinline__ void run_group(const PairDev &P, int cpl, int al, int
                                           volatile int *abort_flag, TopOut *tout,
                                           unsigned long long *counters = nullptr, int lam = 0) {
     if (FAST)
-        run_group_c<4, false, true, TOP, WAIT, DWRITE, COUNT, MOD>(P, al, ar, bl, br, Mg, pitch, sbase, ringn, dw, ndw,
-                                                              globalA, globalB, local_top, status, abort_flag,
-                                                              tout, counters, lam);
+        run_group_c<4, false, true, TOP, WAIT, DWRITE, COUNT, MOD, false>(P, al, ar, bl, br, Mg, pitch, sbase, ringn,
+                                                                          dw, ndw, globalA, globalB, local_top, status,
+                                                                          abort_flag, tout, counters, lam);
     else if (P.flags & PF_ANCHORS)
         run_group_c<4, true, false, TOP, WAIT, DWRITE, COUNT, MOD>(P, al, ar, bl, br, Mg, pitch, sbase, ringn, dw, ndw,
                                                               globalA, globalB, local_top, status, abort_flag,
