@@ -445,6 +445,10 @@ __device__ __forceinline__ void run_group(const PairDev &P, int cpl, int al, int
         run_group_c<4, false, true, TOP, WAIT, DWRITE, COUNT, MOD, false>(P, al, ar, bl, br, Mg, pitch, sbase, ringn,
                                                                           dw, ndw, globalA, globalB, local_top, status,
                                                                           abort_flag, tout, counters, lam);
+    else if ((P.flags & PF_ANCHORS) && (P.flags & PF_SCLS))
+        run_group_c<4, true, true, TOP, WAIT, DWRITE, COUNT, MOD>(P, al, ar, bl, br, Mg, pitch, sbase, ringn, dw, ndw,
+                                                             globalA, globalB, local_top, status, abort_flag,
+                                                             tout, counters, lam);
     else if (P.flags & PF_ANCHORS)
         run_group_c<4, true, false, TOP, WAIT, DWRITE, COUNT, MOD>(P, al, ar, bl, br, Mg, pitch, sbase, ringn, dw, ndw,
                                                               globalA, globalB, local_top, status, abort_flag,

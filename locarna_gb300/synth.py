@@ -59,10 +59,15 @@ class RnaRecord:
                 out[(i, j)] = round(min(self.pairs[(i, j)], pin) * (0.2 + 0.8 * rng.random()), 6)
         return out
 
-    def to_pp(self, stacking=False):
+    def to_pp(self, stacking=False, anchors=None):
         """PP 2.0 text; with ``stacking`` the base-pair section carries the
-        #STACK keyword and p2 columns (stack_probs)."""
-        lines = ["#PP 2.0", "", f"{self.name} {self.seq}", "", "#END", "", "#SECTION BASEPAIRS", ""]
+        #STACK keyword and p2 columns (stack_probs); ``anchors`` (a string of
+        the sequence's length, '.' for no anchor) becomes an #A1 line."""
+        lines = ["#PP 2.0", "", f"{self.name} {self.seq}"]
+        if anchors is not None:
+            assert len(anchors) == len(self.seq)
+            lines.append(f"#A1 {anchors}")
+        lines += ["", "#END", "", "#SECTION BASEPAIRS", ""]
         st = self.stack_probs() if stacking else {}
         if stacking:
             lines.append("#STACK")

@@ -202,7 +202,34 @@ int main(int argc, char **argv) {
                 if (anchors.allowed_match(i, j)) { if (lo < 0) lo = j; hi = j; }
             std::printf(" %ld:%ld", lo, hi);
         }
-        std::printf("\n");
+        // the deletion and insertion ranges (AnchorConstraints::allowed_del /
+        // allowed_ins, anchor_constraints.hh:160-253), checked to be intervals
+        bool intervals = true;
+        std::printf("\nanchor_del");
+        for (size_t i = 1; i <= lenA; ++i) {
+            long lo = -1, hi = -2;
+            for (size_t j = 0; j <= lenB; ++j)
+                if (anchors.allowed_del(i, j)) {
+                    if (lo < 0) lo = j;
+                    else if (hi != (long)j - 1) intervals = false;
+                    hi = j;
+                }
+            std::printf(" %ld:%ld", lo, hi);
+        }
+        std::printf("\nanchor_ins");
+        for (size_t j = 1; j <= lenB; ++j) {
+            long lo = -1, hi = -2;
+            for (size_t i = 0; i <= lenA; ++i)
+                if (anchors.allowed_ins(i, j)) {
+                    if (lo < 0) lo = i;
+                    else if (hi != (long)i - 1) intervals = false;
+                    hi = i;
+                }
+            std::printf(" %ld:%ld", lo, hi);
+        }
+        auto ra = anchors.rightmost_anchor(), la = anchors.leftmost_anchor();
+        std::printf("\nanchor_ends %zu %zu %zu %zu %d %d\n", ra.first, ra.second, la.first, la.second,
+                    (int)anchors.empty(), (int)intervals);
     }
 
     auto make_aligner = [&]() {

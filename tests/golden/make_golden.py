@@ -98,6 +98,14 @@ CASES = {
                        True),
     "p130_noenv": (("p", 130, 5), 99, ("p", 120, 3), 100, {"min_trace_prob": "0"}, True),
     "p250_global": (("p", 250, 3), 101, ("p", 240, 3), 102, {}, True),
+    # anchor constraints (#A1 lines; "anchors" = matched positions A:B, named
+    # A, B, C, ... in order; the reference's strict anchors)
+    "a150_anchors": (150, 81, "h", 82, {"anchors": "20:20,75:75,130:130"}, True),
+    "a150_anchors_seqlocal": (150, 81, "h", 82, {"anchors": "40:40,90:90", "sequ_local": "1"}, True),
+    "a150_anchors_structlocal": (150, 81, "h", 82, {"anchors": "20:20,75:75", "struct_local": "1"}, True),
+    "a150_anchors_free": (150, 81, "h", 82, {"anchors": "30:30,110:110", "free_endgaps": "++++"}, True),
+    "a150_anchors_nolp": (150, 81, "h", 82, {"anchors": "60:60", "no_lonely_pairs": "1"}, True),
+    "a120_anchors_unrel": (120, 21, 130, 22, {"anchors": "10:15,60:70,100:120"}, True),
 }
 
 STACK_KEYS = ("stacking", "new_stacking")
@@ -111,14 +119,21 @@ def make_case(name, spec, workdir):
     else:
         rb = make_profile(lb[1], sb, lb[2]) if isinstance(lb, tuple) else make_rna(lb, sb)
     st = any(k in opts for k in STACK_KEYS)  # inputs with joint (stacking) probabilities
+    anc_a = anc_b = None
+    if "anchors" in opts:
+        anc_a, anc_b = ["."] * len(ra.seq), ["."] * len(rb.seq)
+        for k, ab in enumerate(opts["anchors"].split(",")):
+            x, y = (int(v) for v in ab.split(":"))
+            anc_a[x - 1] = anc_b[y - 1] = chr(ord("A") + k)
+        anc_a, anc_b = "".join(anc_a), "".join(anc_b)
     pa, pb = os.path.join(workdir, name + "_A.pp"), os.path.join(workdir, name + "_B.pp")
-    pp_a = ra.to_pp(stacking=st) if st else ra.to_pp()
-    pp_b = rb.to_pp(stacking=st) if st else rb.to_pp()
+    pp_a = ra.to_pp(stacking=st) if st else (ra.to_pp(anchors=anc_a) if anc_a else ra.to_pp())
+    pp_b = rb.to_pp(stacking=st) if st else (rb.to_pp(anchors=anc_b) if anc_b else rb.to_pp())
     with open(pa, "w") as f:
         f.write(pp_a)
     with open(pb, "w") as f:
         f.write(pp_b)
-    args = [HARNESS, pa, pb] + [f"{k}={v}" for k, v in opts.items()]
+    args = [HARNESS, pa, pb] + [f"{k}={v}" for k, v in opts.items() if k != "anchors"]
     txt = subprocess.run(args, capture_output=True, text=True, check=True).stdout
     ref = parse_ref(txt)
     t = ref["tables"]
@@ -137,6 +152,10 @@ def make_case(name, spec, workdir):
         "am_arcs": t.am_arcs, "am_score": t.am_score,
         "sigma": t.sigma.astype(np.int16) if np.abs(t.sigma).max() < 32000 else t.sigma,
     }
+    if t.anchors is not None:
+        for k_, v_ in t.anchors.items():
+            out["anchor_" + k_] = v_
+        out["anchor_ends"] = np.array(list(t.right_anchor) + list(t.left_anchor), dtype=np.int32)
     if t.am_stack_score is not None:
         out["am_stack_score"] = t.am_stack_score
         out["am_stackable"] = t.am_stackable

@@ -40,7 +40,10 @@ class Golden:
             z["am_arcs"], z["am_score"], self.min_col, self.max_col,
             seq_a=self.seq_a, seq_b=self.seq_b,
             am_stack_score=z["am_stack_score"] if "am_stack_score" in z else None,
-            am_stackable=z["am_stackable"] if "am_stackable" in z else None)
+            am_stackable=z["am_stackable"] if "am_stackable" in z else None,
+            anchors=({k: z["anchor_" + k] for k in PairTables.ANCHOR_FIELDS} if "anchor_match_lo" in z else None),
+            right_anchor=tuple(int(v) for v in z["anchor_ends"][:2]) if "anchor_ends" in z else (0, 0),
+            left_anchor=tuple(int(v) for v in z["anchor_ends"][2:]) if "anchor_ends" in z else None)
 
     @property
     def struct_local(self):
@@ -71,6 +74,11 @@ class Golden:
             pos += ne
             out.append((int(sc), e, tuple(st.split(" "))))
         return out
+
+    @property
+    def has_anchors(self):
+        """inputs with #A anchor lines (the host preparation does not read them)"""
+        return "anchors" in self.opts
 
     @property
     def no_lonely_pairs(self):

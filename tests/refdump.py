@@ -68,4 +68,24 @@ def parse_ref(text):
             io, ex, arcs_a, arcs_b, am[:, :2], am[:, 2], out["min_col"], out["max_col"],
             seq_a=rec["seqA"], seq_b=rec["seqB"], am_stack_score=st, am_stackable=sst)
         out["anchor_match"] = _pairs(rec["anchor_match"])
+        if "anchor_ends" in rec:
+            ra_a, ra_b, la_a, la_b, empty, intervals = (int(x) for x in rec["anchor_ends"])
+            assert intervals, "anchor ranges are not intervals"
+            out["anchor_empty"] = bool(empty)
+            if not empty:
+                # ranges per position, index 0 unused (include/locarna_gb300.h)
+                def arr(pairs, k):
+                    return np.array([0] + [p[k] for p in pairs], dtype=np.int32)
+                m_ = _pairs(rec["anchor_match"])
+                d_ = _pairs(rec["anchor_del"])
+                i_ = _pairs(rec["anchor_ins"])
+                anchors = {"match_lo": arr(m_, 0), "match_hi": arr(m_, 1), "del_lo": arr(d_, 0),
+                           "del_hi": arr(d_, 1), "ins_lo": arr(i_, 0), "ins_hi": arr(i_, 1)}
+                t0 = out["tables"]
+                out["tables"] = PairTables(
+                    t0.len_a, t0.len_b, t0.sigma, t0.gap_a, t0.gap_b, t0.indel_opening, t0.exclusion,
+                    t0.arcs_a, t0.arcs_b, t0.am_arcs, t0.am_score, t0.min_col, t0.max_col,
+                    anchors=anchors, right_anchor=(ra_a, ra_b), left_anchor=(la_a, la_b),
+                    seq_a=t0.seq_a, seq_b=t0.seq_b, am_stack_score=t0.am_stack_score,
+                    am_stackable=t0.am_stackable)
     return out
