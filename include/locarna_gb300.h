@@ -350,8 +350,9 @@ lcg_status lcg_align_score_static(const lcg_pair_tables *pair, const lcg_align_o
  * (basepairs.cc:155-205), sigma / gap / arc weights / arc-match scores
  * (scoring.cc:28-554, RIBOSUM85_60 built in), the max-diff band
  * (trace_controller.cc:360-390) and the sequence envelope
- * (edge_probs.icc:7-268, trace_controller.cc:565-597). Single-sequence
- * inputs without anchors.
+ * (edge_probs.icc:7-268, trace_controller.cc:565-597). Sequences or
+ * profiles (alignment rows); #A anchor lines as strict anchor constraints
+ * (anchor_constraints.cc:10-395, trace_controller.cc:542-563).
  */
 typedef struct lcg_prep_opts {
     double min_prob;              /* --min-prob (0.001) */

@@ -61,7 +61,7 @@ struct RnaInput {
     std::map<std::pair<int, int>, double> arc_probs;  // (i,j) -> p, i<j (sparse matrix)
     // joint probabilities of (i,j) and (i+1,j-1) (the p2 column, read only with stacking)
     std::map<std::pair<int, int>, double> arc2_probs;
-    std::string anchors;
+    std::vector<std::string> anchors;  // the #A<k> lines (k = 1, 2, ...), blocks concatenated
 };
 
 // get_nonempty_line (aux.cc:122-145): skip empty lines and lines starting with
@@ -127,7 +127,7 @@ RnaInput read_pp(const std::string &text, double p_bpcut, bool stacking) {
         }
     } while (next_line(in, line));
     if (names.empty()) perr(LCG_ERR_PARSE, "PP file without sequence");
-    if (!anchors.empty()) perr(LCG_ERR_UNSUPPORTED, "anchor constraints (#A lines) are not supported yet");
+    r.anchors = anchors;
     r.name = names[0];
     // MultipleAlignment::normalize_rna_symbols (multiple_alignment.cc:577-584,
     // aux.cc:65-70) on every row; the rows of an alignment must have equal
@@ -330,6 +330,189 @@ long stack_prob_to_weight(double p, double pe, int struct_weight) {
 // a + b with 64-bit two's-complement wrap-around, as the reference's sums of
 // such weights come out on its targets
 long wrap_add(long a, long b) { return (long)((unsigned long)a + (unsigned long)b); }
+
+// ---------------------------------------------------------------- anchors
+
+// AnchorConstraints with strict names (anchor_constraints.cc:10-395, as the
+// locarna driver constructs it): the allowed match / deletion / insertion
+// ranges per position and the outermost anchors. Positions 1-based.
+struct AnchorRanges {
+    bool empty = true;
+    std::vector<int> match_lo, match_hi, del_lo, del_hi;  // i = 1..lenA (index 0 unused)
+    std::vector<int> ins_lo, ins_hi;                      // j = 1..lenB
+    int ra_a = 0, ra_b = 0, la_a = 0, la_b = 0;
+};
+
+// AnchorConstraints::transform_input (:81-123): the name of every position
+// (its characters over all #A lines) for the non-blank positions, names in
+// strictly increasing order
+std::map<std::string, int> anchor_names(int len, const std::vector<std::string> &rows) {
+    std::vector<std::string> vec(len);
+    for (const auto &x : rows) {
+        if ((int)x.size() != len)
+            perr(LCG_ERR_PARSE, "Error during parsing of anchor constraints. Anchor specification strings must "
+                                "have exactly the same length as the corresponding sequences.");
+        for (int i = 0; i < len; ++i) vec[i].push_back(x[i]);
+    }
+    std::map<std::string, int> tab;
+    std::string last;
+    for (int i = 1; i <= len; ++i) {
+        const std::string &x = vec[i - 1];
+        bool dont_care = true;  // only_dont_care (:74-79)
+        for (char c : x) dont_care = dont_care && (c == ' ' || c == '.' || c == '-');
+        if (dont_care) continue;
+        if (x <= last)
+            perr(LCG_ERR_PARSE, "Error during parsing of constraints. Anchor names not in strict lexicographic "
+                                "order at name \"" + x + "\".");
+        last = x;
+        tab[x] = i;
+    }
+    return tab;
+}
+
+AnchorRanges anchor_ranges(int lenA, const std::vector<std::string> &rowsA, int lenB,
+                           const std::vector<std::string> &rowsB) {
+    AnchorRanges R;
+    // the single-string annotations of both inputs, or none (:40-60)
+    if (rowsA.empty() || rowsB.empty()) return R;
+    if (rowsA.size() != rowsB.size())
+        perr(LCG_ERR_PARSE, "Error while setting up consensus anchor constraints. The anchor names in all input "
+                            "sequences must have the same length.");
+    const auto tabA = anchor_names(lenA, rowsA), tabB = anchor_names(lenB, rowsB);
+    // init_anchors (:125-146): partner position, -1 for a name the other lacks
+    std::vector<long> anA(lenA + 2, 0), anB(lenB + 2, 0);
+    std::vector<std::string> nmA(lenA + 2), nmB(lenB + 2);
+    for (const auto &x : tabA) {
+        nmA[x.second] = x.first;
+        auto it = tabB.find(x.first);
+        anA[x.second] = it != tabB.end() ? it->second : -1;
+    }
+    for (const auto &x : tabB) {
+        nmB[x.second] = x.first;
+        auto it = tabA.find(x.first);
+        anB[x.second] = it != tabA.end() ? it->second : -1;
+    }
+    anA[lenA + 1] = lenA + 1;
+    anB[lenB + 1] = lenB + 1;
+    // init_named_tables (:380-395)
+    auto named_tables = [](int len, const std::vector<long> &an, std::vector<int> &leq, std::vector<int> &geq) {
+        auto named = [&](int i) { return i == 0 || i == len + 1 || an[i] != 0; };
+        leq.assign(len + 1, 0);
+        for (int i = 1; i <= len; ++i) leq[i] = named(i) ? i : leq[i - 1];
+        geq.assign(len + 2, 0);
+        geq[len + 1] = len + 1;
+        for (int i = len; i > 0; --i) geq[i] = named(i) ? i : geq[i + 1];
+    };
+    std::vector<int> leqA, geqA, leqB, geqB;
+    named_tables(lenA, anA, leqA, geqA);
+    named_tables(lenB, anB, leqB, geqB);
+    auto anchoredA = [&](int i) { return i == 0 || i == lenA + 1 || anA[i] > 0; };
+    auto anchoredB = [&](int j) { return j == 0 || j == lenB + 1 || anB[j] > 0; };
+    std::vector<std::pair<long, long>> ar(lenA + 1, {1, lenB}), adr(lenA + 1, {1, lenB}), air(lenB + 1, {1, lenA});
+    // match ranges (:186-235)
+    long last = 0;
+    for (int i = 1; i <= lenA; i++) {
+        if (anA[i] > 0) {
+            last = anA[i];
+            ar[i].first = last;
+        } else if (anA[i] == 0) {
+            ar[i].first = last + 1;
+        } else {
+            for (long j = last + 1; j <= lenB && anB[j] <= 0; j++) {
+                if (anB[j] == -1) {
+                    if (nmB[j] < nmA[i]) last = j;
+                    else break;
+                }
+            }
+            ar[i].first = last + 1;
+        }
+    }
+    last = lenB + 1;
+    for (int i = lenA; i >= 1; i--) {
+        if (anA[i] > 0) {
+            last = anA[i];
+            ar[i].second = last;
+        } else if (anA[i] == 0) {
+            ar[i].second = last - 1;
+        } else {
+            for (long j = last - 1; j >= 1 && anB[j] <= 0; j--) {
+                if (anB[j] == -1) {
+                    if (nmB[j] > nmA[i]) last = j;
+                    else break;
+                }
+            }
+            ar[i].second = last - 1;
+        }
+    }
+    // deletion and insertion ranges (:237-312)
+    nmA[0] = "";
+    nmB[0] = "";
+    const std::string largest = std::max(nmA[leqA[lenA]], nmB[leqB[lenB]]);
+    nmA[lenA + 1] = largest + "X";
+    nmB[lenB + 1] = largest + "X";
+    for (int i = 1, j1 = 0; i <= lenA; ++i) {
+        if (anchoredA(i)) {
+            adr[i] = {lenB + 1, 0};
+        } else {
+            const int i0 = leqA[i], i1 = geqA[i];
+            while (nmB[j1] < nmA[i1]) j1 = geqB[j1 + 1];
+            int j0 = leqB[j1 - 1];
+            while (nmB[j0] > nmA[i0]) j0 = leqB[j0 - 1];
+            adr[i] = {j0, j1 - 1};
+        }
+    }
+    for (int j = 1, i1 = 0; j <= lenB; ++j) {
+        if (anchoredB(j)) {
+            air[j] = {lenA + 1, 0};
+        } else {
+            const int j0 = leqB[j], j1 = geqB[j];
+            while (nmA[i1] < nmB[j1]) i1 = geqA[i1 + 1];
+            int i0 = leqA[i1 - 1];
+            while (nmA[i0] > nmB[j0]) i0 = leqA[i0 - 1];
+            air[j] = {i0, i1 - 1};
+        }
+    }
+    // the ranges clipped to the positions that exist; an empty range as (-1, -2)
+    auto clip = [](std::pair<long, long> r, long hi_max, int &lo, int &hi) {
+        long a = std::max(r.first, 0L), b = std::min(r.second, hi_max);
+        if (a > b) {
+            lo = -1;
+            hi = -2;
+        } else {
+            lo = (int)a;
+            hi = (int)b;
+        }
+    };
+    R.empty = false;
+    R.match_lo.assign(lenA + 1, 0);
+    R.match_hi.assign(lenA + 1, 0);
+    R.del_lo.assign(lenA + 1, 0);
+    R.del_hi.assign(lenA + 1, 0);
+    R.ins_lo.assign(lenB + 1, 0);
+    R.ins_hi.assign(lenB + 1, 0);
+    for (int i = 1; i <= lenA; ++i) {
+        clip(ar[i], lenB, R.match_lo[i], R.match_hi[i]);
+        clip(adr[i], lenB, R.del_lo[i], R.del_hi[i]);
+    }
+    for (int j = 1; j <= lenB; ++j) clip(air[j], lenA, R.ins_lo[j], R.ins_hi[j]);
+    // rightmost_anchor / leftmost_anchor (anchor_constraints.hh:282-306)
+    R.ra_a = R.ra_b = 0;
+    for (int i = lenA; i >= 1; --i)
+        if (anA[i] > 0) {
+            R.ra_a = i;
+            R.ra_b = (int)anA[i];
+            break;
+        }
+    R.la_a = lenA + 1;
+    R.la_b = lenB + 1;
+    for (int i = 0; i <= lenA; ++i)
+        if (anA[i] > 0) {
+            R.la_a = i;
+            R.la_b = (int)anA[i];
+            break;
+        }
+    return R;
+}
 
 // ---------------------------------------------------------------- envelope
 
@@ -543,6 +726,7 @@ struct lcg_prepared_s {
     int32_t indel_opening = 0, exclusion = 0;
     int envelope_ok = 1;
     bool stacking = false;
+    AnchorRanges anchors;  // empty unless both inputs carry #A lines
 };
 
 extern "C" {
@@ -661,6 +845,26 @@ void stage_inputs(std::shared_ptr<const Side> A, std::shared_ptr<const Side> B, 
     S.tc.minc.assign(n + 1, 0);
     S.tc.maxc.assign(n + 1, m);
     if (o.max_diff >= 0) constrain_wo_ref(S.tc, n, m, (size_t)o.max_diff);
+    // anchor constraints (strict names) and TraceController::restrict_by_anchors
+    // (trace_controller.cc:542-563)
+    P->anchors = anchor_ranges(n, sa.in.anchors, m, sb.in.anchors);
+    const AnchorRanges &R = P->anchors;
+    if (!R.empty) {
+        for (int i = 1; i <= n; ++i) {
+            long cmin = S.tc.maxc[i], cmax = S.tc.minc[i];
+            for (long j = S.tc.minc[i]; j <= S.tc.maxc[i]; ++j) {
+                const bool ok = (R.match_lo[i] <= j && j <= R.match_hi[i]) ||
+                                (j > 0 && R.ins_lo[j] <= i && i <= R.ins_hi[j]) ||
+                                (R.del_lo[i] <= j && j <= R.del_hi[i]);
+                if (ok) {
+                    cmin = std::min(cmin, j);
+                    cmax = std::max(cmax, j);
+                }
+            }
+            S.tc.minc[i] = std::max(S.tc.minc[i], cmin);
+            S.tc.maxc[i] = std::min(S.tc.maxc[i], cmax);
+        }
+    }
 }
 
 // the envelope in the reference's precision (edge_probs.icc, trace_controller.cc:565-597)
@@ -761,7 +965,10 @@ void stage_tables(Staged &S) {
         const size_t ib1 = lhi >= llo ? (size_t)B.left_start[llo] : 0;
         for (size_t ib = ib0; ib < ib1; ++ib) {
             const Arc &b = B.arcs[ib];
+            const AnchorRanges &R = P->anchors;
             bool ok = valid_match(a.l, b.l) && valid_match(a.r, b.r) &&
+                      (R.empty || (R.match_lo[a.l] <= b.l && b.l <= R.match_hi[a.l] && R.match_lo[a.r] <= b.r &&
+                                   b.r <= R.match_hi[a.r])) &&
                       (size_t)std::abs((a.r - a.l) - (b.r - b.l)) <= mdam &&
                       (size_t)a.l <= b.l + mdaam && (size_t)b.l <= a.l + mdaam &&
                       (size_t)a.r <= b.r + mdaam && (size_t)b.r <= a.r + mdaam;
@@ -1061,6 +1268,19 @@ lcg_status lcg_prepared_tables(lcg_prepared p, lcg_pair_tables *t) {
     t->right_anchor_b = 0;
     t->left_anchor_a = p->n + 1;
     t->left_anchor_b = p->m + 1;
+    if (!p->anchors.empty) {
+        const AnchorRanges &R = p->anchors;
+        t->match_lo = R.match_lo.data();
+        t->match_hi = R.match_hi.data();
+        t->del_lo = R.del_lo.data();
+        t->del_hi = R.del_hi.data();
+        t->ins_lo = R.ins_lo.data();
+        t->ins_hi = R.ins_hi.data();
+        t->right_anchor_a = R.ra_a;
+        t->right_anchor_b = R.ra_b;
+        t->left_anchor_a = R.la_a;
+        t->left_anchor_b = R.la_b;
+    }
     return LCG_OK;
 }
 

@@ -139,7 +139,11 @@ def _tables_of(lib, h):
         seq_a=lib.lcg_prepared_sequence(h, 0).decode(), seq_b=lib.lcg_prepared_sequence(h, 1).decode(),
         am_stack_score=_arr(t.am_stack_score, nam) if t.am_stack_score else None,
         am_stackable=(np.ctypeslib.as_array(t.am_stackable, shape=(nam,)).copy() if nam else np.zeros(0, np.uint8))
-        if t.am_stack_score else None)
+        if t.am_stack_score else None,
+        anchors=({"match_lo": _arr(t.match_lo, n + 1), "match_hi": _arr(t.match_hi, n + 1),
+                  "del_lo": _arr(t.del_lo, n + 1), "del_hi": _arr(t.del_hi, n + 1),
+                  "ins_lo": _arr(t.ins_lo, m + 1), "ins_hi": _arr(t.ins_hi, m + 1)} if t.match_lo else None),
+        right_anchor=(t.right_anchor_a, t.right_anchor_b), left_anchor=(t.left_anchor_a, t.left_anchor_b))
     pt.name_a = lib.lcg_prepared_sequence(h, 2).decode()
     pt.name_b = lib.lcg_prepared_sequence(h, 3).decode()
     pt.envelope_ok = bool(lib.lcg_prepared_envelope_ok(h))

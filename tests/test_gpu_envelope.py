@@ -21,7 +21,7 @@ def _same_tables(t, r, what):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("name", [n for n in sankoff_golden_names() if not n.startswith("a")])
+@pytest.mark.parametrize("name", sankoff_golden_names())
 def test_gpu_envelope_matches_reference_tables(engine, name):
     from locarna_gb300.prep import prepare_pairs
     g = Golden(name)

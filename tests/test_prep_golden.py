@@ -22,7 +22,7 @@ def prep_kwargs(g):
     return kw
 
 
-@pytest.mark.parametrize("name", [n for n in golden_names() if not n.startswith("a")])
+@pytest.mark.parametrize("name", golden_names())
 def test_prep_matches_reference_tables(name):
     from locarna_gb300.prep import prepare_pair
     g = Golden(name)
@@ -38,6 +38,11 @@ def test_prep_matches_reference_tables(name):
     assert np.array_equal(t.arcs_a, r.arcs_a) and np.array_equal(t.arcs_b, r.arcs_b), "arcs differ"
     assert np.array_equal(t.am_arcs, r.am_arcs), "arc match list differs"
     assert np.array_equal(t.am_score, r.am_score), "arc match scores differ"
+    assert (t.anchors is None) == (r.anchors is None), "anchors on/off differ"
+    if r.anchors is not None:
+        for k in r.anchors:
+            assert np.array_equal(t.anchors[k], r.anchors[k]), f"anchor ranges {k} differ"
+        assert t.right_anchor == r.right_anchor and t.left_anchor == r.left_anchor, "outermost anchors differ"
     assert (t.am_stack_score is None) == (r.am_stack_score is None), "stacking on/off differs"
     if r.am_stack_score is not None:
         assert np.array_equal(t.am_stack_score, r.am_stack_score), "stacked arc match scores differ"
