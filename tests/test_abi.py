@@ -39,14 +39,14 @@ def test_abi_version():
 
 
 def test_ctypes_structs_match_c_layout(tmp_path):
-    """Every ctypes mirror in locarna_gb300.abi has the size and field offsets
+    """Every ctypes mirror in locarna_gb300.abi / .prep has the size and field offsets
     the C compiler gives the header's struct of the same name."""
     import subprocess
 
-    from locarna_gb300 import abi
-    structs = {name: cls for name, cls in vars(abi).items()
+    from locarna_gb300 import abi, prep
+    structs = {name: cls for mod in (abi, prep) for name, cls in vars(mod).items()
                if name.startswith("lcg_") and isinstance(cls, type) and issubclass(cls, C.Structure)}
-    assert "lcg_pf_opts" in structs and "lcg_pair_tables" in structs
+    assert "lcg_pf_opts" in structs and "lcg_pair_tables" in structs and "lcg_prep_opts" in structs
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "locarna_gb300.h"', "int main(void) {"]
     for name, cls in sorted(structs.items()):
         lines.append(f'printf("{name} %zu\\n", sizeof({name}));')
