@@ -170,9 +170,13 @@ def cpu_sample(tables, budget_s, cores, seed=7, worker=None):
 # ---------------------------------------------------------------- clocks
 
 class ClockSampler:
+    """nvidia-smi clock / throttle samples during the timed region, written to
+    LCG_CLOCK_LOG (default: a file in the temporary directory)."""
+
     def __init__(self):
+        import tempfile
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", "bench_clocks.csv")
+        self.path = os.environ.get("LCG_CLOCK_LOG") or os.path.join(tempfile.gettempdir(), "lcg_bench_clocks.csv")
 
     def start(self):
         try:

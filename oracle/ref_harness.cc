@@ -58,6 +58,7 @@ struct Opts {
     double exp_prob = -1;  // --exp-prob; < 0: not given
     int normalized = -1, penalized = -1;  // --normalized L / --penalized PP (-1: off)
     int kbest = 0;                          // --kbest k (0: off)
+    bool relaxed_anchors = false;           // --relaxed-anchors
     long better = -1000000;                 // --better t
     bool dump_tables = true;
     int repeat = 1;
@@ -89,6 +90,7 @@ static void parse(Opts &o, const char *kv) {
     else if (k == "normalized") o.normalized = std::atoi(v.c_str());
     else if (k == "penalized") o.penalized = std::atoi(v.c_str());
     else if (k == "kbest") o.kbest = std::atoi(v.c_str());
+    else if (k == "relaxed_anchors") o.relaxed_anchors = std::atoi(v.c_str());
     else if (k == "better") o.better = std::atol(v.c_str());
     else if (k == "repeat") o.repeat = std::atoi(v.c_str());
     else { std::cerr << "unknown option " << k << "\n"; std::exit(2); }
@@ -122,7 +124,7 @@ int main(int argc, char **argv) {
     AnchorConstraints anchors(
         lenA, seqA.annotation(MultipleAlignment::AnnoType::anchors).single_string(),
         lenB, seqB.annotation(MultipleAlignment::AnnoType::anchors).single_string(),
-        true);
+        !o.relaxed_anchors);
     TraceController tc(seqA, seqB, nullptr, o.max_diff, false);
     tc.restrict_by_anchors(anchors);
 
