@@ -152,6 +152,56 @@ public:
         if (!aligned_) align();
         if (!ap_.do_trace) throw failure("locarna_gb300: trace() needs do_trace");
     }
+    // Aligner::normalized_align(L) (aligner.cc:1521-1588): the normalized
+    // score; the alignment is traced by the same call
+    int64_t normalized_align(int L) {
+        AlignerParams keep = ap_;
+        ap_.normalized = L;
+        ap_.penalized = -1;
+        int64_t s = align();
+        ap_ = keep;
+        return s;
+    }
+    // Aligner::penalized_align(PP) (aligner.cc:1590-1617): the penalised
+    // score; the alignment is traced by the same call
+    int64_t penalized_align(int position_penalty) {
+        AlignerParams keep = ap_;
+        ap_.penalized = position_penalty;
+        ap_.normalized = -1;
+        int64_t s = align();
+        ap_ = keep;
+        return s;
+    }
+    // Aligner::suboptimal (aligner.cc:1384-1512): up to k alignments by
+    // interval splitting with their scores (normalized when the parameters
+    // ask for it), ending below threshold + 1
+    std::vector<std::pair<int64_t, Alignment>> suboptimal(int k, int64_t threshold) {
+        const lcg_pair_tables &t = *ap_.tables;
+        const size_t ne = 2 * (size_t)(t.len_a + t.len_b) + 2, nt = (size_t)std::min(t.len_a, t.len_b) + 1;
+        std::vector<int32_t> edges(ne * (size_t)k), tam(nt * (size_t)k);
+        std::vector<lcg_align_result> r((size_t)k);
+        for (int h = 0; h < k; ++h) {
+            r[h] = lcg_align_result{};
+            r[h].edges = edges.data() + ne * h;
+            r[h].traced_am = tam.data() + nt * h;
+        }
+        const lcg_align_opts o = ap_.opts();
+        int32_t hits = 0;
+        check(lcg_align_kbest(eng_->get(), &t, 1, &o, k, threshold, r.data(), &hits));
+        std::vector<std::pair<int64_t, Alignment>> out;
+        for (int h = 0; h < hits; ++h) {
+            Alignment a;
+            a.max_i = r[h].max_i;
+            a.max_j = r[h].max_j;
+            a.min_i = r[h].min_i;
+            a.min_j = r[h].min_j;
+            for (int q = 0; q < r[h].num_edges; ++q)
+                a.edges.emplace_back(r[h].edges[2 * q], r[h].edges[2 * q + 1]);
+            a.traced_arcmatches.assign(r[h].traced_am, r[h].traced_am + r[h].num_traced_am);
+            out.emplace_back(r[h].score, std::move(a));
+        }
+        return out;
+    }
     const Alignment &get_alignment() const { return alignment_; }
     static bool is_neg_inf(int64_t score) { return score == LCG_NEG_INF; }
 };
