@@ -106,6 +106,10 @@ CASES = {
     "a150_anchors_free": (150, 81, "h", 82, {"anchors": "30:30,110:110", "free_endgaps": "++++"}, True),
     "a150_anchors_nolp": (150, 81, "h", 82, {"anchors": "60:60", "no_lonely_pairs": "1"}, True),
     "a120_anchors_unrel": (120, 21, 130, 22, {"anchors": "10:15,60:70,100:120"}, True),
+    # --max-diff (band around the diagonal), --max-diff-am / --max-diff-at-am (arc-match filters)
+    "c150_maxdiff": (150, 1, 150, 2, {"max_diff": "20"}, True),
+    "h150_maxdiff_am": (150, 81, "h", 82, {"max_diff_am": "5", "max_diff_at_am": "12"}, True),
+    "p120_maxdiff": (("p", 120, 3), 5, ("p", 110, 2), 6, {"max_diff": "30", "sequ_local": "1"}, True),
 }
 
 STACK_KEYS = ("stacking", "new_stacking")

@@ -9,7 +9,9 @@ _OPT_MAP = {"sequ_local": ("sequ_local", int), "free_endgaps": ("free_endgaps", 
             "min_trace_prob": ("min_trace_probability", float), "indel_opening": ("indel_opening", int),
             "struct_local": None, "no_lonely_pairs": None, "stacking": ("stacking", int),
             "new_stacking": ("new_stacking", int), "exp_prob": ("exp_prob", float),
-            "normalized": None, "penalized": None, "kbest": None, "better": None, "anchors": None}
+            "normalized": None, "penalized": None, "kbest": None, "better": None, "anchors": None,
+            "max_diff": ("max_diff", int), "max_diff_am": ("max_diff_am", int),
+            "max_diff_at_am": ("max_diff_at_am", int)}
 
 
 def prep_kwargs(g):
