@@ -377,6 +377,9 @@ typedef struct lcg_prep_opts {
      * #STACK section and fill lcg_pair_tables.am_stack_score/am_stackable */
     int32_t stacking;
     int32_t new_stacking;
+    /* --relaxed-anchors: anchor names need not be ordered (relaxed
+     * AnchorConstraints, anchor_constraints.cc:322-357) */
+    int32_t relaxed_anchors;
 } lcg_prep_opts;
 
 typedef struct lcg_prepared_s *lcg_prepared;

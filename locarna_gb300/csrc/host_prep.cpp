@@ -333,9 +333,10 @@ long wrap_add(long a, long b) { return (long)((unsigned long)a + (unsigned long)
 
 // ---------------------------------------------------------------- anchors
 
-// AnchorConstraints with strict names (anchor_constraints.cc:10-395, as the
-// locarna driver constructs it): the allowed match / deletion / insertion
-// ranges per position and the outermost anchors. Positions 1-based.
+// AnchorConstraints (anchor_constraints.cc:10-395, strict names unless
+// --relaxed-anchors, as the locarna driver constructs it, locarna.cc:553-557):
+// the allowed match / deletion / insertion ranges per position and the
+// outermost anchors. Positions 1-based.
 struct AnchorRanges {
     bool empty = true;
     std::vector<int> match_lo, match_hi, del_lo, del_hi;  // i = 1..lenA (index 0 unused)
@@ -346,7 +347,7 @@ struct AnchorRanges {
 // AnchorConstraints::transform_input (:81-123): the name of every position
 // (its characters over all #A lines) for the non-blank positions, names in
 // strictly increasing order
-std::map<std::string, int> anchor_names(int len, const std::vector<std::string> &rows) {
+std::map<std::string, int> anchor_names(int len, const std::vector<std::string> &rows, bool strict) {
     std::vector<std::string> vec(len);
     for (const auto &x : rows) {
         if ((int)x.size() != len)
@@ -361,24 +362,28 @@ std::map<std::string, int> anchor_names(int len, const std::vector<std::string> 
         bool dont_care = true;  // only_dont_care (:74-79)
         for (char c : x) dont_care = dont_care && (c == ' ' || c == '.' || c == '-');
         if (dont_care) continue;
-        if (x <= last)
-            perr(LCG_ERR_PARSE, "Error during parsing of constraints. Anchor names not in strict lexicographic "
-                                "order at name \"" + x + "\".");
-        last = x;
+        if (strict) {
+            if (x <= last)
+                perr(LCG_ERR_PARSE, "Error during parsing of constraints. Anchor names not in strict lexicographic "
+                                    "order at name \"" + x + "\".");
+            last = x;
+        } else if (tab.count(x)) {
+            perr(LCG_ERR_PARSE, "Error during parsing of constraints. Duplicate constraint name: \"" + x + "\".");
+        }
         tab[x] = i;
     }
     return tab;
 }
 
 AnchorRanges anchor_ranges(int lenA, const std::vector<std::string> &rowsA, int lenB,
-                           const std::vector<std::string> &rowsB) {
+                           const std::vector<std::string> &rowsB, bool strict) {
     AnchorRanges R;
     // the single-string annotations of both inputs, or none (:40-60)
     if (rowsA.empty() || rowsB.empty()) return R;
     if (rowsA.size() != rowsB.size())
         perr(LCG_ERR_PARSE, "Error while setting up consensus anchor constraints. The anchor names in all input "
                             "sequences must have the same length.");
-    const auto tabA = anchor_names(lenA, rowsA), tabB = anchor_names(lenB, rowsB);
+    const auto tabA = anchor_names(lenA, rowsA, strict), tabB = anchor_names(lenB, rowsB, strict);
     // init_anchors (:125-146): partner position, -1 for a name the other lacks
     std::vector<long> anA(lenA + 2, 0), anB(lenB + 2, 0);
     std::vector<std::string> nmA(lenA + 2), nmB(lenB + 2);
@@ -409,9 +414,24 @@ AnchorRanges anchor_ranges(int lenA, const std::vector<std::string> &rowsA, int 
     auto anchoredA = [&](int i) { return i == 0 || i == lenA + 1 || anA[i] > 0; };
     auto anchoredB = [&](int j) { return j == 0 || j == lenB + 1 || anB[j] > 0; };
     std::vector<std::pair<long, long>> ar(lenA + 1, {1, lenB}), adr(lenA + 1, {1, lenB}), air(lenB + 1, {1, lenA});
+    // relaxed names (:322-357): the match ranges from the anchored positions
+    // only; the deletion and insertion ranges keep their initial values
+    // (1..lenB, 1..lenA), as in the reference
+    if (!strict) {
+        long last = 0;
+        for (int i = 1; i <= lenA; i++) {
+            if (anA[i] > 0) last = anA[i];
+            ar[i].first = anA[i] > 0 ? last : last + 1;
+        }
+        last = lenB + 1;
+        for (int i = lenA; i >= 1; i--) {
+            if (anA[i] > 0) last = anA[i];
+            ar[i].second = anA[i] > 0 ? last : last - 1;
+        }
+    }
     // match ranges (:186-235)
     long last = 0;
-    for (int i = 1; i <= lenA; i++) {
+    for (int i = 1; i <= lenA && strict; i++) {
         if (anA[i] > 0) {
             last = anA[i];
             ar[i].first = last;
@@ -428,7 +448,7 @@ AnchorRanges anchor_ranges(int lenA, const std::vector<std::string> &rowsA, int 
         }
     }
     last = lenB + 1;
-    for (int i = lenA; i >= 1; i--) {
+    for (int i = lenA; i >= 1 && strict; i--) {
         if (anA[i] > 0) {
             last = anA[i];
             ar[i].second = last;
@@ -450,7 +470,7 @@ AnchorRanges anchor_ranges(int lenA, const std::vector<std::string> &rowsA, int 
     const std::string largest = std::max(nmA[leqA[lenA]], nmB[leqB[lenB]]);
     nmA[lenA + 1] = largest + "X";
     nmB[lenB + 1] = largest + "X";
-    for (int i = 1, j1 = 0; i <= lenA; ++i) {
+    for (int i = 1, j1 = 0; i <= lenA && strict; ++i) {
         if (anchoredA(i)) {
             adr[i] = {lenB + 1, 0};
         } else {
@@ -461,7 +481,7 @@ AnchorRanges anchor_ranges(int lenA, const std::vector<std::string> &rowsA, int 
             adr[i] = {j0, j1 - 1};
         }
     }
-    for (int j = 1, i1 = 0; j <= lenB; ++j) {
+    for (int j = 1, i1 = 0; j <= lenB && strict; ++j) {
         if (anchoredB(j)) {
             air[j] = {lenA + 1, 0};
         } else {
@@ -847,7 +867,7 @@ void stage_inputs(std::shared_ptr<const Side> A, std::shared_ptr<const Side> B, 
     if (o.max_diff >= 0) constrain_wo_ref(S.tc, n, m, (size_t)o.max_diff);
     // anchor constraints (strict names) and TraceController::restrict_by_anchors
     // (trace_controller.cc:542-563)
-    P->anchors = anchor_ranges(n, sa.in.anchors, m, sb.in.anchors);
+    P->anchors = anchor_ranges(n, sa.in.anchors, m, sb.in.anchors, !o.relaxed_anchors);
     const AnchorRanges &R = P->anchors;
     if (!R.empty) {
         for (int i = 1; i <= n; ++i) {

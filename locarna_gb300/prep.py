@@ -21,7 +21,7 @@ class lcg_prep_opts(C.Structure):
         ("max_diff_am", C.c_int32), ("max_diff_at_am", C.c_int32),
         ("temperature_alipf", C.c_int32), ("sequ_local", C.c_int32),
         ("free_endgaps", C.c_int32), ("pf_precision", C.c_int32), ("exp_prob", C.c_double),
-        ("stacking", C.c_int32), ("new_stacking", C.c_int32),
+        ("stacking", C.c_int32), ("new_stacking", C.c_int32), ("relaxed_anchors", C.c_int32),
     ]
 
 

@@ -51,3 +51,40 @@ def test_reference_example_tables_and_alignment(opts):
 
     res = oracle_align(t, struct_local=opts.get("struct_local") == "1", sequ_local=opts.get("sequ_local") == "1")
     assert_matches_golden(G, res)
+
+
+def test_relaxed_anchors_against_reference(tmp_path):
+    """--relaxed-anchors: anchor names in any order; the host preparation's
+    ranges, band and arc matches and the oracle's alignment against the
+    reference's harness on an anchored synthetic pair."""
+    from checks import assert_matches_golden
+    from locarna_gb300.prep import prepare_pair
+    from locarna_gb300.synth import make_homolog, make_rna
+    from oracle_ffi import oracle_align
+    _example()  # needs the reference tree and its harness
+    a = make_rna(150, 81)
+    b = make_homolog(a, 82)
+    sa, sb = ["."] * 150, ["."] * 150
+    for name, x, y in (("C", 20, 20), ("A", 75, 75), ("B", 130, 130)):  # not in lexicographic order
+        sa[x - 1] = sb[y - 1] = name
+    pa, pb = tmp_path / "a.pp", tmp_path / "b.pp"
+    pa.write_text(a.to_pp(anchors="".join(sa)))
+    pb.write_text(b.to_pp(anchors="".join(sb)))
+    out = subprocess.run([HARNESS, str(pa), str(pb), "relaxed_anchors=1"], capture_output=True, text=True,
+                         check=True).stdout
+    ref = parse_ref(out)
+    r = ref["tables"]
+    t = prepare_pair(pa.read_text(), pb.read_text(), relaxed_anchors=1)
+    for f in ("min_col", "max_col", "am_arcs", "am_score"):
+        assert np.array_equal(getattr(t, f), getattr(r, f)), f
+    for k in r.anchors:
+        assert np.array_equal(t.anchors[k], r.anchors[k]), k
+
+    class G:
+        name = "relaxed anchors"
+        tables = t
+        score = ref["score"]
+        edges = [tuple(e) for e in ref["edges"]]
+        struct_a, struct_b = ref["struct_a"], ref["struct_b"]
+
+    assert_matches_golden(G, oracle_align(t))
