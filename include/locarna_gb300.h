@@ -66,7 +66,8 @@ typedef struct lcg_pair_tables {
     int32_t indel_opening; /* Scoring::indel_opening() (scoring.hh:617) */
     int32_t exclusion;     /* Scoring::exclusion()     (scoring.hh:611) */
     /* arcs in the reference's arc index order (basepairs.cc:155-205):
-     * arcs_x[2k] = left end, arcs_x[2k+1] = right end of arc k */
+     * arcs_x[2k] = left end, arcs_x[2k+1] = right end of arc k, with
+     * right >= left + 3 as BasePairs makes them (others: LCG_ERR_ARG) */
     int32_t num_arcs_a, num_arcs_b;
     const int32_t *arcs_a;
     const int32_t *arcs_b;
