@@ -45,6 +45,21 @@ def log(*a):
     print(*a, file=sys.stderr, flush=True)
 
 
+def int_peak_gops(dpx, device=0):
+    """The measured int32 add+max rate (G ops/s) from the probe library."""
+    import ctypes as C
+
+    from locarna_gb300.build import build_probe
+    lib = C.CDLL(build_probe())
+    lib.lcg_probe_int_peak.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_double)]
+    lib.lcg_probe_int_peak.restype = C.c_int
+    g = C.c_double()
+    rc = lib.lcg_probe_int_peak(device, int(bool(dpx)), C.byref(g))
+    if rc != 0:
+        raise RuntimeError(f"int32 rate probe failed (cuda error {rc})")
+    return g.value
+
+
 def workload_pp():
     """PP texts of the all-pairs workload and its pairs (index pairs)."""
     from locarna_gb300.synth import make_family
@@ -383,7 +398,7 @@ def run_ours(args):
     eng.run_call(call)
     work = eng.last_work()
     eng.set_counting(False)
-    int_peak = max(eng.int_peak_gops(False), eng.int_peak_gops(True))
+    int_peak = max(int_peak_gops(False), int_peak_gops(True))
 
     # L2 flush buffer (larger than the 129 MB L2)
     flush = None

@@ -245,10 +245,6 @@ lcg_status lcg_engine_last_transfer(lcg_engine eng, int64_t *h2d_bytes,
 lcg_status lcg_engine_set_counting(lcg_engine eng, int32_t on);
 lcg_status lcg_engine_last_work(lcg_engine eng, lcg_work_counts *out);
 
-/* Measured device rate of int32 add+max (2 ops each) in G ops/s, with plain
- * add/max instructions (dpx = 0) or the fused __viaddmax_s32 (dpx = 1). */
-lcg_status lcg_measure_int_peak(lcg_engine eng, int32_t dpx, double *gops);
-
 
 /* --------------------------------------------- LocARNA-P forward/backward
  *
@@ -324,17 +320,19 @@ lcg_status lcg_pf_last_timing(lcg_engine eng, double *forward_ms, double *backwa
 /* -------------------------------------------- allocation-free entry point
  *
  * No counterpart in the reference: an addition of this library for callers
- * that must not allocate device memory while they run (work recorded into a
- * CUDA graph, memory reserved up front by another framework, real-time loops
- * where cudaMalloc / cudaFree would synchronise the device). It computes what
- * lcg_align_pairs computes without traceback (the score and the end cell of
- * one pair, plain mode) and takes every device byte from one fixed
- * file-scope device array of LCG_STATIC_SCRATCH_BYTES held per GPU for the
- * life of the process; it calls no cudaMalloc, cudaFree, cudaMallocHost or
- * other allocating CUDA routine. Pairs whose data do not fit are rejected
- * with LCG_ERR_RANGE. All calls share the array: calls whose GPU work
- * overlaps race on it. The first call on a device looks the array's address
- * up (cudaGetSymbolAddress); make it before any stream capture.
+ * that cannot allocate device memory while they run (a service whose GPU
+ * memory is reserved up front by another framework's allocator, a real-time
+ * loop where cudaMalloc / cudaFree would synchronise the device). It computes
+ * what lcg_align_pairs computes without traceback (the score and the end cell
+ * of one pair: global, sequence-local, free end gaps, --noLP, stacking,
+ * anchor constraints) and takes every device byte from one fixed file-scope
+ * device array of LCG_STATIC_SCRATCH_BYTES held per GPU for the life of the
+ * process; it calls no cudaMalloc, cudaFree, cudaMallocHost or other
+ * allocating CUDA routine. Pairs whose data do not fit are rejected with
+ * LCG_ERR_RANGE (about 400 x 400 nt with the default envelope is beyond the
+ * limit). All calls share the array: calls whose GPU work overlaps race on it.
+ * The first call on a device looks the array's address up
+ * (cudaGetSymbolAddress); make it before any stream capture.
  * opts->struct_local and opts->do_trace must be 0. stream is a cudaStream_t
  * (NULL = default stream); the call returns when its results are on the host.
  */

@@ -2,6 +2,9 @@
 
 * ``locarna_gb300/_build/liblocarna_gb300.so``: the CUDA engine (sm_103a) and
   the C ABI of include/locarna_gb300.h;
+* ``locarna_gb300/_build/liblcg_probe.so``: the int32 add+max rate probe the
+  benchmark reports its integer roofline against (measurement only, not part
+  of the engine);
 * ``oracle/_build/liboracle.so``: the plain-C oracle (test infrastructure);
 * ``oracle/_ref/*``: the reference's own sources compiled as an oracle, only
   where the reference sources are present (``oracle/build_ref.sh``).
@@ -24,8 +27,9 @@ GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 # tuning defines for the CUDA sources, e.g. LCG_NVCC_DEFS="-DLCG_FILL_WARPS=4"
 EXTRA_DEFS = os.environ.get("LCG_NVCC_DEFS", "").split()
 
-CUDA_SOURCES = ["engine.cu", "sankoff_kernels.cu", "sankoff_sl_kernels.cu", "microbench.cu", "noalloc.cu",
+CUDA_SOURCES = ["engine.cu", "sankoff_kernels.cu", "sankoff_sl_kernels.cu", "noalloc.cu",
                 "pf_kernels.cu", "engine_pf.cu", "envelope.cu"]
+PROBE_SOURCE = "microbench.cu"  # the measurement probe, a library of its own
 HOST_SOURCES = ["host_prep.cpp"]  # C++ host-only translation units
 
 
@@ -74,6 +78,17 @@ def build_engine(verbose=False, force=False):
     return lib
 
 
+def build_probe(force=False):
+    """The int32 add+max rate probe (lcg_probe_int_peak) as its own library."""
+    os.makedirs(OUT, exist_ok=True)
+    s = os.path.join(CSRC, PROBE_SOURCE)
+    lib = os.path.join(OUT, "liblcg_probe.so")
+    if force or _newer(lib, [s]):
+        _run([NVCC, GENCODE, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-shared", s, "-o", lib,
+              "-lcudart"])
+    return lib
+
+
 def build_oracle():
     out = os.path.join(ORACLE, "_build")
     os.makedirs(out, exist_ok=True)
@@ -93,9 +108,15 @@ def build_oracle():
     return os.path.join(out, "liboracle.so")
 
 
+def reference_tree():
+    """The reference source tree: $LOCARNA_REF, else a checkout named
+    ``reference`` beside the repository."""
+    return os.environ.get("LOCARNA_REF") or os.path.join(os.path.dirname(ROOT), "reference")
+
+
 def build_reference_oracle():
     """Compile the reference sources as an oracle when they are present."""
-    ref = os.environ.get("LOCARNA_REF", "/root/reference")
+    ref = reference_tree()
     if not os.path.isdir(os.path.join(ref, "src", "LocARNA")):
         return None
     _run(["bash", os.path.join(ORACLE, "build_ref.sh")])
@@ -103,11 +124,12 @@ def build_reference_oracle():
 
 
 def build_all(verbose=False):
-    with ThreadPoolExecutor(max_workers=3) as ex:
+    with ThreadPoolExecutor(max_workers=4) as ex:
         f1 = ex.submit(build_engine, verbose)
         f2 = ex.submit(build_oracle)
         f3 = ex.submit(build_reference_oracle)
-        return f1.result(), f2.result(), f3.result()
+        f4 = ex.submit(build_probe)
+        return f1.result(), f2.result(), f3.result(), f4.result()
 
 
 if __name__ == "__main__":

@@ -1123,13 +1123,6 @@ lcg_status lcg_engine_last_work(lcg_engine e, lcg_work_counts *w) {
     return LCG_OK;
 }
 
-lcg_status lcg_measure_int_peak(lcg_engine e, int32_t dpx, double *gops) {
-    if (!e || !gops) return fail(LCG_ERR_ARG, "NULL argument");
-    CUDA_TRY(cudaSetDevice(e->device));
-    CUDA_TRY(measure_int_peak(e->sms, dpx != 0, e->stream, gops));
-    return LCG_OK;
-}
-
 lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t npairs,
                            const lcg_align_opts *opts, lcg_align_result *results) {
     if (!e || !pairs || !opts || !results || npairs < 0) return fail(LCG_ERR_ARG, "NULL argument");

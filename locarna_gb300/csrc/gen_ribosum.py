@@ -7,11 +7,14 @@ RibosumFreq::write_CC_matrix, src/LocARNA/ribosum.cc); this script formats the
 same values the same way, so the C++ literals denote the same doubles.
 The scoring matrices are symmetric and given as lower triangles.
 
-Usage: python gen_ribosum.py [path/to/RIBOSUM85_60] > ribosum85_60.inc
+Usage: python gen_ribosum.py path/to/RIBOSUM85_60 > ribosum85_60.inc
+(the file lies under Data/Matrices/ of the reference tree)
 """
 import sys
 
-path = sys.argv[1] if len(sys.argv) > 1 else "/root/reference/Data/Matrices/RIBOSUM85_60"
+if len(sys.argv) != 2:
+    raise SystemExit(__doc__)
+path = sys.argv[1]
 lines = open(path).read().splitlines()
 
 

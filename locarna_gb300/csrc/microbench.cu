@@ -1,6 +1,7 @@
-// Integer roofline probe: the sustained rate of the operation the Sankoff
-// recursion is made of, an int32 add followed by a max (max(x + y, z)), on
-// every SM. Each thread runs independent dependency chains so the probe is
+// Integer roofline probe (measurement only, built into its own library
+// liblcg_probe.so, not into the alignment engine): the sustained rate of the
+// operation the Sankoff recursion is made of, an int32 add followed by a max
+// (max(x + y, z)), on every SM. Each thread runs independent dependency chains so the probe is
 // throughput-, not latency-bound. One add+max counts as 2 integer ops, the
 // unit of the DP's operation count (10 per cell, 2 per arc-pair candidate).
 #include <cuda_runtime.h>
@@ -63,3 +64,17 @@ cudaError_t measure_int_peak(int sms, bool dpx, cudaStream_t st, double *gops) {
 }
 
 }  // namespace lcg
+
+// Measured int32 add+max rate of CUDA device `device` in G ops/s, with plain
+// add/max instructions (dpx = 0) or the fused __viaddmax_s32 (dpx = 1).
+// Returns 0 on success, else the cudaError_t of the failing call.
+extern "C" int lcg_probe_int_peak(int device, int dpx, double *gops) {
+    if (!gops) return (int)cudaErrorInvalidValue;
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) return (int)e;
+    int sms = 0;
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    if (e != cudaSuccess) return (int)e;
+    e = lcg::measure_int_peak(sms, dpx != 0, (cudaStream_t)0, gops);
+    return (int)e;
+}

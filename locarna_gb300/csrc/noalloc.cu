@@ -1,14 +1,15 @@
 // Allocation-free entry point: the score of one pair computed with every
 // device byte taken from a fixed file-scope device array.
 //
-// Who needs it: callers that must not allocate device memory while they run,
-// e.g. code that records its GPU work into a CUDA graph, a service whose
-// memory is reserved up front by another framework, or a real-time loop in
-// which cudaMalloc / cudaFree (which may synchronise the whole device) are
-// not acceptable. lcg_align_pairs grows its own device and pinned host buffers
-// on demand; this entry point never calls cudaMalloc, cudaFree, cudaMallocHost
-// or any other allocating CUDA or library routine. Host-side preparation of
-// the pair's index structures uses ordinary heap memory.
+// Who needs it: callers that cannot allocate device memory while they run,
+// for example a service whose GPU memory is reserved up front by another
+// framework's allocator (a cudaMalloc of its own would fail or fragment that
+// reservation), or a real-time loop in which cudaMalloc / cudaFree are not
+// acceptable because they may synchronise the whole device.
+// lcg_align_pairs grows its own device and pinned host buffers on demand;
+// this entry point never calls cudaMalloc, cudaFree, cudaMallocHost or any
+// other allocating CUDA or library routine. Host-side preparation of the
+// pair's index structures uses ordinary heap memory.
 //
 // Limits and sharing:
 //  * all device data of a call (copied inputs, the arc-match table, the
@@ -76,6 +77,18 @@ lcg_status static_base(int dev, char **out) {
         cudaError_t _e = (call);                                                               \
         if (_e != cudaSuccess)                                                                 \
             return static_fail(LCG_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(_e)); \
+    } while (0)
+
+// After the launch: on failure, wait for the stream (ignoring its status)
+// before returning, so that no work of this call still uses the shared array
+// when the next call starts overwriting it.
+#define STATIC_TRY_DRAIN(call, s)                                                              \
+    do {                                                                                       \
+        cudaError_t _e = (call);                                                               \
+        if (_e != cudaSuccess) {                                                               \
+            cudaStreamSynchronize(s);                                                          \
+            return static_fail(LCG_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(_e)); \
+        }                                                                                      \
     } while (0)
 
 extern "C" lcg_status lcg_align_score_static(const lcg_pair_tables *pair, const lcg_align_opts *opts,
@@ -247,14 +260,15 @@ extern "C" lcg_status lcg_align_score_static(const lcg_pair_tables *pair, const 
     STATIC_TRY(h2d(o_score, pair->am_score, 4ull * na));
     STATIC_TRY(h2d(o_D, p.Dinit.data(), 4ull * p.num_pos));
 
-    STATIC_TRY(launch_fill((const PairDev *)(base + o_pair), (const int2 *)(base + o_queue),
-                           (int)p.groups.size(), scratch, stride, sw, rb, fast,
-                           (unsigned int *)(base + o_ctrl), (int *)(base + o_ctrl + 4),
-                           (int *)(base + o_ctrl + 8), (int)blocks, s, nullptr));
+    STATIC_TRY_DRAIN(launch_fill((const PairDev *)(base + o_pair), (const int2 *)(base + o_queue),
+                                 (int)p.groups.size(), scratch, stride, sw, rb, fast,
+                                 (unsigned int *)(base + o_ctrl), (int *)(base + o_ctrl + 4),
+                                 (int *)(base + o_ctrl + 8), (int)blocks, s, nullptr),
+                     s);
     int ctrl[4] = {0, 0, 0, 0};
     int res[R_NWORDS] = {0};
-    STATIC_TRY(cudaMemcpyAsync(ctrl, base + o_ctrl, sizeof ctrl, cudaMemcpyDeviceToHost, s));
-    STATIC_TRY(cudaMemcpyAsync(res, base + o_res, sizeof res, cudaMemcpyDeviceToHost, s));
+    STATIC_TRY_DRAIN(cudaMemcpyAsync(ctrl, base + o_ctrl, sizeof ctrl, cudaMemcpyDeviceToHost, s), s);
+    STATIC_TRY_DRAIN(cudaMemcpyAsync(res, base + o_res, sizeof res, cudaMemcpyDeviceToHost, s), s);
     STATIC_TRY(cudaStreamSynchronize(s));
     if (ctrl[1] & ST_TIMEOUT) return static_fail(LCG_ERR_TIMEOUT, "a device wait for an arc-match entry timed out");
     if (ctrl[1]) return static_fail(LCG_ERR_DEVICE, "kernel reported an internal error");

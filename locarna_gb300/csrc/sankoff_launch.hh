@@ -1,5 +1,5 @@
 // Host-side entry points of the Sankoff kernels (sankoff_kernels.cu,
-// sankoff_sl_kernels.cu, microbench.cu) used by engine.cu and noalloc.cu.
+// sankoff_sl_kernels.cu) used by engine.cu and noalloc.cu.
 // sw: scratch row pitch (ints); rb: ring size of the shared-memory rows (a
 // multiple of 32 above the column span of any two consecutive band rows).
 #pragma once
@@ -32,5 +32,4 @@ cudaError_t launch_sl_fill(const PairDev *pairs, const int2 *queue, int nitems, 
                            int *abort_flag, int blocks, cudaStream_t st);
 cudaError_t launch_sl_trace(const PairDev *pairs, int npairs, int *scratch, long long scratch_stride, int sw,
                             int *status, cudaStream_t st, TraceSel sel = TraceSel());
-cudaError_t measure_int_peak(int sms, bool dpx, cudaStream_t st, double *gops);
 }  // namespace lcg

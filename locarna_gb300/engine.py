@@ -67,8 +67,6 @@ def _load_locked(path):
     lib.lcg_engine_set_counting.restype = C.c_int32
     lib.lcg_engine_last_work.argtypes = [C.c_void_p, C.POINTER(lcg_work_counts)]
     lib.lcg_engine_last_work.restype = C.c_int32
-    lib.lcg_measure_int_peak.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_double)]
-    lib.lcg_measure_int_peak.restype = C.c_int32
     lib.lcg_pf_opts_default.argtypes = [C.POINTER(lcg_pf_opts)]
     lib.lcg_pf_opts_default.restype = None
     lib.lcg_pf_forward.argtypes = [C.c_void_p, C.POINTER(lcg_pair_tables), C.c_int32, C.POINTER(lcg_pf_opts),
@@ -190,11 +188,6 @@ class Engine:
         w = lcg_work_counts()
         _check(self.lib, self.lib.lcg_engine_last_work(self.h, C.byref(w)))
         return dict(groups=w.groups, cells=w.cells, visits=w.arc_terms, arc_terms=w.valid_arc_terms)
-
-    def int_peak_gops(self, dpx=False):
-        g = C.c_double()
-        _check(self.lib, self.lib.lcg_measure_int_peak(self.h, int(bool(dpx)), C.byref(g)))
-        return g.value
 
     # ------------------------------------------------------------ LocARNA-P
 

@@ -7,8 +7,10 @@
 # Folding code (rna_ensemble.cc, mcc_matrices.cc, exact_matcher.cc) is left out:
 # PP inputs carry base-pair probabilities, so folding is never reached.
 set -euo pipefail
-REF=${LOCARNA_REF:-/root/reference}
 HERE=$(cd "$(dirname "$0")" && pwd)
+# the reference tree: $LOCARNA_REF, else a checkout named "reference" beside
+# the repository
+REF=${LOCARNA_REF:-$(cd "$HERE/../.." && pwd)/reference}
 OUT=$HERE/_ref
 SRC=$REF/src
 if [ ! -d "$SRC/LocARNA" ]; then

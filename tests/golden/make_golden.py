@@ -12,6 +12,7 @@ import json
 import os
 import subprocess
 import sys
+import tempfile
 
 import numpy as np
 
@@ -183,12 +184,11 @@ def make_case(name, spec, workdir):
 def main():
     if not os.path.exists(HARNESS):
         raise SystemExit("build the reference oracle first: oracle/build_ref.sh")
-    work = os.path.join(ROOT, "_work", "golden_pp")
-    os.makedirs(work, exist_ok=True)
     names = sys.argv[1:] or list(CASES)
-    for name in names:
-        ref = make_case(name, CASES[name], work)
-        print(name, "score", ref["score"], "am", ref["num_am"])
+    with tempfile.TemporaryDirectory(prefix="golden_pp_") as work:
+        for name in names:
+            ref = make_case(name, CASES[name], work)
+            print(name, "score", ref["score"], "am", ref["num_am"])
 
 
 if __name__ == "__main__" and not os.environ.get("LCG_GOLDEN_PF"):
@@ -258,10 +258,9 @@ def make_pf_case(name, spec, workdir):
 
 
 def main_pf():
-    work = os.path.join(ROOT, "_work", "golden_pp")
-    os.makedirs(work, exist_ok=True)
-    for name in sys.argv[1:] or list(PF_CASES):
-        print(name, *make_pf_case(name, PF_CASES[name], work))
+    with tempfile.TemporaryDirectory(prefix="golden_pp_") as work:
+        for name in sys.argv[1:] or list(PF_CASES):
+            print(name, *make_pf_case(name, PF_CASES[name], work))
 
 
 if __name__ == "__main__" and os.environ.get("LCG_GOLDEN_PF"):

@@ -2,14 +2,16 @@
 reference tree: a two-row alignment with two-line anchor names, #BPCUT,
 stacking columns and comment lines) through the host preparation and the
 oracle, against the reference's harness on the same file (CPU). Runs only
-where the reference tree and its compiled harness exist: set LOCARNA_REF to
-the reference tree (oracle/build_ref.sh builds the harness)."""
+where the reference tree and its compiled harness exist: $LOCARNA_REF or a
+checkout named "reference" beside the repository (oracle/build_ref.sh builds
+the harness)."""
 import os
 import subprocess
 
 import numpy as np
 import pytest
 
+from locarna_gb300.build import reference_tree
 from refdump import parse_ref
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -17,10 +19,9 @@ HARNESS = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
 
 
 def _example():
-    ref = os.environ.get("LOCARNA_REF")
-    path = os.path.join(ref, "Data", "Examples", "example.pp") if ref else None
-    if not path or not os.path.exists(path) or not os.path.exists(HARNESS):
-        pytest.skip("reference tree (LOCARNA_REF) or its harness not available")
+    path = os.path.join(reference_tree(), "Data", "Examples", "example.pp")
+    if not os.path.exists(path) or not os.path.exists(HARNESS):
+        pytest.skip("reference tree or its harness not available")
     return path
 
 
