@@ -9,20 +9,31 @@ the all-pairs workload; there is no public dataset involved.
 
 Metric: aligns/s (pairs aligned per second, whole job).
   value : pairs / device time of the kernels (inputs resident in HBM)
-  e2e   : pairs / wall time of the public C-ABI call lcg_align_pairs with
-          host tables in and host results out (all copies inside)
+  e2e   : pairs / wall time of the public C-ABI pipeline from PP texts to
+          alignments, as the locarna command line runs it: lcg_prepare_pairs
+          (parsing, scoring, arc matches, envelopes on the GPU) and
+          lcg_align_pairs (all copies inside)
 
---impl reference times the reference CPU implementation of the same path
-(the plain-C oracle restatement of the reference's Aligner, since the
-reference itself cannot be built on this host) on a bounded sample of the
-same workload with one process per host core.
+With N > 1 ranks (torchrun) the 2,016 pairs are split by estimated work
+(LPT over the host's cell counts, locarna_gb300/shard.py), every rank aligns
+its shard on its own GPU with no exchange, and value = 2,016 / the slowest
+rank's time.
+
+--impl reference times the CPU port of the reference's locarna pipeline
+(oracle/port_locarna: the host table preparation and the plain-C restatement
+of the reference's Aligner; the reference's own sources are not available
+where the bench runs, oracle/calibrate_port.py relates the two rates) from
+PP files, one process per pair over a pool of one worker per host core, as
+mlocarna runs locarna, on a bounded sample of the workload per step.
 """
 import argparse
 import json
 import multiprocessing as mp
 import os
+import random
 import subprocess
 import sys
+import tempfile
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -39,6 +50,12 @@ PF_WORKLOAD_NAME = "locarna_p_allpairs_128rnas_80-500nt"
 PF_BUCKET = 1024
 PF_STRIDE = 32  # the timed LocARNA-P sample: every PF_STRIDE-th pair in size order
 PF_CPU_SECONDS = 20.0
+REF_PAIRS_PER_CORE = 4  # pairs per host core in one step of the reference arm
+# DRAM traffic of the fill kernel per M cell, from the ncu capture of the
+# 496-pair case (profiles/sankoff_fill_small_496pairs.md: dram read + write
+# bytes of one launch / the launch's cells); the traffic of a launch of the
+# workload is this times its cells
+FILL_DRAM_BYTES_PER_CELL = 5.59e9 / 1.20e9
 
 
 def log(*a):
@@ -180,6 +197,54 @@ def cpu_sample(tables, budget_s, cores, seed=7, worker=None):
     done = sum(d for d, _ in res)
     rate = sum(d / t for d, t in res if t > 0)
     return done, rate
+
+
+def write_pp_files(pp, d):
+    paths = []
+    for k, text in enumerate(pp):
+        path = os.path.join(d, f"r{k}.pp")
+        with open(path, "w") as f:
+            f.write(text)
+        paths.append(path)
+    return paths
+
+
+def port_run(paths, pairs, sample, cores):
+    """The CPU port of `locarna A.pp B.pp` (oracle/_build/port_locarna) on
+    pairs[sample], one process per pair, `cores` processes at a time (as
+    mlocarna runs locarna). Returns (pairs done, wall seconds, scores)."""
+    from concurrent.futures import ThreadPoolExecutor
+    port = os.path.join(ROOT, "oracle", "_build", "port_locarna")
+
+    def one(k):
+        a, b = pairs[k]
+        r = subprocess.run([port], input=f"{paths[a]} {paths[b]}\n", capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"port_locarna failed on pair {k}: {r.stderr.strip()}")
+        return int(r.stdout.split()[0])
+
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(cores) as ex:
+        scores = list(ex.map(one, sample))
+    return len(sample), time.perf_counter() - t0, scores
+
+
+def port_baseline(pp, pairs, cores, budget_s, seed=7):
+    """Time-bounded CPU baseline: the port on seeded random pairs of the
+    workload, batches of `cores` pairs until budget_s is spent."""
+    rng = random.Random(seed)
+    order = list(range(len(pairs)))
+    rng.shuffle(order)
+    done, wall = 0, 0.0
+    with tempfile.TemporaryDirectory(prefix="lcg_pp_") as d:
+        paths = write_pp_files(pp, d)
+        for i in range(0, len(order), cores):
+            n, w, _ = port_run(paths, pairs, order[i:i + cores], cores)
+            done += n
+            wall += w
+            if wall >= budget_s:
+                break
+    return done, wall
 
 
 # ---------------------------------------------------------------- clocks
@@ -361,36 +426,85 @@ def run_pf(eng, tables, flush_l2, cpu):
 
 # ---------------------------------------------------------------- arms
 
+def dist_setup():
+    """(rank, world, local_rank); initialises torch.distributed for N > 1."""
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    return rank, world, local
+
+
+def barrier_sync(world):
+    import torch
+    torch.cuda.synchronize()
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+        torch.cuda.synchronize()
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch.distributed as dist
+    vals = [None] * world
+    dist.all_gather_object(vals, x)
+    return max(vals)
+
+
 def run_ours(args):
     import numpy as np
     from locarna_gb300.engine import Engine
+    from locarna_gb300.shard import lpt_partition, pair_weights, shard_loads
+    rank, world, local = dist_setup()
+    lead = rank == 0
+    extras = world == 1  # the secondary lines are measured at N = 1 only
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
         os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    pp, pairs = workload_pp()
     t0 = time.time()
-    tables, pairs = build_tables()
+    all_tables, _ = build_tables()
     host_prep_s = time.time() - t0
-    log(f"host preparation of {len(tables)} pairs: {host_prep_s:.1f} s")
+    if lead:
+        log(f"host preparation of {len(all_tables)} pairs: {host_prep_s:.1f} s")
+    # the pairs of this rank: LPT shards by the host's cell counts
+    weights = pair_weights(all_tables)
+    shards = lpt_partition(weights, world)
+    mine = shards[rank]
+    tables = [all_tables[k] for k in mine]
+    pp_pairs = [(pp[pairs[k][0]], pp[pairs[k][1]]) for k in mine]
+    npairs_total = len(all_tables)
     npairs = len(tables)
-    # CPU baseline first (forked workers must start before the first GPU call):
-    # the oracle restatement of the reference's Aligner on a bounded sample
     cores = os.cpu_count() or 1
-    cpu_done, cpu_rate = cpu_sample(tables, CPU_SAMPLE_SECONDS, cores)
-    log(f"cpu baseline: {cpu_done} pairs, {cpu_rate:.2f} aligns/s on {cores} cores")
+    cpu_rate, cpu_done = None, 0
     pf_tables, pf_cpu = None, None
-    if not args.no_pf:
-        t0 = time.time()
-        pf_tables = build_pf_tables()
-        log(f"host preparation of {len(pf_tables)} LocARNA-P pairs: {time.time() - t0:.1f} s")
-        pf_done, pf_rate = cpu_sample(pf_tables, PF_CPU_SECONDS, cores, seed=9, worker=_cpu_pf_worker)
-        log(f"cpu baseline LocARNA-P: {pf_done} pairs, {pf_rate:.3f} pairs/s on {cores} cores")
-        pf_cpu = {"value": pf_rate, "unit": "pairs/s", "cores": cores, "kind": "port",
-                  "sample": f"{pf_done} of the {len(pf_tables)} pairs (seeded permutation), one process per "
-                            f"core, {PF_CPU_SECONDS:.0f} s per process; the oracle restatement of AlignerP "
-                            f"(inside, outside, arc-match and base-match probabilities)"}
-    eng = Engine(0)
-    table_prep = table_prep_gpu(eng, tables, host_prep_s)
-    log(f"table preparation with GPU envelopes: {table_prep['gpu_envelope_s']:.2f} s "
-        f"({table_prep['host_envelopes']} host envelopes)")
+    if extras:
+        # CPU baselines before the first GPU call (forked pools): the CPU
+        # port of the locarna pipeline on a bounded sample
+        cpu_done, cpu_wall = port_baseline(pp, pairs, cores, CPU_SAMPLE_SECONDS)
+        cpu_rate = cpu_done / cpu_wall
+        log(f"cpu baseline: {cpu_done} pairs, {cpu_rate:.2f} aligns/s on {cores} cores")
+        if not args.no_pf:
+            t0 = time.time()
+            pf_tables = build_pf_tables()
+            log(f"host preparation of {len(pf_tables)} LocARNA-P pairs: {time.time() - t0:.1f} s")
+            pf_done, pf_rate = cpu_sample(pf_tables, PF_CPU_SECONDS, cores, seed=9, worker=_cpu_pf_worker)
+            log(f"cpu baseline LocARNA-P: {pf_done} pairs, {pf_rate:.3f} pairs/s on {cores} cores")
+            pf_cpu = {"value": pf_rate, "unit": "pairs/s", "cores": cores, "kind": "port",
+                      "sample": f"{pf_done} of the {len(pf_tables)} pairs (seeded permutation), one process "
+                                f"per core, {PF_CPU_SECONDS:.0f} s per process; the oracle restatement of "
+                                f"AlignerP (inside, outside, arc-match and base-match probabilities)"}
+    eng = Engine(local)
+    table_prep = None
+    if extras:
+        table_prep = table_prep_gpu(eng, all_tables, host_prep_s)
+        log(f"table preparation with GPU envelopes: {table_prep['gpu_envelope_s']:.2f} s "
+            f"({table_prep['host_envelopes']} host envelopes)")
     call = eng.prepare_call(tables)
 
     # measurement-only runs (outside the timed region): work counts
@@ -398,31 +512,26 @@ def run_ours(args):
     eng.run_call(call)
     work = eng.last_work()
     eng.set_counting(False)
-    int_peak = max(int_peak_gops(False), int_peak_gops(True))
+    int_peak = max(int_peak_gops(False, local), int_peak_gops(True, local))
 
     # L2 flush buffer (larger than the 129 MB L2)
-    flush = None
-    try:
-        import torch
-        flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.int32, device="cuda:0")
-    except Exception:
-        flush = None
+    import torch
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.int32, device=f"cuda:{local}")
 
     def flush_l2():
-        if flush is not None:
-            flush.fill_(1)
-            import torch
-            torch.cuda.synchronize()
+        flush.fill_(1)
+        torch.cuda.synchronize()
 
-    sampler = ClockSampler()
-    sampler.start()
-    # device time: the whole batch as one chunk (one fill + one traceback
-    # launch over inputs already resident in HBM)
+    sampler = ClockSampler() if lead else None
+    if sampler:
+        sampler.start()
+    # device time: the shard as one chunk (one fill + one traceback launch over
+    # inputs already resident in HBM); the slowest rank sets the step time
     eng.set_chunk_pairs(npairs)
     for _ in range(args.warmup):
         eng.run_call(call)
-    kern_ms, fill_ms = 0.0, 0.0
-    launches = 0
+    kern_ms, fill_ms, launches = 0.0, 0.0, 0
+    barrier_sync(world)
     for _ in range(args.steps):
         flush_l2()
         eng.run_call(call)
@@ -431,35 +540,116 @@ def run_ours(args):
         kern_ms += ms
         fill_ms += f
         launches += nl
+    barrier_sync(world)
     res_one = Engine.decode_call(call)
-    # end to end: the public call with its default chunk pipeline (host
-    # preparation of chunk k+1 overlaps the device work of chunk k)
+    # end to end: PP texts in, alignments out through the public pipeline,
+    # lcg_prepare_pairs (envelopes on the GPU) + lcg_align_pairs with its
+    # default chunk pipeline
+    from locarna_gb300.prep import prepare_pairs
     eng.set_chunk_pairs(0)
     for _ in range(max(1, args.warmup // 2)):
-        eng.run_call(call)
-    wall_s = 0.0
+        t_e, _ = prepare_pairs(eng, pp_pairs)
+        res = eng.align_pairs(t_e)
+    wall_s, prep_s = 0.0, 0.0
     phases = [0.0, 0.0, 0.0, 0.0]
     e2e_launches = 0
+    barrier_sync(world)
     for _ in range(args.steps):
         flush_l2()
         s0 = time.perf_counter()
-        eng.run_call(call)  # synchronises inside (results are on the host)
+        t_e, _ = prepare_pairs(eng, pp_pairs)
+        s1 = time.perf_counter()
+        res = eng.align_pairs(t_e)  # synchronises inside (results are on the host)
         wall_s += time.perf_counter() - s0
+        prep_s += s1 - s0
         phases = [a + b for a, b in zip(phases, eng.last_phases())]
-        e2e_launches += eng.last_stats()[1]
-    clocks = sampler.stop()
+        e2e_launches += eng.last_stats()[1] + 1  # + the envelope launch
+    barrier_sync(world)
+    clocks = sampler.stop() if sampler else None
     h2d, d2h = eng.last_transfer()
-    res = Engine.decode_call(call)
+    ph2d, pd2h = eng.last_prep_transfer()
     for k in range(npairs):
         if (res[k].score, res[k].edges) != (res_one[k].score, res_one[k].edges):
-            raise RuntimeError(f"pair {k}: pipelined call differs from the one-chunk call")
-    # spot check: the first pairs against the oracle
+            raise RuntimeError(f"pair {mine[k]}: the end-to-end pipeline differs from the one-chunk call")
+    # spot check against the oracle
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     from checks import assert_same_result
     from oracle_ffi import oracle_align
     for k in range(0, npairs, max(1, npairs // 6)):
-        assert_same_result(res[k], oracle_align(tables[k]), f"pair {k}")
+        assert_same_result(res[k], oracle_align(tables[k]), f"pair {mine[k]}")
 
+    T = max_over_ranks(kern_ms / 1e3 / args.steps, world)
+    Tf_mine = fill_ms / 1e3 / args.steps
+    We = max_over_ranks(wall_s / args.steps, world)
+    if not lead:
+        eng.close()
+        return
+    value = npairs_total / T
+    Tf = Tf_mine
+    ops = 10 * work["cells"] + 2 * max(work["arc_terms"], 0)
+    alg_bytes = h2d + d2h  # every input table read once, every result written once
+    out = {
+        "metric": "aligns/s (Sankoff all-pairs, bit-exact score+traceback)",
+        "value": value,
+        "unit": "aligns/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": T * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "int32",
+        "data": "synthetic (seeded PP inputs, locarna_gb300/synth.py)",
+        "config": {"workload": WORKLOAD_NAME, "pairs": npairs_total, "rnas": WORKLOAD["count"],
+                   "len_range": [WORKLOAD["len_lo"], WORKLOAD["len_hi"]], "seed": WORKLOAD["seed"],
+                   "mode": "global, default locarna scoring, envelope 1e-4",
+                   "parallelism": f"pairs sharded over {world} GPU(s) by LPT of the host cell counts",
+                   "shard_cells": shard_loads(weights, shards),
+                   "l2": "flushed between steps (256 MB write)"},
+        "gcups": sum(weights) / T / 1e9,
+        "e2e": {"value": npairs_total / We, "unit": "aligns/s", "h2d_bytes_per_step": h2d + ph2d,
+                "d2h_bytes_per_step": d2h + pd2h, "ms_per_step": We * 1e3,
+                "what": "PP texts -> alignments: lcg_prepare_pairs (parsing, scoring, arc matches, GPU "
+                        "envelopes) + lcg_align_pairs (default chunk pipeline), all copies inside",
+                "table_prep_ms_per_step": prep_s / args.steps * 1e3,
+                "gpu_launches": e2e_launches,
+                "align_phases_ms_per_step": dict(zip(("host_prep", "pack", "host_waits_for_device", "results"),
+                                                     (x / args.steps for x in phases)))},
+        "gpu_launches": launches,
+        "roofline": {"bound": "int32", "kernel": "sankoff_fill_kernel",
+                     "achieved": ops / Tf / 1e9, "peak": int_peak, "unit": "Gops/s",
+                     "frac": ops / Tf / 1e9 / int_peak,
+                     "traffic": FILL_DRAM_BYTES_PER_CELL * work["cells"],
+                     "traffic_note": "DRAM read + write bytes per launch: bytes per cell of the ncu capture of "
+                                     "the 496-pair case times this launch's cells",
+                     "ops_per_launch": ops, "fill_ms": Tf * 1e3,
+                     "peak_source": "measured int32 add+max rate (locarna_gb300/_build/liblcg_probe.so)",
+                     "hbm_frac_of_measured": alg_bytes / Tf / 1e9 / peaks.get("hbm_gbs", 6800.0)},
+        "int_ops": {"ops_per_step": ops, "cells": work["cells"], "arc_terms": work["arc_terms"],
+                    "groups": work["groups"]},
+        "clocks": clocks,
+    }
+    if extras:
+        out["cpu_baseline"] = {"value": cpu_rate, "unit": "aligns/s", "cores": cores, "kind": "port",
+                               "sample": f"{cpu_done} random workload pairs, PP files to alignments by "
+                                         f"oracle/_build/port_locarna, one process per pair, {cores} at a time, "
+                                         f"~{CPU_SAMPLE_SECONDS:.0f} s"}
+        out.update(run_extras(args, eng, tables, flush_l2, value, table_prep))
+        if pf_tables is not None:
+            out["locarna_p"] = run_pf(eng, pf_tables, flush_l2, pf_cpu)
+    print(json.dumps(out), flush=True)
+    eng.close()
+
+
+def run_extras(args, eng, tables, flush_l2, value, table_prep):
+    """Secondary lines at N = 1: one pair alone (global and structure-local),
+    the workload one pair per call, --noLP, the local alignment modes."""
+    from locarna_gb300.engine import Engine
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from checks import assert_same_result
+    from oracle_ffi import oracle_align
+    npairs = len(tables)
     # per-pair: the 400 x 400 pair alone, and the workload one pair per call
     pt = per_pair_tables()
     pcall = eng.prepare_call([pt])
@@ -514,97 +704,62 @@ def run_ours(args):
     nres = Engine.decode_call(ncall)
     for k in range(0, npairs, max(1, npairs // 6)):
         assert_same_result(nres[k], oracle_align(tables[k], no_lonely_pairs=True), f"pair {k} (noLP)")
-    nolp = {"mode": "global, --noLP (no lonely pairs)", "pairs": npairs,
-            "aligns_per_s": npairs / (sum(nolp_ms) / len(nolp_ms) / 1e3),
-            "e2e_aligns_per_s": npairs / (sum(nolp_wall) / len(nolp_wall)),
-            "stacked_arc_matches_traced": sum(len(r.traced_am) for r in nres)}
-
-    modes = run_modes(eng, tables, flush_l2)
-
-    T = kern_ms / 1e3 / args.steps
-    Tf = fill_ms / 1e3 / args.steps
-    We = wall_s / args.steps
-    value = npairs / T
-    ops = 10 * work["cells"] + 2 * max(work["arc_terms"], 0)
-    hbm_peak = peaks.get("hbm_gbs", 6800.0)
-    alg_bytes = h2d + d2h  # every input table read once, every result written once
-    out = {
-        "metric": "aligns/s (Sankoff all-pairs, bit-exact score+traceback)",
-        "value": value,
-        "unit": "aligns/s",
-        "n_gpus": 1,
-        "steps": args.steps,
-        "warmup": args.warmup,
-        "ms_per_step": T * 1e3,
-        "higher_is_better": True,
-        "scaling": "weak",
-        "vs_baseline": None,
-        "dtype": "int32",
-        "data": "synthetic (seeded PP inputs, locarna_gb300/synth.py)",
-        "config": {"workload": WORKLOAD_NAME, "pairs": npairs, "rnas": WORKLOAD["count"],
-                   "len_range": [WORKLOAD["len_lo"], WORKLOAD["len_hi"]], "seed": WORKLOAD["seed"],
-                   "mode": "global, default locarna scoring, envelope 1e-4",
-                   "l2": "flushed between steps (256 MB write)"},
-        "gcups": work["cells"] / T / 1e9,
-        "e2e": {"value": npairs / We, "unit": "aligns/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h, "ms_per_step": We * 1e3,
-                "chunks_per_step": e2e_launches // (2 * args.steps),
-                "gpu_launches": e2e_launches,
-                "phases_ms_per_step": dict(zip(("host_prep", "pack", "host_waits_for_device", "results"),
-                                               (x / args.steps for x in phases)))},
-        "gpu_launches": launches,
-        "roofline": {"bound": "hbm", "achieved": alg_bytes / Tf / 1e9, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": alg_bytes / Tf / 1e9 / hbm_peak, "traffic": None,
-                     "note": "dominant kernel sankoff_fill_kernel; integer/latency bound, see int_ops"},
-        "int_ops": {"ops_per_step": ops, "achieved_gops": ops / Tf / 1e9, "peak_gops": int_peak,
-                    "frac": ops / Tf / 1e9 / int_peak, "cells": work["cells"],
-                    "arc_terms": work["arc_terms"], "groups": work["groups"]},
+    return {
         "per_pair": {"workload": "one 400x400 nt pair, global", "device_ms": single_ms[len(single_ms) // 2],
                      "aligns_per_s": 1e3 / single_ms[len(single_ms) // 2],
                      "struct_local_device_ms": sl_ms[len(sl_ms) // 2],
                      "per_pair_launch_aligns_per_s_device": len(sample) / (dev_ms_single / 1e3),
                      "per_pair_launch_aligns_per_s_wall": len(sample) / wall_single,
                      "batched_over_per_pair_launch": value / (len(sample) / (dev_ms_single / 1e3))},
-        "cpu_baseline": {"value": cpu_rate, "unit": "aligns/s", "cores": cores, "kind": "port",
-                         "sample": f"{cpu_done} of the {npairs} pairs (seeded permutation), one process "
-                                   f"per core, {CPU_SAMPLE_SECONDS:.0f} s per process"},
-        "clocks": clocks,
         "table_prep": table_prep,
-        "nolp": nolp,
-        "modes": modes,
+        "nolp": {"mode": "global, --noLP (no lonely pairs)", "pairs": npairs,
+                 "aligns_per_s": npairs / (sum(nolp_ms) / len(nolp_ms) / 1e3),
+                 "e2e_aligns_per_s": npairs / (sum(nolp_wall) / len(nolp_wall)),
+                 "stacked_arc_matches_traced": sum(len(r.traced_am) for r in nres)},
+        "modes": run_modes(eng, tables, flush_l2),
     }
-    if pf_tables is not None:
-        out["locarna_p"] = run_pf(eng, pf_tables, flush_l2, pf_cpu)
-    print(json.dumps(out), flush=True)
-    eng.close()
 
 
 def run_reference(args):
+    """The reference arm: the CPU port of the locarna pipeline (PP files in,
+    alignments out; oracle/port_locarna) on the machine's host cores, one process
+    per pair over a pool of one worker per core. Each step aligns a seeded
+    random sample of REF_PAIRS_PER_CORE x cores workload pairs; value = the
+    pairs of the timed steps / their measured wall time. Rank 0 only."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    t0 = time.time()
-    tables, pairs = build_tables()
-    log(f"host preparation of {len(tables)} pairs: {time.time() - t0:.1f} s")
+    from locarna_gb300.build import build_oracle
+    build_oracle()
+    pp, pairs = workload_pp()
     cores = os.cpu_count() or 1
-    budget = max(2.0, 60.0 / max(1, args.steps + args.warmup))
-    vals, dones = [], []
-    for s in range(args.warmup + args.steps):
-        done, rate = cpu_sample(tables, budget, cores, seed=7 + s)
-        if s >= args.warmup:
-            vals.append(rate)
-            dones.append(done)
-    v = sum(vals) / len(vals)
+    per_step = REF_PAIRS_PER_CORE * cores
+    rng = random.Random(11)
+    walls, dones = [], []
+    with tempfile.TemporaryDirectory(prefix="lcg_pp_") as d:
+        paths = write_pp_files(pp, d)
+        for s in range(args.warmup + args.steps):
+            sample = rng.sample(range(len(pairs)), min(per_step, len(pairs)))
+            n, wall, _ = port_run(paths, pairs, sample, cores)
+            if s >= args.warmup:
+                walls.append(wall)
+                dones.append(n)
+    v = sum(dones) / sum(walls)
     out = {
         "metric": "aligns/s (Sankoff all-pairs, bit-exact score+traceback)",
         "value": v, "unit": "aligns/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1e3 * len(tables) / v, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "int64", "data": "synthetic (seeded PP inputs)",
+        "ms_per_step": 1e3 * sum(walls) / len(walls), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int64", "data": "synthetic (seeded PP inputs, locarna_gb300/synth.py)",
         "impl": "reference",
-        "config": {"workload": WORKLOAD_NAME, "pairs": len(tables)},
+        "config": {"workload": WORKLOAD_NAME, "pairs": len(pairs), "rnas": WORKLOAD["count"],
+                   "len_range": [WORKLOAD["len_lo"], WORKLOAD["len_hi"]], "seed": WORKLOAD["seed"],
+                   "mode": "global, default locarna scoring, envelope 1e-4"},
         "cpu_baseline": {"value": v, "unit": "aligns/s", "cores": cores, "kind": "port",
-                         "sample": f"~{sum(dones) // len(dones)} pairs per step of the {len(tables)} "
-                                   f"(time-bounded {budget:.0f} s per process), one process per core"},
+                         "sample": f"{per_step} random workload pairs per step ({REF_PAIRS_PER_CORE} per core), "
+                                   f"PP files to alignments by oracle/_build/port_locarna (host table "
+                                   f"preparation + the C restatement of the reference's Aligner), one process "
+                                   f"per pair, {cores} at a time; oracle/calibrate_port.py relates its rate "
+                                   f"to the reference's locarna"},
         "e2e": {"value": v, "unit": "aligns/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(out), flush=True)
@@ -673,12 +828,10 @@ def main():
     if args.impl == "reference":
         run_reference(args)
         return
-    if int(os.environ.get("WORLD_SIZE", "1")) > 1 and int(os.environ.get("RANK", "0")) != 0:
-        # pairs shard with no exchange; this build measures one GPU
-        return
-    from locarna_gb300.build import build_engine, build_oracle
+    from locarna_gb300.build import build_engine, build_oracle, build_probe
     build_engine()
     build_oracle()
+    build_probe()
     if args.case in ("small", "large"):
         run_small_case(args)
         return

@@ -245,6 +245,16 @@ lcg_status lcg_engine_last_transfer(lcg_engine eng, int64_t *h2d_bytes,
 lcg_status lcg_engine_set_counting(lcg_engine eng, int32_t on);
 lcg_status lcg_engine_last_work(lcg_engine eng, lcg_work_counts *out);
 
+/* Work of one pair before it is aligned, on the host (no GPU): the left-end
+ * groups of align_D (aligner.cc:660-732) and the M cells of their rectangles
+ * plus the top level, as lcg_engine_last_work counts them; arc_terms = the
+ * arc matches whose right ends are band cells (the D entries);
+ * valid_arc_terms = -1. Validates the tables like lcg_align_pairs. The
+ * estimate by which a batch is split across GPUs (the reference's mlocarna
+ * splits its pair list over processes, src/Utils/mlocarna:3547-3625). */
+lcg_status lcg_pair_work(const lcg_pair_tables *pair, const lcg_align_opts *opts,
+                         lcg_work_counts *out);
+
 
 /* --------------------------------------------- LocARNA-P forward/backward
  *

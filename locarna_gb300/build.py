@@ -105,6 +105,15 @@ def build_oracle():
     s = os.path.join(ORACLE, "pf_oracle.c")
     if _newer(lib, [s, hdr]):
         _run(["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-ffp-contract=off", s, "-o", lib, "-lm"])
+    # the CPU port of the locarna pipeline (host table preparation + the C
+    # restatement), timed by bench.py's reference arm
+    port = os.path.join(out, "port_locarna")
+    psrc = [os.path.join(ORACLE, "port_locarna.cc"), os.path.join(ORACLE, "prep_link.cc"),
+            os.path.join(CSRC, "host_prep.cpp")]
+    deps = psrc + [hdr, os.path.join(CSRC, "envelope.hh"), os.path.join(CSRC, "ribosum85_60.inc"), srcs[0]]
+    if _newer(port, deps):
+        _run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-I", os.path.join(ROOT, "include")] + psrc +
+             [os.path.join(out, "sankoff_oracle.o"), "-o", port, "-lpthread", "-lm"])
     return os.path.join(out, "liboracle.so")
 
 

@@ -1101,6 +1101,13 @@ lcg_status lcg_engine_last_transfer(lcg_engine e, int64_t *h2d_bytes, int64_t *d
     return LCG_OK;
 }
 
+lcg_status lcg_engine_last_prep_transfer(lcg_engine e, int64_t *h2d_bytes, int64_t *d2h_bytes) {
+    if (!e || !h2d_bytes || !d2h_bytes) return fail(LCG_ERR_ARG, "NULL argument");
+    *h2d_bytes = e->prep_h2d;
+    *d2h_bytes = e->prep_d2h;
+    return LCG_OK;
+}
+
 lcg_status lcg_engine_last_timing(lcg_engine e, double *fill_ms, double *trace_ms) {
     if (!e) return fail(LCG_ERR_ARG, "engine is NULL");
     if (fill_ms) *fill_ms = e->last_fill_ms;
@@ -1120,6 +1127,17 @@ lcg_status lcg_engine_last_work(lcg_engine e, lcg_work_counts *w) {
     w->cells = e->last_cells;
     w->arc_terms = e->last_visits;
     w->valid_arc_terms = e->last_terms;
+    return LCG_OK;
+}
+
+lcg_status lcg_pair_work(const lcg_pair_tables *pair, const lcg_align_opts *opts, lcg_work_counts *out) {
+    if (!pair || !opts || !out) return fail(LCG_ERR_ARG, "NULL argument");
+    lcg_host::Prep p;
+    if (lcg_host::prep_pair(*pair, *opts, p) != LCG_OK) return fail(p.code, p.err);
+    out->groups = (long long)p.groups.size() - 1;  // without the top level
+    out->cells = p.cells;
+    out->arc_terms = p.num_pos;  // arc matches whose right ends are band cells
+    out->valid_arc_terms = -1;
     return LCG_OK;
 }
 

@@ -50,6 +50,8 @@ struct lcg_engine_s {
     size_t env_dev_cap = 0;
     char *env_host = nullptr;
     size_t env_host_cap = 0;
+    // bytes the last lcg_prepare_pairs call copied host->device / device->host
+    long long prep_h2d = 0, prep_d2h = 0;
 };
 
 namespace lcg_host {

@@ -314,6 +314,11 @@ size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
 
 namespace lcg_env {
 
+void reset_transfer(lcg_engine eng) {
+    eng->prep_h2d = 0;
+    eng->prep_d2h = 0;
+}
+
 lcg_status compute(lcg_engine eng, const Params &Pm, int npairs, const PairIn *in, PairOut *out, std::string &err) {
     if (npairs <= 0) return LCG_OK;
     cudaError_t ce = cudaSetDevice(eng->device);
@@ -451,6 +456,8 @@ lcg_status compute(lcg_engine eng, const Params &Pm, int npairs, const PairIn *i
             cudaSuccess)
             return fail_cuda(ce, "envelope download");
         if ((ce = cudaStreamSynchronize(st)) != cudaSuccess) return fail_cuda(ce, "envelope kernel");
+        eng->prep_h2d += (long long)out_begin;
+        eng->prep_d2h += (long long)(out_end - out_begin);
         for (int k = 0; k < nq; ++k) {
             const int n1 = in[q0 + k].n + 1;
             const int *o = (const int *)(H + out_off[k]);

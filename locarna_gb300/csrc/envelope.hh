@@ -49,4 +49,8 @@ struct PairOut {
 // pair). Returns LCG_OK or an error with err set.
 lcg_status compute(lcg_engine eng, const Params &P, int npairs, const PairIn *in, PairOut *out, std::string &err);
 
+// Zero the engine's count of the bytes a table preparation copied (at the
+// start of each lcg_prepare_pairs call; compute() adds to it).
+void reset_transfer(lcg_engine eng);
+
 }  // namespace lcg_env

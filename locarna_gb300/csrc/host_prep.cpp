@@ -1121,6 +1121,7 @@ lcg_status lcg_prepare_pairs(lcg_engine eng, const char *const *pp_a, const char
         return LCG_ERR_ARG;
     }
     if (host_envelopes) *host_envelopes = 0;
+    lcg_env::reset_transfer(eng);
     for (int q = 0; q < npairs; ++q) out[q] = nullptr;
     if (npairs == 0) return LCG_OK;
     lcg_prep_opts o;

@@ -61,12 +61,16 @@ def _load_locked(path):
     lib.lcg_engine_last_phases.restype = C.c_int32
     lib.lcg_engine_last_transfer.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
     lib.lcg_engine_last_transfer.restype = C.c_int32
+    lib.lcg_engine_last_prep_transfer.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
+    lib.lcg_engine_last_prep_transfer.restype = C.c_int32
     lib.lcg_engine_set_chunk_pairs.argtypes = [C.c_void_p, C.c_int32]
     lib.lcg_engine_set_chunk_pairs.restype = C.c_int32
     lib.lcg_engine_set_counting.argtypes = [C.c_void_p, C.c_int32]
     lib.lcg_engine_set_counting.restype = C.c_int32
     lib.lcg_engine_last_work.argtypes = [C.c_void_p, C.POINTER(lcg_work_counts)]
     lib.lcg_engine_last_work.restype = C.c_int32
+    lib.lcg_pair_work.argtypes = [C.POINTER(lcg_pair_tables), C.POINTER(lcg_align_opts), C.POINTER(lcg_work_counts)]
+    lib.lcg_pair_work.restype = C.c_int32
     lib.lcg_pf_opts_default.argtypes = [C.POINTER(lcg_pf_opts)]
     lib.lcg_pf_opts_default.restype = None
     lib.lcg_pf_forward.argtypes = [C.c_void_p, C.POINTER(lcg_pair_tables), C.c_int32, C.POINTER(lcg_pf_opts),
@@ -83,6 +87,16 @@ def _load_locked(path):
 def _check(lib, rc):
     if rc != 0:
         raise LcgError(rc, lib.lcg_last_error().decode())
+
+
+def pair_work(tables, **kw):
+    """lcg_pair_work: (groups, cells, D entries) of one pair, on the host."""
+    lib = load_library()
+    o = make_opts(**kw)
+    w = lcg_work_counts()
+    ct = tables.to_c()
+    _check(lib, lib.lcg_pair_work(C.byref(ct), C.byref(o), C.byref(w)))
+    return w.groups, w.cells, w.arc_terms
 
 
 class Engine:
@@ -175,6 +189,11 @@ class Engine:
     def last_transfer(self):
         a, b = C.c_int64(), C.c_int64()
         _check(self.lib, self.lib.lcg_engine_last_transfer(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def last_prep_transfer(self):
+        a, b = C.c_int64(), C.c_int64()
+        _check(self.lib, self.lib.lcg_engine_last_prep_transfer(self.h, C.byref(a), C.byref(b)))
         return a.value, b.value
 
     def set_chunk_pairs(self, n):

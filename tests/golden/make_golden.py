@@ -43,6 +43,7 @@ CASES = {
     "c60_short": (60, 41, 70, 42, {}, True),
     "c200_global": (200, 5, 200, 6, {}, True),
     "c400_global": (400, 3, 400, 4, {}, True),
+    "c400_structlocal": (400, 3, 400, 4, {"struct_local": "1"}, True),
     # locarna --noLP: no lonely base pairs in the aligned structure
     "c150_nolp": (150, 1, 150, 2, {"no_lonely_pairs": "1"}, True),
     "c150_nolp_b": (150, 11, 140, 12, {"no_lonely_pairs": "1"}, True),

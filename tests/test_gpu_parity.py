@@ -34,6 +34,34 @@ def test_gpu_batch_matches_oracle(engine):
 
 
 @pytest.mark.gpu
+def test_gpu_allpairs_workload_sample_matches_oracle(engine):
+    """The all-pairs workload itself (64 RNAs of 60-400 nt, seed 2024, the
+    benchmark's family): a length-stratified sample of 202 of its 2,016 pairs
+    (every 10th pair in order of lenA x lenB) aligned in one lcg_align_pairs
+    call, every pair equal to the oracle: score, end cells, raw traceback
+    edges and traced arc matches."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    import bench
+    from locarna_gb300.prep import prepare_pair
+    from oracle_pool import oracle_align_many
+    pp, pairs = bench.workload_pp()
+    from locarna_gb300.synth import make_family
+    W = bench.WORKLOAD
+    fam = make_family(W["count"], W["len_lo"], W["len_hi"], W["seed"], q=W["q"])
+    lens = [len(r.seq) for r in fam]
+    order = sorted(range(len(pairs)), key=lambda k: (lens[pairs[k][0]] * lens[pairs[k][1]], k))
+    sample = [pairs[k] for k in order[::10]]
+    assert len(sample) >= 200
+    with ThreadPoolExecutor(8) as ex:
+        tables = list(ex.map(lambda ab: prepare_pair(pp[ab[0]], pp[ab[1]]), sample))
+    got = engine.align_pairs(tables)
+    ref = oracle_align_many(tables)
+    for k, (r, o) in enumerate(zip(got, ref)):
+        assert_same_result(r, o, f"workload pair {sample[k]}")
+
+
+@pytest.mark.gpu
 def test_gpu_chunk_pipeline_matches_oracle(engine):
     """lcg_align_pairs' chunk pipeline (two buffer sets, host preparation of
     chunk k+1 during the device work of chunk k): automatic chunks for a
