@@ -149,14 +149,18 @@ extern "C" lcg_status lcg_align_score_static(const lcg_pair_tables *pair, const 
     const size_t o_top = take(4ull * (n + 1) * (m + 1));
     const size_t fixed = off;
     const long long stride = (long long)rows_max * sw;  // ints per warp slot
+    const size_t per_block = (size_t)fill_warps_per_block() * (size_t)stride * sizeof(int);
+    if (fixed + per_block > LCG_STATIC_SCRATCH_BYTES)
+        return static_fail(LCG_ERR_RANGE, "pair too large for the static scratch of the allocation-free entry point: needs " +
+                                              std::to_string(fixed + per_block) + " bytes, limit " +
+                                              std::to_string((size_t)LCG_STATIC_SCRATCH_BYTES));
     int blocks_per_sm = 0;
     const int rb = lcg_host::ring_size(p.span);
     const bool fast = (p.flags & PF_SCLS) && !(p.flags & (PF_ANCHORS | PF_NOLP | PF_STACK));
     STATIC_TRY(fill_occupancy(rb, false, fast, &blocks_per_sm));
     int sms = 0;
     STATIC_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    const size_t per_block = (size_t)fill_warps_per_block() * (size_t)stride * sizeof(int);
-    const size_t room = fixed < LCG_STATIC_SCRATCH_BYTES ? LCG_STATIC_SCRATCH_BYTES - fixed : 0;
+    const size_t room = LCG_STATIC_SCRATCH_BYTES - fixed;
     long long blocks = std::min<long long>((long long)sms * std::max(blocks_per_sm, 1), (long long)(room / per_block));
     if (blocks_per_sm < 1 || blocks < 1)
         return static_fail(LCG_ERR_RANGE, "pair too large for the static scratch of the allocation-free entry point: needs " +

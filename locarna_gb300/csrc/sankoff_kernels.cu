@@ -230,6 +230,14 @@ int trace_warps_per_block() { return TRACE_WARPS; }
 
 cudaError_t fill_occupancy(int rb, bool counting, bool fast, int *blocks_per_sm) {
     size_t smem = (size_t)FILL_WARPS * smem_warp_ints(rb) * sizeof(int);
+    int dev = 0, optin = 0;
+    cudaError_t ge = cudaGetDevice(&dev);
+    if (ge == cudaSuccess) ge = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (ge != cudaSuccess) return ge;
+    if (smem > (size_t)optin) {  // band rows too wide for the shared-memory rings
+        *blocks_per_sm = 0;
+        return cudaSuccess;
+    }
     const void *k = counting ? (fast ? fill_fn<true, true>() : fill_fn<true, false>())
                              : (fast ? fill_fn<false, true>() : fill_fn<false, false>());
     if (smem > 48 * 1024) {
