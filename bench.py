@@ -353,7 +353,7 @@ def run_pf(eng, tables, flush_l2, cpu):
     sample = order[::PF_STRIDE]
     buckets = [sample[i:i + PF_BUCKET] for i in range(0, len(sample), PF_BUCKET)]
     for prec in (64, 32):  # warm-up: the smallest bucket
-        eng.pf_forward([tables[k] for k in buckets[0]], precision=prec)
+        eng.pf_forward([tables[k] for k in buckets[0]], precision=prec, min_am_prob=0.0)
         eng.pf_backward(probs=False)
     dev = {64: 0.0, 32: 0.0}
     wall = {64: 0.0, 32: 0.0}
@@ -365,7 +365,7 @@ def run_pf(eng, tables, flush_l2, cpu):
         for prec in (64, 32):
             flush_l2()
             t0 = time.perf_counter()
-            eng.pf_forward(tb, precision=prec)
+            eng.pf_forward(tb, precision=prec, min_am_prob=0.0)
             r = eng.pf_backward(probs=True)
             wall[prec] += time.perf_counter() - t0
             f, bw = eng.pf_last_timing()
@@ -545,26 +545,45 @@ def run_ours(args):
     # end to end: PP texts in, alignments out through the public pipeline,
     # lcg_prepare_pairs (envelopes on the GPU) + lcg_align_pairs with its
     # default chunk pipeline
-    from locarna_gb300.prep import prepare_pairs
+    import ctypes as C
+
+    from locarna_gb300.abi import ResultBuffers, lcg_align_result, make_opts
+    from locarna_gb300.prep import prepare_pairs_batch
     eng.set_chunk_pairs(0)
+    # caller-owned result buffers, allocated once (as a caller of the C ABI would)
+    bufs = [ResultBuffers(t.len_a, t.len_b) for t in tables]
+    cres = (lcg_align_result * npairs)(*[b.c for b in bufs])
+    copts = make_opts()
+
+    def e2e_step():
+        s0 = time.perf_counter()
+        batch = prepare_pairs_batch(eng, pp_pairs)
+        s1 = time.perf_counter()
+        rc = eng.lib.lcg_align_pairs(eng.h, batch.c_tables(), npairs, C.byref(copts), cres)
+        s2 = time.perf_counter()
+        if rc != 0:
+            raise RuntimeError(eng.lib.lcg_last_error().decode())
+        batch.close()
+        return s2 - s0, s1 - s0
+
     for _ in range(max(1, args.warmup // 2)):
-        t_e, _ = prepare_pairs(eng, pp_pairs)
-        res = eng.align_pairs(t_e)
+        e2e_step()
     wall_s, prep_s = 0.0, 0.0
     phases = [0.0, 0.0, 0.0, 0.0]
     e2e_launches = 0
     barrier_sync(world)
     for _ in range(args.steps):
         flush_l2()
-        s0 = time.perf_counter()
-        t_e, _ = prepare_pairs(eng, pp_pairs)
-        s1 = time.perf_counter()
-        res = eng.align_pairs(t_e)  # synchronises inside (results are on the host)
-        wall_s += time.perf_counter() - s0
-        prep_s += s1 - s0
+        w, p = e2e_step()
+        wall_s += w
+        prep_s += p
         phases = [a + b for a, b in zip(phases, eng.last_phases())]
         e2e_launches += eng.last_stats()[1] + 1  # + the envelope launch
     barrier_sync(world)
+    res = []
+    for k, b in enumerate(bufs):
+        b.c = cres[k]
+        res.append(b.decode())
     clocks = sampler.stop() if sampler else None
     h2d, d2h = eng.last_transfer()
     ph2d, pd2h = eng.last_prep_transfer()

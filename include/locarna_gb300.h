@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define LCG_ABI_VERSION 2
+#define LCG_ABI_VERSION 3
 
 typedef int32_t lcg_status;
 #define LCG_OK 0
@@ -284,6 +284,17 @@ typedef struct lcg_pf_opts {
      * (sigma(i,j) plus delta where code_a[i] = x, code_b[j] = y). Offsets
      * [2..18] need the grad specs of lcg_pf_forward. */
     double param_delta[19];
+    /* AlignerPParams::min_am_prob / min_bm_prob (aligner_params.hh:122-156;
+     * locarna_p --min-am-prob / --min-bm-prob, default 0.001 each). With
+     * min_am_prob > 0, bm_prob is what compute_basematch_probabilities
+     * (aligner_p.icc:1201-1327) reports: the contributions of base matches
+     * inside arc matches of probability <= sqrt(min_am_prob) are left out.
+     * min_am_prob = 0 gives the exact base-match marginals. am_prob, log Z
+     * and the gradients do not depend on either; min_bm_prob / min_am_prob
+     * are also the thresholds of the probability writers (aligner_p.icc:
+     * 1404-1435), which the caller applies. */
+    double min_am_prob;
+    double min_bm_prob;
 } lcg_pf_opts;
 
 /* Per pair input of the parameter gradients (all optional, see below). */
@@ -417,6 +428,12 @@ lcg_status lcg_prepare_pairs(lcg_engine eng, const char *const *pp_a, const char
 lcg_status lcg_prepared_tables(lcg_prepared p, lcg_pair_tables *out);
 /* which: 0 sequence A, 1 sequence B, 2 name A, 3 name B */
 const char *lcg_prepared_sequence(lcg_prepared p, int32_t which);
+/* Rows of the inputs (a profile input is an alignment of several rows; a
+ * single sequence has one), as the reference's MultipleAlignment of the PP
+ * sequence section holds them (multiple_alignment.cc:577-584: upper case,
+ * T as U): which = 0 row k of A, 1 row k of B, 2 name of row k of A, 3 name of
+ * row k of B; NULL past the last row. Valid until lcg_prepared_free. */
+const char *lcg_prepared_row(lcg_prepared p, int32_t which, int32_t k);
 /* 0 if the envelope partition function failed (PFGotoh::fail, edge_probs.hh:202) */
 int32_t lcg_prepared_envelope_ok(lcg_prepared p);
 /* Gradient inputs of the prepared pair for lcg_pf_backward: base codes and

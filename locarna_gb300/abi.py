@@ -62,7 +62,7 @@ _P8 = C.POINTER(C.c_int8)
 
 class lcg_pf_opts(C.Structure):
     _fields_ = [("temperature", C.c_double), ("pf_scale", C.c_double), ("precision", C.c_int32),
-                ("param_delta", C.c_double * 19)]
+                ("param_delta", C.c_double * 19), ("min_am_prob", C.c_double), ("min_bm_prob", C.c_double)]
 
 
 class lcg_pf_grad_spec(C.Structure):

@@ -78,6 +78,30 @@ def build_engine(verbose=False, force=False):
     return lib
 
 
+CLI_SOURCES = {"locarna": "locarna.cc", "locarna_p": "locarna_p.cc"}
+
+
+def build_cli(force=False):
+    """The locarna / locarna_p command lines (C++ over the C ABI), linked
+    against liblocarna_gb300.so with an rpath to the build folder."""
+    lib = build_engine()
+    cli = os.path.join(PKG, "cli")
+    hdrs = [os.path.join(cli, f) for f in os.listdir(cli) if f.endswith(".hh")]
+    hdrs += [os.path.join(ROOT, "include", "locarna_gb300.h"), os.path.join(ROOT, "include", "locarna_gb300.hpp")]
+    outs = []
+    jobs = []
+    for exe, src in CLI_SOURCES.items():
+        s = os.path.join(cli, src)
+        out = os.path.join(OUT, exe)
+        outs.append(out)
+        if force or _newer(out, [s, lib] + hdrs):
+            jobs.append(["g++", "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"), s, "-o", out,
+                         "-L", OUT, "-llocarna_gb300", "-Wl,-rpath," + OUT])
+    with ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
+        list(ex.map(_run, jobs))
+    return outs
+
+
 def build_probe(force=False):
     """The int32 add+max rate probe (lcg_probe_int_peak) as its own library."""
     os.makedirs(OUT, exist_ok=True)
@@ -138,7 +162,8 @@ def build_all(verbose=False):
         f2 = ex.submit(build_oracle)
         f3 = ex.submit(build_reference_oracle)
         f4 = ex.submit(build_probe)
-        return f1.result(), f2.result(), f3.result(), f4.result()
+        r = f1.result(), f2.result(), f3.result(), f4.result()
+    return r + (build_cli(),)
 
 
 if __name__ == "__main__":

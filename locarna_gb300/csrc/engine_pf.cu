@@ -61,6 +61,7 @@ struct PFState {
     bool have_forward = false;
     double fwd_ms = 0, back_ms = 0;
     double temperature = 300.0;
+    double min_am_prob = 0.0;  // > 0: base-match probabilities truncated as AlignerP computes them
     std::vector<double> log_z;
     std::vector<std::vector<int>> am_pos;  // per pair: D position of each arc match
 };
@@ -338,6 +339,7 @@ lcg_status pf_forward_t(lcg_engine e, PFState *S, const lcg_pair_tables *pairs, 
         S->log_z[q] = log_z[q];
     }
     S->temperature = temp;
+    S->min_am_prob = o->min_am_prob;
     S->precision = sizeof(T) == 8 ? 64 : 32;
     S->npairs = npairs;
     S->nitems = nitems;
@@ -425,6 +427,42 @@ lcg_status pf_backward_t(lcg_engine e, PFState *S, const lcg_pf_grad_spec *grads
                 for (int k = 0; k < 16; ++k) r.dlogz_dbasematch[k] = cnt[k] * invT;
         }
     }
+    // base-match probabilities as AlignerP::compute_basematch_probabilities
+    // reports them for min_am_prob > 0 (aligner_p.icc:1201-1327): inside an
+    // arc match only the arc matches with probability > sqrt(min_am_prob)
+    // contribute. A second pass over the groups with the final D_bar; the
+    // gradients above keep the exact marginals.
+    bool want_bm = false;
+    for (int q = 0; q < S->npairs; ++q) want_bm |= results[q].bm_prob != nullptr;
+    if (S->min_am_prob > 0.0 && want_bm) {
+        for (int q = 0; q < S->npairs; ++q)
+            PF_TRY(cudaMemsetAsync(Dv + S->lay[q].bmacc, 0, sizeof(double) * std::max(S->lay[q].bandcells, 1), st));
+        PF_TRY(cudaMemsetAsync(Dv + S->off_ctrl, 0, 64, st));
+        PF_TRY(pf_launch_back<T>(Dv + S->off_pairs, (const int2 *)(Dv + S->off_queue), (int)S->nitems,
+                                 S->d_scratch, S->stride, S->sw, S->rb, qhead, status, abort_flag, e->sms * bb, st,
+                                 std::sqrt(S->min_am_prob)));
+        PF_TRY(cudaEventRecord(e->ev2, st));
+        for (int q = 0; q < S->npairs; ++q)
+            PF_TRY(cudaMemcpyAsync(H + S->lay[q].bmacc, Dv + S->lay[q].bmacc,
+                                   sizeof(double) * std::max(S->lay[q].bandcells, 1), cudaMemcpyDeviceToHost, st));
+        PF_TRY(cudaStreamSynchronize(st));
+        cudaEventElapsedTime(&ms, e->ev1, e->ev2);
+        S->back_ms = ms;
+        for (int q = 0; q < S->npairs; ++q) {
+            lcg_pf_result &r = results[q];
+            if (!r.bm_prob) continue;
+            const PFLayout &L = S->lay[q];
+            const double Zs = std::exp(((const double *)(H + L.res))[0]);
+            const double *acc = (const double *)(H + L.bmacc);
+            const int4 *rowinfo = (const int4 *)(H + L.rowinfo);
+            const int n = L.n, m = L.m;
+            for (int i = 1; i <= n; ++i) {
+                const int lo = std::max(1, rowinfo[i].x), hi = std::min(m, rowinfo[i].y);
+                for (int j = lo; j <= hi; ++j)
+                    r.bm_prob[(size_t)i * (m + 1) + j] = acc[rowinfo[i].w + j - rowinfo[i].x] / Zs;
+            }
+        }
+    }
     return LCG_OK;
 }
 
@@ -449,6 +487,8 @@ void lcg_pf_opts_default(lcg_pf_opts *o) {
     o->temperature = 300.0;
     o->pf_scale = 1.0;
     o->precision = 64;
+    o->min_am_prob = 0.001;  // locarna_p --min-am-prob / --min-bm-prob (src/locarna_p.cc:143-146)
+    o->min_bm_prob = 0.001;
 }
 
 lcg_status lcg_pf_forward(lcg_engine e, const lcg_pair_tables *pairs, int32_t npairs, const lcg_pf_opts *opts,

@@ -58,6 +58,7 @@ struct RnaInput {
     // all rows (a multiple alignment: a profile of equal-length rows,
     // MultipleAlignment of the PP sequence section); rows[0] == seq
     std::vector<std::string> rows;
+    std::vector<std::string> row_names;  // names of the rows, in order of appearance
     std::map<std::pair<int, int>, double> arc_probs;  // (i,j) -> p, i<j (sparse matrix)
     // joint probabilities of (i,j) and (i+1,j-1) (the p2 column, read only with stacking)
     std::map<std::pair<int, int>, double> arc2_probs;
@@ -129,6 +130,7 @@ RnaInput read_pp(const std::string &text, double p_bpcut, bool stacking) {
     if (names.empty()) perr(LCG_ERR_PARSE, "PP file without sequence");
     r.anchors = anchors;
     r.name = names[0];
+    r.row_names = names;
     // MultipleAlignment::normalize_rna_symbols (multiple_alignment.cc:577-584,
     // aux.cc:65-70) on every row; the rows of an alignment must have equal
     // lengths (MultipleAlignment::is_proper)
@@ -737,6 +739,7 @@ void constrain_wo_ref(Band &tc, size_t lenA, size_t lenB, size_t delta) {
 struct lcg_prepared_s {
     int n = 0, m = 0;
     std::string seq_a, seq_b, name_a, name_b;
+    std::vector<std::string> rows_a, rows_b, row_names_a, row_names_b;  // all rows of profile inputs
     std::vector<int32_t> sigma, gap_a, gap_b, arcs_a, arcs_b, am_arcs, am_score, min_col, max_col;
     std::vector<double> arc_p_a, arc_p_b;
     std::vector<int8_t> code_a, code_b;  // 0..3 for A,C,G,U, -1 otherwise; index 1..len
@@ -861,6 +864,10 @@ void stage_inputs(std::shared_ptr<const Side> A, std::shared_ptr<const Side> B, 
     P->seq_b = sb.in.seq;
     P->name_a = sa.in.name;
     P->name_b = sb.in.name;
+    P->rows_a = sa.in.rows;
+    P->rows_b = sb.in.rows;
+    P->row_names_a = sa.in.row_names;
+    P->row_names_b = sb.in.row_names;
     // trace controller (no reference alignment, no anchors)
     S.tc.minc.assign(n + 1, 0);
     S.tc.maxc.assign(n + 1, m);
@@ -1314,6 +1321,19 @@ const char *lcg_prepared_sequence(lcg_prepared p, int32_t which) {
     case 3: return p->name_b.c_str();
     default: return "";
     }
+}
+
+const char *lcg_prepared_row(lcg_prepared p, int32_t which, int32_t k) {
+    if (!p || k < 0) return nullptr;
+    const std::vector<std::string> *v = nullptr;
+    switch (which) {
+    case 0: v = &p->rows_a; break;
+    case 1: v = &p->rows_b; break;
+    case 2: v = &p->row_names_a; break;
+    case 3: v = &p->row_names_b; break;
+    default: return nullptr;
+    }
+    return (size_t)k < v->size() ? (*v)[k].c_str() : nullptr;
 }
 
 int32_t lcg_prepared_envelope_ok(lcg_prepared p) { return p ? p->envelope_ok : 0; }

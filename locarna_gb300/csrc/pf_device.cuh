@@ -41,10 +41,12 @@ template <typename T>
 cudaError_t pf_launch_fwd(const void *pairs, const int2 *queue, int nitems, void *scratch,
                           long long stride, int pitch, int rb, unsigned int *qhead, int *status, int *abort_flag,
                           int blocks, bool count_uses, cudaStream_t st);
+// theta > 0: the truncated base-match pass (min_am_prob = theta^2) after a
+// full backward pass; theta = 0: the full adjoint pass
 template <typename T>
 cudaError_t pf_launch_back(const void *pairs, const int2 *queue, int nitems, void *scratch,
                            long long stride, int pitch, int rb, unsigned int *qhead, int *status, int *abort_flag,
-                           int blocks, cudaStream_t st);
+                           int blocks, cudaStream_t st, double theta = 0.0);
 // rb: ring size of the shared-memory rows (a power of two above the span of
 // any two consecutive band rows)
 template <typename T>

@@ -363,11 +363,17 @@ __device__ __forceinline__ T ld_cg(const T *p) { return __ldcg(p); }
 // dZ'/dM(n,m) = 1. Propagates into D_bar of nested arc matches, the per-pair
 // base-match accumulator and the gap counts. Rows bottom-up, chunks right to
 // left; E_bar of the row below lives in the E ring, the row's X_bar in Ar.
-template <typename T>
+// TRUNC: the base-match sums of compute_basematch_probabilities with a
+// positive min_am_prob (aligner_p.icc:1201-1327): D_bar is final (from the
+// full pass), only the group's arc matches with probability D D_bar / Z' >
+// theta seed M_bar, and nothing propagates out of the group (no D_bar, no use
+// counters, no gap counts); the per-band-cell sums go to bmacc.
+template <typename T, bool TRUNC = false>
 __device__ void pf_group_back(const PFPair<T> &P, int al, int ar, int bl, int br, bool top,
                               const T *__restrict__ Mg, const T *__restrict__ Eg, const T *__restrict__ Fg,
                               T *__restrict__ Mb, int pitch, PFRows<T> R, const int4 *__restrict__ dw, int ndw,
-                              int *status, volatile int *abort_flag, double *ext_acc, double *open_acc) {
+                              int *status, volatile int *abort_flag, double *ext_acc, double *open_acc,
+                              double theta_z = 0.0) {
     const int lane = threadIdx.x & 31;
     const int m1 = P.m + 1;
     const T o = P.o, arcf = P.arcf;
@@ -412,7 +418,11 @@ __device__ void pf_group_back(const PFPair<T> &P, int al, int ar, int bl, int br
             int4 e = make_int4(0, -1, 0, 0);
             if (qq >= 0) e = dw[qq];
             const bool mine = qq >= 0 && e.y == i;
-            if (mine) {
+            if (mine && TRUNC) {
+                const double db = P.Dbar[e.x];
+                if ((double)P.D[e.x] * db > theta_z)
+                    atomicAdd(Mb + (size_t)(i - al) * pitch + (e.z - bl), (T)db * P.w[e.x]);
+            } else if (mine) {
                 long long spins = 0;
                 while (*(const volatile int *)(P.cnt + e.x) > 0) {
                     __nanosleep(64);
@@ -564,12 +574,12 @@ __device__ void pf_group_back(const PFPair<T> &P, int al, int ar, int bl, int br
             for (int u = 0; u < 2; ++u) {
                 if (ok[u]) {
                     atomicAdd(Mb + co[u], xb[u] * dv[u] * arcf);
-                    atomicAdd(P.Dbar + e0 + 32 * u + lane, (double)(xb[u] * mv[u] * arcf));
+                    if (!TRUNC) atomicAdd(P.Dbar + e0 + 32 * u + lane, (double)(xb[u] * mv[u] * arcf));
                 }
             }
 #pragma unroll
             for (int u = 0; u < 2; ++u)
-                if (ok[u]) pend |= 1ull << (2 * kb + u);
+                if (ok[u] && !TRUNC) pend |= 1ull << (2 * kb + u);
             if (ball[0] != 0xffffffffu || ball[1] != 0xffffffffu) break;
         }
         drop_uses();
@@ -605,17 +615,17 @@ __device__ void pf_group_back(const PFPair<T> &P, int al, int ar, int bl, int br
         ext += __shfl_xor_sync(0xffffffffu, ext, off);
         opn += __shfl_xor_sync(0xffffffffu, opn, off);
     }
-    if (lane == 0) {
+    if (lane == 0 && !TRUNC) {
         atomicAdd(ext_acc, ext);
         atomicAdd(open_acc, opn);
     }
 }
 
-template <typename T>
+template <typename T, bool TRUNC>
 __global__ void __launch_bounds__(PF_WARPS * 32, pf_min_blocks<T>())
     pf_back_kernel(const PFPair<T> *__restrict__ pairs, const int2 *__restrict__ queue, int nitems,
                    T *scratch, long long stride, int pitch, int rb,
-                   unsigned int *qhead, int *status, int *abort_ptr) {
+                   unsigned int *qhead, int *status, int *abort_ptr, double theta) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     PFRows<T> R = pf_rows<T>(warp, rb);
     T *Mg = scratch + ((long long)blockIdx.x * PF_WARPS + warp) * stride * 4;
@@ -632,12 +642,23 @@ __global__ void __launch_bounds__(PF_WARPS * 32, pf_min_blocks<T>())
         const GroupItem it = P.groups[qi.y];
         const int al = it.top ? 0 : it.al, ar = it.top ? P.n + 1 : it.ar;
         const int bl = it.top ? 0 : it.bl, br = it.top ? P.m + 1 : it.br;
+        // TRUNC: theta Z' (scaled frame); a group none of whose arc matches
+        // passes the threshold contributes nothing
+        const double theta_z = TRUNC ? theta * exp(P.res[0]) : 0.0;
+        if (TRUNC && !it.top) {
+            bool any = false;
+            for (int k = lane; k < it.dw_count && !any; k += 32) {
+                const int pos = P.dw[it.dw_start + k].x;
+                any = (double)P.D[pos] * P.Dbar[pos] > theta_z;
+            }
+            if (!__any_sync(0xffffffffu, any)) continue;
+        }
         pf_group_sweep<T, false, false, false, true>(P, al, ar, bl, br, Mg, Eg, Fg, pitch, R, nullptr, 0, status,
                                                      abort_flag);
         __syncwarp();
-        pf_group_back<T>(P, al, ar, bl, br, it.top != 0, Mg, Eg, Fg, Mb, pitch, R,
-                         it.top ? nullptr : P.dw + it.dw_start, it.top ? 0 : it.dw_count, status, abort_flag,
-                         P.res + 1, P.res + 2);
+        pf_group_back<T, TRUNC>(P, al, ar, bl, br, it.top != 0, Mg, Eg, Fg, Mb, pitch, R,
+                                it.top ? nullptr : P.dw + it.dw_start, it.top ? 0 : it.dw_count, status, abort_flag,
+                                P.res + 1, P.res + 2, theta_z);
         __syncwarp();
     }
 }
@@ -703,24 +724,34 @@ cudaError_t pf_fwd_occupancy(int rb, int *blocks_per_sm) {
 template <typename T>
 cudaError_t pf_launch_back(const void *pairs, const int2 *queue, int nitems, void *scratch,
                            long long stride, int pitch, int rb, unsigned int *qhead, int *status, int *abort_flag,
-                           int blocks, cudaStream_t st) {
+                           int blocks, cudaStream_t st, double theta) {
     const size_t smem = pf_smem<T>(rb);
-    cudaError_t e = cudaFuncSetAttribute(pf_back_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    pf_back_kernel<T><<<blocks, PF_WARPS * 32, smem, st>>>((const PFPair<T> *)pairs, queue,
-                                                             nitems, (T *)scratch, stride, pitch, rb, qhead,
-                                                             status, abort_flag);
+    cudaError_t e;
+    if (theta > 0.0) {
+        e = cudaFuncSetAttribute(pf_back_kernel<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        pf_back_kernel<T, true><<<blocks, PF_WARPS * 32, smem, st>>>((const PFPair<T> *)pairs, queue, nitems,
+                                                                       (T *)scratch, stride, pitch, rb, qhead,
+                                                                       status, abort_flag, theta);
+    } else {
+        e = cudaFuncSetAttribute(pf_back_kernel<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        pf_back_kernel<T, false><<<blocks, PF_WARPS * 32, smem, st>>>((const PFPair<T> *)pairs, queue, nitems,
+                                                                        (T *)scratch, stride, pitch, rb, qhead,
+                                                                        status, abort_flag, 0.0);
+    }
     return cudaGetLastError();
 }
 
 template <typename T>
 cudaError_t pf_back_occupancy(int rb, int *blocks_per_sm) {
     const size_t smem = pf_smem<T>(rb);
-    cudaError_t e = cudaFuncSetAttribute(pf_back_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(pf_back_kernel<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
     if (e != cudaSuccess) return e;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, pf_back_kernel<T>, PF_WARPS * 32, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, pf_back_kernel<T, false>, PF_WARPS * 32, smem);
     if (e != cudaSuccess) return e;
-    return pf_cap_blocks(pf_back_kernel<T>, "LCG_PF_BACK_BPS", smem, blocks_per_sm);
+    return pf_cap_blocks(pf_back_kernel<T, false>, "LCG_PF_BACK_BPS", smem, blocks_per_sm);
 }
 
 int pf_warps_per_block() { return PF_WARPS; }
@@ -732,9 +763,9 @@ template cudaError_t pf_launch_fwd<float>(const void *, const int2 *, int, void 
 template cudaError_t pf_fwd_occupancy<double>(int, int *);
 template cudaError_t pf_fwd_occupancy<float>(int, int *);
 template cudaError_t pf_launch_back<double>(const void *, const int2 *, int, void *, long long, int,
-                                            int, unsigned int *, int *, int *, int, cudaStream_t);
+                                            int, unsigned int *, int *, int *, int, cudaStream_t, double);
 template cudaError_t pf_launch_back<float>(const void *, const int2 *, int, void *, long long, int,
-                                           int, unsigned int *, int *, int *, int, cudaStream_t);
+                                           int, unsigned int *, int *, int *, int, cudaStream_t, double);
 template cudaError_t pf_back_occupancy<double>(int, int *);
 template cudaError_t pf_back_occupancy<float>(int, int *);
 

@@ -126,6 +126,51 @@ def prepare_pairs(engine, pp_pairs, **kw):
                 lib.lcg_prepared_free(C.c_void_p(h))
 
 
+class PreparedBatch:
+    """Handles of lcg_prepare_pairs kept alive: the tables stay in the
+    library's memory and c_tables() gives the lcg_pair_tables views for
+    lcg_align_pairs without copying them into Python. close() frees them."""
+
+    def __init__(self, lib, handles, host_envelopes):
+        self.lib, self.handles, self.host_envelopes = lib, handles, host_envelopes
+
+    def __len__(self):
+        return len(self.handles)
+
+    def c_tables(self):
+        arr = (lcg_pair_tables * len(self.handles))()
+        for k, h in enumerate(self.handles):
+            self.lib.lcg_prepared_tables(h, C.byref(arr[k]))
+        return arr
+
+    def close(self):
+        for h in self.handles:
+            if h:
+                self.lib.lcg_prepared_free(h)
+        self.handles = []
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def prepare_pairs_batch(engine, pp_pairs, **kw):
+    """lcg_prepare_pairs returning the prepared handles (PreparedBatch)."""
+    lib = _lib()
+    o = prep_options(**kw)
+    n = len(pp_pairs)
+    arr_a = (C.c_char_p * n)(*[a.encode() for a, _ in pp_pairs])
+    arr_b = (C.c_char_p * n)(*[b.encode() for _, b in pp_pairs])
+    hs = (C.c_void_p * n)()
+    nhost = C.c_int32()
+    rc = lib.lcg_prepare_pairs(engine.h, arr_a, arr_b, n, C.byref(o), hs, C.byref(nhost))
+    if rc != 0:
+        raise LcgError(rc, lib.lcg_last_error().decode())
+    return PreparedBatch(lib, [C.c_void_p(h) for h in hs], nhost.value)
+
+
 def _tables_of(lib, h):
     """PairTables of a prepared handle (copies)."""
     t = lcg_pair_tables()

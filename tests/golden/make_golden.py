@@ -207,6 +207,11 @@ PF_CASES = {
     "pf90_b": (90, 51, 110, 52, {}),
     # profile inputs (alignment rows)
     "pf_p100": (("p", 100, 3), 61, ("p", 90, 2), 62, {}),
+    # locarna_p's default --min-am-prob 0.001: base-match probabilities
+    # truncated under arc matches of probability <= sqrt(0.001)
+    "pf90_b_default": (90, 51, 110, 52, {"min_am_prob": "0.001"}),
+    "pf100_default": (100, 55, 95, 56, {"min_am_prob": "0.001"}),
+    "pf80_default": (80, 57, 85, 58, {"min_am_prob": "0.001"}),
 }
 
 

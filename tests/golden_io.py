@@ -108,6 +108,9 @@ class GoldenPF:
         self.am_p = z["am_p"]
         self.bm_ij = z["bm"]
         self.bm_p = z["bm_p"]
+        self.opts = json.loads(str(z["opts"])) if "opts" in z else {}
+        # AlignerPParams::min_am_prob the reference ran with (0: exact marginals)
+        self.min_am_prob = float(self.opts.get("min_am_prob", 0.0))
         self.min_col, self.max_col = z["min_col"], z["max_col"]
         n, m = len(self.seq_a), len(self.seq_b)
         self.tables = PairTables(

@@ -10,6 +10,12 @@
   base match). On pf150 / pf200 the reference's outside pass returns
   negative probabilities for hundreds of arc matches and its values change
   with pf_scale; the adjoint pass does neither.
+* These compare the exact marginals (min_am_prob = 0). With locarna_p's
+  default min_am_prob = 0.001 the base-match probabilities leave out the
+  contributions inside arc matches of probability <= sqrt(min_am_prob), as
+  the reference's compute_basematch_probabilities does
+  (aligner_p.icc:1201-1327); test_pf64_default_semantics_match_reference
+  checks them against the reference's default output.
 * FP32 with per-position scaling: probabilities within 1e-5 absolute of the
   FP64 values, log Z within 1e-5 relative.
 * Gradients of log Z from the backward pass against central finite differences
@@ -46,7 +52,7 @@ def _prepared(g):
 @pytest.mark.parametrize("name", PF_CASES)
 def test_pf64_log_z_matches_reference(engine, name):
     g = GoldenPF(name)
-    lz = engine.pf_forward([g.tables], precision=64)[0]
+    lz = engine.pf_forward([g.tables], precision=64, min_am_prob=0.0)[0]
     assert abs(lz - math.log(g.Z)) <= 1e-10 * max(1.0, abs(lz)), (lz, math.log(g.Z))
     r = engine.pf_backward()[0]
     assert r["log_z"] == lz
@@ -59,7 +65,7 @@ def test_pf64_log_z_matches_reference(engine, name):
 def test_pf64_probabilities_are_marginals_of_reference_z(engine, name):
     g = GoldenPF(name)
     f = np.load(os.path.join(GOLDEN_DIR, name + "_marginals.npz"))
-    engine.pf_forward([g.tables], precision=64)
+    engine.pf_forward([g.tables], precision=64, min_am_prob=0.0)
     r = engine.pf_backward()[0]
     assert np.max(np.abs(r["am_prob"][f["am_idx"]] - f["am_fd"])) <= P64_TOL
     assert np.max(np.abs(r["bm_prob"].reshape(-1)[f["bm_idx"]] - f["bm_fd"])) <= P64_TOL
@@ -74,7 +80,7 @@ def test_pf64_probabilities_are_marginals_of_reference_z(engine, name):
 def test_pf64_matches_reference_probabilities(engine, name):
     g = GoldenPF(name)
     t = g.tables
-    engine.pf_forward([t], precision=64)
+    engine.pf_forward([t], precision=64, min_am_prob=0.0)
     r = engine.pf_backward()[0]
     Z, am, bm = oracle_pf(t)
     assert np.max(np.abs(r["am_prob"] - am)) <= P64_TOL
@@ -92,9 +98,9 @@ def test_pf64_matches_reference_probabilities(engine, name):
 def test_pf32_scaled_within_tolerance(engine, name):
     g = GoldenPF(name)
     t = g.tables
-    engine.pf_forward([t], precision=64)
+    engine.pf_forward([t], precision=64, min_am_prob=0.0)
     r64 = engine.pf_backward()[0]
-    lz = engine.pf_forward([t], precision=32)[0]
+    lz = engine.pf_forward([t], precision=32, min_am_prob=0.0)[0]
     r = engine.pf_backward()[0]
     assert abs(lz - math.log(g.Z)) <= LZ32_REL * abs(math.log(g.Z))
     err_am = np.max(np.abs(r["am_prob"] - r64["am_prob"]))
@@ -108,10 +114,10 @@ def test_pf_batch_equals_single(engine):
     gs = [GoldenPF(n) for n in PF_CASES]
     tabs = [g.tables for g in gs] * 2
     for prec in (64, 32):
-        lzb = engine.pf_forward(tabs, precision=prec)
+        lzb = engine.pf_forward(tabs, precision=prec, min_am_prob=0.0)
         rb = engine.pf_backward()
         for k, t in enumerate(tabs):
-            lz = engine.pf_forward([t], precision=prec)[0]
+            lz = engine.pf_forward([t], precision=prec, min_am_prob=0.0)[0]
             r = engine.pf_backward()[0]
             tol = 1e-12 if prec == 64 else 1e-6
             assert abs(lzb[k] - lz) <= tol * max(1.0, abs(lz))
@@ -124,10 +130,10 @@ def test_pf_scale_and_temperature(engine):
     probabilities do not depend on pf_scale (a numerical scale factor)."""
     g = GoldenPF(PF_CASES[0])
     t = g.tables
-    engine.pf_forward([t], precision=64)
+    engine.pf_forward([t], precision=64, min_am_prob=0.0)
     base = engine.pf_backward()[0]
     for temp, scale in ((300.0, 2.0), (300.0, 0.5)):
-        lz = engine.pf_forward([t], temperature=temp, pf_scale=scale, precision=64)[0]
+        lz = engine.pf_forward([t], temperature=temp, pf_scale=scale, precision=64, min_am_prob=0.0)[0]
         r = engine.pf_backward()[0]
         Z, _, _ = oracle_pf(t, temperature=temp, pf_scale=scale, probs=False)
         assert abs(lz - math.log(Z)) <= 1e-10 * max(1.0, abs(lz))
@@ -135,7 +141,7 @@ def test_pf_scale_and_temperature(engine):
         assert np.max(np.abs(r["bm_prob"] - base["bm_prob"])) <= 1e-12
     ge = GoldenPF(EXACT_CASES[0])
     for temp in (150.0, 600.0):
-        lz = engine.pf_forward([ge.tables], temperature=temp, precision=64)[0]
+        lz = engine.pf_forward([ge.tables], temperature=temp, precision=64, min_am_prob=0.0)[0]
         r = engine.pf_backward()[0]
         Z, am, bm = oracle_pf(ge.tables, temperature=temp)
         assert abs(lz - math.log(Z)) <= 1e-10 * max(1.0, abs(lz))
@@ -146,8 +152,8 @@ def test_pf_scale_and_temperature(engine):
 def _fd_check(engine, t, k_param, grad, precision=64):
     d = np.zeros(19)
     d[k_param] = FD_H
-    lp = engine.pf_forward([t], precision=precision, param_delta=d)[0]
-    lm = engine.pf_forward([t], precision=precision, param_delta=-d)[0]
+    lp = engine.pf_forward([t], precision=precision, param_delta=d, min_am_prob=0.0)[0]
+    lm = engine.pf_forward([t], precision=precision, param_delta=-d, min_am_prob=0.0)[0]
     fd = (lp - lm) / (2 * FD_H)
     assert abs(grad - fd) <= GRAD_REL * max(abs(fd), 1e-8), (k_param, grad, fd)
 
@@ -157,7 +163,7 @@ def _fd_check(engine, t, k_param, grad, precision=64):
 def test_pf_gradients_match_finite_differences(engine, name):
     g = GoldenPF(name)
     t = _prepared(g)
-    engine.pf_forward([t], precision=64)
+    engine.pf_forward([t], precision=64, min_am_prob=0.0)
     r = engine.pf_backward()[0]
     grads = [r["dlogz_dindel"], r["dlogz_dindel_opening"], r["dlogz_dstruct_weight"]] + \
         list(r["dlogz_dbasematch"])
@@ -172,9 +178,9 @@ def test_pf32_gradients(engine):
     """FP32 backward: gradients within 1e-4 relative of the FP64 ones."""
     g = GoldenPF(PF_CASES[0])
     t = _prepared(g)
-    engine.pf_forward([t], precision=64)
+    engine.pf_forward([t], precision=64, min_am_prob=0.0)
     r64 = engine.pf_backward()[0]
-    engine.pf_forward([t], precision=32)
+    engine.pf_forward([t], precision=32, min_am_prob=0.0)
     r32 = engine.pf_backward()[0]
     for key in ("dlogz_dindel", "dlogz_dindel_opening", "dlogz_dstruct_weight"):
         assert abs(r32[key] - r64[key]) <= GRAD_REL * abs(r64[key]), key
@@ -185,7 +191,35 @@ def test_pf32_gradients(engine):
 def test_pf_backward_needs_forward(engine):
     from locarna_gb300.engine import LcgError
     g = GoldenPF(PF_CASES[0])
-    engine.pf_forward([g.tables])
+    engine.pf_forward([g.tables], min_am_prob=0.0)
     engine.pf_backward()
     with pytest.raises(LcgError):
         engine.pf_backward()
+
+
+DEFAULT_CASES = [n for n in PF_CASES if n.endswith("_default")]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", DEFAULT_CASES)
+def test_pf64_default_semantics_match_reference(engine, name):
+    """locarna_p's default --min-am-prob 0.001: arc-match probabilities and
+    the truncated base-match probabilities (no contributions from inside arc
+    matches of probability <= sqrt(0.001)) against the reference's own output
+    of the same run (cases where its outside pass agrees with its Z)."""
+    g = GoldenPF(name)
+    assert g.min_am_prob == 0.001
+    t = g.tables
+    engine.pf_forward([t], precision=64, min_am_prob=g.min_am_prob)
+    r = engine.pf_backward()[0]
+    A, B, AM = t.arcs_a.reshape(-1, 2), t.arcs_b.reshape(-1, 2), t.am_arcs.reshape(-1, 2)
+    mine = {(int(A[a][0]), int(A[a][1]), int(B[b][0]), int(B[b][1])): r["am_prob"][k]
+            for k, (a, b) in enumerate(AM)}
+    for key, p in g.am_by_ends().items():
+        assert abs(mine[key] - p) <= P64_TOL, (key, mine[key], p)
+    ref_bm = g.bm_dense()
+    assert np.max(np.abs(r["bm_prob"] - ref_bm)) <= P64_TOL
+    # the exact marginals differ: the truncation is what the reference reports
+    engine.pf_forward([t], precision=64, min_am_prob=0.0)
+    exact = engine.pf_backward()[0]
+    assert np.max(np.abs(exact["bm_prob"] - ref_bm)) > 10 * P64_TOL

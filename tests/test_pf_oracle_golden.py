@@ -13,7 +13,7 @@ from oracle_ffi import oracle_pf
 def test_pf_oracle_matches_reference(name):
     g = GoldenPF(name)
     t = g.tables
-    Z, am, bm = oracle_pf(t)
+    Z, am, bm = oracle_pf(t, min_am_prob=g.min_am_prob)
     assert Z == g.Z
     A, B, AM = t.arcs_a.reshape(-1, 2), t.arcs_b.reshape(-1, 2), t.am_arcs.reshape(-1, 2)
     mine = {(int(A[a][0]), int(A[a][1]), int(B[b][0]), int(B[b][1])): am[k] for k, (a, b) in enumerate(AM)}
