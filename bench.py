@@ -48,7 +48,7 @@ CPU_SAMPLE_SECONDS = 20.0
 PF_WORKLOAD = dict(count=128, len_lo=80, len_hi=500, seed=2025, q=0.05)
 PF_WORKLOAD_NAME = "locarna_p_allpairs_128rnas_80-500nt"
 PF_BUCKET = 1024
-PF_STRIDE = 32  # the timed LocARNA-P sample: every PF_STRIDE-th pair in size order
+PF_FP64_STRIDE = 8  # FP64 (and the FP32 error) on every 8th pair of each launch
 PF_CPU_SECONDS = 20.0
 REF_PAIRS_PER_CORE = 4  # pairs per host core in one step of the reference arm
 # DRAM traffic of the fill kernel per M cell, from the ncu capture of the
@@ -77,23 +77,28 @@ def int_peak_gops(dpx, device=0):
     return g.value
 
 
-def workload_pp():
-    """PP texts of the all-pairs workload and its pairs (index pairs)."""
+def workload_pp(families=1):
+    """PP texts of the all-pairs workload and its pairs (index pairs). With
+    families = N (N GPUs), N families of 64 RNAs (seeds 2024, 2025, ...),
+    all pairs within each family: N x 2,016 pairs."""
     from locarna_gb300.synth import make_family
-    fam = make_family(WORKLOAD["count"], WORKLOAD["len_lo"], WORKLOAD["len_hi"], WORKLOAD["seed"],
-                      q=WORKLOAD["q"])
-    pp = [r.to_pp() for r in fam]
-    pairs = [(a, b) for a in range(len(fam)) for b in range(a + 1, len(fam))]
+    pp, pairs = [], []
+    for f in range(families):
+        fam = make_family(WORKLOAD["count"], WORKLOAD["len_lo"], WORKLOAD["len_hi"], WORKLOAD["seed"] + f,
+                          q=WORKLOAD["q"])
+        base = len(pp)
+        pp += [r.to_pp() for r in fam]
+        pairs += [(base + a, base + b) for a in range(len(fam)) for b in range(a + 1, len(fam))]
     return pp, pairs
 
 
-def build_tables(threads=None):
+def build_tables(threads=None, families=1):
     """Tables of the workload from the host path (lcg_prepare_pair on every
     host thread; the envelope in long double as locarna computes it)."""
     from concurrent.futures import ThreadPoolExecutor
 
     from locarna_gb300.prep import prepare_pair
-    pp, pairs = workload_pp()
+    pp, pairs = workload_pp(families)
     threads = threads or os.cpu_count() or 4
     with ThreadPoolExecutor(threads) as ex:
         tables = list(ex.map(lambda ab: prepare_pair(pp[ab[0]], pp[ab[1]]), pairs))
@@ -343,52 +348,65 @@ def run_modes(eng, tables, flush_l2):
 
 
 def run_pf(eng, tables, flush_l2, cpu):
-    """LocARNA-P: FP64 and FP32-scaled inside + adjoint outside over a
-    size-stratified sample of the pairs (every PF_STRIDE-th pair in size
-    order) in size-sorted buckets; device and end-to-end rates, FP32 error
-    against the FP64 run of the same kernels, and one 200-nt pair with
-    gradients."""
+    """LocARNA-P over the whole workload: all pairs in size order, in
+    launches of PF_BUCKET pairs (length-grouped persistent launches), inside
+    + adjoint outside in FP32 with per-position scaling; FP64 on every
+    PF_FP64_STRIDE-th pair of each launch (size-stratified), and per pair of
+    that subset the largest FP32 error of any arc-match or base-match
+    probability against the FP64 run of the same kernels (exact marginals,
+    min_am_prob 0); one 200-nt pair with gradients."""
     import numpy as np
-    order = sorted(range(len(tables)), key=lambda k: tables[k].len_a * tables[k].len_b)
-    sample = order[::PF_STRIDE]
-    buckets = [sample[i:i + PF_BUCKET] for i in range(0, len(sample), PF_BUCKET)]
-    for prec in (64, 32):  # warm-up: the smallest bucket
-        eng.pf_forward([tables[k] for k in buckets[0]], precision=prec, min_am_prob=0.0)
+    order = sorted(range(len(tables)), key=lambda k: (tables[k].len_a * tables[k].len_b, k))
+    buckets = [order[i:i + PF_BUCKET] for i in range(0, len(order), PF_BUCKET)]
+    for prec in (64, 32):  # warm-up
+        eng.pf_forward([tables[k] for k in buckets[0][:64]], precision=prec, min_am_prob=0.0)
         eng.pf_backward(probs=False)
     dev = {64: 0.0, 32: 0.0}
     wall = {64: 0.0, 32: 0.0}
+    n64 = 0
     err_am, err_bm, pair_err = 0.0, 0.0, []
     launches = 0
     for b in buckets:
         tb = [tables[k] for k in b]
-        res = {}
-        for prec in (64, 32):
-            flush_l2()
-            t0 = time.perf_counter()
-            eng.pf_forward(tb, precision=prec, min_am_prob=0.0)
-            r = eng.pf_backward(probs=True)
-            wall[prec] += time.perf_counter() - t0
-            f, bw = eng.pf_last_timing()
-            dev[prec] += f + bw
-            launches += 2
-            res[prec] = r
-        for r64, r32 in zip(res[64], res[32]):
-            ea = float(np.max(np.abs(r64["am_prob"] - r32["am_prob"]))) if r64["am_prob"].size else 0.0
-            eb = float(np.max(np.abs(r64["bm_prob"] - r32["bm_prob"])))
+        sub = list(range(0, len(b), PF_FP64_STRIDE))
+        flush_l2()
+        t0 = time.perf_counter()
+        eng.pf_forward(tb, precision=32, min_am_prob=0.0)
+        r32 = eng.pf_backward(probs=True)
+        wall[32] += time.perf_counter() - t0
+        f, bw = eng.pf_last_timing()
+        dev[32] += f + bw
+        keep = {k: (r32[k]["am_prob"], r32[k]["bm_prob"]) for k in sub}
+        del r32
+        flush_l2()
+        t0 = time.perf_counter()
+        eng.pf_forward([tb[k] for k in sub], precision=64, min_am_prob=0.0)
+        r64 = eng.pf_backward(probs=True)
+        wall[64] += time.perf_counter() - t0
+        f, bw = eng.pf_last_timing()
+        dev[64] += f + bw
+        n64 += len(sub)
+        launches += 4
+        for k, r in zip(sub, r64):
+            am32, bm32 = keep[k]
+            ea = float(np.max(np.abs(r["am_prob"] - am32))) if r["am_prob"].size else 0.0
+            eb = float(np.max(np.abs(r["bm_prob"] - bm32)))
             err_am, err_bm = max(err_am, ea), max(err_bm, eb)
             pair_err.append(max(ea, eb))
-        del res
-    n = len(sample)
+        del r64, keep
+    n = len(tables)
     pair_err.sort()
     out = {
-        "workload": PF_WORKLOAD_NAME, "workload_pairs": len(tables), "pairs": n,
-        "sample": f"every {PF_STRIDE}th pair of the {len(tables)} in size order (rates are pairs of this "
-                  f"size mix per second)",
+        "workload": PF_WORKLOAD_NAME, "workload_pairs": n,
+        "fp32": {"pairs": n, "pairs_per_s": n / (dev[32] / 1e3), "device_ms": dev[32], "e2e_pairs_per_s": n / wall[32],
+                 "what": "every pair of the workload, inside + adjoint outside, FP32 with per-position scaling"},
+        "fp64": {"pairs": n64, "pairs_per_s": n64 / (dev[64] / 1e3), "device_ms": dev[64],
+                 "e2e_pairs_per_s": n64 / wall[64],
+                 "what": f"every {PF_FP64_STRIDE}th pair of each launch in size order (size-stratified)"},
         "buckets": len(buckets), "bucket_pairs": PF_BUCKET,
-        "fp64": {"pairs_per_s": n / (dev[64] / 1e3), "device_ms": dev[64], "e2e_pairs_per_s": n / wall[64]},
-        "fp32": {"pairs_per_s": n / (dev[32] / 1e3), "device_ms": dev[32], "e2e_pairs_per_s": n / wall[32]},
-        "fp32_over_fp64_device": dev[64] / dev[32], "fp32_over_fp64_e2e": wall[64] / wall[32],
-        "fp32_max_abs_err": {"am_prob": err_am, "bm_prob": err_bm,
+        "fp32_over_fp64_device": (n / dev[32]) / (n64 / dev[64]),
+        "fp32_over_fp64_e2e": (n / wall[32]) / (n64 / wall[64]),
+        "fp32_max_abs_err": {"am_prob": err_am, "bm_prob": err_bm, "pairs_checked": len(pair_err),
                              "pair_max_median": pair_err[len(pair_err) // 2], "pair_max_max": pair_err[-1],
                              "tolerance": 1e-5, "against": "FP64 run of the same kernels"},
         "gpu_launches": launches,
@@ -466,9 +484,10 @@ def run_ours(args):
     extras = world == 1  # the secondary lines are measured at N = 1 only
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
         os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
-    pp, pairs = workload_pp()
+    # weak scaling: N families of the workload for N GPUs, LPT-sharded
+    pp, pairs = workload_pp(world)
     t0 = time.time()
-    all_tables, _ = build_tables()
+    all_tables, _ = build_tables(families=world)
     host_prep_s = time.time() - t0
     if lead:
         log(f"host preparation of {len(all_tables)} pairs: {host_prep_s:.1f} s")
@@ -623,7 +642,8 @@ def run_ours(args):
         "config": {"workload": WORKLOAD_NAME, "pairs": npairs_total, "rnas": WORKLOAD["count"],
                    "len_range": [WORKLOAD["len_lo"], WORKLOAD["len_hi"]], "seed": WORKLOAD["seed"],
                    "mode": "global, default locarna scoring, envelope 1e-4",
-                   "parallelism": f"pairs sharded over {world} GPU(s) by LPT of the host cell counts",
+                   "families": world,
+                   "parallelism": f"{world} x 2016 pairs sharded over {world} GPU(s) by LPT of the host cell counts",
                    "shard_cells": shard_loads(weights, shards),
                    "l2": "flushed between steps (256 MB write)"},
         "gcups": sum(weights) / T / 1e9,

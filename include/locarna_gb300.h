@@ -217,6 +217,48 @@ lcg_status lcg_align_kbest(lcg_engine eng, const lcg_pair_tables *pairs, int32_t
  * at n pairs (n >= npairs: one chunk, one fill and one traceback launch). */
 lcg_status lcg_engine_set_chunk_pairs(lcg_engine eng, int32_t pairs_per_chunk);
 
+/* CUDA graphs (default on): lcg_align_pairs records each chunk's device work
+ * (host->device copy, clearing, fill kernel, traceback kernel, device->host
+ * copies) from its stream into a CUDA graph and launches the graph; a chunk
+ * whose launch parameters (buffers, sizes, grid) equal the previous chunk's
+ * on the same buffer set replays it without capturing again. Normalized,
+ * penalized and k-best alignment, whose top levels iterate with the host,
+ * launch directly. on = 0 launches every chunk directly. */
+lcg_status lcg_engine_set_graphs(lcg_engine eng, int32_t on);
+/* Graph captures and replays of the last lcg_align_pairs call. */
+lcg_status lcg_engine_last_graphs(lcg_engine eng, int64_t *captures, int64_t *replays);
+
+/* ------------------------------------------------------------- autotuner
+ *
+ * The fill kernel's launch configuration chosen per length bucket by
+ * measurement: for the pairs of each bucket (by max(len_a, len_b): <= 128,
+ * <= 224, <= 320, longer) a sample is aligned under every configuration of a
+ * grid (resident blocks per SM of the persistent fill kernel, i.e. warps
+ * per SM; L2 budget of a pair wave of its work queue, i.e. how many pairs'
+ * tables are interleaved at a time) and the fastest fill is kept. With
+ * autotune on, lcg_align_pairs orders a batch by bucket, forms its chunks
+ * within buckets and launches each chunk with its bucket's configuration;
+ * results come back in input order and are the same as without. The
+ * reference has no counterpart (its all-pairs driver mlocarna runs one
+ * locarna process per pair, lib/perl/MLocarna/threaded.pm:28-65). */
+#define LCG_TUNE_BUCKETS 4
+typedef struct lcg_tune_entry {
+    int32_t max_len;        /* bucket: pairs with max(len_a, len_b) <= max_len (last: any) */
+    int32_t pairs_sampled;  /* 0: no pair of the batch in this bucket (defaults kept) */
+    int32_t blocks_per_sm;  /* chosen (0 = as many as fit) */
+    double wave_mb;         /* chosen (0 = default 8 MB) */
+    double best_ms;         /* fill time of the sample under the chosen configuration */
+    double default_ms;      /* fill time of the sample under the default configuration */
+    int32_t trials;         /* configurations measured */
+} lcg_tune_entry;
+/* Measure and store the configuration of every bucket present in the batch
+ * (sample_pairs: pairs per bucket, 0 = 64); report[LCG_TUNE_BUCKETS] may be
+ * NULL. Uses opts' mode; opts->do_trace is ignored (fill only). */
+lcg_status lcg_engine_autotune(lcg_engine eng, const lcg_pair_tables *pairs, int32_t npairs,
+                               const lcg_align_opts *opts, int32_t sample_pairs, lcg_tune_entry *report);
+/* Use the stored configurations in lcg_align_pairs (on = 1) or not (0). */
+lcg_status lcg_engine_set_autotune(lcg_engine eng, int32_t on);
+
 /* Device time (ms) of the last lcg_align_pairs call's kernels (summed over its
  * chunks, whose kernels may overlap on the two streams), and the number of
  * kernel launches it made. */

@@ -56,6 +56,15 @@ class lcg_work_counts(C.Structure):
                 ("arc_terms", C.c_int64), ("valid_arc_terms", C.c_int64)]
 
 
+LCG_TUNE_BUCKETS = 4
+
+
+class lcg_tune_entry(C.Structure):
+    _fields_ = [("max_len", C.c_int32), ("pairs_sampled", C.c_int32), ("blocks_per_sm", C.c_int32),
+                ("wave_mb", C.c_double), ("best_ms", C.c_double), ("default_ms", C.c_double),
+                ("trials", C.c_int32)]
+
+
 _PD = C.POINTER(C.c_double)
 _P8 = C.POINTER(C.c_int8)
 

@@ -513,15 +513,16 @@ struct Slot {
     int **d_scratch;
     size_t *scratch_cap;
     cudaEvent_t ev0, ev1, ev2;
+    lcg_graph_cache *graph;
 };
 
 Slot slot_of(lcg_engine e, int k) {
     if (k == 0)
         return Slot{e->stream, &e->d_arena, &e->arena_cap, &e->h_stage, &e->stage_cap,
-                    &e->d_scratch, &e->scratch_cap, e->ev0, e->ev1, e->ev2};
+                    &e->d_scratch, &e->scratch_cap, e->ev0, e->ev1, e->ev2, &e->graph};
     lcg_buffer_set &b = e->alt;
     return Slot{b.stream, &b.d_arena, &b.arena_cap, &b.h_stage, &b.stage_cap,
-                &b.d_scratch, &b.scratch_cap, b.ev0, b.ev1, b.ev2};
+                &b.d_scratch, &b.scratch_cap, b.ev0, b.ev1, b.ev2, &b.graph};
 }
 
 // byte offsets of one pair's tables in the arena
@@ -547,6 +548,10 @@ struct Chunk {
     long long stride = 0;
     bool sl = false;
     int *scratch = nullptr;
+    // launch configuration: resident fill blocks per SM (0 = as many as fit)
+    // and the L2 budget of a pair wave in MB (0 = default)
+    int bps = 0;
+    double wave_mb = 0;
 };
 
 // pairs per chunk: one chunk for small batches, else up to 8 chunks of at
@@ -746,7 +751,7 @@ lcg_status chunk_launch(lcg_engine e, const Slot &s, const lcg_pair_tables *all,
         for (int q = 0; q < npairs; ++q) ng[q] = prep[q].groups.size();
         lcg_host::queue_order(
             ng, [&](int q) { return 12.0 * prep[q].num_pos + 4.0 * prep[q].bandcells; }, (int2 *)(H + off_queue),
-            [](int n, auto fn) { lcg_host::parallel_for(n, fn); });
+            [](int n, auto fn) { lcg_host::parallel_for(n, fn); }, c.wave_mb * 1048576.0);
     }
     std::memset(H + off_ctrl, 0, 64);
     lcg_host::parallel_for(npairs, [&](int q) {
@@ -866,6 +871,7 @@ lcg_status chunk_launch(lcg_engine e, const Slot &s, const lcg_pair_tables *all,
         CUDA_TRY(trace_prepare(rb));
     }
     if (blocks_per_sm < 1) return fail(LCG_ERR_UNSUPPORTED, "fill kernel does not fit on an SM");
+    if (c.bps > 0 && c.bps < blocks_per_sm) blocks_per_sm = c.bps;
     int blocks = e->sms * blocks_per_sm;
     long long stride = (long long)rows_max * sw;
     // state matrices per slot: fill 1 (plain) / 4 (struct-local); traceback 1 / 8
@@ -884,24 +890,76 @@ lcg_status chunk_launch(lcg_engine e, const Slot &s, const lcg_pair_tables *all,
 
     // ---- transfer + launch + transfer
     cudaStream_t st = s.st;
-    CUDA_TRY(cudaMemcpyAsync(Dv, H, down_begin, cudaMemcpyHostToDevice, st));
-    CUDA_TRY(cudaMemsetAsync(Dv + down_begin, 0, down_end - down_begin, st));
+    // Without host steps between the launches (not normalized / penalized /
+    // k-best), the chunk's device work is one CUDA graph: captured from the
+    // stream on first use, replayed while the launch parameters (buffers,
+    // sizes, grid) stay the same, updated in place otherwise.
+    const bool use_graph = e->graphs && !modv && !c.kbest;
+    std::vector<long long> key;
+    if (use_graph) {
+        key = {(long long)(uintptr_t)Dv, (long long)(uintptr_t)H, (long long)(uintptr_t)scratch, (long long)down_begin,
+               (long long)down_end, (long long)off_ctrl, (long long)off_pairs, (long long)off_queue, (long long)nitems,
+               blocks, sw, rb, stride, fast, e->counting, sl, opts->do_trace, npairs};
+        if (s.graph->exec && s.graph->key == key) {
+            CUDA_TRY(cudaGraphLaunch(s.graph->exec, st));
+            ++e->last_graph_replays;
+            c.launches = opts->do_trace ? 2 : 1;
+            c.off_pairs = off_pairs;
+            c.off_mod = off_mod;
+            c.sw = sw;
+            c.rb = rb;
+            c.stride = stride;
+            c.sl = sl;
+            c.scratch = scratch;
+            c.in_flight = true;
+            e->last_h2d += (long long)down_begin;
+            e->last_d2h += 64 + (long long)(down_end - down_begin);
+            return LCG_OK;
+        }
+        CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    }
+    // timing events: inside a capture an event record becomes a graph node
+    // only when it is marked external
+    auto record = [&](cudaEvent_t ev) {
+        return use_graph ? cudaEventRecordWithFlags(ev, st, cudaEventRecordExternal) : cudaEventRecord(ev, st);
+    };
+    // an error inside the capture ends it before returning
+    auto end_capture = [&]() {
+        if (!use_graph) return;
+        cudaGraph_t g = nullptr;
+        cudaStreamEndCapture(st, &g);
+        if (g) cudaGraphDestroy(g);
+    };
+#undef CUDA_TRY_CAP
+#define CUDA_TRY_CAP(call)                                                                      \
+    do {                                                                                        \
+        cudaError_t _e = (call);                                                                \
+        if (_e != cudaSuccess) {                                                                \
+            end_capture();                                                                      \
+            return fail(LCG_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(_e));      \
+        }                                                                                       \
+    } while (0)
+    CUDA_TRY_CAP(cudaMemcpyAsync(Dv, H, down_begin, cudaMemcpyHostToDevice, st));
+    CUDA_TRY_CAP(cudaMemsetAsync(Dv + down_begin, 0, down_end - down_begin, st));
     unsigned int *qhead = (unsigned int *)(Dv + off_ctrl);
     int *status = (int *)(Dv + off_ctrl + 4);
     int *abort_flag = (int *)(Dv + off_ctrl + 8);
-    CUDA_TRY(cudaEventRecord(s.ev0, st));
+    CUDA_TRY_CAP(record(s.ev0));
     unsigned long long *counters = e->counting ? (unsigned long long *)(Dv + off_ctrl + 16) : nullptr;
     if (sl) {
-        if (counters) return fail(LCG_ERR_UNSUPPORTED, "work counting covers the plain mode only");
-        CUDA_TRY(launch_sl_fill((const PairDev *)(Dv + off_pairs), (const int2 *)(Dv + off_queue),
+        if (counters) {
+            end_capture();
+            return fail(LCG_ERR_UNSUPPORTED, "work counting covers the plain mode only");
+        }
+        CUDA_TRY_CAP(launch_sl_fill((const PairDev *)(Dv + off_pairs), (const int2 *)(Dv + off_queue),
                                 (int)nitems, scratch, stride, sw, rb, qhead,
                                 status, abort_flag, blocks, st));
     } else {
-        CUDA_TRY(launch_fill((const PairDev *)(Dv + off_pairs), (const int2 *)(Dv + off_queue),
+        CUDA_TRY_CAP(launch_fill((const PairDev *)(Dv + off_pairs), (const int2 *)(Dv + off_queue),
                              (int)nitems, scratch, stride, sw, rb, fast, qhead,
                              status, abort_flag, blocks, st, counters));
     }
-    CUDA_TRY(cudaEventRecord(s.ev1, st));
+    CUDA_TRY_CAP(record(s.ev1));
     c.launches = 1;
     TraceSel sel;
     if (modv) {
@@ -918,16 +976,36 @@ lcg_status chunk_launch(lcg_engine e, const Slot &s, const lcg_pair_tables *all,
     c.scratch = scratch;
     if ((opts->do_trace || modv) && !c.kbest) {
         if (sl)
-            CUDA_TRY(launch_sl_trace((const PairDev *)(Dv + off_pairs), npairs, scratch, stride, sw,
+            CUDA_TRY_CAP(launch_sl_trace((const PairDev *)(Dv + off_pairs), npairs, scratch, stride, sw,
                                      status, st, sel));
         else
-            CUDA_TRY(launch_trace((const PairDev *)(Dv + off_pairs), npairs, scratch, stride, sw, rb, status,
+            CUDA_TRY_CAP(launch_trace((const PairDev *)(Dv + off_pairs), npairs, scratch, stride, sw, rb, status,
                                   st, sel));
         ++c.launches;
     }
-    CUDA_TRY(cudaEventRecord(s.ev2, st));
-    CUDA_TRY(cudaMemcpyAsync(H + off_ctrl, Dv + off_ctrl, 64, cudaMemcpyDeviceToHost, st));
-    CUDA_TRY(cudaMemcpyAsync(H + down_begin, Dv + down_begin, down_end - down_begin, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY_CAP(record(s.ev2));
+    CUDA_TRY_CAP(cudaMemcpyAsync(H + off_ctrl, Dv + off_ctrl, 64, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY_CAP(cudaMemcpyAsync(H + down_begin, Dv + down_begin, down_end - down_begin, cudaMemcpyDeviceToHost, st));
+    if (use_graph) {
+        cudaGraph_t g = nullptr;
+        CUDA_TRY(cudaStreamEndCapture(st, &g));
+        cudaGraphExecUpdateResultInfo info;
+        if (!s.graph->exec || cudaGraphExecUpdate(s.graph->exec, g, &info) != cudaSuccess) {
+            cudaGetLastError();  // a failed update leaves the runtime's last error set: clear it
+            if (s.graph->exec) cudaGraphExecDestroy(s.graph->exec);
+            s.graph->exec = nullptr;
+            const cudaError_t ie = cudaGraphInstantiate(&s.graph->exec, g, 0);
+            if (ie != cudaSuccess) {
+                cudaGraphDestroy(g);
+                return fail(LCG_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(ie));
+            }
+        }
+        cudaGraphDestroy(g);
+        s.graph->key = key;
+        ++e->last_graph_captures;
+        CUDA_TRY(cudaGraphLaunch(s.graph->exec, st));
+    }
+#undef CUDA_TRY_CAP
     c.in_flight = true;
     e->last_h2d += (long long)down_begin;
     e->last_d2h += 64 + (long long)(down_end - down_begin);
@@ -969,8 +1047,8 @@ lcg_status chunk_finish(lcg_engine e, const Slot &s, const lcg_align_opts *opts,
     *wait_ms += ms_between(t0, t1);
     const char *H = *s.h_stage;
     float ms = 0, ms1 = 0;
-    cudaEventElapsedTime(&ms, s.ev0, s.ev2);
-    cudaEventElapsedTime(&ms1, s.ev0, s.ev1);
+    CUDA_TRY(cudaEventElapsedTime(&ms, s.ev0, s.ev2));
+    CUDA_TRY(cudaEventElapsedTime(&ms1, s.ev0, s.ev1));
     e->last_ms += ms;
     e->last_fill_ms += ms1;
     e->last_trace_ms += ms - ms1;
@@ -1071,6 +1149,7 @@ lcg_status lcg_engine_destroy(lcg_engine e) {
     if (e->ev1) cudaEventDestroy(e->ev1);
     if (e->ev2) cudaEventDestroy(e->ev2);
     if (e->own_stream) cudaStreamDestroy(e->stream);
+    if (e->graph.exec) cudaGraphExecDestroy(e->graph.exec);
     lcg_buffer_set &b = e->alt;
     if (b.stream) cudaStreamSynchronize(b.stream);
     if (b.d_arena) cudaFree(b.d_arena);
@@ -1080,6 +1159,7 @@ lcg_status lcg_engine_destroy(lcg_engine e) {
     if (b.ev1) cudaEventDestroy(b.ev1);
     if (b.ev2) cudaEventDestroy(b.ev2);
     if (b.own_stream) cudaStreamDestroy(b.stream);
+    if (b.graph.exec) cudaGraphExecDestroy(b.graph.exec);
     if (e->env_dev) cudaFree(e->env_dev);
     if (e->env_host) cudaFreeHost(e->env_host);
     lcg_host::pf_release(e);
@@ -1141,8 +1221,18 @@ lcg_status lcg_pair_work(const lcg_pair_tables *pair, const lcg_align_opts *opts
     return LCG_OK;
 }
 
+// length buckets of the autotuner: max(len_a, len_b) <= kTuneBounds[b]
+constexpr int kTuneBounds[LCG_TUNE_BUCKETS - 1] = {128, 224, 320};
+
+static int tune_bucket(int len) {
+    int b = 0;
+    while (b < LCG_TUNE_BUCKETS - 1 && len > kTuneBounds[b]) ++b;
+    return b;
+}
+
 lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t npairs,
                            const lcg_align_opts *opts, lcg_align_result *results) {
+    lcg_align_result *const results_in = results;
     if (!e || !pairs || !opts || !results || npairs < 0) return fail(LCG_ERR_ARG, "NULL argument");
     if (npairs == 0) return LCG_OK;
     CUDA_TRY(cudaSetDevice(e->device));
@@ -1151,7 +1241,46 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
     // with the host between launches)
     const bool modv = opts->normalized || opts->penalized;
     const int per = modv ? npairs : std::max(1, std::min<int>(npairs, chunk_size(npairs, e->chunk_pairs)));
-    const int nchunks = (npairs + per - 1) / per;
+    // the chunks: consecutive runs of at most `per` pairs; with autotune on,
+    // the batch ordered by length bucket (stable) and no chunk spanning two
+    // buckets, each chunk with its bucket's launch configuration
+    struct Plan {
+        int q0, nq, bps;
+        double wave_mb;
+    };
+    std::vector<Plan> plan;
+    std::vector<int> perm;
+    std::vector<lcg_pair_tables> pairs_p;
+    std::vector<lcg_align_result> results_p;
+    const bool tuned = e->autotune && !modv;
+    if (tuned) {
+        perm.resize(npairs);
+        std::vector<int> bucket(npairs);
+        for (int q = 0; q < npairs; ++q) {
+            perm[q] = q;
+            bucket[q] = tune_bucket(std::max(pairs[q].len_a, pairs[q].len_b));
+        }
+        std::stable_sort(perm.begin(), perm.end(), [&](int x, int y) { return bucket[x] < bucket[y]; });
+        pairs_p.resize(npairs);
+        results_p.resize(npairs);
+        for (int q = 0; q < npairs; ++q) {
+            pairs_p[q] = pairs[perm[q]];
+            results_p[q] = results[perm[q]];
+        }
+        for (int q0 = 0; q0 < npairs;) {
+            const int b = bucket[perm[q0]];
+            int q1 = q0;
+            while (q1 < npairs && q1 - q0 < per && bucket[perm[q1]] == b) ++q1;
+            plan.push_back({q0, q1 - q0, e->tune_bps[b], e->tune_wave_mb[b]});
+            q0 = q1;
+        }
+        pairs = pairs_p.data();
+        results = results_p.data();
+    } else {
+        for (int q0 = 0; q0 < npairs; q0 += per)
+            plan.push_back({q0, std::min(per, npairs - q0), e->force_bps, e->force_wave_mb});
+    }
+    const int nchunks = (int)plan.size();
     if (nchunks > 1) {
         lcg_status st = ensure_alt(e);
         if (st != LCG_OK) return st;
@@ -1161,6 +1290,7 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
     e->last_h2d = e->last_d2h = 0;
     e->last_groups = e->last_cells = 0;
     e->last_terms = e->last_visits = -1;
+    e->last_graph_captures = e->last_graph_replays = 0;
     double t_prep = 0, t_pack = 0, t_wait = 0, t_res = 0;
 
     // Pipeline over chunks of pairs on two buffer sets: the host prepares
@@ -1170,7 +1300,7 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
     std::vector<Prep> next;
     lcg_status rc = LCG_OK;
     for (int k = 0; k < nchunks && rc == LCG_OK; ++k) {
-        const int q0 = k * per, nq = std::min(per, npairs - q0);
+        const int q0 = plan[k].q0, nq = plan[k].nq;
         const auto a = clk::now();
         next.clear();
         next.resize(nq);
@@ -1189,6 +1319,8 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
         c.prep.swap(next);
         c.q0 = q0;
         c.nq = nq;
+        c.bps = plan[k].bps;
+        c.wave_mb = plan[k].wave_mb;
         rc = chunk_launch(e, s, pairs, opts, c, &t_pack);
     }
     // the chunks still in flight, in batch order; after an error only wait
@@ -1212,6 +1344,92 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
     e->last_phase_ms[1] = t_pack;
     e->last_phase_ms[2] = t_wait;
     e->last_phase_ms[3] = t_res;
+    if (tuned && rc == LCG_OK)
+        for (int q = 0; q < npairs; ++q) results_in[perm[q]] = results_p[q];
+    return rc;
+}
+
+lcg_status lcg_engine_set_graphs(lcg_engine e, int32_t on) {
+    if (!e) return fail(LCG_ERR_ARG, "NULL argument");
+    e->graphs = on != 0;
+    return LCG_OK;
+}
+
+lcg_status lcg_engine_last_graphs(lcg_engine e, int64_t *captures, int64_t *replays) {
+    if (!e || !captures || !replays) return fail(LCG_ERR_ARG, "NULL argument");
+    *captures = e->last_graph_captures;
+    *replays = e->last_graph_replays;
+    return LCG_OK;
+}
+
+lcg_status lcg_engine_set_autotune(lcg_engine e, int32_t on) {
+    if (!e) return fail(LCG_ERR_ARG, "NULL argument");
+    e->autotune = on != 0;
+    return LCG_OK;
+}
+
+lcg_status lcg_engine_autotune(lcg_engine e, const lcg_pair_tables *pairs, int32_t npairs,
+                               const lcg_align_opts *opts, int32_t sample_pairs, lcg_tune_entry *report) {
+    if (!e || !pairs || !opts || npairs < 0 || sample_pairs < 0) return fail(LCG_ERR_ARG, "NULL argument");
+    if (opts->normalized || opts->penalized || opts->struct_local)
+        return fail(LCG_ERR_UNSUPPORTED, "the autotuner covers the plain and sequence-local fill");
+    const int sample = sample_pairs > 0 ? sample_pairs : 64;
+    lcg_align_opts o = *opts;
+    o.do_trace = 0;
+    // the grid: resident blocks per SM x wave budget (MB); the first entry
+    // is the default configuration
+    const int bps_grid[] = {0, 3, 2};
+    const double wave_grid[] = {0, 4, 16, 64};
+    const bool keep_auto = e->autotune;
+    const int keep_chunk = e->chunk_pairs;
+    e->autotune = false;
+    lcg_status rc = LCG_OK;
+    for (int b = 0; b < LCG_TUNE_BUCKETS && rc == LCG_OK; ++b) {
+        std::vector<int> idx;
+        for (int q = 0; q < npairs; ++q)
+            if (tune_bucket(std::max(pairs[q].len_a, pairs[q].len_b)) == b) idx.push_back(q);
+        lcg_tune_entry ent{};
+        ent.max_len = b + 1 < LCG_TUNE_BUCKETS ? kTuneBounds[b] : INT32_MAX;
+        if (idx.empty()) {
+            ent.blocks_per_sm = e->tune_bps[b];
+            ent.wave_mb = e->tune_wave_mb[b];
+            if (report) report[b] = ent;
+            continue;
+        }
+        std::vector<lcg_pair_tables> tb;
+        const size_t step = std::max<size_t>(1, idx.size() / (size_t)sample);
+        for (size_t k = 0; k < idx.size() && (int)tb.size() < sample; k += step) tb.push_back(pairs[idx[k]]);
+        std::vector<lcg_align_result> res(tb.size());
+        for (auto &r : res) r = lcg_align_result{};
+        e->chunk_pairs = (int)tb.size();
+        double best = 1e300;
+        for (int bi = 0; bi < 3 && rc == LCG_OK; ++bi)
+            for (int wi = 0; wi < 4 && rc == LCG_OK; ++wi) {
+                e->force_bps = bps_grid[bi];
+                e->force_wave_mb = wave_grid[wi];
+                double ms = 1e300;
+                for (int rep = 0; rep < 2 && rc == LCG_OK; ++rep) {  // the first run warms up
+                    rc = lcg_align_pairs(e, tb.data(), (int32_t)tb.size(), &o, res.data());
+                    if (rep == 1) ms = e->last_fill_ms;
+                }
+                ++ent.trials;
+                if (bi == 0 && wi == 0) ent.default_ms = ms;
+                if (ms < best) {
+                    best = ms;
+                    ent.blocks_per_sm = bps_grid[bi];
+                    ent.wave_mb = wave_grid[wi];
+                }
+            }
+        ent.best_ms = best;
+        ent.pairs_sampled = (int32_t)tb.size();
+        e->tune_bps[b] = ent.blocks_per_sm;
+        e->tune_wave_mb[b] = ent.wave_mb;
+        if (report) report[b] = ent;
+    }
+    e->force_bps = 0;
+    e->force_wave_mb = 0;
+    e->chunk_pairs = keep_chunk;
+    e->autotune = keep_auto;
     return rc;
 }
 

@@ -75,10 +75,11 @@ inline double wave_budget_bytes() {
 // kept. Writes (pair, group index) in queue order to out[0 .. total); one
 // counting sort per wave, waves in parallel.
 template <typename BytesOf, typename ParallelFor>
-void queue_order(const std::vector<size_t> &ngroups, BytesOf bytes, int2 *out, ParallelFor pfor) {
+void queue_order(const std::vector<size_t> &ngroups, BytesOf bytes, int2 *out, ParallelFor pfor,
+                 double budget_bytes = 0.0) {
     const int npairs = (int)ngroups.size();
     constexpr size_t NB = 4096;
-    const double budget = wave_budget_bytes();
+    const double budget = budget_bytes > 0.0 ? budget_bytes : wave_budget_bytes();
     std::vector<int> wave_first;  // first pair of each wave
     std::vector<size_t> wave_off;  // first output slot of each wave
     double acc = 0.0;

@@ -4,6 +4,17 @@
 #include <cuda_runtime.h>
 
 #include <cstddef>
+#include <vector>
+
+#include "../../include/locarna_gb300.h"
+
+// The CUDA graph of one buffer set's last chunk (upload, clear, fill,
+// traceback, download) and the launch parameters it was captured with; a
+// chunk with the same parameters replays it.
+struct lcg_graph_cache {
+    cudaGraphExec_t exec = nullptr;
+    std::vector<long long> key;
+};
 
 // Device arena, pinned staging, fill scratch, stream and events of one
 // in-flight chunk of an lcg_align_pairs call. The engine's own fields are
@@ -18,6 +29,7 @@ struct lcg_buffer_set {
     int *d_scratch = nullptr;
     size_t scratch_cap = 0;  // ints
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr;
+    lcg_graph_cache graph;
 };
 
 struct lcg_engine_s {
@@ -45,6 +57,20 @@ struct lcg_engine_s {
     // second buffer set (created on first use)
     int chunk_pairs = 0;
     lcg_buffer_set alt;
+    // autotuner (lcg_engine_autotune): per length bucket the fill kernel's
+    // resident blocks per SM (0 = as many as fit) and the L2 budget of a pair
+    // wave in MB (0 = default); used by lcg_align_pairs when autotune is on
+    bool autotune = false;
+    int tune_bps[LCG_TUNE_BUCKETS] = {0, 0, 0, 0};
+    double tune_wave_mb[LCG_TUNE_BUCKETS] = {0, 0, 0, 0};
+    // CUDA graphs of the chunks (lcg_engine_set_graphs): the own set's cache
+    // (the second set keeps its own in `alt`) and the counts of the last call
+    bool graphs = true;
+    lcg_graph_cache graph;
+    long long last_graph_captures = 0, last_graph_replays = 0;
+    // a configuration forced for every chunk (the autotuner's trials)
+    int force_bps = 0;
+    double force_wave_mb = 0;
     // batched table preparation (envelope.cu): device arena and pinned staging
     char *env_dev = nullptr;
     size_t env_dev_cap = 0;

@@ -10,7 +10,8 @@ import threading
 
 import numpy as np
 
-from .abi import (ResultBuffers, lcg_align_opts, lcg_align_result, lcg_pair_tables,
+from .abi import (LCG_TUNE_BUCKETS, ResultBuffers, lcg_align_opts, lcg_align_result, lcg_pair_tables,
+                  lcg_tune_entry,
                   lcg_pf_grad_spec, lcg_pf_opts, lcg_pf_result, lcg_work_counts, make_opts)
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
@@ -71,6 +72,15 @@ def _load_locked(path):
     lib.lcg_engine_last_work.restype = C.c_int32
     lib.lcg_pair_work.argtypes = [C.POINTER(lcg_pair_tables), C.POINTER(lcg_align_opts), C.POINTER(lcg_work_counts)]
     lib.lcg_pair_work.restype = C.c_int32
+    lib.lcg_engine_autotune.argtypes = [C.c_void_p, C.POINTER(lcg_pair_tables), C.c_int32, C.POINTER(lcg_align_opts),
+                                        C.c_int32, C.POINTER(lcg_tune_entry)]
+    lib.lcg_engine_autotune.restype = C.c_int32
+    lib.lcg_engine_set_autotune.argtypes = [C.c_void_p, C.c_int32]
+    lib.lcg_engine_set_autotune.restype = C.c_int32
+    lib.lcg_engine_set_graphs.argtypes = [C.c_void_p, C.c_int32]
+    lib.lcg_engine_set_graphs.restype = C.c_int32
+    lib.lcg_engine_last_graphs.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
+    lib.lcg_engine_last_graphs.restype = C.c_int32
     lib.lcg_pf_opts_default.argtypes = [C.POINTER(lcg_pf_opts)]
     lib.lcg_pf_opts_default.restype = None
     lib.lcg_pf_forward.argtypes = [C.c_void_p, C.POINTER(lcg_pair_tables), C.c_int32, C.POINTER(lcg_pf_opts),
@@ -199,6 +209,29 @@ class Engine:
     def set_chunk_pairs(self, n):
         """Pairs per chunk of lcg_align_pairs' pipeline (0: automatic)."""
         _check(self.lib, self.lib.lcg_engine_set_chunk_pairs(self.h, int(n)))
+
+    def autotune(self, tables, sample_pairs=64, **kw):
+        """lcg_engine_autotune: per length bucket, the measured best launch
+        configuration of the fill (a list of dicts, one per bucket)."""
+        o = make_opts(**kw)
+        n = len(tables)
+        arr = (lcg_pair_tables * n)(*[t.to_c() for t in tables])
+        rep = (lcg_tune_entry * LCG_TUNE_BUCKETS)()
+        _check(self.lib, self.lib.lcg_engine_autotune(self.h, arr, n, C.byref(o), int(sample_pairs), rep))
+        return [dict(max_len=r.max_len, pairs_sampled=r.pairs_sampled, blocks_per_sm=r.blocks_per_sm,
+                     wave_mb=r.wave_mb, best_ms=r.best_ms, default_ms=r.default_ms, trials=r.trials) for r in rep]
+
+    def set_graphs(self, on):
+        _check(self.lib, self.lib.lcg_engine_set_graphs(self.h, int(bool(on))))
+
+    def last_graphs(self):
+        """(captures, replays) of CUDA graphs in the last lcg_align_pairs call."""
+        a, b = C.c_int64(), C.c_int64()
+        _check(self.lib, self.lib.lcg_engine_last_graphs(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def set_autotune(self, on):
+        _check(self.lib, self.lib.lcg_engine_set_autotune(self.h, int(bool(on))))
 
     def set_counting(self, on):
         _check(self.lib, self.lib.lcg_engine_set_counting(self.h, int(bool(on))))

@@ -1,0 +1,67 @@
+"""The autotuner (lcg_engine_autotune / lcg_engine_set_autotune) on a GPU:
+per length bucket a measured launch configuration of the fill; with it on,
+lcg_align_pairs orders the batch by bucket and launches each bucket's chunks
+with its configuration, and every pair's result is the same as without it
+(and the oracle's)."""
+import pytest
+
+from checks import assert_same_result
+from oracle_ffi import oracle_align
+
+
+@pytest.mark.gpu
+def test_autotuned_batches_give_the_same_alignments(engine):
+    from concurrent.futures import ThreadPoolExecutor
+
+    from locarna_gb300.prep import prepare_pair
+    from locarna_gb300.synth import make_family
+    fam = make_family(22, 60, 400, 515, q=0.05)
+    pp = [r.to_pp() for r in fam]
+    pairs = [(a, b) for a in range(len(fam)) for b in range(a + 1, len(fam))]
+    with ThreadPoolExecutor(8) as ex:
+        tables = list(ex.map(lambda ab: prepare_pair(pp[ab[0]], pp[ab[1]]), pairs))
+    report = engine.autotune(tables, sample_pairs=12)
+    assert len(report) == 4
+    used = [r for r in report if r["pairs_sampled"] > 0]
+    assert len(used) >= 3
+    for r in used:
+        assert r["trials"] == 12 and r["best_ms"] <= r["default_ms"]
+        assert r["blocks_per_sm"] in (0, 2, 3) and r["wave_mb"] in (0, 4, 16, 64)
+    base = engine.align_pairs(tables)
+    try:
+        engine.set_autotune(True)
+        tuned = engine.align_pairs(tables)
+        assert engine.last_stats()[1] >= 2 * len(used)  # at least one chunk per bucket
+    finally:
+        engine.set_autotune(False)
+    for k, (a, b) in enumerate(zip(tuned, base)):
+        assert_same_result(a, b, f"pair {k}")
+    for k in range(0, len(tables), 37):
+        assert_same_result(tuned[k], oracle_align(tables[k]), f"pair {k} vs oracle")
+
+
+@pytest.mark.gpu
+def test_chunks_replay_their_cuda_graph(engine):
+    """lcg_align_pairs records each chunk's device work as a CUDA graph and
+    replays it for a chunk with the same launch parameters; results equal the
+    directly launched ones."""
+    from golden_io import Golden, sankoff_golden_names
+    gs = [Golden(n) for n in sankoff_golden_names() if n.startswith(("c150_g", "c150_b", "c200", "h150_g"))]
+    tabs = [g.tables for g in gs] * 8
+    try:
+        engine.set_graphs(False)
+        direct = engine.align_pairs(tabs)
+        assert engine.last_graphs() == (0, 0)
+        engine.set_graphs(True)
+        call = engine.prepare_call(tabs)
+        engine.run_call(call)
+        first = engine.last_graphs()
+        engine.run_call(call)
+        again = engine.last_graphs()
+        res = engine.decode_call(call)
+    finally:
+        engine.set_graphs(True)
+    assert first[0] >= 1
+    assert again[1] >= 1 and again[0] == 0
+    for k, (a, b) in enumerate(zip(res, direct)):
+        assert_same_result(a, b, f"pair {k}")
