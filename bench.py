@@ -526,6 +526,10 @@ def run_ours(args):
             f"({table_prep['host_envelopes']} host envelopes)")
     call = eng.prepare_call(tables)
 
+    # the autotuner on this workload (per length bucket, outside the timed
+    # region), reported; the timed runs use the library's default launch (one
+    # persistent fill over the whole batch), which the tuner finds as fast
+    tune = eng.autotune(tables, sample_pairs=64) if extras else None
     # measurement-only runs (outside the timed region): work counts
     eng.set_counting(True)
     eng.run_call(call)
@@ -599,6 +603,7 @@ def run_ours(args):
         phases = [a + b for a, b in zip(phases, eng.last_phases())]
         e2e_launches += eng.last_stats()[1] + 1  # + the envelope launch
     barrier_sync(world)
+    graph_captures, graph_replays = eng.last_graphs()
     res = []
     for k, b in enumerate(bufs):
         b.c = cres[k]
@@ -652,6 +657,7 @@ def run_ours(args):
                 "what": "PP texts -> alignments: lcg_prepare_pairs (parsing, scoring, arc matches, GPU "
                         "envelopes) + lcg_align_pairs (default chunk pipeline), all copies inside",
                 "table_prep_ms_per_step": prep_s / args.steps * 1e3,
+                "cuda_graphs_last_step": {"captures": graph_captures, "replays": graph_replays},
                 "gpu_launches": e2e_launches,
                 "align_phases_ms_per_step": dict(zip(("host_prep", "pack", "host_waits_for_device", "results"),
                                                      (x / args.steps for x in phases)))},
@@ -669,6 +675,10 @@ def run_ours(args):
                     "groups": work["groups"]},
         "clocks": clocks,
     }
+    if tune is not None:
+        out["autotune"] = {"buckets": tune, "note": "per length bucket the measured fastest (resident fill blocks per "
+                           "SM, pair-wave L2 MB) of 12 on a 64-pair sample; 0 = the default (as many blocks as fit, "
+                           "8 MB); value and e2e use the default launch"}
     if extras:
         out["cpu_baseline"] = {"value": cpu_rate, "unit": "aligns/s", "cores": cores, "kind": "port",
                                "sample": f"{cpu_done} random workload pairs, PP files to alignments by "

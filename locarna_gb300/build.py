@@ -47,7 +47,11 @@ def _newer(target, deps):
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def build_engine(verbose=False, force=False):
+def build_engine(verbose=False, force=False, out=None, defs=None):
+    """liblocarna_gb300.so in `out` (default the package's _build) with the
+    extra defines `defs` (default $LCG_NVCC_DEFS)."""
+    OUT = out or globals()["OUT"]
+    EXTRA_DEFS = defs if defs is not None else globals()["EXTRA_DEFS"]
     os.makedirs(OUT, exist_ok=True)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h", ".hh"))]
     headers.append(os.path.join(ROOT, "include", "locarna_gb300.h"))

@@ -438,6 +438,12 @@ lcg_status prep_pair(const lcg_pair_tables &t, const lcg_align_opts &o, Prep &p)
         }
         s = e;
     }
+#ifdef LCG_TEST_DROP_LAST_D_WRITE
+    // test build only (tests/test_zy_wait_timeout.py): the last group's last
+    // D write is moved to a row the group never reaches, so that entry stays
+    // NOT_READY and the top level's bounded wait for it runs out
+    if (!p.dw.empty()) p.dw.back().y = INT_MAX;
+#endif
     // byleft is sorted by (al*(m+1)+bl) descending = al descending, bl descending
     GroupItem top{};
     top.al = 0;
@@ -900,8 +906,12 @@ lcg_status chunk_launch(lcg_engine e, const Slot &s, const lcg_pair_tables *all,
         key = {(long long)(uintptr_t)Dv, (long long)(uintptr_t)H, (long long)(uintptr_t)scratch, (long long)down_begin,
                (long long)down_end, (long long)off_ctrl, (long long)off_pairs, (long long)off_queue, (long long)nitems,
                blocks, sw, rb, stride, fast, e->counting, sl, opts->do_trace, npairs};
-        if (s.graph->exec && s.graph->key == key) {
-            CUDA_TRY(cudaGraphLaunch(s.graph->exec, st));
+        lcg_graph_cache::Entry *hit = nullptr;
+        for (auto &x : s.graph->entries)
+            if (x.key == key) hit = &x;
+        if (hit) {
+            hit->used = ++s.graph->clock;
+            CUDA_TRY(cudaGraphLaunch(hit->exec, st));
             ++e->last_graph_replays;
             c.launches = opts->do_trace ? 2 : 1;
             c.off_pairs = off_pairs;
@@ -989,21 +999,35 @@ lcg_status chunk_launch(lcg_engine e, const Slot &s, const lcg_pair_tables *all,
     if (use_graph) {
         cudaGraph_t g = nullptr;
         CUDA_TRY(cudaStreamEndCapture(st, &g));
+        // a new entry, or the least recently used one updated in place
+        // (re-instantiated when the update is refused)
+        auto &ents = s.graph->entries;
+        lcg_graph_cache::Entry *slot = nullptr;
+        if ((int)ents.size() < lcg_graph_cache::kGraphCache) {
+            ents.emplace_back();
+            slot = &ents.back();
+        } else {
+            slot = &ents[0];
+            for (auto &x : ents)
+                if (x.used < slot->used) slot = &x;
+        }
         cudaGraphExecUpdateResultInfo info;
-        if (!s.graph->exec || cudaGraphExecUpdate(s.graph->exec, g, &info) != cudaSuccess) {
-            cudaGetLastError();  // a failed update leaves the runtime's last error set: clear it
-            if (s.graph->exec) cudaGraphExecDestroy(s.graph->exec);
-            s.graph->exec = nullptr;
-            const cudaError_t ie = cudaGraphInstantiate(&s.graph->exec, g, 0);
+        if (!slot->exec || cudaGraphExecUpdate(slot->exec, g, &info) != cudaSuccess) {
+            cudaGetLastError();  // a refused update leaves the runtime's last error set: clear it
+            if (slot->exec) cudaGraphExecDestroy(slot->exec);
+            slot->exec = nullptr;
+            const cudaError_t ie = cudaGraphInstantiate(&slot->exec, g, 0);
             if (ie != cudaSuccess) {
                 cudaGraphDestroy(g);
+                ents.erase(ents.begin() + (slot - ents.data()));
                 return fail(LCG_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(ie));
             }
         }
         cudaGraphDestroy(g);
-        s.graph->key = key;
+        slot->key = key;
+        slot->used = ++s.graph->clock;
         ++e->last_graph_captures;
-        CUDA_TRY(cudaGraphLaunch(s.graph->exec, st));
+        CUDA_TRY(cudaGraphLaunch(slot->exec, st));
     }
 #undef CUDA_TRY_CAP
     c.in_flight = true;
@@ -1149,7 +1173,6 @@ lcg_status lcg_engine_destroy(lcg_engine e) {
     if (e->ev1) cudaEventDestroy(e->ev1);
     if (e->ev2) cudaEventDestroy(e->ev2);
     if (e->own_stream) cudaStreamDestroy(e->stream);
-    if (e->graph.exec) cudaGraphExecDestroy(e->graph.exec);
     lcg_buffer_set &b = e->alt;
     if (b.stream) cudaStreamSynchronize(b.stream);
     if (b.d_arena) cudaFree(b.d_arena);
@@ -1159,7 +1182,6 @@ lcg_status lcg_engine_destroy(lcg_engine e) {
     if (b.ev1) cudaEventDestroy(b.ev1);
     if (b.ev2) cudaEventDestroy(b.ev2);
     if (b.own_stream) cudaStreamDestroy(b.stream);
-    if (b.graph.exec) cudaGraphExecDestroy(b.graph.exec);
     if (e->env_dev) cudaFree(e->env_dev);
     if (e->env_host) cudaFreeHost(e->env_host);
     lcg_host::pf_release(e);

@@ -8,12 +8,23 @@
 
 #include "../../include/locarna_gb300.h"
 
-// The CUDA graph of one buffer set's last chunk (upload, clear, fill,
-// traceback, download) and the launch parameters it was captured with; a
-// chunk with the same parameters replays it.
+// The CUDA graphs of one buffer set's chunks (upload, clear, fill,
+// traceback, download), each with the launch parameters it was captured
+// with; a chunk with the parameters of a cached graph replays it. At most
+// kGraphCache graphs, the least recently used replaced.
 struct lcg_graph_cache {
-    cudaGraphExec_t exec = nullptr;
-    std::vector<long long> key;
+    static constexpr int kGraphCache = 16;
+    struct Entry {
+        cudaGraphExec_t exec = nullptr;
+        std::vector<long long> key;
+        long long used = 0;
+    };
+    std::vector<Entry> entries;
+    long long clock = 0;
+    ~lcg_graph_cache() {
+        for (auto &x : entries)
+            if (x.exec) cudaGraphExecDestroy(x.exec);
+    }
 };
 
 // Device arena, pinned staging, fill scratch, stream and events of one

@@ -27,7 +27,12 @@ constexpr int FILL_WARPS = LCG_FILL_WARPS;  // warps per block of the fill kerne
 __host__ __device__ inline int smem_warp_ints(int rb) { return 5 * rb + 256; }
 constexpr int FILL_MIN_BLOCKS = LCG_FILL_MIN_BLOCKS;  // resident blocks per SM the register budget targets
 constexpr int TRACE_WARPS = 4;  // warps per block of the trace kernel
-constexpr long long SPIN_LIMIT = 1ll << 22;  // ~ seconds of polling, then ST_TIMEOUT
+// polls of a bounded device wait (~ seconds), then ST_TIMEOUT; a test build
+// shortens it (LCG_SPIN_LIMIT)
+#ifndef LCG_SPIN_LIMIT
+#define LCG_SPIN_LIMIT (1ll << 22)
+#endif
+constexpr long long SPIN_LIMIT = LCG_SPIN_LIMIT;
 
 __device__ __forceinline__ int addc(int x, int y) {
     // saturating add of two values >= 2*NEG; result clamped to >= NEG

@@ -76,6 +76,8 @@ __global__ void __launch_bounds__(TRACE_WARPS * 32)
     const int pair = sel.items ? sel.items[wi] : wi;
     const PairDev &P = pairs[pair];
     if (!(P.flags & PF_TRACE)) return;
+    // a fill that gave up (bounded wait) left the matrices incomplete: no walk
+    if (*(volatile int *)status & ST_TIMEOUT) return;
     const int lam = sel.lam ? sel.lam[pair] : 0;
     const int sbase = warp * smem_warp_ints(rb);
     int *Mg = scratch + (long long)pair * scratch_stride;
