@@ -466,6 +466,17 @@ lcg_status lcg_prepare_pair(const char *pp_a, const char *pp_b, const lcg_prep_o
 lcg_status lcg_prepare_pairs(lcg_engine eng, const char *const *pp_a, const char *const *pp_b,
                              int32_t npairs, const lcg_prep_opts *opts, lcg_prepared *out,
                              int32_t *host_envelopes);
+/* PP texts in, alignments out: lcg_prepare_pairs + lcg_align_pairs as one
+ * pipeline. The inputs, bands and sequence envelopes of all pairs are
+ * computed first (the envelopes in one GPU launch); then, chunk by chunk of
+ * lcg_align_pairs' pipeline, the host builds a chunk's tables while the
+ * device aligns the previous chunk. results[q] as for lcg_align_pairs, with
+ * edge buffers for the PP sequences' lengths (2 (len_a + len_b) int32) and
+ * traced_am buffers of min(len_a, len_b) int32. This is what the locarna
+ * command line does per pair (src/locarna.cc:398-785), for a batch. */
+lcg_status lcg_align_pp_pairs(lcg_engine eng, const char *const *pp_a, const char *const *pp_b, int32_t npairs,
+                              const lcg_prep_opts *prep_opts, const lcg_align_opts *opts,
+                              lcg_align_result *results, int32_t *host_envelopes);
 /* Views into the prepared tables; valid until lcg_prepared_free. */
 lcg_status lcg_prepared_tables(lcg_prepared p, lcg_pair_tables *out);
 /* which: 0 sequence A, 1 sequence B, 2 name A, 3 name B */

@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <functional>
 #include <atomic>
 #include <cstdio>
 #include <chrono>
@@ -1252,8 +1253,12 @@ static int tune_bucket(int len) {
     return b;
 }
 
-lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t npairs,
-                           const lcg_align_opts *opts, lcg_align_result *results) {
+// The chunk pipeline of lcg_align_pairs. ready(q0, nq), when given, is called
+// before a chunk's host preparation and makes pairs[q0 .. q0+nq) valid (the
+// tables of lcg_align_pp_pairs are built chunk by chunk, while the device
+// aligns the previous chunk).
+static lcg_status align_impl(lcg_engine e, const lcg_pair_tables *pairs, int32_t npairs, const lcg_align_opts *opts,
+                             lcg_align_result *results, const std::function<lcg_status(int, int)> *ready) {
     lcg_align_result *const results_in = results;
     if (!e || !pairs || !opts || !results || npairs < 0) return fail(LCG_ERR_ARG, "NULL argument");
     if (npairs == 0) return LCG_OK;
@@ -1274,7 +1279,7 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
     std::vector<int> perm;
     std::vector<lcg_pair_tables> pairs_p;
     std::vector<lcg_align_result> results_p;
-    const bool tuned = e->autotune && !modv;
+    const bool tuned = e->autotune && !modv && !ready;
     if (tuned) {
         perm.resize(npairs);
         std::vector<int> bucket(npairs);
@@ -1324,6 +1329,10 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
     for (int k = 0; k < nchunks && rc == LCG_OK; ++k) {
         const int q0 = plan[k].q0, nq = plan[k].nq;
         const auto a = clk::now();
+        if (ready) {
+            rc = (*ready)(q0, nq);
+            if (rc != LCG_OK) break;
+        }
         next.clear();
         next.resize(nq);
         lcg_host::parallel_for(nq, [&](int q) { prep_pair(pairs[q0 + q], *opts, next[q]); });
@@ -1368,6 +1377,34 @@ lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
     e->last_phase_ms[3] = t_res;
     if (tuned && rc == LCG_OK)
         for (int q = 0; q < npairs; ++q) results_in[perm[q]] = results_p[q];
+    return rc;
+}
+
+lcg_status lcg_align_pairs(lcg_engine e, const lcg_pair_tables *pairs, int32_t npairs,
+                           const lcg_align_opts *opts, lcg_align_result *results) {
+    return align_impl(e, pairs, npairs, opts, results, nullptr);
+}
+
+lcg_status lcg_align_pp_pairs(lcg_engine e, const char *const *pp_a, const char *const *pp_b, int32_t npairs,
+                              const lcg_prep_opts *popts, const lcg_align_opts *opts, lcg_align_result *results,
+                              int32_t *host_envelopes) {
+    if (!e || !pp_a || !pp_b || !opts || !results || npairs < 0) return fail(LCG_ERR_ARG, "NULL argument");
+    if (npairs == 0) return LCG_OK;
+    CUDA_TRY(cudaSetDevice(e->device));
+    lcg_host::StagedBatch *B = nullptr;
+    lcg_status rc = lcg_host::stage_batch(e, pp_a, pp_b, npairs, popts, &B, host_envelopes);
+    if (rc != LCG_OK) return rc;
+    std::vector<lcg_prepared> handles((size_t)npairs, nullptr);
+    std::vector<lcg_pair_tables> tabs((size_t)npairs);
+    const std::function<lcg_status(int, int)> ready = [&](int q0, int nq) {
+        lcg_status r = lcg_host::finish_tables(B, q0, nq, handles.data() + q0);
+        for (int q = q0; q < q0 + nq && r == LCG_OK; ++q) r = lcg_prepared_tables(handles[q], &tabs[q]);
+        return r;
+    };
+    rc = align_impl(e, tabs.data(), npairs, opts, results, &ready);
+    for (auto h : handles)
+        if (h) lcg_prepared_free(h);
+    lcg_host::free_batch(B);
     return rc;
 }
 

@@ -56,6 +56,14 @@ lcg_status prep_pair(const lcg_pair_tables &t, const lcg_align_opts &o, Prep &p)
 
 void set_error(const std::string &msg);
 
+// the two stages of lcg_prepare_pairs (host_prep.cpp): inputs, bands and
+// envelopes of every pair; then the tables of pairs [q0, q0 + nq)
+struct StagedBatch;
+lcg_status stage_batch(lcg_engine eng, const char *const *pp_a, const char *const *pp_b, int32_t npairs,
+                       const lcg_prep_opts *opts, StagedBatch **out, int32_t *host_envelopes);
+lcg_status finish_tables(StagedBatch *B, int q0, int nq, lcg_prepared *out);
+void free_batch(StagedBatch *B);
+
 // ring size of the kernels' shared-memory rows for a set of pairs: the
 // smallest multiple of 32 >= every pair's span
 inline int ring_size(int span) { return (std::max(span, 32) + 31) / 32 * 32; }

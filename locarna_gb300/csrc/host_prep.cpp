@@ -1121,20 +1121,35 @@ void guarded(Staged &S, F &&fn) {
 
 }  // namespace
 
-lcg_status lcg_prepare_pairs(lcg_engine eng, const char *const *pp_a, const char *const *pp_b, int32_t npairs,
-                             const lcg_prep_opts *opts, lcg_prepared *out, int32_t *host_envelopes) {
+namespace lcg_host {
+
+// A batch of pairs between the two stages of lcg_prepare_pairs: inputs read,
+// bands and envelopes done for every pair (stage_batch); the tables built for
+// a range of pairs at a time (finish_tables), so that a caller can build the
+// tables of one chunk while the device aligns the previous one.
+struct StagedBatch {
+    std::vector<Staged> st;
+};
+
+lcg_status stage_batch(lcg_engine eng, const char *const *pp_a, const char *const *pp_b, int32_t npairs,
+                       const lcg_prep_opts *opts, StagedBatch **out, int32_t *host_envelopes) {
     if (!eng || !pp_a || !pp_b || !out || npairs < 0) {
         lcg_host::set_error("NULL argument");
         return LCG_ERR_ARG;
     }
+    *out = nullptr;
     if (host_envelopes) *host_envelopes = 0;
     lcg_env::reset_transfer(eng);
-    for (int q = 0; q < npairs; ++q) out[q] = nullptr;
-    if (npairs == 0) return LCG_OK;
+    auto B = std::make_unique<StagedBatch>();
+    if (npairs == 0) {
+        *out = B.release();
+        return LCG_OK;
+    }
     lcg_prep_opts o;
     if (opts) o = *opts;
     else lcg_prep_opts_default(&o);
-    std::vector<Staged> st(npairs);
+    std::vector<Staged> &st = B->st;
+    st.resize(npairs);
     for (auto &S : st) S.o = o;
     for (int q = 0; q < npairs; ++q)
         if (!pp_a[q] || !pp_b[q]) {
@@ -1256,14 +1271,38 @@ lcg_status lcg_prepare_pairs(lcg_engine eng, const char *const *pp_a, const char
             });
         });
     }
-    host_parallel(npairs, [&](int q) { guarded(st[q], [&]() { stage_tables(st[q]); }); });
-    for (int q = 0; q < npairs; ++q)
-        if (st[q].code != LCG_OK) {
-            lcg_host::set_error("pair " + std::to_string(q) + ": " + st[q].err);
-            return st[q].code;
-        }
-    for (int q = 0; q < npairs; ++q) out[q] = st[q].P.release();
+    *out = B.release();
     return LCG_OK;
+}
+
+lcg_status finish_tables(StagedBatch *B, int q0, int nq, lcg_prepared *out) {
+    std::vector<Staged> &st = B->st;
+    host_parallel(nq, [&](int k) { guarded(st[q0 + k], [&]() { stage_tables(st[q0 + k]); }); });
+    for (int k = 0; k < nq; ++k)
+        if (st[q0 + k].code != LCG_OK) {
+            lcg_host::set_error("pair " + std::to_string(q0 + k) + ": " + st[q0 + k].err);
+            return st[q0 + k].code;
+        }
+    for (int k = 0; k < nq; ++k) out[k] = st[q0 + k].P.release();
+    return LCG_OK;
+}
+
+void free_batch(StagedBatch *B) { delete B; }
+
+}  // namespace lcg_host
+
+lcg_status lcg_prepare_pairs(lcg_engine eng, const char *const *pp_a, const char *const *pp_b, int32_t npairs,
+                             const lcg_prep_opts *opts, lcg_prepared *out, int32_t *host_envelopes) {
+    if (!eng || !pp_a || !pp_b || !out || npairs < 0) {
+        lcg_host::set_error("NULL argument");
+        return LCG_ERR_ARG;
+    }
+    for (int q = 0; q < npairs; ++q) out[q] = nullptr;
+    lcg_host::StagedBatch *B = nullptr;
+    lcg_status rc = lcg_host::stage_batch(eng, pp_a, pp_b, npairs, opts, &B, host_envelopes);
+    if (rc == LCG_OK) rc = lcg_host::finish_tables(B, 0, npairs, out);
+    lcg_host::free_batch(B);
+    return rc;
 }
 
 lcg_status lcg_prepared_tables(lcg_prepared p, lcg_pair_tables *t) {

@@ -77,6 +77,10 @@ def _load_locked(path):
     lib.lcg_engine_autotune.restype = C.c_int32
     lib.lcg_engine_set_autotune.argtypes = [C.c_void_p, C.c_int32]
     lib.lcg_engine_set_autotune.restype = C.c_int32
+    lib.lcg_align_pp_pairs.argtypes = [C.c_void_p, C.POINTER(C.c_char_p), C.POINTER(C.c_char_p), C.c_int32,
+                                       C.c_void_p, C.POINTER(lcg_align_opts), C.POINTER(lcg_align_result),
+                                       C.POINTER(C.c_int32)]
+    lib.lcg_align_pp_pairs.restype = C.c_int32
     lib.lcg_engine_set_graphs.argtypes = [C.c_void_p, C.c_int32]
     lib.lcg_engine_set_graphs.restype = C.c_int32
     lib.lcg_engine_last_graphs.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
@@ -158,6 +162,37 @@ class Engine:
         call = self.prepare_call(tables, opts, **kw)
         self.run_call(call)
         return self.decode_call(call)
+
+    def prepare_pp_call(self, pp_pairs, lens, prep=None, **kw):
+        """Arguments of lcg_align_pp_pairs built once: the PP texts, the
+        preparation options (a lcg_prep_opts, None = defaults), the alignment
+        options and result buffers for the pairs' sequence lengths
+        lens[q] = (len_a, len_b)."""
+        n = len(pp_pairs)
+        enc = [(a.encode(), b.encode()) for a, b in pp_pairs]
+        arr_a = (C.c_char_p * n)(*[a for a, _ in enc])
+        arr_b = (C.c_char_p * n)(*[b for _, b in enc])
+        bufs = [ResultBuffers(la, lb) for la, lb in lens]
+        res = (lcg_align_result * n)(*[b.c for b in bufs])
+        return (arr_a, arr_b, n, prep, make_opts(**kw), res, bufs, enc)
+
+    def run_pp_call(self, call):
+        """One lcg_align_pp_pairs call; returns the number of host envelopes."""
+        arr_a, arr_b, n, prep, opts, res, _, _ = call
+        nhost = C.c_int32()
+        _check(self.lib, self.lib.lcg_align_pp_pairs(self.h, arr_a, arr_b, n,
+                                                      C.byref(prep) if prep is not None else None,
+                                                      C.byref(opts), res, C.byref(nhost)))
+        return nhost.value
+
+    @staticmethod
+    def decode_pp_call(call):
+        _, _, _, _, _, res, bufs, _ = call
+        out = []
+        for k, b in enumerate(bufs):
+            b.c = res[k]
+            out.append(b.decode())
+        return out
 
     def align_kbest(self, tables, k, threshold=-1000000, **kw):
         """lcg_align_kbest: per pair the list of its (up to k) hits, each an

@@ -257,3 +257,28 @@ def test_gpu_kbest_normalized_matches_oracle(engine):
         assert len(got[q]) == len(ref), (q, len(got[q]), len(ref))
         for h, (a, b) in enumerate(zip(got[q], ref)):
             assert_same_result(a, b, f"pair {q} hit {h}")
+
+
+@pytest.mark.gpu
+def test_gpu_pp_pipeline_matches_two_calls(engine):
+    """lcg_align_pp_pairs (tables built chunk by chunk while the device aligns
+    the previous chunk) gives what lcg_prepare_pairs + lcg_align_pairs give,
+    in one chunk and in 9-pair chunks."""
+    from locarna_gb300.prep import prepare_pairs
+    from locarna_gb300.synth import make_family
+    fam = make_family(12, 50, 160, 303, q=0.05)
+    pp = [r.to_pp() for r in fam]
+    pp_pairs = [(pp[a], pp[b]) for a in range(len(fam)) for b in range(a + 1, len(fam))]
+    tables, _ = prepare_pairs(engine, pp_pairs)
+    ref = engine.align_pairs(tables)
+    lens = [(t.len_a, t.len_b) for t in tables]
+    try:
+        for chunk in (0, 9):
+            engine.set_chunk_pairs(chunk)
+            call = engine.prepare_pp_call(pp_pairs, lens)
+            engine.run_pp_call(call)
+            got = engine.decode_pp_call(call)
+            for k, (a, b) in enumerate(zip(got, ref)):
+                assert_same_result(a, b, f"pair {k} (chunk {chunk})")
+    finally:
+        engine.set_chunk_pairs(0)
