@@ -727,7 +727,10 @@ lcg_status chunk_launch(lcg_engine e, const Slot &s, const lcg_pair_tables *all,
     const size_t off_mod = (modv || c.kbest) ? take(dev_only, 4ull * 16 * npairs) : 0;
     size_t total = dev_only;
 
+    // the set's graph addresses its arena, staging and scratch: it goes
+    // before any of them is freed
     if (total > *s.arena_cap) {
+        s.graph->release();
         if (*s.d_arena) cudaFree(*s.d_arena);
         *s.d_arena = nullptr;
         *s.arena_cap = 0;
@@ -736,6 +739,7 @@ lcg_status chunk_launch(lcg_engine e, const Slot &s, const lcg_pair_tables *all,
         *s.arena_cap = cap;
     }
     if (down_end > *s.stage_cap) {
+        s.graph->release();
         if (*s.h_stage) cudaFreeHost(*s.h_stage);
         *s.h_stage = nullptr;
         *s.stage_cap = 0;
@@ -886,6 +890,7 @@ lcg_status chunk_launch(lcg_engine e, const Slot &s, const lcg_pair_tables *all,
     size_t trace_slots = (size_t)npairs * (sl ? 8 : 1);
     size_t need = std::max(fill_slots, trace_slots) * (size_t)stride;
     if (need > *s.scratch_cap) {
+        s.graph->release();
         if (*s.d_scratch) cudaFree(*s.d_scratch);
         *s.d_scratch = nullptr;
         *s.scratch_cap = 0;
@@ -907,12 +912,8 @@ lcg_status chunk_launch(lcg_engine e, const Slot &s, const lcg_pair_tables *all,
         key = {(long long)(uintptr_t)Dv, (long long)(uintptr_t)H, (long long)(uintptr_t)scratch, (long long)down_begin,
                (long long)down_end, (long long)off_ctrl, (long long)off_pairs, (long long)off_queue, (long long)nitems,
                blocks, sw, rb, stride, fast, e->counting, sl, opts->do_trace, npairs};
-        lcg_graph_cache::Entry *hit = nullptr;
-        for (auto &x : s.graph->entries)
-            if (x.key == key) hit = &x;
-        if (hit) {
-            hit->used = ++s.graph->clock;
-            CUDA_TRY(cudaGraphLaunch(hit->exec, st));
+        if (s.graph->exec && s.graph->key == key) {
+            CUDA_TRY(cudaGraphLaunch(s.graph->exec, st));
             ++e->last_graph_replays;
             c.launches = opts->do_trace ? 2 : 1;
             c.off_pairs = off_pairs;
@@ -1000,35 +1001,24 @@ lcg_status chunk_launch(lcg_engine e, const Slot &s, const lcg_pair_tables *all,
     if (use_graph) {
         cudaGraph_t g = nullptr;
         CUDA_TRY(cudaStreamEndCapture(st, &g));
-        // a new entry, or the least recently used one updated in place
-        // (re-instantiated when the update is refused)
-        auto &ents = s.graph->entries;
-        lcg_graph_cache::Entry *slot = nullptr;
-        if ((int)ents.size() < lcg_graph_cache::kGraphCache) {
-            ents.emplace_back();
-            slot = &ents.back();
-        } else {
-            slot = &ents[0];
-            for (auto &x : ents)
-                if (x.used < slot->used) slot = &x;
-        }
+        // the set's graph updated in place, or instantiated again when the
+        // update is refused
+        lcg_graph_cache &gc = *s.graph;
         cudaGraphExecUpdateResultInfo info;
-        if (!slot->exec || cudaGraphExecUpdate(slot->exec, g, &info) != cudaSuccess) {
+        if (!gc.exec || cudaGraphExecUpdate(gc.exec, g, &info) != cudaSuccess) {
             cudaGetLastError();  // a refused update leaves the runtime's last error set: clear it
-            if (slot->exec) cudaGraphExecDestroy(slot->exec);
-            slot->exec = nullptr;
-            const cudaError_t ie = cudaGraphInstantiate(&slot->exec, g, 0);
+            gc.release();
+            const cudaError_t ie = cudaGraphInstantiate(&gc.exec, g, 0);
             if (ie != cudaSuccess) {
+                gc.exec = nullptr;
                 cudaGraphDestroy(g);
-                ents.erase(ents.begin() + (slot - ents.data()));
                 return fail(LCG_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(ie));
             }
         }
         cudaGraphDestroy(g);
-        slot->key = key;
-        slot->used = ++s.graph->clock;
+        gc.key = key;
         ++e->last_graph_captures;
-        CUDA_TRY(cudaGraphLaunch(slot->exec, st));
+        CUDA_TRY(cudaGraphLaunch(gc.exec, st));
     }
 #undef CUDA_TRY_CAP
     c.in_flight = true;
@@ -1167,6 +1157,10 @@ lcg_status lcg_engine_destroy(lcg_engine e) {
     if (!e) return LCG_OK;
     cudaSetDevice(e->device);
     if (e->stream) cudaStreamSynchronize(e->stream);
+    if (e->alt.stream) cudaStreamSynchronize(e->alt.stream);
+    // the graphs first: their nodes address the buffers and record the events
+    e->graph.release();
+    e->alt.graph.release();
     if (e->d_arena) cudaFree(e->d_arena);
     if (e->d_scratch) cudaFree(e->d_scratch);
     if (e->h_stage) cudaFreeHost(e->h_stage);

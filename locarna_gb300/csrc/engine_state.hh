@@ -8,22 +8,20 @@
 
 #include "../../include/locarna_gb300.h"
 
-// The CUDA graphs of one buffer set's chunks (upload, clear, fill,
-// traceback, download), each with the launch parameters it was captured
-// with; a chunk with the parameters of a cached graph replays it. At most
-// kGraphCache graphs, the least recently used replaced.
+// The CUDA graph of one buffer set's last chunk (upload, clear, fill,
+// traceback, download) and the launch parameters it was captured with; a
+// chunk with the same parameters replays it, a chunk with other parameters
+// updates it in place (or instantiates it again when the update is
+// refused). release() destroys it: before any buffer of the set that its
+// nodes address is freed, so that no graph ever refers to freed memory, and
+// at engine teardown.
 struct lcg_graph_cache {
-    static constexpr int kGraphCache = 16;
-    struct Entry {
-        cudaGraphExec_t exec = nullptr;
-        std::vector<long long> key;
-        long long used = 0;
-    };
-    std::vector<Entry> entries;
-    long long clock = 0;
-    ~lcg_graph_cache() {
-        for (auto &x : entries)
-            if (x.exec) cudaGraphExecDestroy(x.exec);
+    cudaGraphExec_t exec = nullptr;
+    std::vector<long long> key;
+    void release() {
+        if (exec) cudaGraphExecDestroy(exec);
+        exec = nullptr;
+        key.clear();
     }
 };
 

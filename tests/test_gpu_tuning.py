@@ -65,3 +65,31 @@ def test_chunks_replay_their_cuda_graph(engine):
     assert again[1] >= 1 and again[0] == 0
     for k, (a, b) in enumerate(zip(res, direct)):
         assert_same_result(a, b, f"pair {k}")
+
+
+@pytest.mark.gpu
+def test_graph_across_many_layouts_keeps_results(engine):
+    """70 chunk layouts in a row through one engine (the arena, staging and
+    scratch grow along the way, which drops the buffer set's graph before
+    the old buffers are freed): every new layout is captured, a repeat of
+    the last one replays, and every call aligns like the oracle."""
+    from golden_io import Golden
+    from oracle_ffi import oracle_align
+    from locarna_gb300.engine import Engine
+    gs = [Golden(n) for n in ("c150_global", "c150_b", "c60_short", "c120_opening0")]
+    ref = [oracle_align(g.tables) for g in gs]
+    eng = Engine(0)  # fresh buffers and graphs
+    try:
+        for n in range(1, 71):  # 70 batch sizes = 70 layouts
+            tabs = [gs[k % 4].tables for k in range(n)]
+            res = eng.align_pairs(tabs)
+            assert eng.last_graphs() == (1, 0), n
+            for k, r in enumerate(res):
+                assert_same_result(r, ref[k % 4], f"batch {n} pair {k}")
+            if n % 10 == 0:
+                again = eng.align_pairs(tabs)
+                assert eng.last_graphs() == (0, 1), n
+                for k, r in enumerate(again):
+                    assert_same_result(r, ref[k % 4], f"replay {n} pair {k}")
+    finally:
+        eng.close()
