@@ -655,7 +655,7 @@ def run_ours(args):
                      "peak_source": "measured int32 add+max rate (locarna_gb300/_build/liblcg_probe.so)",
                      "hbm_frac_of_measured": alg_bytes / Tf / 1e9 / peaks.get("hbm_gbs", 6800.0)},
         "int_ops": {"ops_per_step": ops, "cells": work["cells"], "arc_terms": work["arc_terms"],
-                    "groups": work["groups"]},
+                    "arc_candidates_visited": work["visits"], "groups": work["groups"]},
         "clocks": clocks,
     }
     if tune is not None:
@@ -823,8 +823,14 @@ def run_small_case(args):
             eng.run_call(call)
         ms, nl = eng.last_stats()
         f, t = eng.last_timing()
+        work = None
+        if not mode:  # the work counts of the plain mode (a counting launch)
+            eng.set_counting(True)
+            eng.run_call(call)
+            eng.set_counting(False)
+            work = eng.last_work()
         print(json.dumps({"case": args.case, "mode": mode, "pairs": len(tables), "kernel_ms": ms,
-                          "fill_ms": f, "trace_ms": t, "launches": nl}), flush=True)
+                          "fill_ms": f, "trace_ms": t, "launches": nl, "work": work}), flush=True)
     eng.close()
 
 

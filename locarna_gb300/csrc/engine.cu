@@ -554,6 +554,7 @@ struct Chunk {
     int sw = 0, rb = 0;
     long long stride = 0;
     bool sl = false;
+    bool sl_fast = false;  // struct-local fast routines (every pair: class table, no anchors)
     int *scratch = nullptr;
     // launch configuration: resident fill blocks per SM (0 = as many as fit)
     // and the L2 budget of a pair wave in MB (0 = default)
@@ -619,7 +620,7 @@ lcg_status mod_top_levels(const lcg_align_opts *opts, Chunk &c, const PairDev *d
         ts.nitems = ni;
         ts.lam = d_lam;
         ts.flags = TRACE_TOP_ONLY | (iter ? TRACE_KEEP_MIN : 0);
-        if (sl) CUDA_TRY(launch_sl_trace(dpairs, npairs, scratch, stride, sw, status, st, ts));
+        if (sl) CUDA_TRY(launch_sl_trace(dpairs, npairs, scratch, stride, sw, rb, c.sl_fast, status, st, ts));
         else CUDA_TRY(launch_trace(dpairs, npairs, scratch, stride, sw, rb, status, st, ts));
         CUDA_TRY(launch_gather_res(dpairs, d_items, ni, d_res, st));
         c.launches += 3;
@@ -871,12 +872,16 @@ lcg_status chunk_launch(lcg_engine e, const Slot &s, const lcg_pair_tables *all,
     // ---- scratch
     const bool sl = opts->struct_local != 0;
     const int rb = lcg_host::ring_size(span);
-    bool fast = true;
-    for (auto &p : prep)
+    bool fast = true, sl_fast = true;
+    for (auto &p : prep) {
         fast = fast && (p.flags & PF_SCLS) && !(p.flags & (PF_ANCHORS | PF_NOLP | PF_STACK));
+        sl_fast = sl_fast && (p.flags & PF_SCLS) && !(p.flags & PF_ANCHORS);
+    }
+    c.sl_fast = sl_fast;
+    c.rb = rb;
     int blocks_per_sm = 0;
     if (sl) {
-        CUDA_TRY(sl_prepare(sw, rb, &blocks_per_sm));
+        CUDA_TRY(sl_prepare(sw, rb, sl_fast, &blocks_per_sm));
     } else {
         CUDA_TRY(fill_occupancy(rb, e->counting, fast, &blocks_per_sm));
         CUDA_TRY(trace_prepare(rb));
@@ -911,7 +916,7 @@ lcg_status chunk_launch(lcg_engine e, const Slot &s, const lcg_pair_tables *all,
     if (use_graph) {
         key = {(long long)(uintptr_t)Dv, (long long)(uintptr_t)H, (long long)(uintptr_t)scratch, (long long)down_begin,
                (long long)down_end, (long long)off_ctrl, (long long)off_pairs, (long long)off_queue, (long long)nitems,
-               blocks, sw, rb, stride, fast, e->counting, sl, opts->do_trace, npairs};
+               blocks, sw, rb, stride, fast, e->counting, sl, sl_fast, opts->do_trace, npairs};
         if (s.graph->exec && s.graph->key == key) {
             CUDA_TRY(cudaGraphLaunch(s.graph->exec, st));
             ++e->last_graph_replays;
@@ -964,7 +969,7 @@ lcg_status chunk_launch(lcg_engine e, const Slot &s, const lcg_pair_tables *all,
             return fail(LCG_ERR_UNSUPPORTED, "work counting covers the plain mode only");
         }
         CUDA_TRY_CAP(launch_sl_fill((const PairDev *)(Dv + off_pairs), (const int2 *)(Dv + off_queue),
-                                (int)nitems, scratch, stride, sw, rb, qhead,
+                                (int)nitems, scratch, stride, sw, rb, sl_fast, qhead,
                                 status, abort_flag, blocks, st));
     } else {
         CUDA_TRY_CAP(launch_fill((const PairDev *)(Dv + off_pairs), (const int2 *)(Dv + off_queue),
@@ -988,8 +993,8 @@ lcg_status chunk_launch(lcg_engine e, const Slot &s, const lcg_pair_tables *all,
     c.scratch = scratch;
     if ((opts->do_trace || modv) && !c.kbest) {
         if (sl)
-            CUDA_TRY_CAP(launch_sl_trace((const PairDev *)(Dv + off_pairs), npairs, scratch, stride, sw,
-                                     status, st, sel));
+            CUDA_TRY_CAP(launch_sl_trace((const PairDev *)(Dv + off_pairs), npairs, scratch, stride, sw, rb,
+                                     sl_fast, status, st, sel));
         else
             CUDA_TRY_CAP(launch_trace((const PairDev *)(Dv + off_pairs), npairs, scratch, stride, sw, rb, status,
                                   st, sel));
@@ -1541,7 +1546,7 @@ lcg_status lcg_align_kbest(lcg_engine e, const lcg_pair_tables *pairs, int32_t n
         return r;
     };
     auto trace_launch = [&](const TraceSel &ts) -> lcg_status {
-        if (c.sl) CUDA_TRY(launch_sl_trace(dpairs, npairs, c.scratch, c.stride, c.sw, status, st, ts));
+        if (c.sl) CUDA_TRY(launch_sl_trace(dpairs, npairs, c.scratch, c.stride, c.sw, c.rb, c.sl_fast, status, st, ts));
         else CUDA_TRY(launch_trace(dpairs, npairs, c.scratch, c.stride, c.sw, c.rb, status, st, ts));
         return LCG_OK;
     };

@@ -25,11 +25,13 @@ cudaError_t fill_occupancy(int rb, bool counting, bool fast, int *blocks_per_sm)
 cudaError_t trace_prepare(int rb);
 int fill_warps_per_block();
 int trace_warps_per_block();
-cudaError_t sl_prepare(int sw, int rb, int *blocks_per_sm);
+// fast: every pair has a sigma class table and no anchor constraints
+// (run_group_slf); blocks_per_sm = 0 when the shared memory does not fit
+cudaError_t sl_prepare(int sw, int rb, bool fast, int *blocks_per_sm);
 int sl_fill_warps_per_block();
 cudaError_t launch_sl_fill(const PairDev *pairs, const int2 *queue, int nitems, int *scratch,
-                           long long scratch_stride, int sw, int rb, unsigned int *qhead, int *status,
+                           long long scratch_stride, int sw, int rb, bool fast, unsigned int *qhead, int *status,
                            int *abort_flag, int blocks, cudaStream_t st);
 cudaError_t launch_sl_trace(const PairDev *pairs, int npairs, int *scratch, long long scratch_stride, int sw,
-                            int *status, cudaStream_t st, TraceSel sel = TraceSel());
+                            int rb, bool fast, int *status, cudaStream_t st, TraceSel sel = TraceSel());
 }  // namespace lcg

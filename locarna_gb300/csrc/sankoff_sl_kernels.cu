@@ -304,6 +304,350 @@ __device__ void run_group_sl(const PairDev &P, int al, int ar, int bl, int br, i
     }
 }
 
+// shared ints per warp of the fast fill (run_group_slf) for ring size rb:
+// 15 rows of rb and the 16 x 16 sigma class table
+__host__ __device__ inline int slf_warp_ints(int rb) { return 15 * rb + 256; }
+
+// warp inclusive prefix maximum of v, started from the carry c (in: the
+// previous chunk's, out: this chunk's last lane's), normalised
+__device__ __forceinline__ int prefix_max_carry(int v, int &c, int lane) {
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) v = max(v, __shfl_up_sync(0xffffffffu, v, off));
+    v = norm(max(v, c));
+    c = __shfl_sync(0xffffffffu, v, 31);
+    return v;
+}
+
+// F of one state by the prefix-sum form: F(j) = PA(j) + (go - max(go,0)) +
+// max_{k<j} (X(k) - PA(k)), Pc the running maximum of X(k) - PA(k) over the
+// earlier chunks (in) and through this one (out); returns norm(max(X, F)).
+__device__ __forceinline__ int fscan_prefix(int x, int pa, int gdel, int &Pc, int lane) {
+    const int v = x - pa;
+    int w = __shfl_up_sync(0xffffffffu, v, 1);
+    if (lane == 0) w = Pc;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) w = max(w, __shfl_up_sync(0xffffffffu, w, off));
+    Pc = __shfl_sync(0xffffffffu, max(w, v), 31);
+    return norm(max(x, w + pa + gdel));
+}
+
+// One left-end group with exclusions, fast path: pairs without anchor
+// constraints and with a sigma class table (PF_SCLS). Writes NS state
+// matrices to Mg (state s at Mg + s*mstride; NS = 4 in the fill: the states
+// arc terms read; 8 in the traceback recomputation) and, with DWRITE, the
+// group's D entries.
+// The states, their order and values are those of run_group_sl; what
+// differs is how they are computed:
+//  * shared-memory rows are indexed by ring position (column j at j mod
+//    ringn, as in the plain fill) and kept in place: a lane reads its
+//    column's row i-1 value before writing row i's, and the diagonal comes
+//    from the lane to its left by a shuffle (the chunk's last lane carries it
+//    to the next chunk, the old value at lo-1 starts the row);
+//  * the arc-match terms of row i come from the row's candidate list
+//    (PairDev::crow, a.l descending), 32 entries per step for the whole warp,
+//    each valid term M_s(a.l-1, b.l-1) + D(a,b) reduced into its column b.r
+//    of state s with a shared-memory atomicMax;
+//  * with every insertion allowed, the horizontal chains are prefix maxima:
+//    F of NO_NO / X_NO / NO_X / X_X by the prefix-sum form of the plain fill
+//    (PairDev::gbc holds PA(j)), NO_OP / X_OP by a plain prefix maximum.
+// Shared rows (ring length ringn): 0-3 M of NO_NO, X_NO, NO_X, X_X; 4 M of
+// OP_NO; 5 M of OP_X; 6-9 E of 0-3; 10 gap prefix << 4 | column class;
+// 11-14 arc-term maxima of 0-3; then the class table.
+template <bool WAIT, bool DWRITE, int NS>
+__device__ void run_group_slf(const PairDev &P, int al, int ar, int bl, int br, int *__restrict__ Mg,
+                              long long mstride, int pitch, int sbase, int ringn,
+                              const int4 *__restrict__ dw, int ndw, int *status, volatile int *abort_flag) {
+    const int lane = threadIdx.x & 31;
+    const int go = P.go, X = P.excl;
+    const int gop = max(go, 0), gdel = go - gop;
+    const unsigned rmagic = 0xFFFFFFFFu / (unsigned)ringn + 1u;  // j / ringn = umulhi(j, rmagic), j < 2^20
+    int *const R = lcg_smem + sbase;
+#define ROW(k) (R + (k) * ringn)
+#define RG(j) ((j) - ringn * (int)__umulhi((unsigned)(j), rmagic))
+    int *const gBs = ROW(10);
+    int *const Stab = R + 15 * ringn;
+    const int4 *__restrict__ rowinfo = P.rowinfo;
+    const int2 *__restrict__ rowarc = P.rowarc;
+    const int2 *__restrict__ crow = P.crow;
+    int *const Dp = P.D;
+    for (int c = lane; c < ringn; c += 32) {
+#pragma unroll
+        for (int s = 0; s < 4; ++s) ROW(6 + s)[c] = NEG;
+    }
+    for (int k = lane; k < 256; k += 32) Stab[k] = P.scls[k];
+
+    // ---- row al (init_state, aligner.cc:264-368): NO_NO, X_NO, OP_NO get
+    // go + the gap prefix, NO_X, X_X, OP_X the exclusion X; (al, bl) is 0
+    const int L0 = min(br, rowinfo[al].y + 1);
+    const int PAbl = P.gbc[bl] >> 4;
+    for (int j = bl + 1 + lane; j < L0; j += 32) {
+        const int gbcj = P.gbc[j];
+        const int rj = RG(j);
+        gBs[rj] = gbcj;
+        const int vg = go + (gbcj >> 4) - PAbl - (j - bl) * gop;
+        ROW(0)[rj] = vg;
+        ROW(1)[rj] = vg;
+        ROW(4)[rj] = vg;
+        ROW(2)[rj] = X;
+        ROW(3)[rj] = X;
+        ROW(5)[rj] = X;
+        const int c = j - bl;
+        Mg[c] = vg;
+        Mg[mstride + c] = vg;
+        Mg[2 * mstride + c] = X;
+        Mg[3 * mstride + c] = X;
+        if (NS == 8) {
+            Mg[4 * mstride + c] = vg;
+            Mg[5 * mstride + c] = 0;
+            Mg[6 * mstride + c] = X;
+            Mg[7 * mstride + c] = 0;
+        }
+    }
+    if (lane == 0) {
+        const int r0 = RG(bl);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) ROW(k)[r0] = 0;
+#pragma unroll
+        for (int s = 0; s < NS; ++s) Mg[s * mstride] = 0;
+    }
+    // cells above the band of row al+1
+    if (al + 1 < ar) {
+        const int L1 = min(br, rowinfo[al + 1].y + 1);
+        for (int j = L0 + lane; j < L1; j += 32) {
+            const int rj = RG(j);
+#pragma unroll
+            for (int k = 0; k < 6; ++k) ROW(k)[rj] = NEG;
+            gBs[rj] = P.gbc[j];
+        }
+    }
+    __syncwarp();
+
+    int colg = go;  // M(i, bl) of the gap states
+    int dwp = 0;
+    int dw_row = (DWRITE && ndw > 0) ? dw[0].y : INT_MAX;  // D-write lists are by row ascending
+    int4 rnxt = rowinfo[min(al + 1, P.n + 1)];
+    int2 anxt = rowarc[min(al + 1, P.n + 1)];
+    int cnxt = P.rcls[min(al + 1, P.n + 1)];
+    for (int i = al + 1; i < ar; ++i) {
+        const int4 rcur = rnxt;
+        const int2 acur = anxt;
+        const int rcl16 = cnxt * 16;
+        rnxt = rowinfo[min(i + 1, P.n + 1)];
+        anxt = rowarc[min(i + 1, P.n + 1)];
+        cnxt = P.rcls[min(i + 1, P.n + 1)];
+        const int minc = rcur.x;
+        const int gAi = rcur.z;
+        const int lo = max(bl + 1, minc);
+        const int hi = min(br - 1, rcur.y);
+
+        // ---- arc-match terms of row i into rows 11-14 at columns lo..hi
+        bool rowarcs = false;
+        for (int e0 = acur.x; e0 < acur.y; e0 += 32) {
+            const int e = e0 + lane;
+            const int2 en = e < acur.y ? crow[e] : make_int2(0xffff, 0);
+            const int ca = en.x & 0xffff, cbl = en.x >> 16;  // inner corner (a.l-1, b.l-1)
+            const bool okA = ca >= al && ca != 0xffff;       // a.l > al
+            const unsigned ball = __ballot_sync(0xffffffffu, okA);
+            if (ball == 0u) break;
+            if (!rowarcs) {
+                for (int j = lo + lane; j <= hi; j += 32) {
+                    const int rj = RG(j);
+#pragma unroll
+                    for (int s = 0; s < 4; ++s) ROW(11 + s)[rj] = NEG;
+                }
+                __syncwarp();
+                rowarcs = true;
+            }
+            if (okA && cbl >= bl && en.y >= lo && en.y <= hi) {
+                int dv = WAIT ? ld_volatile(Dp + e) : Dp[e];
+                const long long o = (long long)(ca - al) * pitch + (cbl - bl);
+                int mv[4];
+#pragma unroll
+                for (int s = 0; s < 4; ++s) mv[s] = Mg[s * mstride + o];
+                if (WAIT && dv == NOT_READY) dv = wait_D(Dp, e, status, abort_flag);
+                const int rr = RG(en.y);
+#pragma unroll
+                for (int s = 0; s < 4; ++s) atomicMax(&ROW(11 + s)[rr], mv[s] + dv);
+            }
+            if (ball != 0xffffffffu) break;
+        }
+        __syncwarp();
+
+        // ---- column bl (aligner.cc:264-368 by state) and the row's start
+        int B0 = NEG, B1 = NEG, B4 = NEG;  // NO_NO / NO_X / NO_OP; X_NO / X_X / X_OP; OP_NO / OP_X
+        if (minc <= bl) {
+            colg += gAi;
+            B0 = colg;
+            B1 = X;
+            B4 = 0;
+            if (lane == 0) {
+                const long long r = (long long)(i - al) * pitch;
+                Mg[r] = B0;
+                Mg[mstride + r] = B1;
+                Mg[2 * mstride + r] = B0;
+                Mg[3 * mstride + r] = B1;
+                if (NS == 8) {
+                    Mg[4 * mstride + r] = B4;
+                    Mg[5 * mstride + r] = B0;
+                    Mg[6 * mstride + r] = B4;
+                    Mg[7 * mstride + r] = B1;
+                }
+            }
+        }
+        // lane 0: the diagonal carries (row i-1 at column lo-1), then column
+        // lo-1 of row i
+        int dc0 = NEG, dc1 = NEG, dc2 = NEG, dc3 = NEG;
+        if (lane == 0 && lo - 1 < br) {
+            const int r = RG(lo - 1);
+            dc0 = ROW(0)[r];
+            dc1 = ROW(1)[r];
+            dc2 = ROW(2)[r];
+            dc3 = ROW(3)[r];
+            ROW(0)[r] = B0;
+            ROW(1)[r] = B1;
+            ROW(2)[r] = B0;
+            ROW(3)[r] = B1;
+            ROW(4)[r] = B4;
+            ROW(5)[r] = B4;
+        }
+        const int palo = lo - 1 == bl ? PAbl : (gBs[RG(lo - 1)] >> 4);
+        int Pc0 = B0 - palo, Pc1 = B1 - palo, Pc2 = B0 - palo, Pc3 = B1 - palo;
+        int C5 = B0, C7 = B1;  // NO_OP, X_OP carries
+        const long long roff = (long long)(i - al) * pitch - bl;
+        int rbase = RG(lo);
+        for (int base = lo; base <= hi; base += 32) {
+            const int j = base + lane;
+            const bool act = j <= hi;
+            int rj = rbase + lane;  // ring index of column j
+            if (rj >= ringn) rj -= ringn;
+            rbase += 32;
+            if (rbase >= ringn) rbase -= ringn;
+            int gbc = 0, sg = 0;
+            int p0 = NEG, p1 = NEG, p2 = NEG, p3 = NEG, p4 = NEG, p6 = NEG;
+            int x0 = NEG, x1 = NEG, x2 = NEG, x3 = NEG;
+            int e0v = NEG, e1v = NEG, e2v = NEG, e3v = NEG;
+            if (act) {
+                gbc = gBs[rj];
+                sg = Stab[rcl16 + (gbc & 15)];
+                p0 = ROW(0)[rj];
+                p1 = ROW(1)[rj];
+                p2 = ROW(2)[rj];
+                p3 = ROW(3)[rj];
+                p4 = ROW(4)[rj];
+                p6 = ROW(5)[rj];
+                e0v = ROW(6)[rj];
+                e1v = ROW(7)[rj];
+                e2v = ROW(8)[rj];
+                e3v = ROW(9)[rj];
+            }
+            // diagonal M(i-1, j-1) of states 0-3
+            int d0 = __shfl_up_sync(0xffffffffu, p0, 1);
+            int d1 = __shfl_up_sync(0xffffffffu, p1, 1);
+            int d2 = __shfl_up_sync(0xffffffffu, p2, 1);
+            int d3 = __shfl_up_sync(0xffffffffu, p3, 1);
+            if (lane == 0) {
+                d0 = dc0;
+                d1 = dc1;
+                d2 = dc2;
+                d3 = dc3;
+            }
+            dc0 = __shfl_sync(0xffffffffu, p0, 31);
+            dc1 = __shfl_sync(0xffffffffu, p1, 31);
+            dc2 = __shfl_sync(0xffffffffu, p2, 31);
+            dc3 = __shfl_sync(0xffffffffu, p3, 31);
+            if (act) {
+                // vertical gaps and the no-exclusion part of states 0-3
+                e0v = norm(__viaddmax_s32(e0v, gAi, p0 + gAi + go));
+                e1v = norm(__viaddmax_s32(e1v, gAi, p1 + gAi + go));
+                e2v = norm(__viaddmax_s32(e2v, gAi, p2 + gAi + go));
+                e3v = norm(__viaddmax_s32(e3v, gAi, p3 + gAi + go));
+                ROW(6)[rj] = e0v;
+                ROW(7)[rj] = e1v;
+                ROW(8)[rj] = e2v;
+                ROW(9)[rj] = e3v;
+                x0 = max(d0 + sg, e0v);
+                x1 = max(d1 + sg, e1v);
+                x2 = max(d2 + sg, e2v);
+                x3 = max(d3 + sg, e3v);
+                if (rowarcs) {
+                    x0 = max(x0, ROW(11)[rj]);
+                    x1 = max(x1, ROW(12)[rj]);
+                    x2 = max(x2, ROW(13)[rj]);
+                    x3 = max(x3, ROW(14)[rj]);
+                }
+            }
+            const int pa = gbc >> 4;
+            // NO_NO; OP_NO = max(OP_NO above, NO_NO); NO_OP = prefix max of NO_NO
+            const int M0 = fscan_prefix(x0, pa, gdel, Pc0, lane);
+            const int M4 = act ? norm(max(p4, M0)) : NEG;
+            const int M5 = prefix_max_carry(act ? M0 : NEG, C5, lane);
+            // NO_X with NO_OP + X; OP_X = max(OP_X above, NO_X)
+            const int M2 = fscan_prefix(act ? max(x2, M5 + X) : NEG, pa, gdel, Pc2, lane);
+            const int M6 = act ? norm(max(p6, M2)) : NEG;
+            // X_NO with OP_NO + X; X_OP = prefix max of X_NO
+            const int M1 = fscan_prefix(act ? max(x1, M4 + X) : NEG, pa, gdel, Pc1, lane);
+            const int M7 = prefix_max_carry(act ? M1 : NEG, C7, lane);
+            // X_X with OP_X + X and X_OP + X
+            const int M3 = fscan_prefix(act ? max(x3, max(M6 + X, M7 + X)) : NEG, pa, gdel, Pc3, lane);
+            if (act) {
+                ROW(0)[rj] = M0;
+                ROW(1)[rj] = M1;
+                ROW(2)[rj] = M2;
+                ROW(3)[rj] = M3;
+                ROW(4)[rj] = M4;
+                ROW(5)[rj] = M6;
+                Mg[roff + j] = M0;
+                Mg[mstride + roff + j] = M1;
+                Mg[2 * mstride + roff + j] = M2;
+                Mg[3 * mstride + roff + j] = M3;
+                if (NS == 8) {
+                    Mg[4 * mstride + roff + j] = M4;
+                    Mg[5 * mstride + roff + j] = M5;
+                    Mg[6 * mstride + roff + j] = M6;
+                    Mg[7 * mstride + roff + j] = M7;
+                }
+            }
+        }
+        __syncwarp();
+        if (DWRITE && i == dw_row) {
+            // fill_D_entries (struct-local: the best non-open state); without
+            // lonely pairs or with stacking also the inner arc match's term
+            while (dwp < ndw) {
+                const int q = dwp + lane;
+                int4 e = make_int4(0, -1, 0, 0);
+                if (q < ndw) e = dw[q];
+                const bool mine = q < ndw && e.y == i;
+                if (mine) {
+                    const int rz = RG(e.z);
+                    const int mv = max(max(ROW(0)[rz], ROW(1)[rz]), max(ROW(2)[rz], ROW(3)[rz]));
+                    int v = mv + e.w;
+                    if (P.flags & (PF_NOLP | PF_STACK)) v = max(v, inner_term<WAIT>(P, dw + q, status, abort_flag));
+                    st_volatile(Dp + e.x, norm(v));
+                }
+                const int cnt = __popc(__ballot_sync(0xffffffffu, mine));
+                dwp += cnt;
+                if (cnt < 32) break;
+            }
+            dw_row = dwp < ndw ? dw[dwp].y : INT_MAX;
+        }
+        if (i + 1 < ar) {
+            // columns entering the band with row i+1: M above them is -inf,
+            // their E starts at -inf, their gap prefix is staged
+            const int Ln = min(br, rnxt.y + 1);
+            for (int j = max(hi + 1, bl + 1) + lane; j < Ln; j += 32) {
+                const int rj = RG(j);
+#pragma unroll
+                for (int k = 0; k < 10; ++k) ROW(k)[rj] = NEG;
+                gBs[rj] = P.gbc[j];
+            }
+        }
+        __syncwarp();
+    }
+#undef ROW
+#undef RG
+}
+
+template <bool FAST>
 __global__ void __launch_bounds__(SL_FILL_WARPS * 32)
     sankoff_sl_fill_kernel(const PairDev *__restrict__ pairs, const int2 *__restrict__ queue,
                            int nitems, int *scratch,
@@ -312,7 +656,7 @@ __global__ void __launch_bounds__(SL_FILL_WARPS * 32)
     extern __shared__ int smem[];
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
-    int *sm = smem + warp * sl_warp_ints(sw, rb);
+    int *sm = smem + warp * (FAST ? slf_warp_ints(rb) : sl_warp_ints(sw, rb));
     // 4 state matrices per warp slot
     int *Mg = scratch + ((long long)blockIdx.x * SL_FILL_WARPS + warp) * scratch_stride * 4;
     volatile int *abort_flag = abort_flag_ptr;
@@ -328,6 +672,9 @@ __global__ void __launch_bounds__(SL_FILL_WARPS * 32)
         if (it.top) {
             const int base = (int)(sm - smem);
             run_top<false>(P, it.cpl, base, rb, status, abort_flag, nullptr);
+        } else if (FAST) {
+            run_group_slf<true, true, 4>(P, it.al, it.ar, it.bl, it.br, Mg, scratch_stride, sw, (int)(sm - smem), rb,
+                                dw + it.dw_start, it.dw_count, status, abort_flag);
         } else {
             run_group_sl<true, true, 4>(P, it.al, it.ar, it.bl, it.br, Mg, scratch_stride, sw, sm, sw,
                                         dw + it.dw_start, it.dw_count, status, abort_flag);
@@ -473,9 +820,10 @@ static __device__ __noinline__ void walk_sl(Walker &w, const int *Mg, long long 
 #undef MS
 }
 
+template <bool FAST>
 __global__ void __launch_bounds__(TRACE_WARPS * 32)
     sankoff_sl_trace_kernel(const PairDev *__restrict__ pairs, int npairs, int *scratch,
-                            long long scratch_stride, int sw, int *status, TraceSel sel) {
+                            long long scratch_stride, int sw, int rb, int *status, TraceSel sel) {
     extern __shared__ int smem[];
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
@@ -487,7 +835,7 @@ __global__ void __launch_bounds__(TRACE_WARPS * 32)
     // a fill that gave up (bounded wait) left the matrices incomplete: no walk
     if (*(volatile int *)status & ST_TIMEOUT) return;
     const int lam = sel.lam ? sel.lam[pair] : 0;
-    int *sm = smem + warp * SL_ROWS * sw;
+    int *sm = smem + warp * (FAST ? slf_warp_ints(rb) : SL_ROWS * sw);
     int *Mg = scratch + (long long)pair * scratch_stride * 8;
     int dummy_abort = 0;
     Walker w(P);
@@ -527,8 +875,12 @@ __global__ void __launch_bounds__(TRACE_WARPS * 32)
                 continue;
             }
         }
-        run_group_sl<false, false, 8>(P, ends.x, ends.y, ends.z, ends.w, Mg, scratch_stride, sw, sm, sw,
-                                      nullptr, 0, status, (volatile int *)&dummy_abort);
+        if (FAST)
+            run_group_slf<false, false, 8>(P, ends.x, ends.y, ends.z, ends.w, Mg, scratch_stride, sw,
+                                           (int)(sm - smem), rb, nullptr, 0, status, (volatile int *)&dummy_abort);
+        else
+            run_group_sl<false, false, 8>(P, ends.x, ends.y, ends.z, ends.w, Mg, scratch_stride, sw, sm, sw,
+                                          nullptr, 0, status, (volatile int *)&dummy_abort);
         __syncwarp();
         if (lane == 0) {
             // trace_arcmatch, struct-local branch (aligner.cc:1014-1026): first
@@ -561,38 +913,61 @@ __global__ void __launch_bounds__(TRACE_WARPS * 32)
 
 // ---------------------------------------------------------------- launchers
 
-cudaError_t sl_prepare(int sw, int rb, int *blocks_per_sm) {
-    size_t smem = (size_t)SL_FILL_WARPS * sl_warp_ints(sw, rb) * sizeof(int);
-    size_t smem_t = (size_t)TRACE_WARPS * SL_ROWS * sw * sizeof(int);
-    cudaError_t e = cudaFuncSetAttribute(sankoff_sl_fill_kernel,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+static size_t sl_fill_smem(int sw, int rb, bool fast) {
+    return (size_t)SL_FILL_WARPS * (fast ? slf_warp_ints(rb) : sl_warp_ints(sw, rb)) * sizeof(int);
+}
+static size_t sl_trace_smem(int sw, int rb, bool fast) {
+    return (size_t)TRACE_WARPS * (fast ? slf_warp_ints(rb) : SL_ROWS * sw) * sizeof(int);
+}
+
+cudaError_t sl_prepare(int sw, int rb, bool fast, int *blocks_per_sm) {
+    const size_t smem = sl_fill_smem(sw, rb, fast);
+    const size_t smem_t = sl_trace_smem(sw, rb, fast);
+    int optin = 0, dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(sankoff_sl_trace_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem_t);
+    e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     if (e != cudaSuccess) return e;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, sankoff_sl_fill_kernel,
-                                                         SL_FILL_WARPS * 32, smem);
+    if (smem > (size_t)optin || smem_t > (size_t)optin) {
+        *blocks_per_sm = 0;  // does not fit: the caller reports it
+        return cudaSuccess;
+    }
+    const void *k = fast ? (const void *)sankoff_sl_fill_kernel<true> : (const void *)sankoff_sl_fill_kernel<false>;
+    e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    const void *kt = fast ? (const void *)sankoff_sl_trace_kernel<true> : (const void *)sankoff_sl_trace_kernel<false>;
+    e = cudaFuncSetAttribute(kt, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_t);
+    if (e != cudaSuccess) return e;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k, SL_FILL_WARPS * 32, smem);
 }
 
 int sl_fill_warps_per_block() { return SL_FILL_WARPS; }
 
 cudaError_t launch_sl_fill(const PairDev *pairs, const int2 *queue, int nitems,
-                           int *scratch, long long scratch_stride, int sw, int rb, unsigned int *qhead,
+                           int *scratch, long long scratch_stride, int sw, int rb, bool fast, unsigned int *qhead,
                            int *status, int *abort_flag, int blocks, cudaStream_t st) {
-    size_t smem = (size_t)SL_FILL_WARPS * sl_warp_ints(sw, rb) * sizeof(int);
-    sankoff_sl_fill_kernel<<<blocks, SL_FILL_WARPS * 32, smem, st>>>(
-        pairs, queue, nitems, scratch, scratch_stride, sw, rb, qhead, status, abort_flag);
+    const size_t smem = sl_fill_smem(sw, rb, fast);
+    if (fast)
+        sankoff_sl_fill_kernel<true><<<blocks, SL_FILL_WARPS * 32, smem, st>>>(
+            pairs, queue, nitems, scratch, scratch_stride, sw, rb, qhead, status, abort_flag);
+    else
+        sankoff_sl_fill_kernel<false><<<blocks, SL_FILL_WARPS * 32, smem, st>>>(
+            pairs, queue, nitems, scratch, scratch_stride, sw, rb, qhead, status, abort_flag);
     return cudaGetLastError();
 }
 
-cudaError_t launch_sl_trace(const PairDev *pairs, int npairs, int *scratch,
-                            long long scratch_stride, int sw, int *status, cudaStream_t st, TraceSel sel) {
-    size_t smem = (size_t)TRACE_WARPS * SL_ROWS * sw * sizeof(int);
+cudaError_t launch_sl_trace(const PairDev *pairs, int npairs, int *scratch, long long scratch_stride, int sw,
+                            int rb, bool fast, int *status, cudaStream_t st, TraceSel sel) {
+    const size_t smem = sl_trace_smem(sw, rb, fast);
     const int nw = sel.items ? sel.nitems : npairs;
     if (nw <= 0) return cudaSuccess;
-    int blocks = (nw + TRACE_WARPS - 1) / TRACE_WARPS;
-    sankoff_sl_trace_kernel<<<blocks, TRACE_WARPS * 32, smem, st>>>(pairs, npairs, scratch,
-                                                                    scratch_stride, sw, status, sel);
+    const int blocks = (nw + TRACE_WARPS - 1) / TRACE_WARPS;
+    if (fast)
+        sankoff_sl_trace_kernel<true><<<blocks, TRACE_WARPS * 32, smem, st>>>(pairs, npairs, scratch, scratch_stride,
+                                                                           sw, rb, status, sel);
+    else
+        sankoff_sl_trace_kernel<false><<<blocks, TRACE_WARPS * 32, smem, st>>>(pairs, npairs, scratch,
+                                                                            scratch_stride, sw, rb, status, sel);
     return cudaGetLastError();
 }
 
