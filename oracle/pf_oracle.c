@@ -24,6 +24,17 @@
 
 typedef double pf_t;
 
+/* The value Mprime is filled with before each outside rectangle. The
+ * reference fills -1 ("only for debugging", aligner_p.icc:921), and case 5 of
+ * comp_Mprime_entry (:862-878) then reads virtual_Mprime(a.r, b.r) (:785-797)
+ * at cells outside the band that no loop writes (pf150: Mprime(109, 74), band
+ * of row 109 = 78..129), adding -D(am) pf_scale: the source of the
+ * reference's negative and pf_scale-dependent probabilities. A build with 0
+ * here gives the marginals of the reference's Z (tests/test_pf_outside_fill.py). */
+#ifndef LCG_ORACLE_MPRIME_FILL
+#define LCG_ORACLE_MPRIME_FILL (-1)
+#endif
+
 typedef struct {
     const lcg_pair_tables *t;
     int n, m, na, nb;
@@ -280,7 +291,7 @@ static void align_outside_arcmatch(P *c, size_t al, size_t ar, size_t max_ar, si
     size_t sA = leftmost_covering(c, 1, 1, al, ar), sB = leftmost_covering(c, 0, 1, bl, br);
     align_reverse(c, sA + 1, al - 1, sB + 1, bl - 1, 0);
     size_t cells = (size_t)(c->n + 1) * (c->m + 1);
-    for (size_t q = 0; q < cells; ++q) c->Mprime[q] = -1;
+    for (size_t q = 0; q < cells; ++q) c->Mprime[q] = LCG_ORACLE_MPRIME_FILL;
     pf_t Mal = Mx(c, al - 1, bl - 1);
     if (valid(c, max_ar, max_br)) Mp(c, max_ar, max_br) = Mal * Mr(c, max_ar, max_br) * c->pf_scale;
     size_t i;

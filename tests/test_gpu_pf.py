@@ -9,7 +9,11 @@
   reference's printed probabilities within 1e-9 (pf90_b: every arc match and
   base match). On pf150 / pf200 the reference's outside pass returns
   negative probabilities for hundreds of arc matches and its values change
-  with pf_scale; the adjoint pass does neither.
+  with pf_scale; the adjoint pass does neither. The cause is in the
+  reference: case 5 of comp_Mprime_entry reads Mprime cells outside the band
+  that hold the debugging fill value -1 (aligner_p.icc:921;
+  tests/test_pf_outside_fill.py shows that with 0 there its outside pass
+  gives these marginals).
 * These compare the exact marginals (min_am_prob = 0). With locarna_p's
   default min_am_prob = 0.001 the base-match probabilities leave out the
   contributions inside arc matches of probability <= sqrt(min_am_prob), as
