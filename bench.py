@@ -350,16 +350,18 @@ def run_modes(eng, tables, flush_l2):
 def run_pf(eng, tables, flush_l2, cpu):
     """LocARNA-P over the whole workload: all pairs in size order, in
     launches of PF_BUCKET pairs (length-grouped persistent launches), inside
-    + adjoint outside in FP32 with per-position scaling; FP64 on every
-    PF_FP64_STRIDE-th pair of each launch (size-stratified), and per pair of
-    that subset the largest FP32 error of any arc-match or base-match
-    probability against the FP64 run of the same kernels (exact marginals,
-    min_am_prob 0); one 200-nt pair with gradients."""
+    + adjoint outside in FP32 with per-position scaling, for what locarna_p
+    reports (log Z, arc-match and base-match probabilities; no gap
+    gradients); FP64 on every PF_FP64_STRIDE-th pair of each launch
+    (size-stratified), and per pair of that subset the largest FP32 error of
+    any arc-match or base-match probability against the FP64 run of the same
+    kernels (exact marginals, min_am_prob 0); one 200-nt pair with every
+    gradient."""
     import numpy as np
     order = sorted(range(len(tables)), key=lambda k: (tables[k].len_a * tables[k].len_b, k))
     buckets = [order[i:i + PF_BUCKET] for i in range(0, len(order), PF_BUCKET)]
     for prec in (64, 32):  # warm-up
-        eng.pf_forward([tables[k] for k in buckets[0][:64]], precision=prec, min_am_prob=0.0)
+        eng.pf_forward([tables[k] for k in buckets[0][:64]], precision=prec, min_am_prob=0.0, gap_gradients=False)
         eng.pf_backward(probs=False)
     dev = {64: 0.0, 32: 0.0}
     wall = {64: 0.0, 32: 0.0}
@@ -371,7 +373,7 @@ def run_pf(eng, tables, flush_l2, cpu):
         sub = list(range(0, len(b), PF_FP64_STRIDE))
         flush_l2()
         t0 = time.perf_counter()
-        eng.pf_forward(tb, precision=32, min_am_prob=0.0)
+        eng.pf_forward(tb, precision=32, min_am_prob=0.0, gap_gradients=False)
         r32 = eng.pf_backward(probs=True)
         wall[32] += time.perf_counter() - t0
         f, bw = eng.pf_last_timing()
@@ -380,7 +382,7 @@ def run_pf(eng, tables, flush_l2, cpu):
         del r32
         flush_l2()
         t0 = time.perf_counter()
-        eng.pf_forward([tb[k] for k in sub], precision=64, min_am_prob=0.0)
+        eng.pf_forward([tb[k] for k in sub], precision=64, min_am_prob=0.0, gap_gradients=False)
         r64 = eng.pf_backward(probs=True)
         wall[64] += time.perf_counter() - t0
         f, bw = eng.pf_last_timing()
@@ -399,7 +401,8 @@ def run_pf(eng, tables, flush_l2, cpu):
     out = {
         "workload": PF_WORKLOAD_NAME, "workload_pairs": n,
         "fp32": {"pairs": n, "pairs_per_s": n / (dev[32] / 1e3), "device_ms": dev[32], "e2e_pairs_per_s": n / wall[32],
-                 "what": "every pair of the workload, inside + adjoint outside, FP32 with per-position scaling"},
+                 "what": "every pair of the workload, inside + adjoint outside (log Z, arc-match and base-match "
+                         "probabilities, as locarna_p; no gap gradients), FP32 with per-position scaling"},
         "fp64": {"pairs": n64, "pairs_per_s": n64 / (dev[64] / 1e3), "device_ms": dev[64],
                  "e2e_pairs_per_s": n64 / wall[64],
                  "what": f"every {PF_FP64_STRIDE}th pair of each launch in size order (size-stratified)"},
@@ -836,20 +839,22 @@ def run_small_case(args):
 
 def run_pf_small_case(args):
     """A small LocARNA-P batch for profiling: `--case pf-small` runs the
-    forward and the backward pass (FP32, then FP64) once on every 256th pair
-    of the LocARNA-P workload in size order (32 pairs of 80-500 nt)."""
+    forward and the backward pass (FP32, then FP64; probabilities only, then
+    with the gap gradients) on every 256th pair of the LocARNA-P workload in
+    size order (32 pairs of 80-500 nt)."""
     from locarna_gb300.engine import Engine
     tables = build_pf_tables()
     order = sorted(range(len(tables)), key=lambda k: tables[k].len_a * tables[k].len_b)
     tb = [tables[k] for k in order[::256]]
     eng = Engine(0)
     for prec in (32, 64):
-        for _ in range(max(1, args.warmup)):
-            eng.pf_forward(tb, precision=prec)
-            eng.pf_backward(probs=False)
-        f, b = eng.pf_last_timing()
-        print(json.dumps({"case": "pf-small", "precision": prec, "pairs": len(tb), "forward_ms": f,
-                          "backward_ms": b}), flush=True)
+        for grads in (False, True):
+            for _ in range(max(1, args.warmup)):
+                eng.pf_forward(tb, precision=prec, min_am_prob=0.0, gap_gradients=grads)
+                eng.pf_backward(probs=True)
+            f, b = eng.pf_last_timing()
+            print(json.dumps({"case": "pf-small", "precision": prec, "gap_gradients": grads, "pairs": len(tb),
+                              "forward_ms": f, "backward_ms": b}), flush=True)
     eng.close()
 
 

@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define LCG_ABI_VERSION 3
+#define LCG_ABI_VERSION 4
 
 typedef int32_t lcg_status;
 #define LCG_OK 0
@@ -337,6 +337,12 @@ typedef struct lcg_pf_opts {
      * 1404-1435), which the caller applies. */
     double min_am_prob;
     double min_bm_prob;
+    /* 1 (default): lcg_pf_backward also returns the gap counts and
+     * d log Z / d indel, indel_opening; 0: probabilities (and the struct-weight
+     * and base-match gradients) only, and those four results are NaN. The
+     * gap counts need the E and F matrices, which the backward pass then
+     * keeps and reads besides M; locarna_p prints probabilities only. */
+    int32_t gap_gradients;
 } lcg_pf_opts;
 
 /* Per pair input of the parameter gradients (all optional, see below). */
@@ -355,7 +361,8 @@ typedef struct lcg_pf_result {
     double gap_ext_uses;  /* expected number of gapped positions (uses of gap_a / gap_b) */
     double gap_open_uses; /* expected number of gap openings (uses of indel_opening) */
     /* d log Z / d parameter: indel (gap_a[i] = gap_b[j] = indel), indel_opening
-     * always; struct_weight and the 16 base-match scores (sigma(i,j) =
+     * unless lcg_pf_opts.gap_gradients = 0 (then NaN, as the two gap counts);
+     * struct_weight and the 16 base-match scores (sigma(i,j) =
      * S[code_a[i]][code_b[j]], index 4*x+y) when a grad spec is given */
     double dlogz_dindel;
     double dlogz_dindel_opening;

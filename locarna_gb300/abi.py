@@ -71,7 +71,8 @@ _P8 = C.POINTER(C.c_int8)
 
 class lcg_pf_opts(C.Structure):
     _fields_ = [("temperature", C.c_double), ("pf_scale", C.c_double), ("precision", C.c_int32),
-                ("param_delta", C.c_double * 19), ("min_am_prob", C.c_double), ("min_bm_prob", C.c_double)]
+                ("param_delta", C.c_double * 19), ("min_am_prob", C.c_double), ("min_bm_prob", C.c_double),
+                ("gap_gradients", C.c_int32)]
 
 
 class lcg_pf_grad_spec(C.Structure):

@@ -87,6 +87,7 @@ int run(const Clp &c) {
     o.precision = 64;
     o.min_am_prob = c.min_am_prob;
     o.min_bm_prob = c.min_bm_prob;
+    o.gap_gradients = 0;  // probabilities only
     if (c.verbose) std::cout << "Run inside algorithm." << std::endl;
     double log_z = 0;
     locarna_gb300::check(lcg_pf_forward(eng.get(), &t, 1, &o, nullptr, &log_z));

@@ -9,6 +9,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <limits>
 #include <cstring>
 #include <string>
 #include <thread>
@@ -62,6 +63,7 @@ struct PFState {
     double fwd_ms = 0, back_ms = 0;
     double temperature = 300.0;
     double min_am_prob = 0.0;  // > 0: base-match probabilities truncated as AlignerP computes them
+    bool gap_gradients = true;  // the backward pass accumulates the gap counts
     std::vector<double> log_z;
     std::vector<std::vector<int>> am_pos;  // per pair: D position of each arc match
 };
@@ -340,6 +342,7 @@ lcg_status pf_forward_t(lcg_engine e, PFState *S, const lcg_pair_tables *pairs, 
     }
     S->temperature = temp;
     S->min_am_prob = o->min_am_prob;
+    S->gap_gradients = o->gap_gradients != 0;
     S->precision = sizeof(T) == 8 ? 64 : 32;
     S->npairs = npairs;
     S->nitems = nitems;
@@ -366,7 +369,8 @@ lcg_status pf_backward_t(lcg_engine e, PFState *S, const lcg_pf_grad_spec *grads
     int *abort_flag = (int *)(Dv + S->off_ctrl + 8);
     PF_TRY(cudaEventRecord(e->ev1, st));
     PF_TRY(pf_launch_back<T>(Dv + S->off_pairs, (const int2 *)(Dv + S->off_queue), (int)S->nitems,
-                             S->d_scratch, S->stride, S->sw, S->rb, qhead, status, abort_flag, e->sms * bb, st));
+                             S->d_scratch, S->stride, S->sw, S->rb, qhead, status, abort_flag, e->sms * bb, st, 0.0,
+                             S->gap_gradients));
     PF_TRY(cudaEventRecord(e->ev2, st));
     PF_TRY(cudaMemcpyAsync(H + S->off_ctrl, Dv + S->off_ctrl, 64, cudaMemcpyDeviceToHost, st));
     PF_TRY(cudaMemcpyAsync(H + S->out_begin, Dv + S->out_begin, S->out_end - S->out_begin, cudaMemcpyDeviceToHost, st));
@@ -392,8 +396,10 @@ lcg_status pf_backward_t(lcg_engine e, PFState *S, const lcg_pf_grad_spec *grads
         const int4 *rowinfo = (const int4 *)(H + L.rowinfo);
         const lcg_pf_grad_spec *g = grads ? &grads[q] : nullptr;
         r.log_z = S->log_z[q];
-        r.gap_ext_uses = res[1] / Zs;
-        r.gap_open_uses = res[2] / Zs;
+        // without gap gradients the pass did not accumulate the gap counts
+        const double nan = std::numeric_limits<double>::quiet_NaN();
+        r.gap_ext_uses = S->gap_gradients ? res[1] / Zs : nan;
+        r.gap_open_uses = S->gap_gradients ? res[2] / Zs : nan;
         r.dlogz_dindel = r.gap_ext_uses * invT;
         r.dlogz_dindel_opening = r.gap_open_uses * invT;
         r.dlogz_dstruct_weight = 0.0;
@@ -489,6 +495,7 @@ void lcg_pf_opts_default(lcg_pf_opts *o) {
     o->precision = 64;
     o->min_am_prob = 0.001;  // locarna_p --min-am-prob / --min-bm-prob (src/locarna_p.cc:143-146)
     o->min_bm_prob = 0.001;
+    o->gap_gradients = 1;
 }
 
 lcg_status lcg_pf_forward(lcg_engine e, const lcg_pair_tables *pairs, int32_t npairs, const lcg_pf_opts *opts,

@@ -42,11 +42,12 @@ cudaError_t pf_launch_fwd(const void *pairs, const int2 *queue, int nitems, void
                           long long stride, int pitch, int rb, unsigned int *qhead, int *status, int *abort_flag,
                           int blocks, bool count_uses, cudaStream_t st);
 // theta > 0: the truncated base-match pass (min_am_prob = theta^2) after a
-// full backward pass; theta = 0: the full adjoint pass
+// full backward pass; theta = 0: the full adjoint pass, with the gap counts
+// (the indel / indel-opening gradients) when grads
 template <typename T>
 cudaError_t pf_launch_back(const void *pairs, const int2 *queue, int nitems, void *scratch,
                            long long stride, int pitch, int rb, unsigned int *qhead, int *status, int *abort_flag,
-                           int blocks, cudaStream_t st, double theta = 0.0);
+                           int blocks, cudaStream_t st, double theta = 0.0, bool grads = true);
 // rb: ring size of the shared-memory rows (a power of two above the span of
 // any two consecutive band rows)
 template <typename T>

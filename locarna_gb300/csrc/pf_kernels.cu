@@ -101,13 +101,14 @@ __device__ __forceinline__ PFRows<T> pf_rows(int warp, int rb) {
 }
 
 // Sum-product sweep of one group (or the top level) in the scaled frame; M of
-// the rectangle goes to Mg (row i-al, column j-bl, pitch `pitch`), and with
-// SAVE also E and F (Eg, Fg) and the cells around the band the adjoint reads.
+// the rectangle goes to Mg (row i-al, column j-bl, pitch `pitch`), with SAVE
+// also the cells around the band the adjoint reads, and with SAVE and SAVEEF
+// E and F (Eg, Fg; only the gap gradients read them).
 // Arc terms per row: the row's candidates (arc matches with a.r = i, a.l
 // descending) are read 32 at a time until the first a.l <= al, and each term
 // M(a.l-1,b.l-1) D(am) s is summed into its column with a shared-memory
 // atomicAdd. COUNTU counts the uses of every D entry (for the backward pass).
-template <typename T, bool WAIT, bool DWRITE, bool COUNTU, bool SAVE>
+template <typename T, bool WAIT, bool DWRITE, bool COUNTU, bool SAVE, bool SAVEEF = true>
 __device__ void pf_group_sweep(const PFPair<T> &P, int al, int ar, int bl, int br, T *__restrict__ Mg,
                                T *__restrict__ Eg, T *__restrict__ Fg, int pitch, PFRows<T> R,
                                const int4 *__restrict__ dw, int ndw, int *status, volatile int *abort_flag) {
@@ -115,7 +116,12 @@ __device__ void pf_group_sweep(const PFPair<T> &P, int al, int ar, int bl, int b
     const int m1 = P.m + 1;
     const T o = P.o, arcf = P.arcf;
 #define RG(j) ((j) - R.rb * (int)__umulhi((unsigned)(j), R.magic))
-    for (int c = lane; c < R.rb; c += 32) R.E[c] = T(0);
+    // E and the arc-term sums start at zero; the cell sweep puts zero back
+    // into every arc-term column it reads, so no row needs a clearing pass
+    for (int c = lane; c < R.rb; c += 32) {
+        R.E[c] = T(0);
+        R.Ar[c] = T(0);
+    }
     // row al: M(al,bl) = 1/s, M(al,j) = (o/s) prod gB (aligner_p.icc:149-190)
     const int L0 = min(br, P.rowinfo[al].y + 1);
     {
@@ -133,7 +139,7 @@ __device__ void pf_group_sweep(const PFPair<T> &P, int al, int ar, int bl, int b
                 R.Mp[RG(j)] = val;
                 R.Np[RG(j)] = val;
                 Mg[j - bl] = val;
-                if (SAVE) {
+                if (SAVE && SAVEEF) {
                     Eg[j - bl] = T(0);
                     Fg[j - bl] = T(0);
                 }
@@ -144,7 +150,7 @@ __device__ void pf_group_sweep(const PFPair<T> &P, int al, int ar, int bl, int b
             R.Mp[RG(bl)] = P.inv_s;
             R.Np[RG(bl)] = P.inv_s;
             Mg[0] = P.inv_s;
-            if (SAVE) {
+            if (SAVE && SAVEEF) {
                 Eg[0] = T(0);
                 Fg[0] = T(0);
             }
@@ -156,8 +162,10 @@ __device__ void pf_group_sweep(const PFPair<T> &P, int al, int ar, int bl, int b
                 R.Np[RG(j)] = T(0);
                 if (SAVE) {
                     Mg[j - bl] = T(0);
-                    Eg[j - bl] = T(0);
-                    Fg[j - bl] = T(0);
+                    if (SAVEEF) {
+                        Eg[j - bl] = T(0);
+                        Fg[j - bl] = T(0);
+                    }
                 }
             }
         }
@@ -190,11 +198,7 @@ __device__ void pf_group_sweep(const PFPair<T> &P, int al, int ar, int bl, int b
                 ball[u] = __ballot_sync(0xffffffffu, okA[u]);
             }
             if (ball[0] == 0u) break;
-            if (!rowarcs) {
-                for (int j = lo + lane; j <= hi; j += 32) R.Ar[RG(j)] = T(0);
-                __syncwarp();
-                rowarcs = true;
-            }
+            rowarcs = true;
             bool ok[2];
             T dv[2], mv[2];
 #pragma unroll
@@ -229,8 +233,10 @@ __device__ void pf_group_sweep(const PFPair<T> &P, int al, int ar, int bl, int b
             if (SAVE) {
                 // the cell left of the row's band (column bl, or a zero cell)
                 Mg[(size_t)(i - al) * pitch + (lo - 1 - bl)] = B;
-                Eg[(size_t)(i - al) * pitch + (lo - 1 - bl)] = T(0);
-                Fg[(size_t)(i - al) * pitch + (lo - 1 - bl)] = T(0);
+                if (SAVEEF) {
+                    Eg[(size_t)(i - al) * pitch + (lo - 1 - bl)] = T(0);
+                    Fg[(size_t)(i - al) * pitch + (lo - 1 - bl)] = T(0);
+                }
             }
         }
         const T *bmrow = P.bm + (size_t)i * m1;
@@ -243,7 +249,10 @@ __device__ void pf_group_sweep(const PFPair<T> &P, int al, int ar, int bl, int b
             if (act) {
                 Ei = R.E[RG(j)] * gAi + R.Np[RG(j)] * gAi * o;
                 X = R.Mp[RG(j - 1)] * bmrow[j];
-                if (rowarcs) X += R.Ar[RG(j)];
+                if (rowarcs) {
+                    X += R.Ar[RG(j)];
+                    R.Ar[RG(j)] = T(0);
+                }
                 g = P.gB[j];
             }
             // F(j) = gB(j) F(j-1) + gB(j) o Q(j-1): linear warp scan
@@ -271,7 +280,7 @@ __device__ void pf_group_sweep(const PFPair<T> &P, int al, int ar, int bl, int b
                 R.Mc[RG(j)] = M;
                 R.Nc[RG(j)] = X + F;
                 Mg[roff + j] = M;
-                if (SAVE) {
+                if (SAVE && SAVEEF) {
                     Eg[roff + j] = Ei;
                     Fg[roff + j] = F;
                 }
@@ -304,8 +313,10 @@ __device__ void pf_group_sweep(const PFPair<T> &P, int al, int ar, int bl, int b
                 R.E[RG(j)] = T(0);
                 if (SAVE) {
                     Mg[(size_t)(i - al) * pitch + (j - bl)] = T(0);
-                    Eg[(size_t)(i - al) * pitch + (j - bl)] = T(0);
-                    Fg[(size_t)(i - al) * pitch + (j - bl)] = T(0);
+                    if (SAVEEF) {
+                        Eg[(size_t)(i - al) * pitch + (j - bl)] = T(0);
+                        Fg[(size_t)(i - al) * pitch + (j - bl)] = T(0);
+                    }
                 }
             }
         }
@@ -367,8 +378,10 @@ __device__ __forceinline__ T ld_cg(const T *p) { return __ldcg(p); }
 // positive min_am_prob (aligner_p.icc:1201-1327): D_bar is final (from the
 // full pass), only the group's arc matches with probability D D_bar / Z' >
 // theta seed M_bar, and nothing propagates out of the group (no D_bar, no use
-// counters, no gap counts); the per-band-cell sums go to bmacc.
-template <typename T, bool TRUNC = false>
+// counters, no gap counts); the per-band-cell sums go to bmacc. GRADS: the
+// gap counts (ext_acc / open_acc) are accumulated, which reads E and F;
+// without, only M of the recomputed rectangle is read.
+template <typename T, bool TRUNC = false, bool GRADS = true>
 __device__ void pf_group_back(const PFPair<T> &P, int al, int ar, int bl, int br, bool top,
                               const T *__restrict__ Mg, const T *__restrict__ Eg, const T *__restrict__ Fg,
                               T *__restrict__ Mb, int pitch, PFRows<T> R, const int4 *__restrict__ dw, int ndw,
@@ -465,11 +478,13 @@ __device__ void pf_group_back(const PFPair<T> &P, int al, int ar, int bl, int br
                 Dc[RG(j)] = T(0);
                 Ebn = Eb[RG(j)];  // E_bar(i+1, j)
                 g = P.gB[j];
-                Ev = Eg[roff + c];
-                Fv = Fg[roff + c];
-                Mv = Mg[roff + c];
+                if (GRADS) {
+                    Ev = Eg[roff + c];
+                    Fv = Fg[roff + c];
+                    Mv = Mg[roff + c];
+                    Eup = Eg[roff - pitch + c];
+                }
                 Mup = Mg[roff - pitch + c];
-                Eup = Eg[roff - pitch + c];
                 bmj = bmrow[j];
             }
             T gn = __shfl_down_sync(0xffffffffu, g, 1);  // gB(j+1); 0 past the row's end
@@ -477,8 +492,10 @@ __device__ void pf_group_back(const PFPair<T> &P, int al, int ar, int bl, int br
             T Md = __shfl_up_sync(0xffffffffu, Mup, 1);
             if (lane == 31 && act) gn = (j + 1 <= hi) ? P.gB[j + 1] : T(0);
             if (lane == 0 && act) {
-                Ml = Mg[roff + c - 1];
-                Fl = Fg[roff + c - 1];
+                if (GRADS) {
+                    Ml = Mg[roff + c - 1];
+                    Fl = Fg[roff + c - 1];
+                }
                 Md = Mg[roff - pitch + c - 1];
             }
             const T Nbar = act ? Ebn * gAn * o : T(0);  // N(i,j) feeds E(i+1,j)
@@ -507,8 +524,10 @@ __device__ void pf_group_back(const PFPair<T> &P, int al, int ar, int bl, int br
                 Eb[RG(j)] = Ebar;
                 Xb[RG(j)] = Xbar;
                 // gap derivatives: E(i,j) = gA(i) (E(i-1,j) + N(i-1,j) o)
-                ext += (double)(Ebar * Ev + Fb * Fv);
-                opn += (double)(Ebar * (Mup - Eup) * gAi * o + Fb * (Ml - Fl) * g * o);
+                if (GRADS) {
+                    ext += (double)(Ebar * Ev + Fb * Fv);
+                    opn += (double)(Ebar * (Mup - Eup) * gAi * o + Fb * (Ml - Fl) * g * o);
+                }
                 // diagonal
                 if (j - 1 >= dlo && j - 1 <= dhi)
                     Dn[RG(j - 1)] = Xbar * bmj;
@@ -595,7 +614,7 @@ __device__ void pf_group_back(const PFPair<T> &P, int al, int ar, int bl, int br
         if (*abort_flag) return;
     }
     // boundary values: M(al,j) = (o/s) prod gB, M(i,bl) = (o/s) prod gA
-    {
+    if (GRADS) {
         const int L0 = min(br, P.rowinfo[al].y + 1);
         for (int j = bl + 1 + lane; j < L0; j += 32) {
             const T v = ld_cg(Mb + (j - bl)) * Mg[j - bl];
@@ -615,13 +634,13 @@ __device__ void pf_group_back(const PFPair<T> &P, int al, int ar, int bl, int br
         ext += __shfl_xor_sync(0xffffffffu, ext, off);
         opn += __shfl_xor_sync(0xffffffffu, opn, off);
     }
-    if (lane == 0 && !TRUNC) {
+    if (lane == 0 && !TRUNC && GRADS) {
         atomicAdd(ext_acc, ext);
         atomicAdd(open_acc, opn);
     }
 }
 
-template <typename T, bool TRUNC>
+template <typename T, bool TRUNC, bool GRADS>
 __global__ void __launch_bounds__(PF_WARPS * 32, pf_min_blocks<T>())
     pf_back_kernel(const PFPair<T> *__restrict__ pairs, const int2 *__restrict__ queue, int nitems,
                    T *scratch, long long stride, int pitch, int rb,
@@ -653,10 +672,10 @@ __global__ void __launch_bounds__(PF_WARPS * 32, pf_min_blocks<T>())
             }
             if (!__any_sync(0xffffffffu, any)) continue;
         }
-        pf_group_sweep<T, false, false, false, true>(P, al, ar, bl, br, Mg, Eg, Fg, pitch, R, nullptr, 0, status,
-                                                     abort_flag);
+        pf_group_sweep<T, false, false, false, true, GRADS>(P, al, ar, bl, br, Mg, Eg, Fg, pitch, R, nullptr, 0,
+                                                            status, abort_flag);
         __syncwarp();
-        pf_group_back<T, TRUNC>(P, al, ar, bl, br, it.top != 0, Mg, Eg, Fg, Mb, pitch, R,
+        pf_group_back<T, TRUNC, GRADS>(P, al, ar, bl, br, it.top != 0, Mg, Eg, Fg, Mb, pitch, R,
                                 it.top ? nullptr : P.dw + it.dw_start, it.top ? 0 : it.dw_count, status, abort_flag,
                                 P.res + 1, P.res + 2, theta_z);
         __syncwarp();
@@ -721,37 +740,43 @@ cudaError_t pf_fwd_occupancy(int rb, int *blocks_per_sm) {
     return pf_cap_blocks(pf_fwd_kernel<T, true>, "LCG_PF_FWD_BPS", smem, blocks_per_sm);
 }
 
+template <typename T, bool TRUNC, bool GRADS>
+static cudaError_t pf_launch_back_k(const void *pairs, const int2 *queue, int nitems, void *scratch, long long stride,
+                                    int pitch, int rb, unsigned int *qhead, int *status, int *abort_flag, int blocks,
+                                    cudaStream_t st, double theta) {
+    const size_t smem = pf_smem<T>(rb);
+    cudaError_t e = cudaFuncSetAttribute(pf_back_kernel<T, TRUNC, GRADS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    pf_back_kernel<T, TRUNC, GRADS><<<blocks, PF_WARPS * 32, smem, st>>>(
+        (const PFPair<T> *)pairs, queue, nitems, (T *)scratch, stride, pitch, rb, qhead, status, abort_flag, theta);
+    return cudaGetLastError();
+}
+
 template <typename T>
 cudaError_t pf_launch_back(const void *pairs, const int2 *queue, int nitems, void *scratch,
                            long long stride, int pitch, int rb, unsigned int *qhead, int *status, int *abort_flag,
-                           int blocks, cudaStream_t st, double theta) {
-    const size_t smem = pf_smem<T>(rb);
-    cudaError_t e;
-    if (theta > 0.0) {
-        e = cudaFuncSetAttribute(pf_back_kernel<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        pf_back_kernel<T, true><<<blocks, PF_WARPS * 32, smem, st>>>((const PFPair<T> *)pairs, queue, nitems,
-                                                                       (T *)scratch, stride, pitch, rb, qhead,
-                                                                       status, abort_flag, theta);
-    } else {
-        e = cudaFuncSetAttribute(pf_back_kernel<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        pf_back_kernel<T, false><<<blocks, PF_WARPS * 32, smem, st>>>((const PFPair<T> *)pairs, queue, nitems,
-                                                                        (T *)scratch, stride, pitch, rb, qhead,
-                                                                        status, abort_flag, 0.0);
-    }
-    return cudaGetLastError();
+                           int blocks, cudaStream_t st, double theta, bool grads) {
+    if (theta > 0.0)
+        return pf_launch_back_k<T, true, false>(pairs, queue, nitems, scratch, stride, pitch, rb, qhead, status,
+                                                abort_flag, blocks, st, theta);
+    if (grads)
+        return pf_launch_back_k<T, false, true>(pairs, queue, nitems, scratch, stride, pitch, rb, qhead, status,
+                                                abort_flag, blocks, st, 0.0);
+    return pf_launch_back_k<T, false, false>(pairs, queue, nitems, scratch, stride, pitch, rb, qhead, status,
+                                             abort_flag, blocks, st, 0.0);
 }
 
 template <typename T>
 cudaError_t pf_back_occupancy(int rb, int *blocks_per_sm) {
     const size_t smem = pf_smem<T>(rb);
-    cudaError_t e = cudaFuncSetAttribute(pf_back_kernel<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(pf_back_kernel<T, false, true>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, pf_back_kernel<T, false>, PF_WARPS * 32, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, pf_back_kernel<T, false, true>, PF_WARPS * 32,
+                                                      smem);
     if (e != cudaSuccess) return e;
-    return pf_cap_blocks(pf_back_kernel<T, false>, "LCG_PF_BACK_BPS", smem, blocks_per_sm);
+    return pf_cap_blocks(pf_back_kernel<T, false, true>, "LCG_PF_BACK_BPS", smem, blocks_per_sm);
 }
 
 int pf_warps_per_block() { return PF_WARPS; }
@@ -763,9 +788,9 @@ template cudaError_t pf_launch_fwd<float>(const void *, const int2 *, int, void 
 template cudaError_t pf_fwd_occupancy<double>(int, int *);
 template cudaError_t pf_fwd_occupancy<float>(int, int *);
 template cudaError_t pf_launch_back<double>(const void *, const int2 *, int, void *, long long, int,
-                                            int, unsigned int *, int *, int *, int, cudaStream_t, double);
+                                            int, unsigned int *, int *, int *, int, cudaStream_t, double, bool);
 template cudaError_t pf_launch_back<float>(const void *, const int2 *, int, void *, long long, int,
-                                           int, unsigned int *, int *, int *, int, cudaStream_t, double);
+                                           int, unsigned int *, int *, int *, int, cudaStream_t, double, bool);
 template cudaError_t pf_back_occupancy<double>(int, int *);
 template cudaError_t pf_back_occupancy<float>(int, int *);
 

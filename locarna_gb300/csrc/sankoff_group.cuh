@@ -86,7 +86,9 @@ __device__ __noinline__ int inner_term(const PairDev &P, const int4 *e, int *sta
 // Per row, the arc-match terms come first: the row's candidates (arc matches
 // with a.r = i, sorted by a.l descending) are read 32 at a time by the whole
 // warp until the first a.l <= al; each valid term M(a.l-1,b.l-1) + D(a,b) is
-// reduced into its column with a shared-memory atomicMax. Then lanes own
+// reduced into its column with a shared-memory atomicMax. The maxima row is
+// -inf at the group's start, and the cell sweep puts -inf back into every
+// column it reads, so no row needs a clearing pass. Then lanes own
 // consecutive columns (chunks of 32) for the affine recursion; the horizontal
 // gap chain is a max-plus warp scan. ANCH = false drops every anchor test and
 // uses plain (non-saturating) adds: without anchors every gap term is finite,
@@ -122,7 +124,10 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
 #define CUR(j) lcg_smem[cu + RG(j)]
 #define PREVR(r) lcg_smem[pv + (r)]  // by ring index
 #define CURR(r) lcg_smem[cu + (r)]
-    for (int c = lane; c < ringn; c += 32) E[c] = NEG;
+    for (int c = lane; c < ringn; c += 32) {
+        E[c] = NEG;
+        Arow[c] = NEG;
+    }
     if (SCLS)
         for (int k = lane; k < 256; k += 32) Stab[k] = P.scls[k];
 
@@ -231,11 +236,7 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
                 ball[u] = __ballot_sync(0xffffffffu, okA[u]);
             }
             if (ball[0] == 0u) break;
-            if (!rowarcs) {
-                for (int j = lo + lane; j <= hi; j += 32) Arow[RG(j)] = NEG;
-                __syncwarp();
-                rowarcs = true;
-            }
+            rowarcs = true;
             bool ok[2];
             int dv[2], mv[2];
 #pragma unroll
@@ -311,7 +312,10 @@ __device__ void run_group_c(const PairDev &P, int al, int ar, int bl, int br, in
                 e = norm(e);
                 E[rj] = e;
                 X = max(d, e);
-                if (rowarcs && mok) X = max(X, Arow[rj]);
+                if (rowarcs) {
+                    if (mok) X = max(X, Arow[rj]);
+                    Arow[rj] = NEG;
+                }
             }
             if (TOP && local_top && act && i < la && j < lb) X = max(X, 0);
             int F;

@@ -370,9 +370,14 @@ __device__ void run_group_slf(const PairDev &P, int al, int ar, int bl, int br, 
     const int2 *__restrict__ rowarc = P.rowarc;
     const int2 *__restrict__ crow = P.crow;
     int *const Dp = P.D;
+    // E rows and the arc-term maxima start at -inf; the cell sweep puts -inf
+    // back into every maxima column it reads
     for (int c = lane; c < ringn; c += 32) {
 #pragma unroll
-        for (int s = 0; s < 4; ++s) ROW(6 + s)[c] = NEG;
+        for (int s = 0; s < 4; ++s) {
+            ROW(6 + s)[c] = NEG;
+            ROW(11 + s)[c] = NEG;
+        }
     }
     for (int k = lane; k < 256; k += 32) Stab[k] = P.scls[k];
 
@@ -449,15 +454,7 @@ __device__ void run_group_slf(const PairDev &P, int al, int ar, int bl, int br, 
             const bool okA = ca >= al && ca != 0xffff;       // a.l > al
             const unsigned ball = __ballot_sync(0xffffffffu, okA);
             if (ball == 0u) break;
-            if (!rowarcs) {
-                for (int j = lo + lane; j <= hi; j += 32) {
-                    const int rj = RG(j);
-#pragma unroll
-                    for (int s = 0; s < 4; ++s) ROW(11 + s)[rj] = NEG;
-                }
-                __syncwarp();
-                rowarcs = true;
-            }
+            rowarcs = true;
             if (okA && cbl >= bl && en.y >= lo && en.y <= hi) {
                 int dv = WAIT ? ld_volatile(Dp + e) : Dp[e];
                 const long long o = (long long)(ca - al) * pitch + (cbl - bl);
@@ -574,6 +571,10 @@ __device__ void run_group_slf(const PairDev &P, int al, int ar, int bl, int br, 
                     x1 = max(x1, ROW(12)[rj]);
                     x2 = max(x2, ROW(13)[rj]);
                     x3 = max(x3, ROW(14)[rj]);
+                    ROW(11)[rj] = NEG;
+                    ROW(12)[rj] = NEG;
+                    ROW(13)[rj] = NEG;
+                    ROW(14)[rj] = NEG;
                 }
             }
             const int pa = gbc >> 4;

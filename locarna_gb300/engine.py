@@ -279,13 +279,16 @@ class Engine:
     # ------------------------------------------------------------ LocARNA-P
 
     def pf_opts(self, temperature=300.0, pf_scale=1.0, precision=64, param_delta=None, min_am_prob=0.001,
-                min_bm_prob=0.001):
+                min_bm_prob=0.001, gap_gradients=True):
         """lcg_pf_opts; min_am_prob = 0 gives the exact base-match marginals,
-        > 0 the truncated ones locarna_p reports (its default 0.001)."""
+        > 0 the truncated ones locarna_p reports (its default 0.001);
+        gap_gradients = False: probabilities only (no gap counts, NaN
+        indel / indel-opening gradients)."""
         o = lcg_pf_opts()
         self.lib.lcg_pf_opts_default(C.byref(o))
         o.temperature, o.pf_scale, o.precision = float(temperature), float(pf_scale), int(precision)
         o.min_am_prob, o.min_bm_prob = float(min_am_prob), float(min_bm_prob)
+        o.gap_gradients = 1 if gap_gradients else 0
         if param_delta is not None:
             for k, v in enumerate(param_delta):
                 o.param_delta[k] = float(v)
@@ -311,9 +314,9 @@ class Engine:
         return arr, keep
 
     def pf_forward(self, tables, temperature=300.0, pf_scale=1.0, precision=64, param_delta=None,
-                   min_am_prob=0.001, min_bm_prob=0.001):
+                   min_am_prob=0.001, min_bm_prob=0.001, gap_gradients=True):
         """lcg_pf_forward: log Z of each pair (numpy float64 array)."""
-        o = self.pf_opts(temperature, pf_scale, precision, param_delta, min_am_prob, min_bm_prob)
+        o = self.pf_opts(temperature, pf_scale, precision, param_delta, min_am_prob, min_bm_prob, gap_gradients)
         n = len(tables)
         arr = (lcg_pair_tables * n)(*[t.to_c() for t in tables])
         specs, keep = self._specs(tables)

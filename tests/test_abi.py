@@ -35,7 +35,7 @@ def test_abi_version():
     from locarna_gb300.build import build_engine
     lib = C.CDLL(build_engine())
     lib.lcg_abi_version.restype = C.c_int32
-    assert lib.lcg_abi_version() == 3
+    assert lib.lcg_abi_version() == 4
 
 
 def test_ctypes_structs_match_c_layout(tmp_path):

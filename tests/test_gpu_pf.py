@@ -114,6 +114,32 @@ def test_pf32_scaled_within_tolerance(engine, name):
 
 
 @pytest.mark.gpu
+def test_pf_probabilities_only_pass(engine):
+    """gap_gradients = 0: the backward pass reads only M of each recomputed
+    rectangle; the probabilities (exact and truncated) and the struct-weight /
+    base-match gradients are those of the full pass, the gap counts NaN."""
+    gs = [GoldenPF(n) for n in PF_CASES]
+    tabs = [_prepared(g) for g in gs]
+    for prec in (64, 32):
+        tol = 1e-12 if prec == 64 else 1e-6
+        for mam in (0.0, 0.001):
+            engine.pf_forward(tabs, precision=prec, min_am_prob=mam)
+            full = engine.pf_backward()
+            engine.pf_forward(tabs, precision=prec, min_am_prob=mam, gap_gradients=False)
+            lean = engine.pf_backward()
+            for a, b in zip(full, lean):
+                assert a["log_z"] == b["log_z"]
+                assert np.max(np.abs(a["am_prob"] - b["am_prob"])) <= tol
+                assert np.max(np.abs(a["bm_prob"] - b["bm_prob"])) <= tol
+                assert abs(a["dlogz_dstruct_weight"] - b["dlogz_dstruct_weight"]) <= tol * max(
+                    1.0, abs(a["dlogz_dstruct_weight"]))
+                assert np.max(np.abs(a["dlogz_dbasematch"] - b["dlogz_dbasematch"])) <= tol * max(
+                    1.0, np.max(np.abs(a["dlogz_dbasematch"])))
+                assert math.isfinite(a["dlogz_dindel"]) and math.isnan(b["dlogz_dindel"])
+                assert math.isnan(b["gap_ext_uses"]) and math.isnan(b["gap_open_uses"])
+
+
+@pytest.mark.gpu
 def test_pf_batch_equals_single(engine):
     gs = [GoldenPF(n) for n in PF_CASES]
     tabs = [g.tables for g in gs] * 2
