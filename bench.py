@@ -236,15 +236,18 @@ def port_run(paths, pairs, sample, cores):
 
 def port_baseline(pp, pairs, cores, budget_s, seed=7):
     """Time-bounded CPU baseline: the port on seeded random pairs of the
-    workload, batches of `cores` pairs until budget_s is spent."""
+    workload, batches of REF_PAIRS_PER_CORE x cores pairs (the reference
+    arm's step, so that a long pair does not idle the other cores at every
+    few pairs) until budget_s is spent."""
     rng = random.Random(seed)
     order = list(range(len(pairs)))
     rng.shuffle(order)
     done, wall = 0, 0.0
+    step = REF_PAIRS_PER_CORE * cores
     with tempfile.TemporaryDirectory(prefix="lcg_pp_") as d:
         paths = write_pp_files(pp, d)
-        for i in range(0, len(order), cores):
-            n, w, _ = port_run(paths, pairs, order[i:i + cores], cores)
+        for i in range(0, len(order), step):
+            n, w, _ = port_run(paths, pairs, order[i:i + step], cores)
             done += n
             wall += w
             if wall >= budget_s:
@@ -669,6 +672,7 @@ def run_ours(args):
         out["cpu_baseline"] = {"value": cpu_rate, "unit": "aligns/s", "cores": cores, "kind": "port",
                                "sample": f"{cpu_done} random workload pairs, PP files to alignments by "
                                          f"oracle/_build/port_locarna, one process per pair, {cores} at a time, "
+                                         f"in batches of {REF_PAIRS_PER_CORE * cores} pairs, "
                                          f"~{CPU_SAMPLE_SECONDS:.0f} s"}
         out.update(run_extras(args, eng, tables, flush_l2, value, table_prep))
         if pf_tables is not None:
