@@ -369,6 +369,8 @@ lcg_status prep_pair(const lcg_pair_tables &t, const lcg_align_opts &o, Prep &p)
     };
     p.rows_max = 0;
     p.width_max = 0;
+    p.rect_cells = 0;
+    p.am_rect.assign(std::max(na, 1), make_int2(-1, 0));
     for (size_t s = 0; s < byleft.size();) {
         size_t e = s;
         while (e < byleft.size() && byleft[e].first == byleft[s].first) ++e;
@@ -431,6 +433,23 @@ lcg_status prep_pair(const lcg_pair_tables &t, const lcg_align_opts &o, Prep &p)
                 }
             }
             g.dw_count = (int)p.dw.size() - g.dw_start;
+            // the kept rectangle (rows al..ar-1, columns bl..br-1); the
+            // traceback reads it for the arc matches of this bucket (left
+            // ends (al, bl); without lonely pairs the group's left ends are
+            // shifted, and the traceback recomputes)
+            g.rect_pitch = max_br - bl;
+            g.rect_off = -1;
+            if (p.rect_cells >= 0) {
+                const long long sz = (long long)(max_ar - al) * g.rect_pitch;
+                if (p.rect_cells + sz >= (1ll << 31)) {
+                    p.rect_cells = -1;
+                } else {
+                    g.rect_off = (int)p.rect_cells;
+                    p.rect_cells += sz;
+                    if (!nolp)
+                        for (size_t q = s; q < e; ++q) p.am_rect[byleft[q].second] = make_int2(g.rect_off, g.rect_pitch);
+                }
+            }
             p.cells += rect_cells(al + 1, max_ar, bl + 1, max_br - 1);
             g.cpl = 1;
             p.groups.push_back(g);
@@ -535,7 +554,7 @@ Slot slot_of(lcg_engine e, int k) {
 // byte offsets of one pair's tables in the arena
 struct PairOff {
     size_t sigma, scls, rcls, ccls, gapA, gapB, minc, maxc, bandoff, rowinfo, anc, cre_start, cre, crow, rowarc,
-        am_score, D, topM, res, tok, tq, segs, groups, dw, gbc, dwn, inner, sscore;
+        am_score, D, topM, res, tok, tq, segs, groups, dw, gbc, dwn, inner, sscore, rect, am_rect;
 };
 
 // One chunk of an lcg_align_pairs call: pairs [q0, q0 + nq) of the batch.
@@ -660,6 +679,21 @@ lcg_status chunk_launch(lcg_engine e, const Slot &s, const lcg_pair_tables *all,
         rows_max = std::max(rows_max, p.rows_max + 1);
         span = std::max(span, p.span);
     }
+    // Kept group rectangles: the fill writes every group's M to a rectangle
+    // of its own and the traceback walks traced arc matches on them instead
+    // of recomputing them, when the chunk's rectangles fit the engine's
+    // budget (lcg_engine_set_rect_budget) - single pairs and small batches.
+    // Not with lonely pairs excluded (shifted group left ends) and not in
+    // structure-local mode (the traceback needs all eight states).
+    bool keep = e->rect_budget > 0 && !opts->struct_local;
+    {
+        long long cells = 0;
+        for (auto &p : prep) {
+            if (p.rect_cells < 0 || (p.flags & PF_NOLP)) keep = false;
+            cells += p.rect_cells;
+        }
+        keep = keep && 4.0 * (double)cells <= (double)e->rect_budget;
+    }
     c.off.assign(npairs, PairOff{});
     std::vector<PairOff> &off = c.off;
     size_t up = 0;  // upload section (bytes)
@@ -702,6 +736,7 @@ lcg_status chunk_launch(lcg_engine e, const Slot &s, const lcg_pair_tables *all,
         o.rowarc = take(up, 4ull * p.rowarc.size());
         o.am_score = take(up, 4ull * std::max(t.num_arcmatches, 1));
         o.D = take(up, 4ull * std::max(p.num_pos, 1));
+        o.am_rect = keep ? take(up, 8ull * p.am_rect.size()) : 0;
     }
     c.down_begin = up;
     size_t dn = up;
@@ -720,6 +755,7 @@ lcg_status chunk_launch(lcg_engine e, const Slot &s, const lcg_pair_tables *all,
         PairOff &o = off[q];
         o.tq = take(dev_only, 16ull * p.tq_cap);
         o.topM = take(dev_only, 4ull * (p.n + 1) * (p.m + 1));
+        o.rect = keep ? take(dev_only, 4ull * std::max<long long>(p.rect_cells, 1)) : 0;
     }
     // normalized / penalized alignment: per pair its penalty, the selected
     // pairs and their gathered result words
@@ -810,6 +846,7 @@ lcg_status chunk_launch(lcg_engine e, const Slot &s, const lcg_pair_tables *all,
         if (!p.dwn.empty()) std::memcpy(H + o.dwn, p.dwn.data(), sizeof(int2) * p.dwn.size());
         if (!p.inner.empty()) std::memcpy(H + o.inner, p.inner.data(), sizeof(int2) * p.inner.size());
         if (!p.sscore.empty()) std::memcpy(H + o.sscore, p.sscore.data(), 4ull * p.sscore.size());
+        if (keep) std::memcpy(H + o.am_rect, p.am_rect.data(), 8ull * p.am_rect.size());
         PairDev &d = hp[q];
         std::memset(&d, 0, sizeof d);
         d.n = p.n;
@@ -862,6 +899,8 @@ lcg_status chunk_launch(lcg_engine e, const Slot &s, const lcg_pair_tables *all,
         d.segs = (int4 *)(Dv + o.segs);
         d.gbc = (const int *)(Dv + o.gbc);
         d.groups = (const GroupItem *)(Dv + o.groups);
+        d.rect = keep ? (int *)(Dv + o.rect) : nullptr;
+        d.am_rect = keep ? (const int2 *)(Dv + o.am_rect) : nullptr;
         d.dw = (const int4 *)(Dv + o.dw);
         d.dwn = p.inner.empty() ? nullptr : (const int2 *)(Dv + o.dwn);
         d.inner = p.inner.empty() ? nullptr : (const int2 *)(Dv + o.inner);
@@ -916,7 +955,7 @@ lcg_status chunk_launch(lcg_engine e, const Slot &s, const lcg_pair_tables *all,
     if (use_graph) {
         key = {(long long)(uintptr_t)Dv, (long long)(uintptr_t)H, (long long)(uintptr_t)scratch, (long long)down_begin,
                (long long)down_end, (long long)off_ctrl, (long long)off_pairs, (long long)off_queue, (long long)nitems,
-               blocks, sw, rb, stride, fast, e->counting, sl, sl_fast, opts->do_trace, npairs};
+               blocks, sw, rb, stride, fast, e->counting, sl, sl_fast, keep, opts->do_trace, npairs};
         if (s.graph->exec && s.graph->key == key) {
             CUDA_TRY(cudaGraphLaunch(s.graph->exec, st));
             ++e->last_graph_replays;
@@ -1405,6 +1444,12 @@ lcg_status lcg_align_pp_pairs(lcg_engine e, const char *const *pp_a, const char 
         if (h) lcg_prepared_free(h);
     lcg_host::free_batch(B);
     return rc;
+}
+
+lcg_status lcg_engine_set_rect_budget(lcg_engine e, int64_t bytes) {
+    if (!e) return fail(LCG_ERR_ARG, "null engine");
+    e->rect_budget = bytes > 0 ? bytes : 0;
+    return LCG_OK;
 }
 
 lcg_status lcg_engine_set_graphs(lcg_engine e, int32_t on) {

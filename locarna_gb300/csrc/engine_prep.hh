@@ -44,6 +44,11 @@ struct Prep {
     std::vector<int2> inner;                     // no lonely pairs / stacking: per am (PairDev::inner)
     std::vector<int> sscore;                     // stacking: per am (PairDev::am_sscore)
     int rows_max = 0, width_max = 0;             // over groups
+    // kept group rectangles: (ar-al) x (br-bl) ints per group, in group order
+    // (GroupItem::rect_off / rect_pitch); per arc match its group's
+    // (rect_off, rect_pitch) or (-1, 0); rect_cells = -1: too large to keep
+    long long rect_cells = 0;
+    std::vector<int2> am_rect;
     int token_cap = 0, tq_cap = 0;
     long long cells = 0;                         // M cells of all groups + top level
     std::string err;

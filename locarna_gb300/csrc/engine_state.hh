@@ -70,6 +70,8 @@ struct lcg_engine_s {
     // resident blocks per SM (0 = as many as fit) and the L2 budget of a pair
     // wave in MB (0 = default); used by lcg_align_pairs when autotune is on
     bool autotune = false;
+    // bytes of kept group rectangles a chunk may use (lcg_engine_set_rect_budget)
+    long long rect_budget = 4ll << 30;
     int tune_bps[LCG_TUNE_BUCKETS] = {0, 0, 0, 0};
     double tune_wave_mb[LCG_TUNE_BUCKETS] = {0, 0, 0, 0};
     // CUDA graphs of the chunks (lcg_engine_set_graphs): the own set's cache

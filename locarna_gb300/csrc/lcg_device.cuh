@@ -97,6 +97,14 @@ struct PairDev {
     // PF_STACK: per arc match Scoring::arcmatch(am, true), NEG where the
     // tables give LCG_STACK_NONE
     const int *am_sscore;
+    // Kept group rectangles (nullptr: not kept). The fill writes group g's M
+    // to rect + g.rect_off (row i-al, column j-bl, pitch g.rect_pitch)
+    // instead of the warp's scratch slot, and the traceback walks a traced
+    // arc match on its group's rectangle instead of recomputing it; am_rect
+    // holds per arc match its group's (rect_off, rect_pitch), (-1, 0) when no
+    // group computes it.
+    int *rect;
+    const int2 *am_rect;
 };
 
 // Scoring::basematch(i,j) from the class table or the dense table
@@ -129,6 +137,7 @@ struct GroupItem {
     int dw_start, dw_count;  // D writes: int4 (D index, corner row, corner column, score), rows ascending
     int top;                 // 1 for the top-level item
     int cpl;                 // columns per lane: ceil(widest band row of the group / 32), <= 4
+    int rect_off, rect_pitch;  // the group's kept rectangle in PairDev::rect (when kept)
 };
 
 // anchor helpers: reference AnchorConstraints::allowed_match/del/ins

@@ -58,9 +58,12 @@ __global__ void __launch_bounds__(FILL_WARPS * 32, FILL_MIN_BLOCKS)
         if (it.top) {
             run_top<COUNT, FAST>(P, it.cpl, sbase, rb, status, abort_flag, counters);
         } else {
-            run_group<false, true, true, COUNT, FAST>(P, it.cpl, it.al, it.ar, it.bl, it.br, Mg, sw, sbase, rb,
-                                                dw + it.dw_start, it.dw_count, true, true, false, status,
-                                                abort_flag, nullptr, counters);
+            // the group's own kept rectangle, or the warp's scratch slot
+            const bool kept = P.rect && it.rect_off >= 0;
+            run_group<false, true, true, COUNT, FAST>(P, it.cpl, it.al, it.ar, it.bl, it.br,
+                                                kept ? P.rect + it.rect_off : Mg, kept ? it.rect_pitch : sw,
+                                                sbase, rb, dw + it.dw_start, it.dw_count, true, true, false,
+                                                status, abort_flag, nullptr, counters);
         }
         __syncwarp();
     }
@@ -119,13 +122,23 @@ __global__ void __launch_bounds__(TRACE_WARPS * 32)
                 continue;
             }
         }
-        const int cpl = min(4, max(1, (min(ends.w - ends.z, P.maxband) + 31) / 32));
-        run_group<false, false, false>(P, cpl, ends.x, ends.y, ends.z, ends.w, Mg, sw, sbase, rb, nullptr, 0,
-                                       true, true, false, status, (volatile int *)&dummy_abort, nullptr);
+        // the arc match's rectangle: its group's kept one from the fill, else
+        // recomputed into the pair's scratch slot
+        const int2 kr = P.am_rect ? P.am_rect[k] : make_int2(-1, 0);
+        const int *Mw = Mg;
+        int pw = sw;
+        if (kr.x >= 0) {
+            Mw = P.rect + kr.x;
+            pw = kr.y;
+        } else {
+            const int cpl = min(4, max(1, (min(ends.w - ends.z, P.maxband) + 31) / 32));
+            run_group<false, false, false>(P, cpl, ends.x, ends.y, ends.z, ends.w, Mg, sw, sbase, rb, nullptr, 0,
+                                           true, true, false, status, (volatile int *)&dummy_abort, nullptr);
+        }
         __syncwarp();
         if (lane == 0) {
             const int start = w.ntok;
-            walk(w, Mg, sw, ends.x, ends.z, ends.y - 1, ends.w - 1, false, status);
+            walk(w, Mw, pw, ends.x, ends.z, ends.y - 1, ends.w - 1, false, status);
             if (nseg < P.tq_cap + 1) P.segs[nseg] = make_int4(k, start, w.ntok, 0);
             ++nseg;
         }

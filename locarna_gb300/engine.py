@@ -92,6 +92,8 @@ def _load_locked(path):
     lib.lcg_pf_forward.restype = C.c_int32
     lib.lcg_pf_backward.argtypes = [C.c_void_p, C.POINTER(lcg_pf_grad_spec), C.POINTER(lcg_pf_result)]
     lib.lcg_pf_backward.restype = C.c_int32
+    lib.lcg_engine_set_rect_budget.argtypes = [C.c_void_p, C.c_int64]
+    lib.lcg_engine_set_rect_budget.restype = C.c_int32
     lib.lcg_pf_last_timing.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]
     lib.lcg_pf_last_timing.restype = C.c_int32
     _lib = lib
@@ -264,6 +266,11 @@ class Engine:
         a, b = C.c_int64(), C.c_int64()
         _check(self.lib, self.lib.lcg_engine_last_graphs(self.h, C.byref(a), C.byref(b)))
         return a.value, b.value
+
+    def set_rect_budget(self, nbytes):
+        """lcg_engine_set_rect_budget: bytes of kept group rectangles per
+        chunk (0: the traceback always recomputes)."""
+        _check(self.lib, self.lib.lcg_engine_set_rect_budget(self.h, int(nbytes)))
 
     def set_autotune(self, on):
         _check(self.lib, self.lib.lcg_engine_set_autotune(self.h, int(bool(on))))

@@ -128,7 +128,9 @@ def test_pf_probabilities_only_pass(engine):
             engine.pf_forward(tabs, precision=prec, min_am_prob=mam, gap_gradients=False)
             lean = engine.pf_backward()
             for a, b in zip(full, lean):
-                assert a["log_z"] == b["log_z"]
+                # the forward pass is the same; its arc-term sums are shared-
+                # memory atomics, so the summation order may differ
+                assert abs(a["log_z"] - b["log_z"]) <= tol * max(1.0, abs(a["log_z"]))
                 assert np.max(np.abs(a["am_prob"] - b["am_prob"])) <= tol
                 assert np.max(np.abs(a["bm_prob"] - b["bm_prob"])) <= tol
                 assert abs(a["dlogz_dstruct_weight"] - b["dlogz_dstruct_weight"]) <= tol * max(

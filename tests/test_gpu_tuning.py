@@ -93,3 +93,42 @@ def test_graph_across_many_layouts_keeps_results(engine):
                     assert_same_result(r, ref[k % 4], f"replay {n} pair {k}")
     finally:
         eng.close()
+
+
+@pytest.mark.gpu
+def test_kept_rectangles_give_the_same_alignments(engine):
+    """With the group rectangles kept (the traceback walks the fill's
+    rectangles) and without (it recomputes them), every golden case, a batch
+    and the alignment modes give the same results."""
+    from golden_io import Golden, sankoff_golden_names
+    gs = [Golden(n) for n in sankoff_golden_names()]
+    try:
+        for g in gs:
+            kw = g.align_kwargs()
+            if g.kbest:
+                continue
+            engine.set_rect_budget(4 << 30)
+            a = engine.align_pairs([g.tables], **kw)[0]
+            engine.set_rect_budget(0)
+            b = engine.align_pairs([g.tables], **kw)[0]
+            assert_same_result(a, b, g.name)
+        plain = dict(struct_local=False, sequ_local=False, free_endgaps="----")
+        tabs = [g.tables for g in gs if not g.kbest and g.align_kwargs() == plain][:24]
+        assert len(tabs) >= 8
+        for kw in ({}, {"sequ_local": True}, {"sequ_local": True, "normalized": 100}, {"penalized": 50}):
+            engine.set_rect_budget(4 << 30)
+            a = engine.align_pairs(tabs, **kw)
+            engine.set_rect_budget(0)
+            b = engine.align_pairs(tabs, **kw)
+            for k, (x, y) in enumerate(zip(a, b)):
+                assert_same_result(x, y, f"{kw} pair {k}")
+        engine.set_rect_budget(4 << 30)
+        ka = engine.align_kbest(tabs[:6], 4, sequ_local=True)
+        engine.set_rect_budget(0)
+        kb = engine.align_kbest(tabs[:6], 4, sequ_local=True)
+        for k, (hx, hy) in enumerate(zip(ka, kb)):
+            assert len(hx) == len(hy)
+            for x, y in zip(hx, hy):
+                assert_same_result(x, y, f"kbest pair {k}")
+    finally:
+        engine.set_rect_budget(4 << 30)
