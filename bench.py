@@ -55,7 +55,7 @@ REF_PAIRS_PER_CORE = 4  # pairs per host core in one step of the reference arm
 # 496-pair case (profiles/sankoff_fill_small_496pairs.md: dram read + write
 # bytes of one launch / the launch's cells); the traffic of a launch of the
 # workload is this times its cells
-FILL_DRAM_BYTES_PER_CELL = 5.59e9 / 1.20e9
+FILL_DRAM_BYTES_PER_CELL = (1.598e9 + 3.921e9) / 1.2018e9
 
 
 def log(*a):
