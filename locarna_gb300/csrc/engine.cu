@@ -1429,9 +1429,16 @@ lcg_status lcg_align_pp_pairs(lcg_engine e, const char *const *pp_a, const char 
     if (!e || !pp_a || !pp_b || !opts || !results || npairs < 0) return fail(LCG_ERR_ARG, "NULL argument");
     if (npairs == 0) return LCG_OK;
     CUDA_TRY(cudaSetDevice(e->device));
+    // the first chunk's envelopes are finished before its tables are built;
+    // the other pairs' run on the device meanwhile
+    const bool modv = opts->normalized || opts->penalized;
+    const int first = modv ? npairs : std::min<int>(npairs, chunk_size(npairs, e->chunk_pairs));
     lcg_host::StagedBatch *B = nullptr;
-    lcg_status rc = lcg_host::stage_batch(e, pp_a, pp_b, npairs, popts, &B, host_envelopes);
-    if (rc != LCG_OK) return rc;
+    lcg_status rc = lcg_host::stage_batch(e, pp_a, pp_b, npairs, popts, &B, host_envelopes, first);
+    if (rc != LCG_OK) {
+        lcg_host::free_batch(B);
+        return rc;
+    }
     std::vector<lcg_prepared> handles((size_t)npairs, nullptr);
     std::vector<lcg_pair_tables> tabs((size_t)npairs);
     const std::function<lcg_status(int, int)> ready = [&](int q0, int nq) {
@@ -1442,6 +1449,7 @@ lcg_status lcg_align_pp_pairs(lcg_engine e, const char *const *pp_a, const char 
     rc = align_impl(e, tabs.data(), npairs, opts, results, &ready);
     for (auto h : handles)
         if (h) lcg_prepared_free(h);
+    if (host_envelopes) *host_envelopes = lcg_host::batch_host_envelopes(B);
     lcg_host::free_batch(B);
     return rc;
 }

@@ -64,8 +64,13 @@ void set_error(const std::string &msg);
 // the two stages of lcg_prepare_pairs (host_prep.cpp): inputs, bands and
 // envelopes of every pair; then the tables of pairs [q0, q0 + nq)
 struct StagedBatch;
+// first: the pairs whose GPU envelopes are finished before it returns; the
+// others' are enqueued and finished by the first finish_tables that needs
+// them. host_envelopes: the host-path envelopes so far (batch_host_envelopes
+// gives the final count).
 lcg_status stage_batch(lcg_engine eng, const char *const *pp_a, const char *const *pp_b, int32_t npairs,
-                       const lcg_prep_opts *opts, StagedBatch **out, int32_t *host_envelopes);
+                       const lcg_prep_opts *opts, StagedBatch **out, int32_t *host_envelopes, int32_t first);
+int batch_host_envelopes(const StagedBatch *B);
 lcg_status finish_tables(StagedBatch *B, int q0, int nq, lcg_prepared *out);
 void free_batch(StagedBatch *B);
 

@@ -319,13 +319,21 @@ void reset_transfer(lcg_engine eng) {
     eng->prep_d2h = 0;
 }
 
-lcg_status compute(lcg_engine eng, const Params &Pm, int npairs, const PairIn *in, PairOut *out, std::string &err) {
-    if (npairs <= 0) return LCG_OK;
-    cudaError_t ce = cudaSetDevice(eng->device);
-    if (ce != cudaSuccess) {
-        err = std::string("cudaSetDevice: ") + cudaGetErrorString(ce);
-        return LCG_ERR_CUDA;
-    }
+struct Pending {
+    std::vector<std::pair<int, size_t>> outs;  // (pair, output offset in the pinned staging)
+    PairOut *out = nullptr;
+    const PairIn *in = nullptr;
+    size_t out_begin = 0, out_end = 0;
+    cudaEvent_t done = nullptr;
+};
+
+// One wave (pairs [q0, q1) whose rows fit the device budget) staged,
+// enqueued and, with wait, finished; without wait the wave's outputs are
+// described in *pend.
+static lcg_status enqueue_wave(lcg_engine eng, const EnvConst &C, int q0, int q1, const PairIn *in, PairOut *out,
+                               bool wait, Pending *pend, std::string &err);
+
+static EnvConst make_const(const Params &Pm) {
     EnvConst C;
     C.sw = Pm.sw;
     C.itemp = 1.0 / Pm.temp;
@@ -345,127 +353,209 @@ lcg_status compute(lcg_engine eng, const Params &Pm, int npairs, const PairIn *i
     C.rfe = rfe;
     C.exp_limit = Pm.exp_limit;
 
+    return C;
+}
+
+static size_t wave_end(const PairIn *in, int q0, int npairs) {
     // waves of pairs whose forward rows fit a device budget
     const size_t budget = (size_t)6 << 30;
-    int q0 = 0;
-    while (q0 < npairs) {
-        int q1 = q0;
-        std::vector<size_t> in_off, out_off, dev_off;
-        size_t fz_bytes = 0;
-        auto take = [](size_t &cur, size_t b) {
-            size_t o = cur;
-            cur = align16(cur + b);
-            return o;
-        };
-        for (; q1 < npairs; ++q1) {
-            const size_t n1 = (size_t)in[q1].n + 1, m1 = (size_t)in[q1].m + 1;
-            const size_t f = 8 * (3 * n1 * m1 + 6 * m1) + 4 * n1;
-            if (q1 > q0 && fz_bytes + f > budget) break;
-            fz_bytes += f;
-        }
-        const int nq = q1 - q0;
-        // host staging: [EnvDev x nq][per pair inputs][per pair outputs]
-        size_t hs = 0;
-        const size_t o_pairs = take(hs, sizeof(EnvDev) * nq);
-        in_off.resize(nq);
-        for (int k = 0; k < nq; ++k) {
-            const PairIn &p = in[q0 + k];
-            const size_t n1 = (size_t)p.n + 1, m1 = (size_t)p.m + 1;
-            in_off[k] = take(hs, 4 * (2 * n1) + 8 * (2 * n1 + 2 * m1) + n1 + m1);
-        }
-        const size_t out_begin = hs;
-        out_off.resize(nq);
-        for (int k = 0; k < nq; ++k) out_off[k] = take(hs, 4 * (2 * ((size_t)in[q0 + k].n + 1) + 1));
-        const size_t out_end = hs;
-        size_t ds = hs;  // device-only section after the mirrored staging
-        dev_off.resize(nq);
-        for (int k = 0; k < nq; ++k) {
-            const size_t n1 = (size_t)in[q0 + k].n + 1, m1 = (size_t)in[q0 + k].m + 1;
-            dev_off[k] = take(ds, 8 * (3 * n1 * m1 + 6 * m1) + 4 * n1);
-        }
-        if (ds > eng->env_dev_cap) {
-            if (eng->env_dev) cudaFree(eng->env_dev);
-            eng->env_dev = nullptr;
-            eng->env_dev_cap = 0;
-            if (cudaMalloc(&eng->env_dev, ds + ds / 4) != cudaSuccess) {
-                err = "envelope device allocation failed";
-                return LCG_ERR_NOMEM;
-            }
-            eng->env_dev_cap = ds + ds / 4;
-        }
-        if (out_end > eng->env_host_cap) {
-            if (eng->env_host) cudaFreeHost(eng->env_host);
-            eng->env_host = nullptr;
-            eng->env_host_cap = 0;
-            if (cudaMallocHost(&eng->env_host, out_end + out_end / 4) != cudaSuccess) {
-                err = "envelope pinned allocation failed";
-                return LCG_ERR_NOMEM;
-            }
-            eng->env_host_cap = out_end + out_end / 4;
-        }
-        char *H = eng->env_host, *D = eng->env_dev;
-        EnvDev *hp = (EnvDev *)(H + o_pairs);
-        for (int k = 0; k < nq; ++k) {
-            const PairIn &p = in[q0 + k];
-            const int n1 = p.n + 1, m1 = p.m + 1;
-            char *h = H + in_off[k];
-            char *d = D + in_off[k];
-            int *minc = (int *)h, *maxc = minc + n1;
-            std::memcpy(minc, p.minc, 4ull * n1);
-            std::memcpy(maxc, p.maxc, 4ull * n1);
-            double *sdA = (double *)(h + 8ull * n1), *suA = sdA + n1, *sdB = suA + n1, *suB = sdB + m1;
-            std::memcpy(sdA, p.sdA, 8ull * n1);
-            std::memcpy(suA, p.suA, 8ull * n1);
-            std::memcpy(sdB, p.sdB, 8ull * m1);
-            std::memcpy(suB, p.suB, 8ull * m1);
-            signed char *ca = (signed char *)(suB + m1), *cb = ca + n1;
-            std::memcpy(ca, p.ca, n1);
-            std::memcpy(cb, p.cb, m1);
-            EnvDev &v = hp[k];
-            v.n = p.n;
-            v.m = p.m;
-            v.minc = (const int *)d;
-            v.maxc = (const int *)d + n1;
-            v.sdA = (const double *)(d + 8ull * n1);
-            v.suA = v.sdA + n1;
-            v.sdB = v.suA + n1;
-            v.suB = v.sdB + m1;
-            v.ca = (const signed char *)(v.suB + m1);
-            v.cb = v.ca + n1;
-            char *od = D + out_off[k];
-            v.newmin = (int *)od;
-            v.newmax = (int *)od + n1;
-            v.flag = (int *)od + 2 * n1;
-            char *dd = D + dev_off[k];
-            v.fz = (double *)dd;
-            v.rz = v.fz + 3ull * n1 * m1;
-            v.fexp = (int *)(v.rz + 6ull * m1);
-        }
-        cudaStream_t st = eng->stream;
-        auto fail_cuda = [&](cudaError_t x, const char *what) {
-            err = std::string(what) + ": " + cudaGetErrorString(x);
-            cudaStreamSynchronize(st);
-            return LCG_ERR_CUDA;
-        };
-        if ((ce = cudaMemcpyAsync(D, H, out_begin, cudaMemcpyHostToDevice, st)) != cudaSuccess)
-            return fail_cuda(ce, "envelope upload");
-        const int blocks = (nq + ENV_WARPS - 1) / ENV_WARPS;
-        envelope_kernel<<<blocks, ENV_WARPS * 32, 0, st>>>((const EnvDev *)(D + o_pairs), nq, C);
-        if ((ce = cudaGetLastError()) != cudaSuccess) return fail_cuda(ce, "envelope launch");
-        if ((ce = cudaMemcpyAsync(H + out_begin, D + out_begin, out_end - out_begin, cudaMemcpyDeviceToHost, st)) !=
-            cudaSuccess)
-            return fail_cuda(ce, "envelope download");
-        if ((ce = cudaStreamSynchronize(st)) != cudaSuccess) return fail_cuda(ce, "envelope kernel");
-        eng->prep_h2d += (long long)out_begin;
-        eng->prep_d2h += (long long)(out_end - out_begin);
-        for (int k = 0; k < nq; ++k) {
-            const int n1 = in[q0 + k].n + 1;
-            const int *o = (const int *)(H + out_off[k]);
-            std::memcpy(out[q0 + k].newmin, o, 4ull * n1);
-            std::memcpy(out[q0 + k].newmax, o + n1, 4ull * n1);
-            out[q0 + k].flag = o[2 * n1];
-        }
+    size_t fz_bytes = 0;
+    int q1 = q0;
+    for (; q1 < npairs; ++q1) {
+        const size_t n1 = (size_t)in[q1].n + 1, m1 = (size_t)in[q1].m + 1;
+        const size_t f = 8 * (3 * n1 * m1 + 6 * m1) + 4 * n1;
+        if (q1 > q0 && fz_bytes + f > budget) break;
+        fz_bytes += f;
+    }
+    return (size_t)q1;
+}
+
+lcg_status compute(lcg_engine eng, const Params &Pm, int npairs, const PairIn *in, PairOut *out, std::string &err) {
+    if (npairs <= 0) return LCG_OK;
+    cudaError_t ce = cudaSetDevice(eng->device);
+    if (ce != cudaSuccess) {
+        err = std::string("cudaSetDevice: ") + cudaGetErrorString(ce);
+        return LCG_ERR_CUDA;
+    }
+    const EnvConst C = make_const(Pm);
+    for (int q0 = 0; q0 < npairs;) {
+        const int q1 = (int)wave_end(in, q0, npairs);
+        lcg_status rc = enqueue_wave(eng, C, q0, q1, in, out, true, nullptr, err);
+        if (rc != LCG_OK) return rc;
         q0 = q1;
+    }
+    return LCG_OK;
+}
+
+lcg_status compute_begin(lcg_engine eng, const Params &Pm, int npairs, const PairIn *in, PairOut *out,
+                         Pending **pending, std::string &err) {
+    *pending = nullptr;
+    if (npairs <= 0) return LCG_OK;
+    cudaError_t ce = cudaSetDevice(eng->device);
+    if (ce != cudaSuccess) {
+        err = std::string("cudaSetDevice: ") + cudaGetErrorString(ce);
+        return LCG_ERR_CUDA;
+    }
+    // more than one wave: computed now (the pinned staging holds one wave)
+    if ((int)wave_end(in, 0, npairs) < npairs) return compute(eng, Pm, npairs, in, out, err);
+    auto *p = new Pending;
+    lcg_status rc = enqueue_wave(eng, make_const(Pm), 0, npairs, in, out, false, p, err);
+    if (rc != LCG_OK) {
+        if (p->done) cudaEventDestroy(p->done);
+        delete p;
+        return rc;
+    }
+    *pending = p;
+    return LCG_OK;
+}
+
+lcg_status compute_end(lcg_engine eng, Pending *p, std::string &err) {
+    if (!p) return LCG_OK;
+    const cudaError_t ce = cudaEventSynchronize(p->done);
+    cudaEventDestroy(p->done);
+    if (ce != cudaSuccess) {
+        err = std::string("envelope kernel: ") + cudaGetErrorString(ce);
+        delete p;
+        return LCG_ERR_CUDA;
+    }
+    const char *H = eng->env_host;
+    eng->prep_h2d += (long long)p->out_begin;
+    eng->prep_d2h += (long long)(p->out_end - p->out_begin);
+    for (auto &x : p->outs) {
+        const int n1 = p->in[x.first].n + 1;
+        const int *o = (const int *)(H + x.second);
+        std::memcpy(p->out[x.first].newmin, o, 4ull * n1);
+        std::memcpy(p->out[x.first].newmax, o + n1, 4ull * n1);
+        p->out[x.first].flag = o[2 * n1];
+    }
+    delete p;
+    return LCG_OK;
+}
+
+static lcg_status enqueue_wave(lcg_engine eng, const EnvConst &C, int q0, int q1, const PairIn *in, PairOut *out,
+                               bool wait, Pending *pend, std::string &err) {
+    cudaError_t ce;
+    std::vector<size_t> in_off, out_off, dev_off;
+    auto take = [](size_t &cur, size_t b) {
+        size_t o = cur;
+        cur = align16(cur + b);
+        return o;
+    };
+    const int nq = q1 - q0;
+    // host staging: [EnvDev x nq][per pair inputs][per pair outputs]
+    size_t hs = 0;
+    const size_t o_pairs = take(hs, sizeof(EnvDev) * nq);
+    in_off.resize(nq);
+    for (int k = 0; k < nq; ++k) {
+        const PairIn &p = in[q0 + k];
+        const size_t n1 = (size_t)p.n + 1, m1 = (size_t)p.m + 1;
+        in_off[k] = take(hs, 4 * (2 * n1) + 8 * (2 * n1 + 2 * m1) + n1 + m1);
+    }
+    const size_t out_begin = hs;
+    out_off.resize(nq);
+    for (int k = 0; k < nq; ++k) out_off[k] = take(hs, 4 * (2 * ((size_t)in[q0 + k].n + 1) + 1));
+    const size_t out_end = hs;
+    size_t ds = hs;  // device-only section after the mirrored staging
+    dev_off.resize(nq);
+    for (int k = 0; k < nq; ++k) {
+        const size_t n1 = (size_t)in[q0 + k].n + 1, m1 = (size_t)in[q0 + k].m + 1;
+        dev_off[k] = take(ds, 8 * (3 * n1 * m1 + 6 * m1) + 4 * n1);
+    }
+    // the buffers are reused only after the previous computation ended
+    // (compute waits; a pending one is ended before the next begins)
+    if (ds > eng->env_dev_cap) {
+        if (eng->env_dev) cudaFree(eng->env_dev);
+        eng->env_dev = nullptr;
+        eng->env_dev_cap = 0;
+        if (cudaMalloc(&eng->env_dev, ds + ds / 4) != cudaSuccess) {
+            err = "envelope device allocation failed";
+            return LCG_ERR_NOMEM;
+        }
+        eng->env_dev_cap = ds + ds / 4;
+    }
+    if (out_end > eng->env_host_cap) {
+        if (eng->env_host) cudaFreeHost(eng->env_host);
+        eng->env_host = nullptr;
+        eng->env_host_cap = 0;
+        if (cudaMallocHost(&eng->env_host, out_end + out_end / 4) != cudaSuccess) {
+            err = "envelope pinned allocation failed";
+            return LCG_ERR_NOMEM;
+        }
+        eng->env_host_cap = out_end + out_end / 4;
+    }
+    char *H = eng->env_host, *D = eng->env_dev;
+    EnvDev *hp = (EnvDev *)(H + o_pairs);
+    for (int k = 0; k < nq; ++k) {
+        const PairIn &p = in[q0 + k];
+        const int n1 = p.n + 1, m1 = p.m + 1;
+        char *h = H + in_off[k];
+        char *d = D + in_off[k];
+        int *minc = (int *)h, *maxc = minc + n1;
+        std::memcpy(minc, p.minc, 4ull * n1);
+        std::memcpy(maxc, p.maxc, 4ull * n1);
+        double *sdA = (double *)(h + 8ull * n1), *suA = sdA + n1, *sdB = suA + n1, *suB = sdB + m1;
+        std::memcpy(sdA, p.sdA, 8ull * n1);
+        std::memcpy(suA, p.suA, 8ull * n1);
+        std::memcpy(sdB, p.sdB, 8ull * m1);
+        std::memcpy(suB, p.suB, 8ull * m1);
+        signed char *ca = (signed char *)(suB + m1), *cb = ca + n1;
+        std::memcpy(ca, p.ca, n1);
+        std::memcpy(cb, p.cb, m1);
+        EnvDev &v = hp[k];
+        v.n = p.n;
+        v.m = p.m;
+        v.minc = (const int *)d;
+        v.maxc = (const int *)d + n1;
+        v.sdA = (const double *)(d + 8ull * n1);
+        v.suA = v.sdA + n1;
+        v.sdB = v.suA + n1;
+        v.suB = v.sdB + m1;
+        v.ca = (const signed char *)(v.suB + m1);
+        v.cb = v.ca + n1;
+        char *od = D + out_off[k];
+        v.newmin = (int *)od;
+        v.newmax = (int *)od + n1;
+        v.flag = (int *)od + 2 * n1;
+        char *dd = D + dev_off[k];
+        v.fz = (double *)dd;
+        v.rz = v.fz + 3ull * n1 * m1;
+        v.fexp = (int *)(v.rz + 6ull * m1);
+    }
+    cudaStream_t st = eng->stream;
+    auto fail_cuda = [&](cudaError_t x, const char *what) {
+        err = std::string(what) + ": " + cudaGetErrorString(x);
+        cudaStreamSynchronize(st);
+        return LCG_ERR_CUDA;
+    };
+    if ((ce = cudaMemcpyAsync(D, H, out_begin, cudaMemcpyHostToDevice, st)) != cudaSuccess)
+        return fail_cuda(ce, "envelope upload");
+    const int blocks = (nq + ENV_WARPS - 1) / ENV_WARPS;
+    envelope_kernel<<<blocks, ENV_WARPS * 32, 0, st>>>((const EnvDev *)(D + o_pairs), nq, C);
+    if ((ce = cudaGetLastError()) != cudaSuccess) return fail_cuda(ce, "envelope launch");
+    if ((ce = cudaMemcpyAsync(H + out_begin, D + out_begin, out_end - out_begin, cudaMemcpyDeviceToHost, st)) !=
+        cudaSuccess)
+        return fail_cuda(ce, "envelope download");
+    if (!wait) {
+        // finished by compute_end: an event after the download
+        if ((ce = cudaEventCreateWithFlags(&pend->done, cudaEventDisableTiming)) != cudaSuccess)
+            return fail_cuda(ce, "envelope event");
+        if ((ce = cudaEventRecord(pend->done, st)) != cudaSuccess) return fail_cuda(ce, "envelope event");
+        pend->in = in;
+        pend->out = out;
+        pend->out_begin = out_begin;
+        pend->out_end = out_end;
+        for (int k = 0; k < nq; ++k) pend->outs.emplace_back(q0 + k, out_off[k]);
+        return LCG_OK;
+    }
+    if ((ce = cudaStreamSynchronize(st)) != cudaSuccess) return fail_cuda(ce, "envelope kernel");
+    eng->prep_h2d += (long long)out_begin;
+    eng->prep_d2h += (long long)(out_end - out_begin);
+    for (int k = 0; k < nq; ++k) {
+        const int n1 = in[q0 + k].n + 1;
+        const int *o = (const int *)(H + out_off[k]);
+        std::memcpy(out[q0 + k].newmin, o, 4ull * n1);
+        std::memcpy(out[q0 + k].newmax, o + n1, 4ull * n1);
+        out[q0 + k].flag = o[2 * n1];
     }
     return LCG_OK;
 }

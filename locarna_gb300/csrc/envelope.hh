@@ -49,6 +49,16 @@ struct PairOut {
 // pair). Returns LCG_OK or an error with err set.
 lcg_status compute(lcg_engine eng, const Params &P, int npairs, const PairIn *in, PairOut *out, std::string &err);
 
+// The same, enqueued on the engine's stream without waiting (the inputs are
+// copied before it returns; the outputs stay valid for compute_end). Work
+// enqueued on that stream later runs after it. One pending computation per
+// engine; compute_end waits for it and fills out[]. The pending state is
+// opaque (Pending*); compute_end frees it.
+struct Pending;
+lcg_status compute_begin(lcg_engine eng, const Params &P, int npairs, const PairIn *in, PairOut *out,
+                         Pending **pending, std::string &err);
+lcg_status compute_end(lcg_engine eng, Pending *pending, std::string &err);
+
 // Zero the engine's count of the bytes a table preparation copied (at the
 // start of each lcg_prepare_pairs call; compute() adds to it).
 void reset_transfer(lcg_engine eng);

@@ -1126,13 +1126,70 @@ namespace lcg_host {
 // A batch of pairs between the two stages of lcg_prepare_pairs: inputs read,
 // bands and envelopes done for every pair (stage_batch); the tables built for
 // a range of pairs at a time (finish_tables), so that a caller can build the
-// tables of one chunk while the device aligns the previous one.
+// tables of one chunk while the device aligns the previous one. With
+// first < npairs, stage_batch finishes the GPU envelopes of pairs [0, first)
+// only and leaves those of the other pairs enqueued on the engine's stream
+// (they run while the host builds the first pairs' tables); the first
+// finish_tables past `first` waits for them.
+struct EnvBuf {
+    std::vector<int8_t> ca, cb;
+    std::vector<double> sdA, suA, sdB, suB;
+    std::vector<int32_t> minc, maxc, nmin, nmax;
+};
 struct StagedBatch {
     std::vector<Staged> st;
+    lcg_engine eng = nullptr;
+    std::vector<EnvBuf> buf;               // per pair
+    std::vector<lcg_env::PairIn> in;       // per GPU pair
+    std::vector<lcg_env::PairOut> res;     // per GPU pair
+    std::vector<int> kof;                  // per pair: its GPU index, or -1 (host envelope)
+    int first = 0;                         // pairs whose envelopes stage_batch finished
+    lcg_env::Pending *pending = nullptr;   // the GPU envelopes of the other pairs
+    int host_envelopes = 0;
+    ~StagedBatch() {
+        std::string err;
+        if (pending) lcg_env::compute_end(eng, pending, err);  // nothing of a batch stays in flight
+    }
 };
 
+// the envelope of pairs [q0, q1): the GPU result, or the host path for the
+// pairs the kernel does not take or flagged
+static void apply_envelopes(StagedBatch &B, int q0, int q1) {
+    std::atomic<int> host{0};
+    host_parallel(q1 - q0, [&](int k) {
+        const int q = q0 + k;
+        guarded(B.st[q], [&]() {
+            const int g = B.kof[q];
+            if (g >= 0 && B.res[g].flag == 0) {
+                apply_envelope_rows(B.st[q].tc, B.buf[q].nmin.data(), B.buf[q].nmax.data());
+                B.st[q].P->envelope_ok = 1;
+            } else {
+                ++host;
+                stage_envelope_host(B.st[q]);
+            }
+        });
+    });
+    B.host_envelopes += host.load();
+}
+
+// the pending GPU envelopes (pairs [first, npairs)), once
+static lcg_status finish_envelopes(StagedBatch &B) {
+    if (B.first >= (int)B.st.size()) return LCG_OK;
+    std::string err;
+    lcg_env::Pending *p = B.pending;
+    B.pending = nullptr;
+    lcg_status rc = lcg_env::compute_end(B.eng, p, err);
+    if (rc != LCG_OK) {
+        lcg_host::set_error(err);
+        return rc;
+    }
+    apply_envelopes(B, B.first, (int)B.st.size());
+    B.first = (int)B.st.size();
+    return LCG_OK;
+}
+
 lcg_status stage_batch(lcg_engine eng, const char *const *pp_a, const char *const *pp_b, int32_t npairs,
-                       const lcg_prep_opts *opts, StagedBatch **out, int32_t *host_envelopes) {
+                       const lcg_prep_opts *opts, StagedBatch **out, int32_t *host_envelopes, int32_t first) {
     if (!eng || !pp_a || !pp_b || !out || npairs < 0) {
         lcg_host::set_error("NULL argument");
         return LCG_ERR_ARG;
@@ -1141,6 +1198,8 @@ lcg_status stage_batch(lcg_engine eng, const char *const *pp_a, const char *cons
     if (host_envelopes) *host_envelopes = 0;
     lcg_env::reset_transfer(eng);
     auto B = std::make_unique<StagedBatch>();
+    B->eng = eng;
+    B->first = npairs;
     if (npairs == 0) {
         *out = B.release();
         return LCG_OK;
@@ -1203,27 +1262,26 @@ lcg_status stage_batch(lcg_engine eng, const char *const *pp_a, const char *cons
         const bool dbl = o.pf_precision == 0;
         ep.exp_limit = dbl ? 1000 : 16000;
         const int max_len_sum = dbl ? 1000 : 16000;
-        struct Buf {
-            std::vector<int8_t> ca, cb;
-            std::vector<double> sdA, suA, sdB, suB;
-            std::vector<int32_t> minc, maxc, nmin, nmax;
-        };
-        std::vector<Buf> buf(npairs);
-        std::vector<lcg_env::PairIn> in;
-        std::vector<lcg_env::PairOut> res;
+        std::vector<EnvBuf> &buf = B->buf;
+        buf.resize(npairs);
+        std::vector<lcg_env::PairIn> &in = B->in;
+        std::vector<lcg_env::PairOut> &res = B->res;
         std::vector<int> gpu_q;
+        B->kof.assign(npairs, -1);
         // the kernel scores single sequences; profiles take the host path
         for (int q = 0; q < npairs; ++q)
             if (st[q].pa->len + st[q].pb->len <= max_len_sum && st[q].pa->in.rows.size() == 1 &&
-                st[q].pb->in.rows.size() == 1)
+                st[q].pb->in.rows.size() == 1) {
+                B->kof[q] = (int)gpu_q.size();
                 gpu_q.push_back(q);
+            }
         in.resize(gpu_q.size());
         res.resize(gpu_q.size());
         host_parallel((int)gpu_q.size(), [&](int k) {
             const int q = gpu_q[k];
             const Side &SA = *st[q].pa, &SB = *st[q].pb;
             const Staged &S = st[q];
-            Buf &b = buf[q];
+            EnvBuf &b = buf[q];
             const int n = SA.len, m = SB.len;
             b.ca.assign(n + 1, -1);
             b.cb.assign(m + 1, -1);
@@ -1249,34 +1307,35 @@ lcg_status stage_batch(lcg_engine eng, const char *const *pp_a, const char *cons
                                    b.sdB.data(), b.suB.data(), b.minc.data(), b.maxc.data()};
             res[k] = lcg_env::PairOut{b.nmin.data(), b.nmax.data(), 0};
         });
+        // the first pairs' envelopes now; the others enqueued behind them
+        const int f = std::max(0, std::min<int>(first, npairs));
+        const int kf = (int)(std::lower_bound(gpu_q.begin(), gpu_q.end(), f) - gpu_q.begin());
         std::string err;
-        lcg_status rc = lcg_env::compute(eng, ep, (int)gpu_q.size(), in.data(), res.data(), err);
+        lcg_status rc = lcg_env::compute(eng, ep, kf, in.data(), res.data(), err);
+        if (rc == LCG_OK && kf < (int)gpu_q.size())
+            rc = lcg_env::compute_begin(eng, ep, (int)gpu_q.size() - kf, in.data() + kf, res.data() + kf,
+                                        &B->pending, err);
         if (rc != LCG_OK) {
             lcg_host::set_error(err);
             return rc;
         }
-        std::vector<char> on_gpu(npairs, 0);
-        for (size_t k = 0; k < gpu_q.size(); ++k) on_gpu[gpu_q[k]] = res[k].flag == 0;
-        int fallbacks = 0;
-        for (int q = 0; q < npairs; ++q) fallbacks += !on_gpu[q];
-        if (host_envelopes) *host_envelopes = fallbacks;
-        host_parallel(npairs, [&](int q) {
-            guarded(st[q], [&]() {
-                if (on_gpu[q]) {
-                    apply_envelope_rows(st[q].tc, buf[q].nmin.data(), buf[q].nmax.data());
-                    st[q].P->envelope_ok = 1;
-                } else {
-                    stage_envelope_host(st[q]);
-                }
-            });
-        });
+        B->first = f;
+        apply_envelopes(*B, 0, f);
+        if (f >= npairs) B->first = npairs;
+    } else {
+        B->first = npairs;
     }
+    if (host_envelopes) *host_envelopes = B->host_envelopes;
     *out = B.release();
     return LCG_OK;
 }
 
 lcg_status finish_tables(StagedBatch *B, int q0, int nq, lcg_prepared *out) {
     std::vector<Staged> &st = B->st;
+    if (q0 + nq > B->first) {
+        lcg_status rc = finish_envelopes(*B);
+        if (rc != LCG_OK) return rc;
+    }
     host_parallel(nq, [&](int k) { guarded(st[q0 + k], [&]() { stage_tables(st[q0 + k]); }); });
     for (int k = 0; k < nq; ++k)
         if (st[q0 + k].code != LCG_OK) {
@@ -1289,6 +1348,8 @@ lcg_status finish_tables(StagedBatch *B, int q0, int nq, lcg_prepared *out) {
 
 void free_batch(StagedBatch *B) { delete B; }
 
+int batch_host_envelopes(const StagedBatch *B) { return B ? B->host_envelopes : 0; }
+
 }  // namespace lcg_host
 
 lcg_status lcg_prepare_pairs(lcg_engine eng, const char *const *pp_a, const char *const *pp_b, int32_t npairs,
@@ -1299,7 +1360,7 @@ lcg_status lcg_prepare_pairs(lcg_engine eng, const char *const *pp_a, const char
     }
     for (int q = 0; q < npairs; ++q) out[q] = nullptr;
     lcg_host::StagedBatch *B = nullptr;
-    lcg_status rc = lcg_host::stage_batch(eng, pp_a, pp_b, npairs, opts, &B, host_envelopes);
+    lcg_status rc = lcg_host::stage_batch(eng, pp_a, pp_b, npairs, opts, &B, host_envelopes, npairs);
     if (rc == LCG_OK) rc = lcg_host::finish_tables(B, 0, npairs, out);
     lcg_host::free_batch(B);
     return rc;

@@ -22,5 +22,12 @@ lcg_status compute(lcg_engine, const Params &, int, const PairIn *, PairOut *, s
     err = "the CPU port has no GPU envelope";
     return LCG_ERR_UNSUPPORTED;
 }
+lcg_status compute_begin(lcg_engine, const Params &, int, const PairIn *, PairOut *, Pending **pending,
+                         std::string &err) {
+    *pending = nullptr;
+    err = "the CPU port has no GPU envelope";
+    return LCG_ERR_UNSUPPORTED;
+}
+lcg_status compute_end(lcg_engine, Pending *, std::string &) { return LCG_OK; }
 void reset_transfer(lcg_engine) {}
 }  // namespace lcg_env
