@@ -410,7 +410,7 @@ lcg_status lcg_pf_last_timing(lcg_engine eng, double *forward_ms, double *backwa
  * LCG_ERR_RANGE (about 400 x 400 nt with the default envelope is beyond the
  * limit). All calls share the array: calls whose GPU work overlaps race on it.
  * The first call on a device looks the array's address up
- * (cudaGetSymbolAddress); make it before any stream capture.
+ * (cudaGetSymbolAddress).
  * opts->struct_local and opts->do_trace must be 0. stream is a cudaStream_t
  * (NULL = default stream); the call returns when its results are on the host.
  */

@@ -21,7 +21,7 @@
 //    cleared and every input is copied in at the start of each call, but two
 //    calls whose GPU work overlaps (for example on two streams) race on it;
 //  * the first call on a device looks up the array's device address with
-//    cudaGetSymbolAddress; make that first call before any stream capture.
+//    cudaGetSymbolAddress.
 #include <cuda_runtime.h>
 
 #include <algorithm>
