@@ -437,17 +437,17 @@ lcg_status prep_pair(const lcg_pair_tables &t, const lcg_align_opts &o, Prep &p)
             // traceback reads it for the arc matches of this bucket (left
             // ends (al, bl); without lonely pairs the group's left ends are
             // shifted, and the traceback recomputes)
-            g.rect_pitch = max_br - bl;
+            const int rect_pitch = max_br - bl;
             g.rect_off = -1;
             if (p.rect_cells >= 0) {
-                const long long sz = (long long)(max_ar - al) * g.rect_pitch;
+                const long long sz = (long long)(max_ar - al) * rect_pitch;
                 if (p.rect_cells + sz >= (1ll << 31)) {
                     p.rect_cells = -1;
                 } else {
                     g.rect_off = (int)p.rect_cells;
                     p.rect_cells += sz;
                     if (!nolp)
-                        for (size_t q = s; q < e; ++q) p.am_rect[byleft[q].second] = make_int2(g.rect_off, g.rect_pitch);
+                        for (size_t q = s; q < e; ++q) p.am_rect[byleft[q].second] = make_int2(g.rect_off, rect_pitch);
                 }
             }
             p.cells += rect_cells(al + 1, max_ar, bl + 1, max_br - 1);

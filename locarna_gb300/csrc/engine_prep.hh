@@ -45,8 +45,8 @@ struct Prep {
     std::vector<int> sscore;                     // stacking: per am (PairDev::am_sscore)
     int rows_max = 0, width_max = 0;             // over groups
     // kept group rectangles: (ar-al) x (br-bl) ints per group, in group order
-    // (GroupItem::rect_off / rect_pitch); per arc match its group's
-    // (rect_off, rect_pitch) or (-1, 0); rect_cells = -1: too large to keep
+    // (GroupItem::rect_off, pitch br - bl); per arc match its group's
+    // (rect_off, pitch) or (-1, 0); rect_cells = -1: too large to keep
     long long rect_cells = 0;
     std::vector<int2> am_rect;
     int token_cap = 0, tq_cap = 0;

@@ -98,7 +98,7 @@ struct PairDev {
     // tables give LCG_STACK_NONE
     const int *am_sscore;
     // Kept group rectangles (nullptr: not kept). The fill writes group g's M
-    // to rect + g.rect_off (row i-al, column j-bl, pitch g.rect_pitch)
+    // to rect + g.rect_off (row i-al, column j-bl, pitch g.br - g.bl)
     // instead of the warp's scratch slot, and the traceback walks a traced
     // arc match on its group's rectangle instead of recomputing it; am_rect
     // holds per arc match its group's (rect_off, rect_pitch), (-1, 0) when no
@@ -137,7 +137,7 @@ struct GroupItem {
     int dw_start, dw_count;  // D writes: int4 (D index, corner row, corner column, score), rows ascending
     int top;                 // 1 for the top-level item
     int cpl;                 // columns per lane: ceil(widest band row of the group / 32), <= 4
-    int rect_off, rect_pitch;  // the group's kept rectangle in PairDev::rect (when kept)
+    int rect_off;            // the group's kept rectangle in PairDev::rect (pitch br - bl), when kept
 };
 
 // anchor helpers: reference AnchorConstraints::allowed_match/del/ins

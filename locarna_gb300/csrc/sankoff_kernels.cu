@@ -61,7 +61,7 @@ __global__ void __launch_bounds__(FILL_WARPS * 32, FILL_MIN_BLOCKS)
             // the group's own kept rectangle, or the warp's scratch slot
             const bool kept = P.rect && it.rect_off >= 0;
             run_group<false, true, true, COUNT, FAST>(P, it.cpl, it.al, it.ar, it.bl, it.br,
-                                                kept ? P.rect + it.rect_off : Mg, kept ? it.rect_pitch : sw,
+                                                kept ? P.rect + it.rect_off : Mg, kept ? it.br - it.bl : sw,
                                                 sbase, rb, dw + it.dw_start, it.dw_count, true, true, false,
                                                 status, abort_flag, nullptr, counters);
         }
