@@ -457,6 +457,10 @@ typedef struct lcg_prep_opts {
     /* --relaxed-anchors: anchor names need not be ordered (relaxed
      * AnchorConstraints, anchor_constraints.cc:322-357) */
     int32_t relaxed_anchors;
+    /* --unpaired-penalty (0): subtracted from every gap cost and twice from
+     * every base-match score, before the arc-match scores read them
+     * (Scoring::apply_unpaired_penalty, scoring.cc:65-74) */
+    int32_t unpaired_penalty;
 } lcg_prep_opts;
 
 typedef struct lcg_prepared_s *lcg_prepared;

@@ -144,6 +144,7 @@ int run(const Clp &c) {
     po.exp_prob = c.exp_prob_given ? c.exp_prob : -1.0;
     po.stacking = c.stacking;
     po.new_stacking = c.new_stacking;
+    po.unpaired_penalty = c.unpaired_penalty;
     po.relaxed_anchors = c.relaxed_anchors;
 
     const std::string pa = read_file(c.files[0]), pb = read_file(c.files[1]);
@@ -335,7 +336,6 @@ int main(int argc, char **argv) {
     // restrictions of this build, checked before any work
     const char *why = nullptr;
     if (c.ribosum_file != "RIBOSUM85_60") why = "--ribosum-file: only the built-in RIBOSUM85_60 is available";
-    else if (c.unpaired_penalty != 0) why = "--unpaired-penalty is not supported";
     else if (c.max_bp_span != -1) why = "--maxBPspan applies to folding, which this build does not do";
     if (why) {
         std::cerr << "ERROR: " << why << std::endl;

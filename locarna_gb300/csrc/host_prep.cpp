@@ -972,6 +972,15 @@ void stage_tables(Staged &S) {
     for (int j = 1; j <= m; ++j) P->gap_b[j] = column_gapcost(B.in, j, o.indel);
     P->indel_opening = o.indel_opening;
     P->exclusion = o.exclusion;
+    // Scoring::apply_unpaired_penalty (scoring.cc:65-74): done when the
+    // Scoring is constructed, so the arc-match scores below (which read σ
+    // without RIBOSUM) see the penalised table
+    if (o.unpaired_penalty != 0) {
+        const int32_t up = o.unpaired_penalty;
+        for (auto &v : P->sigma) v -= 2 * up;
+        for (auto &v : P->gap_a) v -= up;
+        for (auto &v : P->gap_b) v -= up;
+    }
 
     // arc matches (arc_matches.cc:130-188), A index outer, B index inner;
     // for arc a only the B arcs whose left end b.l passes

@@ -22,6 +22,7 @@ class lcg_prep_opts(C.Structure):
         ("temperature_alipf", C.c_int32), ("sequ_local", C.c_int32),
         ("free_endgaps", C.c_int32), ("pf_precision", C.c_int32), ("exp_prob", C.c_double),
         ("stacking", C.c_int32), ("new_stacking", C.c_int32), ("relaxed_anchors", C.c_int32),
+        ("unpaired_penalty", C.c_int32),
     ]
 
 

@@ -32,6 +32,9 @@ CASES = {
     "locarna_h180_structlocal_nolp": ("locarna", "h180_nolp_sl",
                                       ["--struct-local", "true", "--noLP", "--write-structure"]),
     "locarna_c150_kbest": ("locarna", "c150_kbest", ["--sequ-local", "true", "--kbest", "3"]),
+    "locarna_c150_unpaired": ("locarna", "c150_global", ["--unpaired-penalty", "40", "--write-structure"]),
+    "locarna_c120_unpaired_noribo": ("locarna", "c120_opening0",
+                                     ["--unpaired-penalty", "10", "--use-ribosum", "false", "--write-structure"]),
     "locarna_p_pf90_default": ("locarna_p", "pf90_b_default",
                                ["--write-arcmatch-probs", "{out}/am.txt", "--write-basematch-probs",
                                 "{out}/bm.txt"]),

@@ -41,3 +41,18 @@ def test_alignment_rows_must_have_equal_lengths():
     pp = _pp(["r1 ACGUACGUACGU", "r2 ACGUACGUAC"])
     with pytest.raises(LcgError, match="different lengths"):
         prepare_pair(pp, pp)
+
+
+def test_unpaired_penalty_shifts_base_match_and_gap_tables():
+    """--unpaired-penalty (Scoring::apply_unpaired_penalty, scoring.cc:65-74):
+    every base-match score lowered by twice the penalty and every gap cost by
+    the penalty; with RIBOSUM the arc-match scores do not read σ and stay."""
+    import numpy as np
+    from locarna_gb300.synth import make_rna
+    a, b = make_rna(70, 41).to_pp(), make_rna(80, 42).to_pp()
+    t0 = prepare_pair(a, b)
+    t1 = prepare_pair(a, b, unpaired_penalty=30)
+    assert np.array_equal(np.asarray(t1.sigma), np.asarray(t0.sigma) - 60)
+    assert np.array_equal(np.asarray(t1.gap_a), np.asarray(t0.gap_a) - 30)
+    assert np.array_equal(np.asarray(t1.gap_b), np.asarray(t0.gap_b) - 30)
+    assert np.array_equal(np.asarray(t1.am_score), np.asarray(t0.am_score))
