@@ -48,7 +48,7 @@ struct Clp {
     bool subopt = false;
     int kbest_k = -1, subopt_threshold = -1000000;
     int temperature_alipf = 300;
-    bool no_lonely_pairs = false, relaxed_anchors = false;
+    bool no_lonely_pairs = false, relaxed_anchors = false, extended_pf = false;
     int max_bp_span = -1;
     std::vector<std::string> files;
 };
@@ -282,8 +282,11 @@ int main(int argc, char **argv) {
     tab.flag("noLP", 0, &c.no_lonely_pairs);
     tab.integer("maxBPspan", 0, &c.max_bp_span);
     tab.flag("relaxed-anchors", 0, &c.relaxed_anchors);
+    // the envelope in long double is locarna's only mode without
+    // --quad-pf (src/locarna.cc:384 sets extended_pf unconditionally)
+    tab.flag("extended-pf", 0, &c.extended_pf);
     // options of the reference outside this build's scope
-    for (const char *o : {"galaxy-xml", "extended-pf", "quad-pf", "pp", "alifold-consensus-dp", "consensus-structure",
+    for (const char *o : {"galaxy-xml", "quad-pf", "pp", "alifold-consensus-dp", "consensus-structure",
                           "consensus-gamma", "score-components", "stopwatch", "max-bps-length-ratio", "max-diff-aln",
                           "max-diff-pw-aln", "max-diff-relax", "mea-alignment", "match-prob-method", "probcons-file",
                           "pf-struct-weight", "mea-gapcost", "mea-alpha", "mea-beta", "mea-gamma", "probability-scale",

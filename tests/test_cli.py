@@ -51,6 +51,14 @@ def test_locarna_refuses_before_any_work(cli, args, msg):
     assert msg in r.stderr, r.stderr
 
 
+def test_locarna_accepts_extended_pf(cli):
+    """--extended-pf is locarna's default envelope precision (always on in
+    src/locarna.cc:384): accepted; the run then fails only on the missing
+    input file, not on the option."""
+    r = subprocess.run([cli[0], "--extended-pf", "no_such_a.pp", "no_such_b.pp"], capture_output=True, text=True)
+    assert "not supported" not in r.stderr and "Unknown option" not in r.stderr, r.stderr
+
+
 def test_locarna_p_refuses_unsupported(cli):
     r = subprocess.run([cli[1], "--fragment-match-probs", "1 2 3 4", "a.pp", "b.pp"], capture_output=True, text=True)
     assert r.returncode != 0 and "not supported" in r.stderr
