@@ -280,7 +280,10 @@ lcg_status lcg_engine_last_timing(lcg_engine eng, double *fill_ms, double *trace
 /* Wall-clock phases (ms) of the last lcg_align_pairs call: host preparation of
  * the pairs' index structures, packing of the upload, time the host waited for
  * copies + kernels, and assembly of the alignments (summed over chunks; with
- * several chunks the device works during the host phases). */
+ * several chunks the device works during the host phases). For
+ * lcg_align_pp_pairs the host preparation also counts the staging of the
+ * inputs (parsing, bands, the first chunk's envelopes) and every chunk's
+ * tables. */
 lcg_status lcg_engine_last_phases(lcg_engine eng, double *prep_ms, double *pack_ms,
                                   double *device_ms, double *results_ms);
 

@@ -1434,7 +1434,9 @@ lcg_status lcg_align_pp_pairs(lcg_engine e, const char *const *pp_a, const char 
     const bool modv = opts->normalized || opts->penalized;
     const int first = modv ? npairs : std::min<int>(npairs, chunk_size(npairs, e->chunk_pairs));
     lcg_host::StagedBatch *B = nullptr;
+    const auto t0 = std::chrono::steady_clock::now();
     lcg_status rc = lcg_host::stage_batch(e, pp_a, pp_b, npairs, popts, &B, host_envelopes, first);
+    const double stage_ms = ms_between(t0, std::chrono::steady_clock::now());
     if (rc != LCG_OK) {
         lcg_host::free_batch(B);
         return rc;
@@ -1447,6 +1449,7 @@ lcg_status lcg_align_pp_pairs(lcg_engine e, const char *const *pp_a, const char 
         return r;
     };
     rc = align_impl(e, tabs.data(), npairs, opts, results, &ready);
+    e->last_phase_ms[0] += stage_ms;  // host preparation includes the staging of the inputs
     for (auto h : handles)
         if (h) lcg_prepared_free(h);
     if (host_envelopes) *host_envelopes = lcg_host::batch_host_envelopes(B);
