@@ -16,6 +16,7 @@ from .abi import (LCG_TUNE_BUCKETS, ResultBuffers, lcg_align_opts, lcg_align_res
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_build", "liblocarna_gb300.so")
+ABI_VERSION = 4  # LCG_ABI_VERSION the structures of abi.py / prep.py mirror
 
 _lib = None
 _lib_lock = threading.Lock()
@@ -44,6 +45,9 @@ def _load_locked(path):
     lib = C.CDLL(path)
     lib.lcg_last_error.restype = C.c_char_p
     lib.lcg_abi_version.restype = C.c_int32
+    if lib.lcg_abi_version() != ABI_VERSION:
+        raise RuntimeError(f"locarna_gb300 library {path} has ABI version {lib.lcg_abi_version()}, the binding "
+                           f"expects {ABI_VERSION}; rebuild with __graft_entry__.build()")
     lib.lcg_engine_create.argtypes = [C.c_int32, C.c_void_p, C.POINTER(C.c_void_p)]
     lib.lcg_engine_create.restype = C.c_int32
     lib.lcg_engine_destroy.argtypes = [C.c_void_p]
