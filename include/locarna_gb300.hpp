@@ -42,7 +42,12 @@ class Engine {
     lcg_engine e_ = nullptr;
 
 public:
-    explicit Engine(int device = 0, void *stream = nullptr) { check(lcg_engine_create(device, stream, &e_)); }
+    explicit Engine(int device = 0, void *stream = nullptr) {
+        // the structures of this header must be the library's
+        if (lcg_abi_version() != LCG_ABI_VERSION)
+            throw failure("locarna_gb300: the library's ABI version differs from the header's");
+        check(lcg_engine_create(device, stream, &e_));
+    }
     ~Engine() {
         if (e_) lcg_engine_destroy(e_);
     }
