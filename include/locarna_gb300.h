@@ -507,7 +507,9 @@ const char *lcg_prepared_sequence(lcg_prepared p, int32_t which);
  * single sequence has one), as the reference's MultipleAlignment of the PP
  * sequence section holds them (multiple_alignment.cc:577-584: upper case,
  * T as U): which = 0 row k of A, 1 row k of B, 2 name of row k of A, 3 name of
- * row k of B; NULL past the last row. Valid until lcg_prepared_free. */
+ * row k of B, 4 anchor line k+1 of A (its #A<k+1> lines concatenated,
+ * multiple_alignment.cc:324-346), 5 anchor line k+1 of B; NULL past the last
+ * row. Valid until lcg_prepared_free. */
 const char *lcg_prepared_row(lcg_prepared p, int32_t which, int32_t k);
 /* 0 if the envelope partition function failed (PFGotoh::fail, edge_probs.hh:202) */
 int32_t lcg_prepared_envelope_ok(lcg_prepared p);

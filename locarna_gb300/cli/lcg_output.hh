@@ -6,6 +6,9 @@
 //   structure         Alignment::dot_bracket_structureA/B (alignment.cc:215-239)
 //                     with add_basepairA/B               (alignment.cc:97-107)
 //   rows              MultipleAlignment(const Alignment&) (multiple_alignment.cc:153-245)
+//   anchor_consensus  SequenceAnnotation(edges, A, B)     (sequence_annotation.cc:15-51)
+//                     kept unless duplicate_names()       (multiple_alignment.cc:157-165,
+//                                                          sequence_annotation.cc:103-120)
 //   write_blocks      MultipleAlignment::write            (multiple_alignment.cc:995-1085)
 //
 // Edge ends are ints: a position p >= 1, or a gap -1 - code with the
@@ -14,6 +17,7 @@
 #pragma once
 #include <algorithm>
 #include <ostream>
+#include <set>
 #include <string>
 #include <utility>
 #include <vector>
@@ -101,23 +105,65 @@ inline std::vector<Row> rows(const Edges &edges, const std::vector<Row> &in_a, c
     return out;
 }
 
+// Consensus of the inputs' anchor lines along the edges: one string per
+// character of the anchor names (line k holds character k of every column's
+// name). A column aligned to a gap takes the other side's name; a match
+// takes the non-neutral name, or the smaller of two (a name is neutral when
+// it holds only ' ' and '.'). Empty when either input has no anchor lines,
+// or when two non-neutral columns share a name (the reference then sets no
+// anchor annotation).
+inline std::vector<std::string> anchor_consensus(const Edges &edges, const std::vector<std::string> &in_a,
+                                                 const std::vector<std::string> &in_b) {
+    if (in_a.empty() || in_b.empty() || in_a[0].empty() || in_b[0].empty()) return {};
+    const size_t nl = in_a.size();
+    auto name_of = [](const std::vector<std::string> &lines, int pos) {
+        std::string nm;
+        for (const auto &l : lines) nm += (size_t)pos <= l.size() ? l[pos - 1] : ' ';
+        return nm;
+    };
+    auto neutral = [](const std::string &nm) {
+        return std::all_of(nm.begin(), nm.end(), [](char c) { return c == ' ' || c == '.'; });
+    };
+    std::vector<std::string> out(nl);
+    std::set<std::string> seen;
+    for (const auto &e : edges) {
+        std::string nm;
+        if (e.first <= 0) {
+            nm = name_of(in_b, e.second);
+        } else if (e.second <= 0) {
+            nm = name_of(in_a, e.first);
+        } else {
+            const std::string na = name_of(in_a, e.first), nb = name_of(in_b, e.second);
+            nm = neutral(na) ? nb : neutral(nb) ? na : std::min(na, nb);
+        }
+        if (!neutral(nm) && !seen.insert(nm).second) return {};
+        for (size_t k = 0; k < nl; ++k) out[k] += k < nm.size() ? nm[k] : ' ';
+    }
+    return out;
+}
+
 // blocks of `width` columns, "name sequence" lines with the name padded to
-// max(18, longest name), a blank line between blocks; Stockholm ends with "//"
-inline void write_blocks(std::ostream &out, const std::vector<Row> &rs, size_t width, bool stockholm) {
+// max(18, longest row name), then per block the anchor lines tagged "#A<k>"
+// ("#=GC cA<k>" in Stockholm), a blank line between blocks; Stockholm ends
+// with "//"
+inline void write_blocks(std::ostream &out, const std::vector<Row> &rs, size_t width, bool stockholm,
+                         const std::vector<std::string> &anchors = {}) {
     size_t namew = 18, len = 0;
     for (const auto &r : rs) {
         namew = std::max(namew, r.name.size());
         len = std::max(len, r.seq.size());
     }
     if (width == 0) width = len;
+    auto line = [&](std::string name, const std::string &seq, size_t start, size_t end) {
+        if (name.size() < namew) name.append(namew - name.size(), ' ');
+        out << name << " " << seq.substr(std::min(start, seq.size()), end - start) << "\n";
+    };
     size_t start = 0;
     do {
         const size_t end = std::min(len, start + width);
-        for (const auto &r : rs) {
-            std::string name = r.name;
-            if (name.size() < namew) name.append(namew - name.size(), ' ');
-            out << name << " " << r.seq.substr(start, end - start) << "\n";
-        }
+        for (const auto &r : rs) line(r.name, r.seq, start, end);
+        for (size_t k = 0; k < anchors.size(); ++k)
+            line(std::string(stockholm ? "#=GC cA" : "#A") + std::to_string(k + 1), anchors[k], start, end);
         start = end;
         if (start < len) out << "\n";
     } while (start < len);

@@ -107,6 +107,25 @@ Traced traced(const lcg_pair_tables &t, const locarna_gb300::Alignment &al) {
     return tr;
 }
 
+// the #A<k> lines of input `side` (0 A, 1 B)
+std::vector<std::string> input_anchors(lcg_prepared p, int side) {
+    std::vector<std::string> out;
+    for (int k = 0;; ++k) {
+        const char *l = lcg_prepared_row(p, side + 4, k);
+        if (!l) break;
+        out.push_back(l);
+    }
+    return out;
+}
+
+// the consensus anchor lines the reference's MultipleAlignment of the
+// alignment carries (multiple_alignment.cc:153-165)
+std::vector<std::string> alignment_anchors(const lcg_pair_tables &t, lcg_prepared p, const Traced &tr,
+                                           bool only_local) {
+    return anchor_consensus(alignment_edges(tr.raw, t.len_a, t.len_b, only_local), input_anchors(p, 0),
+                            input_anchors(p, 1));
+}
+
 std::vector<Row> alignment_rows(const lcg_pair_tables &t, lcg_prepared p, const Traced &tr, bool only_local,
                                 bool with_structure) {
     const Edges edges = alignment_edges(tr.raw, t.len_a, t.len_b, only_local);
@@ -178,7 +197,8 @@ int run(const Clp &c) {
                           << " " << e.second << " " << std::endl;
             } else {
                 std::cout << "Score: " << score_str(h.first) << std::endl;
-                write_blocks(std::cout, alignment_rows(t, prep, tr, true, false), 120, false);
+                write_blocks(std::cout, alignment_rows(t, prep, tr, true, false), 120, false,
+                             alignment_anchors(t, prep, tr, true));
                 std::cout << std::endl << std::endl;
             }
         }
@@ -196,7 +216,8 @@ int run(const Clp &c) {
             if (input_rows(prep, 0).size() == 1 && input_rows(prep, 1).size() == 1)
                 out << " --- Score: " << score_str(score);
             out << std::endl << std::endl;
-            write_blocks(out, alignment_rows(t, prep, tr, c.local_file_output, c.write_structure), c.width, false);
+            write_blocks(out, alignment_rows(t, prep, tr, c.local_file_output, c.write_structure), c.width, false,
+                         alignment_anchors(t, prep, tr, c.local_file_output));
         } else {
             std::cerr << "ERROR: Cannot write to " << c.clustal << "." << std::endl;
             rc = -1;
@@ -209,7 +230,7 @@ int run(const Clp &c) {
             out << "# STOCKHOLM 1.0" << std::endl;
             out << "#=GF CC Generated by " << LCG_CLI_PACKAGE_STRING << std::endl;
             out << "#=GF SQ " << rs.size() << std::endl << std::endl;
-            write_blocks(out, rs, c.width, true);
+            write_blocks(out, rs, c.width, true, alignment_anchors(t, prep, tr, c.local_file_output));
         } else {
             std::cerr << "ERROR: Cannot write to " << c.stockholm << "." << std::endl;
             rc = -1;
@@ -227,7 +248,8 @@ int run(const Clp &c) {
             auto s = start_positions(tr.raw, t.len_a, t.len_b);
             std::cout << "\t+" << s.first << std::endl << "\t+" << s.second << std::endl << std::endl << std::endl;
         }
-        write_blocks(std::cout, alignment_rows(t, prep, tr, c.local_output, c.write_structure), c.width, false);
+        write_blocks(std::cout, alignment_rows(t, prep, tr, c.local_output, c.write_structure), c.width, false,
+                     alignment_anchors(t, prep, tr, c.local_output));
         if (c.pos_output) {
             auto e = end_positions(tr.raw);
             std::cout << std::endl << "\t+" << e.first << std::endl << "\t+" << e.second << std::endl << std::endl;

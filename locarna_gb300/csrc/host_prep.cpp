@@ -740,6 +740,7 @@ struct lcg_prepared_s {
     int n = 0, m = 0;
     std::string seq_a, seq_b, name_a, name_b;
     std::vector<std::string> rows_a, rows_b, row_names_a, row_names_b;  // all rows of profile inputs
+    std::vector<std::string> anchor_rows_a, anchor_rows_b;              // the #A<k> lines of the inputs
     std::vector<int32_t> sigma, gap_a, gap_b, arcs_a, arcs_b, am_arcs, am_score, min_col, max_col;
     std::vector<double> arc_p_a, arc_p_b;
     std::vector<int8_t> code_a, code_b;  // 0..3 for A,C,G,U, -1 otherwise; index 1..len
@@ -868,6 +869,8 @@ void stage_inputs(std::shared_ptr<const Side> A, std::shared_ptr<const Side> B, 
     P->rows_b = sb.in.rows;
     P->row_names_a = sa.in.row_names;
     P->row_names_b = sb.in.row_names;
+    P->anchor_rows_a = sa.in.anchors;
+    P->anchor_rows_b = sb.in.anchors;
     // trace controller (no reference alignment, no anchors)
     S.tc.minc.assign(n + 1, 0);
     S.tc.maxc.assign(n + 1, m);
@@ -1440,6 +1443,8 @@ const char *lcg_prepared_row(lcg_prepared p, int32_t which, int32_t k) {
     case 1: v = &p->rows_b; break;
     case 2: v = &p->row_names_a; break;
     case 3: v = &p->row_names_b; break;
+    case 4: v = &p->anchor_rows_a; break;
+    case 5: v = &p->anchor_rows_b; break;
     default: return nullptr;
     }
     return (size_t)k < v->size() ? (*v)[k].c_str() : nullptr;

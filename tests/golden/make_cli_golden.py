@@ -33,6 +33,17 @@ CASES = {
                                       ["--struct-local", "true", "--noLP", "--write-structure"]),
     "locarna_c150_kbest": ("locarna", "c150_kbest", ["--sequ-local", "true", "--kbest", "3"]),
     "locarna_c150_unpaired": ("locarna", "c150_global", ["--unpaired-penalty", "40", "--write-structure"]),
+    "locarna_c150_bothstack": ("locarna", "c150_bothstack",
+                               ["--stacking", "--new-stacking", "--exp-prob", "0.005", "--write-structure"]),
+    "locarna_c150_freeleft": ("locarna", "c150_freeleft", ["--free-endgaps", "+-+-", "--pos-output"]),
+    "locarna_c150_maxdiff": ("locarna", "c150_maxdiff", ["--max-diff", "20", "--write-structure"]),
+    "locarna_c150_normalized": ("locarna", "c150_global", ["--sequ-local", "true", "--normalized", "100"]),
+    "locarna_h180_penalized_sl": ("locarna", "h180_penalized_sl",
+                                  ["--sequ-local", "true", "--struct-local", "true", "--penalized", "25"]),
+    "locarna_a150_anchors": ("locarna", "a150_anchors", ["--write-structure"]),
+    "locarna_c150_params": ("locarna", "c150_global",
+                            ["--indel", "-200", "--indel-opening", "-500", "--struct-weight", "150", "--tau", "100",
+                             "--width", "100"]),
     "locarna_c120_unpaired_noribo": ("locarna", "c120_opening0",
                                      ["--unpaired-penalty", "10", "--use-ribosum", "false", "--write-structure"]),
     "locarna_p_pf90_default": ("locarna_p", "pf90_b_default",

@@ -72,10 +72,13 @@ def writer():
     return exe
 
 
-def _write(writer, rows_a, rows_b, edges, width, stockholm):
+def _write(writer, rows_a, rows_b, edges, width, stockholm, anchors=None):
     inp = f"{len(rows_a)} {len(rows_b)} {width} {int(stockholm)}\n"
     inp += "".join(f"{n} {s}\n" for n, s in rows_a + rows_b)
     inp += f"{len(edges)}\n" + "".join(f"{a} {b}\n" for a, b in edges)
+    if anchors is not None:
+        for lines in anchors:
+            inp += f"{len(lines)}\n" + "".join(x + "\n" for x in lines)
     r = subprocess.run([writer], input=inp, capture_output=True, text=True, check=True)
     return r.stdout
 
@@ -94,6 +97,18 @@ def _rows(pp):
             rows.append([name, ""])
         rows[seen[name]][1] += seq.strip()
     return [(n, s.upper().replace("T", "U")) for n, s in rows]
+
+
+def _anchor_lines(pp):
+    """The #A<k> lines of a PP text's sequence section, blocks concatenated."""
+    lines = {}
+    for line in pp.splitlines():
+        if line.startswith("#SECTION"):
+            break
+        if line.startswith("#A") and line[2:3].isdigit():
+            k, s = line[2:].split()
+            lines[int(k)] = lines.get(int(k), "") + s
+    return [lines[k] for k in sorted(lines)]
 
 
 @pytest.mark.parametrize("case,fname,width,sto", [
@@ -118,3 +133,25 @@ def test_writer_prints_the_reference_text(writer, case, fname, width, sto):
         text = "\n".join(l for l in text.splitlines() if l.strip()) + "\n"
         body = "\n".join(l for l in body.splitlines() if l.strip()) + "\n"
     assert text.replace("\n\n", "\n") == body.replace("\n\n", "\n")
+
+
+def test_writer_prints_the_consensus_anchor_lines(writer):
+    """The anchor lines of both inputs become one consensus line per name
+    character, printed after each block's rows ("#A1"; "#=GC cA1" in
+    Stockholm); two columns with the same name drop them."""
+    spec = json.load(open(os.path.join(CLI_GOLDEN, "locarna_a150_anchors.args.json")))
+    g = Golden(spec["case"])
+    edges = [(a if a > 0 else -1, b if b > 0 else -1) for a, b in g.edges]
+    anch = (_anchor_lines(g.pp_a), _anchor_lines(g.pp_b))
+    assert anch[0] and anch[1]
+    text = _write(writer, _rows(g.pp_a), _rows(g.pp_b), edges, 120, False, anch)
+    ref = open(os.path.join(CLI_GOLDEN, "locarna_a150_anchors.stdout")).read()
+    body = [l for l in ref.splitlines()[2:] if l.strip() and not l.startswith(" " * 18)]
+    assert [l for l in text.splitlines() if l.strip()] == body
+    assert any(l.startswith("#A1 ") for l in body)
+    sto = _write(writer, _rows(g.pp_a), _rows(g.pp_b), edges, 120, True, anch)
+    assert [l[:8] for l in sto.splitlines() if l.startswith("#")] == ["#=GC cA1"] * 2
+    # a name twice in the consensus: no anchor lines
+    a2 = [anch[0][0].replace(".", "A", 1)]
+    dup = _write(writer, _rows(g.pp_a), _rows(g.pp_b), edges, 120, False, (a2, anch[1]))
+    assert not any(l.startswith("#A") for l in dup.splitlines())
