@@ -225,13 +225,16 @@ lcg_status lcg_engine_set_chunk_pairs(lcg_engine eng, int32_t pairs_per_chunk);
  * penalized and k-best alignment, whose top levels iterate with the host,
  * launch directly. on = 0 launches every chunk directly. */
 lcg_status lcg_engine_set_graphs(lcg_engine eng, int32_t on);
-/* Kept group rectangles (default budget 4 GiB): when a chunk's left-end
- * groups, stored as full rectangles ((ar-al) x (br-bl) int32 each), fit in
- * `bytes`, the fill writes every group's M matrix to a rectangle of its own
- * and the traceback walks each traced arc match on its group's rectangle
- * instead of recomputing it (the reference recomputes too, trace_arcmatch,
- * aligner.cc:967-1028); the results are the same. Single pairs and small
- * batches; not with --noLP or --struct-local. bytes = 0 always recomputes. */
+/* Kept group rectangles: when a chunk's left-end groups, stored as full
+ * rectangles ((ar-al) x (br-bl) cells each; 4 bytes per cell, 32 with
+ * --struct-local, whose traceback switches between the eight state
+ * matrices), fit in `bytes`, the fill writes every group's matrices to a
+ * rectangle of its own and the traceback walks each traced arc match on its
+ * group's rectangle instead of recomputing it (the reference recomputes too,
+ * trace_arcmatch, aligner.cc:967-1028); the results are the same. Single
+ * pairs and small batches; not with --noLP. bytes = 0 always recomputes;
+ * bytes < 0 restores the default budgets, 4 GiB for plain chunks and 32 GiB
+ * for structure-local chunks (a 400 x 400 nt pair takes ~25 GB). */
 lcg_status lcg_engine_set_rect_budget(lcg_engine eng, int64_t bytes);
 /* Graph captures and replays of the last lcg_align_pairs call. */
 lcg_status lcg_engine_last_graphs(lcg_engine eng, int64_t *captures, int64_t *replays);

@@ -683,16 +683,21 @@ lcg_status chunk_launch(lcg_engine e, const Slot &s, const lcg_pair_tables *all,
     // of its own and the traceback walks traced arc matches on them instead
     // of recomputing them, when the chunk's rectangles fit the engine's
     // budget (lcg_engine_set_rect_budget) - single pairs and small batches.
-    // Not with lonely pairs excluded (shifted group left ends) and not in
-    // structure-local mode (the traceback needs all eight states).
-    bool keep = e->rect_budget > 0 && !opts->struct_local;
+    // Structure-local rectangles hold all eight states (32 bytes per cell,
+    // the traceback switches between them). Not with lonely pairs excluded
+    // (shifted group left ends).
+    const long long rect_bytes_per_cell = opts->struct_local ? 32 : 4;
+    bool keep;
     {
+        const long long budget = e->rect_budget >= 0 ? e->rect_budget
+                                                     : (opts->struct_local ? RECT_BUDGET_SL : RECT_BUDGET_PLAIN);
+        keep = budget > 0;
         long long cells = 0;
         for (auto &p : prep) {
             if (p.rect_cells < 0 || (p.flags & PF_NOLP)) keep = false;
             cells += p.rect_cells;
         }
-        keep = keep && 4.0 * (double)cells <= (double)e->rect_budget;
+        keep = keep && (double)rect_bytes_per_cell * (double)cells <= (double)budget;
     }
     c.off.assign(npairs, PairOff{});
     std::vector<PairOff> &off = c.off;
@@ -755,7 +760,7 @@ lcg_status chunk_launch(lcg_engine e, const Slot &s, const lcg_pair_tables *all,
         PairOff &o = off[q];
         o.tq = take(dev_only, 16ull * p.tq_cap);
         o.topM = take(dev_only, 4ull * (p.n + 1) * (p.m + 1));
-        o.rect = keep ? take(dev_only, 4ull * std::max<long long>(p.rect_cells, 1)) : 0;
+        o.rect = keep ? take(dev_only, (size_t)rect_bytes_per_cell * std::max<long long>(p.rect_cells, 1)) : 0;
     }
     // normalized / penalized alignment: per pair its penalty, the selected
     // pairs and their gathered result words
@@ -920,7 +925,7 @@ lcg_status chunk_launch(lcg_engine e, const Slot &s, const lcg_pair_tables *all,
     c.rb = rb;
     int blocks_per_sm = 0;
     if (sl) {
-        CUDA_TRY(sl_prepare(sw, rb, sl_fast, &blocks_per_sm));
+        CUDA_TRY(sl_prepare(sw, rb, sl_fast, keep, &blocks_per_sm));
     } else {
         CUDA_TRY(fill_occupancy(rb, e->counting, fast, &blocks_per_sm));
         CUDA_TRY(trace_prepare(rb));
@@ -1008,7 +1013,7 @@ lcg_status chunk_launch(lcg_engine e, const Slot &s, const lcg_pair_tables *all,
             return fail(LCG_ERR_UNSUPPORTED, "work counting covers the plain mode only");
         }
         CUDA_TRY_CAP(launch_sl_fill((const PairDev *)(Dv + off_pairs), (const int2 *)(Dv + off_queue),
-                                (int)nitems, scratch, stride, sw, rb, sl_fast, qhead,
+                                (int)nitems, scratch, stride, sw, rb, sl_fast, keep, qhead,
                                 status, abort_flag, blocks, st));
     } else {
         CUDA_TRY_CAP(launch_fill((const PairDev *)(Dv + off_pairs), (const int2 *)(Dv + off_queue),
@@ -1459,7 +1464,7 @@ lcg_status lcg_align_pp_pairs(lcg_engine e, const char *const *pp_a, const char 
 
 lcg_status lcg_engine_set_rect_budget(lcg_engine e, int64_t bytes) {
     if (!e) return fail(LCG_ERR_ARG, "null engine");
-    e->rect_budget = bytes > 0 ? bytes : 0;
+    e->rect_budget = bytes < 0 ? -1 : bytes;
     return LCG_OK;
 }
 

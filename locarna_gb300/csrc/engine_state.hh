@@ -41,6 +41,11 @@ struct lcg_buffer_set {
     lcg_graph_cache graph;
 };
 
+// default budgets of kept group rectangles (bytes): plain chunks, and
+// structure-local chunks, whose rectangles hold eight state matrices
+constexpr long long RECT_BUDGET_PLAIN = 4ll << 30;
+constexpr long long RECT_BUDGET_SL = 32ll << 30;
+
 struct lcg_engine_s {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -70,8 +75,9 @@ struct lcg_engine_s {
     // resident blocks per SM (0 = as many as fit) and the L2 budget of a pair
     // wave in MB (0 = default); used by lcg_align_pairs when autotune is on
     bool autotune = false;
-    // bytes of kept group rectangles a chunk may use (lcg_engine_set_rect_budget)
-    long long rect_budget = 4ll << 30;
+    // bytes of kept group rectangles a chunk may use (lcg_engine_set_rect_budget;
+    // < 0: RECT_BUDGET_PLAIN / RECT_BUDGET_SL by the chunk's mode)
+    long long rect_budget = -1;
     int tune_bps[LCG_TUNE_BUCKETS] = {0, 0, 0, 0};
     double tune_wave_mb[LCG_TUNE_BUCKETS] = {0, 0, 0, 0};
     // CUDA graphs of the chunks (lcg_engine_set_graphs): the own set's cache

@@ -26,12 +26,14 @@ cudaError_t trace_prepare(int rb);
 int fill_warps_per_block();
 int trace_warps_per_block();
 // fast: every pair has a sigma class table and no anchor constraints
-// (run_group_slf); blocks_per_sm = 0 when the shared memory does not fit
-cudaError_t sl_prepare(int sw, int rb, bool fast, int *blocks_per_sm);
+// (run_group_slf); keep: the instantiation for kept rectangles;
+// blocks_per_sm = 0 when the shared memory does not fit
+cudaError_t sl_prepare(int sw, int rb, bool fast, bool keep, int *blocks_per_sm);
 int sl_fill_warps_per_block();
+// keep: the pairs' group rectangles are kept (PairDev::rect, eight states)
 cudaError_t launch_sl_fill(const PairDev *pairs, const int2 *queue, int nitems, int *scratch,
-                           long long scratch_stride, int sw, int rb, bool fast, unsigned int *qhead, int *status,
-                           int *abort_flag, int blocks, cudaStream_t st);
+                           long long scratch_stride, int sw, int rb, bool fast, bool keep, unsigned int *qhead,
+                           int *status, int *abort_flag, int blocks, cudaStream_t st);
 cudaError_t launch_sl_trace(const PairDev *pairs, int npairs, int *scratch, long long scratch_stride, int sw,
                             int rb, bool fast, int *status, cudaStream_t st, TraceSel sel = TraceSel());
 }  // namespace lcg

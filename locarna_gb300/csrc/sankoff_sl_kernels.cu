@@ -648,7 +648,11 @@ __device__ void run_group_slf(const PairDev &P, int al, int ar, int bl, int br, 
 #undef RG
 }
 
-template <bool FAST>
+// KEEP: the chunk keeps its group rectangles (PairDev::rect); a group with
+// a kept rectangle writes all eight states there, interleaved by row (row
+// i-al of state s at rect + 8 rect_off + (i-al) 8w + s w, w = br - bl), so
+// that the traceback walks it instead of recomputing it.
+template <bool FAST, bool KEEP>
 __global__ void __launch_bounds__(SL_FILL_WARPS * 32)
     sankoff_sl_fill_kernel(const PairDev *__restrict__ pairs, const int2 *__restrict__ queue,
                            int nitems, int *scratch,
@@ -673,6 +677,15 @@ __global__ void __launch_bounds__(SL_FILL_WARPS * 32)
         if (it.top) {
             const int base = (int)(sm - smem);
             run_top<false>(P, it.cpl, base, rb, status, abort_flag, nullptr);
+        } else if (KEEP && P.rect && it.rect_off >= 0) {
+            const int w = it.br - it.bl;
+            int *Mk = P.rect + 8ll * it.rect_off;
+            if (FAST)
+                run_group_slf<true, true, 8>(P, it.al, it.ar, it.bl, it.br, Mk, w, 8 * w, (int)(sm - smem), rb,
+                                             dw + it.dw_start, it.dw_count, status, abort_flag);
+            else
+                run_group_sl<true, true, 8>(P, it.al, it.ar, it.bl, it.br, Mk, w, 8 * w, sm, sw,
+                                            dw + it.dw_start, it.dw_count, status, abort_flag);
         } else if (FAST) {
             run_group_slf<true, true, 4>(P, it.al, it.ar, it.bl, it.br, Mg, scratch_stride, sw, (int)(sm - smem), rb,
                                 dw + it.dw_start, it.dw_count, status, abort_flag);
@@ -876,12 +889,23 @@ __global__ void __launch_bounds__(TRACE_WARPS * 32)
                 continue;
             }
         }
-        if (FAST)
+        // the arc match's eight state matrices: its group's kept rectangle
+        // from the fill, else recomputed into the pair's scratch slot
+        const int2 kr = P.am_rect ? P.am_rect[k] : make_int2(-1, 0);
+        const int *Mw = Mg;
+        long long ms = scratch_stride;
+        int pw = sw;
+        if (kr.x >= 0) {
+            Mw = P.rect + 8ll * kr.x;
+            ms = kr.y;
+            pw = 8 * kr.y;
+        } else if (FAST) {
             run_group_slf<false, false, 8>(P, ends.x, ends.y, ends.z, ends.w, Mg, scratch_stride, sw,
                                            (int)(sm - smem), rb, nullptr, 0, status, (volatile int *)&dummy_abort);
-        else
+        } else {
             run_group_sl<false, false, 8>(P, ends.x, ends.y, ends.z, ends.w, Mg, scratch_stride, sw, sm, sw,
                                           nullptr, 0, status, (volatile int *)&dummy_abort);
+        }
         __syncwarp();
         if (lane == 0) {
             // trace_arcmatch, struct-local branch (aligner.cc:1014-1026): first
@@ -889,13 +913,13 @@ __global__ void __launch_bounds__(TRACE_WARPS * 32)
             // match of a no-lonely-pairs stack (aligner.cc:1062-1074) the
             // queue entry carries D(outer) - score(outer) - score(am)
             const int ar = ends.y, br = ends.w;
-            const long long o = (long long)(ar - 1 - ends.x) * sw + (br - 1 - ends.z);
+            const long long o = (long long)(ar - 1 - ends.x) * pw + (br - 1 - ends.z);
             const bool nolp = P.flags & PF_NOLP;
             const int dv = nolp ? kpos : P.D[kpos], sc = nolp ? 0 : P.am_score[k];
             const int start = w.ntok;
             for (int s2 = 0; s2 < 4; ++s2) {
-                if (dv == Mg[s2 * scratch_stride + o] + sc) {
-                    walk_sl(w, Mg, scratch_stride, sw, ends.x, ends.z, s2, ar - 1, br - 1, false, status);
+                if (dv == Mw[s2 * ms + o] + sc) {
+                    walk_sl(w, Mw, ms, pw, ends.x, ends.z, s2, ar - 1, br - 1, false, status);
                     break;
                 }
             }
@@ -921,7 +945,7 @@ static size_t sl_trace_smem(int sw, int rb, bool fast) {
     return (size_t)TRACE_WARPS * (fast ? slf_warp_ints(rb) : SL_ROWS * sw) * sizeof(int);
 }
 
-cudaError_t sl_prepare(int sw, int rb, bool fast, int *blocks_per_sm) {
+cudaError_t sl_prepare(int sw, int rb, bool fast, bool keep, int *blocks_per_sm) {
     const size_t smem = sl_fill_smem(sw, rb, fast);
     const size_t smem_t = sl_trace_smem(sw, rb, fast);
     int optin = 0, dev = 0;
@@ -933,27 +957,30 @@ cudaError_t sl_prepare(int sw, int rb, bool fast, int *blocks_per_sm) {
         *blocks_per_sm = 0;  // does not fit: the caller reports it
         return cudaSuccess;
     }
-    const void *k = fast ? (const void *)sankoff_sl_fill_kernel<true> : (const void *)sankoff_sl_fill_kernel<false>;
+    const void *k = fast ? (const void *)sankoff_sl_fill_kernel<true, false>
+                         : (const void *)sankoff_sl_fill_kernel<false, false>;
+    const void *kk = fast ? (const void *)sankoff_sl_fill_kernel<true, true>
+                          : (const void *)sankoff_sl_fill_kernel<false, true>;
     e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(kk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     const void *kt = fast ? (const void *)sankoff_sl_trace_kernel<true> : (const void *)sankoff_sl_trace_kernel<false>;
     e = cudaFuncSetAttribute(kt, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_t);
     if (e != cudaSuccess) return e;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k, SL_FILL_WARPS * 32, smem);
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, keep ? kk : k, SL_FILL_WARPS * 32, smem);
 }
 
 int sl_fill_warps_per_block() { return SL_FILL_WARPS; }
 
 cudaError_t launch_sl_fill(const PairDev *pairs, const int2 *queue, int nitems,
-                           int *scratch, long long scratch_stride, int sw, int rb, bool fast, unsigned int *qhead,
-                           int *status, int *abort_flag, int blocks, cudaStream_t st) {
+                           int *scratch, long long scratch_stride, int sw, int rb, bool fast, bool keep,
+                           unsigned int *qhead, int *status, int *abort_flag, int blocks, cudaStream_t st) {
     const size_t smem = sl_fill_smem(sw, rb, fast);
-    if (fast)
-        sankoff_sl_fill_kernel<true><<<blocks, SL_FILL_WARPS * 32, smem, st>>>(
-            pairs, queue, nitems, scratch, scratch_stride, sw, rb, qhead, status, abort_flag);
-    else
-        sankoff_sl_fill_kernel<false><<<blocks, SL_FILL_WARPS * 32, smem, st>>>(
-            pairs, queue, nitems, scratch, scratch_stride, sw, rb, qhead, status, abort_flag);
+    auto kern = fast ? (keep ? sankoff_sl_fill_kernel<true, true> : sankoff_sl_fill_kernel<true, false>)
+                     : (keep ? sankoff_sl_fill_kernel<false, true> : sankoff_sl_fill_kernel<false, false>);
+    kern<<<blocks, SL_FILL_WARPS * 32, smem, st>>>(pairs, queue, nitems, scratch, scratch_stride, sw, rb, qhead,
+                                                   status, abort_flag);
     return cudaGetLastError();
 }
 

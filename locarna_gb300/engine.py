@@ -273,7 +273,8 @@ class Engine:
 
     def set_rect_budget(self, nbytes):
         """lcg_engine_set_rect_budget: bytes of kept group rectangles per
-        chunk (0: the traceback always recomputes)."""
+        chunk (0: the traceback always recomputes; negative: the defaults,
+        4 GiB for plain and 32 GiB for structure-local chunks)."""
         _check(self.lib, self.lib.lcg_engine_set_rect_budget(self.h, int(nbytes)))
 
     def set_autotune(self, on):

@@ -98,8 +98,9 @@ def test_graph_across_many_layouts_keeps_results(engine):
 @pytest.mark.gpu
 def test_kept_rectangles_give_the_same_alignments(engine):
     """With the group rectangles kept (the traceback walks the fill's
-    rectangles) and without (it recomputes them), every golden case, a batch
-    and the alignment modes give the same results."""
+    rectangles; eight state matrices for structure-local alignment) and
+    without (it recomputes them), every golden case, a batch and the
+    alignment modes give the same results."""
     from golden_io import Golden, sankoff_golden_names
     gs = [Golden(n) for n in sankoff_golden_names()]
     try:
@@ -115,8 +116,9 @@ def test_kept_rectangles_give_the_same_alignments(engine):
         plain = dict(struct_local=False, sequ_local=False, free_endgaps="----")
         tabs = [g.tables for g in gs if not g.kbest and g.align_kwargs() == plain][:24]
         assert len(tabs) >= 8
-        for kw in ({}, {"sequ_local": True}, {"sequ_local": True, "normalized": 100}, {"penalized": 50}):
-            engine.set_rect_budget(4 << 30)
+        for kw in ({}, {"sequ_local": True}, {"sequ_local": True, "normalized": 100}, {"penalized": 50},
+                   {"struct_local": True}, {"struct_local": True, "sequ_local": True}):
+            engine.set_rect_budget(64 << 30)
             a = engine.align_pairs(tabs, **kw)
             engine.set_rect_budget(0)
             b = engine.align_pairs(tabs, **kw)
@@ -131,4 +133,4 @@ def test_kept_rectangles_give_the_same_alignments(engine):
             for x, y in zip(hx, hy):
                 assert_same_result(x, y, f"kbest pair {k}")
     finally:
-        engine.set_rect_budget(4 << 30)
+        engine.set_rect_budget(-1)
