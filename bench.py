@@ -365,6 +365,10 @@ def run_pf(eng, tables, flush_l2, cpu):
     import numpy as np
     order = sorted(range(len(tables)), key=lambda k: (tables[k].len_a * tables[k].len_b, k))
     buckets = [order[i:i + PF_BUCKET] for i in range(0, len(order), PF_BUCKET)]
+    # both precisions on the same path: the backward recomputes the groups'
+    # rectangles (the workload's launches exceed the kept-rectangle budget;
+    # a smaller FP64 subset could otherwise keep them)
+    eng.set_rect_budget(0)
     for prec in (64, 32):  # warm-up
         eng.pf_forward([tables[k] for k in buckets[0][:64]], precision=prec, min_am_prob=0.0, gap_gradients=False)
         eng.pf_backward(probs=False)
@@ -420,7 +424,10 @@ def run_pf(eng, tables, flush_l2, cpu):
         "gpu_launches": launches,
         "cpu_baseline": cpu,
     }
-    # one pair of 200 nt: log Z and gradients, FP64 and FP32
+    # one pair of 200 nt: log Z and gradients, FP64 and FP32 with the
+    # engine's defaults (in FP64 the forward keeps the groups' rectangles for
+    # the backward)
+    eng.set_rect_budget(-1)
     from locarna_gb300.prep import prepare_pair
     from locarna_gb300.synth import make_rna
     t = prepare_pair(make_rna(200, 11).to_pp(), make_rna(200, 12).to_pp(), min_trace_probability=1e-5,

@@ -234,7 +234,11 @@ lcg_status lcg_engine_set_graphs(lcg_engine eng, int32_t on);
  * trace_arcmatch, aligner.cc:967-1028); the results are the same. Single
  * pairs and small batches; not with --noLP. bytes = 0 always recomputes;
  * bytes < 0 restores the default budgets, 4 GiB for plain chunks and 32 GiB
- * for structure-local chunks (a 400 x 400 nt pair takes ~25 GB). */
+ * for structure-local chunks (a 400 x 400 nt pair takes ~25 GB).
+ * LocARNA-P (lcg_pf_forward / lcg_pf_backward) keeps the groups' M (and E, F
+ * for the gap gradients) from the forward for the backward pass under the
+ * same budget, by default in FP64 only (4 GiB; in FP32 the backward's
+ * recomputation is faster than reading the kept values back). */
 lcg_status lcg_engine_set_rect_budget(lcg_engine eng, int64_t bytes);
 /* Graph captures and replays of the last lcg_align_pairs call. */
 lcg_status lcg_engine_last_graphs(lcg_engine eng, int64_t *captures, int64_t *replays);

@@ -41,7 +41,7 @@ size_t up16(size_t x) { return (x + 15) / 16 * 16; }
 
 struct PFLayout {
     int n, m, na, npos, bandcells;  // npos: D entries (arc matches with a band cell as right ends)
-    size_t rowinfo, crow, rowarc, groups, dw, bm, gA, gB, w, D, Dbar, cnt, bmacc, res, topM;
+    size_t rowinfo, crow, rowarc, groups, dw, bm, gA, gB, w, D, Dbar, cnt, bmacc, res, topM, rect;
     double log_c_total;  // (n+m) log c
 };
 
@@ -185,6 +185,29 @@ lcg_status pf_forward_t(lcg_engine e, PFState *S, const lcg_pair_tables *pairs, 
     }
     const size_t out_end = up;
     for (int q = 0; q < npairs; ++q) S->lay[q].topM = take(up, sizeof(T) * (S->lay[q].n + 1) * (S->lay[q].m + 1));
+    // Kept group rectangles: the forward writes every group's M (and, for
+    // the gap gradients, E and F) to a rectangle of its own and the backward
+    // reads them instead of recomputing the groups, when the pairs'
+    // rectangles fit the engine's budget (lcg_engine_set_rect_budget) -
+    // single pairs and small batches. By default FP64 only: an FP32
+    // recomputation into the warp's slot, read back from L2, is faster than
+    // reading the kept rectangle from DRAM (200-nt pair: backward 3.37 ms
+    // recomputing, 3.60 ms kept; FP64 7.51 against 6.06 ms).
+    const int rect_states = o->gap_gradients ? 3 : 1;
+    bool keep;
+    {
+        const long long budget =
+            e->rect_budget >= 0 ? e->rect_budget : (sizeof(T) == 8 ? RECT_BUDGET_PLAIN : 0);
+        keep = budget > 0;
+        long long cells = 0;
+        for (auto &p : prep) {
+            if (p.rect_cells < 0) keep = false;
+            cells += p.rect_cells;
+        }
+        keep = keep && (double)cells * rect_states * sizeof(T) <= (double)budget;
+    }
+    for (int q = 0; q < npairs; ++q)
+        S->lay[q].rect = keep ? take(up, sizeof(T) * rect_states * std::max<long long>(prep[q].rect_cells, 1)) : 0;
     const size_t total = up;
     if (total > S->cap) {
         if (S->d_arena) cudaFree(S->d_arena);
@@ -298,6 +321,8 @@ lcg_status pf_forward_t(lcg_engine e, PFState *S, const lcg_pair_tables *pairs, 
         d.topM = (T *)(Dv + L.topM);
         d.bmacc = (double *)(Dv + L.bmacc);
         d.res = (double *)(Dv + L.res);
+        d.rect = keep ? (T *)(Dv + L.rect) : nullptr;
+        d.rect_states = rect_states;
     };
     lcg_host::parallel_for(npairs, pack);
     // scratch: forward one rectangle per warp, backward four
@@ -325,7 +350,8 @@ lcg_status pf_forward_t(lcg_engine e, PFState *S, const lcg_pair_tables *pairs, 
     int *abort_flag = (int *)(Dv + S->off_ctrl + 8);
     PF_TRY(cudaEventRecord(e->ev0, st));
     PF_TRY(pf_launch_fwd<T>(Dv + S->off_pairs, (const int2 *)(Dv + S->off_queue), (int)nitems,
-                            S->d_scratch, stride, sw, rb, qhead, status, abort_flag, e->sms * bf, true, st));
+                            S->d_scratch, stride, sw, rb, qhead, status, abort_flag, e->sms * bf, true, st,
+                            keep ? rect_states : 0));
     PF_TRY(cudaEventRecord(e->ev1, st));
     PF_TRY(cudaMemcpyAsync(H + S->off_ctrl, Dv + S->off_ctrl, 64, cudaMemcpyDeviceToHost, st));
     for (int q = 0; q < npairs; ++q)

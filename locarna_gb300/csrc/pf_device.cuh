@@ -32,15 +32,23 @@ struct PFPair {
     double *res;           // [0] log Z', [1] gap-extension uses, [2] gap-opening uses
     const GroupItem *groups;  // left-end groups (work items) in dependency order, top level last
     const int4 *dw;           // D writes: (D index, ar-1, br-1, -), by group, ar ascending
+    // Kept group rectangles (nullptr: the backward recomputes them): the
+    // forward writes group g's M (rect_states 1) or M, E, F (3; the gap
+    // gradients read E and F) to rect + rect_states g.rect_off, state k at
+    // k (ar-al)(br-bl), row i-al, column j-bl, pitch br-bl; the backward
+    // reads them instead of recomputing the group.
+    T *rect;
+    int rect_states;
 };
 
 
 
 template <typename T>
-// queue: (pair, group) work items in dependency-respecting order
+// queue: (pair, group) work items in dependency-respecting order;
+// keep_states: 0, or the pairs' PFPair::rect_states (rectangles kept)
 cudaError_t pf_launch_fwd(const void *pairs, const int2 *queue, int nitems, void *scratch,
                           long long stride, int pitch, int rb, unsigned int *qhead, int *status, int *abort_flag,
-                          int blocks, bool count_uses, cudaStream_t st);
+                          int blocks, bool count_uses, cudaStream_t st, int keep_states = 0);
 // theta > 0: the truncated base-match pass (min_am_prob = theta^2) after a
 // full backward pass; theta = 0: the full adjoint pass, with the gap counts
 // (the indel / indel-opening gradients) when grads

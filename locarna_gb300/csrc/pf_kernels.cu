@@ -328,7 +328,9 @@ __device__ void pf_group_sweep(const PFPair<T> &P, int al, int ar, int bl, int b
 #undef RG
 }
 
-template <typename T, bool COUNTU>
+// KEEP: 0, or the pairs' rect_states (the groups' rectangles are kept for
+// the backward pass, M alone or M, E and F)
+template <typename T, bool COUNTU, int KEEP = 0>
 __global__ void __launch_bounds__(PF_WARPS * 32, pf_min_blocks<T>())
     pf_fwd_kernel(const PFPair<T> *__restrict__ pairs, const int2 *__restrict__ queue, int nitems,
                   T *scratch, long long stride, int pitch, int rb,
@@ -353,6 +355,13 @@ __global__ void __launch_bounds__(PF_WARPS * 32, pf_min_blocks<T>())
                 const T z = P.topM[(size_t)P.n * (P.m + 1) + P.m];
                 P.res[0] = log((double)z);
             }
+        } else if (KEEP > 0 && P.rect && it.rect_off >= 0) {
+            const int w = it.br - it.bl;
+            const size_t sz = (size_t)(it.ar - it.al) * w;
+            T *Mk = P.rect + (size_t)KEEP * it.rect_off;
+            pf_group_sweep<T, true, true, COUNTU, true, KEEP == 3>(P, it.al, it.ar, it.bl, it.br, Mk, Mk + sz,
+                                                                   Mk + 2 * sz, w, R, P.dw + it.dw_start,
+                                                                   it.dw_count, status, abort_flag);
         } else {
             pf_group_sweep<T, true, true, COUNTU, false>(P, it.al, it.ar, it.bl, it.br, Mg, nullptr, nullptr,
                                                          pitch, R, P.dw + it.dw_start, it.dw_count, status,
@@ -672,10 +681,22 @@ __global__ void __launch_bounds__(PF_WARPS * 32, pf_min_blocks<T>())
             }
             if (!__any_sync(0xffffffffu, any)) continue;
         }
-        pf_group_sweep<T, false, false, false, true, GRADS>(P, al, ar, bl, br, Mg, Eg, Fg, pitch, R, nullptr, 0,
-                                                            status, abort_flag);
+        // the group's rectangles: kept by the forward pass, else recomputed
+        // into the warp's slot (the adjoint rectangle Mb takes the same pitch)
+        const T *Mw = Mg, *Ew = Eg, *Fw = Fg;
+        int pw = pitch;
+        if (!it.top && P.rect && it.rect_off >= 0 && (!GRADS || P.rect_states == 3)) {
+            pw = br - bl;
+            const size_t sz = (size_t)(ar - al) * pw;
+            Mw = P.rect + (size_t)P.rect_states * it.rect_off;
+            Ew = Mw + sz;
+            Fw = Ew + sz;
+        } else {
+            pf_group_sweep<T, false, false, false, true, GRADS>(P, al, ar, bl, br, Mg, Eg, Fg, pitch, R, nullptr,
+                                                                0, status, abort_flag);
+        }
         __syncwarp();
-        pf_group_back<T, TRUNC, GRADS>(P, al, ar, bl, br, it.top != 0, Mg, Eg, Fg, Mb, pitch, R,
+        pf_group_back<T, TRUNC, GRADS>(P, al, ar, bl, br, it.top != 0, Mw, Ew, Fw, Mb, pw, R,
                                 it.top ? nullptr : P.dw + it.dw_start, it.top ? 0 : it.dw_count, status, abort_flag,
                                 P.res + 1, P.res + 2, theta_z);
         __syncwarp();
@@ -692,10 +713,16 @@ static size_t pf_smem(int rb) {
 template <typename T>
 cudaError_t pf_launch_fwd(const void *pairs, const int2 *queue, int nitems, void *scratch,
                           long long stride, int pitch, int rb, unsigned int *qhead, int *status, int *abort_flag,
-                          int blocks, bool count_uses, cudaStream_t st) {
+                          int blocks, bool count_uses, cudaStream_t st, int keep_states) {
     const size_t smem = pf_smem<T>(rb);
     cudaError_t e;
-    if (count_uses) {
+    if (count_uses && keep_states > 0) {
+        auto k = keep_states == 3 ? pf_fwd_kernel<T, true, 3> : pf_fwd_kernel<T, true, 1>;
+        e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        k<<<blocks, PF_WARPS * 32, smem, st>>>((const PFPair<T> *)pairs, queue, nitems, (T *)scratch, stride, pitch,
+                                               rb, qhead, status, abort_flag);
+    } else if (count_uses) {
         e = cudaFuncSetAttribute(pf_fwd_kernel<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         pf_fwd_kernel<T, true><<<blocks, PF_WARPS * 32, smem, st>>>(
@@ -782,9 +809,9 @@ cudaError_t pf_back_occupancy(int rb, int *blocks_per_sm) {
 int pf_warps_per_block() { return PF_WARPS; }
 
 template cudaError_t pf_launch_fwd<double>(const void *, const int2 *, int, void *, long long, int,
-                                           int, unsigned int *, int *, int *, int, bool, cudaStream_t);
+                                           int, unsigned int *, int *, int *, int, bool, cudaStream_t, int);
 template cudaError_t pf_launch_fwd<float>(const void *, const int2 *, int, void *, long long, int,
-                                          int, unsigned int *, int *, int *, int, bool, cudaStream_t);
+                                          int, unsigned int *, int *, int *, int, bool, cudaStream_t, int);
 template cudaError_t pf_fwd_occupancy<double>(int, int *);
 template cudaError_t pf_fwd_occupancy<float>(int, int *);
 template cudaError_t pf_launch_back<double>(const void *, const int2 *, int, void *, long long, int,

@@ -255,3 +255,35 @@ def test_pf64_default_semantics_match_reference(engine, name):
     engine.pf_forward([t], precision=64, min_am_prob=0.0)
     exact = engine.pf_backward()[0]
     assert np.max(np.abs(exact["bm_prob"] - ref_bm)) > 10 * P64_TOL
+
+
+@pytest.mark.gpu
+def test_pf_kept_rectangles_give_the_same_results(engine):
+    """With the groups' rectangles kept by the forward pass (the backward
+    reads them; M alone, or M, E and F for the gap gradients) and without
+    (the backward recomputes them), log Z, the probabilities (exact and
+    truncated) and every gradient agree."""
+    gs = [GoldenPF(n) for n in PF_CASES]
+    tabs = [_prepared(g) for g in gs]
+    keys = ("dlogz_dindel", "dlogz_dindel_opening", "dlogz_dstruct_weight")
+    try:
+        for prec in (64, 32):
+            tol = 1e-12 if prec == 64 else 1e-6
+            for mam in (0.0, 0.001):
+                for grads in (True, False):
+                    out = []
+                    for budget in (16 << 30, 0):
+                        engine.set_rect_budget(budget)
+                        lz = engine.pf_forward(tabs, precision=prec, min_am_prob=mam, gap_gradients=grads)
+                        out.append((lz, engine.pf_backward()))
+                    (lza, ra), (lzb, rb) = out
+                    for k, (a, b) in enumerate(zip(ra, rb)):
+                        assert abs(lza[k] - lzb[k]) <= tol * max(1.0, abs(lzb[k]))
+                        assert np.max(np.abs(a["am_prob"] - b["am_prob"])) <= tol
+                        assert np.max(np.abs(a["bm_prob"] - b["bm_prob"])) <= tol
+                        for key in keys if grads else keys[2:]:
+                            assert abs(a[key] - b[key]) <= tol * max(1.0, abs(b[key])), key
+                        assert np.max(np.abs(a["dlogz_dbasematch"] - b["dlogz_dbasematch"])) <= tol * max(
+                            1.0, np.max(np.abs(b["dlogz_dbasematch"])))
+    finally:
+        engine.set_rect_budget(-1)
