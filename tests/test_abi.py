@@ -62,3 +62,44 @@ def test_ctypes_structs_match_c_layout(tmp_path):
         assert int(got[name]) == C.sizeof(cls), name
         for f in cls._fields_:
             assert int(got[f"{name}.{f[0]}"]) == getattr(cls, f[0]).offset, (name, f[0])
+
+
+def test_prepared_rows_and_anchor_lines():
+    """lcg_prepared_row: the inputs' rows and names, and (which 4 / 5) their
+    #A<k> anchor lines, the blocks of each k concatenated; NULL past the end
+    and for an unknown `which`."""
+    import sys
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from golden_io import Golden
+    from locarna_gb300.prep import _lib, prep_options
+    lib = _lib()
+    lib.lcg_prepared_row.argtypes = [C.c_void_p, C.c_int32, C.c_int32]
+    lib.lcg_prepared_row.restype = C.c_char_p
+    g = Golden("a150_anchors")
+
+    def anchor_lines(pp):
+        lines = {}
+        for line in pp.splitlines():
+            if line.startswith("#SECTION"):
+                break
+            if line.startswith("#A") and line[2:3].isdigit():
+                k, s = line[2:].split()
+                lines[int(k)] = lines.get(int(k), "") + s
+        return [lines[k] for k in sorted(lines)]
+
+    h = C.c_void_p()
+    o = prep_options()
+    assert lib.lcg_prepare_pair(g.pp_a.encode(), g.pp_b.encode(), C.byref(o), C.byref(h)) == 0
+    try:
+        for side, pp in ((0, g.pp_a), (1, g.pp_b)):
+            want = anchor_lines(pp)
+            assert want and len(want[0]) == len(lib.lcg_prepared_row(h, side, 0))
+            got = []
+            while (r := lib.lcg_prepared_row(h, side + 4, len(got))) is not None:
+                got.append(r.decode())
+            assert got == want
+            assert lib.lcg_prepared_row(h, side + 2, 0).decode()  # the row's name
+        assert lib.lcg_prepared_row(h, 6, 0) is None
+        assert lib.lcg_prepared_row(h, 0, 1) is None  # single-sequence inputs: one row
+    finally:
+        lib.lcg_prepared_free(h)
