@@ -378,8 +378,8 @@ __device__ __forceinline__ T ld_cg(const T *p) { return __ldcg(p); }
 
 // Adjoint of one group's forward sweep, on Mg, Eg, Fg as the forward kept
 // them or as pf_group_sweep<SAVE> recomputed them. Mb (same layout as Mg)
-// accumulates dZ'/dM for every
-// cell of the rectangle, boundaries included. Seeds: the group's own D
+// accumulates dZ'/dM for every cell of the rectangle, boundaries included.
+// Seeds: the group's own D
 // entries (dZ'/dD(am) w(am) into M(ar-1,br-1)) or, for the top level,
 // dZ'/dM(n,m) = 1. Propagates into D_bar of nested arc matches, the per-pair
 // base-match accumulator and the gap counts. Rows bottom-up, chunks right to
