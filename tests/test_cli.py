@@ -155,3 +155,4 @@ def test_writer_prints_the_consensus_anchor_lines(writer):
     a2 = [anch[0][0].replace(".", "A", 1)]
     dup = _write(writer, _rows(g.pp_a), _rows(g.pp_b), edges, 120, False, (a2, anch[1]))
     assert not any(l.startswith("#A") for l in dup.splitlines())
+
